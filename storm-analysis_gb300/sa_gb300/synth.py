@@ -1,0 +1,309 @@
+"""
+Seeded synthetic localisation workloads for the LM fitter.
+
+No public dataset is involved: every workload is drawn from numpy's
+``default_rng(seed)``.  Shapes, densities and value ranges follow the five
+benchmark configurations of the fitting step:
+
+  cfg 0  '2d'  1 x 256^2, 200 emitters (>= 4 px apart), sigma 1.3 px,
+         height U(500, 3000), background 20, Poisson, roi 10
+  cfg 1  '3d'  64 x 512^2, Poisson(0.5 /um^2) emitters (~3355 / frame),
+         sigma_x, sigma_y U(1, 2) px, height log-U(200, 5000),
+         background U(5, 50) per frame, Poisson, roi 18
+  cfg 2  'Z'   128 x 256^2, 1000 emitters, w0 1.6 px, c +-0.15 um, d 0.4 um,
+         z U(-0.4, 0.4) um, height U(1000, 4000), sCMOS camera noise
+         (offset N(100, 2), variance Gamma(2, 2) ADU^2, gain N(2, 0.05)), roi 12
+  cfg 3  spline 256 x 256^2, 800 emitters, 21^3-knot tricubic spline of the
+         cfg-2 astigmatic PSF with a 0.05-amplitude smooth random aberration,
+         z U(-0.5, 0.5) um, Poisson
+  cfg 4  serving mix of the above models and sizes (see ``serving_requests``)
+
+The camera model and pre-processing follow the reference:
+sCMOS noise per simulator/camera.py:121-137 and ADU -> e- conversion with
+the clip to >= 1 per sa_library/analysis_io.py:243-260.
+
+Initial guesses for every configuration: x/y = truth + N(0, 0.3 px),
+height and sigma x U(0.8, 1.2), background = truth, Z: z = truth + N(0, 0.05 um).
+They are passed in the reference's pre-specified ("hdf5") peak format so
+both the oracle and the GPU engine start from identical parameters.
+"""
+import math
+
+import numpy
+
+PIXEL_UM = 0.160
+
+# Z model defocus curves: [w0 (px), c (um), d (um), A, B] (sa_library/parameters.py:557-574 units).
+WX_PARAMS = numpy.array([1.6, 0.15, 0.4, 0.0, 0.0])
+WY_PARAMS = numpy.array([1.6, -0.15, 0.4, 0.0, 0.0])
+Z_RANGE = (-0.5, 0.5)
+
+SPLINE_ZMIN_NM = -600.0
+SPLINE_ZMAX_NM = 600.0
+SPLINE_KNOTS = 21
+
+
+def _widths_from_z(z, wp):
+    """sigma_x or sigma_y (px) of the Z model at z (um) (dao_fit.c:1009-1035)."""
+    z0 = (z - wp[1]) / wp[2]
+    t = 1.0 + z0 * z0 + wp[3] * z0 ** 3 + wp[4] * z0 ** 4
+    # width = 2/(w0^2 t) = 1/(2 sigma^2)  ->  sigma = w0 sqrt(t) / 2
+    return 0.5 * wp[0] * numpy.sqrt(t)
+
+
+def _place_uniform(rng, n, nx, ny, margin, min_sep=0.0):
+    """Uniform positions inside [margin, size - margin - 1], optional min separation."""
+    lo = float(margin)
+    hix = float(nx - margin - 1)
+    hiy = float(ny - margin - 1)
+    if min_sep <= 0.0:
+        return rng.uniform(lo, hix, n), rng.uniform(lo, hiy, n)
+    xs, ys = [], []
+    tries = 0
+    while len(xs) < n and tries < 200 * n:
+        tries += 1
+        x = rng.uniform(lo, hix)
+        y = rng.uniform(lo, hiy)
+        ok = True
+        for (a, b) in zip(xs, ys):
+            if (a - x) ** 2 + (b - y) ** 2 < min_sep * min_sep:
+                ok = False
+                break
+        if ok:
+            xs.append(x)
+            ys.append(y)
+    return numpy.array(xs), numpy.array(ys)
+
+
+def _render_gauss(nx, ny, x, y, h, sx, sy, out):
+    """Add h * exp(-(c-x)^2/(2 sx^2) - (r-y)^2/(2 sy^2)) at pixel centres (c, r)."""
+    rad = 8
+    for i in range(x.size):
+        cx, cy = int(round(x[i])), int(round(y[i]))
+        rad_x = int(min(max(rad, 5.0 * sx[i]), 40))
+        rad_y = int(min(max(rad, 5.0 * sy[i]), 40))
+        c0, c1 = max(0, cx - rad_x), min(nx, cx + rad_x + 1)
+        r0, r1 = max(0, cy - rad_y), min(ny, cy + rad_y + 1)
+        cc = numpy.arange(c0, c1) - x[i]
+        rr = numpy.arange(r0, r1) - y[i]
+        gx = numpy.exp(-cc * cc / (2.0 * sx[i] * sx[i]))
+        gy = numpy.exp(-rr * rr / (2.0 * sy[i] * sy[i]))
+        out[r0:r1, c0:c1] += h[i] * numpy.outer(gy, gx)
+
+
+def _camera_poisson(rng, expected, offset=100.0, gain=1.0):
+    """Poisson camera, then the reference's pre-processing (ADU -> e-, clip >= 1)."""
+    adu = rng.poisson(expected).astype(numpy.float64) * gain + offset
+    img = (adu - offset) / gain
+    img[img < 1.0] = 1.0
+    return img
+
+
+def _camera_scmos(rng, expected, rqe, offset, variance, gain):
+    """sCMOS camera (simulator/camera.py:121-137) + pre-processing (analysis_io.py:243-260)."""
+    e = rng.poisson(expected * rqe).astype(numpy.float64)
+    adu = e * gain + rng.normal(0.0, 1.0, size=e.shape) * numpy.sqrt(variance) + offset
+    img = (adu - offset) / gain / rqe
+    img[img < 1.0] = 1.0
+    return img
+
+
+# ----------------------------------------------------------------------------
+# spline PSF
+# ----------------------------------------------------------------------------
+
+_CR = numpy.array([[0.0, 1.0, 0.0, 0.0],
+                   [-0.5, 0.0, 0.5, 0.0],
+                   [1.0, -2.5, 2.0, -0.5],
+                   [-0.5, 1.5, -1.5, 0.5]])
+
+
+def tricubic_coefficients(samples):
+    """Per-cell monomial coefficients of a C1 tricubic (Catmull-Rom) interpolant.
+
+    samples: (n, n, n) knot values indexed [x, y, z].  Returns (n-1, n-1, n-1, 64)
+    with coefficient i*16+j*4+k multiplying dx^i dy^j dz^k, the layout the
+    fitter reads (spliner/cubic_spline.c:509-522, spliner/spline3D.py:72-102).
+    """
+    s = numpy.asarray(samples, dtype=numpy.float64)
+    n = s.shape[0]
+    p = numpy.pad(s, ((1, 2), (1, 2), (1, 2)), mode="edge")
+    w = numpy.lib.stride_tricks.sliding_window_view(p, (4, 4, 4))[:n - 1, :n - 1, :n - 1]
+    c = numpy.einsum("im,jn,ko,abcmno->abcijk", _CR, _CR, _CR, w, optimize=True)
+    return numpy.ascontiguousarray(c.reshape(n - 1, n - 1, n - 1, 64))
+
+
+def bicubic_coefficients(samples):
+    """2D analogue: (n, n) knots [x, y] -> (n-1, n-1, 16), index 4*i+j <-> dx^i dy^j."""
+    s = numpy.asarray(samples, dtype=numpy.float64)
+    n = s.shape[0]
+    p = numpy.pad(s, ((1, 2), (1, 2)), mode="edge")
+    w = numpy.lib.stride_tricks.sliding_window_view(p, (4, 4))[:n - 1, :n - 1]
+    c = numpy.einsum("im,jn,abmn->abij", _CR, _CR, w, optimize=True)
+    return numpy.ascontiguousarray(c.reshape(n - 1, n - 1, 16))
+
+
+def _aberrated_psf(dx, dy, z_um, coef):
+    sx = _widths_from_z(z_um, WX_PARAMS)
+    sy = _widths_from_z(z_um, WY_PARAMS)
+    g = numpy.exp(-dx * dx / (2.0 * sx * sx) - dy * dy / (2.0 * sy * sy))
+    u, v = dx / 10.0, dy / 10.0
+    poly = (coef[0] * u + coef[1] * v + coef[2] * (u * u - v * v) + coef[3] * u * v +
+            coef[4] * z_um * u + coef[5] * z_um * v)
+    return g * (1.0 + 0.05 * numpy.tanh(poly))
+
+
+def make_spline(seed=3, knots=SPLINE_KNOTS):
+    """Spline PSF for cfg 3: knots^3 samples, spline z in [0, knots-1] <-> [zmin, zmax] nm."""
+    rng = numpy.random.default_rng(1000 + seed)
+    coef = rng.normal(0.0, 1.0, 6)
+    half = (knots - 1) / 2.0
+    a = numpy.arange(knots) - half
+    zs = SPLINE_ZMIN_NM + numpy.arange(knots) * (SPLINE_ZMAX_NM - SPLINE_ZMIN_NM) / (knots - 1)
+    X, Y, Z = numpy.meshgrid(a, a, zs * 1.0e-3, indexing="ij")
+    samples = _aberrated_psf(X, Y, Z, coef)
+    return {"coeff": tricubic_coefficients(samples), "coef_ab": coef,
+            "zmin": SPLINE_ZMIN_NM, "zmax": SPLINE_ZMAX_NM, "size": knots - 1}
+
+
+def spline_scaled_z(z_um, size):
+    """spliner/spline_to_psf.py:202-203 getScaledZ (z given in nm there)."""
+    return float(size) * (z_um * 1000.0 - SPLINE_ZMIN_NM) / (SPLINE_ZMAX_NM - SPLINE_ZMIN_NM)
+
+
+# ----------------------------------------------------------------------------
+# workloads
+# ----------------------------------------------------------------------------
+
+CONFIGS = {
+    0: dict(model="2d", frames=1, nx=256, ny=256, roi=10),
+    1: dict(model="3d", frames=64, nx=512, ny=512, roi=18),
+    2: dict(model="Z", frames=128, nx=256, ny=256, roi=12),
+    3: dict(model="spline3D", frames=256, nx=256, ny=256, roi=19),
+}
+
+
+def fitter_kwargs(cfg, spline=None):
+    """Constructor arguments of the MultiFitter sub-class for a configuration."""
+    c = CONFIGS[cfg]
+    if c["model"] == "2d":
+        return dict(model="2d", roi_size=10, sigma_range=[0.5, 3.0])
+    if c["model"] == "3d":
+        return dict(model="3d", roi_size=18, sigma_range=[0.5, 4.0])
+    if c["model"] == "Z":
+        return dict(model="Z", roi_size=12, wx_params=WX_PARAMS.copy(),
+                    wy_params=WY_PARAMS.copy(), min_z=Z_RANGE[0], max_z=Z_RANGE[1])
+    return dict(model="spline3D", spline=spline)
+
+
+def make_workload(cfg, frames=None, nx=None, ny=None, seed=None, n_emitters=None):
+    """Return a dict with per-frame images, backgrounds, truth and initial guesses.
+
+    images[f] and backgrounds[f] are float64 (ny, nx) arrays in photo-electrons;
+    guesses[f] is the dict of columns for newPeaks(..., "hdf5").
+    """
+    c = dict(CONFIGS[cfg])
+    if frames is not None:
+        c["frames"] = frames
+    if nx is not None:
+        c["nx"] = nx
+    if ny is not None:
+        c["ny"] = ny
+    seed = cfg if seed is None else seed
+    rng = numpy.random.default_rng(seed)
+    nx, ny, roi = c["nx"], c["ny"], c["roi"]
+    margin = roi // 2 + 2
+    out = dict(cfg=cfg, model=c["model"], nx=nx, ny=ny, roi=roi, images=[], backgrounds=[],
+               truth=[], guesses=[], rqe=numpy.ones((ny, nx)), scmos_cal=numpy.zeros((ny, nx)))
+    spline = None
+    if cfg == 3:
+        spline = make_spline(seed)
+        out["spline"] = spline
+    if cfg == 2:
+        offset = rng.normal(100.0, 2.0, size=(ny, nx))
+        variance = rng.gamma(2.0, 2.0, size=(ny, nx))
+        gain = rng.normal(2.0, 0.05, size=(ny, nx))
+        out["scmos_cal"] = variance / (gain * gain)
+    area_um2 = (nx * PIXEL_UM) * (ny * PIXEL_UM)
+    for f in range(c["frames"]):
+        if cfg == 0:
+            n = 200 if n_emitters is None else n_emitters
+            x, y = _place_uniform(rng, n, nx, ny, margin, min_sep=4.0)
+            n = x.size
+            sx = numpy.full(n, 1.3)
+            sy = sx.copy()
+            h = rng.uniform(500.0, 3000.0, n)
+            bg = 20.0
+            z = numpy.zeros(n)
+        elif cfg == 1:
+            n = rng.poisson(0.5 * area_um2) if n_emitters is None else n_emitters
+            x, y = _place_uniform(rng, n, nx, ny, margin)
+            sx = rng.uniform(1.0, 2.0, n)
+            sy = rng.uniform(1.0, 2.0, n)
+            h = numpy.exp(rng.uniform(math.log(200.0), math.log(5000.0), n))
+            bg = rng.uniform(5.0, 50.0)
+            z = numpy.zeros(n)
+        elif cfg == 2:
+            n = 1000 if n_emitters is None else n_emitters
+            x, y = _place_uniform(rng, n, nx, ny, margin)
+            z = rng.uniform(-0.4, 0.4, n)
+            sx = _widths_from_z(z, WX_PARAMS)
+            sy = _widths_from_z(z, WY_PARAMS)
+            h = rng.uniform(1000.0, 4000.0, n)
+            bg = 20.0
+        else:
+            n = 800 if n_emitters is None else n_emitters
+            x, y = _place_uniform(rng, n, nx, ny, margin)
+            z = rng.uniform(-0.5, 0.5, n)
+            h = rng.uniform(1000.0, 4000.0, n)
+            bg = 20.0
+            sx = sy = None
+        expected = numpy.full((ny, nx), float(bg))
+        if cfg == 3:
+            half = 10
+            coef = spline["coef_ab"]
+            for i in range(n):
+                cx, cy = int(round(x[i])), int(round(y[i]))
+                c0, c1 = max(0, cx - half), min(nx, cx + half + 1)
+                r0, r1 = max(0, cy - half), min(ny, cy + half + 1)
+                dxg, dyg = numpy.meshgrid(numpy.arange(c0, c1) - x[i], numpy.arange(r0, r1) - y[i])
+                expected[r0:r1, c0:c1] += h[i] * _aberrated_psf(dxg, dyg, z[i], coef)
+        else:
+            _render_gauss(nx, ny, x, y, h, sx, sy, expected)
+        if cfg == 2:
+            img = _camera_scmos(rng, expected, out["rqe"], offset, variance, gain)
+        else:
+            img = _camera_poisson(rng, expected)
+        # Initial guesses (identical for the oracle and the engine).
+        gx = x + rng.normal(0.0, 0.3, n)
+        gy = y + rng.normal(0.0, 0.3, n)
+        gh = h * rng.uniform(0.8, 1.2, n)
+        g = {"x": gx, "y": gy, "background": numpy.full(n, float(bg)), "height": gh}
+        if cfg == 3:
+            g["z"] = numpy.array([spline_scaled_z(zz, spline["size"]) for zz in
+                                  (z + rng.normal(0.0, 0.05, n))])
+        else:
+            fs = rng.uniform(0.8, 1.2, n)
+            if c["model"] == "2d":
+                g["xsigma"] = sx * fs
+                g["ysigma"] = sx * fs
+            else:
+                g["xsigma"] = sx * fs
+                g["ysigma"] = sy * rng.uniform(0.8, 1.2, n)
+            g["z"] = (z + rng.normal(0.0, 0.05, n)) if cfg == 2 else numpy.zeros(n)
+        out["images"].append(img)
+        out["backgrounds"].append(numpy.full((ny, nx), float(bg)))
+        out["truth"].append({"x": x, "y": y, "z": z, "height": h})
+        out["guesses"].append(g)
+    out["fitter"] = fitter_kwargs(cfg, spline)
+    return out
+
+
+def serving_requests(n_requests=10000, rate_hz=2000.0, seed=4):
+    """Request stream of cfg 4: arrival times, frame size, density and model per request."""
+    rng = numpy.random.default_rng(seed)
+    t = numpy.cumsum(rng.exponential(1.0 / rate_hz, n_requests))
+    sizes = rng.choice([128, 256, 512, 2048], n_requests)
+    dens = numpy.exp(rng.uniform(math.log(0.05), math.log(2.0), n_requests))
+    models = rng.choice(["2d", "3d", "Z", "spline3D"], n_requests)
+    return dict(t=t, size=sizes, density=dens, model=models)
