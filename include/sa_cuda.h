@@ -1,0 +1,221 @@
+/*
+ * sa_cuda.h -- C ABI of libsa_cuda.so, the GB300 multi-emitter
+ * Levenberg-Marquardt fitting engine behind storm-analysis's MultiFitter
+ * classes.
+ *
+ * The first group of entry points keeps the names, argument meaning and
+ * call order of the reference's fitting libraries (libdao_fit.so and
+ * libcubic_fit.so), as bound by sa_library/dao_fit_c.py:147-238 and
+ * spliner/cubic_fit_c.py:21-98, so either Python binding can load this
+ * library instead.  Each declaration cites the reference function it
+ * replaces.  Pointers are host pointers to C-contiguous arrays, as in the
+ * reference; the library copies what it needs to the GPU.
+ *
+ * The second group (sa*) is new: error reporting, precision selection,
+ * device-driven doFit and the batched multi-frame engine.
+ *
+ * Error behaviour: the reference's entry points return nothing and print on
+ * bad input; here they print the same message, record it (saGetLastError)
+ * and leave the handle unchanged.  The sa* entry points return 0 on success
+ * and a negative value on failure.
+ */
+#ifndef SA_CUDA_H
+#define SA_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/*
+ * Handle.  Its leading fields have the layout of the reference's fitData
+ * (sa_library/multi_fit.h:80-143) because Python reads nfit, max_nfit,
+ * jac_size, roi_n_index, roi_x_index/roi_y_index and the counters through a
+ * ctypes mirror of that struct (sa_library/dao_fit_c.py:22-77) and writes
+ * n_iterations.  Pointer fields other than roi_x_index/roi_y_index are NULL:
+ * the per-pixel arrays live on the GPU.
+ */
+typedef struct saFitData {
+  int n_dposv;
+  int n_iterations;
+  int n_lost;
+  int n_margin;
+  int n_neg_fi;
+  int n_neg_height;
+  int n_non_converged;
+  int n_non_decr;
+
+  int fit_size_x;
+  int fit_size_y;
+  int image_size_x;
+  int image_size_y;
+  int jac_size;
+  int max_nfit;
+  int nfit;
+  int roi_n_index;
+
+  double minimum_height;
+  double xoff;
+  double yoff;
+  double zoff;
+  double tolerance;
+
+  int *bg_counts;
+  int *roi_x_index;
+  int *roi_y_index;
+  int *stale;
+
+  double *as_xi;
+  double *bg_data;
+  double *bg_estimate;
+  double *err_i;
+  double *f_data;
+  double *rqe;
+  double *scmos_term;
+  double *t_fi;
+  double *x_data;
+
+  void *working_peak;
+  void *fit;
+  void *fit_model;
+
+  void *fn_reserved[9];
+
+  void *engine;             /* private */
+} saFitData;
+
+/* ---- Gaussian fitters (sa_library/dao_fit.c) ---------------------------- */
+
+/* dao_fit.c:1251 daoInitialize */
+saFitData *daoInitialize(double *rqe, double *scmos_calibration, double tol, int im_size_x,
+                         int im_size_y, int roi_size);
+/* dao_fit.c:1319 daoInitialize2DFixed */
+void daoInitialize2DFixed(saFitData *fit);
+/* dao_fit.c:1395 daoInitialize2D */
+void daoInitialize2D(saFitData *fit, double width_min, double width_max);
+/* dao_fit.c:1518 daoInitialize3D */
+void daoInitialize3D(saFitData *fit, double width_min, double width_max);
+/* dao_fit.c:1545 daoInitializeZ */
+void daoInitializeZ(saFitData *fit, double *wx_vs_z, double *wy_vs_z, double z_min, double z_max);
+/* dao_fit.c:1582 daoNewPeaks */
+void daoNewPeaks(saFitData *fit, double *peak_params, char *p_type, int n_peaks);
+/* dao_fit.c:1181 daoCleanup */
+void daoCleanup(saFitData *fit);
+
+/* Error-model variants of dao_fit.c:1337-1503 (ALS, LS, DWLS, FWLS).  Exported
+ * so the reference bindings load; this engine implements the MLE model only
+ * and these report an error. */
+void daoInitialize2DFixedALS(saFitData *fit);
+void daoInitialize2DFixedLS(saFitData *fit);
+void daoInitialize2DFixedDWLS(saFitData *fit);
+void daoInitialize2DFixedFWLS(saFitData *fit);
+void daoInitialize2DALS(saFitData *fit, double width_min, double width_max);
+void daoInitialize2DLS(saFitData *fit, double width_min, double width_max);
+void daoInitialize2DDWLS(saFitData *fit, double width_min, double width_max);
+void daoInitialize2DFWLS(saFitData *fit, double width_min, double width_max);
+
+/* ---- spline fitter (spliner/cubic_fit.c, spliner/cubic_spline.c) -------- */
+
+/* cubic_spline.c:698 initSpline2D */
+void *initSpline2D(double *aij, int xsize, int ysize);
+/* cubic_spline.c:749 initSpline3D */
+void *initSpline3D(double *aij, int xsize, int ysize, int zsize);
+/* cubic_spline.c:862 splineCleanup */
+void splineCleanup(void *spline_data);
+/* cubic_spline.c:660-687 getXSize / getYSize / getZSize */
+int getXSize(void *spline_data);
+int getYSize(void *spline_data);
+int getZSize(void *spline_data);
+/* cubic_fit.c:602 cfInitialize */
+saFitData *cfInitialize(void *spline_data, double *rqe, double *scmos_calibration, double tol,
+                        int im_size_x, int im_size_y);
+/* cubic_fit.c:674 cfInitialize2D */
+void cfInitialize2D(saFitData *fit);
+/* cubic_fit.c:690 cfInitialize3D */
+void cfInitialize3D(saFitData *fit);
+/* cubic_fit.c:707-748 error-model variants (report an error, see above) */
+void cfInitialize3DALS(saFitData *fit);
+void cfInitialize3DLS(saFitData *fit);
+void cfInitialize3DFWLS(saFitData *fit);
+/* cubic_fit.c:758 cfNewPeaks */
+void cfNewPeaks(saFitData *fit, double *peak_params, char *p_type, int n_peaks);
+/* cubic_fit.c:511 cfCleanup (also frees the spline) */
+void cfCleanup(saFitData *fit);
+
+/* ---- shared LM core (sa_library/multi_fit.c) ----------------------------- */
+
+/* multi_fit.c:90 mFitAnscombeTransformImage (ALS only; reports an error) */
+void mFitAnscombeTransformImage(saFitData *fit);
+/* multi_fit.c:708 mFitGetFitImage */
+void mFitGetFitImage(saFitData *fit, double *fit_image);
+/* multi_fit.c:730 mFitGetNError */
+int mFitGetNError(saFitData *fit);
+/* multi_fit.c:754 mFitGetPeakPropertyDouble */
+void mFitGetPeakPropertyDouble(saFitData *fit, double *values, char *what);
+/* multi_fit.c:851 mFitGetPeakPropertyInt */
+void mFitGetPeakPropertyInt(saFitData *fit, int32_t *values, char *what);
+/* multi_fit.c:880 mFitGetResidual */
+void mFitGetResidual(saFitData *fit, double *residual);
+/* multi_fit.c:898 mFitGetUnconverged */
+int mFitGetUnconverged(saFitData *fit);
+/* multi_fit.c:1072 mFitIterateLM: one Gauss-Seidel LM sweep */
+void mFitIterateLM(saFitData *fit);
+/* multi_fit.c:1360 mFitNewBackground */
+void mFitNewBackground(saFitData *fit, double *background);
+/* multi_fit.c:1382 mFitNewImage */
+void mFitNewImage(saFitData *fit, double *new_image);
+/* multi_fit.c:1704 mFitRemoveErrorPeaks */
+void mFitRemoveErrorPeaks(saFitData *fit);
+/* multi_fit.c:1750 mFitRemoveRunningPeaks */
+void mFitRemoveRunningPeaks(saFitData *fit);
+/* multi_fit.c:1809 mFitSetPeakStatus */
+void mFitSetPeakStatus(saFitData *fit, int32_t *status);
+
+/* ---- engine extensions (no reference counterpart) ------------------------ */
+
+/* Copy the last error message into buf; returns its length (0: none). */
+int saGetLastError(char *buf, int len);
+/* Forget the last error message. */
+void saClearLastError(void);
+/* Number of CUDA devices visible (0 when none); never fails loudly. */
+int saDeviceCount(void);
+/* Pixel arithmetic precision, 32 (FP32 model/Jacobian, FP64 solve and
+ * decisions) or 64 (FP64 throughout).  Call before the first image. */
+int saSetPrecision(saFitData *fit, int bits);
+/* Footprint dilation (pixels) used by the dependency scheduler; default 2. */
+int saSetDilation(saFitData *fit, int pixels);
+/* Use this CUDA stream (cudaStream_t) for all work of the handle. */
+int saSetStream(saFitData *fit, void *stream);
+/* The whole doFit loop of dao_fit_c.py:332-356 on the device: one sweep,
+ * then sweeps while any peak is RUNNING, at most max_iterations more.
+ * Returns the number of sweeps made, or < 0 on error. */
+int saDoFit(saFitData *fit, int max_iterations);
+/* Counters (multi_fit.h:87-94 order, then the starting-error failures). */
+int saGetCounters(saFitData *fit, int64_t *out9);
+/* Scheduler statistics: [sweep attempts beyond the first, escapes]. */
+int saGetSchedStats(saFitData *fit, int64_t *out2);
+
+/* Batched frame sets: n_frames frames of the handle's image size share the
+ * model, rqe and sCMOS calibration.  Frame f's peaks are rows
+ * [sum(counts[:f]), sum(counts[:f+1])) of the concatenated input. */
+int saSetFrames(saFitData *fit, int n_frames, int peaks_per_frame_capacity);
+int saNewImages(saFitData *fit, const void *images, int n_frames, int dtype_bits, int on_device);
+int saNewBackgrounds(saFitData *fit, const void *backgrounds, int n_frames, int dtype_bits,
+                     int on_device);
+int saNewPeaksBatch(saFitData *fit, const double *peaks, const int32_t *counts, int n_frames,
+                    const char *p_type);
+int saDoFitBatch(saFitData *fit, int max_iterations);
+int saGetNFitBatch(saFitData *fit, int32_t *counts);
+int saGetPeakPropertyBatch(saFitData *fit, double *values, const char *what);
+int saGetPeakPropertyIntBatch(saFitData *fit, int32_t *values, const char *what);
+/* Device time of the sweep kernels since the last reset, for profiling:
+ * enable with saSetTiming(fit, 1); returns total ms and launch count. */
+int saSetTiming(saFitData *fit, int on);
+int saGetTiming(saFitData *fit, double *total_ms, int64_t *launches, int64_t *ticks);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

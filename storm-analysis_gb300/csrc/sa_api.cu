@@ -1,0 +1,1238 @@
+// sa_api.cu -- host side of libsa_cuda.so: handles, device memory, the
+// device-driven sweep loop and the reference-named C ABI (include/sa_cuda.h).
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sa_launch.h"
+#include "sa_cuda.h"
+
+using namespace sa;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  fprintf(stderr, "libsa_cuda: %s\n", buf);
+}
+
+#define CK(call)                                                              \
+  do {                                                                        \
+    cudaError_t e__ = (call);                                                 \
+    if (e__ != cudaSuccess) {                                                 \
+      set_error("%s failed: %s", #call, cudaGetErrorString(e__));             \
+      return -1;                                                              \
+    }                                                                         \
+  } while (0)
+
+struct SplineH {
+  int type;  // 0: 2D, 1: 3D
+  int xs, ys, zs;
+  std::vector<double> aij;
+};
+
+template <typename P>
+void dfree(P*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+struct Engine {
+  ModelCfg cfg{};
+  bool model_set = false;
+  bool unsupported = false;
+  int prec = 32;
+  std::vector<double> rqe_h, scmos_h;
+  std::vector<double> aij_h;
+  std::vector<unsigned short> roi_xy;
+  std::vector<int> roi_x, roi_y;
+  SplineH* spline = nullptr;
+
+  // frames
+  int F = 0;
+  long long npix = 0;
+  void* d_x = nullptr;
+  void* d_rqe = nullptr;
+  void* d_scmos = nullptr;
+  void* d_aij = nullptr;
+  long long* d_f = nullptr;
+  long long* d_bg = nullptr;
+  int* d_cnt = nullptr;
+  double* d_bgest = nullptr;
+  FrameCtl* d_ctl = nullptr;
+  int* d_cellstart = nullptr;
+  unsigned* d_err = nullptr;
+  unsigned short* d_roi = nullptr;
+  void* d_stage = nullptr;
+  size_t stage_bytes = 0;
+
+  // peaks
+  int cap_total = 0;
+  std::vector<int> pk_off, cap_f, nfit;
+  PeakRec* d_pk = nullptr;
+  PeakRec* d_snap = nullptr;
+  int* d_pkoff = nullptr;
+  int* d_nfit = nullptr;
+  int* d_run = nullptr;
+  unsigned* d_anchor = nullptr;
+  int* d_done = nullptr;
+  int* d_cellitems = nullptr;
+  int* d_stepctr = nullptr;
+
+  // scheduling
+  cudaStream_t stream = 0;
+  int epoch = 0;
+  int sweep_grid = 0;
+  size_t sweep_smem = 0, cta_smem = 0, warp_smem = 0;
+  bool configured = false;
+
+  // host mirrors
+  std::vector<PeakRec> host_pk;   // frame 0 records (valid when host_valid)
+  bool host_valid = false;
+  long long ctr_seen[NCOUNTERS] = {0};
+  int unconv_cache = -1;
+
+  // timing
+  bool timing = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double sweep_ms = 0.0;
+  long long sweep_launches = 0, ticks = 0;
+
+  ~Engine() { release(); }
+
+  void release_peaks() {
+    dfree(d_pk); dfree(d_snap); dfree(d_pkoff); dfree(d_nfit); dfree(d_run); dfree(d_anchor);
+    dfree(d_done); dfree(d_cellitems); dfree(d_stepctr);
+    cap_total = 0;
+  }
+  void release() {
+    release_peaks();
+    dfree(d_x); dfree(d_rqe); dfree(d_scmos); dfree(d_aij); dfree(d_f); dfree(d_bg); dfree(d_cnt);
+    dfree(d_bgest); dfree(d_ctl); dfree(d_cellstart); dfree(d_err); dfree(d_roi); dfree(d_stage);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    ev0 = ev1 = nullptr;
+    F = 0;
+  }
+
+  size_t tsize() const { return prec == 32 ? sizeof(float) : sizeof(double); }
+
+  template <typename T>
+  FrameSet<T> fs() const {
+    FrameSet<T> s;
+    s.F = F;
+    s.npix = npix;
+    s.x = (const T*)d_x;
+    s.rqe = (const T*)d_rqe;
+    s.scmos = (const T*)d_scmos;
+    s.f = d_f;
+    s.bg = d_bg;
+    s.cnt = d_cnt;
+    s.bgest = d_bgest;
+    s.aij = (const T*)d_aij;
+    s.pk = d_pk;
+    s.snap = d_snap;
+    s.pk_off = d_pkoff;
+    s.nfit = d_nfit;
+    s.run = d_run;
+    s.anchor0 = d_anchor;
+    s.done = d_done;
+    s.cell_start = d_cellstart;
+    s.cell_items = d_cellitems;
+    s.stepctr = d_stepctr;
+    s.ctl = d_ctl;
+    s.err_flag = d_err;
+    s.roi_xy = d_roi;
+    return s;
+  }
+
+  int stage(size_t bytes) {
+    if (bytes <= stage_bytes) return 0;
+    dfree(d_stage);
+    CK(cudaMalloc(&d_stage, bytes));
+    stage_bytes = bytes;
+    return 0;
+  }
+
+  // Convert a double host array to the pixel type on the device.
+  int upload_t(void** dst, const double* src, size_t n) {
+    dfree(*dst);
+    CK(cudaMalloc(dst, n * tsize()));
+    if (prec == 32) {
+      std::vector<float> tmp(src, src + n);
+      CK(cudaMemcpy(*dst, tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    } else {
+      CK(cudaMemcpy(*dst, src, n * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    return 0;
+  }
+
+  int configure() {
+    if (configured) return 0;
+    if (!model_set) {
+      set_error("the fitting model has not been initialised");
+      return -1;
+    }
+    cudaError_t e = (prec == 32) ? Launch<float>::configure(cfg, &sweep_grid, &sweep_smem, &cta_smem, &warp_smem)
+                                 : Launch<double>::configure(cfg, &sweep_grid, &sweep_smem, &cta_smem, &warp_smem);
+    if (e != cudaSuccess) {
+      set_error("kernel configuration failed (ROI %d, %d pixels): %s", cfg.roi, cfg.nroi,
+                cudaGetErrorString(e));
+      return -1;
+    }
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
+    configured = true;
+    return 0;
+  }
+
+  // Allocate the frame arrays for n frames (keeps contents when unchanged).
+  int set_frames(int n) {
+    if (configure()) return -1;
+    if (n == F && d_x) return 0;
+    dfree(d_x); dfree(d_f); dfree(d_bg); dfree(d_cnt); dfree(d_bgest); dfree(d_ctl); dfree(d_cellstart);
+    const size_t np = (size_t)npix * n;
+    CK(cudaMalloc(&d_x, np * tsize()));
+    CK(cudaMalloc(&d_f, np * sizeof(long long)));
+    CK(cudaMalloc(&d_bg, np * sizeof(long long)));
+    CK(cudaMalloc(&d_cnt, np * sizeof(int)));
+    CK(cudaMalloc(&d_bgest, np * sizeof(double)));
+    CK(cudaMemset(d_f, 0, np * sizeof(long long)));
+    CK(cudaMemset(d_bg, 0, np * sizeof(long long)));
+    CK(cudaMemset(d_cnt, 0, np * sizeof(int)));
+    CK(cudaMemset(d_bgest, 0, np * sizeof(double)));
+    CK(cudaMalloc(&d_ctl, sizeof(FrameCtl) * n));
+    CK(cudaMemset(d_ctl, 0, sizeof(FrameCtl) * n));
+    CK(cudaMalloc(&d_cellstart, sizeof(int) * (size_t)n * (cfg.gx * cfg.gy + 1)));
+    if (!d_err) {
+      CK(cudaMalloc(&d_err, sizeof(unsigned)));
+      CK(cudaMemset(d_err, 0, sizeof(unsigned)));
+    }
+    if (!d_rqe) {
+      if (upload_t(&d_rqe, rqe_h.data(), npix)) return -1;
+      if (upload_t(&d_scmos, scmos_h.data(), npix)) return -1;
+      if (!aij_h.empty() && upload_t(&d_aij, aij_h.data(), aij_h.size())) return -1;
+      CK(cudaMalloc(&d_roi, roi_xy.size() * sizeof(unsigned short)));
+      CK(cudaMemcpy(d_roi, roi_xy.data(), roi_xy.size() * sizeof(unsigned short), cudaMemcpyHostToDevice));
+    }
+    F = n;
+    pk_off.assign(n, 0);
+    cap_f.assign(n, 0);
+    nfit.assign(n, 0);
+    release_peaks();
+    host_pk.clear();
+    host_valid = true;
+    return 0;
+  }
+
+  // Peak storage: capacity caps[f] per frame (contents dropped).
+  int set_peak_caps(const std::vector<int>& caps) {
+    release_peaks();
+    int tot = 0;
+    for (int f = 0; f < F; f++) {
+      pk_off[f] = tot;
+      cap_f[f] = caps[f];
+      tot += caps[f];
+    }
+    cap_total = std::max(tot, 1);
+    const size_t c = cap_total;
+    CK(cudaMalloc(&d_pk, c * sizeof(PeakRec)));
+    CK(cudaMalloc(&d_snap, c * sizeof(PeakRec)));
+    CK(cudaMalloc(&d_run, c * sizeof(int)));
+    CK(cudaMalloc(&d_anchor, c * sizeof(unsigned)));
+    CK(cudaMalloc(&d_done, c * sizeof(int)));
+    CK(cudaMalloc(&d_cellitems, c * sizeof(int)));
+    CK(cudaMalloc(&d_stepctr, c * NCOUNTERS * sizeof(int)));
+    CK(cudaMemset(d_pk, 0, c * sizeof(PeakRec)));
+    CK(cudaMemset(d_done, 0xff, c * sizeof(int)));
+    CK(cudaMemset(d_stepctr, 0, c * NCOUNTERS * sizeof(int)));
+    CK(cudaMalloc(&d_pkoff, F * sizeof(int)));
+    CK(cudaMalloc(&d_nfit, F * sizeof(int)));
+    CK(cudaMemcpy(d_pkoff, pk_off.data(), F * sizeof(int), cudaMemcpyHostToDevice));
+    return sync_nfit();
+  }
+
+  int sync_nfit() {
+    CK(cudaMemcpyAsync(d_nfit, nfit.data(), F * sizeof(int), cudaMemcpyHostToDevice, stream));
+    return 0;
+  }
+
+  int check_err_flag() {
+    unsigned e = 0;
+    CK(cudaMemcpy(&e, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (e) {
+      cudaMemset(d_err, 0, sizeof(unsigned));
+      set_error("device wait timed out (flag 0x%x); results of this call are invalid", e);
+      return -1;
+    }
+    return 0;
+  }
+
+  int tick() {
+    ticks++;
+    if (prec == 32) {
+      FrameSet<float> s = fs<float>();
+      CK(Launch<float>::prepare(cfg, s, cta_smem, stream));
+      epoch++;
+      if (timing) CK(cudaEventRecord(ev0, stream));
+      CK(Launch<float>::sweep(cfg, s, epoch, sweep_grid, sweep_smem, stream));
+      if (timing) CK(cudaEventRecord(ev1, stream));
+      CK(Launch<float>::post(cfg, s, cta_smem, stream));
+    } else {
+      FrameSet<double> s = fs<double>();
+      CK(Launch<double>::prepare(cfg, s, cta_smem, stream));
+      epoch++;
+      if (timing) CK(cudaEventRecord(ev0, stream));
+      CK(Launch<double>::sweep(cfg, s, epoch, sweep_grid, sweep_smem, stream));
+      if (timing) CK(cudaEventRecord(ev1, stream));
+      CK(Launch<double>::post(cfg, s, cta_smem, stream));
+    }
+    if (timing) {
+      CK(cudaEventSynchronize(ev1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, ev0, ev1));
+      sweep_ms += ms;
+      sweep_launches++;
+    }
+    return 0;
+  }
+
+  // Run ticks until no frame is pending.  Frames start in SWEEP_PENDING
+  // with max_sweeps set by the caller.
+  int run_until_done(std::vector<FrameCtl>& ctl) {
+    for (;;) {
+      const int burst = 2;
+      for (int i = 0; i < burst; i++)
+        if (tick()) return -1;
+      CK(cudaMemcpyAsync(ctl.data(), d_ctl, sizeof(FrameCtl) * F, cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
+      if (check_err_flag()) return -1;
+      bool active = false;
+      for (int f = 0; f < F; f++)
+        if (ctl[f].phase != PH_DONE && ctl[f].phase != PH_IDLE) active = true;
+      if (!active) break;
+    }
+    return 0;
+  }
+
+  // Start a fit (max_sweeps sweeps at most) on all frames and run it.
+  int fit(int max_sweeps, int* sweeps_out) {
+    if (!d_pk) {
+      if (sweeps_out) *sweeps_out = 0;
+      return 0;
+    }
+    std::vector<FrameCtl> ctl(F);
+    CK(cudaMemcpy(ctl.data(), d_ctl, sizeof(FrameCtl) * F, cudaMemcpyDeviceToHost));
+    for (int f = 0; f < F; f++) {
+      ctl[f].phase = PH_SWEEP_PENDING;
+      ctl[f].sweeps = 0;
+      ctl[f].max_sweeps = max_sweeps;
+    }
+    CK(cudaMemcpy(d_ctl, ctl.data(), sizeof(FrameCtl) * F, cudaMemcpyHostToDevice));
+    if (run_until_done(ctl)) return -1;
+    int sw = 0;
+    for (int f = 0; f < F; f++) sw = std::max(sw, ctl[f].sweeps);
+    unconv_cache = (F == 1) ? ctl[0].unconverged : -1;
+    host_valid = false;
+    if (sweeps_out) *sweeps_out = sw;
+    return 0;
+  }
+
+  int pull_records() {
+    if (host_valid) return 0;
+    host_pk.resize(nfit[0]);
+    if (nfit[0] > 0)
+      CK(cudaMemcpy(host_pk.data(), d_pk + pk_off[0], sizeof(PeakRec) * nfit[0], cudaMemcpyDeviceToHost));
+    host_valid = true;
+    return 0;
+  }
+
+  int push_records() {
+    if (!host_pk.empty())
+      CK(cudaMemcpy(d_pk + pk_off[0], host_pk.data(), sizeof(PeakRec) * host_pk.size(), cudaMemcpyHostToDevice));
+    nfit[0] = (int)host_pk.size();
+    if (sync_nfit()) return -1;
+    CK(cudaStreamSynchronize(stream));
+    host_valid = true;
+    unconv_cache = -1;
+    return 0;
+  }
+
+  int read_counters(long long* out) {
+    std::vector<FrameCtl> ctl(F);
+    CK(cudaMemcpy(ctl.data(), d_ctl, sizeof(FrameCtl) * F, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < NCOUNTERS; i++) out[i] = 0;
+    for (int f = 0; f < F; f++)
+      for (int i = 0; i < NCOUNTERS; i++) out[i] += ctl[f].ctr[i];
+    return 0;
+  }
+};
+
+Engine* E(saFitData* h) { return h ? reinterpret_cast<Engine*>(h->engine) : nullptr; }
+
+// Fold new device counter totals into the reference-layout fields.
+void sync_counters(saFitData* h) {
+  Engine* e = E(h);
+  if (!e || !e->d_ctl) return;
+  long long tot[NCOUNTERS];
+  if (e->read_counters(tot)) return;
+  int* fields[8] = {&h->n_dposv, &h->n_iterations, &h->n_lost, &h->n_margin,
+                    &h->n_neg_fi, &h->n_neg_height, &h->n_non_converged, &h->n_non_decr};
+  for (int i = 0; i < 8; i++) {
+    *fields[i] += (int)(tot[i] - e->ctr_seen[i]);
+    e->ctr_seen[i] = tot[i];
+  }
+  e->ctr_seen[C_STARTFAIL] = tot[C_STARTFAIL];
+}
+
+// Circular ROI, mFitInitializeROIIndexing multi_fit.c:1031-1060.
+void roi_index(Engine* e, int roi) {
+  const double c = 0.5 * (double)roi, rr = c * c;
+  e->roi_x.clear();
+  e->roi_y.clear();
+  e->roi_xy.clear();
+  for (int i = 0; i < roi; i++) {
+    const double dy = (double)i - c + 0.5;
+    for (int j = 0; j < roi; j++) {
+      const double dx = (double)j - c + 0.5;
+      if ((dx * dx + dy * dy) <= rr) {
+        e->roi_x.push_back(j);
+        e->roi_y.push_back(i);
+        e->roi_xy.push_back((unsigned short)(j | (i << 8)));
+      }
+    }
+  }
+  e->cfg.roi = roi;
+  e->cfg.nroi = (int)e->roi_x.size();
+}
+
+void finish_geometry(Engine* e) {
+  ModelCfg& c = e->cfg;
+  if (c.dil < 0) c.dil = 2;
+  c.cell = c.roi + 2 * c.dil;
+  // keep the grid small enough for shared memory
+  while ((long long)((c.nx + c.cell - 1) / c.cell) * ((c.ny + c.cell - 1) / c.cell) > 40000) c.cell *= 2;
+  c.gx = (c.nx + c.cell - 1) / c.cell;
+  c.gy = (c.ny + c.cell - 1) / c.cell;
+}
+
+saFitData* new_handle(const double* rqe, const double* scmos, double tol, int nx, int ny) {
+  if (nx <= 0 || ny <= 0 || nx > 65535 || ny > 65535) {
+    set_error("unsupported image size %d x %d", nx, ny);
+    return nullptr;
+  }
+  saFitData* h = (saFitData*)calloc(1, sizeof(saFitData));
+  Engine* e = new Engine();
+  h->engine = e;
+  e->cfg.nx = nx;
+  e->cfg.ny = ny;
+  e->cfg.tol = tol;
+  e->cfg.min_height = -1.0;   // multi_fit.c:965
+  e->cfg.dil = -1;
+  e->npix = (long long)nx * ny;
+  e->rqe_h.assign(rqe, rqe + e->npix);
+  e->scmos_h.assign(scmos, scmos + e->npix);
+  const char* pe = getenv("SA_CUDA_PRECISION");
+  if (pe && atoi(pe) == 64) e->prec = 64;
+  h->image_size_x = nx;
+  h->image_size_y = ny;
+  h->tolerance = tol;
+  h->minimum_height = -1.0;
+  return h;
+}
+
+void publish_geometry(saFitData* h) {
+  Engine* e = E(h);
+  h->fit_size_x = e->cfg.roi;
+  h->fit_size_y = e->cfg.roi;
+  h->roi_n_index = e->cfg.nroi;
+  h->roi_x_index = e->roi_x.data();
+  h->roi_y_index = e->roi_y.data();
+  h->xoff = e->cfg.xoff;
+  h->yoff = e->cfg.yoff;
+  h->zoff = e->cfg.zoff;
+}
+
+void set_model(saFitData* h, int model, int jac) {
+  Engine* e = E(h);
+  if (!e) return;
+  e->cfg.model = model;
+  e->cfg.jac = jac;
+  e->model_set = true;
+  h->jac_size = jac;
+  finish_geometry(e);
+}
+
+void unsupported(saFitData* h, const char* what) {
+  Engine* e = E(h);
+  if (e) e->unsupported = true;
+  set_error("%s: only the MLE error model is implemented by this engine", what);
+}
+
+int parse_ptype(const char* t) {
+  if (!t) return -1;
+  if (!strcmp(t, "finder")) return PT_FINDER;
+  if (!strcmp(t, "testing")) return PT_TESTING;
+  if (!strcmp(t, "text") || !strcmp(t, "hdf5")) return PT_TEXT;
+  return -1;
+}
+
+int ncol_for(const Engine* e, int ptype) {
+  const bool spl = e->cfg.model >= M_SPLINE2D;
+  if (ptype == PT_TEXT) return spl ? 5 : 7;
+  return spl ? 3 : 4;
+}
+
+// Insert new peaks for frames [0, nframes) (rows concatenated per frame).
+int insert_peaks(Engine* e, const double* rows, const std::vector<int>& counts, int ptype) {
+  const int ncol = ncol_for(e, ptype);
+  int n = 0;
+  for (int c : counts) n += c;
+  if (n == 0) return 0;
+  std::vector<int> slots(n), frames(n), ffirst(counts.size()), fn(counts.size());
+  int i = 0;
+  for (size_t f = 0; f < counts.size(); f++) {
+    ffirst[f] = i;
+    fn[f] = counts[f];
+    for (int j = 0; j < counts[f]; j++, i++) {
+      slots[i] = e->pk_off[f] + e->nfit[f] + j;
+      frames[i] = (int)f;
+    }
+  }
+  const size_t rb = (size_t)n * ncol * sizeof(double);
+  const size_t ib = (size_t)n * sizeof(int);
+  const size_t fb = counts.size() * sizeof(int);
+  if (e->stage(rb + 2 * ib + 2 * fb + 64)) return -1;
+  char* st = (char*)e->d_stage;
+  double* d_rows = (double*)st;
+  int* d_slots = (int*)(st + rb);
+  int* d_frames = (int*)(st + rb + ib);
+  int* d_ff = (int*)(st + rb + 2 * ib);
+  int* d_fn = (int*)(st + rb + 2 * ib + fb);
+  CK(cudaMemcpyAsync(d_rows, rows, rb, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(d_slots, slots.data(), ib, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(d_frames, frames.data(), ib, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(d_ff, ffirst.data(), fb, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(d_fn, fn.data(), fb, cudaMemcpyHostToDevice, e->stream));
+  if (e->prec == 32) {
+    FrameSet<float> s = e->fs<float>();
+    CK(Launch<float>::new_peaks(e->cfg, s, d_rows, ncol, ptype, d_slots, d_frames, n,
+                                ptype != PT_FINDER, e->warp_smem, e->stream));
+    if (ptype == PT_FINDER)
+      CK(Launch<float>::new_peaks_finder(e->cfg, s, d_slots, d_ff, d_fn, (int)counts.size(), e->warp_smem, e->stream));
+    CK(Launch<float>::peak_error(e->cfg, s, d_slots, d_frames, n, e->stream));
+  } else {
+    FrameSet<double> s = e->fs<double>();
+    CK(Launch<double>::new_peaks(e->cfg, s, d_rows, ncol, ptype, d_slots, d_frames, n,
+                                 ptype != PT_FINDER, e->warp_smem, e->stream));
+    if (ptype == PT_FINDER)
+      CK(Launch<double>::new_peaks_finder(e->cfg, s, d_slots, d_ff, d_fn, (int)counts.size(), e->warp_smem, e->stream));
+    CK(Launch<double>::peak_error(e->cfg, s, d_slots, d_frames, n, e->stream));
+  }
+  for (size_t f = 0; f < counts.size(); f++) e->nfit[f] += counts[f];
+  if (e->sync_nfit()) return -1;
+  CK(cudaStreamSynchronize(e->stream));
+  e->host_valid = false;
+  e->unconv_cache = -1;
+  return 0;
+}
+
+// mFitNewPeaks storage growth with ERROR compaction (multi_fit.c:1428-1477),
+// single frame.
+int grow_frame0(Engine* e, int n_new) {
+  const int nf = e->nfit[0];
+  if (e->d_pk && nf + n_new <= e->cap_f[0]) return 0;
+  const int n_alloc = 500 * ((nf + n_new) / 500 + 1);
+  std::vector<PeakRec> keep;
+  if (e->d_pk && nf > 0) {
+    if (e->pull_records()) return -1;
+    for (const PeakRec& r : e->host_pk)
+      if (r.status != ERROR) keep.push_back(r);
+  }
+  std::vector<int> caps(1, n_alloc);
+  if (e->set_peak_caps(caps)) return -1;
+  e->host_pk = keep;
+  return e->push_records();
+}
+
+int new_peaks_single(saFitData* h, double* peaks, const char* p_type, int n) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if (e->unsupported) {
+    set_error("handle uses an unsupported error model");
+    return -1;
+  }
+  const int pt = parse_ptype(p_type);
+  if (pt < 0) {
+    set_error("Unrecognized peak type '%s'!", p_type ? p_type : "(null)");
+    return -1;
+  }
+  if (!e->d_x) {
+    set_error("newPeaks before newImage");
+    return -1;
+  }
+  if (n <= 0) return 0;
+  if (grow_frame0(e, n)) return -1;
+  std::vector<int> counts(1, n);
+  if (insert_peaks(e, peaks, counts, pt)) return -1;
+  h->nfit = e->nfit[0];
+  h->max_nfit = e->cap_f[0];
+  sync_counters(h);
+  return 0;
+}
+
+int image_single(saFitData* h, const double* img, bool background) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if (e->set_frames(e->F > 0 ? e->F : 1)) return -1;
+  const size_t bytes = (size_t)e->npix * sizeof(double);
+  if (e->stage(bytes)) return -1;
+  CK(cudaMemcpyAsync(e->d_stage, img, bytes, cudaMemcpyHostToDevice, e->stream));
+  if (e->prec == 32) {
+    FrameSet<float> s = e->fs<float>();
+    CK(background ? Launch<float>::new_background(s, e->d_stage, 64, 0, 1, e->stream)
+                  : Launch<float>::new_image(s, e->d_stage, 64, 0, 1, e->stream));
+  } else {
+    FrameSet<double> s = e->fs<double>();
+    CK(background ? Launch<double>::new_background(s, e->d_stage, 64, 0, 1, e->stream)
+                  : Launch<double>::new_image(s, e->d_stage, 64, 0, 1, e->stream));
+  }
+  CK(cudaStreamSynchronize(e->stream));
+  if (!background) {
+    // mFitNewImage resets nfit (multi_fit.c:1407)
+    e->nfit[0] = 0;
+    if (e->sync_nfit()) return -1;
+    e->host_pk.clear();
+    e->host_valid = true;
+    e->unconv_cache = -1;
+    h->nfit = 0;
+  }
+  return 0;
+}
+
+int props_device(Engine* e, int frame0, const std::vector<int>& counts, double* sum, double* fg,
+                 double* bg, double* jac) {
+  int n = 0;
+  for (int c : counts) n += c;
+  if (n == 0) return 0;
+  std::vector<int> slots(n), frames(n);
+  int i = 0;
+  for (size_t f = 0; f < counts.size(); f++)
+    for (int j = 0; j < counts[f]; j++, i++) {
+      slots[i] = e->pk_off[frame0 + f] + j;
+      frames[i] = frame0 + (int)f;
+    }
+  const int k = e->cfg.jac;
+  const size_t ib = (size_t)n * sizeof(int);
+  const size_t db = (size_t)n * sizeof(double);
+  const size_t jb = (size_t)n * k * sizeof(double);
+  if (e->stage(2 * ib + 3 * db + jb + 64)) return -1;
+  char* st = (char*)e->d_stage;
+  int* d_slots = (int*)st;
+  int* d_frames = (int*)(st + ib);
+  double* d_sum = (double*)(st + 2 * ib);
+  double* d_fg = d_sum + n;
+  double* d_bg = d_fg + n;
+  double* d_jac = d_bg + n;
+  CK(cudaMemcpyAsync(d_slots, slots.data(), ib, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(d_frames, frames.data(), ib, cudaMemcpyHostToDevice, e->stream));
+  if (e->prec == 32)
+    CK(Launch<float>::peak_props(e->cfg, e->fs<float>(), d_slots, d_frames, n, d_sum, d_fg, d_bg,
+                                 jac ? d_jac : nullptr, e->warp_smem, e->stream));
+  else
+    CK(Launch<double>::peak_props(e->cfg, e->fs<double>(), d_slots, d_frames, n, d_sum, d_fg, d_bg,
+                                  jac ? d_jac : nullptr, e->warp_smem, e->stream));
+  if (sum) CK(cudaMemcpyAsync(sum, d_sum, db, cudaMemcpyDeviceToHost, e->stream));
+  if (fg) CK(cudaMemcpyAsync(fg, d_fg, db, cudaMemcpyDeviceToHost, e->stream));
+  if (bg) CK(cudaMemcpyAsync(bg, d_bg, db, cudaMemcpyDeviceToHost, e->stream));
+  if (jac) CK(cudaMemcpyAsync(jac, d_jac, jb, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+// Property of one record (multi_fit.c:754-868); returns false if unknown.
+bool record_prop(const Engine* e, const PeakRec& r, const char* what, double* v) {
+  if (!strcmp(what, "background")) *v = r.p[PBG];
+  else if (!strcmp(what, "error")) *v = r.error;
+  else if (!strcmp(what, "height")) *v = r.p[PH];
+  else if (!strcmp(what, "x")) *v = r.p[PX] + e->cfg.xoff;
+  else if (!strcmp(what, "xsigma")) *v = sqrt(1.0 / (2.0 * r.p[PXW]));
+  else if (!strcmp(what, "y")) *v = r.p[PY] + e->cfg.yoff;
+  else if (!strcmp(what, "ysigma")) *v = sqrt(1.0 / (2.0 * r.p[PYW]));
+  else if (!strcmp(what, "z")) *v = r.p[PZ] + e->cfg.zoff;
+  else return false;
+  return true;
+}
+
+int get_double_props(Engine* e, int frame0, int nframes, double* values, const char* what) {
+  std::vector<int> counts(e->nfit.begin() + frame0, e->nfit.begin() + frame0 + nframes);
+  int n = 0;
+  for (int c : counts) n += c;
+  if (!strcmp(what, "bg_sum") || !strcmp(what, "fg_sum") || !strcmp(what, "fg_sum_sc") ||
+      !strcmp(what, "sum") || !strcmp(what, "jacobian")) {
+    std::vector<double> a(n), b(n), c(n);
+    std::vector<double> jac;
+    const bool jj = !strcmp(what, "jacobian");
+    if (jj) jac.resize((size_t)n * e->cfg.jac);
+    if (props_device(e, frame0, counts, a.data(), b.data(), c.data(), jj ? jac.data() : nullptr)) return -1;
+    const std::vector<double>& src = jj ? jac : (!strcmp(what, "sum") ? a : (!strcmp(what, "bg_sum") ? c : b));
+    memcpy(values, src.data(), src.size() * sizeof(double));
+    return 0;
+  }
+  std::vector<PeakRec> recs(n);
+  size_t o = 0;
+  for (int f = 0; f < nframes; f++) {
+    if (counts[f] > 0)
+      CK(cudaMemcpy(recs.data() + o, e->d_pk + e->pk_off[frame0 + f], sizeof(PeakRec) * counts[f],
+                    cudaMemcpyDeviceToHost));
+    o += counts[f];
+  }
+  for (int i = 0; i < n; i++) {
+    if (!record_prop(e, recs[i], what, values + i)) {
+      set_error("Unrecognized parameter '%s'!", what);
+      return -1;
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+int saGetLastError(char* buf, int len) {
+  const int n = (int)g_last_error.size();
+  if (buf && len > 0) {
+    strncpy(buf, g_last_error.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return n;
+}
+
+void saClearLastError(void) { g_last_error.clear(); }
+
+int saDeviceCount(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+saFitData* daoInitialize(double* rqe, double* scmos, double tol, int nx, int ny, int roi) {
+  if (roi < 2 || roi > MAX_ROI || roi > 255) {
+    set_error("unsupported ROI size %d (2..%d)", roi, MAX_ROI);
+    return nullptr;
+  }
+  saFitData* h = new_handle(rqe, scmos, tol, nx, ny);
+  if (!h) return nullptr;
+  Engine* e = E(h);
+  roi_index(e, roi);
+  // dao_fit.c:1264-1271: the same offset for even and odd ROI sizes.
+  e->cfg.xoff = 0.5 * ((double)roi) - 1.0;
+  e->cfg.yoff = e->cfg.xoff;
+  publish_geometry(h);
+  return h;
+}
+
+void daoInitialize2DFixed(saFitData* h) { set_model(h, M_2DFIXED, 4); }
+
+void daoInitialize2D(saFitData* h, double wmin, double wmax) {
+  if (!E(h)) return;
+  E(h)->cfg.wmin = wmin;
+  E(h)->cfg.wmax = wmax;
+  set_model(h, M_2D, 5);
+}
+
+void daoInitialize3D(saFitData* h, double wmin, double wmax) {
+  if (!E(h)) return;
+  E(h)->cfg.wmin = wmin;
+  E(h)->cfg.wmax = wmax;
+  set_model(h, M_3D, 6);
+}
+
+void daoInitializeZ(saFitData* h, double* wx, double* wy, double zmin, double zmax) {
+  Engine* e = E(h);
+  if (!e) return;
+  for (int i = 0; i < 5; i++) {
+    e->cfg.wx[i] = wx[i];
+    e->cfg.wy[i] = wy[i];
+  }
+  // dao_fit.c:1566-1567: w0 squared
+  e->cfg.wx[0] = e->cfg.wx[0] * e->cfg.wx[0];
+  e->cfg.wy[0] = e->cfg.wy[0] * e->cfg.wy[0];
+  e->cfg.zmin = zmin;
+  e->cfg.zmax = zmax;
+  set_model(h, M_Z, 5);
+}
+
+void daoInitialize2DFixedALS(saFitData* h) { unsupported(h, "daoInitialize2DFixedALS"); }
+void daoInitialize2DFixedLS(saFitData* h) { unsupported(h, "daoInitialize2DFixedLS"); }
+void daoInitialize2DFixedDWLS(saFitData* h) { unsupported(h, "daoInitialize2DFixedDWLS"); }
+void daoInitialize2DFixedFWLS(saFitData* h) { unsupported(h, "daoInitialize2DFixedFWLS"); }
+void daoInitialize2DALS(saFitData* h, double, double) { unsupported(h, "daoInitialize2DALS"); }
+void daoInitialize2DLS(saFitData* h, double, double) { unsupported(h, "daoInitialize2DLS"); }
+void daoInitialize2DDWLS(saFitData* h, double, double) { unsupported(h, "daoInitialize2DDWLS"); }
+void daoInitialize2DFWLS(saFitData* h, double, double) { unsupported(h, "daoInitialize2DFWLS"); }
+void cfInitialize3DALS(saFitData* h) { unsupported(h, "cfInitialize3DALS"); }
+void cfInitialize3DLS(saFitData* h) { unsupported(h, "cfInitialize3DLS"); }
+void cfInitialize3DFWLS(saFitData* h) { unsupported(h, "cfInitialize3DFWLS"); }
+void mFitAnscombeTransformImage(saFitData* h) { unsupported(h, "mFitAnscombeTransformImage"); }
+
+void daoNewPeaks(saFitData* h, double* peaks, char* p_type, int n) { new_peaks_single(h, peaks, p_type, n); }
+void cfNewPeaks(saFitData* h, double* peaks, char* p_type, int n) { new_peaks_single(h, peaks, p_type, n); }
+
+void daoCleanup(saFitData* h) {
+  if (!h) return;
+  delete E(h);
+  free(h);
+}
+
+void* initSpline2D(double* aij, int xs, int ys) {
+  SplineH* s = new SplineH();
+  s->type = 0;
+  s->xs = xs;
+  s->ys = ys;
+  s->zs = 0;
+  s->aij.assign(aij, aij + (size_t)xs * ys * 16);
+  return s;
+}
+
+void* initSpline3D(double* aij, int xs, int ys, int zs) {
+  SplineH* s = new SplineH();
+  s->type = 1;
+  s->xs = xs;
+  s->ys = ys;
+  s->zs = zs;
+  s->aij.assign(aij, aij + (size_t)xs * ys * zs * 64);
+  return s;
+}
+
+void splineCleanup(void* sp) { delete reinterpret_cast<SplineH*>(sp); }
+int getXSize(void* sp) { return sp ? reinterpret_cast<SplineH*>(sp)->xs : 0; }
+int getYSize(void* sp) { return sp ? reinterpret_cast<SplineH*>(sp)->ys : 0; }
+int getZSize(void* sp) { return sp ? reinterpret_cast<SplineH*>(sp)->zs : 0; }
+
+saFitData* cfInitialize(void* spline, double* rqe, double* scmos, double tol, int nx, int ny) {
+  SplineH* s = reinterpret_cast<SplineH*>(spline);
+  if (!s) {
+    set_error("cfInitialize: NULL spline");
+    return nullptr;
+  }
+  const int sx = s->xs - 1, sy = s->ys - 1;
+  if (sx != sy) {
+    // The reference exits the process here (cubic_fit.c:646-649).
+    set_error("PSF must be square in X/Y!");
+    return nullptr;
+  }
+  if (sx < 2 || sx > MAX_ROI) {
+    set_error("unsupported spline size %d", s->xs);
+    return nullptr;
+  }
+  saFitData* h = new_handle(rqe, scmos, tol, nx, ny);
+  if (!h) return nullptr;
+  Engine* e = E(h);
+  e->spline = s;
+  e->cfg.sx = s->xs;
+  e->cfg.sy = s->ys;
+  e->cfg.sz = s->zs;
+  e->aij_h = s->aij;
+  // cubic_fit.c:627-641
+  if ((sx % 2) == 1) {
+    e->cfg.xoff = (double)(sx / 2) - 0.5;
+    e->cfg.yoff = (double)(sy / 2) - 0.5;
+  } else {
+    e->cfg.xoff = (double)(sx / 2) - 1.0;
+    e->cfg.yoff = (double)(sy / 2) - 1.0;
+  }
+  roi_index(e, sx);
+  publish_geometry(h);
+  return h;
+}
+
+void cfInitialize2D(saFitData* h) {
+  Engine* e = E(h);
+  if (!e) return;
+  if (e->spline && e->spline->type != 0) {
+    set_error("cfInitialize2D needs a 2D spline");
+    e->unsupported = true;
+    return;
+  }
+  set_model(h, M_SPLINE2D, 4);
+}
+
+void cfInitialize3D(saFitData* h) {
+  Engine* e = E(h);
+  if (!e) return;
+  if (e->spline && e->spline->type != 1) {
+    set_error("cfInitialize3D needs a 3D spline");
+    e->unsupported = true;
+    return;
+  }
+  set_model(h, M_SPLINE3D, 5);
+}
+
+void cfCleanup(saFitData* h) {
+  if (!h) return;
+  Engine* e = E(h);
+  if (e && e->spline) {
+    delete e->spline;
+    e->spline = nullptr;
+  }
+  daoCleanup(h);
+}
+
+void mFitNewImage(saFitData* h, double* img) { image_single(h, img, false); }
+void mFitNewBackground(saFitData* h, double* bg) { image_single(h, bg, true); }
+
+void mFitIterateLM(saFitData* h) {
+  Engine* e = E(h);
+  if (!e || !e->d_x) return;
+  int sw = 0;
+  e->fit(1, &sw);
+  sync_counters(h);
+}
+
+int saDoFit(saFitData* h, int max_iterations) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if (!e->d_x) {
+    set_error("doFit before newImage");
+    return -1;
+  }
+  int sw = 0;
+  if (e->fit(max_iterations + 1, &sw)) return -1;
+  sync_counters(h);
+  return sw;
+}
+
+int mFitGetUnconverged(saFitData* h) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk) return 0;
+  if (e->unconv_cache >= 0) return e->unconv_cache;
+  if (e->pull_records()) return 0;
+  int c = 0;
+  for (const PeakRec& r : e->host_pk) c += (r.status == RUNNING);
+  e->unconv_cache = c;
+  return c;
+}
+
+int mFitGetNError(saFitData* h) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk) return 0;
+  if (e->pull_records()) return 0;
+  int c = 0;
+  for (const PeakRec& r : e->host_pk) c += (r.status == ERROR);
+  return c;
+}
+
+void mFitGetPeakPropertyDouble(saFitData* h, double* values, char* what) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk || e->nfit[0] == 0) return;
+  get_double_props(e, 0, 1, values, what);
+}
+
+void mFitGetPeakPropertyInt(saFitData* h, int32_t* values, char* what) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk || e->nfit[0] == 0) return;
+  const bool it = !strcmp(what, "iterations");
+  if (!it && strcmp(what, "status")) {
+    set_error("Unrecognized parameter '%s'!", what);
+    return;
+  }
+  if (e->pull_records()) return;
+  for (size_t i = 0; i < e->host_pk.size(); i++)
+    values[i] = it ? e->host_pk[i].iterations : e->host_pk[i].status;
+}
+
+static void fit_image_common(saFitData* h, double* out, int residual) {
+  Engine* e = E(h);
+  if (!e || !e->d_x) return;
+  const size_t bytes = (size_t)e->npix * sizeof(double);
+  if (e->stage(bytes)) return;
+  cudaError_t err = (e->prec == 32)
+                        ? Launch<float>::fit_image(e->fs<float>(), 0, (double*)e->d_stage, residual, e->stream)
+                        : Launch<double>::fit_image(e->fs<double>(), 0, (double*)e->d_stage, residual, e->stream);
+  if (err != cudaSuccess) {
+    set_error("fit image: %s", cudaGetErrorString(err));
+    return;
+  }
+  cudaMemcpyAsync(out, e->d_stage, bytes, cudaMemcpyDeviceToHost, e->stream);
+  cudaStreamSynchronize(e->stream);
+}
+
+void mFitGetFitImage(saFitData* h, double* out) { fit_image_common(h, out, 0); }
+void mFitGetResidual(saFitData* h, double* out) { fit_image_common(h, out, 1); }
+
+void mFitSetPeakStatus(saFitData* h, int32_t* status) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk) return;
+  const int n = e->nfit[0];
+  if (n == 0) return;
+  std::vector<int> slots(n), frames(n, 0);
+  for (int i = 0; i < n; i++) slots[i] = e->pk_off[0] + i;
+  const size_t ib = (size_t)n * sizeof(int);
+  if (e->stage(3 * ib)) return;
+  int* d_slots = (int*)e->d_stage;
+  int* d_frames = d_slots + n;
+  int* d_status = d_frames + n;
+  cudaMemcpyAsync(d_slots, slots.data(), ib, cudaMemcpyHostToDevice, e->stream);
+  cudaMemcpyAsync(d_frames, frames.data(), ib, cudaMemcpyHostToDevice, e->stream);
+  cudaMemcpyAsync(d_status, status, ib, cudaMemcpyHostToDevice, e->stream);
+  cudaError_t err = (e->prec == 32)
+                        ? Launch<float>::set_status(e->cfg, e->fs<float>(), d_slots, d_frames, d_status, n, e->warp_smem, e->stream)
+                        : Launch<double>::set_status(e->cfg, e->fs<double>(), d_slots, d_frames, d_status, n, e->warp_smem, e->stream);
+  if (err != cudaSuccess) set_error("set status: %s", cudaGetErrorString(err));
+  cudaStreamSynchronize(e->stream);
+  e->host_valid = false;
+  e->unconv_cache = -1;
+}
+
+static void remove_peaks(saFitData* h, int drop_status) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk) return;
+  if (e->pull_records()) return;
+  std::vector<PeakRec> keep;
+  keep.reserve(e->host_pk.size());
+  for (const PeakRec& r : e->host_pk) {
+    if (r.status != drop_status) keep.push_back(r);
+    else if (drop_status == RUNNING) h->n_non_converged++;   // multi_fit.c:1775
+  }
+  e->host_pk = keep;
+  e->push_records();
+  h->nfit = e->nfit[0];
+}
+
+void mFitRemoveErrorPeaks(saFitData* h) { remove_peaks(h, ERROR); }
+void mFitRemoveRunningPeaks(saFitData* h) { remove_peaks(h, RUNNING); }
+
+int saSetPrecision(saFitData* h, int bits) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if (bits != 32 && bits != 64) {
+    set_error("precision must be 32 or 64");
+    return -1;
+  }
+  if (e->configured && e->prec != bits) {
+    set_error("precision must be set before the first image");
+    return -1;
+  }
+  e->prec = bits;
+  return 0;
+}
+
+int saSetDilation(saFitData* h, int pixels) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if (e->configured || pixels < 0 || pixels > 16) {
+    set_error("dilation must be 0..16 and set before the first image");
+    return -1;
+  }
+  e->cfg.dil = pixels;
+  if (e->model_set) finish_geometry(e);
+  return 0;
+}
+
+int saSetStream(saFitData* h, void* stream) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  e->stream = (cudaStream_t)stream;
+  return 0;
+}
+
+int saGetCounters(saFitData* h, int64_t* out) {
+  Engine* e = E(h);
+  if (!e || !e->d_ctl) {
+    for (int i = 0; i < NCOUNTERS; i++) out[i] = 0;
+    return 0;
+  }
+  long long tot[NCOUNTERS];
+  if (e->read_counters(tot)) return -1;
+  for (int i = 0; i < NCOUNTERS; i++) out[i] = tot[i];
+  return 0;
+}
+
+int saGetSchedStats(saFitData* h, int64_t* out2) {
+  Engine* e = E(h);
+  if (!e || !e->d_ctl) {
+    out2[0] = out2[1] = 0;
+    return 0;
+  }
+  std::vector<FrameCtl> ctl(e->F);
+  CK(cudaMemcpy(ctl.data(), e->d_ctl, sizeof(FrameCtl) * e->F, cudaMemcpyDeviceToHost));
+  long long reruns = 0, barriers = 0;
+  for (const FrameCtl& c : ctl) {
+    reruns += c.attempts > 1 ? c.attempts - 1 : 0;
+    barriers += c.n_barrier;
+  }
+  out2[0] = reruns;
+  out2[1] = barriers;
+  return 0;
+}
+
+int saSetFrames(saFitData* h, int n_frames, int cap) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if (n_frames <= 0) {
+    set_error("n_frames must be positive");
+    return -1;
+  }
+  if (e->set_frames(n_frames)) return -1;
+  std::vector<int> caps(n_frames, std::max(cap, 1));
+  if (e->set_peak_caps(caps)) return -1;
+  h->nfit = 0;
+  h->max_nfit = caps[0];
+  return 0;
+}
+
+int saNewImages(saFitData* h, const void* images, int n_frames, int bits, int on_device) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if (n_frames != e->F) {
+    set_error("saNewImages: %d frames given, frame set holds %d", n_frames, e->F);
+    return -1;
+  }
+  if (bits != 16 && bits != 32 && bits != 64) {
+    set_error("saNewImages: dtype bits must be 16, 32 or 64");
+    return -1;
+  }
+  const void* src = images;
+  if (!on_device) {
+    const size_t bytes = (size_t)e->npix * n_frames * (bits / 8);
+    if (e->stage(bytes)) return -1;
+    CK(cudaMemcpyAsync(e->d_stage, images, bytes, cudaMemcpyHostToDevice, e->stream));
+    src = e->d_stage;
+  }
+  if (e->prec == 32) CK(Launch<float>::new_image(e->fs<float>(), src, bits, 0, n_frames, e->stream));
+  else CK(Launch<double>::new_image(e->fs<double>(), src, bits, 0, n_frames, e->stream));
+  std::fill(e->nfit.begin(), e->nfit.end(), 0);
+  if (e->sync_nfit()) return -1;
+  e->host_pk.clear();
+  e->host_valid = true;
+  e->unconv_cache = -1;
+  h->nfit = 0;
+  return 0;
+}
+
+int saNewBackgrounds(saFitData* h, const void* bgs, int n_frames, int bits, int on_device) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if (n_frames != e->F || (bits != 32 && bits != 64)) {
+    set_error("saNewBackgrounds: bad frame count or dtype");
+    return -1;
+  }
+  const void* src = bgs;
+  if (!on_device) {
+    const size_t bytes = (size_t)e->npix * n_frames * (bits / 8);
+    if (e->stage(bytes)) return -1;
+    CK(cudaMemcpyAsync(e->d_stage, bgs, bytes, cudaMemcpyHostToDevice, e->stream));
+    src = e->d_stage;
+  }
+  if (e->prec == 32) CK(Launch<float>::new_background(e->fs<float>(), src, bits, 0, n_frames, e->stream));
+  else CK(Launch<double>::new_background(e->fs<double>(), src, bits, 0, n_frames, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+int saNewPeaksBatch(saFitData* h, const double* peaks, const int32_t* counts, int n_frames,
+                    const char* p_type) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  const int pt = parse_ptype(p_type);
+  if (pt < 0) {
+    set_error("Unrecognized peak type '%s'!", p_type ? p_type : "(null)");
+    return -1;
+  }
+  if (n_frames != e->F || !e->d_pk) {
+    set_error("saNewPeaksBatch: frame set not prepared (saSetFrames)");
+    return -1;
+  }
+  std::vector<int> cnt(counts, counts + n_frames);
+  for (int f = 0; f < n_frames; f++) {
+    if (e->nfit[f] + cnt[f] > e->cap_f[f]) {
+      set_error("saNewPeaksBatch: frame %d needs %d peaks, capacity %d", f, e->nfit[f] + cnt[f], e->cap_f[f]);
+      return -1;
+    }
+  }
+  if (insert_peaks(e, peaks, cnt, pt)) return -1;
+  h->nfit = e->nfit[0];
+  return 0;
+}
+
+int saDoFitBatch(saFitData* h, int max_iterations) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  int sw = 0;
+  if (e->fit(max_iterations + 1, &sw)) return -1;
+  sync_counters(h);
+  return sw;
+}
+
+int saGetNFitBatch(saFitData* h, int32_t* counts) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  for (int f = 0; f < e->F; f++) counts[f] = e->nfit[f];
+  return 0;
+}
+
+int saGetPeakPropertyBatch(saFitData* h, double* values, const char* what) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk) return -1;
+  return get_double_props(e, 0, e->F, values, what);
+}
+
+int saGetPeakPropertyIntBatch(saFitData* h, int32_t* values, const char* what) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk) return -1;
+  const bool it = !strcmp(what, "iterations");
+  if (!it && strcmp(what, "status")) {
+    set_error("Unrecognized parameter '%s'!", what);
+    return -1;
+  }
+  size_t o = 0;
+  for (int f = 0; f < e->F; f++) {
+    std::vector<PeakRec> recs(e->nfit[f]);
+    if (e->nfit[f] > 0)
+      CK(cudaMemcpy(recs.data(), e->d_pk + e->pk_off[f], sizeof(PeakRec) * e->nfit[f], cudaMemcpyDeviceToHost));
+    for (const PeakRec& r : recs) values[o++] = it ? r.iterations : r.status;
+  }
+  return 0;
+}
+
+int saSetTiming(saFitData* h, int on) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  e->timing = on != 0;
+  e->sweep_ms = 0.0;
+  e->sweep_launches = 0;
+  e->ticks = 0;
+  return 0;
+}
+
+int saGetTiming(saFitData* h, double* total_ms, int64_t* launches, int64_t* ticks) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  *total_ms = e->sweep_ms;
+  *launches = e->sweep_launches;
+  *ticks = e->ticks;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+// sa_common.cuh -- shared definitions of the GB300 multi-emitter LM engine.
+//
+// Layout in HBM (one "frame set" = F frames of identical size and model):
+//   x      [F][ny*nx]  T      image * rqe + sCMOS term (mFitNewImage, multi_fit.c:1394-1396)
+//   f      [F][ny*nx]  int64  fit image, fixed point 2^-36 (f_data, multi_fit.c:52)
+//   bg     [F][ny*nx]  int64  summed peak backgrounds, fixed point (bg_data, multi_fit.c:54)
+//   cnt    [F][ny*nx]  int32  peaks covering each pixel (bg_counts, multi_fit.c:53)
+//   bgest  [F][ny*nx]  double background estimate * rqe (multi_fit.c:1367)
+//   rqe, scmos [ny*nx] T      shared by all frames (multi_fit.c:972-981)
+//   pk     [peaks]     PeakRec, 128-byte records, frame f at pk_off[f]
+//
+// The fit image and background sums are kept as 64-bit fixed point so that
+// adding and then subtracting a peak restores the pixel bit-exactly and so
+// that contributions of different peaks commute.  That makes recentering,
+// rollback and new-peak insertion order-independent, hence deterministic
+// with plain integer atomics.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sa {
+
+// Parameter slots (multi_fit.h:20-26).
+enum { PH = 0, PX = 1, PXW = 2, PY = 3, PYW = 4, PBG = 5, PZ = 6 };
+// Peak status (multi_fit.h:33-35).
+enum { RUNNING = 0, CONVERGED = 1, ERROR = 2 };
+// Models.
+enum { M_2DFIXED = 0, M_2D = 1, M_3D = 2, M_Z = 3, M_SPLINE2D = 4, M_SPLINE3D = 5 };
+// Counter slots in the reference's fitData order (multi_fit.h:87-94), plus
+// one diagnostic slot of our own: starting-error evaluations that met fi <= 0.
+enum { C_DPOSV = 0, C_ITER, C_LOST, C_MARGIN, C_NEGFI, C_NEGH, C_NONCONV, C_NONDECR, C_STARTFAIL,
+       NCOUNTERS };
+
+// LM schedule (multi_fit.h:42-46).
+constexpr double LAMBDA_START = 1.0;
+constexpr double LAMBDA_DOWN = 0.75;
+constexpr double LAMBDA_MAX = 1.0e+20;
+constexpr double LAMBDA_MIN = 1.0e-3;
+constexpr double LAMBDA_UP = 4.0;
+
+// Fixed point of the fit image / background accumulators.
+constexpr double FX_SCALE = 68719476736.0;        // 2^36
+constexpr double FX_INV = 1.0 / 68719476736.0;
+
+// Peak input formats (dao_fit.c:1603-1753).
+enum { PT_FINDER = 0, PT_TESTING = 1, PT_TEXT = 2 };
+
+// Frame phases of the device-side doFit state machine.
+enum { PH_IDLE = 0, PH_SWEEP_PENDING = 1, PH_IN_SWEEP = 2, PH_RERUN_PENDING = 3, PH_DONE = 4 };
+
+constexpr int MAX_BARRIERS = 48;      // per frame; beyond this the frame runs in index order
+constexpr int MAX_ESCAPES = 48;
+constexpr int MAX_ROI = 64;           // ROI edge limit (ext/eyt tables)
+constexpr int MAX_JAC = 7;
+
+struct __align__(16) PeakRec {
+  double p[7];          // height, x, x-width, y, y-width, background, z
+  double error;
+  double lambda;
+  double wxt, wyt;      // Z model squared width polynomials (dao_fit.c:1021-1032)
+  int xi, yi, zi;
+  int status, iterations, added;
+  int pad[4];
+};
+static_assert(sizeof(PeakRec) == 128, "PeakRec must be one 128-byte line");
+
+// Constant model description (one per fitter).
+struct ModelCfg {
+  int model;
+  int jac;
+  int nx, ny;
+  int roi, nroi;
+  int sx, sy, sz;        // spline cells (x, y, z)
+  int dil;               // footprint dilation (pixels)
+  int cell;              // scheduling grid cell (pixels)
+  int gx, gy;            // grid cells per frame
+  double xoff, yoff, zoff;
+  double tol;
+  double wmin, wmax;
+  double wx[5], wy[5];   // w0 stored squared (dao_fit.c:1566-1567)
+  double zmin, zmax;
+  double min_height;
+};
+
+// Per-frame control block of the device state machine.
+struct FrameCtl {
+  int phase;
+  int sweeps;            // completed sweeps
+  int max_sweeps;        // 1 + max_iterations (dao_fit_c.py:340-346)
+  int start;             // first run rank of the current attempt
+  int grab;              // next run rank to hand out
+  int escaped_min;       // lowest escaped run rank of this attempt (INT_MAX: none)
+  int n_escaped;
+  int escaped[MAX_ESCAPES];
+  int n_barrier;
+  int barrier[MAX_BARRIERS];
+  int serial;            // 1: every peak waits for its predecessor (index order)
+  int unconverged;
+  int nrun;
+  int attempts;
+  long long ctr[NCOUNTERS];
+};
+
+// Device pointers of a frame set.  T is the pixel arithmetic type.
+template <typename T>
+struct FrameSet {
+  int F;
+  long long npix;
+  const T* x;
+  const T* rqe;
+  const T* scmos;
+  long long* f;
+  long long* bg;
+  int* cnt;
+  const double* bgest;
+  const T* aij;
+  PeakRec* pk;
+  PeakRec* snap;
+  const int* pk_off;
+  int* nfit;
+  int* run;              // run list: local peak index per run rank
+  unsigned* anchor0;     // packed (xi | yi << 16) per run rank at sweep start
+  int* done;             // epoch per run rank
+  int* cell_start;       // [F][gx*gy+1]
+  int* cell_items;       // run ranks grouped by cell
+  int* stepctr;          // [peaks][NCOUNTERS] counters of the latest step of each peak
+  FrameCtl* ctl;
+  unsigned* err_flag;    // bit 0: wait timeout, bit 1: ROI too large
+  const unsigned short* roi_xy;  // packed (rx | ry << 8)
+};
+
+__host__ __device__ inline long long fx_q(double v) {
+#ifdef __CUDA_ARCH__
+  return __double2ll_rn(v * FX_SCALE);
+#else
+  return (long long)llrint(v * FX_SCALE);
+#endif
+}
+
+}  // namespace sa

@@ -1,0 +1,585 @@
+// sa_device.cuh -- device building blocks: memory-model helpers, warp
+// reductions, the FP64 Cholesky solve, the MLE deviance and the PSF models.
+#pragma once
+
+#include <climits>
+#include "sa_common.cuh"
+
+namespace sa {
+
+// ---------------------------------------------------------------------------
+// memory model helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait (all lanes, warp-uniform) until done[idx] == epoch.  Bounded: after
+// ~4 s the wait gives up, raises bit 0 of err_flag and returns false.
+__device__ __forceinline__ bool wait_epoch(const int* done, int epoch, unsigned* err_flag) {
+  if (ld_acquire(done) == epoch) return true;
+  unsigned long long t0 = global_ns();
+  while (ld_acquire(done) != epoch) {
+    __nanosleep(100);
+    if (global_ns() - t0 > 4000000000ull) {
+      atomicOr(err_flag, 1u);
+      return false;
+    }
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// warp reductions
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Reduce 32 values held by every lane; afterwards lane l holds the warp
+// total of value l.  31 shuffles instead of 32*5.
+template <typename T>
+__device__ __forceinline__ T warp_transpose_sum32(T (&v)[32], int lane) {
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool up = (lane & h) != 0;
+#pragma unroll
+    for (int i = 0; i < h; i++) {
+      T send = up ? v[i] : v[i + h];
+      T keep = up ? v[i + h] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+    }
+  }
+  return v[0];
+}
+
+// ---------------------------------------------------------------------------
+// FP64 Cholesky solve of the damped normal equations (replaces LAPACK
+// dposv("Lower"), multi_fit.c:1839-1883).  a: k x k, only a[i*k+j] with
+// j >= i is read.  Returns 0 on success; nonzero when not positive definite
+// or the solution has a NaN (multi_fit.c:1857-1863).
+// ---------------------------------------------------------------------------
+
+__device__ inline int chol_solve(const double* a, double* b, int n) {
+  double L[MAX_JAC * MAX_JAC];
+  double inv[MAX_JAC];
+  for (int j = 0; j < n; j++) {
+    double d = a[j * n + j];
+    for (int k = 0; k < j; k++) d = d - L[j * MAX_JAC + k] * L[j * MAX_JAC + k];
+    if (!(d > 0.0)) return j + 1;
+    d = sqrt(d);
+    L[j * MAX_JAC + j] = d;
+    inv[j] = 1.0 / d;
+    for (int i = j + 1; i < n; i++) {
+      double s = a[j * n + i];
+      for (int k = 0; k < j; k++) s = s - L[i * MAX_JAC + k] * L[j * MAX_JAC + k];
+      L[i * MAX_JAC + j] = s * inv[j];
+    }
+  }
+  for (int i = 0; i < n; i++) {
+    double s = b[i];
+    for (int k = 0; k < i; k++) s = s - L[i * MAX_JAC + k] * b[k];
+    b[i] = s * inv[i];
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    double s = b[i];
+    for (int k = i + 1; k < n; k++) s = s - L[k * MAX_JAC + i] * b[k];
+    b[i] = s * inv[i];
+  }
+  for (int i = 0; i < n; i++)
+    if (isnan(b[i])) return 1;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// MLE per-pixel deviance 2((f - x) - x log(f/x))  (multi_fit.c:174)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double deviance(double fi, double x) {
+  return 2.0 * ((fi - x) - x * log(fi / x));
+}
+
+// FP32 form without the cancellation of the direct formula when f ~ x:
+// with r = (f - x)/x,  dev = 2 x (r - log1p(r)).  For |r| < 1/2 the bracket
+// is evaluated from the atanh series of log1p: with u = r/(2+r),
+//   r - log1p(r) = u r - 2 u^3 (1/3 + u^2/5 + u^4/7 + ...),
+// whose two terms do not cancel; elsewhere the direct form is well
+// conditioned.
+__device__ __forceinline__ float deviance(float fi, float x) {
+  const float r = __fdiv_rn(fi - x, x);
+  float t;
+  if (fabsf(r) < 0.5f) {
+    const float u = __fdiv_rn(r, 2.0f + r);
+    const float u2 = u * u;
+    float s = 1.0f / 19.0f;
+    s = fmaf(u2, s, 1.0f / 17.0f);
+    s = fmaf(u2, s, 1.0f / 15.0f);
+    s = fmaf(u2, s, 1.0f / 13.0f);
+    s = fmaf(u2, s, 1.0f / 11.0f);
+    s = fmaf(u2, s, 1.0f / 9.0f);
+    s = fmaf(u2, s, 1.0f / 7.0f);
+    s = fmaf(u2, s, 1.0f / 5.0f);
+    s = fmaf(u2, s, 1.0f / 3.0f);
+    t = fmaf(u, r, -2.0f * u * u2 * s);
+  } else {
+    t = r - log1pf(r);
+  }
+  return 2.0f * x * t;
+}
+
+// Explicitly rounded products so that a contribution computed in one
+// kernel is bit-identical to the one recomputed in another.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float exp_t(float v) { return expf(v); }
+__device__ __forceinline__ double exp_t(double v) { return exp(v); }
+
+// Fit-image contribution of a peak at one pixel: h * psf * rqe
+// (multi_fit.c:52) and its background term bg * rqe + scmos (:54).
+template <typename T>
+__device__ __forceinline__ T contrib_f(double h, T psf, T rqe) {
+  return mul_rn(mul_rn((T)h, psf), rqe);
+}
+template <typename T>
+__device__ __forceinline__ T contrib_bg(double bg, T rqe, T scmos) {
+  return add_rn(mul_rn((T)bg, rqe), scmos);
+}
+
+// ---------------------------------------------------------------------------
+// per-warp workspace in shared memory
+// ---------------------------------------------------------------------------
+
+template <typename T>
+struct WarpWS {
+  T* Fb;      // base fit image (without this peak) at the cached anchor
+  T* Bs;      // base background sum + this pixel's sCMOS term
+  T* R;       // rqe
+  T* X;       // data
+  T* IC;      // 1 / (base count + 1)
+  T* psf;     // current peak shape
+  T* ext;     // Gaussian x factors / spline deltas (4*64)
+  T* eyt;
+  T* xt;
+  T* yt;
+  double* jh; // 36: jacobian (7) + upper Hessian (up to 28)
+  double* scratch;  // 16
+  PeakRec* w;
+};
+
+template <typename T>
+__host__ __device__ inline size_t warp_ws_bytes(int nroi) {
+  size_t n = (size_t)((nroi + 31) / 32) * 32;
+  size_t b = 6 * n * sizeof(T);
+  b += 4 * 64 * sizeof(T) * 2;   // ext/eyt/xt/yt (Gaussian) or 4 delta tables (spline)
+  b = (b + 15) & ~(size_t)15;
+  b += 36 * sizeof(double) + 16 * sizeof(double);
+  b += sizeof(PeakRec);
+  return (b + 127) & ~(size_t)127;
+}
+
+template <typename T>
+__device__ inline WarpWS<T> warp_ws(char* base, int nroi) {
+  WarpWS<T> ws;
+  size_t n = (size_t)((nroi + 31) / 32) * 32;
+  T* t = reinterpret_cast<T*>(base);
+  ws.Fb = t;
+  ws.Bs = t + n;
+  ws.R = t + 2 * n;
+  ws.X = t + 3 * n;
+  ws.IC = t + 4 * n;
+  ws.psf = t + 5 * n;
+  T* tab = t + 6 * n;
+  ws.ext = tab;
+  ws.eyt = tab + 128;
+  ws.xt = tab + 256;
+  ws.yt = tab + 384;
+  size_t off = 6 * n * sizeof(T) + 4 * 64 * sizeof(T) * 2;
+  off = (off + 15) & ~(size_t)15;
+  ws.jh = reinterpret_cast<double*>(base + off);
+  ws.scratch = ws.jh + 36;
+  ws.w = reinterpret_cast<PeakRec*>(base + off + 52 * sizeof(double));
+  return ws;
+}
+
+// ---------------------------------------------------------------------------
+// model pieces (all lanes participate; results in the warp workspace)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ bool is_spline(int model) { return model >= M_SPLINE2D; }
+
+// Gaussian separable factors, daoCalcPeakShape dao_fit.c:968-998.  The y
+// offset uses xoff as the reference does (:979).
+template <typename T>
+__device__ inline void gauss_tables(const ModelCfg& cfg, const double* p, int xi, int yi,
+                                    WarpWS<T>& ws, int lane) {
+  const double xo = -(p[PX] - (double)xi) - cfg.xoff;
+  const double yo = -(p[PY] - (double)yi) - cfg.xoff;
+  const T wx = (T)p[PXW], wy = (T)p[PYW];
+  for (int i = lane; i < cfg.roi; i += 32) {
+    T tx = (T)((double)i + xo);
+    T ty = (T)((double)i + yo);
+    ws.xt[i] = tx;
+    ws.yt[i] = ty;
+    ws.ext[i] = exp_t(mul_rn(mul_rn(-tx, tx), wx));
+    ws.eyt[i] = exp_t(mul_rn(mul_rn(-ty, ty), wy));
+  }
+}
+
+// Spline cell position of a peak, cfCalcPeakShape cubic_fit.c:455-480.
+struct SplinePos {
+  int xs, ys, zi;
+  double xd, yd, zd;
+};
+
+__device__ inline SplinePos spline_pos(const double* p, int xi, int yi, int zi) {
+  SplinePos s;
+  double xd = 1.5 - (p[PX] - xi);
+  double yd = 1.5 - (p[PY] - yi);
+  s.xs = 0;
+  if (xd >= 1.0) { xd -= 1.0; s.xs = 1; }
+  s.ys = 0;
+  if (yd >= 1.0) { yd -= 1.0; s.ys = 1; }
+  s.zi = zi;
+  s.xd = xd;
+  s.yd = yd;
+  s.zd = p[PZ] - zi;
+  return s;
+}
+
+__device__ __forceinline__ double clamp01(double v) { return v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v); }
+
+template <typename T>
+__device__ __forceinline__ T pw(T v, int e) {
+  T r = (T)1;
+  for (int i = 0; i < e; i++) r = mul_rn(r, v);
+  return r;
+}
+
+// Monomial tables for value / d/dx / d/dy / d/dz (computeDelta3D,
+// cubic_spline.c:105-138; computeDelta2D :66-91).  Deltas are clamped to
+// [0, 1] as rangeCheckD does (:798-826).
+template <typename T>
+__device__ inline void spline_tables(const ModelCfg& cfg, const SplinePos& s, WarpWS<T>& ws,
+                                     int lane) {
+  const T x = (T)clamp01(s.xd), y = (T)clamp01(s.yd);
+  if (cfg.model == M_SPLINE3D) {
+    const T z = (T)clamp01(s.zd);
+    for (int id = lane; id < 64; id += 32) {
+      const int a = id >> 4, b = (id >> 2) & 3, c = id & 3;
+      const T px = pw(x, a), py = pw(y, b), pz = pw(z, c);
+      ws.ext[id] = mul_rn(mul_rn(px, py), pz);
+      // derivative tables are indexed by the coefficient they multiply
+      ws.ext[64 + id] = (a > 0) ? mul_rn(mul_rn(mul_rn((T)a, pw(x, a - 1)), py), pz) : (T)0;
+      ws.eyt[id] = (b > 0) ? mul_rn(mul_rn(px, mul_rn((T)b, pw(y, b - 1))), pz) : (T)0;
+      ws.eyt[64 + id] = (c > 0) ? mul_rn(mul_rn(px, py), mul_rn((T)c, pw(z, c - 1))) : (T)0;
+    }
+  } else {
+    for (int id = lane; id < 16; id += 32) {
+      const int a = id >> 2, b = id & 3;
+      const T px = pw(x, a), py = pw(y, b);
+      ws.ext[id] = mul_rn(px, py);
+      ws.ext[64 + id] = (a > 0) ? mul_rn(mul_rn((T)a, pw(x, a - 1)), py) : (T)0;
+      ws.eyt[id] = (b > 0) ? mul_rn(px, mul_rn((T)b, pw(y, b - 1))) : (T)0;
+    }
+  }
+}
+
+__device__ __forceinline__ int clampi(int v, int hi_excl) {
+  return v < 0 ? 0 : (v >= hi_excl ? hi_excl - 1 : v);
+}
+
+// Spline cell base (fAt3D index clamps, cubic_spline.c:509-522).
+template <typename T>
+__device__ __forceinline__ const T* spline_cell(const ModelCfg& cfg, const T* aij, int zc, int yc,
+                                                int xc) {
+  xc = clampi(xc, cfg.sx);
+  yc = clampi(yc, cfg.sy);
+  if (cfg.model == M_SPLINE3D) {
+    zc = clampi(zc, cfg.sz);
+    return aij + ((size_t)xc * (cfg.sy * cfg.sz) + (size_t)yc * cfg.sz + zc) * 64;
+  }
+  return aij + ((size_t)xc * cfg.sy + yc) * 16;
+}
+
+// Dot of a spline cell with one of the monomial tables, in a fixed order.
+template <typename T>
+__device__ __forceinline__ T spline_dot(const T* c, const T* tab, int n) {
+  T acc = (T)0;
+#pragma unroll 8
+  for (int i = 0; i < n; i++) acc = fma_rn(__ldg(c + i), tab[i], acc);
+  return acc;
+}
+
+// Peak shape at ROI pixel p for the tables currently in the workspace.
+template <typename T>
+__device__ __forceinline__ T psf_at(const ModelCfg& cfg, const T* aij, const WarpWS<T>& ws,
+                                    const SplinePos& s, int rx, int ry) {
+  if (!is_spline(cfg.model)) return mul_rn(ws.eyt[ry], ws.ext[rx]);
+  const int nc = (cfg.model == M_SPLINE3D) ? 64 : 16;
+  const T* c = spline_cell(cfg, aij, s.zi, ry + s.ys, rx + s.xs);
+  return spline_dot(c, ws.ext, nc);
+}
+
+// Widths from z for the Z model, daoCalcWidthsFromZ dao_fit.c:1009-1035.
+__device__ inline void widths_from_z(const ModelCfg& cfg, PeakRec& w) {
+  double z0 = (w.p[PZ] - cfg.wx[1]) / cfg.wx[2];
+  double z1 = z0 * z0, z2 = z1 * z0, z3 = z2 * z0;
+  double t = 1.0 + z1 + cfg.wx[3] * z2 + cfg.wx[4] * z3;
+  w.wxt = t * t;
+  w.p[PXW] = 2.0 / (cfg.wx[0] * t);
+  z0 = (w.p[PZ] - cfg.wy[1]) / cfg.wy[2];
+  z1 = z0 * z0;
+  z2 = z1 * z0;
+  z3 = z2 * z0;
+  t = 1.0 + z1 + cfg.wy[3] * z2 + cfg.wy[4] * z3;
+  w.wyt = t * t;
+  w.p[PYW] = 2.0 / (cfg.wy[0] * t);
+}
+
+// ROI re-anchor, mFitUpdate multi_fit.c:1933-1946.
+__device__ inline void anchor_update(PeakRec& w) {
+  double dx = w.p[PX] - w.xi;
+  if ((dx < -0.5) || (dx > 1.5)) w.xi = (int)floor(w.p[PX]);
+  double dy = w.p[PY] - w.yi;
+  if ((dy < -0.5) || (dy > 1.5)) w.yi = (int)floor(w.p[PY]);
+}
+
+// Apply the solved step in each model's delta order (dao_fit.c:1777-1880,
+// cubic_fit.c:939-1005).
+__device__ inline void apply_update(const ModelCfg& cfg, PeakRec& w, const double* d) {
+  switch (cfg.model) {
+    case M_2DFIXED:
+    case M_SPLINE2D:
+      w.p[PH] -= d[0]; w.p[PX] -= d[1]; w.p[PY] -= d[2]; w.p[PBG] -= d[3];
+      anchor_update(w);
+      break;
+    case M_2D:
+      w.p[PH] -= d[0]; w.p[PX] -= d[1]; w.p[PY] -= d[2]; w.p[PXW] -= d[3]; w.p[PBG] -= d[4];
+      w.p[PYW] = w.p[PXW];
+      anchor_update(w);
+      break;
+    case M_3D:
+      w.p[PH] -= d[0]; w.p[PX] -= d[1]; w.p[PXW] -= d[2]; w.p[PY] -= d[3]; w.p[PYW] -= d[4];
+      w.p[PBG] -= d[5];
+      anchor_update(w);
+      break;
+    case M_Z:
+      w.p[PH] -= d[0]; w.p[PX] -= d[1]; w.p[PY] -= d[2]; w.p[PZ] -= d[3]; w.p[PBG] -= d[4];
+      if (w.p[PZ] < cfg.zmin) w.p[PZ] = cfg.zmin;
+      if (w.p[PZ] > cfg.zmax) w.p[PZ] = cfg.zmax;
+      anchor_update(w);
+      widths_from_z(cfg, w);
+      break;
+    default: {  // M_SPLINE3D, with cfZRangeCheck
+      w.p[PH] -= d[0]; w.p[PX] -= d[1]; w.p[PY] -= d[2]; w.p[PZ] -= d[3]; w.p[PBG] -= d[4];
+      anchor_update(w);
+      if (w.p[PZ] < 1.0e-12) w.p[PZ] = 1.0e-12;
+      const double zmax = ((double)cfg.sz) - 1.0e-12;
+      if (w.p[PZ] > zmax) w.p[PZ] = zmax;
+      w.zi = (int)(w.p[PZ]);
+      break;
+    }
+  }
+}
+
+// mFitCheck multi_fit.c:470-502; returns 0 (ok), 1 (margin), 2 (height).
+__device__ inline int base_check(const ModelCfg& cfg, const PeakRec& w) {
+  if ((w.xi < 0) || (w.xi >= (cfg.nx - cfg.roi)) || (w.yi < 0) || (w.yi >= (cfg.ny - cfg.roi)))
+    return 1;
+  if (w.p[PH] < 0.0) return 2;
+  return 0;
+}
+
+// Model check with the width clamps of daoCheck2D / daoCheck3D
+// (dao_fit.c:1061-1119).
+__device__ inline int model_check(const ModelCfg& cfg, PeakRec& w) {
+  int c = base_check(cfg, w);
+  if (c) return c;
+  if ((cfg.model == M_2D) || (cfg.model == M_3D)) {
+    if (w.p[PXW] < cfg.wmin) w.p[PXW] = cfg.wmin;
+    else if (w.p[PXW] > cfg.wmax) w.p[PXW] = cfg.wmax;
+  }
+  if (cfg.model == M_3D) {
+    if (w.p[PYW] < cfg.wmin) w.p[PYW] = cfg.wmin;
+    else if (w.p[PYW] > cfg.wmax) w.p[PYW] = cfg.wmax;
+  }
+  return 0;
+}
+
+__device__ __forceinline__ int check_for(const ModelCfg& cfg, PeakRec& w) {
+  return is_spline(cfg.model) ? base_check(cfg, w) : model_check(cfg, w);
+}
+
+// Prepare the shape tables of peak w (all lanes) and return its spline
+// position (unused for Gaussians).
+template <typename T>
+__device__ inline SplinePos shape_tables(const ModelCfg& cfg, const PeakRec& w, WarpWS<T>& ws,
+                                         int lane) {
+  SplinePos s;
+  if (is_spline(cfg.model)) {
+    s = spline_pos(w.p, w.xi, w.yi, w.zi);
+    spline_tables(cfg, s, ws, lane);
+  } else {
+    s.xs = s.ys = s.zi = 0;
+    s.xd = s.yd = s.zd = 0.0;
+    gauss_tables(cfg, w.p, w.xi, w.yi, ws, lane);
+  }
+  __syncwarp();
+  return s;
+}
+
+__device__ __forceinline__ void roi_rc(const unsigned short* roi_xy, int p, int& rx, int& ry) {
+  unsigned short v = roi_xy[p];
+  rx = v & 0xff;
+  ry = v >> 8;
+}
+
+// Per-pixel Jacobian row jt (MLE models): daoCalcJH2DFixed dao_fit.c:48-105,
+// daoCalcJH2D :409-467, daoCalcJH3D :811-871, daoCalcJHZ :883-958,
+// cfCalcJH2D cubic_fit.c:48-108, cfCalcJH3D :120-182.
+template <typename T>
+__device__ __forceinline__ void jt_row(const ModelCfg& cfg, const T* aij, const WarpWS<T>& ws,
+                                       const SplinePos& s, const PeakRec& w, T gx, T gy, int rx,
+                                       int ry, T rq, T psf, T* jt) {
+  const T h = (T)w.p[PH];
+  switch (cfg.model) {
+    case M_2DFIXED: {
+      const T e_t = psf, wd = (T)w.p[PXW];
+      jt[0] = rq * e_t;
+      jt[1] = rq * (T)2 * h * wd * ws.xt[rx] * e_t;
+      jt[2] = rq * (T)2 * h * wd * ws.yt[ry] * e_t;
+      jt[3] = rq;
+      break;
+    }
+    case M_2D: {
+      const T e_t = psf, wd = (T)w.p[PXW], xt = ws.xt[rx], yt = ws.yt[ry];
+      jt[0] = rq * e_t;
+      jt[1] = rq * (T)2 * h * wd * xt * e_t;
+      jt[2] = rq * (T)2 * h * wd * yt * e_t;
+      jt[3] = rq * (-h * xt * xt * e_t - h * yt * yt * e_t);
+      jt[4] = rq;
+      break;
+    }
+    case M_3D: {
+      const T e_t = psf, xt = ws.xt[rx], yt = ws.yt[ry];
+      jt[0] = rq * e_t;
+      jt[1] = rq * (T)2 * h * (T)w.p[PXW] * xt * e_t;
+      jt[2] = rq * (-h * xt * xt * e_t);
+      jt[3] = rq * (T)2 * h * (T)w.p[PYW] * yt * e_t;
+      jt[4] = rq * (-h * yt * yt * e_t);
+      jt[5] = rq;
+      break;
+    }
+    case M_Z: {
+      const T e_t = psf, xt = ws.xt[rx], yt = ws.yt[ry];
+      jt[0] = rq * e_t;
+      jt[1] = rq * (T)2 * h * (T)w.p[PXW] * xt * e_t;
+      jt[2] = rq * (T)2 * h * (T)w.p[PYW] * yt * e_t;
+      jt[3] = rq * (-h * xt * xt * gx * e_t - h * yt * yt * gy * e_t);
+      jt[4] = rq;
+      break;
+    }
+    case M_SPLINE3D: {
+      const T* c = spline_cell(cfg, aij, s.zi, ry + s.ys, rx + s.xs);
+      T dx = (T)0, dy = (T)0, dz = (T)0;
+#pragma unroll 8
+      for (int i = 0; i < 64; i++) {
+        const T ci = __ldg(c + i);
+        dx = fma_rn(ci, ws.ext[64 + i], dx);
+        dy = fma_rn(ci, ws.eyt[i], dy);
+        dz = fma_rn(ci, ws.eyt[64 + i], dz);
+      }
+      jt[0] = rq * psf;
+      jt[1] = -rq * h * dx;
+      jt[2] = -rq * h * dy;
+      jt[3] = rq * h * dz;
+      jt[4] = rq;
+      break;
+    }
+    default: {  // M_SPLINE2D
+      const T* c = spline_cell(cfg, aij, 0, ry + s.ys, rx + s.xs);
+      T dx = (T)0, dy = (T)0;
+#pragma unroll 8
+      for (int i = 0; i < 16; i++) {
+        const T ci = __ldg(c + i);
+        dx = fma_rn(ci, ws.ext[64 + i], dx);
+        dy = fma_rn(ci, ws.eyt[i], dy);
+      }
+      jt[0] = rq * psf;
+      jt[1] = -rq * h * dx;
+      jt[2] = -rq * h * dy;
+      jt[3] = rq;
+      break;
+    }
+  }
+}
+
+// d width / dz factors of the Z model (dao_fit.c:904-916).
+__device__ inline void z_factors(const ModelCfg& cfg, const PeakRec& w, double& gx, double& gy) {
+  gx = gy = 0.0;
+  if (cfg.model != M_Z) return;
+  double z0 = (w.p[PZ] - cfg.wx[1]) / cfg.wx[2];
+  double z1 = z0 * z0, z2 = z1 * z0;
+  double zt = 2.0 * z0 + 3.0 * cfg.wx[3] * z1 + 4.0 * cfg.wx[4] * z2;
+  gx = -2.0 * zt / (cfg.wx[0] * w.wxt);
+  z0 = (w.p[PZ] - cfg.wy[1]) / cfg.wy[2];
+  z1 = z0 * z0;
+  z2 = z1 * z0;
+  zt = 2.0 * z0 + 3.0 * cfg.wy[3] * z1 + 4.0 * cfg.wy[4] * z2;
+  gy = -2.0 * zt / (cfg.wy[0] * w.wyt);
+}
+
+__device__ __forceinline__ long long pix_index(const ModelCfg& cfg, int xi, int yi, int rx, int ry) {
+  return (long long)(yi + ry) * cfg.nx + (xi + rx);
+}
+
+// Add (sign +1) or subtract (sign -1) a peak's contribution over its ROI
+// with integer atomics (mFitAddPeak multi_fit.c:28-57, mFitSubtractPeak
+// :1894-1922).  The shape tables of w must be in the workspace.
+template <typename T>
+__device__ inline void add_peak(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
+                                const PeakRec& w, const SplinePos& s, const WarpWS<T>& ws,
+                                int sign, int lane) {
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(fs.roi_xy, p, rx, ry);
+    const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
+    const T rq = __ldg(fs.rqe + k), sc = __ldg(fs.scmos + k);
+    const T psf = psf_at(cfg, fs.aij, ws, s, rx, ry);
+    const long long cf = fx_q((double)contrib_f(w.p[PH], psf, rq));
+    const long long cb = fx_q((double)contrib_bg(w.p[PBG], rq, sc));
+    atomicAdd(reinterpret_cast<unsigned long long*>(fs.f + fbase + k),
+              (unsigned long long)(sign > 0 ? cf : -cf));
+    atomicAdd(reinterpret_cast<unsigned long long*>(fs.bg + fbase + k),
+              (unsigned long long)(sign > 0 ? cb : -cb));
+    atomicAdd(fs.cnt + fbase + k, sign);
+  }
+}
+
+// Pixel model value from the global fixed-point state (f + bg/cnt, multi_fit.c:143).
+__device__ __forceinline__ double fi_global(long long f, long long bg, int cnt) {
+  return (double)f * FX_INV + ((double)bg * FX_INV) / (double)cnt;
+}
+
+}  // namespace sa

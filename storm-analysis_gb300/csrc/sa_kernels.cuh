@@ -1,0 +1,984 @@
+// sa_kernels.cuh -- kernels of the GB300 multi-emitter LM engine.
+//
+// One LM sweep (mFitIterateLM, multi_fit.c:1072-1349) over a frame set is
+//   k_prepare   per frame: list RUNNING peaks in index order ("run ranks"),
+//               snapshot them, bin their dilated footprints into a grid
+//               (or, after an escape, roll back and mark barriers)
+//   k_sweep     persistent warps; one warp runs one peak's LM step.  A peak
+//               waits until every lower-index RUNNING peak whose dilated
+//               footprint overlaps its own has finished, which reproduces
+//               the reference's Gauss-Seidel order for every pixel.  A trial
+//               step that would leave the footprint "escapes": the peak
+//               restores itself, the frame's later peaks are rolled back and
+//               re-run with the escaped peak as a barrier.
+//   k_post      per frame: recenter (mFitRecenterPeaks :1644-1690), sum the
+//               counters, count RUNNING peaks and decide whether the frame
+//               needs another sweep (dao_fit_c.py:332-356).
+#pragma once
+
+#include "sa_device.cuh"
+
+namespace sa {
+
+// ---------------------------------------------------------------------------
+// block scan (blockDim.x == 1024)
+// ---------------------------------------------------------------------------
+
+__device__ inline int block_excl_scan(int v, int* smem32, int& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) smem32[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    int s = smem32[lane];
+    int si = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, si, o);
+      if (lane >= o) si += t;
+    }
+    smem32[lane] = si - s;
+    if (lane == 31) smem32[32] = si;
+  }
+  __syncthreads();
+  int res = smem32[wid] + inc - v;
+  total = smem32[32];
+  __syncthreads();
+  return res;
+}
+
+__device__ __forceinline__ unsigned pack_anchor(int xi, int yi) {
+  return ((unsigned)xi & 0xffffu) | ((unsigned)yi << 16);
+}
+
+__device__ __forceinline__ void load_rec(const PeakRec* src, PeakRec& dst) {
+  const double2* s = reinterpret_cast<const double2*>(src);
+  double2* d = reinterpret_cast<double2*>(&dst);
+#pragma unroll
+  for (int i = 0; i < 8; i++) d[i] = __ldcg(s + i);
+}
+
+// ---------------------------------------------------------------------------
+// the LM step of one peak (one warp)
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ T ic_store(int c) {
+  // FP32 keeps 1/count and multiplies; FP64 keeps the count and divides as
+  // the reference does (multi_fit.c:143).
+  if (sizeof(T) == 4) return c > 0 ? (T)1 / (T)c : (T)0;
+  return (T)c;
+}
+template <typename T>
+__device__ __forceinline__ T bg_div(T b, T ic) {
+  if (sizeof(T) == 4) return b * ic;
+  return b / ic;
+}
+
+// Load the base pixel state (fit image without this peak) at anchor (ax, ay).
+template <typename T>
+__device__ inline void load_base(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase, int ax,
+                                 int ay, WarpWS<T>& ws, int lane) {
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(fs.roi_xy, p, rx, ry);
+    const long long k = pix_index(cfg, ax, ay, rx, ry);
+    const long long Fg = __ldcg(fs.f + fbase + k);
+    const long long Bg = __ldcg(fs.bg + fbase + k);
+    const int Cg = __ldcg(fs.cnt + fbase + k);
+    const T sc = __ldg(fs.scmos + k);
+    ws.Fb[p] = (T)((double)Fg * FX_INV);
+    ws.Bs[p] = (T)((double)Bg * FX_INV + (double)sc);
+    ws.R[p] = __ldg(fs.rqe + k);
+    ws.X[p] = __ldg(fs.x + fbase + k);
+    ws.IC[p] = ic_store<T>(Cg + 1);
+  }
+}
+
+enum { ACT_EVAL = 0, ACT_CONTINUE = 1, ACT_BREAK = 2, ACT_BREAK_ADDED = 3, ACT_ESCAPE = 4 };
+
+// Returns true if the step escaped its footprint (nothing changed).
+template <typename T>
+__device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase, PeakRec* recp,
+                        bool unbounded, WarpWS<T>& ws, int* ctr_out, int lane) {
+  PeakRec orig;
+  load_rec(recp, orig);
+  const int k = cfg.jac;
+  const int nh = k + k * (k + 1) / 2;
+
+  // -- 1. starting error, Jacobian / Hessian, subtract (multi_fit.c:1107-1142)
+  SplinePos s0 = shape_tables(cfg, orig, ws, lane);
+  double gxd, gyd;
+  z_factors(cfg, orig, gxd, gyd);
+  const T gx = (T)gxd, gy = (T)gyd;
+  T acc[32];
+#pragma unroll
+  for (int i = 0; i < 32; i++) acc[i] = (T)0;
+  double dev = 0.0;
+  bool fail = false;
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(fs.roi_xy, p, rx, ry);
+    const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
+    const long long Fg = __ldcg(fs.f + fbase + kk);
+    const long long Bg = __ldcg(fs.bg + fbase + kk);
+    const int Cg = __ldcg(fs.cnt + fbase + kk);
+    const T xv = __ldg(fs.x + fbase + kk);
+    const T rq = __ldg(fs.rqe + kk);
+    const T sc = __ldg(fs.scmos + kk);
+    const T psf = psf_at(cfg, fs.aij, ws, s0, rx, ry);
+    const double fi0 = fi_global(Fg, Bg, Cg);
+    if (!(fi0 > 0.0)) fail = true;
+    else dev += (double)deviance((T)fi0, xv);
+    const T fiT = (T)fi0;
+    const T t1 = (T)2 * ((T)1 - xv / fiT);
+    const T t2 = (T)2 * xv / (fiT * fiT);
+    T jt[MAX_JAC];
+    jt_row(cfg, fs.aij, ws, s0, orig, gx, gy, rx, ry, rq, psf, jt);
+    int idx = 0;
+#pragma unroll
+    for (int l = 0; l < MAX_JAC; l++) {
+      if (l < k) acc[l] += t1 * jt[l];
+    }
+    idx = k;
+#pragma unroll
+    for (int l = 0; l < MAX_JAC; l++) {
+#pragma unroll
+      for (int m = l; m < MAX_JAC; m++) {
+        if (l < k && m < k) {
+          // packed upper triangle, row-major
+          const int id = k + l * k - (l * (l - 1)) / 2 + (m - l);
+          if (id < 32) acc[id] += t2 * jt[l] * jt[m];
+        }
+      }
+    }
+    (void)idx;
+    // subtract this peak (multi_fit.c:1141) and keep the base state
+    const long long cf = fx_q((double)contrib_f(orig.p[PH], psf, rq));
+    const long long cb = fx_q((double)contrib_bg(orig.p[PBG], rq, sc));
+    atomicAdd(reinterpret_cast<unsigned long long*>(fs.f + fbase + kk), (unsigned long long)(-cf));
+    atomicAdd(reinterpret_cast<unsigned long long*>(fs.bg + fbase + kk), (unsigned long long)(-cb));
+    atomicAdd(fs.cnt + fbase + kk, -1);
+    ws.Fb[p] = (T)((double)(Fg - cf) * FX_INV);
+    ws.Bs[p] = (T)((double)(Bg - cb) * FX_INV + (double)sc);
+    ws.R[p] = rq;
+    ws.X[p] = xv;
+    ws.IC[p] = ic_store<T>(Cg);   // (Cg - 1) + 1 once the peak is re-added
+  }
+  dev = warp_sum(dev);
+  fail = __any_sync(0xffffffffu, fail);
+  {
+    T v = warp_transpose_sum32(acc, lane);
+    if (lane < nh) ws.jh[lane] = (double)v;
+  }
+  __syncwarp();
+
+  // -- 2. LM loop (multi_fit.c:1145-1325); lane 0 holds the scalar state.
+  PeakRec w = orig;
+  double se = 0.0;
+  int ctr[NCOUNTERS];
+#pragma unroll
+  for (int i = 0; i < NCOUNTERS; i++) ctr[i] = 0;
+  if (lane == 0) {
+    if (!fail) w.error = dev;
+    else ctr[C_STARTFAIL]++;
+    se = w.error;
+  }
+  int cax = orig.xi, cay = orig.yi;   // anchor of the cached base arrays
+  bool added_end = false, escaped = false;
+  for (;;) {
+    int act = ACT_EVAL;
+    if (lane == 0) {
+      if (w.lambda > LAMBDA_MAX) {
+        ctr[C_LOST]++;
+        w.status = ERROR;
+        act = ACT_BREAK;
+      } else {
+        w.iterations++;
+        ctr[C_ITER]++;
+        w.status = RUNNING;
+        double A[MAX_JAC * MAX_JAC], b[MAX_JAC];
+        const double* jh = ws.jh;
+        int id = k;
+        for (int l = 0; l < k; l++) {
+          b[l] = jh[l];
+          for (int m = l; m < k; m++) {
+            A[l * k + m] = (l == m) ? (1.0 + w.lambda) * jh[id] : jh[id];
+            id++;
+          }
+        }
+        if (chol_solve(A, b, k) != 0) {
+          ctr[C_DPOSV]++;
+          w.status = ERROR;
+          w.lambda = w.lambda * LAMBDA_UP;
+          act = ACT_CONTINUE;
+        } else {
+          PeakRec t = w;
+          apply_update(cfg, t, b);
+          const int c = check_for(cfg, t);
+          if (c) {
+            ctr[c == 1 ? C_MARGIN : C_NEGH]++;
+            const double lam = w.lambda;
+            w = orig;                      // mFitResetPeak multi_fit.c:1788-1798
+            w.lambda = lam * LAMBDA_UP;
+            w.status = ERROR;
+            act = ACT_CONTINUE;
+          } else if (!unbounded && (abs(t.xi - orig.xi) > cfg.dil || abs(t.yi - orig.yi) > cfg.dil)) {
+            act = ACT_ESCAPE;
+          } else {
+            w = t;
+            act = ACT_EVAL;
+          }
+        }
+      }
+      *ws.w = w;
+    }
+    act = __shfl_sync(0xffffffffu, act, 0);
+    __syncwarp();
+    if (act == ACT_CONTINUE) continue;
+    if (act == ACT_BREAK) break;
+    if (act == ACT_ESCAPE) {
+      escaped = true;
+      break;
+    }
+    // -- trial evaluation: shape, add, error (multi_fit.c:1229-1256)
+    PeakRec wl = *ws.w;
+    SplinePos s = shape_tables(cfg, wl, ws, lane);
+    if (wl.xi != cax || wl.yi != cay) {
+      __threadfence();
+      __syncwarp();
+      load_base(cfg, fs, fbase, wl.xi, wl.yi, ws, lane);
+      __syncwarp();
+      cax = wl.xi;
+      cay = wl.yi;
+    }
+    dev = 0.0;
+    fail = false;
+    const double hh = wl.p[PH], bgv = wl.p[PBG];
+    const T bgT = (T)bgv;
+    for (int p = lane; p < cfg.nroi; p += 32) {
+      int rx, ry;
+      roi_rc(fs.roi_xy, p, rx, ry);
+      const T psf = psf_at(cfg, fs.aij, ws, s, rx, ry);
+      ws.psf[p] = psf;
+      const T rq = ws.R[p];
+      const T fi = ws.Fb[p] + contrib_f(hh, psf, rq) + bg_div(ws.Bs[p] + bgT * rq, ws.IC[p]);
+      if (!(fi > (T)0)) fail = true;
+      else dev += (double)deviance(fi, ws.X[p]);
+    }
+    dev = warp_sum(dev);
+    fail = __any_sync(0xffffffffu, fail);
+    if (lane == 0) {
+      if (fail) {
+        ctr[C_NEGFI]++;
+        const double lam = w.lambda;
+        w = orig;
+        w.lambda = lam * LAMBDA_UP;
+        w.status = ERROR;
+        act = ACT_CONTINUE;
+      } else {
+        w.error = dev;
+        if (w.error > se) {
+          if (((w.error - se) / se) < cfg.tol) {
+            w.status = CONVERGED;
+            act = ACT_BREAK_ADDED;
+          } else {
+            ctr[C_NONDECR]++;
+            const double lam = w.lambda;
+            w = orig;
+            w.lambda = lam * LAMBDA_UP;
+            act = ACT_CONTINUE;
+          }
+        } else {
+          if (((se - w.error) / se) < cfg.tol) {
+            w.status = CONVERGED;
+          } else if (w.lambda > LAMBDA_MIN) {
+            w.lambda = LAMBDA_DOWN * w.lambda;
+          }
+          act = ACT_BREAK_ADDED;
+        }
+      }
+    }
+    act = __shfl_sync(0xffffffffu, act, 0);
+    if (act == ACT_BREAK_ADDED) {
+      added_end = true;
+      break;
+    }
+  }
+
+  // -- 3. write back
+  if (escaped) {
+    // Restore the start-of-step contribution; the record is untouched.
+    SplinePos so = shape_tables(cfg, orig, ws, lane);
+    add_peak(cfg, fs, fbase, orig, so, ws, +1, lane);
+    return true;
+  }
+  if (lane == 0) {
+    w.added = orig.added - 1 + (added_end ? 1 : 0);
+    *ws.w = w;
+  }
+  __syncwarp();
+  if (added_end) {
+    const PeakRec wl = *ws.w;
+    for (int p = lane; p < cfg.nroi; p += 32) {
+      int rx, ry;
+      roi_rc(fs.roi_xy, p, rx, ry);
+      const long long kk = pix_index(cfg, wl.xi, wl.yi, rx, ry);
+      const T rq = ws.R[p];
+      const T sc = __ldg(fs.scmos + kk);
+      const long long cf = fx_q((double)contrib_f(wl.p[PH], ws.psf[p], rq));
+      const long long cb = fx_q((double)contrib_bg(wl.p[PBG], rq, sc));
+      atomicAdd(reinterpret_cast<unsigned long long*>(fs.f + fbase + kk), (unsigned long long)cf);
+      atomicAdd(reinterpret_cast<unsigned long long*>(fs.bg + fbase + kk), (unsigned long long)cb);
+      atomicAdd(fs.cnt + fbase + kk, 1);
+    }
+  }
+  if (lane == 0) {
+    *recp = w;
+    for (int i = 0; i < NCOUNTERS; i++) ctr_out[i] = ctr[i];
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// k_sweep: persistent warps over the run ranks of all frames in IN_SWEEP
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
+  extern __shared__ __align__(16) char smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(cfg.nroi), cfg.nroi);
+  const int gwarp = blockIdx.x * wpb + wib;
+  const int fp = 2 * cfg.roi + 2 * cfg.dil;   // overlap span of two dilated footprints
+  int f = gwarp % fs.F;
+  int misses = 0;
+  while (misses < fs.F) {
+    FrameCtl* c = fs.ctl + f;
+    int r = -1;
+    if (lane == 0) {
+      if (*((volatile int*)&c->phase) == PH_IN_SWEEP) {
+        r = atomicAdd(&c->grab, 1);
+        if (r >= c->nrun) r = -1;
+      }
+    }
+    r = __shfl_sync(0xffffffffu, r, 0);
+    if (r < 0) {
+      f = (f + 1) % fs.F;
+      misses++;
+      continue;
+    }
+    misses = 0;
+    const int base = fs.pk_off[f];
+    const int start = c->start;
+    const unsigned a0 = fs.anchor0[base + r];
+    const int ax = a0 & 0xffff, ay = a0 >> 16;
+    bool barrier = c->serial != 0;
+    bool ok = true;
+    // -- dependencies
+    if (c->serial) {
+      if (r - 1 >= start) ok = wait_epoch(fs.done + base + r - 1, epoch, fs.err_flag);
+    } else {
+      const int nb = c->n_barrier;
+      for (int bi = 0; bi < nb && ok; bi++) {
+        const int b = c->barrier[bi];
+        if (b == r) barrier = true;
+      }
+      if (barrier) {
+        for (int q = start; q < r && ok; q++) ok = wait_epoch(fs.done + base + q, epoch, fs.err_flag);
+      } else {
+        for (int bi = 0; bi < nb && ok; bi++) {
+          const int b = c->barrier[bi];
+          if (b < r && b >= start) ok = wait_epoch(fs.done + base + b, epoch, fs.err_flag);
+        }
+        // lower-index RUNNING neighbours whose dilated footprints overlap
+        const int cw = cfg.cell;
+        const int cx = ax / cw, cy = ay / cw;
+        const int* cs = fs.cell_start + (size_t)f * (cfg.gx * cfg.gy + 1);
+        for (int yy = max(cy - 1, 0); yy <= min(cy + 1, cfg.gy - 1) && ok; yy++) {
+          for (int xx = max(cx - 1, 0); xx <= min(cx + 1, cfg.gx - 1) && ok; xx++) {
+            const int c0 = cs[yy * cfg.gx + xx], c1 = cs[yy * cfg.gx + xx + 1];
+            for (int j0 = c0; j0 < c1 && ok; j0 += 32) {
+              int q = -1;
+              if (j0 + lane < c1) {
+                const int cand = fs.cell_items[base + j0 + lane];
+                if (cand < r && cand >= start) {
+                  const unsigned b0 = fs.anchor0[base + cand];
+                  const int bx = b0 & 0xffff, by = b0 >> 16;
+                  if (abs(bx - ax) < fp - cfg.roi && abs(by - ay) < fp - cfg.roi) q = cand;
+                }
+              }
+              unsigned m = __ballot_sync(0xffffffffu, q >= 0);
+              while (m && ok) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                const int qq = __shfl_sync(0xffffffffu, q, src);
+                ok = wait_epoch(fs.done + base + qq, epoch, fs.err_flag);
+              }
+            }
+          }
+        }
+      }
+    }
+    if (!ok) return;   // a wait timed out: err_flag is set, the host reports it
+    __threadfence();
+    // -- the step
+    const int li = fs.run[base + r];
+    const bool esc = lm_step(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, ws,
+                             fs.stepctr + (size_t)(base + li) * NCOUNTERS, lane);
+    if (esc && lane == 0) {
+      atomicMin(&c->escaped_min, r);
+      int slot = atomicAdd(&c->n_escaped, 1);
+      if (slot < MAX_ESCAPES) c->escaped[slot] = r;
+    }
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) st_release(fs.done + base + r, epoch);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_prepare: one CTA (1024 threads) per frame
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ int sc32[33];
+  __shared__ int s_total;
+  const int f = blockIdx.x;
+  FrameCtl* c = fs.ctl + f;
+  const int phase = c->phase;
+  const int base = fs.pk_off[f];
+  const int tid = threadIdx.x;
+  if (phase == PH_SWEEP_PENDING) {
+    const int n = fs.nfit[f];
+    int nrun = 0;
+    for (int c0 = 0; c0 < n; c0 += 1024) {
+      const int i = c0 + tid;
+      int flag = 0;
+      if (i < n && fs.pk[base + i].status == RUNNING) {
+        // A RUNNING peak always has an in-image ROI, except one re-marked
+        // RUNNING by the caller after a failed placement; it cannot be
+        // fitted (its ROI is outside the image) and is set to ERROR.
+        const PeakRec& q = fs.pk[base + i];
+        if (q.xi < 0 || q.yi < 0 || q.xi >= cfg.nx - cfg.roi || q.yi >= cfg.ny - cfg.roi)
+          fs.pk[base + i].status = ERROR;
+        else
+          flag = 1;
+      }
+      int tot;
+      const int pos = block_excl_scan(flag, sc32, tot);
+      if (flag) {
+        const PeakRec& rec = fs.pk[base + i];
+        fs.run[base + nrun + pos] = i;
+        fs.snap[base + i] = rec;
+        fs.anchor0[base + nrun + pos] = pack_anchor(rec.xi, rec.yi);
+      }
+      nrun += tot;
+    }
+    // grid of dilated-footprint anchors (counting sort by cell)
+    const int ncell = cfg.gx * cfg.gy;
+    int* cntc = reinterpret_cast<int*>(smem);
+    for (int i = tid; i < ncell; i += 1024) cntc[i] = 0;
+    __syncthreads();
+    for (int r = tid; r < nrun; r += 1024) {
+      const unsigned a = fs.anchor0[base + r];
+      const int cell = ((a >> 16) / cfg.cell) * cfg.gx + (a & 0xffff) / cfg.cell;
+      atomicAdd(&cntc[cell], 1);
+    }
+    __syncthreads();
+    int* cs = fs.cell_start + (size_t)f * (ncell + 1);
+    // exclusive scan of ncell counts: per-thread contiguous chunk
+    const int per = (ncell + 1023) / 1024;
+    const int lo = tid * per, hi = min(lo + per, ncell);
+    int local = 0;
+    for (int i = lo; i < hi; i++) local += cntc[i];
+    int tot;
+    int off = block_excl_scan(local, sc32, tot);
+    for (int i = lo; i < hi; i++) {
+      const int v = cntc[i];
+      cs[i] = off;
+      cntc[i] = off;   // becomes the fill cursor
+      off += v;
+    }
+    if (tid == 0) cs[ncell] = tot;
+    __syncthreads();
+    for (int r = tid; r < nrun; r += 1024) {
+      const unsigned a = fs.anchor0[base + r];
+      const int cell = ((a >> 16) / cfg.cell) * cfg.gx + (a & 0xffff) / cfg.cell;
+      const int slot = atomicAdd(&cntc[cell], 1);
+      fs.cell_items[base + slot] = r;
+    }
+    if (tid == 0) {
+      c->nrun = nrun;
+      c->start = 0;
+      c->grab = 0;
+      c->escaped_min = INT_MAX;
+      c->n_escaped = 0;
+      c->n_barrier = 0;
+      c->serial = 0;
+      c->attempts = 1;
+      c->phase = nrun > 0 ? PH_IN_SWEEP : PH_IN_SWEEP;
+    }
+  } else if (phase == PH_RERUN_PENDING) {
+    const int b = c->escaped_min;
+    const int nrun = c->nrun;
+    // barriers: merge the escaped run ranks
+    if (tid == 0) {
+      const int ne = min(c->n_escaped, MAX_ESCAPES);
+      for (int e = 0; e < ne; e++) {
+        const int r = c->escaped[e];
+        bool have = false;
+        for (int q = 0; q < c->n_barrier; q++) have |= (c->barrier[q] == r);
+        if (!have) {
+          if (c->n_barrier < MAX_BARRIERS) c->barrier[c->n_barrier++] = r;
+          else c->serial = 1;
+        }
+      }
+      if (c->n_escaped > MAX_ESCAPES) c->serial = 1;
+      s_total = 0;
+    }
+    __syncthreads();
+    // roll back run ranks > b: remove the current contribution, restore the snapshot
+    const int lane = tid & 31, wid = tid >> 5;
+    WarpWS<T> ws = warp_ws<T>(smem + (size_t)wid * warp_ws_bytes<T>(0), 0);
+    const long long fbase = (long long)f * fs.npix;
+    for (int r = b + 1 + wid; r < nrun; r += 32) {
+      const int li = fs.run[base + r];
+      PeakRec cur, sn;
+      load_rec(fs.pk + base + li, cur);
+      load_rec(fs.snap + base + li, sn);
+      if (cur.added > 0) {
+        SplinePos s = shape_tables(cfg, cur, ws, lane);
+        add_peak(cfg, fs, fbase, cur, s, ws, -1, lane);
+      }
+      __syncwarp();
+      if (sn.added > 0) {
+        SplinePos s = shape_tables(cfg, sn, ws, lane);
+        add_peak(cfg, fs, fbase, sn, s, ws, +1, lane);
+      }
+      __syncwarp();
+      if (lane == 0) fs.pk[base + li] = sn;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+      c->start = b;
+      c->grab = b;
+      c->escaped_min = INT_MAX;
+      c->n_escaped = 0;
+      c->attempts += 1;
+      c->phase = PH_IN_SWEEP;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_post: one CTA (1024 threads) per frame
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ long long s_ctr[NCOUNTERS];
+  __shared__ int s_unconv;
+  const int f = blockIdx.x;
+  FrameCtl* c = fs.ctl + f;
+  if (c->phase != PH_IN_SWEEP) return;
+  const int tid = threadIdx.x;
+  if (c->escaped_min != INT_MAX) {
+    __syncthreads();
+    if (tid == 0) c->phase = PH_RERUN_PENDING;
+    return;
+  }
+  if (tid < NCOUNTERS) s_ctr[tid] = 0;
+  if (tid == 0) s_unconv = 0;
+  __syncthreads();
+  const int base = fs.pk_off[f];
+  const int nrun = c->nrun;
+  const int lane = tid & 31, wid = tid >> 5;
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wid * warp_ws_bytes<T>(0), 0);
+  const long long fbase = (long long)f * fs.npix;
+  // recenter (mFitRecenterPeaks multi_fit.c:1644-1690); order-free with
+  // fixed-point accumulation
+  int lost = 0, margin = 0, negh = 0, unconv = 0;
+  for (int r = wid; r < nrun; r += 32) {
+    const int li = fs.run[base + r];
+    PeakRec rec;
+    load_rec(fs.pk + base + li, rec);
+    if (rec.status != RUNNING) continue;
+    const double dx = rec.p[PX] - rec.xi, dy = rec.p[PY] - rec.yi;
+    if ((dx < -0.25) || (dx > 1.25) || (dy < -0.25) || (dy > 1.25)) {
+      SplinePos s = shape_tables(cfg, rec, ws, lane);
+      add_peak(cfg, fs, fbase, rec, s, ws, -1, lane);
+      __syncwarp();
+      rec.added -= 1;
+      rec.xi = (int)floor(rec.p[PX]);
+      rec.yi = (int)floor(rec.p[PY]);
+      const int chk = base_check(cfg, rec);
+      if (chk) {
+        if (lane == 0) {
+          lost++;
+          if (chk == 1) margin++;
+          else negh++;
+        }
+        rec.status = ERROR;
+      } else {
+        SplinePos s2 = shape_tables(cfg, rec, ws, lane);
+        add_peak(cfg, fs, fbase, rec, s2, ws, +1, lane);
+        rec.added += 1;
+      }
+      __syncwarp();
+      if (lane == 0) fs.pk[base + li] = rec;
+    }
+    if (lane == 0 && rec.status == RUNNING) unconv++;
+  }
+  // counters of this sweep's steps
+  long long loc[NCOUNTERS];
+  for (int i = 0; i < NCOUNTERS; i++) loc[i] = 0;
+  for (int r = tid; r < nrun; r += 1024) {
+    const int li = fs.run[base + r];
+    const int* sc = fs.stepctr + (size_t)(base + li) * NCOUNTERS;
+    for (int i = 0; i < NCOUNTERS; i++) loc[i] += sc[i];
+  }
+  loc[C_LOST] += lost;
+  loc[C_MARGIN] += margin;
+  loc[C_NEGH] += negh;
+  for (int i = 0; i < NCOUNTERS; i++) {
+    long long v = loc[i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0 && v) atomicAdd(reinterpret_cast<unsigned long long*>(&s_ctr[i]), (unsigned long long)v);
+  }
+  if (lane == 0 && unconv) atomicAdd(&s_unconv, unconv);
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    for (int i = 0; i < NCOUNTERS; i++) c->ctr[i] += s_ctr[i];
+    c->unconverged = s_unconv;
+    c->sweeps += 1;
+    c->phase = (s_unconv == 0 || c->sweeps >= c->max_sweeps) ? PH_DONE : PH_SWEEP_PENDING;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// frame ingest
+// ---------------------------------------------------------------------------
+
+// mFitNewImage multi_fit.c:1382-1408: x = image * rqe + scmos; reset the fit.
+template <typename T, typename I>
+__global__ void k_new_image(FrameSet<T> fs, const I* img, int frame0, int nframes) {
+  const long long n = fs.npix * nframes;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long k = i % fs.npix;
+    const long long g = (long long)frame0 * fs.npix + i;
+    const double v = (double)img[i] * (double)fs.rqe[k] + (double)fs.scmos[k];
+    const_cast<T*>(fs.x)[g] = (T)v;
+    fs.f[g] = 0;
+    fs.bg[g] = 0;
+    fs.cnt[g] = 0;
+  }
+}
+
+// mFitNewBackground multi_fit.c:1360-1370: bg_estimate = background * rqe.
+template <typename T, typename I>
+__global__ void k_new_background(FrameSet<T> fs, const I* bgin, int frame0, int nframes) {
+  const long long n = fs.npix * nframes;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long k = i % fs.npix;
+    const long long g = (long long)frame0 * fs.npix + i;
+    const_cast<double*>(fs.bgest)[g] = (double)bgin[i] * (double)fs.rqe[k];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// new peaks (daoNewPeaks dao_fit.c:1582-1766, cfNewPeaks cubic_fit.c:758-928)
+// ---------------------------------------------------------------------------
+
+// Parameters of a new peak from its input row; returns the record.
+__device__ inline PeakRec new_peak_rec(const ModelCfg& cfg, const double* q, int ptype) {
+  PeakRec w;
+  for (int i = 0; i < 7; i++) w.p[i] = 0.0;
+  w.error = 0.0;
+  w.lambda = LAMBDA_START;
+  w.wxt = w.wyt = 0.0;
+  w.added = 0;
+  w.iterations = 0;
+  w.status = RUNNING;
+  w.zi = 0;
+  for (int i = 0; i < 4; i++) w.pad[i] = 0;
+  const bool spl = is_spline(cfg.model);
+  w.p[PX] = q[0] - cfg.xoff;
+  w.p[PY] = q[1] - cfg.yoff;
+  w.p[PZ] = q[2] - cfg.zoff;
+  if (ptype == PT_TEXT) {
+    w.p[PBG] = q[3];
+    w.p[PH] = q[4];
+    if (!spl) {
+      w.p[PXW] = 1.0 / (2.0 * q[5] * q[5]);
+      w.p[PYW] = 1.0 / (2.0 * q[6] * q[6]);
+      if (cfg.model == M_Z) widths_from_z(cfg, w);
+    }
+  } else if (!spl) {
+    if (cfg.model == M_Z) {
+      widths_from_z(cfg, w);
+    } else {
+      const double wd = 1.0 / (2.0 * q[3] * q[3]);
+      w.p[PXW] = wd;
+      w.p[PYW] = wd;
+    }
+  }
+  w.xi = (int)floor(w.p[PX]);
+  w.yi = (int)floor(w.p[PY]);
+  if (spl) w.zi = (int)w.p[PZ];
+  if (ptype != PT_TEXT) {
+    w.p[PBG] = 1.0;
+    w.p[PH] = 1.0;
+  }
+  return w;
+}
+
+// Initialise (and for "testing"/"text" add) the new peaks; warp per peak.
+// slots[i] = global peak slot; frames[i] = frame of peak i.
+template <typename T>
+__global__ void k_newpeaks(ModelCfg cfg, FrameSet<T> fs, const double* rows, int ncol, int ptype,
+                           const int* slots, const int* frames, int n, int do_add) {
+  extern __shared__ __align__(16) char smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(0), 0);
+  const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int i = gw; i < n; i += nw) {
+    PeakRec w = new_peak_rec(cfg, rows + (size_t)i * ncol, ptype);
+    const int f = frames[i];
+    const long long fbase = (long long)f * fs.npix;
+    const int chk = check_for(cfg, w);
+    if (chk) {
+      w.status = ERROR;
+      if (lane == 0) {
+        fs.pk[slots[i]] = w;
+        atomicAdd(reinterpret_cast<unsigned long long*>(&fs.ctl[f].ctr[chk == 1 ? C_MARGIN : C_NEGH]), 1ull);
+      }
+      continue;
+    }
+    SplinePos s = shape_tables(cfg, w, ws, lane);
+    if (ptype != PT_TEXT) {
+      // mFitEstimatePeakBackground multi_fit.c:638-662
+      double t = 0.0;
+      for (int p = lane; p < cfg.nroi; p += 32) {
+        int rx, ry;
+        roi_rc(fs.roi_xy, p, rx, ry);
+        const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
+        t += fs.bgest[fbase + k] / (double)__ldg(fs.rqe + k);
+      }
+      t = warp_sum(t);
+      w.p[PBG] = t / ((double)cfg.nroi);
+    }
+    if (do_add) {
+      add_peak(cfg, fs, fbase, w, s, ws, +1, lane);
+      w.added = 1;
+    }
+    if (lane == 0) fs.pk[slots[i]] = w;
+    __syncwarp();
+  }
+}
+
+// "finder" peaks, one warp per frame in input order: the height estimate
+// (mFitEstimatePeakHeight multi_fit.c:678-700) reads the fit image that
+// already holds the earlier new peaks.
+template <typename T>
+__global__ void k_newpeaks_finder(ModelCfg cfg, FrameSet<T> fs, const int* slots, const int* frame_first,
+                                  const int* frame_n, int nframes) {
+  extern __shared__ __align__(16) char smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(0), 0);
+  const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (gw >= nframes) return;
+  const int i0 = frame_first[gw], n = frame_n[gw];
+  for (int j = 0; j < n; j++) {
+    const int slot = slots[i0 + j];
+    PeakRec w;
+    load_rec(fs.pk + slot, w);
+    if (w.status != RUNNING) continue;
+    const int f = gw;
+    const long long fbase = (long long)f * fs.npix;
+    SplinePos s = shape_tables(cfg, w, ws, lane);
+    double sp = 0.0, sx = 0.0;
+    for (int p = lane; p < cfg.nroi; p += 32) {
+      int rx, ry;
+      roi_rc(fs.roi_xy, p, rx, ry);
+      const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
+      const double t = (double)psf_at(cfg, fs.aij, ws, s, rx, ry) * (double)__ldg(fs.rqe + k);
+      sp += t * t * t;
+      const double fv = (double)__ldcg(fs.f + fbase + k) * FX_INV;
+      sx += t * t * ((double)__ldg(fs.x + fbase + k) - fv - fs.bgest[fbase + k]);
+    }
+    sp = warp_sum(sp);
+    sx = warp_sum(sx);
+    w.p[PH] = sx / sp;
+    if (w.p[PH] < cfg.min_height) w.p[PH] = cfg.min_height;
+    if (w.p[PH] <= 0.0) {
+      w.status = ERROR;
+    } else {
+      add_peak(cfg, fs, fbase, w, s, ws, +1, lane);
+      w.added = 1;
+    }
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) fs.pk[slot] = w;
+    __syncwarp();
+  }
+}
+
+// Initial error of the new peaks (dao_fit.c:1757-1763), warp per peak.
+template <typename T>
+__global__ void k_peak_error(ModelCfg cfg, FrameSet<T> fs, const int* slots, const int* frames, int n) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = gw; i < n; i += nw) {
+    const int slot = slots[i];
+    PeakRec w;
+    load_rec(fs.pk + slot, w);
+    if (w.status != RUNNING) continue;
+    const long long fbase = (long long)frames[i] * fs.npix;
+    double dev = 0.0;
+    bool fail = false;
+    for (int p = lane; p < cfg.nroi; p += 32) {
+      int rx, ry;
+      roi_rc(fs.roi_xy, p, rx, ry);
+      const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
+      const double fi = fi_global(__ldcg(fs.f + fbase + k), __ldcg(fs.bg + fbase + k),
+                                  __ldcg(fs.cnt + fbase + k));
+      const T xv = __ldg(fs.x + fbase + k);
+      if (!(fi > 0.0)) fail = true;
+      else dev += (double)deviance((T)fi, xv);
+    }
+    dev = warp_sum(dev);
+    fail = __any_sync(0xffffffffu, fail);
+    if (lane == 0) {
+      if (fail) atomicAdd(reinterpret_cast<unsigned long long*>(&fs.ctl[frames[i]].ctr[C_NEGFI]), 1ull);
+      else fs.pk[slot].error = dev;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// properties and status edits
+// ---------------------------------------------------------------------------
+
+// Per-peak sums (mFitPeakSum :1620-1632, mFitPeakFgSum :1578-1610,
+// mFitPeakBgSum :1518-1565) and, optionally, the Jacobian with the current
+// model values (mFitGetPeakPropertyDouble "jacobian", :791-805).
+template <typename T>
+__global__ void k_peak_props(ModelCfg cfg, FrameSet<T> fs, const int* slots, const int* frames, int n,
+                             double* out_sum, double* out_fg, double* out_bg, double* out_jac) {
+  extern __shared__ __align__(16) char smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(0), 0);
+  const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int i = gw; i < n; i += nw) {
+    PeakRec w;
+    load_rec(fs.pk + slots[i], w);
+    const long long fbase = (long long)frames[i] * fs.npix;
+    const bool inside = (w.xi >= 0) && (w.yi >= 0) && (w.xi + cfg.roi <= cfg.nx) && (w.yi + cfg.roi <= cfg.ny);
+    if (!inside) {
+      if (lane == 0) {
+        if (out_sum) { out_sum[i] = 0.0; out_fg[i] = 1.0; out_bg[i] = 1.0; }
+        if (out_jac) for (int l = 0; l < cfg.jac; l++) out_jac[(size_t)i * cfg.jac + l] = 0.0;
+      }
+      continue;
+    }
+    SplinePos s = shape_tables(cfg, w, ws, lane);
+    double ps = 0.0, ps2 = 0.0, bs = 0.0;
+    double gxd, gyd;
+    z_factors(cfg, w, gxd, gyd);
+    T acc[32];
+    for (int q = 0; q < 32; q++) acc[q] = (T)0;
+    for (int p = lane; p < cfg.nroi; p += 32) {
+      int rx, ry;
+      roi_rc(fs.roi_xy, p, rx, ry);
+      const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
+      const T psfT = psf_at(cfg, fs.aij, ws, s, rx, ry);
+      const double psf = (double)psfT;
+      ps += psf;
+      ps2 += psf * psf;
+      const double xv = (double)__ldg(fs.x + fbase + k);
+      const double bgv = (xv - (double)__ldg(fs.scmos + k)) / (double)__ldg(fs.rqe + k) - w.p[PH] * psf;
+      bs += bgv * psf * psf;
+      if (out_jac) {
+        const double fi = fi_global(__ldcg(fs.f + fbase + k), __ldcg(fs.bg + fbase + k),
+                                    __ldcg(fs.cnt + fbase + k));
+        const T fiT = (T)fi;
+        const T t1 = (T)2 * ((T)1 - (T)xv / fiT);
+        T jt[MAX_JAC];
+        jt_row(cfg, fs.aij, ws, s, w, (T)gxd, (T)gyd, rx, ry, __ldg(fs.rqe + k), psfT, jt);
+        for (int l = 0; l < MAX_JAC; l++)
+          if (l < cfg.jac) acc[l] += t1 * jt[l];
+      }
+    }
+    ps = warp_sum(ps);
+    ps2 = warp_sum(ps2);
+    bs = warp_sum(bs);
+    if (out_jac) {
+      for (int l = 0; l < cfg.jac; l++) {
+        T v = warp_sum(acc[l]);
+        if (lane == 0) out_jac[(size_t)i * cfg.jac + l] = (double)v;
+      }
+    }
+    if (lane == 0 && out_sum) {
+      out_sum[i] = ps * w.p[PH];
+      out_fg[i] = (ps > 0.0) ? (w.p[PH] * ps2) / ps : 1.0;
+      out_bg[i] = ((bs > 0.0) && (ps > 0.0)) ? bs / (ps * ps) : 1.0;
+    }
+  }
+}
+
+// mFitSetPeakStatus multi_fit.c:1809-1831: ERROR peaks still in the image
+// are subtracted first.
+template <typename T>
+__global__ void k_set_status(ModelCfg cfg, FrameSet<T> fs, const int* slots, const int* frames,
+                             const int* status, int n) {
+  extern __shared__ __align__(16) char smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(0), 0);
+  const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int i = gw; i < n; i += nw) {
+    PeakRec w;
+    load_rec(fs.pk + slots[i], w);
+    const bool inside = (w.xi >= 0) && (w.yi >= 0) && (w.xi < cfg.nx - cfg.roi) && (w.yi < cfg.ny - cfg.roi);
+    if (status[i] == ERROR && w.added > 0 && inside) {
+      SplinePos s = shape_tables(cfg, w, ws, lane);
+      add_peak(cfg, fs, (long long)frames[i] * fs.npix, w, s, ws, -1, lane);
+      w.added -= 1;
+    }
+    w.status = status[i];
+    __syncwarp();
+    if (lane == 0) fs.pk[slots[i]] = w;
+  }
+}
+
+// Fit image f / rqe (mFitGetFitImage :708-720) or residual x - f
+// (mFitGetResidual :880-888).
+template <typename T>
+__global__ void k_fit_image(FrameSet<T> fs, int frame, double* out, int residual) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < fs.npix;
+       k += (long long)gridDim.x * blockDim.x) {
+    const long long g = (long long)frame * fs.npix + k;
+    const double fv = (double)fs.f[g] * FX_INV;
+    out[k] = residual ? ((double)fs.x[g] - fv) : fv / (double)fs.rqe[k];
+  }
+}
+
+}  // namespace sa

@@ -1,0 +1,3 @@
+// FP32 pixel arithmetic instantiation of the engine kernels.
+#include "sa_launch_impl.cuh"
+template struct sa::Launch<float>;

@@ -1,0 +1,148 @@
+// sa_launch_impl.cuh -- definitions of the launchers; included once per
+// pixel type by sa_launch_f32.cu / sa_launch_f64.cu.
+#pragma once
+
+#include "sa_kernels.cuh"
+#include "sa_launch.h"
+
+namespace sa {
+
+constexpr int SWEEP_BLOCK = 128;    // 4 warps, one peak each
+constexpr int CTA_BLOCK = 1024;     // per-frame kernels
+constexpr int AUX_BLOCK = 256;      // warp-per-peak auxiliary kernels
+
+template <typename T>
+cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* sweep_smem,
+                                 size_t* cta_smem, size_t* warp_smem) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int nsm = 0, max_smem = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t ws = warp_ws_bytes<T>(cfg.nroi);
+  const size_t s_sweep = ws * (SWEEP_BLOCK / 32);
+  const size_t ws0 = warp_ws_bytes<T>(0);
+  const size_t grid_bytes = (size_t)(cfg.gx * cfg.gy + 1) * sizeof(int);
+  const size_t s_cta = ws0 * (CTA_BLOCK / 32) > grid_bytes ? ws0 * (CTA_BLOCK / 32) : grid_bytes;
+  const size_t s_aux = ws0 * (AUX_BLOCK / 32);
+  if (s_sweep > (size_t)max_smem || s_cta > (size_t)max_smem) return cudaErrorInvalidConfiguration;
+  e = cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s_sweep);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_prepare<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s_cta);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_post<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s_cta);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<T>, SWEEP_BLOCK, s_sweep);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  *sweep_grid = nsm * per_sm;
+  *sweep_smem = s_sweep;
+  *cta_smem = s_cta;
+  *warp_smem = s_aux;
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t Launch<T>::prepare(const ModelCfg& cfg, const FrameSet<T>& fs, size_t smem, cudaStream_t s) {
+  k_prepare<T><<<fs.F, CTA_BLOCK, smem, s>>>(cfg, fs);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::sweep(const ModelCfg& cfg, const FrameSet<T>& fs, int epoch, int grid,
+                             size_t smem, cudaStream_t s) {
+  k_sweep<T><<<grid, SWEEP_BLOCK, smem, s>>>(cfg, fs, epoch);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::post(const ModelCfg& cfg, const FrameSet<T>& fs, size_t smem, cudaStream_t s) {
+  k_post<T><<<fs.F, CTA_BLOCK, smem, s>>>(cfg, fs);
+  return cudaGetLastError();
+}
+
+static inline int grid_for(long long n, int block) {
+  long long g = (n + block - 1) / block;
+  if (g > 4096) g = 4096;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+template <typename T>
+cudaError_t Launch<T>::new_image(const FrameSet<T>& fs, const void* img, int bits, int frame0,
+                                 int nframes, cudaStream_t s) {
+  const int g = grid_for(fs.npix * nframes, 256);
+  if (bits == 32) k_new_image<T, float><<<g, 256, 0, s>>>(fs, (const float*)img, frame0, nframes);
+  else if (bits == 16) k_new_image<T, unsigned short><<<g, 256, 0, s>>>(fs, (const unsigned short*)img, frame0, nframes);
+  else k_new_image<T, double><<<g, 256, 0, s>>>(fs, (const double*)img, frame0, nframes);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::new_background(const FrameSet<T>& fs, const void* bg, int bits, int frame0,
+                                      int nframes, cudaStream_t s) {
+  const int g = grid_for(fs.npix * nframes, 256);
+  if (bits == 32) k_new_background<T, float><<<g, 256, 0, s>>>(fs, (const float*)bg, frame0, nframes);
+  else k_new_background<T, double><<<g, 256, 0, s>>>(fs, (const double*)bg, frame0, nframes);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::new_peaks(const ModelCfg& cfg, const FrameSet<T>& fs, const double* rows,
+                                 int ncol, int ptype, const int* slots, const int* frames, int n,
+                                 int do_add, size_t warp_smem, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int g = grid_for((long long)n * 32, AUX_BLOCK);
+  k_newpeaks<T><<<g, AUX_BLOCK, warp_smem, s>>>(cfg, fs, rows, ncol, ptype, slots, frames, n, do_add);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::new_peaks_finder(const ModelCfg& cfg, const FrameSet<T>& fs, const int* slots,
+                                        const int* frame_first, const int* frame_n, int nframes,
+                                        size_t warp_smem, cudaStream_t s) {
+  const int g = (nframes * 32 + AUX_BLOCK - 1) / AUX_BLOCK;
+  k_newpeaks_finder<T><<<g, AUX_BLOCK, warp_smem, s>>>(cfg, fs, slots, frame_first, frame_n, nframes);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::peak_error(const ModelCfg& cfg, const FrameSet<T>& fs, const int* slots,
+                                  const int* frames, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int g = grid_for((long long)n * 32, AUX_BLOCK);
+  k_peak_error<T><<<g, AUX_BLOCK, 0, s>>>(cfg, fs, slots, frames, n);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::peak_props(const ModelCfg& cfg, const FrameSet<T>& fs, const int* slots,
+                                  const int* frames, int n, double* sum, double* fg, double* bg,
+                                  double* jac, size_t warp_smem, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int g = grid_for((long long)n * 32, AUX_BLOCK);
+  k_peak_props<T><<<g, AUX_BLOCK, warp_smem, s>>>(cfg, fs, slots, frames, n, sum, fg, bg, jac);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::set_status(const ModelCfg& cfg, const FrameSet<T>& fs, const int* slots,
+                                  const int* frames, const int* status, int n, size_t warp_smem,
+                                  cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int g = grid_for((long long)n * 32, AUX_BLOCK);
+  k_set_status<T><<<g, AUX_BLOCK, warp_smem, s>>>(cfg, fs, slots, frames, status, n);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::fit_image(const FrameSet<T>& fs, int frame, double* out, int residual,
+                                 cudaStream_t s) {
+  const int g = grid_for(fs.npix, 256);
+  k_fit_image<T><<<g, 256, 0, s>>>(fs, frame, out, residual);
+  return cudaGetLastError();
+}
+
+}  // namespace sa

@@ -1,0 +1,188 @@
+"""
+Batched multi-frame fitting: many frames of one size and model in one
+frame set on the GPU, all fitted by the same device-driven sweep loop.
+
+    fitter = BatchFitter("3d", (512, 512), n_frames=64, roi_size=18,
+                         sigma_range=[0.5, 4.0])
+    fitter.load(images, backgrounds, peaks_per_frame, "hdf5")
+    fitter.fit(max_iterations=200)
+    res = fitter.results()          # dict of per-peak arrays + "frame"
+
+Per frame the result is the reference's MultiFitter result for the same
+frame (sa_library/dao_fit_c.py): peaks of different frames never interact,
+and within a frame the engine keeps the reference's peak order.
+"""
+import ctypes
+
+import numpy
+
+from . import loadclib
+from .dao_fit_c import MultiFitterException, formatPeaksArbitraryPSF, formatPeaksGaussianPSF
+
+MODEL_INIT = {"2dfixed", "2d", "3d", "Z", "spline2D", "spline3D"}
+
+RESULT_PROPS = ("x", "y", "z", "height", "background", "xsigma", "ysigma", "error")
+
+
+class BatchFitter(object):
+    def __init__(self, model, shape, n_frames, roi_size=10, sigma_range=None, rqe=None,
+                 scmos_cal=None, wx_params=None, wy_params=None, min_z=None, max_z=None,
+                 spline=None, precision=32, peaks_capacity=None, tol=1.0e-6, dilation=None,
+                 stream=None):
+        if model not in MODEL_INIT:
+            raise MultiFitterException("unknown model '%s'" % model)
+        self.clib = loadclib.load()
+        self.model = model
+        self.shape = tuple(shape)
+        self.n_frames = int(n_frames)
+        ny, nx = self.shape
+        rqe = numpy.ones(self.shape) if rqe is None else rqe
+        scmos_cal = numpy.zeros(self.shape) if scmos_cal is None else scmos_cal
+        self.rqe = numpy.ascontiguousarray(rqe, dtype=numpy.float64)
+        self.scmos_cal = numpy.ascontiguousarray(scmos_cal, dtype=numpy.float64)
+        self.spline = spline
+        lib = self.clib
+        if model.startswith("spline"):
+            sp = spline.getCPointer()
+            self.h = lib.cfInitialize(sp, self.rqe, self.scmos_cal, tol, nx, ny)
+        else:
+            self.h = lib.daoInitialize(self.rqe, self.scmos_cal, tol, nx, ny, roi_size)
+        if not self.h:
+            raise MultiFitterException(loadclib.last_error())
+        if lib.saSetPrecision(self.h, int(precision)) != 0:
+            raise MultiFitterException(loadclib.last_error())
+        if dilation is not None and lib.saSetDilation(self.h, int(dilation)) != 0:
+            raise MultiFitterException(loadclib.last_error())
+        if stream is not None:
+            lib.saSetStream(self.h, ctypes.c_void_p(stream))
+        if model in ("2d", "3d"):
+            wmax = 1.0 / (2.0 * sigma_range[0] * sigma_range[0])
+            wmin = 1.0 / (2.0 * sigma_range[1] * sigma_range[1])
+            (lib.daoInitialize2D if model == "2d" else lib.daoInitialize3D)(self.h, wmin, wmax)
+        elif model == "2dfixed":
+            lib.daoInitialize2DFixed(self.h)
+        elif model == "Z":
+            lib.daoInitializeZ(self.h, numpy.ascontiguousarray(wx_params, dtype=numpy.float64),
+                               numpy.ascontiguousarray(wy_params, dtype=numpy.float64),
+                               float(min_z), float(max_z))
+        elif model == "spline3D":
+            lib.cfInitialize3D(self.h)
+        else:
+            lib.cfInitialize2D(self.h)
+        self.capacity = peaks_capacity
+        self._framed = False
+        self.sweeps = 0
+
+    def _ok(self, r, what):
+        if r < 0:
+            raise MultiFitterException(what + ": " + loadclib.last_error())
+        return r
+
+    def ensure_frames(self, capacity):
+        if not self._framed or capacity > (self.capacity or 0):
+            self.capacity = max(int(capacity), self.capacity or 0)
+            self._ok(self.clib.saSetFrames(self.h, self.n_frames, self.capacity), "saSetFrames")
+            self._framed = True
+
+    def format(self, peaks, peaks_type):
+        if self.model.startswith("spline"):
+            return formatPeaksArbitraryPSF(peaks, peaks_type)
+        return formatPeaksGaussianPSF(peaks, peaks_type)
+
+    def load_images(self, images, on_device=False, dtype_bits=None):
+        """images: (F, ny, nx) host numpy array, or a device pointer (int) when on_device."""
+        if on_device:
+            return self._ok(self.clib.saNewImages(self.h, ctypes.c_void_p(images), self.n_frames,
+                                                  dtype_bits, 1), "saNewImages")
+        a = numpy.ascontiguousarray(images)
+        bits = {numpy.dtype(numpy.float64): 64, numpy.dtype(numpy.float32): 32,
+                numpy.dtype(numpy.uint16): 16}[a.dtype]
+        return self._ok(self.clib.saNewImages(self.h, a.ctypes.data_as(ctypes.c_void_p), self.n_frames,
+                                              bits, 0), "saNewImages")
+
+    def load_backgrounds(self, bgs, on_device=False, dtype_bits=None):
+        if on_device:
+            return self._ok(self.clib.saNewBackgrounds(self.h, ctypes.c_void_p(bgs), self.n_frames,
+                                                       dtype_bits, 1), "saNewBackgrounds")
+        a = numpy.ascontiguousarray(bgs)
+        bits = 64 if a.dtype == numpy.float64 else 32
+        if a.dtype not in (numpy.float64, numpy.float32):
+            a = a.astype(numpy.float64)
+            bits = 64
+        return self._ok(self.clib.saNewBackgrounds(self.h, a.ctypes.data_as(ctypes.c_void_p),
+                                                   self.n_frames, bits, 0), "saNewBackgrounds")
+
+    def load_peaks(self, peaks_per_frame, peaks_type):
+        rows = [self.format(p, peaks_type) for p in peaks_per_frame]
+        counts = numpy.array([r.shape[0] for r in rows], dtype=numpy.int32)
+        self.ensure_frames(int(counts.max()) if counts.size else 1)
+        allrows = numpy.ascontiguousarray(numpy.concatenate(rows, axis=0), dtype=numpy.float64)
+        return self._ok(self.clib.saNewPeaksBatch(self.h, allrows, counts, self.n_frames,
+                                                  ctypes.c_char_p(peaks_type.encode())), "saNewPeaksBatch")
+
+    def load(self, images, backgrounds, peaks_per_frame, peaks_type="hdf5"):
+        counts = max(len(self.format(p, peaks_type)) for p in peaks_per_frame)
+        self.ensure_frames(counts)
+        self.load_images(images)
+        self.load_backgrounds(backgrounds)
+        self.load_peaks(peaks_per_frame, peaks_type)
+
+    def fit(self, max_iterations=2000):
+        self.sweeps = self._ok(self.clib.saDoFitBatch(self.h, int(max_iterations)), "saDoFitBatch")
+        return self.sweeps
+
+    def counts(self):
+        c = numpy.zeros(self.n_frames, dtype=numpy.int32)
+        self.clib.saGetNFitBatch(self.h, c)
+        return c
+
+    def prop(self, name):
+        n = int(self.counts().sum())
+        if name in ("status", "iterations"):
+            v = numpy.zeros(n, dtype=numpy.int32)
+            self._ok(self.clib.saGetPeakPropertyIntBatch(self.h, v, ctypes.c_char_p(name.encode())), name)
+            return v
+        v = numpy.zeros(n, dtype=numpy.float64)
+        self._ok(self.clib.saGetPeakPropertyBatch(self.h, v, ctypes.c_char_p(name.encode())), name)
+        return v
+
+    def results(self, props=RESULT_PROPS):
+        out = {p: self.prop(p) for p in props}
+        out["status"] = self.prop("status")
+        out["iterations"] = self.prop("iterations")
+        out["frame"] = numpy.repeat(numpy.arange(self.n_frames), self.counts())
+        return out
+
+    def counters(self):
+        out = numpy.zeros(9, dtype=numpy.int64)
+        self.clib.saGetCounters(self.h, out)
+        return out
+
+    def sched_stats(self):
+        out = numpy.zeros(2, dtype=numpy.int64)
+        self.clib.saGetSchedStats(self.h, out)
+        return {"reruns": int(out[0]), "barriers": int(out[1])}
+
+    def set_timing(self, on):
+        self.clib.saSetTiming(self.h, 1 if on else 0)
+
+    def timing(self):
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        t = ctypes.c_int64()
+        self.clib.saGetTiming(self.h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(t))
+        return ms.value, n.value, t.value
+
+    def close(self):
+        if self.h:
+            if self.model.startswith("spline"):
+                self.clib.cfCleanup(self.h)
+            else:
+                self.clib.daoCleanup(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

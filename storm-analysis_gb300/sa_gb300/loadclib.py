@@ -1,0 +1,148 @@
+"""
+Load libsa_cuda.so, the GPU fitting engine, and declare its C ABI
+(include/sa_cuda.h).
+
+This is the only way the package reaches the engine.  There is no CPU
+fallback: a missing library or a machine without a CUDA device raises.
+"""
+import ctypes
+import os
+
+import numpy
+from numpy.ctypeslib import ndpointer
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsa_cuda.so")
+
+_lib = None
+
+
+class EngineUnavailable(RuntimeError):
+    pass
+
+
+class saFitData(ctypes.Structure):
+    """The handle's leading fields, laid out as the reference's fitData."""
+    _fields_ = ([(n, ctypes.c_int) for n in
+                 ["n_dposv", "n_iterations", "n_lost", "n_margin", "n_neg_fi", "n_neg_height",
+                  "n_non_converged", "n_non_decr", "fit_size_x", "fit_size_y", "image_size_x",
+                  "image_size_y", "jac_size", "max_nfit", "nfit", "roi_n_index"]] +
+                [(n, ctypes.c_double) for n in ["minimum_height", "xoff", "yoff", "zoff", "tolerance"]] +
+                [("bg_counts", ctypes.POINTER(ctypes.c_int)),
+                 ("roi_x_index", ctypes.POINTER(ctypes.c_int)),
+                 ("roi_y_index", ctypes.POINTER(ctypes.c_int)),
+                 ("stale", ctypes.POINTER(ctypes.c_int))] +
+                [(n, ctypes.POINTER(ctypes.c_double)) for n in
+                 ["as_xi", "bg_data", "bg_estimate", "err_i", "f_data", "rqe", "scmos_term", "t_fi",
+                  "x_data"]] +
+                [("working_peak", ctypes.c_void_p), ("fit", ctypes.c_void_p), ("fit_model", ctypes.c_void_p),
+                 ("fn_reserved", ctypes.c_void_p * 9), ("engine", ctypes.c_void_p)])
+
+
+def last_error():
+    lib = load(require_device=False)
+    buf = ctypes.create_string_buffer(1024)
+    lib.saGetLastError(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def load(require_device=True):
+    """Return the loaded library (declaring argument types once)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise EngineUnavailable("libsa_cuda.so is not built; run "
+                                    "'python -c \"import __graft_entry__ as g; g.build()\"'")
+        lib = ctypes.cdll.LoadLibrary(LIB_PATH)
+        _declare(lib)
+        _lib = lib
+    if require_device and _lib.saDeviceCount() < 1:
+        raise EngineUnavailable("no CUDA device is visible; the GPU engine cannot run")
+    return _lib
+
+
+def _declare(lib):
+    f64 = ndpointer(dtype=numpy.float64, flags="C_CONTIGUOUS")
+    i32 = ndpointer(dtype=numpy.int32, flags="C_CONTIGUOUS")
+    i64 = ndpointer(dtype=numpy.int64, flags="C_CONTIGUOUS")
+    vp = ctypes.c_void_p
+    hp = ctypes.POINTER(saFitData)
+    ci, cd, cs = ctypes.c_int, ctypes.c_double, ctypes.c_char_p
+
+    lib.daoInitialize.argtypes = [f64, f64, cd, ci, ci, ci]
+    lib.daoInitialize.restype = hp
+    lib.cfInitialize.argtypes = [vp, f64, f64, cd, ci, ci]
+    lib.cfInitialize.restype = hp
+    for name in ["daoInitialize2DFixed", "daoInitialize2DFixedALS", "daoInitialize2DFixedLS",
+                 "daoInitialize2DFixedDWLS", "daoInitialize2DFixedFWLS", "cfInitialize2D",
+                 "cfInitialize3D", "cfInitialize3DALS", "cfInitialize3DLS", "cfInitialize3DFWLS",
+                 "daoCleanup", "cfCleanup", "mFitIterateLM", "mFitRemoveErrorPeaks",
+                 "mFitRemoveRunningPeaks", "mFitAnscombeTransformImage"]:
+        getattr(lib, name).argtypes = [hp]
+        getattr(lib, name).restype = None
+    for name in ["daoInitialize2D", "daoInitialize2DALS", "daoInitialize2DLS", "daoInitialize2DDWLS",
+                 "daoInitialize2DFWLS", "daoInitialize3D"]:
+        getattr(lib, name).argtypes = [hp, cd, cd]
+        getattr(lib, name).restype = None
+    lib.daoInitializeZ.argtypes = [hp, f64, f64, cd, cd]
+    lib.daoInitializeZ.restype = None
+    lib.daoNewPeaks.argtypes = [hp, f64, cs, ci]
+    lib.daoNewPeaks.restype = None
+    lib.cfNewPeaks.argtypes = [hp, f64, cs, ci]
+    lib.cfNewPeaks.restype = None
+    lib.initSpline2D.argtypes = [f64, ci, ci]
+    lib.initSpline2D.restype = vp
+    lib.initSpline3D.argtypes = [f64, ci, ci, ci]
+    lib.initSpline3D.restype = vp
+    lib.splineCleanup.argtypes = [vp]
+    for name in ["getXSize", "getYSize", "getZSize"]:
+        getattr(lib, name).argtypes = [vp]
+        getattr(lib, name).restype = ci
+    lib.mFitGetFitImage.argtypes = [hp, f64]
+    lib.mFitGetResidual.argtypes = [hp, f64]
+    lib.mFitGetNError.argtypes = [hp]
+    lib.mFitGetNError.restype = ci
+    lib.mFitGetUnconverged.argtypes = [hp]
+    lib.mFitGetUnconverged.restype = ci
+    lib.mFitGetPeakPropertyDouble.argtypes = [hp, f64, cs]
+    lib.mFitGetPeakPropertyInt.argtypes = [hp, i32, cs]
+    lib.mFitNewImage.argtypes = [hp, f64]
+    lib.mFitNewBackground.argtypes = [hp, f64]
+    lib.mFitSetPeakStatus.argtypes = [hp, i32]
+
+    lib.saGetLastError.argtypes = [ctypes.c_char_p, ci]
+    lib.saGetLastError.restype = ci
+    lib.saClearLastError.argtypes = []
+    lib.saClearLastError.restype = None
+    lib.saDeviceCount.argtypes = []
+    lib.saDeviceCount.restype = ci
+    for name, args in [("saSetPrecision", [hp, ci]), ("saSetDilation", [hp, ci]),
+                       ("saSetStream", [hp, vp]), ("saDoFit", [hp, ci]),
+                       ("saGetCounters", [hp, i64]), ("saGetSchedStats", [hp, i64]),
+                       ("saSetFrames", [hp, ci, ci]), ("saNewImages", [hp, vp, ci, ci, ci]),
+                       ("saNewBackgrounds", [hp, vp, ci, ci, ci]),
+                       ("saNewPeaksBatch", [hp, f64, i32, ci, cs]), ("saDoFitBatch", [hp, ci]),
+                       ("saGetNFitBatch", [hp, i32]), ("saGetPeakPropertyBatch", [hp, f64, cs]),
+                       ("saGetPeakPropertyIntBatch", [hp, i32, cs]), ("saSetTiming", [hp, ci]),
+                       ("saGetTiming", [hp, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)])]:
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ci
+
+
+EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoInitialize3D",
+           "daoInitializeZ", "daoNewPeaks", "daoCleanup", "daoInitialize2DFixedALS",
+           "daoInitialize2DFixedLS", "daoInitialize2DFixedDWLS", "daoInitialize2DFixedFWLS",
+           "daoInitialize2DALS", "daoInitialize2DLS", "daoInitialize2DDWLS", "daoInitialize2DFWLS",
+           "initSpline2D", "initSpline3D", "splineCleanup", "getXSize", "getYSize", "getZSize",
+           "cfInitialize", "cfInitialize2D", "cfInitialize3D", "cfInitialize3DALS",
+           "cfInitialize3DLS", "cfInitialize3DFWLS", "cfNewPeaks", "cfCleanup",
+           "mFitAnscombeTransformImage", "mFitGetFitImage", "mFitGetNError",
+           "mFitGetPeakPropertyDouble", "mFitGetPeakPropertyInt", "mFitGetResidual",
+           "mFitGetUnconverged", "mFitIterateLM", "mFitNewBackground", "mFitNewImage",
+           "mFitRemoveErrorPeaks", "mFitRemoveRunningPeaks", "mFitSetPeakStatus",
+           "saGetLastError", "saClearLastError", "saDeviceCount", "saSetPrecision", "saSetDilation", "saSetStream",
+           "saDoFit", "saGetCounters", "saGetSchedStats", "saSetFrames", "saNewImages",
+           "saNewBackgrounds", "saNewPeaksBatch", "saDoFitBatch", "saGetNFitBatch",
+           "saGetPeakPropertyBatch", "saGetPeakPropertyIntBatch", "saSetTiming", "saGetTiming"]

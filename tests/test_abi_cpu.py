@@ -1,0 +1,108 @@
+"""CPU checks of the engine library: it builds, loads, exports every entry
+point its header declares, and refuses to run without a GPU."""
+import os
+import re
+import subprocess
+
+import numpy
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "sa_cuda.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", src)
+    skip = {"if", "for", "while", "return", "sizeof"}
+    return sorted(set(n for n in names if n not in skip))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sa_gb300 import build, loadclib
+    build.build()
+    return loadclib.load(require_device=False)
+
+
+def test_library_exports_header(lib):
+    from sa_gb300 import loadclib
+    nm = subprocess.run(["nm", "-D", "--defined-only", loadclib.LIB_PATH], capture_output=True,
+                        text=True, check=True).stdout
+    exported = set(line.split()[-1] for line in nm.splitlines() if " T " in line)
+    declared = header_functions()
+    assert len(declared) > 50
+    missing = [n for n in declared if n not in exported]
+    assert missing == []
+    assert sorted(loadclib.EXPORTS) == sorted(declared)
+
+
+def test_no_device_here_fails_loudly(lib):
+    from sa_gb300 import dao_fit_c, loadclib
+    if lib.saDeviceCount() > 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(loadclib.EngineUnavailable):
+        dao_fit_c.MultiFitter2D(sigma_range=[1.0, 2.0])
+
+
+def test_handle_layout_matches_reference_fitdata(lib):
+    """Fields Python reads through the reference's ctypes mirror of fitData
+    (sa_library/dao_fit_c.py:22-77) sit at the same offsets."""
+    import ctypes
+    from sa_gb300 import loadclib
+    s = loadclib.saFitData
+    ints = ["n_dposv", "n_iterations", "n_lost", "n_margin", "n_neg_fi", "n_neg_height",
+            "n_non_converged", "n_non_decr", "fit_size_x", "fit_size_y", "image_size_x",
+            "image_size_y", "jac_size", "max_nfit", "nfit", "roi_n_index"]
+    for i, n in enumerate(ints):
+        assert getattr(s, n).offset == 4 * i
+    assert s.minimum_height.offset == 64
+    assert s.roi_x_index.offset == 64 + 5 * 8 + ctypes.sizeof(ctypes.c_void_p)
+
+
+def test_handle_creation_without_device(lib):
+    """Handle set-up is host-only; ROI geometry follows multi_fit.c:1031-1060."""
+    from sa_gb300 import loadclib
+    from oracle.oracle import OracleFitter
+    img = numpy.ones((40, 40))
+    for r in [7, 8, 9, 12, 15, 20]:
+        h = lib.daoInitialize(img, numpy.zeros((40, 40)), 1e-6, 40, 40, r)
+        lib.daoInitialize2DFixed(h)
+        c = h.contents
+        n = c.roi_n_index
+        rx = numpy.array([c.roi_x_index[i] for i in range(n)])
+        ry = numpy.array([c.roi_y_index[i] for i in range(n)])
+        o = OracleFitter("2dfixed", (40, 40), roi_size=r)
+        ox, oy = o.roiIndex()
+        assert numpy.array_equal(rx, ox) and numpy.array_equal(ry, oy)
+        assert c.jac_size == 4 and c.fit_size_x == r
+        assert abs(c.xoff - (0.5 * r - 1.0)) < 1e-15
+        lib.daoCleanup(h)
+        o.cleanup()
+
+
+def test_bad_inputs_report_errors(lib):
+    from sa_gb300 import loadclib
+    img = numpy.ones((40, 40))
+    assert not lib.daoInitialize(img, img, 1e-6, 40, 40, 1)
+    assert "ROI" in loadclib.last_error()
+    sp = lib.initSpline2D(numpy.zeros(6 * 5 * 16), 6, 5)
+    assert not lib.cfInitialize(sp, img, img, 1e-6, 40, 40)
+    assert "square" in loadclib.last_error()
+    lib.splineCleanup(sp)
+    h = lib.daoInitialize(img, img * 0, 1e-6, 40, 40, 10)
+    lib.daoInitialize2DFixedALS(h)
+    assert "MLE" in loadclib.last_error()
+    lib.daoCleanup(h)
+
+
+def test_synthetic_workloads_shapes():
+    from sa_gb300 import synth
+    wl = synth.make_workload(1, frames=2, nx=128, ny=128)
+    assert len(wl["images"]) == 2 and wl["images"][0].shape == (128, 128)
+    assert (wl["images"][0] >= 1.0).all()
+    g = wl["guesses"][0]
+    assert set(g) >= {"x", "y", "z", "background", "height", "xsigma", "ysigma"}
+    wl3 = synth.make_workload(3, frames=1, nx=64, ny=64, n_emitters=5)
+    assert wl3["spline"]["coeff"].shape == (20, 20, 20, 64)
