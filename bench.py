@@ -1,0 +1,437 @@
+#!/usr/bin/env python
+"""
+bench.py -- localizations/s of the multi-emitter Levenberg-Marquardt fitting
+step (storm-analysis 3D-DAOSTORM '3d' model) on GB300.
+
+Workload (one "step"): benchmark configuration 1 -- 64 frames of 512 x 512,
+Poisson(0.5 / um^2) emitters per frame (~3355, overlapping ROIs), '3d'
+Gaussian model, MLE, roi_size 18, tolerance 1e-6, at most 200 sweeps, seeded
+synthetic data, initial guesses = truth + jitter ("hdf5" peak format).  One
+step fits all 64 frames to termination through the batched engine.
+
+  value   localizations/s with the frames, backgrounds and peak rows already
+          resident in HBM (device pointers into the engine's C ABI)
+  e2e     the same through the public API with pinned host buffers: host ->
+          device copies of images, backgrounds and peak rows and the
+          device -> host read of all results inside the timed region
+  plain   the one-frame-per-launch GPU fitter (MultiFitter with the
+          reference's host-driven sweep loop), for comparison
+  cpu_baseline  the FP64 CPU oracle (our C restatement of the reference's
+          fitter) on the host cores, one process per core, a bounded sample
+
+`python bench.py --impl reference` times the CPU oracle on all host cores on
+the same workload and prints the same JSON line with "impl": "reference".
+
+Multi-GPU: frames are independent and a frame does not shard, so N GPUs run
+N independent replicas (weak scaling); no collective is on the data path.
+"""
+import argparse
+import json
+import math
+import multiprocessing
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "storm-analysis_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+MAX_IT = 200
+
+
+# ----------------------------------------------------------------------------
+# CPU side (oracle); workers are spawned, never forked from a CUDA process
+# ----------------------------------------------------------------------------
+
+def _cpu_worker(args):
+    import oracle.oracle as O
+    frames, fitter_kw, shape, rqe, scmos = args
+    kw = dict(fitter_kw)
+    model = kw.pop("model")
+    kw.pop("spline", None)
+    f = O.OracleFitter(model, shape, rqe=rqe, scmos_cal=scmos, **kw)
+    n = 0
+    t0 = time.perf_counter()
+    for img, bg, g in frames:
+        f.newImage(img)
+        f.newBackground(bg)
+        f.newPeaks(g, "hdf5")
+        f.doFit(MAX_IT)
+        n += f.getNFit()
+        f.getPeakProperty("x")
+    dt = time.perf_counter() - t0
+    f.cleanup()
+    return n, dt
+
+
+def cpu_sample(wl, n_frames, cores, pool):
+    """Fit n_frames of the workload on `cores` processes; returns (peaks, wall s)."""
+    shape = (wl["ny"], wl["nx"])
+    jobs = [[] for _ in range(cores)]
+    for i in range(n_frames):
+        f = i % len(wl["images"])
+        jobs[i % cores].append((wl["images"][f], wl["backgrounds"][f], wl["guesses"][f]))
+    args = [(j, wl["fitter"], shape, wl["rqe"], wl["scmos_cal"]) for j in jobs if j]
+    t0 = time.perf_counter()
+    res = pool.map(_cpu_worker, args)
+    wall = time.perf_counter() - t0
+    return sum(r[0] for r in res), wall
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so"], check=True)
+
+
+# ----------------------------------------------------------------------------
+# clocks
+# ----------------------------------------------------------------------------
+
+class ClockSampler(object):
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# GPU side
+# ----------------------------------------------------------------------------
+
+def flops_per_iteration(model, nroi):
+    """Algorithmic FP32 work of one LM inner iteration of one peak (counted per
+    ROI pixel): Jacobian row + normal-equation accumulation 2(k(k+1)/2 + k) + 3k + 5,
+    the model (1) and the error / add / subtract terms (20)."""
+    k = {"2dfixed": 4, "2d": 5, "3d": 6, "Z": 5, "spline2D": 4, "spline3D": 5}[model]
+    per_px = 2 * (k * (k + 1) // 2 + k) + 3 * k + 5 + 1 + 20
+    if model.startswith("spline"):
+        per_px += 512
+    return per_px * nroi
+
+
+def roi_pixels(roi):
+    c = 0.5 * roi
+    n = 0
+    for i in range(roi):
+        for j in range(roi):
+            if ((j - c + 0.5) ** 2 + (i - c + 0.5) ** 2) <= c * c:
+                n += 1
+    return n
+
+
+def load_profile_traffic():
+    p = os.path.join(ROOT, "profiles", "k_sweep_cfg1_traffic.json")
+    if os.path.exists(p):
+        with open(p) as fp:
+            return json.load(fp)
+    return None
+
+
+def peaks_rows(wl):
+    from sa_gb300.dao_fit_c import formatPeaksGaussianPSF
+    rows = [formatPeaksGaussianPSF(g, "hdf5") for g in wl["guesses"]]
+    counts = numpy.array([r.shape[0] for r in rows], dtype=numpy.int32)
+    return numpy.ascontiguousarray(numpy.concatenate(rows)), counts
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from sa_gb300 import engine, loadclib, synth
+
+    lib = loadclib.load()
+    lib.saSetDevice(local_rank)
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    cfg = args.config
+    wl = synth.make_workload(cfg, frames=args.frames, seed=cfg + 1000 * rank)
+    kw = dict(wl["fitter"])
+    model = kw.pop("model")
+    kw.pop("spline", None)
+    F = len(wl["images"])
+    shape = (wl["ny"], wl["nx"])
+    images = numpy.ascontiguousarray(numpy.stack(wl["images"]).astype(numpy.float32))
+    bgs = numpy.ascontiguousarray(numpy.stack(wl["backgrounds"]).astype(numpy.float32))
+    rows, counts = peaks_rows(wl)
+    units = int(counts.sum())
+
+    fit = engine.BatchFitter(model, shape, F, rqe=wl["rqe"], scmos_cal=wl["scmos_cal"],
+                             precision=args.precision, peaks_capacity=int(counts.max()), **kw)
+    # resident inputs
+    d_img = torch.from_numpy(images).cuda()
+    d_bg = torch.from_numpy(bgs).cuda()
+    d_rows = torch.from_numpy(rows).cuda()
+    torch.cuda.synchronize()
+
+    def step_resident():
+        fit.load_images(d_img.data_ptr(), on_device=True, dtype_bits=32)
+        fit.load_backgrounds(d_bg.data_ptr(), on_device=True, dtype_bits=32)
+        fit.load_peaks_device(d_rows.data_ptr(), counts, "hdf5")
+        fit.fit(MAX_IT)
+
+    p_img = torch.from_numpy(images).pin_memory()
+    p_bg = torch.from_numpy(bgs).pin_memory()
+    p_rows = torch.from_numpy(rows).pin_memory()
+    p_img_np, p_bg_np, p_rows_np = p_img.numpy(), p_bg.numpy(), p_rows.numpy()
+    out_vals = {}
+
+    def step_e2e():
+        fit.load_images(p_img_np)
+        fit.load_backgrounds(p_bg_np)
+        fit.clib.saNewPeaksBatch(fit.h, p_rows_np, counts, F, b"hdf5")
+        fit.fit(MAX_IT)
+        out_vals["v"] = fit.results_fast()
+
+    def timed(fn, k):
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(k):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    for _ in range(args.warmup):
+        step_resident()
+    launches0 = fit.kernel_launches()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ms_value = timed(step_resident, args.steps)
+    clk = clocks.stop()
+    launches = (fit.kernel_launches() - launches0) // max(args.steps, 1)
+
+    # roofline pass: one resident step with the sweep kernels timed by events
+    c0 = fit.counters()
+    fit.set_timing(True)
+    step_resident()
+    sweep_ms, sweep_launches, ticks = fit.timing()
+    fit.set_timing(False)
+    c1 = fit.counters()
+    iters = int(c1[1] - c0[1])
+    nroi = roi_pixels(kw.get("roi_size", 10)) if not model.startswith("spline") else None
+    flops = flops_per_iteration(model, nroi) * iters
+    res_vals, res_ints = fit.results_fast()
+    status = res_ints[:, 0]
+
+    for _ in range(max(1, args.warmup // 2)):
+        step_e2e()
+    ms_e2e = timed(step_e2e, args.steps)
+    h2d = images.nbytes + bgs.nbytes + rows.nbytes + counts.nbytes
+    d2h = int(units * 128)
+
+    # plain one-frame-per-launch fitter (host-driven sweep loop), bounded sample
+    plain = None
+    if not args.no_plain and rank == 0:
+        from sa_gb300 import dao_fit_c
+        cls = {"2d": dao_fit_c.MultiFitter2D, "3d": dao_fit_c.MultiFitter3D,
+               "Z": dao_fit_c.MultiFitterZ, "2dfixed": dao_fit_c.MultiFitter2DFixed}[model]
+        pf = cls(rqe=wl["rqe"], scmos_cal=wl["scmos_cal"], precision=args.precision, device_loop=False, **kw)
+        pf.initializeC(wl["images"][0])
+        nplain = min(args.plain_frames, F)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n = 0
+        for i in range(nplain):
+            pf.newImage(wl["images"][i])
+            pf.newBackground(wl["backgrounds"][i])
+            pf.newPeaks(wl["guesses"][i], "hdf5")
+            pf.doFit(MAX_IT)
+            n += pf.getNFit()
+            pf.getPeakProperty("x")
+        plain = {"value": n / (time.perf_counter() - t0), "frames": nplain}
+        pf.cleanup(verbose=False)
+
+    value = units * world / (ms_value / 1e3)
+    e2e = units * world / (ms_e2e / 1e3)
+    props = torch.cuda.get_device_properties(local_rank)
+    nsm = props.multi_processor_count
+    mx = clk["sm_max_mhz"] or 2070.0
+    if args.precision == 32:
+        peak_tf = nsm * 128 * 2 * mx * 1e6 / 1e12
+        bound = "fp32"
+    else:
+        peak_tf = 1.25
+        bound = "fp64"
+    achieved = flops / (sweep_ms / 1e3) / 1e12 if sweep_ms > 0 else None
+    traffic = load_profile_traffic()
+    line = {
+        "metric": "localizations/s (LM to convergence)",
+        "value": value,
+        "unit": "localizations/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_value,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 model+Jacobian / fp64 solve+decisions" if args.precision == 32 else "fp64",
+        "data": "synthetic (seeded, benchmark configuration %d shapes)" % cfg,
+        "config": {"workload": "cfg%d: %s model, %d frames %dx%d, %d emitters, roi %s, max %d sweeps"
+                               % (cfg, model, F, shape[1], shape[0], units, kw.get("roi_size"), MAX_IT),
+                   "frames_per_step": F, "localizations_per_step": units,
+                   "l2": "working set %.2f GB per step > 129 MB L2" % (F * shape[0] * shape[1] * 32 / 1e9),
+                   "parallelism": "replicas x%d" % world},
+        "e2e": {"value": e2e, "unit": "localizations/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
+        "gpu_launches": int(launches * args.steps),
+        "clocks": clk,
+        "roofline": {"bound": bound, "kernel": "k_sweep", "achieved": achieved, "peak": peak_tf,
+                     "unit": "TFLOP/s", "frac": (achieved / peak_tf) if achieved else None,
+                     "peak_source": "nominal %d SMs x 128 FP32 lanes x 2 x %.0f MHz" % (nsm, mx)
+                     if bound == "fp32" else "nominal FP64",
+                     "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                     "sweep_launches": int(sweep_launches), "sweep_ms_per_step": sweep_ms,
+                     "lm_iterations_per_step": iters, "flops_per_iteration": flops_per_iteration(model, nroi)},
+        "fit": {"converged": int((status == 1).sum()), "error": int((status == 2).sum()),
+                "running": int((status == 0).sum()), "sweeps": fit.sweeps,
+                "scheduler": fit.sched_stats()},
+    }
+    if plain is not None:
+        line["plain_gpu"] = {"value": plain["value"], "unit": "localizations/s",
+                             "frames": plain["frames"], "speedup_batched_vs_plain": value / world / plain["value"]}
+    if rank == 0 and not args.no_cpu:
+        build_oracle()
+        cores = args.cpu_cores or os.cpu_count()
+        ctx = multiprocessing.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            n_cpu, wall = cpu_sample(wl, min(cores, F), cores, pool)
+        line["cpu_baseline"] = {"value": n_cpu / wall, "unit": "localizations/s", "cores": cores,
+                                "kind": "port", "sample": "%d frames of the step's workload, one "
+                                "process per core, %.1f s wall" % (min(cores, F), wall)}
+    if dist is not None:
+        dist.destroy_process_group()
+    fit.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU fitter (the oracle port of it) on all host cores."""
+    if rank != 0:
+        return
+    from sa_gb300 import synth
+    build_oracle()
+    cfg = args.config
+    wl = synth.make_workload(cfg, frames=args.frames, seed=cfg)
+    cores = args.cpu_cores or os.cpu_count()
+    ctx = multiprocessing.get_context("spawn")
+    sample = min(cores, len(wl["images"]))
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup if args.warmup < 2 else 1):
+            cpu_sample(wl, sample, cores, pool)
+        vals = []
+        t_all = 0.0
+        n_all = 0
+        for _ in range(args.steps):
+            n, wall = cpu_sample(wl, sample, cores, pool)
+            vals.append(n / wall)
+            t_all += wall
+            n_all += n
+    value = n_all / t_all
+    kw = wl["fitter"]
+    line = {"impl": "reference", "metric": "localizations/s (LM to convergence)", "value": value,
+            "unit": "localizations/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_all / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded, benchmark configuration %d shapes)" % cfg,
+            "config": {"workload": "cfg%d: %s model, frames %dx%d, roi %s, max %d sweeps; each step a %d-frame "
+                                   "sample" % (cfg, kw["model"], wl["nx"], wl["ny"], kw.get("roi_size"), MAX_IT, sample)},
+            "cpu_baseline": {"value": value, "unit": "localizations/s", "cores": cores, "kind": "port",
+                             "sample": "%d frames per step, one process per core" % sample},
+            "e2e": {"value": value, "unit": "localizations/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2])
+    ap.add_argument("--frames", type=int, default=None)
+    ap.add_argument("--plain-frames", type=int, default=2)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-cores", type=int, default=None)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

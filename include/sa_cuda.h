@@ -205,14 +205,25 @@ int saNewBackgrounds(saFitData *fit, const void *backgrounds, int n_frames, int 
                      int on_device);
 int saNewPeaksBatch(saFitData *fit, const double *peaks, const int32_t *counts, int n_frames,
                     const char *p_type);
+/* As saNewPeaksBatch, with the peak rows already in device memory. */
+int saNewPeaksBatchDevice(saFitData *fit, const double *d_peaks, const int32_t *counts, int n_frames,
+                          const char *p_type);
 int saDoFitBatch(saFitData *fit, int max_iterations);
 int saGetNFitBatch(saFitData *fit, int32_t *counts);
 int saGetPeakPropertyBatch(saFitData *fit, double *values, const char *what);
 int saGetPeakPropertyIntBatch(saFitData *fit, int32_t *values, const char *what);
+/* All frames' results with one device-to-host copy: per peak 8 doubles
+ * (x, y, z, height, background, xsigma, ysigma, error) and 2 ints (status,
+ * iterations), frames in order.  Returns the number of peaks. */
+int saGetResultsBatch(saFitData *fit, double *values, int32_t *ints);
+/* Make device `device` current for this thread (cudaSetDevice). */
+int saSetDevice(int device);
 /* Device time of the sweep kernels since the last reset, for profiling:
  * enable with saSetTiming(fit, 1); returns total ms and launch count. */
 int saSetTiming(saFitData *fit, int on);
 int saGetTiming(saFitData *fit, double *total_ms, int64_t *launches, int64_t *ticks);
+/* Number of kernels this handle has launched. */
+int64_t saGetKernelLaunches(saFitData *fit);
 
 #ifdef __cplusplus
 }

@@ -104,11 +104,15 @@ struct Engine {
   long long ctr_seen[NCOUNTERS] = {0};
   int unconv_cache = -1;
 
-  // timing
+  // timing: a pool of event pairs around the sweep launches, read once at
+  // saGetTiming so that timing adds no synchronisation
   bool timing = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<cudaEvent_t> pool;
+  size_t pool_used = 0;
   double sweep_ms = 0.0;
   long long sweep_launches = 0, ticks = 0;
+  long long launches = 0;   // kernels launched by this handle
 
   ~Engine() { release(); }
 
@@ -124,6 +128,9 @@ struct Engine {
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     ev0 = ev1 = nullptr;
+    for (cudaEvent_t ev : pool) cudaEventDestroy(ev);
+    pool.clear();
+    pool_used = 0;
     F = 0;
   }
 
@@ -204,13 +211,14 @@ struct Engine {
     if (n == F && d_x) return 0;
     dfree(d_x); dfree(d_f); dfree(d_bg); dfree(d_cnt); dfree(d_bgest); dfree(d_ctl); dfree(d_cellstart);
     const size_t np = (size_t)npix * n;
+    const size_t words = (prec == 64) ? 2 : 1;   // accumulator words per pixel
     CK(cudaMalloc(&d_x, np * tsize()));
-    CK(cudaMalloc(&d_f, np * sizeof(long long)));
-    CK(cudaMalloc(&d_bg, np * sizeof(long long)));
+    CK(cudaMalloc(&d_f, np * words * sizeof(long long)));
+    CK(cudaMalloc(&d_bg, np * words * sizeof(long long)));
     CK(cudaMalloc(&d_cnt, np * sizeof(int)));
     CK(cudaMalloc(&d_bgest, np * sizeof(double)));
-    CK(cudaMemset(d_f, 0, np * sizeof(long long)));
-    CK(cudaMemset(d_bg, 0, np * sizeof(long long)));
+    CK(cudaMemset(d_f, 0, np * words * sizeof(long long)));
+    CK(cudaMemset(d_bg, 0, np * words * sizeof(long long)));
     CK(cudaMemset(d_cnt, 0, np * sizeof(int)));
     CK(cudaMemset(d_bgest, 0, np * sizeof(double)));
     CK(cudaMalloc(&d_ctl, sizeof(FrameCtl) * n));
@@ -265,6 +273,7 @@ struct Engine {
   }
 
   int sync_nfit() {
+    if (!d_nfit || F == 0) return 0;
     CK(cudaMemcpyAsync(d_nfit, nfit.data(), F * sizeof(int), cudaMemcpyHostToDevice, stream));
     return 0;
   }
@@ -280,31 +289,54 @@ struct Engine {
     return 0;
   }
 
+  // Next pair of timing events from the pool.
+  int timing_pair(cudaEvent_t* a, cudaEvent_t* b) {
+    while (pool.size() < pool_used + 2) {
+      cudaEvent_t ev;
+      CK(cudaEventCreate(&ev));
+      pool.push_back(ev);
+    }
+    *a = pool[pool_used];
+    *b = pool[pool_used + 1];
+    pool_used += 2;
+    return 0;
+  }
+
+  // Read and forget the recorded sweep timings (synchronises on the last).
+  int drain_timing() {
+    if (pool_used == 0) return 0;
+    CK(cudaEventSynchronize(pool[pool_used - 1]));
+    for (size_t i = 0; i + 1 < pool_used; i += 2) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, pool[i], pool[i + 1]));
+      sweep_ms += ms;
+      sweep_launches++;
+    }
+    pool_used = 0;
+    return 0;
+  }
+
   int tick() {
     ticks++;
+    launches += 3;
+    cudaEvent_t ta = nullptr, tb = nullptr;
+    if (timing && timing_pair(&ta, &tb)) return -1;
     if (prec == 32) {
       FrameSet<float> s = fs<float>();
       CK(Launch<float>::prepare(cfg, s, cta_smem, stream));
       epoch++;
-      if (timing) CK(cudaEventRecord(ev0, stream));
+      if (timing) CK(cudaEventRecord(ta, stream));
       CK(Launch<float>::sweep(cfg, s, epoch, sweep_grid, sweep_smem, stream));
-      if (timing) CK(cudaEventRecord(ev1, stream));
+      if (timing) CK(cudaEventRecord(tb, stream));
       CK(Launch<float>::post(cfg, s, cta_smem, stream));
     } else {
       FrameSet<double> s = fs<double>();
       CK(Launch<double>::prepare(cfg, s, cta_smem, stream));
       epoch++;
-      if (timing) CK(cudaEventRecord(ev0, stream));
+      if (timing) CK(cudaEventRecord(ta, stream));
       CK(Launch<double>::sweep(cfg, s, epoch, sweep_grid, sweep_smem, stream));
-      if (timing) CK(cudaEventRecord(ev1, stream));
+      if (timing) CK(cudaEventRecord(tb, stream));
       CK(Launch<double>::post(cfg, s, cta_smem, stream));
-    }
-    if (timing) {
-      CK(cudaEventSynchronize(ev1));
-      float ms = 0.f;
-      CK(cudaEventElapsedTime(&ms, ev0, ev1));
-      sweep_ms += ms;
-      sweep_launches++;
     }
     return 0;
   }
@@ -446,6 +478,8 @@ saFitData* new_handle(const double* rqe, const double* scmos, double tol, int nx
   e->scmos_h.assign(scmos, scmos + e->npix);
   const char* pe = getenv("SA_CUDA_PRECISION");
   if (pe && atoi(pe) == 64) e->prec = 64;
+  const char* ps = getenv("SA_CUDA_SERIAL");
+  e->cfg.force_serial = (ps && atoi(ps) == 1) ? 1 : 0;
   h->image_size_x = nx;
   h->image_size_y = ny;
   h->tolerance = tol;
@@ -496,7 +530,8 @@ int ncol_for(const Engine* e, int ptype) {
 }
 
 // Insert new peaks for frames [0, nframes) (rows concatenated per frame).
-int insert_peaks(Engine* e, const double* rows, const std::vector<int>& counts, int ptype) {
+int insert_peaks(Engine* e, const double* rows, const std::vector<int>& counts, int ptype,
+                 bool rows_on_device = false) {
   const int ncol = ncol_for(e, ptype);
   int n = 0;
   for (int c : counts) n += c;
@@ -521,7 +556,8 @@ int insert_peaks(Engine* e, const double* rows, const std::vector<int>& counts, 
   int* d_frames = (int*)(st + rb + ib);
   int* d_ff = (int*)(st + rb + 2 * ib);
   int* d_fn = (int*)(st + rb + 2 * ib + fb);
-  CK(cudaMemcpyAsync(d_rows, rows, rb, cudaMemcpyHostToDevice, e->stream));
+  if (rows_on_device) d_rows = const_cast<double*>(rows);
+  else CK(cudaMemcpyAsync(d_rows, rows, rb, cudaMemcpyHostToDevice, e->stream));
   CK(cudaMemcpyAsync(d_slots, slots.data(), ib, cudaMemcpyHostToDevice, e->stream));
   CK(cudaMemcpyAsync(d_frames, frames.data(), ib, cudaMemcpyHostToDevice, e->stream));
   CK(cudaMemcpyAsync(d_ff, ffirst.data(), fb, cudaMemcpyHostToDevice, e->stream));
@@ -541,6 +577,7 @@ int insert_peaks(Engine* e, const double* rows, const std::vector<int>& counts, 
       CK(Launch<double>::new_peaks_finder(e->cfg, s, d_slots, d_ff, d_fn, (int)counts.size(), e->warp_smem, e->stream));
     CK(Launch<double>::peak_error(e->cfg, s, d_slots, d_frames, n, e->stream));
   }
+  e->launches += (ptype == PT_FINDER) ? 3 : 2;
   for (size_t f = 0; f < counts.size(); f++) e->nfit[f] += counts[f];
   if (e->sync_nfit()) return -1;
   CK(cudaStreamSynchronize(e->stream));
@@ -1079,8 +1116,8 @@ int saGetSchedStats(saFitData* h, int64_t* out2) {
   CK(cudaMemcpy(ctl.data(), e->d_ctl, sizeof(FrameCtl) * e->F, cudaMemcpyDeviceToHost));
   long long reruns = 0, barriers = 0;
   for (const FrameCtl& c : ctl) {
-    reruns += c.attempts > 1 ? c.attempts - 1 : 0;
-    barriers += c.n_barrier;
+    reruns += c.reruns_total;
+    barriers += c.barriers_total;
   }
   out2[0] = reruns;
   out2[1] = barriers;
@@ -1122,6 +1159,7 @@ int saNewImages(saFitData* h, const void* images, int n_frames, int bits, int on
   }
   if (e->prec == 32) CK(Launch<float>::new_image(e->fs<float>(), src, bits, 0, n_frames, e->stream));
   else CK(Launch<double>::new_image(e->fs<double>(), src, bits, 0, n_frames, e->stream));
+  e->launches += 1;
   std::fill(e->nfit.begin(), e->nfit.end(), 0);
   if (e->sync_nfit()) return -1;
   e->host_pk.clear();
@@ -1147,12 +1185,13 @@ int saNewBackgrounds(saFitData* h, const void* bgs, int n_frames, int bits, int 
   }
   if (e->prec == 32) CK(Launch<float>::new_background(e->fs<float>(), src, bits, 0, n_frames, e->stream));
   else CK(Launch<double>::new_background(e->fs<double>(), src, bits, 0, n_frames, e->stream));
+  e->launches += 1;
   CK(cudaStreamSynchronize(e->stream));
   return 0;
 }
 
-int saNewPeaksBatch(saFitData* h, const double* peaks, const int32_t* counts, int n_frames,
-                    const char* p_type) {
+static int new_peaks_batch(saFitData* h, const double* peaks, const int32_t* counts, int n_frames,
+                           const char* p_type, bool on_device) {
   Engine* e = E(h);
   if (!e) return -1;
   const int pt = parse_ptype(p_type);
@@ -1171,9 +1210,19 @@ int saNewPeaksBatch(saFitData* h, const double* peaks, const int32_t* counts, in
       return -1;
     }
   }
-  if (insert_peaks(e, peaks, cnt, pt)) return -1;
+  if (insert_peaks(e, peaks, cnt, pt, on_device)) return -1;
   h->nfit = e->nfit[0];
   return 0;
+}
+
+int saNewPeaksBatch(saFitData* h, const double* peaks, const int32_t* counts, int n_frames,
+                    const char* p_type) {
+  return new_peaks_batch(h, peaks, counts, n_frames, p_type, false);
+}
+
+int saNewPeaksBatchDevice(saFitData* h, const double* d_peaks, const int32_t* counts, int n_frames,
+                          const char* p_type) {
+  return new_peaks_batch(h, d_peaks, counts, n_frames, p_type, true);
 }
 
 int saDoFitBatch(saFitData* h, int max_iterations) {
@@ -1216,9 +1265,39 @@ int saGetPeakPropertyIntBatch(saFitData* h, int32_t* values, const char* what) {
   return 0;
 }
 
+int saSetDevice(int device) {
+  CK(cudaSetDevice(device));
+  return 0;
+}
+
+int saGetResultsBatch(saFitData* h, double* values, int32_t* ints) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk) return -1;
+  int n = 0;
+  for (int f = 0; f < e->F; f++) n += e->nfit[f];
+  if (n == 0) return 0;
+  // one device-to-host copy of the records of all frames
+  const size_t rb = (size_t)e->cap_total * sizeof(PeakRec);
+  std::vector<PeakRec> recs(e->cap_total);
+  CK(cudaMemcpyAsync(recs.data(), e->d_pk, rb, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  const char* names[8] = {"x", "y", "z", "height", "background", "xsigma", "ysigma", "error"};
+  size_t o = 0;
+  for (int f = 0; f < e->F; f++) {
+    for (int j = 0; j < e->nfit[f]; j++, o++) {
+      const PeakRec& r = recs[(size_t)e->pk_off[f] + j];
+      for (int q = 0; q < 8; q++) record_prop(e, r, names[q], values + o * 8 + q);
+      ints[o * 2] = r.status;
+      ints[o * 2 + 1] = r.iterations;
+    }
+  }
+  return n;
+}
+
 int saSetTiming(saFitData* h, int on) {
   Engine* e = E(h);
   if (!e) return -1;
+  e->drain_timing();
   e->timing = on != 0;
   e->sweep_ms = 0.0;
   e->sweep_launches = 0;
@@ -1229,10 +1308,16 @@ int saSetTiming(saFitData* h, int on) {
 int saGetTiming(saFitData* h, double* total_ms, int64_t* launches, int64_t* ticks) {
   Engine* e = E(h);
   if (!e) return -1;
+  if (e->drain_timing()) return -1;
   *total_ms = e->sweep_ms;
   *launches = e->sweep_launches;
   *ticks = e->ticks;
   return 0;
+}
+
+int64_t saGetKernelLaunches(saFitData* h) {
+  Engine* e = E(h);
+  return e ? e->launches : -1;
 }
 
 }  // extern "C"

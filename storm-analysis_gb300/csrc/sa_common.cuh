@@ -81,6 +81,7 @@ struct ModelCfg {
   double wx[5], wy[5];   // w0 stored squared (dao_fit.c:1566-1567)
   double zmin, zmax;
   double min_height;
+  int force_serial;      // 1: every frame runs its peaks strictly in index order
 };
 
 // Per-frame control block of the device state machine.
@@ -99,6 +100,8 @@ struct FrameCtl {
   int unconverged;
   int nrun;
   int attempts;
+  int reruns_total;      // sweep attempts beyond the first, all sweeps
+  int barriers_total;    // escaped peaks made barriers, all sweeps
   long long ctr[NCOUNTERS];
 };
 
@@ -130,12 +133,54 @@ struct FrameSet {
   const unsigned short* roi_xy;  // packed (rx | ry << 8)
 };
 
-__host__ __device__ inline long long fx_q(double v) {
+// Fit-image / background accumulators.  FP32 pixel arithmetic keeps one
+// int64 word per pixel in units of 2^-36; FP64 keeps two words (units 2^-18
+// and 2^-50) whose sum resolves 8.9e-16 absolute, finer than a double at
+// the pixel magnitudes of a fit, so that FP64 runs follow the reference's
+// double arithmetic to rounding while add/subtract stay exact and
+// order-free.
+template <typename T>
+struct AccW {
+  static constexpr int W = sizeof(T) == 8 ? 2 : 1;
+};
+
+struct Q2 {
+  long long h, l;
+};
+
+template <int W>
+__host__ __device__ inline Q2 acc_quant(double v) {
+  Q2 q;
+  if (W == 1) {
 #ifdef __CUDA_ARCH__
-  return __double2ll_rn(v * FX_SCALE);
+    q.h = __double2ll_rn(v * FX_SCALE);
 #else
-  return (long long)llrint(v * FX_SCALE);
+    q.h = (long long)llrint(v * FX_SCALE);
 #endif
+    q.l = 0;
+  } else {
+    const double s = v * 262144.0;   // 2^18, exact
+#ifdef __CUDA_ARCH__
+    q.h = __double2ll_rd(s);
+#else
+    q.h = (long long)floor(s);
+#endif
+    const double r = v - (double)q.h * (1.0 / 262144.0);   // exact, in [0, 2^-18)
+#ifdef __CUDA_ARCH__
+    q.l = __double2ll_rn(r * 1125899906842624.0);         // 2^50
+#else
+    q.l = (long long)llrint(r * 1125899906842624.0);
+#endif
+  }
+  return q;
 }
+
+template <int W>
+__host__ __device__ inline double acc_value(Q2 q) {
+  if (W == 1) return (double)q.h * FX_INV;
+  return (double)q.h * (1.0 / 262144.0) + (double)q.l * (1.0 / 1125899906842624.0);
+}
+
+__host__ __device__ inline long long fx_q(double v) { return acc_quant<1>(v).h; }
 
 }  // namespace sa

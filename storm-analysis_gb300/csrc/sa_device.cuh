@@ -122,9 +122,7 @@ __device__ __forceinline__ double deviance(double fi, double x) {
 //   r - log1p(r) = u r - 2 u^3 (1/3 + u^2/5 + u^4/7 + ...),
 // whose two terms do not cancel; elsewhere the direct form is well
 // conditioned.
-__device__ __forceinline__ float deviance(float fi, float x) {
-  const float r = __fdiv_rn(fi - x, x);
-  float t;
+__device__ __forceinline__ float r_minus_log1p(float r) {
   if (fabsf(r) < 0.5f) {
     const float u = __fdiv_rn(r, 2.0f + r);
     const float u2 = u * u;
@@ -137,11 +135,28 @@ __device__ __forceinline__ float deviance(float fi, float x) {
     s = fmaf(u2, s, 1.0f / 7.0f);
     s = fmaf(u2, s, 1.0f / 5.0f);
     s = fmaf(u2, s, 1.0f / 3.0f);
-    t = fmaf(u, r, -2.0f * u * u2 * s);
-  } else {
-    t = r - log1pf(r);
+    return fmaf(u, r, -2.0f * u * u2 * s);
   }
-  return 2.0f * x * t;
+  return r - log1pf(r);
+}
+
+// Deviance from the residual res = f - x, which the caller computes
+// accurately: 2 x (r - log1p(r)) with r = res / x.
+__device__ __forceinline__ float dev_res(float res, float x) {
+  return 2.0f * x * r_minus_log1p(__fdiv_rn(res, x));
+}
+
+__device__ __forceinline__ float deviance(float fi, float x) { return dev_res(fi - x, x); }
+
+// Change of the deviance when the model value f0 (residual rho0 = f0 - x)
+// changes by df: 2[df - x log1p(df/f0)] = 2[df rho0/f0 + x (r - log1p(r))],
+// r = df/f0.  Both terms are accurate relative to the change itself, so an
+// FP32 evaluation decides "error went up / down / by less than tol" as an
+// FP64 evaluation of the two absolute errors would.
+__device__ __forceinline__ float dev_delta(float df, float f0, float rho0, float x) {
+  const float r = __fdiv_rn(df, f0);
+  if (fabsf(r) < 0.5f) return 2.0f * (__fdiv_rn(df * rho0, f0) + x * r_minus_log1p(r));
+  return 2.0f * (df - x * log1pf(r));
 }
 
 // Explicitly rounded products so that a contribution computed in one
@@ -178,6 +193,9 @@ struct WarpWS {
   T* X;       // data
   T* IC;      // 1 / (base count + 1)
   T* psf;     // current peak shape
+  T* psf0;    // FP32 only: shape at the start of the step
+  T* f0;      // FP32 only: model value at the start of the step
+  T* rho;     // FP32 only: residual f0 - x, computed in FP64
   T* ext;     // Gaussian x factors / spline deltas (4*64)
   T* eyt;
   T* xt;
@@ -188,9 +206,14 @@ struct WarpWS {
 };
 
 template <typename T>
+__host__ __device__ constexpr int ws_pixel_arrays() {
+  return sizeof(T) == 4 ? 9 : 6;
+}
+
+template <typename T>
 __host__ __device__ inline size_t warp_ws_bytes(int nroi) {
   size_t n = (size_t)((nroi + 31) / 32) * 32;
-  size_t b = 6 * n * sizeof(T);
+  size_t b = ws_pixel_arrays<T>() * n * sizeof(T);
   b += 4 * 64 * sizeof(T) * 2;   // ext/eyt/xt/yt (Gaussian) or 4 delta tables (spline)
   b = (b + 15) & ~(size_t)15;
   b += 36 * sizeof(double) + 16 * sizeof(double);
@@ -209,12 +232,15 @@ __device__ inline WarpWS<T> warp_ws(char* base, int nroi) {
   ws.X = t + 3 * n;
   ws.IC = t + 4 * n;
   ws.psf = t + 5 * n;
-  T* tab = t + 6 * n;
+  ws.psf0 = t + 6 * n;   // only valid when ws_pixel_arrays<T>() == 9
+  ws.f0 = t + 7 * n;
+  ws.rho = t + 8 * n;
+  T* tab = t + ws_pixel_arrays<T>() * n;
   ws.ext = tab;
   ws.eyt = tab + 128;
   ws.xt = tab + 256;
   ws.yt = tab + 384;
-  size_t off = 6 * n * sizeof(T) + 4 * 64 * sizeof(T) * 2;
+  size_t off = ws_pixel_arrays<T>() * n * sizeof(T) + 4 * 64 * sizeof(T) * 2;
   off = (off + 15) & ~(size_t)15;
   ws.jh = reinterpret_cast<double*>(base + off);
   ws.scratch = ws.jh + 36;
@@ -535,6 +561,85 @@ __device__ __forceinline__ void jt_row(const ModelCfg& cfg, const T* aij, const 
   }
 }
 
+// ---------------------------------------------------------------------------
+// differential shape evaluation (FP32 engine)
+//
+// For a trial at the same ROI anchor the change of the peak shape is
+// computed from differences that are accurate relative to the step:
+//  Gaussian: ext1 - ext0 = ext0 * expm1(a1 - a0), a = -t^2 w, with
+//            a1 - a0 = -[dt (2 t0 + dt) w1 + t0^2 (w1 - w0)], dt = -(x1 - x0);
+//  spline:   m1 - m0 for each monomial x^a y^b z^c, telescoped as
+//            d(x^a) y1^b z1^c + x0^a d(y^b) z1^c + x0^a y0^b d(z^c),
+//            d(p^n) = dp * sum_j p1^j p0^(n-1-j).
+// Tables: Gaussian start factors at ext[64+i] / eyt[64+i], differences at
+// xt[64+i] / yt[64+i]; spline monomial differences at xt[0..63].
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ inline void diff_tables(const ModelCfg& cfg, const PeakRec& w0, const PeakRec& w1,
+                                   const SplinePos& s0, const SplinePos& s1, WarpWS<T>& ws, int lane) {
+  if (!is_spline(cfg.model)) {
+    const double xo0 = -(w0.p[PX] - (double)w0.xi) - cfg.xoff;
+    const double yo0 = -(w0.p[PY] - (double)w0.yi) - cfg.xoff;
+    const double dtx = (w0.p[PX] - w1.p[PX]);
+    const double dty = (w0.p[PY] - w1.p[PY]);
+    const double wx1 = w1.p[PXW], dwx = w1.p[PXW] - w0.p[PXW];
+    const double wy1 = w1.p[PYW], dwy = w1.p[PYW] - w0.p[PYW];
+    for (int i = lane; i < cfg.roi; i += 32) {
+      const double tx = (double)i + xo0, ty = (double)i + yo0;
+      const double dax = -(dtx * (2.0 * tx + dtx) * wx1 + tx * tx * dwx);
+      const double day = -(dty * (2.0 * ty + dty) * wy1 + ty * ty * dwy);
+      ws.xt[64 + i] = ws.ext[64 + i] * (T)expm1f((float)dax);
+      ws.yt[64 + i] = ws.eyt[64 + i] * (T)expm1f((float)day);
+    }
+  } else {
+    const double x0 = clamp01(s0.xd), x1 = clamp01(s1.xd);
+    const double y0 = clamp01(s0.yd), y1 = clamp01(s1.yd);
+    const double z0 = clamp01(s0.zd), z1 = clamp01(s1.zd);
+    const T dx = (T)(x1 - x0), dy = (T)(y1 - y0), dz = (T)(z1 - z0);
+    const T X0 = (T)x0, X1 = (T)x1, Y0 = (T)y0, Y1 = (T)y1, Z0 = (T)z0, Z1 = (T)z1;
+    const bool three = (cfg.model == M_SPLINE3D);
+    const int nmono = three ? 64 : 16;
+    for (int id = lane; id < nmono; id += 32) {
+      const int a = three ? (id >> 4) : (id >> 2);
+      const int b = three ? ((id >> 2) & 3) : (id & 3);
+      const int c = three ? (id & 3) : 0;
+      // d(p^n) via the telescoped sum
+      T sx = (T)0, sy = (T)0, sz = (T)0;
+      for (int j = 0; j < a; j++) sx += pw(X1, j) * pw(X0, a - 1 - j);
+      for (int j = 0; j < b; j++) sy += pw(Y1, j) * pw(Y0, b - 1 - j);
+      for (int j = 0; j < c; j++) sz += pw(Z1, j) * pw(Z0, c - 1 - j);
+      ws.xt[id] = (dx * sx) * pw(Y1, b) * pw(Z1, c) + pw(X0, a) * (dy * sy) * pw(Z1, c) +
+                  pw(X0, a) * pw(Y0, b) * (dz * sz);
+    }
+  }
+}
+
+// Trial shape (canonical, from the trial tables) and its change from the
+// start of the step at ROI pixel (rx, ry).
+template <typename T>
+__device__ __forceinline__ void psf_and_delta(const ModelCfg& cfg, const T* aij, const WarpWS<T>& ws,
+                                              const SplinePos& s, int rx, int ry, T& psf, T& dpsf) {
+  if (!is_spline(cfg.model)) {
+    psf = mul_rn(ws.eyt[ry], ws.ext[rx]);
+    const T ex0 = ws.ext[64 + rx], dex = ws.xt[64 + rx];
+    const T ey0 = ws.eyt[64 + ry], dey = ws.yt[64 + ry];
+    dpsf = ey0 * dex + dey * (ex0 + dex);
+    return;
+  }
+  const int nc = (cfg.model == M_SPLINE3D) ? 64 : 16;
+  const T* c = spline_cell(cfg, aij, s.zi, ry + s.ys, rx + s.xs);
+  T acc = (T)0, dacc = (T)0;
+#pragma unroll 8
+  for (int i = 0; i < nc; i++) {
+    const T ci = __ldg(c + i);
+    acc = fma_rn(ci, ws.ext[i], acc);
+    dacc = fma_rn(ci, ws.xt[i], dacc);
+  }
+  psf = acc;
+  dpsf = dacc;
+}
+
 // d width / dz factors of the Z model (dao_fit.c:904-916).
 __device__ inline void z_factors(const ModelCfg& cfg, const PeakRec& w, double& gx, double& gy) {
   gx = gy = 0.0;
@@ -554,6 +659,29 @@ __device__ __forceinline__ long long pix_index(const ModelCfg& cfg, int xi, int 
   return (long long)(yi + ry) * cfg.nx + (xi + rx);
 }
 
+// Accumulator access: pixel i of a W-word array (see acc_quant).
+template <int W>
+__device__ __forceinline__ Q2 acc_load(const long long* a, long long i) {
+  Q2 q;
+  q.h = __ldcg(a + i * W);
+  q.l = (W == 2) ? __ldcg(a + i * W + 1) : 0;
+  return q;
+}
+
+template <int W>
+__device__ __forceinline__ void acc_red(long long* a, long long i, Q2 q, int sign) {
+  unsigned long long* p = reinterpret_cast<unsigned long long*>(a + i * W);
+  atomicAdd(p, (unsigned long long)(sign > 0 ? q.h : -q.h));
+  if (W == 2) atomicAdd(p + 1, (unsigned long long)(sign > 0 ? q.l : -q.l));
+}
+
+__device__ __forceinline__ Q2 q_sub(Q2 a, Q2 b) {
+  Q2 r;
+  r.h = a.h - b.h;
+  r.l = a.l - b.l;
+  return r;
+}
+
 // Add (sign +1) or subtract (sign -1) a peak's contribution over its ROI
 // with integer atomics (mFitAddPeak multi_fit.c:28-57, mFitSubtractPeak
 // :1894-1922).  The shape tables of w must be in the workspace.
@@ -561,25 +689,24 @@ template <typename T>
 __device__ inline void add_peak(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
                                 const PeakRec& w, const SplinePos& s, const WarpWS<T>& ws,
                                 int sign, int lane) {
+  constexpr int W = AccW<T>::W;
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
     roi_rc(fs.roi_xy, p, rx, ry);
     const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
     const T rq = __ldg(fs.rqe + k), sc = __ldg(fs.scmos + k);
     const T psf = psf_at(cfg, fs.aij, ws, s, rx, ry);
-    const long long cf = fx_q((double)contrib_f(w.p[PH], psf, rq));
-    const long long cb = fx_q((double)contrib_bg(w.p[PBG], rq, sc));
-    atomicAdd(reinterpret_cast<unsigned long long*>(fs.f + fbase + k),
-              (unsigned long long)(sign > 0 ? cf : -cf));
-    atomicAdd(reinterpret_cast<unsigned long long*>(fs.bg + fbase + k),
-              (unsigned long long)(sign > 0 ? cb : -cb));
+    acc_red<W>(fs.f, fbase + k, acc_quant<W>((double)contrib_f(w.p[PH], psf, rq)), sign);
+    acc_red<W>(fs.bg, fbase + k, acc_quant<W>((double)contrib_bg(w.p[PBG], rq, sc)), sign);
     atomicAdd(fs.cnt + fbase + k, sign);
   }
 }
 
-// Pixel model value from the global fixed-point state (f + bg/cnt, multi_fit.c:143).
-__device__ __forceinline__ double fi_global(long long f, long long bg, int cnt) {
-  return (double)f * FX_INV + ((double)bg * FX_INV) / (double)cnt;
+// Pixel model value from the global accumulator state (f + bg/cnt, multi_fit.c:143).
+template <typename T>
+__device__ __forceinline__ double fi_global(const FrameSet<T>& fs, long long g) {
+  constexpr int W = AccW<T>::W;
+  return acc_value<W>(acc_load<W>(fs.f, g)) + acc_value<W>(acc_load<W>(fs.bg, g)) / (double)__ldcg(fs.cnt + g);
 }
 
 }  // namespace sa

@@ -84,16 +84,17 @@ __device__ __forceinline__ T bg_div(T b, T ic) {
 template <typename T>
 __device__ inline void load_base(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase, int ax,
                                  int ay, WarpWS<T>& ws, int lane) {
+  constexpr int W = AccW<T>::W;
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
     roi_rc(fs.roi_xy, p, rx, ry);
     const long long k = pix_index(cfg, ax, ay, rx, ry);
-    const long long Fg = __ldcg(fs.f + fbase + k);
-    const long long Bg = __ldcg(fs.bg + fbase + k);
+    const double Fg = acc_value<W>(acc_load<W>(fs.f, fbase + k));
+    const double Bg = acc_value<W>(acc_load<W>(fs.bg, fbase + k));
     const int Cg = __ldcg(fs.cnt + fbase + k);
     const T sc = __ldg(fs.scmos + k);
-    ws.Fb[p] = (T)((double)Fg * FX_INV);
-    ws.Bs[p] = (T)((double)Bg * FX_INV + (double)sc);
+    ws.Fb[p] = (T)Fg;
+    ws.Bs[p] = (T)(Bg + (double)sc);
     ws.R[p] = __ldg(fs.rqe + k);
     ws.X[p] = __ldg(fs.x + fbase + k);
     ws.IC[p] = ic_store<T>(Cg + 1);
@@ -125,16 +126,26 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     int rx, ry;
     roi_rc(fs.roi_xy, p, rx, ry);
     const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
-    const long long Fg = __ldcg(fs.f + fbase + kk);
-    const long long Bg = __ldcg(fs.bg + fbase + kk);
+    const Q2 Fq = acc_load<AccW<T>::W>(fs.f, fbase + kk);
+    const Q2 Bq = acc_load<AccW<T>::W>(fs.bg, fbase + kk);
     const int Cg = __ldcg(fs.cnt + fbase + kk);
     const T xv = __ldg(fs.x + fbase + kk);
     const T rq = __ldg(fs.rqe + kk);
     const T sc = __ldg(fs.scmos + kk);
     const T psf = psf_at(cfg, fs.aij, ws, s0, rx, ry);
-    const double fi0 = fi_global(Fg, Bg, Cg);
-    if (!(fi0 > 0.0)) fail = true;
-    else dev += (double)deviance((T)fi0, xv);
+    const double fi0 = acc_value<AccW<T>::W>(Fq) + acc_value<AccW<T>::W>(Bq) / (double)Cg;
+    if constexpr (sizeof(T) == 4) {
+      // keep the start state for the differential trial evaluation
+      const float rho = (float)(fi0 - (double)xv);
+      ws.psf0[p] = psf;
+      ws.f0[p] = (float)fi0;
+      ws.rho[p] = rho;
+      if (!(fi0 > 0.0)) fail = true;
+      else dev += (double)dev_res(rho, xv);
+    } else {
+      if (!(fi0 > 0.0)) fail = true;
+      else dev += (double)deviance((T)fi0, xv);
+    }
     const T fiT = (T)fi0;
     const T t1 = (T)2 * ((T)1 - xv / fiT);
     const T t2 = (T)2 * xv / (fiT * fiT);
@@ -159,13 +170,13 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     }
     (void)idx;
     // subtract this peak (multi_fit.c:1141) and keep the base state
-    const long long cf = fx_q((double)contrib_f(orig.p[PH], psf, rq));
-    const long long cb = fx_q((double)contrib_bg(orig.p[PBG], rq, sc));
-    atomicAdd(reinterpret_cast<unsigned long long*>(fs.f + fbase + kk), (unsigned long long)(-cf));
-    atomicAdd(reinterpret_cast<unsigned long long*>(fs.bg + fbase + kk), (unsigned long long)(-cb));
+    const Q2 cf = acc_quant<AccW<T>::W>((double)contrib_f(orig.p[PH], psf, rq));
+    const Q2 cb = acc_quant<AccW<T>::W>((double)contrib_bg(orig.p[PBG], rq, sc));
+    acc_red<AccW<T>::W>(fs.f, fbase + kk, cf, -1);
+    acc_red<AccW<T>::W>(fs.bg, fbase + kk, cb, -1);
     atomicAdd(fs.cnt + fbase + kk, -1);
-    ws.Fb[p] = (T)((double)(Fg - cf) * FX_INV);
-    ws.Bs[p] = (T)((double)(Bg - cb) * FX_INV + (double)sc);
+    ws.Fb[p] = (T)acc_value<AccW<T>::W>(q_sub(Fq, cf));
+    ws.Bs[p] = (T)(acc_value<AccW<T>::W>(q_sub(Bq, cb)) + (double)sc);
     ws.R[p] = rq;
     ws.X[p] = xv;
     ws.IC[p] = ic_store<T>(Cg);   // (Cg - 1) + 1 once the peak is re-added
@@ -175,6 +186,15 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
   {
     T v = warp_transpose_sum32(acc, lane);
     if (lane < nh) ws.jh[lane] = (double)v;
+  }
+  if constexpr (sizeof(T) == 4) {
+    // Gaussian start-of-step factors for the differential evaluation.
+    if (!is_spline(cfg.model)) {
+      for (int i = lane; i < cfg.roi; i += 32) {
+        ws.ext[64 + i] = ws.ext[i];
+        ws.eyt[64 + i] = ws.eyt[i];
+      }
+    }
   }
   __syncwarp();
 
@@ -259,17 +279,55 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     }
     dev = 0.0;
     fail = false;
+    bool is_delta = false;
     const double hh = wl.p[PH], bgv = wl.p[PBG];
     const T bgT = (T)bgv;
-    for (int p = lane; p < cfg.nroi; p += 32) {
-      int rx, ry;
-      roi_rc(fs.roi_xy, p, rx, ry);
-      const T psf = psf_at(cfg, fs.aij, ws, s, rx, ry);
-      ws.psf[p] = psf;
-      const T rq = ws.R[p];
-      const T fi = ws.Fb[p] + contrib_f(hh, psf, rq) + bg_div(ws.Bs[p] + bgT * rq, ws.IC[p]);
-      if (!(fi > (T)0)) fail = true;
-      else dev += (double)deviance(fi, ws.X[p]);
+    if constexpr (sizeof(T) == 4) {
+      // FP32: evaluate the change of the error from the start of the step
+      // when the ROI and (for splines) the spline cell are unchanged.
+      is_delta = (wl.xi == orig.xi) && (wl.yi == orig.yi) &&
+                 (!is_spline(cfg.model) || (s.xs == s0.xs && s.ys == s0.ys && s.zi == s0.zi));
+      if (is_delta) {
+        diff_tables(cfg, orig, wl, s0, s, ws, lane);
+        __syncwarp();
+        const float h1 = (float)hh;
+        const float dh = (float)(hh - orig.p[PH]);
+        const float dbg = (float)(bgv - orig.p[PBG]);
+        for (int p = lane; p < cfg.nroi; p += 32) {
+          int rx, ry;
+          roi_rc(fs.roi_xy, p, rx, ry);
+          float psf, dpsf;
+          psf_and_delta(cfg, fs.aij, ws, s, rx, ry, psf, dpsf);
+          ws.psf[p] = psf;
+          const float rq = ws.R[p];
+          const float df = rq * fmaf(h1, dpsf, dh * ws.psf0[p]) + dbg * rq * ws.IC[p];
+          const float f1 = ws.f0[p] + df;
+          if (!(f1 > 0.0f)) fail = true;
+          else dev += (double)dev_delta(df, ws.f0[p], ws.rho[p], ws.X[p]);
+        }
+      } else {
+        for (int p = lane; p < cfg.nroi; p += 32) {
+          int rx, ry;
+          roi_rc(fs.roi_xy, p, rx, ry);
+          const T psf = psf_at(cfg, fs.aij, ws, s, rx, ry);
+          ws.psf[p] = psf;
+          const T rq = ws.R[p];
+          const T fi = ws.Fb[p] + contrib_f(hh, psf, rq) + bg_div(ws.Bs[p] + bgT * rq, ws.IC[p]);
+          if (!(fi > (T)0)) fail = true;
+          else dev += (double)dev_res(fi - ws.X[p], ws.X[p]);
+        }
+      }
+    } else {
+      for (int p = lane; p < cfg.nroi; p += 32) {
+        int rx, ry;
+        roi_rc(fs.roi_xy, p, rx, ry);
+        const T psf = psf_at(cfg, fs.aij, ws, s, rx, ry);
+        ws.psf[p] = psf;
+        const T rq = ws.R[p];
+        const T fi = ws.Fb[p] + contrib_f(hh, psf, rq) + bg_div(ws.Bs[p] + bgT * rq, ws.IC[p]);
+        if (!(fi > (T)0)) fail = true;
+        else dev += (double)deviance(fi, ws.X[p]);
+      }
     }
     dev = warp_sum(dev);
     fail = __any_sync(0xffffffffu, fail);
@@ -282,9 +340,11 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
         w.status = ERROR;
         act = ACT_CONTINUE;
       } else {
-        w.error = dev;
-        if (w.error > se) {
-          if (((w.error - se) / se) < cfg.tol) {
+        w.error = is_delta ? se + dev : dev;
+        // change of the error, exact from the differential evaluation
+        const double change = is_delta ? dev : w.error - se;
+        if (is_delta ? (change > 0.0) : (w.error > se)) {
+          if ((change / se) < cfg.tol) {
             w.status = CONVERGED;
             act = ACT_BREAK_ADDED;
           } else {
@@ -295,7 +355,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
             act = ACT_CONTINUE;
           }
         } else {
-          if (((se - w.error) / se) < cfg.tol) {
+          if ((-change / se) < cfg.tol) {
             w.status = CONVERGED;
           } else if (w.lambda > LAMBDA_MIN) {
             w.lambda = LAMBDA_DOWN * w.lambda;
@@ -331,10 +391,8 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
       const long long kk = pix_index(cfg, wl.xi, wl.yi, rx, ry);
       const T rq = ws.R[p];
       const T sc = __ldg(fs.scmos + kk);
-      const long long cf = fx_q((double)contrib_f(wl.p[PH], ws.psf[p], rq));
-      const long long cb = fx_q((double)contrib_bg(wl.p[PBG], rq, sc));
-      atomicAdd(reinterpret_cast<unsigned long long*>(fs.f + fbase + kk), (unsigned long long)cf);
-      atomicAdd(reinterpret_cast<unsigned long long*>(fs.bg + fbase + kk), (unsigned long long)cb);
+      acc_red<AccW<T>::W>(fs.f, fbase + kk, acc_quant<AccW<T>::W>((double)contrib_f(wl.p[PH], ws.psf[p], rq)), +1);
+      acc_red<AccW<T>::W>(fs.bg, fbase + kk, acc_quant<AccW<T>::W>((double)contrib_bg(wl.p[PBG], rq, sc)), +1);
       atomicAdd(fs.cnt + fbase + kk, 1);
     }
   }
@@ -524,7 +582,7 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
       c->escaped_min = INT_MAX;
       c->n_escaped = 0;
       c->n_barrier = 0;
-      c->serial = 0;
+      c->serial = cfg.force_serial;
       c->attempts = 1;
       c->phase = nrun > 0 ? PH_IN_SWEEP : PH_IN_SWEEP;
     }
@@ -576,6 +634,8 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
       c->escaped_min = INT_MAX;
       c->n_escaped = 0;
       c->attempts += 1;
+      c->reruns_total += 1;
+      c->barriers_total = c->barriers_total + c->n_barrier;
       c->phase = PH_IN_SWEEP;
     }
   }
@@ -682,8 +742,10 @@ __global__ void k_new_image(FrameSet<T> fs, const I* img, int frame0, int nframe
     const long long g = (long long)frame0 * fs.npix + i;
     const double v = (double)img[i] * (double)fs.rqe[k] + (double)fs.scmos[k];
     const_cast<T*>(fs.x)[g] = (T)v;
-    fs.f[g] = 0;
-    fs.bg[g] = 0;
+    for (int w = 0; w < AccW<T>::W; w++) {
+      fs.f[g * AccW<T>::W + w] = 0;
+      fs.bg[g * AccW<T>::W + w] = 0;
+    }
     fs.cnt[g] = 0;
   }
 }
@@ -819,7 +881,7 @@ __global__ void k_newpeaks_finder(ModelCfg cfg, FrameSet<T> fs, const int* slots
       const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
       const double t = (double)psf_at(cfg, fs.aij, ws, s, rx, ry) * (double)__ldg(fs.rqe + k);
       sp += t * t * t;
-      const double fv = (double)__ldcg(fs.f + fbase + k) * FX_INV;
+      const double fv = acc_value<AccW<T>::W>(acc_load<AccW<T>::W>(fs.f, fbase + k));
       sx += t * t * ((double)__ldg(fs.x + fbase + k) - fv - fs.bgest[fbase + k]);
     }
     sp = warp_sum(sp);
@@ -857,8 +919,7 @@ __global__ void k_peak_error(ModelCfg cfg, FrameSet<T> fs, const int* slots, con
       int rx, ry;
       roi_rc(fs.roi_xy, p, rx, ry);
       const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
-      const double fi = fi_global(__ldcg(fs.f + fbase + k), __ldcg(fs.bg + fbase + k),
-                                  __ldcg(fs.cnt + fbase + k));
+      const double fi = fi_global(fs, fbase + k);
       const T xv = __ldg(fs.x + fbase + k);
       if (!(fi > 0.0)) fail = true;
       else dev += (double)deviance((T)fi, xv);
@@ -917,8 +978,7 @@ __global__ void k_peak_props(ModelCfg cfg, FrameSet<T> fs, const int* slots, con
       const double bgv = (xv - (double)__ldg(fs.scmos + k)) / (double)__ldg(fs.rqe + k) - w.p[PH] * psf;
       bs += bgv * psf * psf;
       if (out_jac) {
-        const double fi = fi_global(__ldcg(fs.f + fbase + k), __ldcg(fs.bg + fbase + k),
-                                    __ldcg(fs.cnt + fbase + k));
+        const double fi = fi_global(fs, fbase + k);
         const T fiT = (T)fi;
         const T t1 = (T)2 * ((T)1 - (T)xv / fiT);
         T jt[MAX_JAC];
@@ -976,7 +1036,7 @@ __global__ void k_fit_image(FrameSet<T> fs, int frame, double* out, int residual
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < fs.npix;
        k += (long long)gridDim.x * blockDim.x) {
     const long long g = (long long)frame * fs.npix + k;
-    const double fv = (double)fs.f[g] * FX_INV;
+    const double fv = acc_value<AccW<T>::W>(acc_load<AccW<T>::W>(fs.f, g));
     out[k] = residual ? ((double)fs.x[g] - fv) : fv / (double)fs.rqe[k];
   }
 }

@@ -66,8 +66,9 @@ class MultiFitter(object):
     newPeaks, doFit, getPeakProperty, cleanup)."""
 
     def __init__(self, rqe=None, scmos_cal=None, verbose=False, min_z=None, max_z=None,
-                 precision=32, device_loop=True, **kwds):
+                 precision=32, device_loop=True, dilation=None, **kwds):
         super(MultiFitter, self).__init__(**kwds)
+        self.dilation = dilation
         self.clib = loadclib.load()
         self.default_tol = 1.0e-6
         self.device_loop = device_loop
@@ -198,6 +199,8 @@ class MultiFitter(object):
         if not self.mfit:
             raise MultiFitterException(what + " failed: " + loadclib.last_error())
         if self.clib.saSetPrecision(self.mfit, int(self.precision)) != 0:
+            raise MultiFitterException(loadclib.last_error())
+        if self.dilation is not None and self.clib.saSetDilation(self.mfit, int(self.dilation)) != 0:
             raise MultiFitterException(loadclib.last_error())
 
     def isInitialized(self):

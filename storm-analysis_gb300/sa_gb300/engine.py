@@ -69,9 +69,11 @@ class BatchFitter(object):
             lib.cfInitialize3D(self.h)
         else:
             lib.cfInitialize2D(self.h)
-        self.capacity = peaks_capacity
+        self.capacity = None
         self._framed = False
         self.sweeps = 0
+        if peaks_capacity:
+            self.ensure_frames(int(peaks_capacity))
 
     def _ok(self, r, what):
         if r < 0:
@@ -119,6 +121,28 @@ class BatchFitter(object):
         allrows = numpy.ascontiguousarray(numpy.concatenate(rows, axis=0), dtype=numpy.float64)
         return self._ok(self.clib.saNewPeaksBatch(self.h, allrows, counts, self.n_frames,
                                                   ctypes.c_char_p(peaks_type.encode())), "saNewPeaksBatch")
+
+    def load_peaks_device(self, d_rows, counts, peaks_type):
+        """Peak rows already on the device (pointer), counts per frame (host)."""
+        counts = numpy.ascontiguousarray(counts, dtype=numpy.int32)
+        self.ensure_frames(int(counts.max()) if counts.size else 1)
+        return self._ok(self.clib.saNewPeaksBatchDevice(self.h, ctypes.c_void_p(d_rows), counts,
+                                                        self.n_frames,
+                                                        ctypes.c_char_p(peaks_type.encode())),
+                        "saNewPeaksBatchDevice")
+
+    def results_fast(self):
+        """All results with one device-to-host copy: (values[n, 8], ints[n, 2]) with
+        columns x, y, z, height, background, xsigma, ysigma, error / status, iterations."""
+        n = int(self.counts().sum())
+        vals = numpy.zeros((n, 8), dtype=numpy.float64)
+        ints = numpy.zeros((n, 2), dtype=numpy.int32)
+        if n:
+            self._ok(self.clib.saGetResultsBatch(self.h, vals, ints), "saGetResultsBatch")
+        return vals, ints
+
+    def kernel_launches(self):
+        return int(self.clib.saGetKernelLaunches(self.h))
 
     def load(self, images, backgrounds, peaks_per_frame, peaks_type="hdf5"):
         counts = max(len(self.format(p, peaks_type)) for p in peaks_per_frame)

@@ -122,6 +122,7 @@ def _declare(lib):
                        ("saSetFrames", [hp, ci, ci]), ("saNewImages", [hp, vp, ci, ci, ci]),
                        ("saNewBackgrounds", [hp, vp, ci, ci, ci]),
                        ("saNewPeaksBatch", [hp, f64, i32, ci, cs]), ("saDoFitBatch", [hp, ci]),
+                       ("saNewPeaksBatchDevice", [hp, vp, i32, ci, cs]),
                        ("saGetNFitBatch", [hp, i32]), ("saGetPeakPropertyBatch", [hp, f64, cs]),
                        ("saGetPeakPropertyIntBatch", [hp, i32, cs]), ("saSetTiming", [hp, ci]),
                        ("saGetTiming", [hp, ctypes.POINTER(ctypes.c_double),
@@ -129,6 +130,12 @@ def _declare(lib):
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = ci
+    lib.saGetKernelLaunches.argtypes = [hp]
+    lib.saGetKernelLaunches.restype = ctypes.c_int64
+    lib.saGetResultsBatch.argtypes = [hp, f64, i32]
+    lib.saGetResultsBatch.restype = ci
+    lib.saSetDevice.argtypes = [ci]
+    lib.saSetDevice.restype = ci
 
 
 EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoInitialize3D",
@@ -144,5 +151,6 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "mFitRemoveErrorPeaks", "mFitRemoveRunningPeaks", "mFitSetPeakStatus",
            "saGetLastError", "saClearLastError", "saDeviceCount", "saSetPrecision", "saSetDilation", "saSetStream",
            "saDoFit", "saGetCounters", "saGetSchedStats", "saSetFrames", "saNewImages",
-           "saNewBackgrounds", "saNewPeaksBatch", "saDoFitBatch", "saGetNFitBatch",
-           "saGetPeakPropertyBatch", "saGetPeakPropertyIntBatch", "saSetTiming", "saGetTiming"]
+           "saNewBackgrounds", "saNewPeaksBatch", "saNewPeaksBatchDevice", "saDoFitBatch", "saGetNFitBatch",
+           "saGetPeakPropertyBatch", "saGetPeakPropertyIntBatch", "saSetTiming", "saGetTiming",
+           "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice"]
