@@ -203,6 +203,7 @@ struct WarpWS {
   double* jh; // 36: jacobian (7) + upper Hessian (up to 28)
   double* scratch;  // 16
   PeakRec* w;
+  float* red; // FP32 only: 32 x 33 per-lane partial sums of the normal equations
 };
 
 template <typename T>
@@ -218,6 +219,7 @@ __host__ __device__ inline size_t warp_ws_bytes(int nroi) {
   b = (b + 15) & ~(size_t)15;
   b += 36 * sizeof(double) + 16 * sizeof(double);
   b += sizeof(PeakRec);
+  if (sizeof(T) == 4 && nroi > 0) b += 32 * 33 * sizeof(float);
   return (b + 127) & ~(size_t)127;
 }
 
@@ -245,6 +247,7 @@ __device__ inline WarpWS<T> warp_ws(char* base, int nroi) {
   ws.jh = reinterpret_cast<double*>(base + off);
   ws.scratch = ws.jh + 36;
   ws.w = reinterpret_cast<PeakRec*>(base + off + 52 * sizeof(double));
+  ws.red = reinterpret_cast<float*>(base + off + 52 * sizeof(double) + sizeof(PeakRec));
   return ws;
 }
 

@@ -147,7 +147,9 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
       else dev += (double)deviance((T)fi0, xv);
     }
     const T fiT = (T)fi0;
-    const T t1 = (T)2 * ((T)1 - xv / fiT);
+    // FP32: t1 = 2(1 - x/f) = 2(f - x)/f from the FP64 residual (no
+    // cancellation); FP64: the reference's form (dao_fit.c:454).
+    const T t1 = (sizeof(T) == 4) ? (T)(2.0 * (fi0 - (double)xv) / fi0) : (T)2 * ((T)1 - xv / fiT);
     const T t2 = (T)2 * xv / (fiT * fiT);
     T jt[MAX_JAC];
     jt_row(cfg, fs.aij, ws, s0, orig, gx, gy, rx, ry, rq, psf, jt);
@@ -183,7 +185,20 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
   }
   dev = warp_sum(dev);
   fail = __any_sync(0xffffffffu, fail);
-  {
+  if constexpr (sizeof(T) == 4) {
+    // Per-lane partial sums (a few pixels each) are summed across the warp
+    // in FP64: the cross-lane sums are where the gradient cancels.
+    float* red = ws.red;
+#pragma unroll
+    for (int i = 0; i < 32; i++)
+      if (i < nh) red[lane * 33 + i] = acc[i];
+    __syncwarp();
+    if (lane < nh) {
+      double s = 0.0;
+      for (int j = 0; j < 32; j++) s += (double)red[j * 33 + lane];
+      ws.jh[lane] = s;
+    }
+  } else {
     T v = warp_transpose_sum32(acc, lane);
     if (lane < nh) ws.jh[lane] = (double)v;
   }
