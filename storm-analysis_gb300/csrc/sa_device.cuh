@@ -53,6 +53,32 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Float-float accumulation (Knuth's TwoSum): hi + lo carries about 48 bits.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float v) {
+  const float s = hi + v;
+  const float bb = s - hi;
+  const float err = (hi - (s - bb)) + (v - bb);
+  hi = s;
+  lo += err;
+}
+
+// Warp sum of FP32 partials in float-float arithmetic, returned as double
+// (three FP64 instructions per warp instead of a double reduction).
+__device__ __forceinline__ double warp_sum_ff(float v) {
+  float hi = v, lo = 0.0f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    const float s = hi + oh;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (oh - bb);
+    hi = s;
+    lo = lo + ol + err;
+  }
+  return (double)hi + (double)lo;
+}
+
 // Reduce 32 values held by every lane; afterwards lane l holds the warp
 // total of value l.  31 shuffles instead of 32*5.
 template <typename T>
@@ -106,6 +132,34 @@ __device__ inline int chol_solve(const double* a, double* b, int n) {
   for (int i = 0; i < n; i++)
     if (isnan(b[i])) return 1;
   return 0;
+}
+
+// Packed upper-triangle index of (r, c) with r <= c after the k gradient
+// entries: the layout of the normal equations in the warp workspace.
+__device__ __forceinline__ int hes_index(int k, int r, int c) {
+  if (r > c) {
+    const int t = r;
+    r = c;
+    c = t;
+  }
+  return k + r * k - (r * (r - 1)) / 2 + (c - r);
+}
+
+// Damped normal equations (H + lam diag H) d = b, solved on lane 0 in FP64
+// (multi_fit.c:1174-1203 with dposv).  Returns the solver status on lane 0.
+__device__ inline int solve_fp64_lane0(const double* jh, int k, double lam, double* out) {
+  double A[MAX_JAC * MAX_JAC], b[MAX_JAC];
+  int id = k;
+  for (int l = 0; l < k; l++) {
+    b[l] = jh[l];
+    for (int m = l; m < k; m++) {
+      A[l * k + m] = (l == m) ? (1.0 + lam) * jh[id] : jh[id];
+      id++;
+    }
+  }
+  const int info = chol_solve(A, b, k);
+  for (int l = 0; l < k; l++) out[l] = b[l];
+  return info;
 }
 
 // ---------------------------------------------------------------------------
@@ -202,7 +256,9 @@ struct WarpWS {
   T* yt;
   double* jh; // 36: jacobian (7) + upper Hessian (up to 28)
   double* scratch;  // 16
-  PeakRec* w;
+  PeakRec* w;     // working record (lane 0 writes)
+  PeakRec* orig;  // record at the start of the step
+  PeakRec* t;     // trial record (lane 0)
   float* red; // FP32 only: 32 x 33 per-lane partial sums of the normal equations
 };
 
@@ -218,7 +274,7 @@ __host__ __device__ inline size_t warp_ws_bytes(int nroi) {
   b += 4 * 64 * sizeof(T) * 2;   // ext/eyt/xt/yt (Gaussian) or 4 delta tables (spline)
   b = (b + 15) & ~(size_t)15;
   b += 36 * sizeof(double) + 16 * sizeof(double);
-  b += sizeof(PeakRec);
+  b += 3 * sizeof(PeakRec);
   if (sizeof(T) == 4 && nroi > 0) b += 32 * 33 * sizeof(float);
   return (b + 127) & ~(size_t)127;
 }
@@ -247,7 +303,9 @@ __device__ inline WarpWS<T> warp_ws(char* base, int nroi) {
   ws.jh = reinterpret_cast<double*>(base + off);
   ws.scratch = ws.jh + 36;
   ws.w = reinterpret_cast<PeakRec*>(base + off + 52 * sizeof(double));
-  ws.red = reinterpret_cast<float*>(base + off + 52 * sizeof(double) + sizeof(PeakRec));
+  ws.orig = ws.w + 1;
+  ws.t = ws.w + 2;
+  ws.red = reinterpret_cast<float*>(base + off + 52 * sizeof(double) + 3 * sizeof(PeakRec));
   return ws;
 }
 
@@ -582,18 +640,19 @@ template <typename T>
 __device__ inline void diff_tables(const ModelCfg& cfg, const PeakRec& w0, const PeakRec& w1,
                                    const SplinePos& s0, const SplinePos& s1, WarpWS<T>& ws, int lane) {
   if (!is_spline(cfg.model)) {
-    const double xo0 = -(w0.p[PX] - (double)w0.xi) - cfg.xoff;
-    const double yo0 = -(w0.p[PY] - (double)w0.yi) - cfg.xoff;
-    const double dtx = (w0.p[PX] - w1.p[PX]);
-    const double dty = (w0.p[PY] - w1.p[PY]);
-    const double wx1 = w1.p[PXW], dwx = w1.p[PXW] - w0.p[PXW];
-    const double wy1 = w1.p[PYW], dwy = w1.p[PYW] - w0.p[PYW];
+    // per-warp scalars from the FP64 parameters (differences taken in FP64)
+    const float xo0 = (float)(-(w0.p[PX] - (double)w0.xi) - cfg.xoff);
+    const float yo0 = (float)(-(w0.p[PY] - (double)w0.yi) - cfg.xoff);
+    const float dtx = (float)(w0.p[PX] - w1.p[PX]);
+    const float dty = (float)(w0.p[PY] - w1.p[PY]);
+    const float wx1 = (float)w1.p[PXW], dwx = (float)(w1.p[PXW] - w0.p[PXW]);
+    const float wy1 = (float)w1.p[PYW], dwy = (float)(w1.p[PYW] - w0.p[PYW]);
     for (int i = lane; i < cfg.roi; i += 32) {
-      const double tx = (double)i + xo0, ty = (double)i + yo0;
-      const double dax = -(dtx * (2.0 * tx + dtx) * wx1 + tx * tx * dwx);
-      const double day = -(dty * (2.0 * ty + dty) * wy1 + ty * ty * dwy);
-      ws.xt[64 + i] = ws.ext[64 + i] * (T)expm1f((float)dax);
-      ws.yt[64 + i] = ws.eyt[64 + i] * (T)expm1f((float)day);
+      const float tx = (float)i + xo0, ty = (float)i + yo0;
+      const float dax = -(dtx * (2.0f * tx + dtx) * wx1 + tx * tx * dwx);
+      const float day = -(dty * (2.0f * ty + dty) * wy1 + ty * ty * dwy);
+      ws.xt[64 + i] = ws.ext[64 + i] * (T)expm1f(dax);
+      ws.yt[64 + i] = ws.eyt[64 + i] * (T)expm1f(day);
     }
   } else {
     const double x0 = clamp01(s0.xd), x1 = clamp01(s1.xd);
@@ -643,6 +702,129 @@ __device__ __forceinline__ void psf_and_delta(const ModelCfg& cfg, const T* aij,
   dpsf = dacc;
 }
 
+// ---------------------------------------------------------------------------
+// Damped solve of the FP32 engine (warp-collective).
+//
+// The reference solves (H + lam diag H) d = b in FP64 with dposv
+// (multi_fit.c:1839-1883).  Here: Jacobi-scale the system to unit diagonal,
+// factor it in FP32 on lane 0, and refine the solution twice with the
+// residual r = b - A d evaluated in FP64 by lanes 0..k-1 in parallel
+// (one row each).  Each refinement shrinks the error by about
+// cond(A_scaled) * 2^-24, so the result carries FP64-level accuracy for
+// any system the FP32 factorisation accepts, at a few dozen FP64
+// instructions per warp instead of a few hundred.  When the scaled
+// diagonal is not positive or the FP32 factorisation fails, lane 0 falls
+// back to the FP64 Cholesky, which decides failure exactly as dposv does.
+// The solution (lane 0) is written to out[0..k).
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ inline int solve_damped(WarpWS<T>& ws, int k, double lam, double* out, int lane) {
+  int info = 0;
+  if (lane == 0) info = solve_fp64_lane0(ws.jh, k, lam, out);
+  return info;
+}
+
+template <>
+__device__ inline int solve_damped<float>(WarpWS<float>& ws, int k, double lam, double* out, int lane) {
+  float* sm = ws.red;           // free during the solve
+  float* As = sm;               // k x k scaled matrix
+  float* L = sm + 64;           // FP32 Cholesky factor (stride 7)
+  float* rhs = sm + 128;
+  float* sol = sm + 136;
+  float* sc = sm + 144;         // Jacobi scales
+  double* xs = ws.scratch;      // solution being refined
+  const double* jh = ws.jh;
+  double Ai[MAX_JAC];
+  double bi = 0.0, dii = 0.0;
+  float si = 0.0f;
+  bool bad = false;
+  if (lane < k) {
+    bi = jh[lane];
+#pragma unroll
+    for (int j = 0; j < MAX_JAC; j++) {
+      if (j < k) {
+        const double a = jh[hes_index(k, lane, j)];
+        Ai[j] = (j == lane) ? (1.0 + lam) * a : a;
+        if (j == lane) dii = Ai[j];
+      }
+    }
+    const float df = (float)dii;
+    bad = !(dii > 0.0) || !(df > 1.0e-30f) || !(df < 1.0e30f);
+    si = bad ? 0.0f : rsqrtf(df);
+    sc[lane] = si;
+  }
+  int status = __any_sync(0xffffffffu, bad) ? 2 : 0;
+  __syncwarp();
+  if (status == 0) {
+    if (lane < k) {
+#pragma unroll
+      for (int j = 0; j < MAX_JAC; j++)
+        if (j < k) As[lane * k + j] = ((float)Ai[j] * si) * sc[j];
+      rhs[lane] = (float)bi * si;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      for (int j = 0; j < k && status == 0; j++) {
+        float d = As[j * k + j];
+        for (int m = 0; m < j; m++) d -= L[j * 7 + m] * L[j * 7 + m];
+        if (!(d > 0.0f)) {
+          status = 2;
+          break;
+        }
+        d = sqrtf(d);
+        L[j * 7 + j] = d;
+        const float inv = 1.0f / d;
+        for (int i = j + 1; i < k; i++) {
+          float s = As[i * k + j];
+          for (int m = 0; m < j; m++) s -= L[i * 7 + m] * L[j * 7 + m];
+          L[i * 7 + j] = s * inv;
+        }
+      }
+    }
+    status = __shfl_sync(0xffffffffu, status, 0);
+  }
+  if (status == 0) {
+    // first solve + two refinements
+    for (int it = 0; it < 3; it++) {
+      if (it > 0 && lane < k) {
+        double r = bi;
+#pragma unroll
+        for (int j = 0; j < MAX_JAC; j++)
+          if (j < k) r -= Ai[j] * xs[j];
+        rhs[lane] = (float)r * si;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        for (int i = 0; i < k; i++) {
+          float s = rhs[i];
+          for (int m = 0; m < i; m++) s -= L[i * 7 + m] * sol[m];
+          sol[i] = s / L[i * 7 + i];
+        }
+        for (int i = k - 1; i >= 0; i--) {
+          float s = sol[i];
+          for (int m = i + 1; m < k; m++) s -= L[m * 7 + i] * sol[m];
+          sol[i] = s / L[i * 7 + i];
+        }
+      }
+      __syncwarp();
+      if (lane < k) {
+        const double c = (double)(sol[lane] * si);
+        xs[lane] = (it == 0) ? c : xs[lane] + c;
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      for (int i = 0; i < k; i++) {
+        out[i] = xs[i];
+        if (isnan(out[i])) status = 1;   // multi_fit.c:1857-1863
+      }
+    }
+  }
+  if (lane == 0 && status == 2) status = solve_fp64_lane0(jh, k, lam, out);
+  return status;
+}
+
 // d width / dz factors of the Z model (dao_fit.c:904-916).
 __device__ inline void z_factors(const ModelCfg& cfg, const PeakRec& w, double& gx, double& gy) {
   gx = gy = 0.0;
@@ -660,6 +842,28 @@ __device__ inline void z_factors(const ModelCfg& cfg, const PeakRec& w, double& 
 
 __device__ __forceinline__ long long pix_index(const ModelCfg& cfg, int xi, int yi, int rx, int ry) {
   return (long long)(yi + ry) * cfg.nx + (xi + rx);
+}
+
+// Quantisation of a contribution in the pixel type: FP32 contributions go
+// to one word with float-only instructions (the value v * 2^36 is exact in
+// float, so rounding it to an integer equals acc_quant<1>), FP64 ones to two.
+template <typename T>
+__device__ __forceinline__ Q2 quant_t(T v);
+template <>
+__device__ __forceinline__ Q2 quant_t<float>(float v) {
+  Q2 q;
+  q.h = __float2ll_rn(v * 68719476736.0f);
+  q.l = 0;
+  return q;
+}
+template <>
+__device__ __forceinline__ Q2 quant_t<double>(double v) {
+  return acc_quant<2>(v);
+}
+
+// One-word accumulator value as float (FP32 engine).
+__device__ __forceinline__ float fx_to_float(long long q) {
+  return __ll2float_rn(q) * 1.4551915228366852e-11f;   // 2^-36
 }
 
 // Accumulator access: pixel i of a W-word array (see acc_quant).
@@ -699,8 +903,8 @@ __device__ inline void add_peak(const ModelCfg& cfg, const FrameSet<T>& fs, long
     const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
     const T rq = __ldg(fs.rqe + k), sc = __ldg(fs.scmos + k);
     const T psf = psf_at(cfg, fs.aij, ws, s, rx, ry);
-    acc_red<W>(fs.f, fbase + k, acc_quant<W>((double)contrib_f(w.p[PH], psf, rq)), sign);
-    acc_red<W>(fs.bg, fbase + k, acc_quant<W>((double)contrib_bg(w.p[PBG], rq, sc)), sign);
+    acc_red<W>(fs.f, fbase + k, quant_t<T>(contrib_f(w.p[PH], psf, rq)), sign);
+    acc_red<W>(fs.bg, fbase + k, quant_t<T>(contrib_bg(w.p[PBG], rq, sc)), sign);
     atomicAdd(fs.cnt + fbase + k, sign);
   }
 }

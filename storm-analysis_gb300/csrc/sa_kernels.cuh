@@ -89,12 +89,17 @@ __device__ inline void load_base(const ModelCfg& cfg, const FrameSet<T>& fs, lon
     int rx, ry;
     roi_rc(fs.roi_xy, p, rx, ry);
     const long long k = pix_index(cfg, ax, ay, rx, ry);
-    const double Fg = acc_value<W>(acc_load<W>(fs.f, fbase + k));
-    const double Bg = acc_value<W>(acc_load<W>(fs.bg, fbase + k));
+    const Q2 Fq = acc_load<W>(fs.f, fbase + k);
+    const Q2 Bq = acc_load<W>(fs.bg, fbase + k);
     const int Cg = __ldcg(fs.cnt + fbase + k);
     const T sc = __ldg(fs.scmos + k);
-    ws.Fb[p] = (T)Fg;
-    ws.Bs[p] = (T)(Bg + (double)sc);
+    if constexpr (sizeof(T) == 4) {
+      ws.Fb[p] = fx_to_float(Fq.h);
+      ws.Bs[p] = fx_to_float(Bq.h) + sc;
+    } else {
+      ws.Fb[p] = (T)acc_value<W>(Fq);
+      ws.Bs[p] = (T)(acc_value<W>(Bq) + (double)sc);
+    }
     ws.R[p] = __ldg(fs.rqe + k);
     ws.X[p] = __ldg(fs.x + fbase + k);
     ws.IC[p] = ic_store<T>(Cg + 1);
@@ -107,8 +112,13 @@ enum { ACT_EVAL = 0, ACT_CONTINUE = 1, ACT_BREAK = 2, ACT_BREAK_ADDED = 3, ACT_E
 template <typename T>
 __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase, PeakRec* recp,
                         bool unbounded, WarpWS<T>& ws, int* ctr_out, int lane) {
-  PeakRec orig;
-  load_rec(recp, orig);
+  // The start-of-step, working and trial records live in the warp's shared
+  // workspace; only lane 0 writes them.
+  if (lane < 8) {
+    reinterpret_cast<double2*>(ws.orig)[lane] = __ldcg(reinterpret_cast<const double2*>(recp) + lane);
+  }
+  __syncwarp();
+  const PeakRec& orig = *ws.orig;
   const int k = cfg.jac;
   const int nh = k + k * (k + 1) / 2;
 
@@ -121,6 +131,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
 #pragma unroll
   for (int i = 0; i < 32; i++) acc[i] = (T)0;
   double dev = 0.0;
+  float devf = 0.0f;   // FP32 engine: per-lane partial sum
   bool fail = false;
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
@@ -133,24 +144,30 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     const T rq = __ldg(fs.rqe + kk);
     const T sc = __ldg(fs.scmos + kk);
     const T psf = psf_at(cfg, fs.aij, ws, s0, rx, ry);
-    const double fi0 = acc_value<AccW<T>::W>(Fq) + acc_value<AccW<T>::W>(Bq) / (double)Cg;
+    T t1, t2;
     if constexpr (sizeof(T) == 4) {
-      // keep the start state for the differential trial evaluation
-      const float rho = (float)(fi0 - (double)xv);
+      // FP32 engine, float and integer instructions only.  The residual
+      // rho = f + bg/cnt - x keeps f - x exact by subtracting in fixed point
+      // (x * 2^36 is an exact integer for data >= 2^-12).
+      const long long Xq = __float2ll_rn(xv * 68719476736.0f);
+      const float rho = fx_to_float(Fq.h - Xq) + __fdiv_rn(fx_to_float(Bq.h), (float)Cg);
+      const float f0 = xv + rho;
       ws.psf0[p] = psf;
-      ws.f0[p] = (float)fi0;
+      ws.f0[p] = f0;
       ws.rho[p] = rho;
-      if (!(fi0 > 0.0)) fail = true;
-      else dev += (double)dev_res(rho, xv);
+      if (!(f0 > 0.0f)) fail = true;
+      else devf += dev_res(rho, xv);
+      // t1 = 2(1 - x/f) = 2 rho / f without cancellation, t2 = 2x/f^2
+      t1 = __fdiv_rn(2.0f * rho, f0);
+      t2 = __fdiv_rn(2.0f * xv, f0 * f0);
     } else {
+      const double fi0 = acc_value<AccW<T>::W>(Fq) + acc_value<AccW<T>::W>(Bq) / (double)Cg;
       if (!(fi0 > 0.0)) fail = true;
       else dev += (double)deviance((T)fi0, xv);
+      // the reference's forms (dao_fit.c:454-460)
+      t1 = (T)2 * ((T)1 - xv / (T)fi0);
+      t2 = (T)2 * xv / ((T)fi0 * (T)fi0);
     }
-    const T fiT = (T)fi0;
-    // FP32: t1 = 2(1 - x/f) = 2(f - x)/f from the FP64 residual (no
-    // cancellation); FP64: the reference's form (dao_fit.c:454).
-    const T t1 = (sizeof(T) == 4) ? (T)(2.0 * (fi0 - (double)xv) / fi0) : (T)2 * ((T)1 - xv / fiT);
-    const T t2 = (T)2 * xv / (fiT * fiT);
     T jt[MAX_JAC];
     jt_row(cfg, fs.aij, ws, s0, orig, gx, gy, rx, ry, rq, psf, jt);
     int idx = 0;
@@ -172,31 +189,38 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     }
     (void)idx;
     // subtract this peak (multi_fit.c:1141) and keep the base state
-    const Q2 cf = acc_quant<AccW<T>::W>((double)contrib_f(orig.p[PH], psf, rq));
-    const Q2 cb = acc_quant<AccW<T>::W>((double)contrib_bg(orig.p[PBG], rq, sc));
+    const Q2 cf = quant_t<T>(contrib_f(orig.p[PH], psf, rq));
+    const Q2 cb = quant_t<T>(contrib_bg(orig.p[PBG], rq, sc));
     acc_red<AccW<T>::W>(fs.f, fbase + kk, cf, -1);
     acc_red<AccW<T>::W>(fs.bg, fbase + kk, cb, -1);
     atomicAdd(fs.cnt + fbase + kk, -1);
-    ws.Fb[p] = (T)acc_value<AccW<T>::W>(q_sub(Fq, cf));
-    ws.Bs[p] = (T)(acc_value<AccW<T>::W>(q_sub(Bq, cb)) + (double)sc);
+    if constexpr (sizeof(T) == 4) {
+      ws.Fb[p] = fx_to_float(Fq.h - cf.h);
+      ws.Bs[p] = fx_to_float(Bq.h - cb.h) + sc;
+    } else {
+      ws.Fb[p] = (T)acc_value<AccW<T>::W>(q_sub(Fq, cf));
+      ws.Bs[p] = (T)(acc_value<AccW<T>::W>(q_sub(Bq, cb)) + (double)sc);
+    }
     ws.R[p] = rq;
     ws.X[p] = xv;
     ws.IC[p] = ic_store<T>(Cg);   // (Cg - 1) + 1 once the peak is re-added
   }
-  dev = warp_sum(dev);
+  if constexpr (sizeof(T) == 4) dev = warp_sum_ff(devf);
+  else dev = warp_sum(dev);
   fail = __any_sync(0xffffffffu, fail);
   if constexpr (sizeof(T) == 4) {
     // Per-lane partial sums (a few pixels each) are summed across the warp
-    // in FP64: the cross-lane sums are where the gradient cancels.
+    // in float-float arithmetic: the cross-lane sums are where the gradient
+    // cancels.
     float* red = ws.red;
 #pragma unroll
     for (int i = 0; i < 32; i++)
       if (i < nh) red[lane * 33 + i] = acc[i];
     __syncwarp();
     if (lane < nh) {
-      double s = 0.0;
-      for (int j = 0; j < 32; j++) s += (double)red[j * 33 + lane];
-      ws.jh[lane] = s;
+      float hi = 0.0f, lo = 0.0f;
+      for (int j = 0; j < 32; j++) ff_add(hi, lo, red[j * 33 + lane]);
+      ws.jh[lane] = (double)hi + (double)lo;
     }
   } else {
     T v = warp_transpose_sum32(acc, lane);
@@ -214,12 +238,13 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
   __syncwarp();
 
   // -- 2. LM loop (multi_fit.c:1145-1325); lane 0 holds the scalar state.
-  PeakRec w = orig;
+  PeakRec& w = *ws.w;
   double se = 0.0;
   int ctr[NCOUNTERS];
 #pragma unroll
   for (int i = 0; i < NCOUNTERS; i++) ctr[i] = 0;
   if (lane == 0) {
+    w = orig;
     if (!fail) w.error = dev;
     else ctr[C_STARTFAIL]++;
     se = w.error;
@@ -228,6 +253,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
   bool added_end = false, escaped = false;
   for (;;) {
     int act = ACT_EVAL;
+    // lambda bound and iteration count (multi_fit.c:1153-1171)
     if (lane == 0) {
       if (w.lambda > LAMBDA_MAX) {
         ctr[C_LOST]++;
@@ -237,41 +263,38 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
         w.iterations++;
         ctr[C_ITER]++;
         w.status = RUNNING;
-        double A[MAX_JAC * MAX_JAC], b[MAX_JAC];
-        const double* jh = ws.jh;
-        int id = k;
-        for (int l = 0; l < k; l++) {
-          b[l] = jh[l];
-          for (int m = l; m < k; m++) {
-            A[l * k + m] = (l == m) ? (1.0 + w.lambda) * jh[id] : jh[id];
-            id++;
-          }
-        }
-        if (chol_solve(A, b, k) != 0) {
-          ctr[C_DPOSV]++;
+      }
+    }
+    act = __shfl_sync(0xffffffffu, act, 0);
+    if (act == ACT_BREAK) break;
+    // damped solve (multi_fit.c:1174-1203), warp-collective
+    const double lam = __shfl_sync(0xffffffffu, w.lambda, 0);
+    double b[MAX_JAC];
+    const int info = solve_damped<T>(ws, k, lam, b, lane);
+    if (lane == 0) {
+      if (info != 0) {
+        ctr[C_DPOSV]++;
+        w.status = ERROR;
+        w.lambda = w.lambda * LAMBDA_UP;
+        act = ACT_CONTINUE;
+      } else {
+        PeakRec& t = *ws.t;
+        t = w;
+        apply_update(cfg, t, b);
+        const int c = check_for(cfg, t);
+        if (c) {
+          ctr[c == 1 ? C_MARGIN : C_NEGH]++;
+          w = orig;                      // mFitResetPeak multi_fit.c:1788-1798
+          w.lambda = lam * LAMBDA_UP;
           w.status = ERROR;
-          w.lambda = w.lambda * LAMBDA_UP;
           act = ACT_CONTINUE;
+        } else if (!unbounded && (abs(t.xi - orig.xi) > cfg.dil || abs(t.yi - orig.yi) > cfg.dil)) {
+          act = ACT_ESCAPE;
         } else {
-          PeakRec t = w;
-          apply_update(cfg, t, b);
-          const int c = check_for(cfg, t);
-          if (c) {
-            ctr[c == 1 ? C_MARGIN : C_NEGH]++;
-            const double lam = w.lambda;
-            w = orig;                      // mFitResetPeak multi_fit.c:1788-1798
-            w.lambda = lam * LAMBDA_UP;
-            w.status = ERROR;
-            act = ACT_CONTINUE;
-          } else if (!unbounded && (abs(t.xi - orig.xi) > cfg.dil || abs(t.yi - orig.yi) > cfg.dil)) {
-            act = ACT_ESCAPE;
-          } else {
-            w = t;
-            act = ACT_EVAL;
-          }
+          w = t;
+          act = ACT_EVAL;
         }
       }
-      *ws.w = w;
     }
     act = __shfl_sync(0xffffffffu, act, 0);
     __syncwarp();
@@ -282,7 +305,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
       break;
     }
     // -- trial evaluation: shape, add, error (multi_fit.c:1229-1256)
-    PeakRec wl = *ws.w;
+    const PeakRec& wl = *ws.w;
     SplinePos s = shape_tables(cfg, wl, ws, lane);
     if (wl.xi != cax || wl.yi != cay) {
       __threadfence();
@@ -293,6 +316,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
       cay = wl.yi;
     }
     dev = 0.0;
+    devf = 0.0f;
     fail = false;
     bool is_delta = false;
     const double hh = wl.p[PH], bgv = wl.p[PBG];
@@ -318,7 +342,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
           const float df = rq * fmaf(h1, dpsf, dh * ws.psf0[p]) + dbg * rq * ws.IC[p];
           const float f1 = ws.f0[p] + df;
           if (!(f1 > 0.0f)) fail = true;
-          else dev += (double)dev_delta(df, ws.f0[p], ws.rho[p], ws.X[p]);
+          else devf += dev_delta(df, ws.f0[p], ws.rho[p], ws.X[p]);
         }
       } else {
         for (int p = lane; p < cfg.nroi; p += 32) {
@@ -329,7 +353,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
           const T rq = ws.R[p];
           const T fi = ws.Fb[p] + contrib_f(hh, psf, rq) + bg_div(ws.Bs[p] + bgT * rq, ws.IC[p]);
           if (!(fi > (T)0)) fail = true;
-          else dev += (double)dev_res(fi - ws.X[p], ws.X[p]);
+          else devf += dev_res(fi - ws.X[p], ws.X[p]);
         }
       }
     } else {
@@ -344,7 +368,8 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
         else dev += (double)deviance(fi, ws.X[p]);
       }
     }
-    dev = warp_sum(dev);
+    if constexpr (sizeof(T) == 4) dev = warp_sum_ff(devf);
+    else dev = warp_sum(dev);
     fail = __any_sync(0xffffffffu, fail);
     if (lane == 0) {
       if (fail) {
@@ -393,21 +418,18 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     add_peak(cfg, fs, fbase, orig, so, ws, +1, lane);
     return true;
   }
-  if (lane == 0) {
-    w.added = orig.added - 1 + (added_end ? 1 : 0);
-    *ws.w = w;
-  }
+  if (lane == 0) w.added = orig.added - 1 + (added_end ? 1 : 0);
   __syncwarp();
   if (added_end) {
-    const PeakRec wl = *ws.w;
+    const PeakRec& wl = *ws.w;
     for (int p = lane; p < cfg.nroi; p += 32) {
       int rx, ry;
       roi_rc(fs.roi_xy, p, rx, ry);
       const long long kk = pix_index(cfg, wl.xi, wl.yi, rx, ry);
       const T rq = ws.R[p];
       const T sc = __ldg(fs.scmos + kk);
-      acc_red<AccW<T>::W>(fs.f, fbase + kk, acc_quant<AccW<T>::W>((double)contrib_f(wl.p[PH], ws.psf[p], rq)), +1);
-      acc_red<AccW<T>::W>(fs.bg, fbase + kk, acc_quant<AccW<T>::W>((double)contrib_bg(wl.p[PBG], rq, sc)), +1);
+      acc_red<AccW<T>::W>(fs.f, fbase + kk, quant_t<T>(contrib_f(wl.p[PH], ws.psf[p], rq)), +1);
+      acc_red<AccW<T>::W>(fs.bg, fbase + kk, quant_t<T>(contrib_bg(wl.p[PBG], rq, sc)), +1);
       atomicAdd(fs.cnt + fbase + kk, 1);
     }
   }
@@ -423,7 +445,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
 // ---------------------------------------------------------------------------
 
 template <typename T>
-__global__ void __launch_bounds__(128) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
+__global__ void __launch_bounds__(128, 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
   extern __shared__ __align__(16) char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
