@@ -271,6 +271,7 @@ def run_ours(args, rank, world, local_rank):
     c0 = fit.counters()
     fit.set_timing(True)
     step_resident()
+    per_sweep = fit.sweep_times()
     sweep_ms, sweep_launches, ticks = fit.timing()
     fit.set_timing(False)
     c1 = fit.counters()
@@ -349,7 +350,10 @@ def run_ours(args, rank, world, local_rank):
                      if bound == "fp32" else "nominal FP64",
                      "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
                      "sweep_launches": int(sweep_launches), "sweep_ms_per_step": sweep_ms,
-                     "lm_iterations_per_step": iters, "flops_per_iteration": flops_per_iteration(model, nroi)},
+                     "lm_iterations_per_step": iters, "flops_per_iteration": flops_per_iteration(model, nroi),
+                     "sweep_ms_first5": [round(float(v), 3) for v in per_sweep[:5]],
+                     "sweep_ms_median_after20": float(numpy.median(per_sweep[20:])) if per_sweep.size > 20 else None,
+                     "sweep_ms_sum_after20": float(per_sweep[20:].sum()) if per_sweep.size > 20 else None},
         "fit": {"converged": int((status == 1).sum()), "error": int((status == 2).sum()),
                 "running": int((status == 0).sum()), "sweeps": fit.sweeps,
                 "scheduler": fit.sched_stats()},

@@ -222,6 +222,9 @@ int saSetDevice(int device);
  * enable with saSetTiming(fit, 1); returns total ms and launch count. */
 int saSetTiming(saFitData *fit, int on);
 int saGetTiming(saFitData *fit, double *total_ms, int64_t *launches, int64_t *ticks);
+/* Per-launch sweep kernel times (ms) recorded since saSetTiming(fit, 1);
+ * returns how many were written (at most max_n). */
+int saGetSweepTimes(saFitData *fit, float *out, int max_n);
 /* Number of kernels this handle has launched. */
 int64_t saGetKernelLaunches(saFitData *fit);
 

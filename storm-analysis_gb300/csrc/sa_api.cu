@@ -111,6 +111,7 @@ struct Engine {
   std::vector<cudaEvent_t> pool;
   size_t pool_used = 0;
   double sweep_ms = 0.0;
+  std::vector<float> sweep_times;   // per sweep launch, ms
   long long sweep_launches = 0, ticks = 0;
   long long launches = 0;   // kernels launched by this handle
 
@@ -311,6 +312,7 @@ struct Engine {
       CK(cudaEventElapsedTime(&ms, pool[i], pool[i + 1]));
       sweep_ms += ms;
       sweep_launches++;
+      sweep_times.push_back(ms);
     }
     pool_used = 0;
     return 0;
@@ -1300,6 +1302,7 @@ int saSetTiming(saFitData* h, int on) {
   e->drain_timing();
   e->timing = on != 0;
   e->sweep_ms = 0.0;
+  e->sweep_times.clear();
   e->sweep_launches = 0;
   e->ticks = 0;
   return 0;
@@ -1313,6 +1316,15 @@ int saGetTiming(saFitData* h, double* total_ms, int64_t* launches, int64_t* tick
   *launches = e->sweep_launches;
   *ticks = e->ticks;
   return 0;
+}
+
+int saGetSweepTimes(saFitData* h, float* out, int max_n) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if (e->drain_timing()) return -1;
+  const int n = (int)std::min<size_t>(e->sweep_times.size(), (size_t)max_n);
+  for (int i = 0; i < n; i++) out[i] = e->sweep_times[i];
+  return n;
 }
 
 int64_t saGetKernelLaunches(saFitData* h) {

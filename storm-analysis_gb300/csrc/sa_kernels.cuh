@@ -459,7 +459,8 @@ __global__ void __launch_bounds__(128, 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, 
     FrameCtl* c = fs.ctl + f;
     int r = -1;
     if (lane == 0) {
-      if (*((volatile int*)&c->phase) == PH_IN_SWEEP) {
+      // a plain read first: exhausted frames cost no atomic
+      if (*((volatile int*)&c->phase) == PH_IN_SWEEP && *((volatile int*)&c->grab) < c->nrun) {
         r = atomicAdd(&c->grab, 1);
         if (r >= c->nrun) r = -1;
       }

@@ -141,6 +141,12 @@ class BatchFitter(object):
             self._ok(self.clib.saGetResultsBatch(self.h, vals, ints), "saGetResultsBatch")
         return vals, ints
 
+    def sweep_times(self, max_n=100000):
+        """Per-launch sweep kernel times (ms) recorded while timing was on."""
+        out = numpy.zeros(max_n, dtype=numpy.float32)
+        n = self.clib.saGetSweepTimes(self.h, out, max_n)
+        return out[:max(n, 0)]
+
     def kernel_launches(self):
         return int(self.clib.saGetKernelLaunches(self.h))
 

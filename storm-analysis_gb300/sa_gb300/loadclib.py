@@ -136,6 +136,8 @@ def _declare(lib):
     lib.saGetResultsBatch.restype = ci
     lib.saSetDevice.argtypes = [ci]
     lib.saSetDevice.restype = ci
+    lib.saGetSweepTimes.argtypes = [hp, ndpointer(dtype=numpy.float32, flags="C_CONTIGUOUS"), ci]
+    lib.saGetSweepTimes.restype = ci
 
 
 EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoInitialize3D",
@@ -153,4 +155,4 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "saDoFit", "saGetCounters", "saGetSchedStats", "saSetFrames", "saNewImages",
            "saNewBackgrounds", "saNewPeaksBatch", "saNewPeaksBatchDevice", "saDoFitBatch", "saGetNFitBatch",
            "saGetPeakPropertyBatch", "saGetPeakPropertyIntBatch", "saSetTiming", "saGetTiming",
-           "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice"]
+           "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice", "saGetSweepTimes"]
