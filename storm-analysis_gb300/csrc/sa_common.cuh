@@ -111,6 +111,7 @@ struct FrameSet {
   int F;
   long long npix;
   const T* x;
+  const long long* xq;    // FP32 engine: the data in fixed point (2^-36), exact
   const T* rqe;
   const T* scmos;
   long long* f;

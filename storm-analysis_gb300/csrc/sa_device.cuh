@@ -97,37 +97,175 @@ __device__ __forceinline__ T warp_transpose_sum32(T (&v)[32], int lane) {
 }
 
 // ---------------------------------------------------------------------------
+// float-float ("ff") arithmetic: a value is hi + lo with |lo| <= ulp(hi)/2,
+// about 48 significant bits, from FP32 instructions only (Dekker's and
+// Knuth's error-free transformations; Shewchuk 1997, Hida-Li-Bailey 2001).
+// Every operation is explicitly rounded so the compiler cannot contract or
+// reorder it.
+// ---------------------------------------------------------------------------
+
+struct ff {
+  float h, l;
+};
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return ff{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+// requires |a| >= |b| (or a == 0)
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return ff{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const ff s = two_sum(a.h, b.h);
+  return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
+
+__device__ __forceinline__ ff ff_add_f(ff a, float b) {
+  const ff s = two_sum(a.h, b);
+  return fast_two_sum(s.h, __fadd_rn(s.l, a.l));
+}
+
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+  const float p = __fmul_rn(a.h, b);
+  const float e = __fmaf_rn(a.h, b, -p);
+  return fast_two_sum(p, __fmaf_rn(a.l, b, e));
+}
+
+// a / b: one correction of the FP32 quotient (relative error ~1e-14).
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+  const float inv = __frcp_rn(b.h);
+  const float q1 = __fmul_rn(a.h, inv);
+  const ff r = ff_sub(a, ff_mul_f(b, q1));
+  return fast_two_sum(q1, __fmul_rn(r.h, inv));
+}
+
+__device__ __forceinline__ ff ff_from_double(double d) {
+  const float h = __double2float_rn(d);
+  return ff{h, __double2float_rn(d - (double)h)};
+}
+
+__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.h + (double)a.l; }
+
+// One-word fixed-point value q * 2^-36 as an exact float-float pair.
+__device__ __forceinline__ ff ff_from_fixed(long long q) {
+  const float h = __ll2float_rn(q);
+  const long long r = q - __float2ll_rn(h);
+  return ff{__fmul_rn(h, 1.4551915228366852e-11f), __fmul_rn(__ll2float_rn(r), 1.4551915228366852e-11f)};
+}
+
+// Float-float value rounded to the one-word fixed-point grid (2^-36).
+__device__ __forceinline__ long long fixed_from_ff(ff a) {
+  return __float2ll_rn(__fmul_rn(a.h, 68719476736.0f)) + __float2ll_rn(__fmul_rn(a.l, 68719476736.0f));
+}
+
+__device__ __forceinline__ ff shfl_xor_ff(ff v, int o) {
+  return ff{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+}
+
+// Warp total of a float-float value (every lane gets it: ff_add commutes).
+__device__ __forceinline__ ff warp_sum_ffv(ff v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = ff_add(v, shfl_xor_ff(v, o));
+  return v;
+}
+
+// Reduce 8 float-float values held by every lane: afterwards lane L holds
+// the warp total of value 4*b4 + 2*b3 + b2 (b = bits of L).  9 additions
+// instead of 40.
+__device__ __forceinline__ ff warp_reduce8_ff(ff (&v)[8], int lane) {
+#pragma unroll
+  for (int h = 16, m = 8; h >= 4; h >>= 1, m >>= 1) {
+    const bool up = (lane & h) != 0;
+#pragma unroll
+    for (int i = 0; i < m / 2; i++) {
+      const ff send = up ? v[i] : v[i + m / 2];
+      const ff keep = up ? v[i + m / 2] : v[i];
+      v[i] = ff_add(keep, shfl_xor_ff(send, h));
+    }
+  }
+  v[0] = ff_add(v[0], shfl_xor_ff(v[0], 2));
+  v[0] = ff_add(v[0], shfl_xor_ff(v[0], 1));
+  return v[0];
+}
+__device__ __forceinline__ int reduce8_index(int lane) {
+  return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+}
+
+// warp_transpose_sum32 with float-float additions: lane l gets the warp
+// total of float value l to ~1e-14 (no rounding beyond the inputs').
+__device__ __forceinline__ ff warp_transpose_sum32_ff(float (&v)[32], int lane) {
+  ff w[16];
+  {
+    const bool up = (lane & 16) != 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const float send = up ? v[i] : v[i + 16];
+      const float keep = up ? v[i + 16] : v[i];
+      w[i] = two_sum(keep, __shfl_xor_sync(0xffffffffu, send, 16));
+    }
+  }
+#pragma unroll
+  for (int h = 8; h >= 1; h >>= 1) {
+    const bool up = (lane & h) != 0;
+#pragma unroll
+    for (int i = 0; i < h; i++) {
+      const ff send = up ? w[i] : w[i + h];
+      const ff keep = up ? w[i + h] : w[i];
+      w[i] = ff_add(keep, shfl_xor_ff(send, h));
+    }
+  }
+  return w[0];
+}
+
+// ---------------------------------------------------------------------------
 // FP64 Cholesky solve of the damped normal equations (replaces LAPACK
 // dposv("Lower"), multi_fit.c:1839-1883).  a: k x k, only a[i*k+j] with
 // j >= i is read.  Returns 0 on success; nonzero when not positive definite
-// or the solution has a NaN (multi_fit.c:1857-1863).
+// or the solution has a NaN (multi_fit.c:1857-1863).  Products, differences
+// and divisions are separately rounded, in the unblocked Cholesky order, so
+// ill-conditioned systems (a peak started at height 1) give the LAPACK
+// result to the last bit as often as possible.
 // ---------------------------------------------------------------------------
 
 __device__ inline int chol_solve(const double* a, double* b, int n) {
   double L[MAX_JAC * MAX_JAC];
-  double inv[MAX_JAC];
   for (int j = 0; j < n; j++) {
     double d = a[j * n + j];
-    for (int k = 0; k < j; k++) d = d - L[j * MAX_JAC + k] * L[j * MAX_JAC + k];
+    for (int k = 0; k < j; k++) d = __dsub_rn(d, __dmul_rn(L[j * MAX_JAC + k], L[j * MAX_JAC + k]));
     if (!(d > 0.0)) return j + 1;
     d = sqrt(d);
     L[j * MAX_JAC + j] = d;
-    inv[j] = 1.0 / d;
     for (int i = j + 1; i < n; i++) {
       double s = a[j * n + i];
-      for (int k = 0; k < j; k++) s = s - L[i * MAX_JAC + k] * L[j * MAX_JAC + k];
-      L[i * MAX_JAC + j] = s * inv[j];
+      for (int k = 0; k < j; k++) s = __dsub_rn(s, __dmul_rn(L[i * MAX_JAC + k], L[j * MAX_JAC + k]));
+      L[i * MAX_JAC + j] = s / d;
     }
   }
   for (int i = 0; i < n; i++) {
     double s = b[i];
-    for (int k = 0; k < i; k++) s = s - L[i * MAX_JAC + k] * b[k];
-    b[i] = s * inv[i];
+    for (int k = 0; k < i; k++) s = __dsub_rn(s, __dmul_rn(L[i * MAX_JAC + k], b[k]));
+    b[i] = s / L[i * MAX_JAC + i];
   }
   for (int i = n - 1; i >= 0; i--) {
     double s = b[i];
-    for (int k = i + 1; k < n; k++) s = s - L[k * MAX_JAC + i] * b[k];
-    b[i] = s * inv[i];
+    for (int k = i + 1; k < n; k++) s = __dsub_rn(s, __dmul_rn(L[k * MAX_JAC + i], b[k]));
+    b[i] = s / L[i * MAX_JAC + i];
   }
   for (int i = 0; i < n; i++)
     if (isnan(b[i])) return 1;
@@ -239,6 +377,16 @@ __device__ __forceinline__ T contrib_bg(double bg, T rqe, T scmos) {
 // per-warp workspace in shared memory
 // ---------------------------------------------------------------------------
 
+__host__ __device__ __forceinline__ bool is_spline(int model) { return model >= M_SPLINE2D; }
+
+// The FP32 engine fits the Gaussian models with compensated (float-float)
+// arithmetic on the quantities that decide steps; it has its own, smaller
+// workspace layout.
+template <typename T>
+__host__ __device__ __forceinline__ bool gauss32(const ModelCfg& cfg) {
+  return sizeof(T) == 4 && !is_spline(cfg.model);
+}
+
 template <typename T>
 struct WarpWS {
   T* Fb;      // base fit image (without this peak) at the cached anchor
@@ -259,7 +407,14 @@ struct WarpWS {
   PeakRec* w;     // working record (lane 0 writes)
   PeakRec* orig;  // record at the start of the step
   PeakRec* t;     // trial record (lane 0)
-  float* red; // FP32 only: 32 x 33 per-lane partial sums of the normal equations
+  float* red; // FP32: 32 x 33 per-lane partial sums (splines) / solve scratch
+  // FP32 Gaussian layout
+  float* t1h;   // t1 = 2 (f0 - x) / f0 at the start of the step, float-float
+  float* t1l;
+  float* f0g;   // f0 (float)
+  float* tab0;  // shape tables of the step's start: ex hi, ex lo, ey hi, ey lo, xt, yt
+  float* tab1;  // trial tables (same layout) / pass-1 gradient tables / solve scratch
+  int ts;       // table stride (ROI size rounded up to 32)
 };
 
 template <typename T>
@@ -267,45 +422,75 @@ __host__ __device__ constexpr int ws_pixel_arrays() {
   return sizeof(T) == 4 ? 9 : 6;
 }
 
+__host__ __device__ __forceinline__ int table_stride(int roi) { return (roi + 31) & ~31; }
+
 template <typename T>
-__host__ __device__ inline size_t warp_ws_bytes(int nroi) {
+__host__ __device__ inline size_t warp_ws_bytes(const ModelCfg& cfg, int nroi) {
   size_t n = (size_t)((nroi + 31) / 32) * 32;
-  size_t b = ws_pixel_arrays<T>() * n * sizeof(T);
-  b += 4 * 64 * sizeof(T) * 2;   // ext/eyt/xt/yt (Gaussian) or 4 delta tables (spline)
+  size_t b;
+  if (gauss32<T>(cfg)) {
+    b = 3 * n * sizeof(float) + 14 * (size_t)table_stride(cfg.roi) * sizeof(float);
+  } else {
+    b = ws_pixel_arrays<T>() * n * sizeof(T);
+    b += 4 * 64 * sizeof(T) * 2;   // ext/eyt/xt/yt (Gaussian) or 4 delta tables (spline)
+  }
   b = (b + 15) & ~(size_t)15;
   b += 36 * sizeof(double) + 16 * sizeof(double);
   b += 3 * sizeof(PeakRec);
-  if (sizeof(T) == 4 && nroi > 0) b += 32 * 33 * sizeof(float);
+  if (sizeof(T) == 4 && !gauss32<T>(cfg) && nroi > 0) b += 32 * 33 * sizeof(float);
   return (b + 127) & ~(size_t)127;
 }
 
 template <typename T>
-__device__ inline WarpWS<T> warp_ws(char* base, int nroi) {
+__device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
   WarpWS<T> ws;
   size_t n = (size_t)((nroi + 31) / 32) * 32;
-  T* t = reinterpret_cast<T*>(base);
-  ws.Fb = t;
-  ws.Bs = t + n;
-  ws.R = t + 2 * n;
-  ws.X = t + 3 * n;
-  ws.IC = t + 4 * n;
-  ws.psf = t + 5 * n;
-  ws.psf0 = t + 6 * n;   // only valid when ws_pixel_arrays<T>() == 9
-  ws.f0 = t + 7 * n;
-  ws.rho = t + 8 * n;
-  T* tab = t + ws_pixel_arrays<T>() * n;
-  ws.ext = tab;
-  ws.eyt = tab + 128;
-  ws.xt = tab + 256;
-  ws.yt = tab + 384;
-  size_t off = ws_pixel_arrays<T>() * n * sizeof(T) + 4 * 64 * sizeof(T) * 2;
+  size_t off;
+  if (gauss32<T>(cfg)) {
+    const int ts = table_stride(cfg.roi);
+    float* t = reinterpret_cast<float*>(base);
+    ws.t1h = t;
+    ws.t1l = t + n;
+    ws.f0g = t + 2 * n;
+    ws.tab0 = t + 3 * n;
+    ws.tab1 = ws.tab0 + 6 * ts;
+    ws.ts = ts;
+    // generic views used by the auxiliary kernels (jt_row reads xt / yt)
+    ws.Fb = ws.Bs = ws.R = ws.X = ws.IC = ws.psf = ws.psf0 = ws.f0 = ws.rho = nullptr;
+    ws.ext = reinterpret_cast<T*>(ws.tab0);
+    ws.eyt = reinterpret_cast<T*>(ws.tab0 + 2 * ts);
+    ws.xt = reinterpret_cast<T*>(ws.tab0 + 4 * ts);
+    ws.yt = reinterpret_cast<T*>(ws.tab0 + 5 * ts);
+    ws.red = ws.tab1;
+    off = 3 * n * sizeof(float) + 14 * (size_t)ts * sizeof(float);
+  } else {
+    T* t = reinterpret_cast<T*>(base);
+    ws.Fb = t;
+    ws.Bs = t + n;
+    ws.R = t + 2 * n;
+    ws.X = t + 3 * n;
+    ws.IC = t + 4 * n;
+    ws.psf = t + 5 * n;
+    ws.psf0 = t + 6 * n;   // only valid when ws_pixel_arrays<T>() == 9
+    ws.f0 = t + 7 * n;
+    ws.rho = t + 8 * n;
+    T* tab = t + ws_pixel_arrays<T>() * n;
+    ws.ext = tab;
+    ws.eyt = tab + 128;
+    ws.xt = tab + 256;
+    ws.yt = tab + 384;
+    ws.t1h = ws.t1l = ws.f0g = ws.tab0 = ws.tab1 = nullptr;
+    ws.ts = 0;
+    off = ws_pixel_arrays<T>() * n * sizeof(T) + 4 * 64 * sizeof(T) * 2;
+  }
   off = (off + 15) & ~(size_t)15;
   ws.jh = reinterpret_cast<double*>(base + off);
   ws.scratch = ws.jh + 36;
   ws.w = reinterpret_cast<PeakRec*>(base + off + 52 * sizeof(double));
   ws.orig = ws.w + 1;
   ws.t = ws.w + 2;
-  ws.red = reinterpret_cast<float*>(base + off + 52 * sizeof(double) + 3 * sizeof(PeakRec));
+  if (!gauss32<T>(cfg))
+    ws.red = reinterpret_cast<float*>(base + off + 52 * sizeof(double) + 3 * sizeof(PeakRec));
   return ws;
 }
 
@@ -313,7 +498,42 @@ __device__ inline WarpWS<T> warp_ws(char* base, int nroi) {
 // model pieces (all lanes participate; results in the warp workspace)
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ bool is_spline(int model) { return model >= M_SPLINE2D; }
+// FP32 Gaussian shape tables: per axis the factor exp(-t^2 w) as a
+// float-float pair (evaluated in FP64 once per table entry) and the offset
+// t as a float.  dst layout (stride ts): ex hi, ex lo, ey hi, ey lo, xt, yt.
+__device__ inline void g32_tables(const ModelCfg& cfg, const PeakRec& w, float* dst, int ts, int lane) {
+  const double xo = -(w.p[PX] - (double)w.xi) - cfg.xoff;
+  const double yo = -(w.p[PY] - (double)w.yi) - cfg.xoff;   // dao_fit.c:979 uses xoff
+  const double wx = w.p[PXW], wy = w.p[PYW];
+  for (int i = lane; i < cfg.roi; i += 32) {
+    const double tx = (double)i + xo, ty = (double)i + yo;
+    const ff ex = ff_from_double(exp((-tx * tx) * wx));
+    const ff ey = ff_from_double(exp((-ty * ty) * wy));
+    dst[i] = ex.h;
+    dst[ts + i] = ex.l;
+    dst[2 * ts + i] = ey.h;
+    dst[3 * ts + i] = ey.l;
+    dst[4 * ts + i] = (float)tx;
+    dst[5 * ts + i] = (float)ty;
+  }
+}
+
+__device__ __forceinline__ ff g32_psf(const float* tab, int ts, int rx, int ry) {
+  return ff_mul(ff{tab[rx], tab[ts + rx]}, ff{tab[2 * ts + ry], tab[3 * ts + ry]});
+}
+
+// Fit-image contributions of an FP32 Gaussian peak at one pixel, quantised:
+// f: h * (psf * rqe), bg: bg * rqe + scmos (multi_fit.c:52-54), both
+// float-float.  Every add and subtract of the same record goes through
+// this one function, so they cancel exactly.
+__device__ __forceinline__ void g32_contrib(const float* tab, int ts, ff H, ff BG, int rx, int ry,
+                                            float rq, float sc, Q2& qf, Q2& qb) {
+  const ff ps = ff_mul_f(g32_psf(tab, ts, rx, ry), rq);
+  qf.h = fixed_from_ff(ff_mul(H, ps));
+  qf.l = 0;
+  qb.h = fixed_from_ff(ff_add_f(ff_mul_f(BG, rq), sc));
+  qb.l = 0;
+}
 
 // Gaussian separable factors, daoCalcPeakShape dao_fit.c:968-998.  The y
 // offset uses xoff as the reference does (:979).
@@ -422,7 +642,10 @@ __device__ __forceinline__ T spline_dot(const T* c, const T* tab, int n) {
 template <typename T>
 __device__ __forceinline__ T psf_at(const ModelCfg& cfg, const T* aij, const WarpWS<T>& ws,
                                     const SplinePos& s, int rx, int ry) {
-  if (!is_spline(cfg.model)) return mul_rn(ws.eyt[ry], ws.ext[rx]);
+  if (!is_spline(cfg.model)) {
+    if constexpr (sizeof(T) == 4) return g32_psf(ws.tab0, ws.ts, rx, ry).h;
+    else return mul_rn(ws.eyt[ry], ws.ext[rx]);
+  }
   const int nc = (cfg.model == M_SPLINE3D) ? 64 : 16;
   const T* c = spline_cell(cfg, aij, s.zi, ry + s.ys, rx + s.xs);
   return spline_dot(c, ws.ext, nc);
@@ -530,7 +753,8 @@ __device__ inline SplinePos shape_tables(const ModelCfg& cfg, const PeakRec& w, 
   } else {
     s.xs = s.ys = s.zi = 0;
     s.xd = s.yd = s.zd = 0.0;
-    gauss_tables(cfg, w.p, w.xi, w.yi, ws, lane);
+    if constexpr (sizeof(T) == 4) g32_tables(cfg, w, ws.tab0, ws.ts, lane);
+    else gauss_tables(cfg, w.p, w.xi, w.yi, ws, lane);
   }
   __syncwarp();
   return s;
@@ -897,6 +1121,22 @@ __device__ inline void add_peak(const ModelCfg& cfg, const FrameSet<T>& fs, long
                                 const PeakRec& w, const SplinePos& s, const WarpWS<T>& ws,
                                 int sign, int lane) {
   constexpr int W = AccW<T>::W;
+  if constexpr (sizeof(T) == 4) {
+    if (!is_spline(cfg.model)) {
+      const ff H = ff_from_double(w.p[PH]), BG = ff_from_double(w.p[PBG]);
+      for (int p = lane; p < cfg.nroi; p += 32) {
+        int rx, ry;
+        roi_rc(fs.roi_xy, p, rx, ry);
+        const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
+        Q2 qf, qb;
+        g32_contrib(ws.tab0, ws.ts, H, BG, rx, ry, __ldg(fs.rqe + k), __ldg(fs.scmos + k), qf, qb);
+        acc_red<1>(fs.f, fbase + k, qf, sign);
+        acc_red<1>(fs.bg, fbase + k, qb, sign);
+        atomicAdd(fs.cnt + fbase + k, sign);
+      }
+      return;
+    }
+  }
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
     roi_rc(fs.roi_xy, p, rx, ry);

@@ -1,0 +1,429 @@
+// sa_g32.cuh -- the LM step of one peak in the FP32 engine for the Gaussian
+// models (2dfixed, 2d, 3d, Z); one warp per peak.
+//
+// Precision plan.  The step's Hessian, its FP32 Cholesky factor and the
+// per-pixel model shape are FP32; what decides the step -- the gradient and
+// the change of the MLE error between the start of the step and a trial --
+// is carried in float-float ("ff", ~48 bits) from exact inputs:
+//   * the fit image and a copy of the data are fixed point, so f - x is
+//     exact and becomes an ff residual without rounding;
+//   * the shape factors exp(-t^2 w) are evaluated in FP64 per ROI row and
+//     column (2 * roi exponentials per table) and kept as ff pairs;
+//   * the change of the error for a trial at the same ROI anchor is
+//     summed per pixel as  df * t1 + 2 x (r - log1p r),  t1 = 2 (f0 - x)/f0,
+//     r = df / f0, with df = h1 psf1 - h0 psf0 (+ background change) in ff:
+//     the first-order term, whose pixel sum cancels near convergence, is ff;
+//     the second-order term is positive and FP32.
+// This keeps the accept / reject / converged decisions of the reference
+// (multi_fit.c:1229-1318, evaluated there in FP64) except where they sit
+// within ~1e-12 of a threshold.
+#pragma once
+
+#include "sa_device.cuh"
+
+namespace sa {
+
+enum { ACT_EVAL = 0, ACT_CONTINUE = 1, ACT_BREAK = 2, ACT_BREAK_ADDED = 3, ACT_ESCAPE = 4 };
+
+// Per-axis Jacobian factors of pass 1 in tab1 (ff pairs, stride ts):
+// a1 = 2 h wx t_x, a2 = -h t_x^2 (x gx for Z), b1 = 2 h wy t_y, b2 = -h t_y^2
+// (x gy), so that with ps = rqe * psf the Jacobian row is
+//   2dfixed [ps, ps a1, ps b1, rqe]            (dao_fit.c:48-105)
+//   2d      [ps, ps a1, ps b1, ps (a2+b2), rqe] (:409-467)
+//   3d      [ps, ps a1, ps a2, ps b1, ps b2, rqe] (:811-871)
+//   Z       [ps, ps a1, ps b1, ps (a2+b2), rqe] (:883-958)
+__device__ inline void g32_grad_tables(const ModelCfg& cfg, const PeakRec& w, double gx, double gy,
+                                       float* g, int ts, int lane) {
+  const double h = w.p[PH];
+  const double xo = -(w.p[PX] - (double)w.xi) - cfg.xoff;
+  const double yo = -(w.p[PY] - (double)w.yi) - cfg.xoff;
+  const bool one_width = (cfg.model == M_2DFIXED) || (cfg.model == M_2D);
+  const double wx = w.p[PXW], wy = one_width ? w.p[PXW] : w.p[PYW];
+  for (int i = lane; i < cfg.roi; i += 32) {
+    const double tx = (double)i + xo, ty = (double)i + yo;
+    double a2 = -h * tx * tx, b2 = -h * ty * ty;
+    if (cfg.model == M_Z) {
+      a2 *= gx;
+      b2 *= gy;
+    }
+    ff v = ff_from_double(2.0 * h * wx * tx);
+    g[i] = v.h;
+    g[ts + i] = v.l;
+    v = ff_from_double(a2);
+    g[2 * ts + i] = v.h;
+    g[3 * ts + i] = v.l;
+    v = ff_from_double(2.0 * h * wy * ty);
+    g[4 * ts + i] = v.h;
+    g[5 * ts + i] = v.l;
+    v = ff_from_double(b2);
+    g[6 * ts + i] = v.h;
+    g[7 * ts + i] = v.l;
+  }
+}
+
+struct G32Pix {
+  long long F, B, X;
+  int C;
+  float x, rq;
+};
+
+template <typename T>
+__device__ __forceinline__ void g32_load(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
+                                         int ax, int ay, int p, G32Pix& v) {
+  int rx, ry;
+  roi_rc(fs.roi_xy, p, rx, ry);
+  const long long k = pix_index(cfg, ax, ay, rx, ry);
+  v.F = __ldcg(fs.f + fbase + k);
+  v.B = __ldcg(fs.bg + fbase + k);
+  v.C = __ldcg(fs.cnt + fbase + k);
+  v.X = __ldg(fs.xq + fbase + k);
+  v.x = (float)__ldg(fs.x + fbase + k);
+  v.rq = (float)__ldg(fs.rqe + k);
+}
+
+// Pass 1 over the ROI for model M: start error terms, t1 / f0 per pixel,
+// ff gradient and FP32 Hessian partial sums of this lane.
+template <int M, typename T>
+__device__ inline void g32_pass1(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
+                                 const PeakRec& o, WarpWS<T>& ws, int lane, ff (&g)[8],
+                                 float (&acc)[32], float& devf, bool& fail) {
+  constexpr int K = (M == M_2DFIXED) ? 4 : ((M == M_3D) ? 6 : 5);
+  const int ts = ws.ts;
+  const float* t0 = ws.tab0;
+  const float* gt = ws.tab1;
+  G32Pix cur, nxt;
+  int p = lane;
+  if (p < cfg.nroi) g32_load(cfg, fs, fbase, o.xi, o.yi, p, cur);
+  for (; p < cfg.nroi; p += 32) {
+    // the next pixel's loads are issued before this pixel's stores
+    if (p + 32 < cfg.nroi) g32_load(cfg, fs, fbase, o.xi, o.yi, p + 32, nxt);
+    int rx, ry;
+    roi_rc(fs.roi_xy, p, rx, ry);
+    // f0 = f + bg / cnt and rho = f0 - x, exact up to the division
+    // (multi_fit.c:143); the data are kept in fixed point for this
+    const ff bgc = ff_div(ff_from_fixed(cur.B), ff{(float)cur.C, 0.0f});
+    const ff rho = ff_add(ff_from_fixed(cur.F - cur.X), bgc);
+    const ff f0 = ff_add(ff_from_fixed(cur.F), bgc);
+    if (!(f0.h > 0.0f)) fail = true;
+    else devf += dev_res(rho.h, cur.x);
+    const ff t1 = ff_div(ff{2.0f * rho.h, 2.0f * rho.l}, f0);
+    ws.t1h[p] = t1.h;
+    ws.t1l[p] = t1.l;
+    ws.f0g[p] = f0.h;
+    const float t2 = __fdiv_rn(2.0f * cur.x, f0.h * f0.h);
+    const ff ps = ff_mul_f(g32_psf(t0, ts, rx, ry), cur.rq);
+    const ff u = ff_mul(t1, ps);
+    const ff A1{gt[rx], gt[ts + rx]}, A2{gt[2 * ts + rx], gt[3 * ts + rx]};
+    const ff B1{gt[4 * ts + ry], gt[5 * ts + ry]}, B2{gt[6 * ts + ry], gt[7 * ts + ry]};
+    float jf[K];
+    jf[0] = ps.h;
+    g[0] = ff_add(g[0], u);
+    if constexpr (M == M_3D) {
+      g[1] = ff_add(g[1], ff_mul(u, A1));
+      g[2] = ff_add(g[2], ff_mul(u, A2));
+      g[3] = ff_add(g[3], ff_mul(u, B1));
+      g[4] = ff_add(g[4], ff_mul(u, B2));
+      jf[1] = ps.h * A1.h;
+      jf[2] = ps.h * A2.h;
+      jf[3] = ps.h * B1.h;
+      jf[4] = ps.h * B2.h;
+    } else {
+      g[1] = ff_add(g[1], ff_mul(u, A1));
+      g[2] = ff_add(g[2], ff_mul(u, B1));
+      jf[1] = ps.h * A1.h;
+      jf[2] = ps.h * B1.h;
+      if constexpr (M != M_2DFIXED) {
+        const ff W = ff_add(A2, B2);
+        g[3] = ff_add(g[3], ff_mul(u, W));
+        jf[3] = ps.h * W.h;
+      }
+    }
+    g[K - 1] = ff_add(g[K - 1], ff_mul_f(t1, cur.rq));
+    jf[K - 1] = cur.rq;
+#pragma unroll
+    for (int l = 0; l < K; l++) {
+#pragma unroll
+      for (int m = l; m < K; m++) acc[l * K - (l * (l - 1)) / 2 + (m - l)] += t2 * jf[l] * jf[m];
+    }
+    cur = nxt;
+  }
+}
+
+// Change of the MLE error for a trial at the start anchor (see the header
+// comment); the trial tables are in tab1.  Returns the lane's ff first-order
+// sum in s1 and FP32 second-order sum in s2.
+template <typename T>
+__device__ inline void g32_delta(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
+                                 const PeakRec& o, const PeakRec& t, WarpWS<T>& ws, int lane, ff& s1,
+                                 float& s2, bool& fail) {
+  const int ts = ws.ts;
+  const ff H0 = ff_from_double(o.p[PH]), H1 = ff_from_double(t.p[PH]);
+  const ff DBG = ff_from_double(t.p[PBG] - o.p[PBG]);
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(fs.roi_xy, p, rx, ry);
+    const long long k = pix_index(cfg, o.xi, o.yi, rx, ry);
+    const float xv = (float)__ldg(fs.x + fbase + k);
+    const float rq = (float)__ldg(fs.rqe + k);
+    const int C = __ldcg(fs.cnt + fbase + k);   // without this peak
+    const ff d = ff_mul_f(ff_sub(ff_mul(H1, g32_psf(ws.tab1, ts, rx, ry)), ff_mul(H0, g32_psf(ws.tab0, ts, rx, ry))), rq);
+    const ff bgd = ff_div(ff_mul_f(DBG, rq), ff{(float)(C + 1), 0.0f});
+    const ff df = ff_add(d, bgd);
+    const float f0 = ws.f0g[p];
+    if (!(f0 + df.h > 0.0f)) {
+      fail = true;
+    } else {
+      s1 = ff_add(s1, ff_mul(df, ff{ws.t1h[p], ws.t1l[p]}));
+      s2 += 2.0f * xv * r_minus_log1p(__fdiv_rn(df.h, f0));
+    }
+  }
+}
+
+// MLE error of a trial at another anchor, from the fit image without this
+// peak (FP32 with the exact fixed-point residual).
+template <typename T>
+__device__ inline float g32_absolute(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
+                                     const PeakRec& t, WarpWS<T>& ws, int lane, bool& fail) {
+  const int ts = ws.ts;
+  const float h1 = (float)t.p[PH], bg1 = (float)t.p[PBG];
+  float devf = 0.0f;
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(fs.roi_xy, p, rx, ry);
+    const long long k = pix_index(cfg, t.xi, t.yi, rx, ry);
+    const long long F = __ldcg(fs.f + fbase + k), B = __ldcg(fs.bg + fbase + k);
+    const int C = __ldcg(fs.cnt + fbase + k);
+    const float xv = (float)__ldg(fs.x + fbase + k);
+    const float rq = (float)__ldg(fs.rqe + k), sc = (float)__ldg(fs.scmos + k);
+    const long long Xq = __ldg(fs.xq + fbase + k);
+    const float psf = g32_psf(ws.tab1, ts, rx, ry).h;
+    const float res = fx_to_float(F - Xq) + h1 * psf * rq +
+                      __fdiv_rn(fx_to_float(B) + bg1 * rq + sc, (float)(C + 1));
+    if (!(xv + res > 0.0f)) fail = true;
+    else devf += dev_res(res, xv);
+  }
+  return devf;
+}
+
+// Returns true if the step escaped its footprint (nothing changed).
+template <typename T>
+__device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase, PeakRec* recp,
+                            bool unbounded, WarpWS<T>& ws, int* ctr_out, int lane) {
+  if constexpr (sizeof(T) != 4) {
+    return false;
+  } else {
+    if (lane < 8) {
+      reinterpret_cast<double2*>(ws.orig)[lane] = __ldcg(reinterpret_cast<const double2*>(recp) + lane);
+    }
+    __syncwarp();
+    const PeakRec& orig = *ws.orig;
+    const int k = cfg.jac;
+    const int nhes = k * (k + 1) / 2;
+    const int ts = ws.ts;
+
+    // -- 1. starting error, gradient / Hessian, subtract (multi_fit.c:1107-1142)
+    g32_tables(cfg, orig, ws.tab0, ts, lane);
+    double gxd, gyd;
+    z_factors(cfg, orig, gxd, gyd);
+    g32_grad_tables(cfg, orig, gxd, gyd, ws.tab1, ts, lane);
+    __syncwarp();
+    ff g[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) g[i] = ff{0.0f, 0.0f};
+    float acc[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++) acc[i] = 0.0f;
+    float devf = 0.0f;
+    bool fail = false;
+    switch (cfg.model) {
+      case M_2DFIXED: g32_pass1<M_2DFIXED>(cfg, fs, fbase, orig, ws, lane, g, acc, devf, fail); break;
+      case M_2D: g32_pass1<M_2D>(cfg, fs, fbase, orig, ws, lane, g, acc, devf, fail); break;
+      case M_3D: g32_pass1<M_3D>(cfg, fs, fbase, orig, ws, lane, g, acc, devf, fail); break;
+      default: g32_pass1<M_Z>(cfg, fs, fbase, orig, ws, lane, g, acc, devf, fail); break;
+    }
+    // subtract this peak (multi_fit.c:1141)
+    const ff H0 = ff_from_double(orig.p[PH]), BG0 = ff_from_double(orig.p[PBG]);
+    for (int p = lane; p < cfg.nroi; p += 32) {
+      int rx, ry;
+      roi_rc(fs.roi_xy, p, rx, ry);
+      const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
+      Q2 qf, qb;
+      g32_contrib(ws.tab0, ts, H0, BG0, rx, ry, (float)__ldg(fs.rqe + kk), (float)__ldg(fs.scmos + kk), qf, qb);
+      acc_red<1>(fs.f, fbase + kk, qf, -1);
+      acc_red<1>(fs.bg, fbase + kk, qb, -1);
+      atomicAdd(fs.cnt + fbase + kk, -1);
+    }
+    const double dev0 = warp_sum_ff(devf);
+    fail = __any_sync(0xffffffffu, fail);
+    {
+      const ff hv = warp_transpose_sum32_ff(acc, lane);
+      if (lane < nhes) ws.jh[k + lane] = ff_to_double(hv);
+      const ff gv = warp_reduce8_ff(g, lane);
+      const int gi = reduce8_index(lane);
+      if ((lane & 3) == 0 && gi < k) ws.jh[gi] = ff_to_double(gv);
+    }
+    __syncwarp();
+
+    // -- 2. LM loop (multi_fit.c:1145-1325); lane 0 holds the scalar state.
+    PeakRec& w = *ws.w;
+    double se = 0.0;
+    int ctr[NCOUNTERS];
+#pragma unroll
+    for (int i = 0; i < NCOUNTERS; i++) ctr[i] = 0;
+    if (lane == 0) {
+      w = orig;
+      if (!fail) w.error = dev0;
+      else ctr[C_STARTFAIL]++;
+      se = w.error;
+    }
+    bool added_end = false, escaped = false;
+    for (;;) {
+      int act = ACT_EVAL;
+      // lambda bound and iteration count (multi_fit.c:1153-1171)
+      if (lane == 0) {
+        if (w.lambda > LAMBDA_MAX) {
+          ctr[C_LOST]++;
+          w.status = ERROR;
+          act = ACT_BREAK;
+        } else {
+          w.iterations++;
+          ctr[C_ITER]++;
+          w.status = RUNNING;
+        }
+      }
+      act = __shfl_sync(0xffffffffu, act, 0);
+      if (act == ACT_BREAK) break;
+      // damped solve (multi_fit.c:1174-1203), warp-collective
+      const double lam = __shfl_sync(0xffffffffu, w.lambda, 0);
+      double b[MAX_JAC];
+      const int info = solve_damped<T>(ws, k, lam, b, lane);
+      if (lane == 0) {
+        if (info != 0) {
+          ctr[C_DPOSV]++;
+          w.status = ERROR;
+          w.lambda = w.lambda * LAMBDA_UP;
+          act = ACT_CONTINUE;
+        } else {
+          PeakRec& t = *ws.t;
+          t = w;
+          apply_update(cfg, t, b);
+          const int c = check_for(cfg, t);
+          if (c) {
+            ctr[c == 1 ? C_MARGIN : C_NEGH]++;
+            w = orig;                      // mFitResetPeak multi_fit.c:1788-1798
+            w.lambda = lam * LAMBDA_UP;
+            w.status = ERROR;
+            act = ACT_CONTINUE;
+          } else if (!unbounded && (abs(t.xi - orig.xi) > cfg.dil || abs(t.yi - orig.yi) > cfg.dil)) {
+            act = ACT_ESCAPE;
+          } else {
+            w = t;
+            act = ACT_EVAL;
+          }
+        }
+      }
+      act = __shfl_sync(0xffffffffu, act, 0);
+      __syncwarp();
+      if (act == ACT_CONTINUE) continue;
+      if (act == ACT_BREAK) break;
+      if (act == ACT_ESCAPE) {
+        escaped = true;
+        break;
+      }
+      // -- trial evaluation: shape, add, error (multi_fit.c:1229-1256)
+      const PeakRec& wl = *ws.w;
+      g32_tables(cfg, wl, ws.tab1, ts, lane);
+      __syncwarp();
+      const bool is_delta = (wl.xi == orig.xi) && (wl.yi == orig.yi);
+      double dev;
+      fail = false;
+      if (is_delta) {
+        ff s1{0.0f, 0.0f};
+        float s2 = 0.0f;
+        g32_delta(cfg, fs, fbase, orig, wl, ws, lane, s1, s2, fail);
+        dev = ff_to_double(warp_sum_ffv(s1)) + warp_sum_ff(s2);
+      } else {
+        __threadfence();
+        __syncwarp();
+        dev = warp_sum_ff(g32_absolute(cfg, fs, fbase, wl, ws, lane, fail));
+      }
+      fail = __any_sync(0xffffffffu, fail);
+      if (lane == 0) {
+        if (fail) {
+          ctr[C_NEGFI]++;
+          const double lm = w.lambda;
+          w = orig;
+          w.lambda = lm * LAMBDA_UP;
+          w.status = ERROR;
+          act = ACT_CONTINUE;
+        } else {
+          w.error = is_delta ? se + dev : dev;
+          const double change = is_delta ? dev : w.error - se;
+          if (change > 0.0) {
+            if ((change / se) < cfg.tol) {
+              w.status = CONVERGED;
+              act = ACT_BREAK_ADDED;
+            } else {
+              ctr[C_NONDECR]++;
+              const double lm = w.lambda;
+              w = orig;
+              w.lambda = lm * LAMBDA_UP;
+              act = ACT_CONTINUE;
+            }
+          } else {
+            if ((-change / se) < cfg.tol) {
+              w.status = CONVERGED;
+            } else if (w.lambda > LAMBDA_MIN) {
+              w.lambda = LAMBDA_DOWN * w.lambda;
+            }
+            act = ACT_BREAK_ADDED;
+          }
+        }
+      }
+      act = __shfl_sync(0xffffffffu, act, 0);
+      if (act == ACT_BREAK_ADDED) {
+        added_end = true;
+        break;
+      }
+    }
+
+    // -- 3. write back
+    if (escaped) {
+      // restore the start-of-step contribution; the record is untouched
+      for (int p = lane; p < cfg.nroi; p += 32) {
+        int rx, ry;
+        roi_rc(fs.roi_xy, p, rx, ry);
+        const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
+        Q2 qf, qb;
+        g32_contrib(ws.tab0, ts, H0, BG0, rx, ry, (float)__ldg(fs.rqe + kk), (float)__ldg(fs.scmos + kk), qf, qb);
+        acc_red<1>(fs.f, fbase + kk, qf, +1);
+        acc_red<1>(fs.bg, fbase + kk, qb, +1);
+        atomicAdd(fs.cnt + fbase + kk, 1);
+      }
+      return true;
+    }
+    if (lane == 0) w.added = orig.added - 1 + (added_end ? 1 : 0);
+    __syncwarp();
+    if (added_end) {
+      const PeakRec& wl = *ws.w;
+      const ff H1 = ff_from_double(wl.p[PH]), BG1 = ff_from_double(wl.p[PBG]);
+      for (int p = lane; p < cfg.nroi; p += 32) {
+        int rx, ry;
+        roi_rc(fs.roi_xy, p, rx, ry);
+        const long long kk = pix_index(cfg, wl.xi, wl.yi, rx, ry);
+        Q2 qf, qb;
+        g32_contrib(ws.tab1, ts, H1, BG1, rx, ry, (float)__ldg(fs.rqe + kk), (float)__ldg(fs.scmos + kk), qf, qb);
+        acc_red<1>(fs.f, fbase + kk, qf, +1);
+        acc_red<1>(fs.bg, fbase + kk, qb, +1);
+        atomicAdd(fs.cnt + fbase + kk, 1);
+      }
+    }
+    if (lane == 0) {
+      *recp = w;
+      for (int i = 0; i < NCOUNTERS; i++) ctr_out[i] = ctr[i];
+    }
+    return false;
+  }
+}
+
+}  // namespace sa

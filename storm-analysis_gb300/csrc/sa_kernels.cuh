@@ -16,7 +16,7 @@
 //               needs another sweep (dao_fit_c.py:332-356).
 #pragma once
 
-#include "sa_device.cuh"
+#include "sa_g32.cuh"
 
 namespace sa {
 
@@ -106,7 +106,6 @@ __device__ inline void load_base(const ModelCfg& cfg, const FrameSet<T>& fs, lon
   }
 }
 
-enum { ACT_EVAL = 0, ACT_CONTINUE = 1, ACT_BREAK = 2, ACT_BREAK_ADDED = 3, ACT_ESCAPE = 4 };
 
 // Returns true if the step escaped its footprint (nothing changed).
 template <typename T>
@@ -444,13 +443,14 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
 // k_sweep: persistent warps over the run ranks of all frames in IN_SWEEP
 // ---------------------------------------------------------------------------
 
-template <typename T>
+// G32: the FP32 Gaussian step (lm_step_g32); otherwise lm_step.
+template <typename T, bool G32>
 __global__ void __launch_bounds__(128, 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
   extern __shared__ __align__(16) char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
-  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(cfg.nroi), cfg.nroi);
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(cfg, cfg.nroi), cfg, cfg.nroi);
   const int gwarp = blockIdx.x * wpb + wib;
   const int fp = 2 * cfg.roi + 2 * cfg.dil;   // overlap span of two dilated footprints
   int f = gwarp % fs.F;
@@ -527,8 +527,11 @@ __global__ void __launch_bounds__(128, 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, 
     __threadfence();
     // -- the step
     const int li = fs.run[base + r];
-    const bool esc = lm_step(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, ws,
-                             fs.stepctr + (size_t)(base + li) * NCOUNTERS, lane);
+    const bool esc =
+        G32 ? lm_step_g32(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, ws,
+                          fs.stepctr + (size_t)(base + li) * NCOUNTERS, lane)
+            : lm_step(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, ws,
+                      fs.stepctr + (size_t)(base + li) * NCOUNTERS, lane);
     if (esc && lane == 0) {
       atomicMin(&c->escaped_min, r);
       int slot = atomicAdd(&c->n_escaped, 1);
@@ -645,7 +648,7 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
     __syncthreads();
     // roll back run ranks > b: remove the current contribution, restore the snapshot
     const int lane = tid & 31, wid = tid >> 5;
-    WarpWS<T> ws = warp_ws<T>(smem + (size_t)wid * warp_ws_bytes<T>(0), 0);
+    WarpWS<T> ws = warp_ws<T>(smem + (size_t)wid * warp_ws_bytes<T>(cfg, 0), cfg, 0);
     const long long fbase = (long long)f * fs.npix;
     for (int r = b + 1 + wid; r < nrun; r += 32) {
       const int li = fs.run[base + r];
@@ -703,7 +706,7 @@ __global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
   const int base = fs.pk_off[f];
   const int nrun = c->nrun;
   const int lane = tid & 31, wid = tid >> 5;
-  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wid * warp_ws_bytes<T>(0), 0);
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wid * warp_ws_bytes<T>(cfg, 0), cfg, 0);
   const long long fbase = (long long)f * fs.npix;
   // recenter (mFitRecenterPeaks multi_fit.c:1644-1690); order-free with
   // fixed-point accumulation
@@ -780,6 +783,7 @@ __global__ void k_new_image(FrameSet<T> fs, const I* img, int frame0, int nframe
     const long long g = (long long)frame0 * fs.npix + i;
     const double v = (double)img[i] * (double)fs.rqe[k] + (double)fs.scmos[k];
     const_cast<T*>(fs.x)[g] = (T)v;
+    if (fs.xq) const_cast<long long*>(fs.xq)[g] = __double2ll_rn(v * 68719476736.0);
     for (int w = 0; w < AccW<T>::W; w++) {
       fs.f[g * AccW<T>::W + w] = 0;
       fs.bg[g * AccW<T>::W + w] = 0;
@@ -854,7 +858,7 @@ __global__ void k_newpeaks(ModelCfg cfg, FrameSet<T> fs, const double* rows, int
                            const int* slots, const int* frames, int n, int do_add) {
   extern __shared__ __align__(16) char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(0), 0);
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(cfg, 0), cfg, 0);
   const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
   const int nw = gridDim.x * (blockDim.x >> 5);
   for (int i = gw; i < n; i += nw) {
@@ -900,7 +904,7 @@ __global__ void k_newpeaks_finder(ModelCfg cfg, FrameSet<T> fs, const int* slots
                                   const int* frame_n, int nframes) {
   extern __shared__ __align__(16) char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(0), 0);
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(cfg, 0), cfg, 0);
   const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
   if (gw >= nframes) return;
   const int i0 = frame_first[gw], n = frame_n[gw];
@@ -983,7 +987,7 @@ __global__ void k_peak_props(ModelCfg cfg, FrameSet<T> fs, const int* slots, con
                              double* out_sum, double* out_fg, double* out_bg, double* out_jac) {
   extern __shared__ __align__(16) char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(0), 0);
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(cfg, 0), cfg, 0);
   const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
   const int nw = gridDim.x * (blockDim.x >> 5);
   for (int i = gw; i < n; i += nw) {
@@ -1049,7 +1053,7 @@ __global__ void k_set_status(ModelCfg cfg, FrameSet<T> fs, const int* slots, con
                              const int* status, int n) {
   extern __shared__ __align__(16) char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(0), 0);
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(cfg, 0), cfg, 0);
   const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
   const int nw = gridDim.x * (blockDim.x >> 5);
   for (int i = gw; i < n; i += nw) {

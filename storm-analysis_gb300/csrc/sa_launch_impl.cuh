@@ -20,21 +20,24 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
   int nsm = 0, max_smem = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t ws = warp_ws_bytes<T>(cfg.nroi);
+  const size_t ws = warp_ws_bytes<T>(cfg, cfg.nroi);
   const size_t s_sweep = ws * (SWEEP_BLOCK / 32);
-  const size_t ws0 = warp_ws_bytes<T>(0);
+  const size_t ws0 = warp_ws_bytes<T>(cfg, 0);
   const size_t grid_bytes = (size_t)(cfg.gx * cfg.gy + 1) * sizeof(int);
   const size_t s_cta = ws0 * (CTA_BLOCK / 32) > grid_bytes ? ws0 * (CTA_BLOCK / 32) : grid_bytes;
   const size_t s_aux = ws0 * (AUX_BLOCK / 32);
   if (s_sweep > (size_t)max_smem || s_cta > (size_t)max_smem) return cudaErrorInvalidConfiguration;
-  e = cudaFuncSetAttribute(k_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s_sweep);
+  const bool g32 = gauss32<T>(cfg);
+  e = cudaFuncSetAttribute(g32 ? k_sweep<T, true> : k_sweep<T, false>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s_sweep);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_prepare<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s_cta);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_post<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s_cta);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<T>, SWEEP_BLOCK, s_sweep);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g32 ? k_sweep<T, true> : k_sweep<T, false>,
+                                                    SWEEP_BLOCK, s_sweep);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   *sweep_grid = nsm * per_sm;
@@ -53,7 +56,8 @@ cudaError_t Launch<T>::prepare(const ModelCfg& cfg, const FrameSet<T>& fs, size_
 template <typename T>
 cudaError_t Launch<T>::sweep(const ModelCfg& cfg, const FrameSet<T>& fs, int epoch, int grid,
                              size_t smem, cudaStream_t s) {
-  k_sweep<T><<<grid, SWEEP_BLOCK, smem, s>>>(cfg, fs, epoch);
+  if (gauss32<T>(cfg)) k_sweep<T, true><<<grid, SWEEP_BLOCK, smem, s>>>(cfg, fs, epoch);
+  else k_sweep<T, false><<<grid, SWEEP_BLOCK, smem, s>>>(cfg, fs, epoch);
   return cudaGetLastError();
 }
 
