@@ -37,10 +37,16 @@ void set_error(const char* fmt, ...) {
     }                                                                         \
   } while (0)
 
+// Spline handle.  Its fields have the layout of the reference's splineData
+// (spliner/cubic_spline.h:16-26): cfInitialize reads type, sizes and aij,
+// so it accepts a spline made by this library's initSpline2D/3D or by the
+// reference's libcubic_spline.  splineCleanup frees every array the struct
+// points to, whichever library allocated it (both use malloc).
 struct SplineH {
-  int type;  // 0: 2D, 1: 3D
+  int type;  // 0: 2D, 1: 3D (S2D / S3D)
   int xs, ys, zs;
-  std::vector<double> aij;
+  double* aij;
+  double* reserved[4];   // the reference's delta tables; unused here
 };
 
 template <typename P>
@@ -848,27 +854,37 @@ void daoCleanup(saFitData* h) {
   free(h);
 }
 
-void* initSpline2D(double* aij, int xs, int ys) {
-  SplineH* s = new SplineH();
-  s->type = 0;
-  s->xs = xs;
-  s->ys = ys;
-  s->zs = 0;
-  s->aij.assign(aij, aij + (size_t)xs * ys * 16);
-  return s;
-}
-
-void* initSpline3D(double* aij, int xs, int ys, int zs) {
-  SplineH* s = new SplineH();
-  s->type = 1;
+static void* new_spline(int type, const double* aij, int xs, int ys, int zs, size_t n) {
+  SplineH* s = static_cast<SplineH*>(calloc(1, sizeof(SplineH)));
+  if (!s) return nullptr;
+  s->aij = static_cast<double*>(malloc(sizeof(double) * (n > 0 ? n : 1)));
+  if (!s->aij) {
+    free(s);
+    return nullptr;
+  }
+  if (n) memcpy(s->aij, aij, sizeof(double) * n);
+  s->type = type;
   s->xs = xs;
   s->ys = ys;
   s->zs = zs;
-  s->aij.assign(aij, aij + (size_t)xs * ys * zs * 64);
   return s;
 }
 
-void splineCleanup(void* sp) { delete reinterpret_cast<SplineH*>(sp); }
+void* initSpline2D(double* aij, int xs, int ys) {
+  return new_spline(0, aij, xs, ys, 0, (size_t)xs * ys * 16);
+}
+
+void* initSpline3D(double* aij, int xs, int ys, int zs) {
+  return new_spline(1, aij, xs, ys, zs, (size_t)xs * ys * zs * 64);
+}
+
+void splineCleanup(void* sp) {
+  SplineH* s = reinterpret_cast<SplineH*>(sp);
+  if (!s) return;
+  free(s->aij);
+  for (double* r : s->reserved) free(r);
+  free(s);
+}
 int getXSize(void* sp) { return sp ? reinterpret_cast<SplineH*>(sp)->xs : 0; }
 int getYSize(void* sp) { return sp ? reinterpret_cast<SplineH*>(sp)->ys : 0; }
 int getZSize(void* sp) { return sp ? reinterpret_cast<SplineH*>(sp)->zs : 0; }
@@ -896,7 +912,8 @@ saFitData* cfInitialize(void* spline, double* rqe, double* scmos, double tol, in
   e->cfg.sx = s->xs;
   e->cfg.sy = s->ys;
   e->cfg.sz = s->zs;
-  e->aij_h = s->aij;
+  const size_t ncoef = (size_t)s->xs * s->ys * (s->type == 1 ? (size_t)s->zs * 64 : 16);
+  e->aij_h.assign(s->aij, s->aij + ncoef);
   // cubic_fit.c:627-641
   if ((sx % 2) == 1) {
     e->cfg.xoff = (double)(sx / 2) - 0.5;
@@ -936,7 +953,7 @@ void cfCleanup(saFitData* h) {
   if (!h) return;
   Engine* e = E(h);
   if (e && e->spline) {
-    delete e->spline;
+    splineCleanup(e->spline);   // cubic_fit.c:528-530
     e->spline = nullptr;
   }
   daoCleanup(h);

@@ -106,3 +106,32 @@ def test_synthetic_workloads_shapes():
     assert set(g) >= {"x", "y", "z", "background", "height", "xsigma", "ysigma"}
     wl3 = synth.make_workload(3, frames=1, nx=64, ny=64, n_emitters=5)
     assert wl3["spline"]["coeff"].shape == (20, 20, 20, 64)
+
+
+def test_spline_handle_from_reference_library(lib):
+    """cfInitialize accepts a spline made by the reference's own
+    initSpline3D (spliner/cubic_spline.c:749, splineData layout
+    cubic_spline.h:16-26), as the reference's cubic_spline_c.py would pass
+    it after a library swap, and cfCleanup frees it."""
+    import ctypes
+    import os
+    ref = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref",
+                       "libcubic_fit.so")
+    if not os.path.exists(ref):
+        pytest.skip("the reference's compiled C is not present")
+    rlib = ctypes.CDLL(ref)
+    f64 = numpy.ctypeslib.ndpointer(dtype=numpy.float64, flags="C_CONTIGUOUS")
+    rlib.initSpline3D.argtypes = [f64, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    rlib.initSpline3D.restype = ctypes.c_void_p
+    coeff = numpy.random.default_rng(3).uniform(0, 1, 9 * 9 * 9 * 64)
+    img = numpy.ones((40, 40))
+    geo = []
+    for make in (rlib.initSpline3D, lib.initSpline3D):
+        sp = make(coeff, 9, 9, 9)
+        h = lib.cfInitialize(sp, img, img * 0, 1e-6, 40, 40)
+        assert h, "cfInitialize refused the spline"
+        lib.cfInitialize3D(h)
+        c = h.contents
+        geo.append((c.roi_n_index, c.fit_size_x, c.jac_size, c.xoff))
+        lib.cfCleanup(h)
+    assert geo[0] == geo[1] and geo[0][1] == 8 and geo[0][2] == 5
