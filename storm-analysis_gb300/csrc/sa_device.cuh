@@ -174,6 +174,40 @@ __device__ __forceinline__ long long fixed_from_ff(ff a) {
   return __float2ll_rn(__fmul_rn(a.h, 68719476736.0f)) + __float2ll_rn(__fmul_rn(a.l, 68719476736.0f));
 }
 
+__device__ __forceinline__ ff two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return ff{p, __fmaf_rn(a, b, -p)};
+}
+
+// exp(a) of a float-float a in [-87, 40], in FP32 instructions: Cody-Waite
+// reduction a = k ln2 + r (ln2 split in three parts, the first with 16
+// significant bits so that k * part1 is exact), the Taylor series of
+// exp(r / 32) to degree 6 in Horner form, five squarings, and the exact
+// scaling by 2^k.  Relative error <= 2.7e-13 for a in [-60, 0] (checked
+// against 60-digit arithmetic and against FP64 exp on the GPU); a < -87
+// (or NaN) returns 0; a > 40 is taken as 40.
+__device__ __forceinline__ ff ff_exp(ff a) {
+  if (!(a.h >= -87.0f)) return ff{0.0f, 0.0f};
+  if (a.h > 40.0f) a = ff{40.0f, 0.0f};
+  const float k = rintf(a.h * 1.44269504088896341f);
+  ff r = ff_add_f(a, -k * 0.693145751953125f);
+  const ff kc = two_prod(k, 1.428606765330187e-06f);
+  r = ff_sub(r, kc);
+  r = ff_add_f(r, -k * 5.497923148104107e-14f);
+  const ff s{r.h * 0.03125f, r.l * 0.03125f};
+  ff e{1.3888889225199819e-03f, -3.3631094437103215e-11f};                          // 1/6!
+  e = ff_add(ff_mul(e, s), ff{8.333333767950535e-03f, -4.34617203337595e-10f});     // 1/5!
+  e = ff_add(ff_mul(e, s), ff{4.16666679084301e-02f, -1.2417634698280722e-09f});    // 1/4!
+  e = ff_add(ff_mul(e, s), ff{0.1666666716337204f, -4.967053879312289e-09f});       // 1/3!
+  e = ff_add(ff_mul(e, s), ff{0.5f, 0.0f});
+  e = ff_add(ff_mul(e, s), ff{1.0f, 0.0f});
+  e = ff_add(ff_mul(e, s), ff{1.0f, 0.0f});
+#pragma unroll
+  for (int i = 0; i < 5; i++) e = ff_mul(e, e);
+  const float scale = __int_as_float(((int)k + 127) << 23);   // 2^k, k in [-126, 58]
+  return ff{e.h * scale, e.l * scale};
+}
+
 __device__ __forceinline__ ff shfl_xor_ff(ff v, int o) {
   return ff{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
 }
@@ -412,6 +446,9 @@ struct WarpWS {
   float* t1h;   // t1 = 2 (f0 - x) / f0 at the start of the step, float-float
   float* t1l;
   float* f0g;   // f0 (float)
+  float* Xs;    // data, rqe and peak count (with this peak) at the start anchor
+  float* Rs;
+  float* Cs;
   float* tab0;  // shape tables of the step's start: ex hi, ex lo, ey hi, ey lo, xt, yt
   float* tab1;  // trial tables (same layout) / pass-1 gradient tables / solve scratch
   int ts;       // table stride (ROI size rounded up to 32)
@@ -429,7 +466,7 @@ __host__ __device__ inline size_t warp_ws_bytes(const ModelCfg& cfg, int nroi) {
   size_t n = (size_t)((nroi + 31) / 32) * 32;
   size_t b;
   if (gauss32<T>(cfg)) {
-    b = 3 * n * sizeof(float) + 14 * (size_t)table_stride(cfg.roi) * sizeof(float);
+    b = 6 * n * sizeof(float) + 14 * (size_t)table_stride(cfg.roi) * sizeof(float);
   } else {
     b = ws_pixel_arrays<T>() * n * sizeof(T);
     b += 4 * 64 * sizeof(T) * 2;   // ext/eyt/xt/yt (Gaussian) or 4 delta tables (spline)
@@ -452,7 +489,10 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
     ws.t1h = t;
     ws.t1l = t + n;
     ws.f0g = t + 2 * n;
-    ws.tab0 = t + 3 * n;
+    ws.Xs = t + 3 * n;
+    ws.Rs = t + 4 * n;
+    ws.Cs = t + 5 * n;
+    ws.tab0 = t + 6 * n;
     ws.tab1 = ws.tab0 + 6 * ts;
     ws.ts = ts;
     // generic views used by the auxiliary kernels (jt_row reads xt / yt)
@@ -462,7 +502,7 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
     ws.xt = reinterpret_cast<T*>(ws.tab0 + 4 * ts);
     ws.yt = reinterpret_cast<T*>(ws.tab0 + 5 * ts);
     ws.red = ws.tab1;
-    off = 3 * n * sizeof(float) + 14 * (size_t)ts * sizeof(float);
+    off = 6 * n * sizeof(float) + 14 * (size_t)ts * sizeof(float);
   } else {
     T* t = reinterpret_cast<T*>(base);
     ws.Fb = t;
@@ -479,7 +519,7 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
     ws.eyt = tab + 128;
     ws.xt = tab + 256;
     ws.yt = tab + 384;
-    ws.t1h = ws.t1l = ws.f0g = ws.tab0 = ws.tab1 = nullptr;
+    ws.t1h = ws.t1l = ws.f0g = ws.Xs = ws.Rs = ws.Cs = ws.tab0 = ws.tab1 = nullptr;
     ws.ts = 0;
     off = ws_pixel_arrays<T>() * n * sizeof(T) + 4 * 64 * sizeof(T) * 2;
   }
@@ -498,23 +538,44 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
 // model pieces (all lanes participate; results in the warp workspace)
 // ---------------------------------------------------------------------------
 
+// Offsets of the first ROI column / row from the peak centre
+// (daoCalcPeakShape dao_fit.c:968-998; the y offset uses xoff, :979) and
+// the widths, as float-float values (a few FP64 instructions per table).
+struct G32Axes {
+  ff xo, yo, wx, wy;
+};
+__device__ __forceinline__ G32Axes g32_axes(const ModelCfg& cfg, const PeakRec& w) {
+  G32Axes a;
+  a.xo = ff_from_double(-(w.p[PX] - (double)w.xi) - cfg.xoff);
+  a.yo = ff_from_double(-(w.p[PY] - (double)w.yi) - cfg.xoff);
+  a.wx = ff_from_double(w.p[PXW]);
+  a.wy = ff_from_double(w.p[PYW]);
+  return a;
+}
+
 // FP32 Gaussian shape tables: per axis the factor exp(-t^2 w) as a
-// float-float pair (evaluated in FP64 once per table entry) and the offset
-// t as a float.  dst layout (stride ts): ex hi, ex lo, ey hi, ey lo, xt, yt.
+// float-float pair and the offset t as a float, all in FP32 instructions.
+// dst layout (stride ts): ex hi, ex lo, ey hi, ey lo, xt, yt.
+// A width can be negative: the '2d' model clamps XWIDTH only and copies the
+// unclamped value to YWIDTH (dao_fit.c:1061-1085, :1801-1816).  Factors
+// above e^30 are taken as e^30: a trial with such a factor has a model value
+// of 1e13 or more at that pixel, an error far above any start error, and is
+// rejected whatever the exact value (as the reference rejects it).
 __device__ inline void g32_tables(const ModelCfg& cfg, const PeakRec& w, float* dst, int ts, int lane) {
-  const double xo = -(w.p[PX] - (double)w.xi) - cfg.xoff;
-  const double yo = -(w.p[PY] - (double)w.yi) - cfg.xoff;   // dao_fit.c:979 uses xoff
-  const double wx = w.p[PXW], wy = w.p[PYW];
+  const G32Axes ax = g32_axes(cfg, w);
   for (int i = lane; i < cfg.roi; i += 32) {
-    const double tx = (double)i + xo, ty = (double)i + yo;
-    const ff ex = ff_from_double(exp((-tx * tx) * wx));
-    const ff ey = ff_from_double(exp((-ty * ty) * wy));
+    const ff tx = ff_add_f(ax.xo, (float)i), ty = ff_add_f(ax.yo, (float)i);
+    ff argx = ff_neg(ff_mul(ff_mul(tx, tx), ax.wx)), argy = ff_neg(ff_mul(ff_mul(ty, ty), ax.wy));
+    if (argx.h > 30.0f) argx = ff{30.0f, 0.0f};
+    if (argy.h > 30.0f) argy = ff{30.0f, 0.0f};
+    const ff ex = ff_exp(argx);
+    const ff ey = ff_exp(argy);
     dst[i] = ex.h;
     dst[ts + i] = ex.l;
     dst[2 * ts + i] = ey.h;
     dst[3 * ts + i] = ey.l;
-    dst[4 * ts + i] = (float)tx;
-    dst[5 * ts + i] = (float)ty;
+    dst[4 * ts + i] = tx.h;
+    dst[5 * ts + i] = ty.h;
   }
 }
 
@@ -930,16 +991,15 @@ __device__ __forceinline__ void psf_and_delta(const ModelCfg& cfg, const T* aij,
 // Damped solve of the FP32 engine (warp-collective).
 //
 // The reference solves (H + lam diag H) d = b in FP64 with dposv
-// (multi_fit.c:1839-1883).  Here: Jacobi-scale the system to unit diagonal,
-// factor it in FP32 on lane 0, and refine the solution twice with the
-// residual r = b - A d evaluated in FP64 by lanes 0..k-1 in parallel
-// (one row each).  Each refinement shrinks the error by about
-// cond(A_scaled) * 2^-24, so the result carries FP64-level accuracy for
-// any system the FP32 factorisation accepts, at a few dozen FP64
-// instructions per warp instead of a few hundred.  When the scaled
-// diagonal is not positive or the FP32 factorisation fails, lane 0 falls
-// back to the FP64 Cholesky, which decides failure exactly as dposv does.
-// The solution (lane 0) is written to out[0..k).
+// (multi_fit.c:1839-1883).  Here lane i (< k) holds row i of the system:
+// the rows are Jacobi-scaled to unit diagonal and eliminated in FP32
+// without pivoting (the matrix is symmetric positive definite; a pivot
+// <= 0 means it is not, numerically), pivot rows broadcast by shuffles.
+// The solution is refined twice with the residual b - A d evaluated in
+// FP64 (one row per lane), which leaves an error of about
+// (cond(A_scaled) * 2^-24)^3.  When a pivot is not positive the FP64
+// Cholesky on lane 0 decides, exactly as dposv does.  The solution
+// (lane 0) is written to out[0..k).
 // ---------------------------------------------------------------------------
 
 template <typename T>
@@ -949,99 +1009,101 @@ __device__ inline int solve_damped(WarpWS<T>& ws, int k, double lam, double* out
   return info;
 }
 
+// Forward and back substitution with the factors held in r (multipliers
+// left of the diagonal, U from the diagonal on), one row per lane.
+__device__ __forceinline__ float lu_substitute(const float (&r)[MAX_JAC], float c, int k, int lane) {
+#pragma unroll
+  for (int j = 0; j < MAX_JAC; j++) {
+    if (j < k) {
+      const float cj = __shfl_sync(0xffffffffu, c, j);
+      if (lane > j && lane < k) c = fmaf(-r[j], cj, c);
+    }
+  }
+#pragma unroll
+  for (int j = MAX_JAC - 1; j >= 0; j--) {
+    if (j < k) {
+      if (lane == j) c = __fdiv_rn(c, r[j]);
+      const float xj = __shfl_sync(0xffffffffu, c, j);
+      if (lane < j) c = fmaf(-r[j], xj, c);
+    }
+  }
+  return c;
+}
+
 template <>
 __device__ inline int solve_damped<float>(WarpWS<float>& ws, int k, double lam, double* out, int lane) {
-  float* sm = ws.red;           // free during the solve
-  float* As = sm;               // k x k scaled matrix
-  float* L = sm + 64;           // FP32 Cholesky factor (stride 7)
-  float* rhs = sm + 128;
-  float* sol = sm + 136;
-  float* sc = sm + 144;         // Jacobi scales
-  double* xs = ws.scratch;      // solution being refined
   const double* jh = ws.jh;
+  const bool act = lane < k;
   double Ai[MAX_JAC];
-  double bi = 0.0, dii = 0.0;
-  float si = 0.0f;
-  bool bad = false;
-  if (lane < k) {
-    bi = jh[lane];
+  float r[MAX_JAC];
+  double bi = 0.0, dii = 1.0;
+#pragma unroll
+  for (int j = 0; j < MAX_JAC; j++) {
+    Ai[j] = 0.0;
+    if (act && j < k) {
+      const double a = jh[hes_index(k, lane, j)];
+      Ai[j] = (j == lane) ? (1.0 + lam) * a : a;
+      if (j == lane) dii = Ai[j];
+    }
+  }
+  if (act) bi = jh[lane];
+  const float dfl = (float)dii;
+  const bool bad = act && (!(dii > 0.0) || !(dfl > 1.0e-30f) || !(dfl < 1.0e30f));
+  int status = __any_sync(0xffffffffu, bad) ? 2 : 0;
+  const float si = act && !bad ? rsqrtf(dfl) : 0.0f;
+  if (status == 0) {
+#pragma unroll
+    for (int j = 0; j < MAX_JAC; j++) {
+      const float sj = __shfl_sync(0xffffffffu, si, j);
+      r[j] = (act && j < k) ? ((float)Ai[j] * si) * sj : 0.0f;
+    }
+    // elimination, pivot row j broadcast from lane j
+#pragma unroll
+    for (int j = 0; j < MAX_JAC; j++) {
+      if (j < k && status == 0) {
+        const float piv = __shfl_sync(0xffffffffu, r[j], j);
+        if (!(piv > 0.0f)) {
+          status = 2;
+        } else {
+          const bool below = act && lane > j;
+          const float m = below ? __fdiv_rn(r[j], piv) : 0.0f;
+#pragma unroll
+          for (int l = j + 1; l < MAX_JAC; l++) {
+            if (l < k) {
+              const float pl = __shfl_sync(0xffffffffu, r[l], j);
+              if (below) r[l] = fmaf(-m, pl, r[l]);
+            }
+          }
+          if (below) r[j] = m;
+        }
+      }
+    }
+  }
+  if (status == 0) {
+    float c = act ? (float)bi * si : 0.0f;
+    c = lu_substitute(r, c, k, lane);
+    double xs = act ? (double)(c * si) : 0.0;
+    for (int it = 0; it < 2; it++) {
+      double res = bi;
+#pragma unroll
+      for (int j = 0; j < MAX_JAC; j++) {
+        if (j < k) {
+          const double dj = __shfl_sync(0xffffffffu, xs, j);
+          if (act) res = fma(-Ai[j], dj, res);
+        }
+      }
+      c = act ? (float)res * si : 0.0f;
+      c = lu_substitute(r, c, k, lane);
+      if (act) xs += (double)(c * si);
+    }
 #pragma unroll
     for (int j = 0; j < MAX_JAC; j++) {
       if (j < k) {
-        const double a = jh[hes_index(k, lane, j)];
-        Ai[j] = (j == lane) ? (1.0 + lam) * a : a;
-        if (j == lane) dii = Ai[j];
-      }
-    }
-    const float df = (float)dii;
-    bad = !(dii > 0.0) || !(df > 1.0e-30f) || !(df < 1.0e30f);
-    si = bad ? 0.0f : rsqrtf(df);
-    sc[lane] = si;
-  }
-  int status = __any_sync(0xffffffffu, bad) ? 2 : 0;
-  __syncwarp();
-  if (status == 0) {
-    if (lane < k) {
-#pragma unroll
-      for (int j = 0; j < MAX_JAC; j++)
-        if (j < k) As[lane * k + j] = ((float)Ai[j] * si) * sc[j];
-      rhs[lane] = (float)bi * si;
-    }
-    __syncwarp();
-    if (lane == 0) {
-      for (int j = 0; j < k && status == 0; j++) {
-        float d = As[j * k + j];
-        for (int m = 0; m < j; m++) d -= L[j * 7 + m] * L[j * 7 + m];
-        if (!(d > 0.0f)) {
-          status = 2;
-          break;
+        const double v = __shfl_sync(0xffffffffu, xs, j);
+        if (lane == 0) {
+          out[j] = v;
+          if (isnan(v)) status = 1;   // multi_fit.c:1857-1863
         }
-        d = sqrtf(d);
-        L[j * 7 + j] = d;
-        const float inv = 1.0f / d;
-        for (int i = j + 1; i < k; i++) {
-          float s = As[i * k + j];
-          for (int m = 0; m < j; m++) s -= L[i * 7 + m] * L[j * 7 + m];
-          L[i * 7 + j] = s * inv;
-        }
-      }
-    }
-    status = __shfl_sync(0xffffffffu, status, 0);
-  }
-  if (status == 0) {
-    // first solve + two refinements
-    for (int it = 0; it < 3; it++) {
-      if (it > 0 && lane < k) {
-        double r = bi;
-#pragma unroll
-        for (int j = 0; j < MAX_JAC; j++)
-          if (j < k) r -= Ai[j] * xs[j];
-        rhs[lane] = (float)r * si;
-      }
-      __syncwarp();
-      if (lane == 0) {
-        for (int i = 0; i < k; i++) {
-          float s = rhs[i];
-          for (int m = 0; m < i; m++) s -= L[i * 7 + m] * sol[m];
-          sol[i] = s / L[i * 7 + i];
-        }
-        for (int i = k - 1; i >= 0; i--) {
-          float s = sol[i];
-          for (int m = i + 1; m < k; m++) s -= L[m * 7 + i] * sol[m];
-          sol[i] = s / L[i * 7 + i];
-        }
-      }
-      __syncwarp();
-      if (lane < k) {
-        const double c = (double)(sol[lane] * si);
-        xs[lane] = (it == 0) ? c : xs[lane] + c;
-      }
-      __syncwarp();
-    }
-    if (lane == 0) {
-      for (int i = 0; i < k; i++) {
-        out[i] = xs[i];
-        if (isnan(out[i])) status = 1;   // multi_fit.c:1857-1863
       }
     }
   }

@@ -34,31 +34,127 @@ enum { ACT_EVAL = 0, ACT_CONTINUE = 1, ACT_BREAK = 2, ACT_BREAK_ADDED = 3, ACT_E
 //   Z       [ps, ps a1, ps b1, ps (a2+b2), rqe] (:883-958)
 __device__ inline void g32_grad_tables(const ModelCfg& cfg, const PeakRec& w, double gx, double gy,
                                        float* g, int ts, int lane) {
-  const double h = w.p[PH];
-  const double xo = -(w.p[PX] - (double)w.xi) - cfg.xoff;
-  const double yo = -(w.p[PY] - (double)w.yi) - cfg.xoff;
+  const G32Axes ax = g32_axes(cfg, w);
   const bool one_width = (cfg.model == M_2DFIXED) || (cfg.model == M_2D);
-  const double wx = w.p[PXW], wy = one_width ? w.p[PXW] : w.p[PYW];
+  const ff H = ff_from_double(w.p[PH]);
+  const ff H2 = ff{2.0f * H.h, 2.0f * H.l};
+  const ff HX = ff_mul(H2, ax.wx), HY = ff_mul(H2, one_width ? ax.wx : ax.wy);   // 2 h w
+  const ff NX = (cfg.model == M_Z) ? ff_neg(ff_mul(H, ff_from_double(gx))) : ff_neg(H);
+  const ff NY = (cfg.model == M_Z) ? ff_neg(ff_mul(H, ff_from_double(gy))) : ff_neg(H);
   for (int i = lane; i < cfg.roi; i += 32) {
-    const double tx = (double)i + xo, ty = (double)i + yo;
-    double a2 = -h * tx * tx, b2 = -h * ty * ty;
-    if (cfg.model == M_Z) {
-      a2 *= gx;
-      b2 *= gy;
-    }
-    ff v = ff_from_double(2.0 * h * wx * tx);
+    const ff tx = ff_add_f(ax.xo, (float)i), ty = ff_add_f(ax.yo, (float)i);
+    ff v = ff_mul(HX, tx);
     g[i] = v.h;
     g[ts + i] = v.l;
-    v = ff_from_double(a2);
+    v = ff_mul(NX, ff_mul(tx, tx));
     g[2 * ts + i] = v.h;
     g[3 * ts + i] = v.l;
-    v = ff_from_double(2.0 * h * wy * ty);
+    v = ff_mul(HY, ty);
     g[4 * ts + i] = v.h;
     g[5 * ts + i] = v.l;
-    v = ff_from_double(b2);
+    v = ff_mul(NY, ff_mul(ty, ty));
     g[6 * ts + i] = v.h;
     g[7 * ts + i] = v.l;
   }
+}
+
+// The normal equations of a step as float-float values, in the memory of
+// ws.jh: hi parts at [0, 36), lo parts at [36, 72); gradient first, then
+// the packed upper Hessian (hes_index).
+__device__ __forceinline__ float* g32_jh(WarpWS<float>& ws) { return reinterpret_cast<float*>(ws.jh); }
+
+__device__ __forceinline__ ff shfl_ff(ff v, int src) {
+  return ff{__shfl_sync(0xffffffffu, v.h, src), __shfl_sync(0xffffffffu, v.l, src)};
+}
+
+// Damped solve (H + lam diag H) d = b of the FP32 Gaussian step
+// (multi_fit.c:1174-1203 with dposv :1839-1883), warp-collective, FP32
+// instructions only: lane i holds row i, Jacobi-scaled and eliminated in
+// FP32 (lu_substitute), then two refinements with the residual in
+// float-float.  A pivot <= 0 hands the system to the FP64 Cholesky on
+// lane 0, which decides failure as dposv does.  Solution on lane 0.
+__device__ inline int solve_g32(WarpWS<float>& ws, int k, double lam, double* out, int lane) {
+  const float* jh = g32_jh(ws);
+  const bool act = lane < k;
+  const ff L1 = ff_from_double(1.0 + lam);
+  ff Ai[MAX_JAC];
+  float r[MAX_JAC];
+  ff bi{0.0f, 0.0f}, dii{1.0f, 0.0f};
+#pragma unroll
+  for (int j = 0; j < MAX_JAC; j++) {
+    Ai[j] = ff{0.0f, 0.0f};
+    if (act && j < k) {
+      const int id = hes_index(k, lane, j);
+      const ff a{jh[id], jh[36 + id]};
+      Ai[j] = (j == lane) ? ff_mul(L1, a) : a;
+      if (j == lane) dii = Ai[j];
+    }
+  }
+  if (act) bi = ff{jh[lane], jh[36 + lane]};
+  const bool bad = act && !(dii.h > 1.0e-30f && dii.h < 1.0e30f);
+  int status = __any_sync(0xffffffffu, bad) ? 2 : 0;
+  const float si = act && !bad ? rsqrtf(dii.h) : 0.0f;
+  if (status == 0) {
+#pragma unroll
+    for (int j = 0; j < MAX_JAC; j++) {
+      const float sj = __shfl_sync(0xffffffffu, si, j);
+      r[j] = (act && j < k) ? (Ai[j].h * si) * sj : 0.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < MAX_JAC; j++) {
+      if (j < k && status == 0) {
+        const float piv = __shfl_sync(0xffffffffu, r[j], j);
+        if (!(piv > 0.0f)) {
+          status = 2;
+        } else {
+          const bool below = act && lane > j;
+          const float m = below ? __fdiv_rn(r[j], piv) : 0.0f;
+#pragma unroll
+          for (int l = j + 1; l < MAX_JAC; l++) {
+            if (l < k) {
+              const float pl = __shfl_sync(0xffffffffu, r[l], j);
+              if (below) r[l] = fmaf(-m, pl, r[l]);
+            }
+          }
+          if (below) r[j] = m;
+        }
+      }
+    }
+  }
+  if (status == 0) {
+    float c = act ? bi.h * si : 0.0f;
+    c = lu_substitute(r, c, k, lane);
+    ff xs = act ? two_prod(c, si) : ff{0.0f, 0.0f};
+    for (int it = 0; it < 2; it++) {
+      ff res = bi;
+#pragma unroll
+      for (int j = 0; j < MAX_JAC; j++) {
+        if (j < k) {
+          const ff dj = shfl_ff(xs, j);
+          if (act) res = ff_sub(res, ff_mul(Ai[j], dj));
+        }
+      }
+      c = act ? res.h * si : 0.0f;
+      c = lu_substitute(r, c, k, lane);
+      if (act) xs = ff_add(xs, two_prod(c, si));
+    }
+#pragma unroll
+    for (int j = 0; j < MAX_JAC; j++) {
+      if (j < k) {
+        const ff v = shfl_ff(xs, j);
+        if (lane == 0) {
+          out[j] = ff_to_double(v);
+          if (isnan(v.h)) status = 1;   // multi_fit.c:1857-1863
+        }
+      }
+    }
+  }
+  if (lane == 0 && status == 2) {
+    double jd[36];
+    for (int i = 0; i < 36; i++) jd[i] = (double)jh[i] + (double)jh[36 + i];
+    status = solve_fp64_lane0(jd, k, lam, out);
+  }
+  return status;
 }
 
 struct G32Pix {
@@ -110,6 +206,9 @@ __device__ inline void g32_pass1(const ModelCfg& cfg, const FrameSet<T>& fs, lon
     ws.t1h[p] = t1.h;
     ws.t1l[p] = t1.l;
     ws.f0g[p] = f0.h;
+    ws.Xs[p] = cur.x;
+    ws.Rs[p] = cur.rq;
+    ws.Cs[p] = (float)cur.C;
     const float t2 = __fdiv_rn(2.0f * cur.x, f0.h * f0.h);
     const ff ps = ff_mul_f(g32_psf(t0, ts, rx, ry), cur.rq);
     const ff u = ff_mul(t1, ps);
@@ -162,12 +261,9 @@ __device__ inline void g32_delta(const ModelCfg& cfg, const FrameSet<T>& fs, lon
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
     roi_rc(fs.roi_xy, p, rx, ry);
-    const long long k = pix_index(cfg, o.xi, o.yi, rx, ry);
-    const float xv = (float)__ldg(fs.x + fbase + k);
-    const float rq = (float)__ldg(fs.rqe + k);
-    const int C = __ldcg(fs.cnt + fbase + k);   // without this peak
+    const float xv = ws.Xs[p], rq = ws.Rs[p];
     const ff d = ff_mul_f(ff_sub(ff_mul(H1, g32_psf(ws.tab1, ts, rx, ry)), ff_mul(H0, g32_psf(ws.tab0, ts, rx, ry))), rq);
-    const ff bgd = ff_div(ff_mul_f(DBG, rq), ff{(float)(C + 1), 0.0f});
+    const ff bgd = ff_div(ff_mul_f(DBG, rq), ff{ws.Cs[p], 0.0f});
     const ff df = ff_add(d, bgd);
     const float f0 = ws.f0g[p];
     if (!(f0 + df.h > 0.0f)) {
@@ -179,23 +275,45 @@ __device__ inline void g32_delta(const ModelCfg& cfg, const FrameSet<T>& fs, lon
   }
 }
 
-// MLE error of a trial at another anchor, from the fit image without this
-// peak (FP32 with the exact fixed-point residual).
+// Is ROI pixel (rx, ry) inside the circular ROI (multi_fit.c:1031-1060)?
+// Exact in FP32: every term is a multiple of 1/4.
+__device__ __forceinline__ bool in_roi(int rx, int ry, int roi) {
+  if (rx < 0 || ry < 0 || rx >= roi || ry >= roi) return false;
+  const float c = 0.5f * (float)roi;
+  const float dx = (float)rx - c + 0.5f, dy = (float)ry - c + 0.5f;
+  return dx * dx + dy * dy <= c * c;
+}
+
+// MLE error of a trial at another anchor (FP32 with the exact fixed-point
+// residual).  The peak is still in the fit image at its start anchor o; its
+// contribution is taken out here, pixel by pixel, exactly as the write-back
+// will take it out.
 template <typename T>
 __device__ inline float g32_absolute(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
-                                     const PeakRec& t, WarpWS<T>& ws, int lane, bool& fail) {
+                                     const PeakRec& o, const PeakRec& t, WarpWS<T>& ws, int lane,
+                                     bool& fail) {
   const int ts = ws.ts;
   const float h1 = (float)t.p[PH], bg1 = (float)t.p[PBG];
+  const ff H0 = ff_from_double(o.p[PH]), BG0 = ff_from_double(o.p[PBG]);
+  const int dx = t.xi - o.xi, dy = t.yi - o.yi;
   float devf = 0.0f;
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
     roi_rc(fs.roi_xy, p, rx, ry);
     const long long k = pix_index(cfg, t.xi, t.yi, rx, ry);
-    const long long F = __ldcg(fs.f + fbase + k), B = __ldcg(fs.bg + fbase + k);
-    const int C = __ldcg(fs.cnt + fbase + k);
+    long long F = __ldcg(fs.f + fbase + k), B = __ldcg(fs.bg + fbase + k);
+    int C = __ldcg(fs.cnt + fbase + k);
     const float xv = (float)__ldg(fs.x + fbase + k);
     const float rq = (float)__ldg(fs.rqe + k), sc = (float)__ldg(fs.scmos + k);
     const long long Xq = __ldg(fs.xq + fbase + k);
+    const int ox = rx + dx, oy = ry + dy;   // the same image pixel in the start ROI
+    if (in_roi(ox, oy, cfg.roi)) {
+      Q2 qf, qb;
+      g32_contrib(ws.tab0, ts, H0, BG0, ox, oy, rq, sc, qf, qb);
+      F -= qf.h;
+      B -= qb.h;
+      C -= 1;
+    }
     const float psf = g32_psf(ws.tab1, ts, rx, ry).h;
     const float res = fx_to_float(F - Xq) + h1 * psf * rq +
                       __fdiv_rn(fx_to_float(B) + bg1 * rq + sc, (float)(C + 1));
@@ -241,26 +359,26 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
       case M_3D: g32_pass1<M_3D>(cfg, fs, fbase, orig, ws, lane, g, acc, devf, fail); break;
       default: g32_pass1<M_Z>(cfg, fs, fbase, orig, ws, lane, g, acc, devf, fail); break;
     }
-    // subtract this peak (multi_fit.c:1141)
+    // The reference subtracts the peak here (multi_fit.c:1141) and adds the
+    // accepted trial back.  No other warp touches this ROI during the step,
+    // so the subtraction is deferred to the write-back, which applies the
+    // net change once; the trial evaluations account for it.
     const ff H0 = ff_from_double(orig.p[PH]), BG0 = ff_from_double(orig.p[PBG]);
-    for (int p = lane; p < cfg.nroi; p += 32) {
-      int rx, ry;
-      roi_rc(fs.roi_xy, p, rx, ry);
-      const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
-      Q2 qf, qb;
-      g32_contrib(ws.tab0, ts, H0, BG0, rx, ry, (float)__ldg(fs.rqe + kk), (float)__ldg(fs.scmos + kk), qf, qb);
-      acc_red<1>(fs.f, fbase + kk, qf, -1);
-      acc_red<1>(fs.bg, fbase + kk, qb, -1);
-      atomicAdd(fs.cnt + fbase + kk, -1);
-    }
     const double dev0 = warp_sum_ff(devf);
     fail = __any_sync(0xffffffffu, fail);
     {
+      float* jh = g32_jh(ws);
       const ff hv = warp_transpose_sum32_ff(acc, lane);
-      if (lane < nhes) ws.jh[k + lane] = ff_to_double(hv);
+      if (lane < nhes) {
+        jh[k + lane] = hv.h;
+        jh[36 + k + lane] = hv.l;
+      }
       const ff gv = warp_reduce8_ff(g, lane);
       const int gi = reduce8_index(lane);
-      if ((lane & 3) == 0 && gi < k) ws.jh[gi] = ff_to_double(gv);
+      if ((lane & 3) == 0 && gi < k) {
+        jh[gi] = gv.h;
+        jh[36 + gi] = gv.l;
+      }
     }
     __syncwarp();
 
@@ -296,7 +414,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
       // damped solve (multi_fit.c:1174-1203), warp-collective
       const double lam = __shfl_sync(0xffffffffu, w.lambda, 0);
       double b[MAX_JAC];
-      const int info = solve_damped<T>(ws, k, lam, b, lane);
+      const int info = solve_g32(ws, k, lam, b, lane);
       if (lane == 0) {
         if (info != 0) {
           ctr[C_DPOSV]++;
@@ -343,10 +461,11 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
         g32_delta(cfg, fs, fbase, orig, wl, ws, lane, s1, s2, fail);
         dev = ff_to_double(warp_sum_ffv(s1)) + warp_sum_ff(s2);
       } else {
-        __threadfence();
-        __syncwarp();
-        dev = warp_sum_ff(g32_absolute(cfg, fs, fbase, wl, ws, lane, fail));
+        dev = warp_sum_ff(g32_absolute(cfg, fs, fbase, orig, wl, ws, lane, fail));
       }
+      // A trial whose error overflows FP32 has an error astronomically above
+      // the start error in the reference's FP64 too: reject it.
+      if (!(fabs(dev) < 1.0e300)) dev = 1.0e300;
       fail = __any_sync(0xffffffffu, fail);
       if (lane == 0) {
         if (fail) {
@@ -387,26 +506,38 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
       }
     }
 
-    // -- 3. write back
-    if (escaped) {
-      // restore the start-of-step contribution; the record is untouched
+    // -- 3. write back: the net change of the fit image (subtract the start
+    // contribution, add the accepted one)
+    if (escaped) return true;   // nothing was changed
+    if (lane == 0) w.added = orig.added - 1 + (added_end ? 1 : 0);
+    __syncwarp();
+    const PeakRec& wl = *ws.w;
+    const ff H1 = ff_from_double(wl.p[PH]), BG1 = ff_from_double(wl.p[PBG]);
+    if (added_end && wl.xi == orig.xi && wl.yi == orig.yi) {
+      for (int p = lane; p < cfg.nroi; p += 32) {
+        int rx, ry;
+        roi_rc(fs.roi_xy, p, rx, ry);
+        const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
+        const float rq = ws.Rs[p], sc = (float)__ldg(fs.scmos + kk);
+        Q2 q0f, q0b, q1f, q1b;
+        g32_contrib(ws.tab0, ts, H0, BG0, rx, ry, rq, sc, q0f, q0b);
+        g32_contrib(ws.tab1, ts, H1, BG1, rx, ry, rq, sc, q1f, q1b);
+        acc_red<1>(fs.f, fbase + kk, q_sub(q1f, q0f), +1);
+        acc_red<1>(fs.bg, fbase + kk, q_sub(q1b, q0b), +1);
+      }
+    } else {
       for (int p = lane; p < cfg.nroi; p += 32) {
         int rx, ry;
         roi_rc(fs.roi_xy, p, rx, ry);
         const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
         Q2 qf, qb;
-        g32_contrib(ws.tab0, ts, H0, BG0, rx, ry, (float)__ldg(fs.rqe + kk), (float)__ldg(fs.scmos + kk), qf, qb);
-        acc_red<1>(fs.f, fbase + kk, qf, +1);
-        acc_red<1>(fs.bg, fbase + kk, qb, +1);
-        atomicAdd(fs.cnt + fbase + kk, 1);
+        g32_contrib(ws.tab0, ts, H0, BG0, rx, ry, ws.Rs[p], (float)__ldg(fs.scmos + kk), qf, qb);
+        acc_red<1>(fs.f, fbase + kk, qf, -1);
+        acc_red<1>(fs.bg, fbase + kk, qb, -1);
+        atomicAdd(fs.cnt + fbase + kk, -1);
       }
-      return true;
     }
-    if (lane == 0) w.added = orig.added - 1 + (added_end ? 1 : 0);
-    __syncwarp();
-    if (added_end) {
-      const PeakRec& wl = *ws.w;
-      const ff H1 = ff_from_double(wl.p[PH]), BG1 = ff_from_double(wl.p[PBG]);
+    if (added_end && (wl.xi != orig.xi || wl.yi != orig.yi)) {
       for (int p = lane; p < cfg.nroi; p += 32) {
         int rx, ry;
         roi_rc(fs.roi_xy, p, rx, ry);

@@ -445,7 +445,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
 
 // G32: the FP32 Gaussian step (lm_step_g32); otherwise lm_step.
 template <typename T, bool G32>
-__global__ void __launch_bounds__(128, 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
+__global__ void __launch_bounds__(128, G32 ? 6 : 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
   extern __shared__ __align__(16) char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
