@@ -175,11 +175,29 @@ def roi_pixels(roi):
 
 
 def load_profile_traffic():
+    """DRAM bytes of sweep-kernel launches from one ncu capture (see
+    profiles/k_sweep_cfg1.md), per frame of the workload."""
     p = os.path.join(ROOT, "profiles", "k_sweep_cfg1_traffic.json")
     if os.path.exists(p):
         with open(p) as fp:
             return json.load(fp)
     return None
+
+
+def load_measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fp:
+            return json.load(fp)
+    return {}
+
+
+def bytes_per_iteration(nroi):
+    """Algorithmic bytes of one LM inner iteration of one peak: per ROI pixel
+    the start state (fit image and background words 8 + 8, count 4, data
+    8 + 4, rqe 4) read once and the fit-image / background update (8 + 8)
+    written once: 52 B."""
+    return 52 * nroi
 
 
 def peaks_rows(wl):
@@ -322,6 +340,13 @@ def run_ours(args, rank, world, local_rank):
         bound = "fp64"
     achieved = flops / (sweep_ms / 1e3) / 1e12 if sweep_ms > 0 else None
     traffic = load_profile_traffic()
+    peaks = load_measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs")
+    alg_bytes = bytes_per_iteration(nroi) * iters if nroi else None
+    hbm_achieved = alg_bytes / (sweep_ms / 1e3) / 1e9 if (alg_bytes and sweep_ms > 0) else None
+    traffic_launch = None
+    if traffic and traffic.get("dram_bytes_per_frame_first_sweep"):
+        traffic_launch = traffic["dram_bytes_per_frame_first_sweep"] * F
     line = {
         "metric": "localizations/s (LM to convergence)",
         "value": value,
@@ -333,7 +358,8 @@ def run_ours(args, rank, world, local_rank):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "fp32 model+Jacobian / fp64 solve+decisions" if args.precision == 32 else "fp64",
+        "dtype": ("f32 (float-float gradient, error change and solve refinement)"
+                  if args.precision == 32 else "f64"),
         "data": "synthetic (seeded, benchmark configuration %d shapes)" % cfg,
         "config": {"workload": "cfg%d: %s model, %d frames %dx%d, %d emitters, roi %s, max %d sweeps"
                                % (cfg, model, F, shape[1], shape[0], units, kw.get("roi_size"), MAX_IT),
@@ -348,12 +374,21 @@ def run_ours(args, rank, world, local_rank):
                      "unit": "TFLOP/s", "frac": (achieved / peak_tf) if achieved else None,
                      "peak_source": "nominal %d SMs x 128 FP32 lanes x 2 x %.0f MHz" % (nsm, mx)
                      if bound == "fp32" else "nominal FP64",
-                     "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                     "traffic": traffic_launch,
+                     "traffic_note": "ncu DRAM read+write bytes of the first sweep launch, "
+                                     "per frame of a 16-frame capture, times the frames of this step"
+                     if traffic_launch else None,
                      "sweep_launches": int(sweep_launches), "sweep_ms_per_step": sweep_ms,
                      "lm_iterations_per_step": iters, "flops_per_iteration": flops_per_iteration(model, nroi),
                      "sweep_ms_first5": [round(float(v), 3) for v in per_sweep[:5]],
                      "sweep_ms_median_after20": float(numpy.median(per_sweep[20:])) if per_sweep.size > 20 else None,
                      "sweep_ms_sum_after20": float(per_sweep[20:].sum()) if per_sweep.size > 20 else None},
+        "roofline_hbm": {"bound": "hbm", "kernel": "k_sweep", "achieved": hbm_achieved,
+                         "peak": hbm_peak, "unit": "GB/s",
+                         "frac": (hbm_achieved / hbm_peak) if (hbm_achieved and hbm_peak) else None,
+                         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_peak else None,
+                         "traffic": traffic_launch,
+                         "bytes_per_iteration": bytes_per_iteration(nroi) if nroi else None},
         "fit": {"converged": int((status == 1).sum()), "error": int((status == 2).sum()),
                 "running": int((status == 0).sum()), "sweeps": fit.sweeps,
                 "scheduler": fit.sched_stats()},
