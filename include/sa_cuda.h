@@ -228,6 +228,22 @@ int saGetSweepTimes(saFitData *fit, float *out, int max_n);
 /* Number of kernels this handle has launched. */
 int64_t saGetKernelLaunches(saFitData *fit);
 
+/* No reference counterpart.  Fit image (residual = 0, as mFitGetFitImage) or
+ * residual (residual = 1, as mFitGetResidual) of frame `frame` of the frame
+ * set, written to the host array out (image_size_x * image_size_y doubles),
+ * without allocating device memory: the kernel writes into a fixed 8 MiB
+ * device scratch array compiled into the library, so frames of at most
+ * 1,048,576 pixels are accepted (larger ones return -1).  For callers that
+ * must not allocate: cudaMalloc / cudaFree (which the other output paths
+ * may call to grow their staging buffer) can synchronise the whole device,
+ * and a serving loop with work in flight on other streams, or one that has
+ * reserved its device memory up front, cannot afford that.  The first call
+ * on each device looks the scratch address up (cudaGetSymbolAddress); make
+ * it before any stream capture.  Calls that overlap in time (other threads
+ * or streams, any handle) share the one scratch array and race.
+ * Returns 0 on success, -1 on error (saGetLastError). */
+int saGetFitImageNoAlloc(saFitData *fit, int frame, double *out, int residual);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,38 @@ void dfree(P*& p) {
   p = nullptr;
 }
 
+}  // namespace
+
+// Device scratch of saGetFitImageNoAlloc: 8 MiB compiled into the library
+// (one copy per device), enough for a 1024 x 1024 frame of doubles.  It is
+// reached through cudaGetSymbolAddress, never allocated or freed.
+constexpr size_t kNoAllocPixels = (size_t)1 << 20;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocPixels];
+
+namespace {
+
+// The scratch's device address on the current device, looked up once per
+// device (the first call on a device makes this set-up call).
+double* noalloc_scratch() {
+  static double* addr[64] = {nullptr};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) {
+    set_error("saGetFitImageNoAlloc: no current device (%s)", cudaGetErrorString(e));
+    return nullptr;
+  }
+  if (!addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("saGetFitImageNoAlloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return nullptr;
+    }
+    addr[dev] = static_cast<double*>(p);
+  }
+  return addr[dev];
+}
+
 struct Engine {
   ModelCfg cfg{};
   bool model_set = false;
@@ -1040,6 +1072,35 @@ static void fit_image_common(saFitData* h, double* out, int residual) {
 
 void mFitGetFitImage(saFitData* h, double* out) { fit_image_common(h, out, 0); }
 void mFitGetResidual(saFitData* h, double* out) { fit_image_common(h, out, 1); }
+
+int saGetFitImageNoAlloc(saFitData* h, int frame, double* out, int residual) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if ((size_t)e->npix > kNoAllocPixels) {
+    set_error("saGetFitImageNoAlloc: %lld pixels exceed the scratch capacity of %zu",
+              (long long)e->npix, kNoAllocPixels);
+    return -1;
+  }
+  if (!e->d_x || frame < 0 || frame >= e->F) {
+    set_error("saGetFitImageNoAlloc: no image or frame %d out of range", frame);
+    return -1;
+  }
+  double* scratch = noalloc_scratch();
+  if (!scratch) return -1;
+  // The kernel writes every element that is copied out: nothing in the
+  // scratch has to start at zero.
+  cudaError_t err = (e->prec == 32)
+                        ? Launch<float>::fit_image(e->fs<float>(), frame, scratch, residual, e->stream)
+                        : Launch<double>::fit_image(e->fs<double>(), frame, scratch, residual, e->stream);
+  if (err != cudaSuccess) {
+    set_error("saGetFitImageNoAlloc: %s", cudaGetErrorString(err));
+    return -1;
+  }
+  e->launches += 1;
+  CK(cudaMemcpyAsync(out, scratch, (size_t)e->npix * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
 
 void mFitSetPeakStatus(saFitData* h, int32_t* status) {
   Engine* e = E(h);

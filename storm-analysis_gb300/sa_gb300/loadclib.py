@@ -138,6 +138,8 @@ def _declare(lib):
     lib.saSetDevice.restype = ci
     lib.saGetSweepTimes.argtypes = [hp, ndpointer(dtype=numpy.float32, flags="C_CONTIGUOUS"), ci]
     lib.saGetSweepTimes.restype = ci
+    lib.saGetFitImageNoAlloc.argtypes = [hp, ci, f64, ci]
+    lib.saGetFitImageNoAlloc.restype = ci
 
 
 EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoInitialize3D",
@@ -155,4 +157,5 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "saDoFit", "saGetCounters", "saGetSchedStats", "saSetFrames", "saNewImages",
            "saNewBackgrounds", "saNewPeaksBatch", "saNewPeaksBatchDevice", "saDoFitBatch", "saGetNFitBatch",
            "saGetPeakPropertyBatch", "saGetPeakPropertyIntBatch", "saSetTiming", "saGetTiming",
-           "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice", "saGetSweepTimes"]
+           "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice", "saGetSweepTimes",
+           "saGetFitImageNoAlloc"]
