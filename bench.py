@@ -449,6 +449,68 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_serving(args, local_rank):
+    """Serving stream (benchmark configuration 4, reduced): requests of frame
+    size 128/256/512, density log-uniform 0.05-2 /um^2 and model 2d/3d/Z/
+    spline3D arriving Poisson at args.rate frames/s, fitted by the
+    continuous-batching FitServer.  Prints one JSON line with the stream's
+    localizations/s and the p50 / p99 request latency (arrival to result)."""
+    import torch
+    from sa_gb300 import loadclib, synth
+    from sa_gb300.serving import FitServer
+    loadclib.load().saSetDevice(local_rank)
+    torch.cuda.set_device(local_rank)
+    sizes = tuple(int(s) for s in args.serving_sizes.split(","))
+    st = synth.serving_requests(args.requests + args.warmup, rate_hz=args.rate, seed=4, sizes=sizes)
+    reqs = []
+    for i in range(len(st["t"])):
+        model, size, dens = str(st["model"][i]), int(st["size"][i]), float(st["density"][i])
+        wl = synth.serving_frame(model, size, dens, seed=1000 + i)
+        reqs.append({"model": model, "image": wl["images"][0], "background": wl["backgrounds"][0],
+                     "peaks": wl["guesses"][0], "ptype": "hdf5", "fitter": wl["fitter"], "rqe": wl["rqe"],
+                     "scmos_cal": wl["scmos_cal"], "camera": (model, size), "max_iterations": MAX_IT})
+    server = FitServer(mem_cap_bytes=40e9, slots=args.slots, precision=args.precision)
+    warm = reqs[:args.warmup]
+    if warm:
+        server.run(warm)
+    timed = reqs[args.warmup:]
+    arrivals = st["t"][args.warmup:] - st["t"][args.warmup]
+    launches0 = sum(l.fitter.kernel_launches() for l in server.lanes.values())
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ids = server.run(timed, arrivals)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    lat = server.latencies(ids) * 1e3
+    locs = sum(len(server.done[i]["x"]) for i in ids)
+    big = [j for j, r in enumerate(timed) if r["image"].shape[0] == 512]
+    launches = sum(l.fitter.kernel_launches() for l in server.lanes.values()) - launches0
+    line = {
+        "metric": "localizations/s (serving stream, continuous batching)",
+        "value": locs / wall, "unit": "localizations/s", "n_gpus": 1, "steps": 1,
+        "warmup": args.warmup, "ms_per_step": wall * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (float-float step decisions)" if args.precision == 32 else "f64",
+        "data": "synthetic (seeded, benchmark configuration 4 shapes, sizes %s)" % (sizes,),
+        "config": {"workload": "cfg4 serving: %d requests Poisson at %.0f frames/s, models 2d/3d/Z/spline3D, "
+                               "density log-U(0.05, 2) /um^2" % (len(timed), args.rate),
+                   "slots_per_lane": args.slots, "memory_cap_gb": 40,
+                   "lanes": len(server.lanes), "localizations": int(locs)},
+        "latency_ms": {"p50": float(numpy.percentile(lat, 50)), "p99": float(numpy.percentile(lat, 99)),
+                       "max": float(lat.max()),
+                       "p50_512": float(numpy.percentile(lat[big], 50)) if big else None,
+                       "p99_512": float(numpy.percentile(lat[big], 99)) if big else None},
+        "e2e": {"value": locs / wall, "unit": "localizations/s", "note": "host frames in, results out"},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    server.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -462,11 +524,19 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-cores", type=int, default=None)
+    ap.add_argument("--serving", action="store_true", help="run the serving stream instead")
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--serving-sizes", default="128,256,512")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
-    if args.impl == "reference":
+    if args.serving and args.impl == "ours":
+        if rank == 0:
+            run_serving(args, local_rank)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world, local_rank)

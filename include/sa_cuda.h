@@ -185,6 +185,10 @@ int saDeviceCount(void);
 int saSetPrecision(saFitData *fit, int bits);
 /* Footprint dilation (pixels) used by the dependency scheduler; default 2. */
 int saSetDilation(saFitData *fit, int pixels);
+/* At most `ctas` CTAs (4 warps each) for the handle's sweep kernel; 0 (the
+ * default) uses the full persistent grid.  A small cap lets the sweeps of
+ * several handles run side by side on the device (serving lanes). */
+int saSetSweepCTAs(saFitData *fit, int ctas);
 /* Use this CUDA stream (cudaStream_t) for all work of the handle. */
 int saSetStream(saFitData *fit, void *stream);
 /* The whole doFit loop of dao_fit_c.py:332-356 on the device: one sweep,
@@ -227,6 +231,25 @@ int saGetTiming(saFitData *fit, double *total_ms, int64_t *launches, int64_t *ti
 int saGetSweepTimes(saFitData *fit, float *out, int max_n);
 /* Number of kernels this handle has launched. */
 int64_t saGetKernelLaunches(saFitData *fit);
+
+/* Serving slots (no reference counterpart).  The frames of a frame set
+ * (saSetFrames) are slots that fit independently: a slot can be loaded with
+ * a new frame while the others are mid-fit, and the device state machine
+ * runs every loaded slot's sweeps as in saDoFit.
+ *   saSlotLoad    frame + background (host, bits 32/64) + peak rows into one
+ *                 slot and start its fit (max_iterations as doFit); the
+ *                 handle's stream is synchronised (call it between bursts)
+ *   saSlotLaunch  enqueue n_ticks sweep ticks for all slots and an
+ *                 asynchronous read-back of the slots' states
+ *   saSlotPoll    wait for that read-back; phases (PH_* : 0 idle, 4 done) and
+ *                 sweeps per slot; returns the number of slots still fitting
+ *   saSlotResults one slot's results as saGetResultsBatch; returns its peak
+ *                 count */
+int saSlotLoad(saFitData *fit, int slot, const void *image, const void *background, int bits,
+               const double *peaks, int n_peaks, const char *p_type, int max_iterations);
+int saSlotLaunch(saFitData *fit, int n_ticks);
+int saSlotPoll(saFitData *fit, int32_t *phases, int32_t *sweeps);
+int saSlotResults(saFitData *fit, int slot, double *values, int32_t *ints);
 
 /* No reference counterpart.  Fit image (residual = 0, as mFitGetFitImage) or
  * residual (residual = 1, as mFitGetResidual) of frame `frame` of the frame

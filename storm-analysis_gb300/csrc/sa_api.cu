@@ -134,6 +134,7 @@ struct Engine {
   cudaStream_t stream = 0;
   int epoch = 0;
   int sweep_grid = 0;
+  int sweep_ctas_cap = 0;   // 0: the full persistent grid
   size_t sweep_smem = 0, cta_smem = 0, warp_smem = 0;
   bool configured = false;
 
@@ -154,7 +155,17 @@ struct Engine {
   long long sweep_launches = 0, ticks = 0;
   long long launches = 0;   // kernels launched by this handle
 
-  ~Engine() { release(); }
+  // serving slots: frame control blocks copied back after each launched
+  // burst of ticks (pinned, read once the event has completed)
+  FrameCtl* h_ctl = nullptr;
+  int h_ctl_n = 0;
+  cudaEvent_t ev_poll = nullptr;
+
+  ~Engine() {
+    release();
+    if (h_ctl) cudaFreeHost(h_ctl);
+    if (ev_poll) cudaEventDestroy(ev_poll);
+  }
 
   void release_peaks() {
     dfree(d_pk); dfree(d_snap); dfree(d_pkoff); dfree(d_nfit); dfree(d_run); dfree(d_anchor);
@@ -360,6 +371,10 @@ struct Engine {
     return 0;
   }
 
+  int grid() const {
+    return (sweep_ctas_cap > 0 && sweep_ctas_cap < sweep_grid) ? sweep_ctas_cap : sweep_grid;
+  }
+
   int tick() {
     ticks++;
     launches += 3;
@@ -370,7 +385,7 @@ struct Engine {
       CK(Launch<float>::prepare(cfg, s, cta_smem, stream));
       epoch++;
       if (timing) CK(cudaEventRecord(ta, stream));
-      CK(Launch<float>::sweep(cfg, s, epoch, sweep_grid, sweep_smem, stream));
+      CK(Launch<float>::sweep(cfg, s, epoch, grid(), sweep_smem, stream));
       if (timing) CK(cudaEventRecord(tb, stream));
       CK(Launch<float>::post(cfg, s, cta_smem, stream));
     } else {
@@ -378,7 +393,7 @@ struct Engine {
       CK(Launch<double>::prepare(cfg, s, cta_smem, stream));
       epoch++;
       if (timing) CK(cudaEventRecord(ta, stream));
-      CK(Launch<double>::sweep(cfg, s, epoch, sweep_grid, sweep_smem, stream));
+      CK(Launch<double>::sweep(cfg, s, epoch, grid(), sweep_smem, stream));
       if (timing) CK(cudaEventRecord(tb, stream));
       CK(Launch<double>::post(cfg, s, cta_smem, stream));
     }
@@ -1171,6 +1186,13 @@ int saSetDilation(saFitData* h, int pixels) {
   return 0;
 }
 
+int saSetSweepCTAs(saFitData* h, int ctas) {
+  Engine* e = E(h);
+  if (!e || ctas < 0) return -1;
+  e->sweep_ctas_cap = ctas;
+  return 0;
+}
+
 int saSetStream(saFitData* h, void* stream) {
   Engine* e = E(h);
   if (!e) return -1;
@@ -1412,6 +1434,110 @@ int saGetSweepTimes(saFitData* h, float* out, int max_n) {
 int64_t saGetKernelLaunches(saFitData* h) {
   Engine* e = E(h);
   return e ? e->launches : -1;
+}
+
+// ---- serving slots ---------------------------------------------------------
+
+int saSlotLoad(saFitData* h, int slot, const void* image, const void* background, int bits,
+               const double* peaks, int n_peaks, const char* p_type, int max_iterations) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  if (!e->d_pk || slot < 0 || slot >= e->F) {
+    set_error("saSlotLoad: slot %d is not in the frame set (saSetFrames first)", slot);
+    return -1;
+  }
+  if (bits != 32 && bits != 64) {
+    set_error("saSlotLoad: dtype bits must be 32 or 64");
+    return -1;
+  }
+  const int pt = parse_ptype(p_type);
+  if (pt < 0) {
+    set_error("Unrecognized peak type '%s'!", p_type ? p_type : "(null)");
+    return -1;
+  }
+  if (n_peaks < 0 || n_peaks > e->cap_f[slot]) {
+    set_error("saSlotLoad: %d peaks, slot capacity %d", n_peaks, e->cap_f[slot]);
+    return -1;
+  }
+  // the slot is idle while its frame and peaks are replaced
+  FrameCtl c;
+  memset(&c, 0, sizeof(c));
+  c.phase = PH_IDLE;
+  c.escaped_min = INT_MAX;
+  CK(cudaMemcpyAsync(e->d_ctl + slot, &c, sizeof(c), cudaMemcpyHostToDevice, e->stream));
+  const size_t bytes = (size_t)e->npix * (bits / 8);
+  if (e->stage(2 * bytes)) return -1;
+  char* st = (char*)e->d_stage;
+  CK(cudaMemcpyAsync(st, image, bytes, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(st + bytes, background, bytes, cudaMemcpyHostToDevice, e->stream));
+  if (e->prec == 32) {
+    CK(Launch<float>::new_image(e->fs<float>(), st, bits, slot, 1, e->stream));
+    CK(Launch<float>::new_background(e->fs<float>(), st + bytes, bits, slot, 1, e->stream));
+  } else {
+    CK(Launch<double>::new_image(e->fs<double>(), st, bits, slot, 1, e->stream));
+    CK(Launch<double>::new_background(e->fs<double>(), st + bytes, bits, slot, 1, e->stream));
+  }
+  e->launches += 2;
+  CK(cudaStreamSynchronize(e->stream));   // the stage buffer is reused below
+  e->nfit[slot] = 0;
+  std::vector<int> counts(e->F, 0);
+  counts[slot] = n_peaks;
+  if (insert_peaks(e, peaks, counts, pt)) return -1;
+  c.phase = PH_SWEEP_PENDING;
+  c.max_sweeps = max_iterations + 1;   // dao_fit_c.py:340-346
+  CK(cudaMemcpyAsync(e->d_ctl + slot, &c, sizeof(c), cudaMemcpyHostToDevice, e->stream));
+  return 0;
+}
+
+int saSlotLaunch(saFitData* h, int n_ticks) {
+  Engine* e = E(h);
+  if (!e || !e->d_ctl) return -1;
+  if (!e->h_ctl || e->h_ctl_n < e->F) {
+    if (e->h_ctl) cudaFreeHost(e->h_ctl);
+    e->h_ctl = nullptr;
+    CK(cudaMallocHost((void**)&e->h_ctl, sizeof(FrameCtl) * e->F));
+    e->h_ctl_n = e->F;
+  }
+  if (!e->ev_poll) CK(cudaEventCreateWithFlags(&e->ev_poll, cudaEventDisableTiming));
+  for (int i = 0; i < n_ticks; i++)
+    if (e->tick()) return -1;
+  CK(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(FrameCtl) * e->F, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaEventRecord(e->ev_poll, e->stream));
+  return 0;
+}
+
+int saSlotPoll(saFitData* h, int32_t* phases, int32_t* sweeps) {
+  Engine* e = E(h);
+  if (!e || !e->h_ctl || !e->ev_poll) return -1;
+  CK(cudaEventSynchronize(e->ev_poll));
+  if (e->check_err_flag()) return -1;
+  int active = 0;
+  for (int f = 0; f < e->F; f++) {
+    const int ph = e->h_ctl[f].phase;
+    if (phases) phases[f] = ph;
+    if (sweeps) sweeps[f] = e->h_ctl[f].sweeps;
+    if (ph != PH_DONE && ph != PH_IDLE) active++;
+  }
+  e->host_valid = false;
+  return active;
+}
+
+int saSlotResults(saFitData* h, int slot, double* values, int32_t* ints) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk || slot < 0 || slot >= e->F) return -1;
+  const int n = e->nfit[slot];
+  if (n == 0) return 0;
+  std::vector<PeakRec> recs(n);
+  CK(cudaMemcpyAsync(recs.data(), e->d_pk + e->pk_off[slot], sizeof(PeakRec) * n, cudaMemcpyDeviceToHost,
+                     e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  const char* names[8] = {"x", "y", "z", "height", "background", "xsigma", "ysigma", "error"};
+  for (int j = 0; j < n; j++) {
+    for (int q = 0; q < 8; q++) record_prop(e, recs[j], names[q], values + (size_t)j * 8 + q);
+    ints[j * 2] = recs[j].status;
+    ints[j * 2 + 1] = recs[j].iterations;
+  }
+  return n;
 }
 
 }  // extern "C"

@@ -28,12 +28,22 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
   const size_t s_aux = ws0 * (AUX_BLOCK / 32);
   if (s_sweep > (size_t)max_smem || s_cta > (size_t)max_smem) return cudaErrorInvalidConfiguration;
   const bool g32 = gauss32<T>(cfg);
-  e = cudaFuncSetAttribute(g32 ? k_sweep<T, true> : k_sweep<T, false>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s_sweep);
+  // The limit is a property of the kernel, shared by every handle of the
+  // process (handles of different models and ROI sizes may run side by
+  // side), so it is raised to the device maximum rather than to this
+  // handle's need.
+  auto raise_limit = [max_smem](const void* fn) {
+    cudaFuncAttributes a;
+    cudaError_t r = cudaFuncGetAttributes(&a, fn);
+    if (r != cudaSuccess) return r;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                max_smem - (int)a.sharedSizeBytes);
+  };
+  e = raise_limit((const void*)(g32 ? k_sweep<T, true> : k_sweep<T, false>));
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_prepare<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s_cta);
+  e = raise_limit((const void*)k_prepare<T>);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_post<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s_cta);
+  e = raise_limit((const void*)k_post<T>);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g32 ? k_sweep<T, true> : k_sweep<T, false>,

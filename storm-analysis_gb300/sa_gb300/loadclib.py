@@ -140,6 +140,16 @@ def _declare(lib):
     lib.saGetSweepTimes.restype = ci
     lib.saGetFitImageNoAlloc.argtypes = [hp, ci, f64, ci]
     lib.saGetFitImageNoAlloc.restype = ci
+    lib.saSetSweepCTAs.argtypes = [hp, ci]
+    lib.saSetSweepCTAs.restype = ci
+    lib.saSlotLoad.argtypes = [hp, ci, vp, vp, ci, f64, ci, cs, ci]
+    lib.saSlotLoad.restype = ci
+    lib.saSlotLaunch.argtypes = [hp, ci]
+    lib.saSlotLaunch.restype = ci
+    lib.saSlotPoll.argtypes = [hp, i32, i32]
+    lib.saSlotPoll.restype = ci
+    lib.saSlotResults.argtypes = [hp, ci, f64, i32]
+    lib.saSlotResults.restype = ci
 
 
 EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoInitialize3D",
@@ -158,4 +168,5 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "saNewBackgrounds", "saNewPeaksBatch", "saNewPeaksBatchDevice", "saDoFitBatch", "saGetNFitBatch",
            "saGetPeakPropertyBatch", "saGetPeakPropertyIntBatch", "saSetTiming", "saGetTiming",
            "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice", "saGetSweepTimes",
-           "saGetFitImageNoAlloc"]
+           "saGetFitImageNoAlloc", "saSlotLoad", "saSlotLaunch", "saSlotPoll", "saSlotResults",
+           "saSetSweepCTAs"]

@@ -58,20 +58,32 @@ def _place_uniform(rng, n, nx, ny, margin, min_sep=0.0):
     hiy = float(ny - margin - 1)
     if min_sep <= 0.0:
         return rng.uniform(lo, hix, n), rng.uniform(lo, hiy, n)
+    # rejection sampling; accepted points are binned in min_sep cells so that
+    # a candidate is checked against the 3 x 3 neighbouring cells only
     xs, ys = [], []
+    grid = {}
+    s2 = min_sep * min_sep
     tries = 0
     while len(xs) < n and tries < 200 * n:
         tries += 1
         x = rng.uniform(lo, hix)
         y = rng.uniform(lo, hiy)
+        cx, cy = int(x // min_sep), int(y // min_sep)
         ok = True
-        for (a, b) in zip(xs, ys):
-            if (a - x) ** 2 + (b - y) ** 2 < min_sep * min_sep:
-                ok = False
+        for gx in (cx - 1, cx, cx + 1):
+            for gy in (cy - 1, cy, cy + 1):
+                for (a, b) in grid.get((gx, gy), ()):
+                    if (a - x) ** 2 + (b - y) ** 2 < s2:
+                        ok = False
+                        break
+                if not ok:
+                    break
+            if not ok:
                 break
         if ok:
             xs.append(x)
             ys.append(y)
+            grid.setdefault((cx, cy), []).append((x, y))
     return numpy.array(xs), numpy.array(ys)
 
 
@@ -196,11 +208,24 @@ def fitter_kwargs(cfg, spline=None):
     return dict(model="spline3D", spline=spline)
 
 
-def make_workload(cfg, frames=None, nx=None, ny=None, seed=None, n_emitters=None):
+_SPLINES = {}
+
+
+def cached_spline(seed):
+    if seed not in _SPLINES:
+        _SPLINES[seed] = make_spline(seed)
+    return _SPLINES[seed]
+
+
+def make_workload(cfg, frames=None, nx=None, ny=None, seed=None, n_emitters=None, camera_seed=None,
+                  min_sep=4.0):
     """Return a dict with per-frame images, backgrounds, truth and initial guesses.
 
     images[f] and backgrounds[f] are float64 (ny, nx) arrays in photo-electrons;
-    guesses[f] is the dict of columns for newPeaks(..., "hdf5").
+    guesses[f] is the dict of columns for newPeaks(..., "hdf5").  camera_seed
+    fixes the camera (sCMOS calibration, spline PSF) independently of the
+    frame content, as for frames of one camera in a request stream.
+    min_sep is the minimum emitter separation (px) of configuration 0.
     """
     c = dict(CONFIGS[cfg])
     if frames is not None:
@@ -216,19 +241,20 @@ def make_workload(cfg, frames=None, nx=None, ny=None, seed=None, n_emitters=None
     out = dict(cfg=cfg, model=c["model"], nx=nx, ny=ny, roi=roi, images=[], backgrounds=[],
                truth=[], guesses=[], rqe=numpy.ones((ny, nx)), scmos_cal=numpy.zeros((ny, nx)))
     spline = None
+    cam = rng if camera_seed is None else numpy.random.default_rng(camera_seed)
     if cfg == 3:
-        spline = make_spline(seed)
+        spline = make_spline(seed) if camera_seed is None else cached_spline(camera_seed)
         out["spline"] = spline
     if cfg == 2:
-        offset = rng.normal(100.0, 2.0, size=(ny, nx))
-        variance = rng.gamma(2.0, 2.0, size=(ny, nx))
-        gain = rng.normal(2.0, 0.05, size=(ny, nx))
+        offset = cam.normal(100.0, 2.0, size=(ny, nx))
+        variance = cam.gamma(2.0, 2.0, size=(ny, nx))
+        gain = cam.normal(2.0, 0.05, size=(ny, nx))
         out["scmos_cal"] = variance / (gain * gain)
     area_um2 = (nx * PIXEL_UM) * (ny * PIXEL_UM)
     for f in range(c["frames"]):
         if cfg == 0:
             n = 200 if n_emitters is None else n_emitters
-            x, y = _place_uniform(rng, n, nx, ny, margin, min_sep=4.0)
+            x, y = _place_uniform(rng, n, nx, ny, margin, min_sep=min_sep)
             n = x.size
             sx = numpy.full(n, 1.3)
             sy = sx.copy()
@@ -299,11 +325,27 @@ def make_workload(cfg, frames=None, nx=None, ny=None, seed=None, n_emitters=None
     return out
 
 
-def serving_requests(n_requests=10000, rate_hz=2000.0, seed=4):
+def serving_requests(n_requests=10000, rate_hz=2000.0, seed=4, sizes=(128, 256, 512, 2048),
+                     models=("2d", "3d", "Z", "spline3D")):
     """Request stream of cfg 4: arrival times, frame size, density and model per request."""
     rng = numpy.random.default_rng(seed)
     t = numpy.cumsum(rng.exponential(1.0 / rate_hz, n_requests))
-    sizes = rng.choice([128, 256, 512, 2048], n_requests)
+    sizes = rng.choice(list(sizes), n_requests)
     dens = numpy.exp(rng.uniform(math.log(0.05), math.log(2.0), n_requests))
-    models = rng.choice(["2d", "3d", "Z", "spline3D"], n_requests)
+    models = rng.choice(list(models), n_requests)
     return dict(t=t, size=sizes, density=dens, model=models)
+
+
+MODEL_CFG = {"2d": 0, "3d": 1, "Z": 2, "spline3D": 3}
+
+
+def serving_frame(model, size, density, seed):
+    """One request of the serving stream: a single frame of `size` x `size`
+    pixels at `density` emitters / um^2 (uniform positions, no minimum
+    separation) with the model's configuration parameters; the camera
+    (calibration, spline) is fixed per model and size.  Returns the
+    make_workload dict of one frame."""
+    cfg = MODEL_CFG[model]
+    n = max(1, int(round(density * (size * PIXEL_UM) ** 2)))
+    return make_workload(cfg, frames=1, nx=size, ny=size, seed=seed, n_emitters=n,
+                         camera_seed=10000 + 97 * cfg + size, min_sep=0.0)
