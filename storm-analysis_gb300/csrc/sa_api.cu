@@ -511,7 +511,8 @@ void roi_index(Engine* e, int roi) {
 
 void finish_geometry(Engine* e) {
   ModelCfg& c = e->cfg;
-  if (c.dil < 0) c.dil = 2;
+  if (c.dil < 0) c.dil = 3;
+  if (c.dil_late < 0 || c.dil_late > c.dil) c.dil_late = c.dil;
   c.cell = c.roi + 2 * c.dil;
   // keep the grid small enough for shared memory
   while ((long long)((c.nx + c.cell - 1) / c.cell) * ((c.ny + c.cell - 1) / c.cell) > 40000) c.cell *= 2;
@@ -531,7 +532,11 @@ saFitData* new_handle(const double* rqe, const double* scmos, double tol, int nx
   e->cfg.ny = ny;
   e->cfg.tol = tol;
   e->cfg.min_height = -1.0;   // multi_fit.c:965
-  e->cfg.dil = -1;
+  e->cfg.dil = -1;                // 3 pixels (finish_geometry) unless set
+  // After 20 sweeps most peaks have converged and the rest move little:
+  // dependencies then use the undilated footprint (an anchor move escapes).
+  e->cfg.dil_late = 0;
+  e->cfg.dil_switch = 20;
   e->npix = (long long)nx * ny;
   e->rqe_h.assign(rqe, rqe + e->npix);
   e->scmos_h.assign(scmos, scmos + e->npix);

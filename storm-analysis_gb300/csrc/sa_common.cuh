@@ -82,6 +82,8 @@ struct ModelCfg {
   double zmin, zmax;
   double min_height;
   int force_serial;      // 1: every frame runs its peaks strictly in index order
+  int dil_late;          // dilation from sweep dil_switch on (<= dil)
+  int dil_switch;
 };
 
 // Per-frame control block of the device state machine.
@@ -102,6 +104,7 @@ struct FrameCtl {
   int attempts;
   int reruns_total;      // sweep attempts beyond the first, all sweeps
   int barriers_total;    // escaped peaks made barriers, all sweeps
+  int dil;               // footprint dilation of the current sweep
   long long ctr[NCOUNTERS];
 };
 

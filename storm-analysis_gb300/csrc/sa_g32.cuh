@@ -326,7 +326,7 @@ __device__ inline float g32_absolute(const ModelCfg& cfg, const FrameSet<T>& fs,
 // Returns true if the step escaped its footprint (nothing changed).
 template <typename T>
 __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase, PeakRec* recp,
-                            bool unbounded, WarpWS<T>& ws, int* ctr_out, int lane) {
+                            bool unbounded, int dil, WarpWS<T>& ws, int* ctr_out, int lane) {
   if constexpr (sizeof(T) != 4) {
     return false;
   } else {
@@ -432,7 +432,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
             w.lambda = lam * LAMBDA_UP;
             w.status = ERROR;
             act = ACT_CONTINUE;
-          } else if (!unbounded && (abs(t.xi - orig.xi) > cfg.dil || abs(t.yi - orig.yi) > cfg.dil)) {
+          } else if (!unbounded && (abs(t.xi - orig.xi) > dil || abs(t.yi - orig.yi) > dil)) {
             act = ACT_ESCAPE;
           } else {
             w = t;

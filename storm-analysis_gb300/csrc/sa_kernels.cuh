@@ -110,7 +110,7 @@ __device__ inline void load_base(const ModelCfg& cfg, const FrameSet<T>& fs, lon
 // Returns true if the step escaped its footprint (nothing changed).
 template <typename T>
 __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase, PeakRec* recp,
-                        bool unbounded, WarpWS<T>& ws, int* ctr_out, int lane) {
+                        bool unbounded, int dil, WarpWS<T>& ws, int* ctr_out, int lane) {
   // The start-of-step, working and trial records live in the warp's shared
   // workspace; only lane 0 writes them.
   if (lane < 8) {
@@ -287,7 +287,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
           w.lambda = lam * LAMBDA_UP;
           w.status = ERROR;
           act = ACT_CONTINUE;
-        } else if (!unbounded && (abs(t.xi - orig.xi) > cfg.dil || abs(t.yi - orig.yi) > cfg.dil)) {
+        } else if (!unbounded && (abs(t.xi - orig.xi) > dil || abs(t.yi - orig.yi) > dil)) {
           act = ACT_ESCAPE;
         } else {
           w = t;
@@ -452,7 +452,6 @@ __global__ void __launch_bounds__(128, G32 ? 6 : 5) k_sweep(ModelCfg cfg, FrameS
   const int wpb = blockDim.x >> 5;
   WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(cfg, cfg.nroi), cfg, cfg.nroi);
   const int gwarp = blockIdx.x * wpb + wib;
-  const int fp = 2 * cfg.roi + 2 * cfg.dil;   // overlap span of two dilated footprints
   int f = gwarp % fs.F;
   int misses = 0;
   while (misses < fs.F) {
@@ -474,6 +473,8 @@ __global__ void __launch_bounds__(128, G32 ? 6 : 5) k_sweep(ModelCfg cfg, FrameS
     misses = 0;
     const int base = fs.pk_off[f];
     const int start = c->start;
+    const int dil = c->dil;
+    const int span = cfg.roi + 2 * dil;   // anchors closer than this: dilated footprints overlap
     const unsigned a0 = fs.anchor0[base + r];
     const int ax = a0 & 0xffff, ay = a0 >> 16;
     bool barrier = c->serial != 0;
@@ -508,7 +509,7 @@ __global__ void __launch_bounds__(128, G32 ? 6 : 5) k_sweep(ModelCfg cfg, FrameS
                 if (cand < r && cand >= start) {
                   const unsigned b0 = fs.anchor0[base + cand];
                   const int bx = b0 & 0xffff, by = b0 >> 16;
-                  if (abs(bx - ax) < fp - cfg.roi && abs(by - ay) < fp - cfg.roi) q = cand;
+                  if (abs(bx - ax) < span && abs(by - ay) < span) q = cand;
                 }
               }
               unsigned m = __ballot_sync(0xffffffffu, q >= 0);
@@ -528,9 +529,9 @@ __global__ void __launch_bounds__(128, G32 ? 6 : 5) k_sweep(ModelCfg cfg, FrameS
     // -- the step
     const int li = fs.run[base + r];
     const bool esc =
-        G32 ? lm_step_g32(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, ws,
+        G32 ? lm_step_g32(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, dil, ws,
                           fs.stepctr + (size_t)(base + li) * NCOUNTERS, lane)
-            : lm_step(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, ws,
+            : lm_step(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, dil, ws,
                       fs.stepctr + (size_t)(base + li) * NCOUNTERS, lane);
     if (esc && lane == 0) {
       atomicMin(&c->escaped_min, r);
@@ -624,6 +625,7 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
       c->n_escaped = 0;
       c->n_barrier = 0;
       c->serial = cfg.force_serial;
+      c->dil = (c->sweeps >= cfg.dil_switch) ? cfg.dil_late : cfg.dil;
       c->attempts = 1;
       c->phase = nrun > 0 ? PH_IN_SWEEP : PH_IN_SWEEP;
     }
