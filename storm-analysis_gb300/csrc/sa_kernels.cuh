@@ -525,6 +525,14 @@ __global__ void __launch_bounds__(128, G32 ? 6 : 5) k_sweep(ModelCfg cfg, FrameS
       }
     }
     if (!ok) return;   // a wait timed out: err_flag is set, the host reports it
+    // A lower rank of this attempt escaped: every rank above it re-runs in
+    // the next attempt, so this one is skipped now (record and image stay
+    // as they are, nothing to roll back).
+    if (*((volatile int*)&c->escaped_min) < r) {
+      __syncwarp();
+      if (lane == 0) st_release(fs.done + base + r, epoch);
+      continue;
+    }
     __threadfence();
     // -- the step
     const int li = fs.run[base + r];
@@ -657,6 +665,13 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
       PeakRec cur, sn;
       load_rec(fs.pk + base + li, cur);
       load_rec(fs.snap + base + li, sn);
+      // ranks skipped after the escape (or escaped themselves) are untouched
+      bool same = true;
+      const long long* wa = reinterpret_cast<const long long*>(&cur);
+      const long long* wb = reinterpret_cast<const long long*>(&sn);
+#pragma unroll
+      for (int q = 0; q < (int)(sizeof(PeakRec) / 8); q++) same = same && (wa[q] == wb[q]);
+      if (same) continue;
       if (cur.added > 0) {
         SplinePos s = shape_tables(cfg, cur, ws, lane);
         add_peak(cfg, fs, fbase, cur, s, ws, -1, lane);
