@@ -737,9 +737,10 @@ __device__ inline void anchor_update(PeakRec& w) {
 }
 
 // Apply the solved step in each model's delta order (dao_fit.c:1777-1880,
-// cubic_fit.c:939-1005).
-__device__ inline void apply_update(const ModelCfg& cfg, PeakRec& w, const double* d) {
-  switch (cfg.model) {
+// cubic_fit.c:939-1005).  model is cfg.model (a constant where the caller
+// is compiled for one model).
+__device__ inline void apply_update(const ModelCfg& cfg, int model, PeakRec& w, const double* d) {
+  switch (model) {
     case M_2DFIXED:
     case M_SPLINE2D:
       w.p[PH] -= d[0]; w.p[PX] -= d[1]; w.p[PY] -= d[2]; w.p[PBG] -= d[3];
@@ -784,22 +785,22 @@ __device__ inline int base_check(const ModelCfg& cfg, const PeakRec& w) {
 
 // Model check with the width clamps of daoCheck2D / daoCheck3D
 // (dao_fit.c:1061-1119).
-__device__ inline int model_check(const ModelCfg& cfg, PeakRec& w) {
+__device__ inline int model_check(const ModelCfg& cfg, int model, PeakRec& w) {
   int c = base_check(cfg, w);
   if (c) return c;
-  if ((cfg.model == M_2D) || (cfg.model == M_3D)) {
+  if ((model == M_2D) || (model == M_3D)) {
     if (w.p[PXW] < cfg.wmin) w.p[PXW] = cfg.wmin;
     else if (w.p[PXW] > cfg.wmax) w.p[PXW] = cfg.wmax;
   }
-  if (cfg.model == M_3D) {
+  if (model == M_3D) {
     if (w.p[PYW] < cfg.wmin) w.p[PYW] = cfg.wmin;
     else if (w.p[PYW] > cfg.wmax) w.p[PYW] = cfg.wmax;
   }
   return 0;
 }
 
-__device__ __forceinline__ int check_for(const ModelCfg& cfg, PeakRec& w) {
-  return is_spline(cfg.model) ? base_check(cfg, w) : model_check(cfg, w);
+__device__ __forceinline__ int check_for(const ModelCfg& cfg, int model, PeakRec& w) {
+  return is_spline(model) ? base_check(cfg, w) : model_check(cfg, model, w);
 }
 
 // Prepare the shape tables of peak w (all lanes) and return its spline
@@ -1112,9 +1113,10 @@ __device__ inline int solve_damped<float>(WarpWS<float>& ws, int k, double lam, 
 }
 
 // d width / dz factors of the Z model (dao_fit.c:904-916).
-__device__ inline void z_factors(const ModelCfg& cfg, const PeakRec& w, double& gx, double& gy) {
+__device__ inline void z_factors(const ModelCfg& cfg, int model, const PeakRec& w, double& gx,
+                                 double& gy) {
   gx = gy = 0.0;
-  if (cfg.model != M_Z) return;
+  if (model != M_Z) return;
   double z0 = (w.p[PZ] - cfg.wx[1]) / cfg.wx[2];
   double z1 = z0 * z0, z2 = z1 * z0;
   double zt = 2.0 * z0 + 3.0 * cfg.wx[3] * z1 + 4.0 * cfg.wx[4] * z2;

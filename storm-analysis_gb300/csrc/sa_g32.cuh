@@ -7,8 +7,8 @@
 // is carried in float-float ("ff", ~48 bits) from exact inputs:
 //   * the fit image and a copy of the data are fixed point, so f - x is
 //     exact and becomes an ff residual without rounding;
-//   * the shape factors exp(-t^2 w) are evaluated in FP64 per ROI row and
-//     column (2 * roi exponentials per table) and kept as ff pairs;
+//   * the shape factors exp(-t^2 w) are evaluated in ff per ROI row and
+//     column (2 * roi exponentials per table, ff_exp) and kept as ff pairs;
 //   * the change of the error for a trial at the same ROI anchor is
 //     summed per pixel as  df * t1 + 2 x (r - log1p r),  t1 = 2 (f0 - x)/f0,
 //     r = df / f0, with df = h1 psf1 - h0 psf0 (+ background change) in ff:
@@ -32,15 +32,16 @@ enum { ACT_EVAL = 0, ACT_CONTINUE = 1, ACT_BREAK = 2, ACT_BREAK_ADDED = 3, ACT_E
 //   2d      [ps, ps a1, ps b1, ps (a2+b2), rqe] (:409-467)
 //   3d      [ps, ps a1, ps a2, ps b1, ps b2, rqe] (:811-871)
 //   Z       [ps, ps a1, ps b1, ps (a2+b2), rqe] (:883-958)
+template <int M>
 __device__ inline void g32_grad_tables(const ModelCfg& cfg, const PeakRec& w, double gx, double gy,
                                        float* g, int ts, int lane) {
   const G32Axes ax = g32_axes(cfg, w);
-  const bool one_width = (cfg.model == M_2DFIXED) || (cfg.model == M_2D);
+  constexpr bool one_width = (M == M_2DFIXED) || (M == M_2D);
   const ff H = ff_from_double(w.p[PH]);
   const ff H2 = ff{2.0f * H.h, 2.0f * H.l};
   const ff HX = ff_mul(H2, ax.wx), HY = ff_mul(H2, one_width ? ax.wx : ax.wy);   // 2 h w
-  const ff NX = (cfg.model == M_Z) ? ff_neg(ff_mul(H, ff_from_double(gx))) : ff_neg(H);
-  const ff NY = (cfg.model == M_Z) ? ff_neg(ff_mul(H, ff_from_double(gy))) : ff_neg(H);
+  const ff NX = (M == M_Z) ? ff_neg(ff_mul(H, ff_from_double(gx))) : ff_neg(H);
+  const ff NY = (M == M_Z) ? ff_neg(ff_mul(H, ff_from_double(gy))) : ff_neg(H);
   for (int i = lane; i < cfg.roi; i += 32) {
     const ff tx = ff_add_f(ax.xo, (float)i), ty = ff_add_f(ax.yo, (float)i);
     ff v = ff_mul(HX, tx);
@@ -65,6 +66,15 @@ __device__ __forceinline__ float* g32_jh(WarpWS<float>& ws) { return reinterpret
 
 __device__ __forceinline__ ff shfl_ff(ff v, int src) {
   return ff{__shfl_sync(0xffffffffu, v.h, src), __shfl_sync(0xffffffffu, v.l, src)};
+}
+
+// The FP64 Cholesky of the ff normal equations (lane 0).  Kept out of line:
+// it is the rare path, and its arrays would otherwise weigh on the register
+// allocation of the whole step.
+static __device__ __noinline__ int solve_g32_fallback(const float* jh, int k, double lam, double* out) {
+  double jd[36];
+  for (int i = 0; i < 36; i++) jd[i] = (double)jh[i] + (double)jh[36 + i];
+  return solve_fp64_lane0(jd, k, lam, out);
 }
 
 // Damped solve (H + lam diag H) d = b of the FP32 Gaussian step
@@ -150,9 +160,10 @@ __device__ inline int solve_g32(WarpWS<float>& ws, int k, double lam, double* ou
     }
   }
   if (lane == 0 && status == 2) {
-    double jd[36];
-    for (int i = 0; i < 36; i++) jd[i] = (double)jh[i] + (double)jh[36 + i];
-    status = solve_fp64_lane0(jd, k, lam, out);
+    double o[MAX_JAC];
+    status = solve_g32_fallback(jh, k, lam, o);
+#pragma unroll
+    for (int j = 0; j < MAX_JAC; j++) out[j] = o[j];
   }
   return status;
 }
@@ -177,40 +188,68 @@ __device__ __forceinline__ void g32_load(const ModelCfg& cfg, const FrameSet<T>&
   v.rq = (float)__ldg(fs.rqe + k);
 }
 
-// Pass 1 over the ROI for model M: start error terms, t1 / f0 per pixel,
-// ff gradient and FP32 Hessian partial sums of this lane.
+// Per-pixel state of the step's start, from the loaded pixel: f0 = f + bg /
+// cnt and rho = f0 - x, exact up to the division (multi_fit.c:143; the data
+// are kept in fixed point for this), t1 = 2 rho / f0, and the start error
+// term.
+__device__ __forceinline__ void g32_pixel_state(const G32Pix& v, int p, WarpWS<float>& ws, float& devf,
+                                                bool& fail) {
+  const ff bgc = ff_div(ff_from_fixed(v.B), ff{(float)v.C, 0.0f});
+  const ff rho = ff_add(ff_from_fixed(v.F - v.X), bgc);
+  const ff f0 = ff_add(ff_from_fixed(v.F), bgc);
+  if (!(f0.h > 0.0f)) fail = true;
+  else devf += dev_res(rho.h, v.x);
+  const ff t1 = ff_div(ff{2.0f * rho.h, 2.0f * rho.l}, f0);
+  ws.t1h[p] = t1.h;
+  ws.t1l[p] = t1.l;
+  ws.f0g[p] = f0.h;
+  ws.Xs[p] = v.x;
+  ws.Rs[p] = v.rq;
+  ws.Cs[p] = (float)v.C;
+}
+
+// Pass 1a: the ROI's pixels are loaded G32_GROUP per lane at a time (all
+// loads of a group in flight together) and their start state goes to the
+// warp workspace; returns the lane's start error terms.
+constexpr int G32_GROUP = 4;
+
+template <typename T>
+__device__ inline void g32_gather(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
+                                  const PeakRec& o, WarpWS<T>& ws, int lane, float& devf, bool& fail) {
+  if constexpr (sizeof(T) == 4) {
+    for (int p0 = lane; p0 < cfg.nroi; p0 += 32 * G32_GROUP) {
+      G32Pix v[G32_GROUP];
+#pragma unroll
+      for (int j = 0; j < G32_GROUP; j++) {
+        const int p = p0 + 32 * j;
+        if (p < cfg.nroi) g32_load(cfg, fs, fbase, o.xi, o.yi, p, v[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < G32_GROUP; j++) {
+        const int p = p0 + 32 * j;
+        if (p < cfg.nroi) g32_pixel_state(v[j], p, ws, devf, fail);
+      }
+    }
+  }
+}
+
+// Pass 1b over the ROI for model M: ff gradient and FP32 Hessian partial
+// sums of this lane, from the start state in the warp workspace.
 template <int M, typename T>
 __device__ inline void g32_pass1(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
                                  const PeakRec& o, WarpWS<T>& ws, int lane, ff (&g)[8],
-                                 float (&acc)[32], float& devf, bool& fail) {
+                                 float (&acc)[32]) {
   constexpr int K = (M == M_2DFIXED) ? 4 : ((M == M_3D) ? 6 : 5);
   const int ts = ws.ts;
   const float* t0 = ws.tab0;
   const float* gt = ws.tab1;
-  G32Pix cur, nxt;
-  int p = lane;
-  if (p < cfg.nroi) g32_load(cfg, fs, fbase, o.xi, o.yi, p, cur);
-  for (; p < cfg.nroi; p += 32) {
-    // the next pixel's loads are issued before this pixel's stores
-    if (p + 32 < cfg.nroi) g32_load(cfg, fs, fbase, o.xi, o.yi, p + 32, nxt);
+  for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
     roi_rc(fs.roi_xy, p, rx, ry);
-    // f0 = f + bg / cnt and rho = f0 - x, exact up to the division
-    // (multi_fit.c:143); the data are kept in fixed point for this
-    const ff bgc = ff_div(ff_from_fixed(cur.B), ff{(float)cur.C, 0.0f});
-    const ff rho = ff_add(ff_from_fixed(cur.F - cur.X), bgc);
-    const ff f0 = ff_add(ff_from_fixed(cur.F), bgc);
-    if (!(f0.h > 0.0f)) fail = true;
-    else devf += dev_res(rho.h, cur.x);
-    const ff t1 = ff_div(ff{2.0f * rho.h, 2.0f * rho.l}, f0);
-    ws.t1h[p] = t1.h;
-    ws.t1l[p] = t1.l;
-    ws.f0g[p] = f0.h;
-    ws.Xs[p] = cur.x;
-    ws.Rs[p] = cur.rq;
-    ws.Cs[p] = (float)cur.C;
-    const float t2 = __fdiv_rn(2.0f * cur.x, f0.h * f0.h);
-    const ff ps = ff_mul_f(g32_psf(t0, ts, rx, ry), cur.rq);
+    const ff t1{ws.t1h[p], ws.t1l[p]};
+    const float f0h = ws.f0g[p], xv = ws.Xs[p], rq = ws.Rs[p];
+    const float t2 = __fdiv_rn(2.0f * xv, f0h * f0h);
+    const ff ps = ff_mul_f(g32_psf(t0, ts, rx, ry), rq);
     const ff u = ff_mul(t1, ps);
     const ff A1{gt[rx], gt[ts + rx]}, A2{gt[2 * ts + rx], gt[3 * ts + rx]};
     const ff B1{gt[4 * ts + ry], gt[5 * ts + ry]}, B2{gt[6 * ts + ry], gt[7 * ts + ry]};
@@ -237,14 +276,13 @@ __device__ inline void g32_pass1(const ModelCfg& cfg, const FrameSet<T>& fs, lon
         jf[3] = ps.h * W.h;
       }
     }
-    g[K - 1] = ff_add(g[K - 1], ff_mul_f(t1, cur.rq));
-    jf[K - 1] = cur.rq;
+    g[K - 1] = ff_add(g[K - 1], ff_mul_f(t1, rq));
+    jf[K - 1] = rq;
 #pragma unroll
     for (int l = 0; l < K; l++) {
 #pragma unroll
       for (int m = l; m < K; m++) acc[l * K - (l * (l - 1)) / 2 + (m - l)] += t2 * jf[l] * jf[m];
     }
-    cur = nxt;
   }
 }
 
@@ -323,11 +361,12 @@ __device__ inline float g32_absolute(const ModelCfg& cfg, const FrameSet<T>& fs,
   return devf;
 }
 
-// Returns true if the step escaped its footprint (nothing changed).
-template <typename T>
+// The step of a peak of Gaussian model M (cfg.model == M).  Returns true
+// if the step escaped its footprint (nothing changed).
+template <int M, typename T>
 __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase, PeakRec* recp,
                             bool unbounded, int dil, WarpWS<T>& ws, int* ctr_out, int lane) {
-  if constexpr (sizeof(T) != 4) {
+  if constexpr (sizeof(T) != 4 || M > M_Z) {
     return false;
   } else {
     if (lane < 8) {
@@ -335,15 +374,18 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     }
     __syncwarp();
     const PeakRec& orig = *ws.orig;
-    const int k = cfg.jac;
-    const int nhes = k * (k + 1) / 2;
+    constexpr int k = (M == M_2DFIXED) ? 4 : ((M == M_3D) ? 6 : 5);
+    constexpr int nhes = k * (k + 1) / 2;
     const int ts = ws.ts;
 
     // -- 1. starting error, gradient / Hessian, subtract (multi_fit.c:1107-1142)
+    float devf = 0.0f;
+    bool fail = false;
+    g32_gather(cfg, fs, fbase, orig, ws, lane, devf, fail);
     g32_tables(cfg, orig, ws.tab0, ts, lane);
     double gxd, gyd;
-    z_factors(cfg, orig, gxd, gyd);
-    g32_grad_tables(cfg, orig, gxd, gyd, ws.tab1, ts, lane);
+    z_factors(cfg, M, orig, gxd, gyd);
+    g32_grad_tables<M>(cfg, orig, gxd, gyd, ws.tab1, ts, lane);
     __syncwarp();
     ff g[8];
 #pragma unroll
@@ -351,14 +393,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     float acc[32];
 #pragma unroll
     for (int i = 0; i < 32; i++) acc[i] = 0.0f;
-    float devf = 0.0f;
-    bool fail = false;
-    switch (cfg.model) {
-      case M_2DFIXED: g32_pass1<M_2DFIXED>(cfg, fs, fbase, orig, ws, lane, g, acc, devf, fail); break;
-      case M_2D: g32_pass1<M_2D>(cfg, fs, fbase, orig, ws, lane, g, acc, devf, fail); break;
-      case M_3D: g32_pass1<M_3D>(cfg, fs, fbase, orig, ws, lane, g, acc, devf, fail); break;
-      default: g32_pass1<M_Z>(cfg, fs, fbase, orig, ws, lane, g, acc, devf, fail); break;
-    }
+    g32_pass1<M>(cfg, fs, fbase, orig, ws, lane, g, acc);
     // The reference subtracts the peak here (multi_fit.c:1141) and adds the
     // accepted trial back.  No other warp touches this ROI during the step,
     // so the subtraction is deferred to the write-back, which applies the
@@ -385,10 +420,12 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     // -- 2. LM loop (multi_fit.c:1145-1325); lane 0 holds the scalar state.
     PeakRec& w = *ws.w;
     double se = 0.0;
-    int ctr[NCOUNTERS];
-#pragma unroll
-    for (int i = 0; i < NCOUNTERS; i++) ctr[i] = 0;
+    // the step's counters (lane 0) live in the warp workspace, not in
+    // registers that every lane would carry through the loop
+    int* ctr = reinterpret_cast<int*>(ws.scratch);
     if (lane == 0) {
+#pragma unroll
+      for (int i = 0; i < NCOUNTERS; i++) ctr[i] = 0;
       w = orig;
       if (!fail) w.error = dev0;
       else ctr[C_STARTFAIL]++;
@@ -424,10 +461,11 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
         } else {
           PeakRec& t = *ws.t;
           t = w;
-          apply_update(cfg, t, b);
-          const int c = check_for(cfg, t);
+          apply_update(cfg, M, t, b);
+          const int c = check_for(cfg, M, t);
           if (c) {
-            ctr[c == 1 ? C_MARGIN : C_NEGH]++;
+            if (c == 1) ctr[C_MARGIN]++;
+            else ctr[C_NEGH]++;
             w = orig;                      // mFitResetPeak multi_fit.c:1788-1798
             w.lambda = lam * LAMBDA_UP;
             w.status = ERROR;

@@ -124,7 +124,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
   // -- 1. starting error, Jacobian / Hessian, subtract (multi_fit.c:1107-1142)
   SplinePos s0 = shape_tables(cfg, orig, ws, lane);
   double gxd, gyd;
-  z_factors(cfg, orig, gxd, gyd);
+  z_factors(cfg, cfg.model, orig, gxd, gyd);
   const T gx = (T)gxd, gy = (T)gyd;
   T acc[32];
 #pragma unroll
@@ -279,10 +279,11 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
       } else {
         PeakRec& t = *ws.t;
         t = w;
-        apply_update(cfg, t, b);
-        const int c = check_for(cfg, t);
+        apply_update(cfg, cfg.model, t, b);
+        const int c = check_for(cfg, cfg.model, t);
         if (c) {
-          ctr[c == 1 ? C_MARGIN : C_NEGH]++;
+          if (c == 1) ctr[C_MARGIN]++;
+          else ctr[C_NEGH]++;
           w = orig;                      // mFitResetPeak multi_fit.c:1788-1798
           w.lambda = lam * LAMBDA_UP;
           w.status = ERROR;
@@ -443,9 +444,10 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
 // k_sweep: persistent warps over the run ranks of all frames in IN_SWEEP
 // ---------------------------------------------------------------------------
 
-// G32: the FP32 Gaussian step (lm_step_g32); otherwise lm_step.
-template <typename T, bool G32>
-__global__ void __launch_bounds__(128, G32 ? 6 : 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
+// G32 >= 0: the FP32 Gaussian step (lm_step_g32) of model G32 (one
+// instantiation per model); G32 < 0: lm_step.
+template <typename T, int G32>
+__global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
   extern __shared__ __align__(16) char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -536,11 +538,13 @@ __global__ void __launch_bounds__(128, G32 ? 6 : 5) k_sweep(ModelCfg cfg, FrameS
     __threadfence();
     // -- the step
     const int li = fs.run[base + r];
-    const bool esc =
-        G32 ? lm_step_g32(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, dil, ws,
-                          fs.stepctr + (size_t)(base + li) * NCOUNTERS, lane)
-            : lm_step(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, dil, ws,
-                      fs.stepctr + (size_t)(base + li) * NCOUNTERS, lane);
+    bool esc;
+    if constexpr (G32 >= 0)
+      esc = lm_step_g32<G32>(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, dil, ws,
+                             fs.stepctr + (size_t)(base + li) * NCOUNTERS, lane);
+    else
+      esc = lm_step(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, dil, ws,
+                    fs.stepctr + (size_t)(base + li) * NCOUNTERS, lane);
     if (esc && lane == 0) {
       atomicMin(&c->escaped_min, r);
       int slot = atomicAdd(&c->n_escaped, 1);
@@ -882,7 +886,7 @@ __global__ void k_newpeaks(ModelCfg cfg, FrameSet<T> fs, const double* rows, int
     PeakRec w = new_peak_rec(cfg, rows + (size_t)i * ncol, ptype);
     const int f = frames[i];
     const long long fbase = (long long)f * fs.npix;
-    const int chk = check_for(cfg, w);
+    const int chk = check_for(cfg, cfg.model, w);
     if (chk) {
       w.status = ERROR;
       if (lane == 0) {
@@ -1022,7 +1026,7 @@ __global__ void k_peak_props(ModelCfg cfg, FrameSet<T> fs, const int* slots, con
     SplinePos s = shape_tables(cfg, w, ws, lane);
     double ps = 0.0, ps2 = 0.0, bs = 0.0;
     double gxd, gyd;
-    z_factors(cfg, w, gxd, gyd);
+    z_factors(cfg, cfg.model, w, gxd, gyd);
     T acc[32];
     for (int q = 0; q < 32; q++) acc[q] = (T)0;
     for (int p = lane; p < cfg.nroi; p += 32) {

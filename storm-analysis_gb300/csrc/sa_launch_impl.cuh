@@ -11,6 +11,23 @@ constexpr int SWEEP_BLOCK = 128;    // 4 warps, one peak each
 constexpr int CTA_BLOCK = 1024;     // per-frame kernels
 constexpr int AUX_BLOCK = 256;      // warp-per-peak auxiliary kernels
 
+// The sweep kernel of a configuration: the FP32 Gaussian models have one
+// instantiation each, everything else shares the generic step.
+template <typename T>
+void (*sweep_kernel(const ModelCfg& cfg))(ModelCfg, FrameSet<T>, int) {
+  if constexpr (sizeof(T) == 4) {
+    if (gauss32<T>(cfg)) {
+      switch (cfg.model) {
+        case M_2DFIXED: return k_sweep<T, M_2DFIXED>;
+        case M_2D: return k_sweep<T, M_2D>;
+        case M_3D: return k_sweep<T, M_3D>;
+        default: return k_sweep<T, M_Z>;
+      }
+    }
+  }
+  return k_sweep<T, -1>;
+}
+
 template <typename T>
 cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* sweep_smem,
                                  size_t* cta_smem, size_t* warp_smem) {
@@ -27,7 +44,6 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
   const size_t s_cta = ws0 * (CTA_BLOCK / 32) > grid_bytes ? ws0 * (CTA_BLOCK / 32) : grid_bytes;
   const size_t s_aux = ws0 * (AUX_BLOCK / 32);
   if (s_sweep > (size_t)max_smem || s_cta > (size_t)max_smem) return cudaErrorInvalidConfiguration;
-  const bool g32 = gauss32<T>(cfg);
   // The limit is a property of the kernel, shared by every handle of the
   // process (handles of different models and ROI sizes may run side by
   // side), so it is raised to the device maximum rather than to this
@@ -39,15 +55,14 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 max_smem - (int)a.sharedSizeBytes);
   };
-  e = raise_limit((const void*)(g32 ? k_sweep<T, true> : k_sweep<T, false>));
+  e = raise_limit((const void*)sweep_kernel<T>(cfg));
   if (e != cudaSuccess) return e;
   e = raise_limit((const void*)k_prepare<T>);
   if (e != cudaSuccess) return e;
   e = raise_limit((const void*)k_post<T>);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g32 ? k_sweep<T, true> : k_sweep<T, false>,
-                                                    SWEEP_BLOCK, s_sweep);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T>(cfg), SWEEP_BLOCK, s_sweep);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   *sweep_grid = nsm * per_sm;
@@ -66,8 +81,7 @@ cudaError_t Launch<T>::prepare(const ModelCfg& cfg, const FrameSet<T>& fs, size_
 template <typename T>
 cudaError_t Launch<T>::sweep(const ModelCfg& cfg, const FrameSet<T>& fs, int epoch, int grid,
                              size_t smem, cudaStream_t s) {
-  if (gauss32<T>(cfg)) k_sweep<T, true><<<grid, SWEEP_BLOCK, smem, s>>>(cfg, fs, epoch);
-  else k_sweep<T, false><<<grid, SWEEP_BLOCK, smem, s>>>(cfg, fs, epoch);
+  sweep_kernel<T>(cfg)<<<grid, SWEEP_BLOCK, smem, s>>>(cfg, fs, epoch);
   return cudaGetLastError();
 }
 
