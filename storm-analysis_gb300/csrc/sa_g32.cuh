@@ -171,7 +171,7 @@ __device__ inline int solve_g32(WarpWS<float>& ws, int k, double lam, double* ou
 struct G32Pix {
   long long F, B, X;
   int C;
-  float x, rq;
+  float rq;
 };
 
 template <typename T>
@@ -184,7 +184,6 @@ __device__ __forceinline__ void g32_load(const ModelCfg& cfg, const FrameSet<T>&
   v.B = __ldcg(fs.bg + fbase + k);
   v.C = __ldcg(fs.cnt + fbase + k);
   v.X = __ldg(fs.xq + fbase + k);
-  v.x = (float)__ldg(fs.x + fbase + k);
   v.rq = (float)__ldg(fs.rqe + k);
 }
 
@@ -194,16 +193,19 @@ __device__ __forceinline__ void g32_load(const ModelCfg& cfg, const FrameSet<T>&
 // term.
 __device__ __forceinline__ void g32_pixel_state(const G32Pix& v, int p, WarpWS<float>& ws, float& devf,
                                                 bool& fail) {
+  // the data value for the FP32 terms, rounded from its fixed-point copy
+  // (one load less per pixel than reading the float copy)
+  const float vx = fx_to_float(v.X);
   const ff bgc = ff_div(ff_from_fixed(v.B), ff{(float)v.C, 0.0f});
   const ff rho = ff_add(ff_from_fixed(v.F - v.X), bgc);
   const ff f0 = ff_add(ff_from_fixed(v.F), bgc);
   if (!(f0.h > 0.0f)) fail = true;
-  else devf += dev_res(rho.h, v.x);
+  else devf += dev_res(rho.h, vx);
   const ff t1 = ff_div(ff{2.0f * rho.h, 2.0f * rho.l}, f0);
   ws.t1h[p] = t1.h;
   ws.t1l[p] = t1.l;
   ws.f0g[p] = f0.h;
-  ws.Xs[p] = v.x;
+  ws.Xs[p] = vx;
   ws.Rs[p] = v.rq;
   ws.Cs[p] = (float)v.C;
 }
@@ -211,7 +213,7 @@ __device__ __forceinline__ void g32_pixel_state(const G32Pix& v, int p, WarpWS<f
 // Pass 1a: the ROI's pixels are loaded G32_GROUP per lane at a time (all
 // loads of a group in flight together) and their start state goes to the
 // warp workspace; returns the lane's start error terms.
-constexpr int G32_GROUP = 4;
+constexpr int G32_GROUP = 2;
 
 template <typename T>
 __device__ inline void g32_gather(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
@@ -361,18 +363,35 @@ __device__ inline float g32_absolute(const ModelCfg& cfg, const FrameSet<T>& fs,
   return devf;
 }
 
-// The step of a peak of Gaussian model M (cfg.model == M).  Returns true
-// if the step escaped its footprint (nothing changed).
+// What the step of a peak needs before it reads the fit image: its record
+// (ws.orig), its shape tables (tab0) and Jacobian factors (tab1).  Only the
+// peak's own step changes its record, so this runs before the dependency
+// waits of the sweep and overlaps them.
+template <int M, typename T>
+__device__ inline void g32_prologue(const ModelCfg& cfg, const PeakRec* recp, WarpWS<T>& ws, int lane) {
+  if constexpr (sizeof(T) == 4 && M <= M_Z) {
+    if (lane < 8) {
+      reinterpret_cast<double2*>(ws.orig)[lane] = __ldcg(reinterpret_cast<const double2*>(recp) + lane);
+    }
+    __syncwarp();
+    const PeakRec& orig = *ws.orig;
+    g32_tables(cfg, orig, ws.tab0, ws.ts, lane);
+    double gxd, gyd;
+    z_factors(cfg, M, orig, gxd, gyd);
+    g32_grad_tables<M>(cfg, orig, gxd, gyd, ws.tab1, ws.ts, lane);
+    __syncwarp();
+  }
+}
+
+// The step of a peak of Gaussian model M (cfg.model == M), after
+// g32_prologue.  Returns true if the step escaped its footprint (nothing
+// changed).
 template <int M, typename T>
 __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase, PeakRec* recp,
                             bool unbounded, int dil, WarpWS<T>& ws, int* ctr_out, int lane) {
   if constexpr (sizeof(T) != 4 || M > M_Z) {
     return false;
   } else {
-    if (lane < 8) {
-      reinterpret_cast<double2*>(ws.orig)[lane] = __ldcg(reinterpret_cast<const double2*>(recp) + lane);
-    }
-    __syncwarp();
     const PeakRec& orig = *ws.orig;
     constexpr int k = (M == M_2DFIXED) ? 4 : ((M == M_3D) ? 6 : 5);
     constexpr int nhes = k * (k + 1) / 2;
@@ -382,10 +401,6 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     float devf = 0.0f;
     bool fail = false;
     g32_gather(cfg, fs, fbase, orig, ws, lane, devf, fail);
-    g32_tables(cfg, orig, ws.tab0, ts, lane);
-    double gxd, gyd;
-    z_factors(cfg, M, orig, gxd, gyd);
-    g32_grad_tables<M>(cfg, orig, gxd, gyd, ws.tab1, ts, lane);
     __syncwarp();
     ff g[8];
 #pragma unroll

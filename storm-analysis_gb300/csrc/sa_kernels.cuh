@@ -479,6 +479,8 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
     const int span = cfg.roi + 2 * dil;   // anchors closer than this: dilated footprints overlap
     const unsigned a0 = fs.anchor0[base + r];
     const int ax = a0 & 0xffff, ay = a0 >> 16;
+    const int li = fs.run[base + r];
+    if constexpr (G32 >= 0) g32_prologue<G32>(cfg, fs.pk + base + li, ws, lane);
     bool barrier = c->serial != 0;
     bool ok = true;
     // -- dependencies
@@ -537,7 +539,6 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
     }
     __threadfence();
     // -- the step
-    const int li = fs.run[base + r];
     bool esc;
     if constexpr (G32 >= 0)
       esc = lm_step_g32<G32>(cfg, fs, (long long)f * fs.npix, fs.pk + base + li, barrier, dil, ws,
