@@ -713,6 +713,8 @@ __global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
   extern __shared__ __align__(16) char smem[];
   __shared__ long long s_ctr[NCOUNTERS];
   __shared__ int s_unconv;
+  __shared__ int s_nmove;
+  __shared__ int s_move[1024];
   const int f = blockIdx.x;
   FrameCtl* c = fs.ctl + f;
   if (c->phase != PH_IN_SWEEP) return;
@@ -731,15 +733,27 @@ __global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
   WarpWS<T> ws = warp_ws<T>(smem + (size_t)wid * warp_ws_bytes<T>(cfg, 0), cfg, 0);
   const long long fbase = (long long)f * fs.npix;
   // recenter (mFitRecenterPeaks multi_fit.c:1644-1690); order-free with
-  // fixed-point accumulation
+  // fixed-point accumulation.  The run ranks are scanned a thread each; the
+  // peaks that move their ROI are listed and then re-added a warp each.
   int lost = 0, margin = 0, negh = 0, unconv = 0;
-  for (int r = wid; r < nrun; r += 32) {
-    const int li = fs.run[base + r];
-    PeakRec rec;
-    load_rec(fs.pk + base + li, rec);
-    if (rec.status != RUNNING) continue;
-    const double dx = rec.p[PX] - rec.xi, dy = rec.p[PY] - rec.yi;
-    if ((dx < -0.25) || (dx > 1.25) || (dy < -0.25) || (dy > 1.25)) {
+  for (int c0 = 0; c0 < nrun; c0 += 1024) {
+    if (tid == 0) s_nmove = 0;
+    __syncthreads();
+    const int rr = c0 + tid;
+    if (rr < nrun) {
+      const PeakRec* q = fs.pk + base + fs.run[base + rr];
+      if (__ldcg(&q->status) == RUNNING) {
+        const double dx = __ldcg(&q->p[PX]) - __ldcg(&q->xi), dy = __ldcg(&q->p[PY]) - __ldcg(&q->yi);
+        if ((dx < -0.25) || (dx > 1.25) || (dy < -0.25) || (dy > 1.25)) s_move[atomicAdd(&s_nmove, 1)] = rr;
+        else unconv++;
+      }
+    }
+    __syncthreads();
+    const int nmove = s_nmove;
+    for (int m = wid; m < nmove; m += 32) {
+      const int li = fs.run[base + s_move[m]];
+      PeakRec rec;
+      load_rec(fs.pk + base + li, rec);
       SplinePos s = shape_tables(cfg, rec, ws, lane);
       add_peak(cfg, fs, fbase, rec, s, ws, -1, lane);
       __syncwarp();
@@ -760,9 +774,12 @@ __global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
         rec.added += 1;
       }
       __syncwarp();
-      if (lane == 0) fs.pk[base + li] = rec;
+      if (lane == 0) {
+        fs.pk[base + li] = rec;
+        if (rec.status == RUNNING) unconv++;
+      }
     }
-    if (lane == 0 && rec.status == RUNNING) unconv++;
+    __syncthreads();
   }
   // counters of this sweep's steps
   long long loc[NCOUNTERS];
@@ -780,6 +797,7 @@ __global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0 && v) atomicAdd(reinterpret_cast<unsigned long long*>(&s_ctr[i]), (unsigned long long)v);
   }
+  for (int o = 16; o > 0; o >>= 1) unconv += __shfl_xor_sync(0xffffffffu, unconv, o);
   if (lane == 0 && unconv) atomicAdd(&s_unconv, unconv);
   __threadfence();
   __syncthreads();
