@@ -194,10 +194,10 @@ def load_measured_peaks():
 
 def bytes_per_iteration(nroi):
     """Algorithmic bytes of one LM inner iteration of one peak: per ROI pixel
-    the start state (fit image and background words 8 + 8, count 4, data
-    8 + 4, rqe 4) read once and the fit-image / background update (8 + 8)
-    written once: 52 B."""
-    return 52 * nroi
+    the start state (fit image and background words 8 + 8, count 4, the
+    fixed-point data 8, rqe 4) read once and the fit-image / background
+    update (8 + 8) written once: 48 B."""
+    return 48 * nroi
 
 
 def peaks_rows(wl):
@@ -344,9 +344,12 @@ def run_ours(args, rank, world, local_rank):
     hbm_peak = peaks.get("hbm_gbs")
     alg_bytes = bytes_per_iteration(nroi) * iters if nroi else None
     hbm_achieved = alg_bytes / (sweep_ms / 1e3) / 1e9 if (alg_bytes and sweep_ms > 0) else None
+    # DRAM bytes per launch: the ncu capture's bytes per LM step of a first
+    # sweep times this step's average LM iterations per sweep launch
     traffic_launch = None
-    if traffic and traffic.get("dram_bytes_per_frame_first_sweep"):
-        traffic_launch = traffic["dram_bytes_per_frame_first_sweep"] * F
+    if traffic and traffic.get("dram_bytes_per_step_first_sweep") and sweep_launches:
+        traffic_launch = traffic["dram_bytes_per_step_first_sweep"] * iters / float(sweep_launches)
+    alg_launch = alg_bytes / float(sweep_launches) if (alg_bytes and sweep_launches) else None
     line = {
         "metric": "localizations/s (LM to convergence)",
         "value": value,
@@ -370,25 +373,26 @@ def run_ours(args, rank, world, local_rank):
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
         "gpu_launches": int(launches * args.steps),
         "clocks": clk,
-        "roofline": {"bound": bound, "kernel": "k_sweep", "achieved": achieved, "peak": peak_tf,
-                     "unit": "TFLOP/s", "frac": (achieved / peak_tf) if achieved else None,
-                     "peak_source": "nominal %d SMs x 128 FP32 lanes x 2 x %.0f MHz" % (nsm, mx)
-                     if bound == "fp32" else "nominal FP64",
+        "roofline": {"bound": "hbm", "kernel": "k_sweep", "achieved": hbm_achieved,
+                     "peak": hbm_peak, "unit": "GB/s",
+                     "frac": (hbm_achieved / hbm_peak) if (hbm_achieved and hbm_peak) else None,
+                     "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_peak else None,
                      "traffic": traffic_launch,
-                     "traffic_note": "ncu DRAM read+write bytes of the first sweep launch, "
-                                     "per frame of a 16-frame capture, times the frames of this step"
+                     "algorithmic_bytes_per_launch": alg_launch,
+                     "traffic_note": "ncu DRAM read+write bytes per LM step of a first-sweep launch "
+                                     "(16-frame capture) times this step's LM iterations per sweep launch"
                      if traffic_launch else None,
+                     "bytes_per_iteration": bytes_per_iteration(nroi) if nroi else None,
                      "sweep_launches": int(sweep_launches), "sweep_ms_per_step": sweep_ms,
-                     "lm_iterations_per_step": iters, "flops_per_iteration": flops_per_iteration(model, nroi),
+                     "lm_iterations_per_step": iters,
                      "sweep_ms_first5": [round(float(v), 3) for v in per_sweep[:5]],
                      "sweep_ms_median_after20": float(numpy.median(per_sweep[20:])) if per_sweep.size > 20 else None,
                      "sweep_ms_sum_after20": float(per_sweep[20:].sum()) if per_sweep.size > 20 else None},
-        "roofline_hbm": {"bound": "hbm", "kernel": "k_sweep", "achieved": hbm_achieved,
-                         "peak": hbm_peak, "unit": "GB/s",
-                         "frac": (hbm_achieved / hbm_peak) if (hbm_achieved and hbm_peak) else None,
-                         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_peak else None,
-                         "traffic": traffic_launch,
-                         "bytes_per_iteration": bytes_per_iteration(nroi) if nroi else None},
+        "roofline_fp32": {"bound": bound, "kernel": "k_sweep", "achieved": achieved, "peak": peak_tf,
+                          "unit": "TFLOP/s", "frac": (achieved / peak_tf) if achieved else None,
+                          "peak_source": "nominal %d SMs x 128 FP32 lanes x 2 x %.0f MHz" % (nsm, mx)
+                          if bound == "fp32" else "nominal FP64",
+                          "flops_per_iteration": flops_per_iteration(model, nroi)},
         "fit": {"converged": int((status == 1).sum()), "error": int((status == 2).sum()),
                 "running": int((status == 0).sum()), "sweeps": fit.sweeps,
                 "scheduler": fit.sched_stats()},
