@@ -103,6 +103,7 @@ struct Engine {
   long long npix = 0;
   void* d_x = nullptr;
   long long* d_xq = nullptr;   // FP32: data in fixed point
+  float2* d_xff = nullptr;     // FP32: the fixed-point data as float-float
   void* d_rqe = nullptr;
   void* d_scmos = nullptr;
   void* d_aij = nullptr;
@@ -174,7 +175,7 @@ struct Engine {
   }
   void release() {
     release_peaks();
-    dfree(d_x); dfree(d_xq); dfree(d_rqe); dfree(d_scmos); dfree(d_aij); dfree(d_f); dfree(d_bg); dfree(d_cnt);
+    dfree(d_x); dfree(d_xq); dfree(d_xff); dfree(d_rqe); dfree(d_scmos); dfree(d_aij); dfree(d_f); dfree(d_bg); dfree(d_cnt);
     dfree(d_bgest); dfree(d_ctl); dfree(d_cellstart); dfree(d_err); dfree(d_roi); dfree(d_stage);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -194,6 +195,7 @@ struct Engine {
     s.npix = npix;
     s.x = (const T*)d_x;
     s.xq = d_xq;
+    s.xff = d_xff;
     s.rqe = (const T*)d_rqe;
     s.scmos = (const T*)d_scmos;
     s.f = d_f;
@@ -261,12 +263,13 @@ struct Engine {
   int set_frames(int n) {
     if (configure()) return -1;
     if (n == F && d_x) return 0;
-    dfree(d_x); dfree(d_xq); dfree(d_f); dfree(d_bg); dfree(d_cnt); dfree(d_bgest); dfree(d_ctl);
+    dfree(d_x); dfree(d_xq); dfree(d_xff); dfree(d_f); dfree(d_bg); dfree(d_cnt); dfree(d_bgest); dfree(d_ctl);
     dfree(d_cellstart);
     const size_t np = (size_t)npix * n;
     const size_t words = (prec == 64) ? 2 : 1;   // accumulator words per pixel
     CK(cudaMalloc(&d_x, np * tsize()));
     if (prec == 32) CK(cudaMalloc(&d_xq, np * sizeof(long long)));
+    if (prec == 32) CK(cudaMalloc(&d_xff, np * sizeof(float2)));
     CK(cudaMalloc(&d_f, np * words * sizeof(long long)));
     CK(cudaMalloc(&d_bg, np * words * sizeof(long long)));
     CK(cudaMalloc(&d_cnt, np * sizeof(int)));

@@ -115,6 +115,7 @@ struct FrameSet {
   long long npix;
   const T* x;
   const long long* xq;    // FP32 engine: the data in fixed point (2^-36), exact
+  const float2* xff;      // FP32 engine: the same value as a float-float pair
   const T* rqe;
   const T* scmos;
   long long* f;

@@ -170,6 +170,7 @@ __device__ inline int solve_g32(WarpWS<float>& ws, int k, double lam, double* ou
 
 struct G32Pix {
   long long F, B, X;
+  float2 x;   // the data X 2^-36 as a float-float pair
   int C;
   float rq;
 };
@@ -184,6 +185,7 @@ __device__ __forceinline__ void g32_load(const ModelCfg& cfg, const FrameSet<T>&
   v.B = __ldcg(fs.bg + fbase + k);
   v.C = __ldcg(fs.cnt + fbase + k);
   v.X = __ldg(fs.xq + fbase + k);
+  v.x = __ldg(fs.xff + fbase + k);
   v.rq = (float)__ldg(fs.rqe + k);
 }
 
@@ -193,12 +195,12 @@ __device__ __forceinline__ void g32_load(const ModelCfg& cfg, const FrameSet<T>&
 // term.
 __device__ __forceinline__ void g32_pixel_state(const G32Pix& v, int p, WarpWS<float>& ws, float& devf,
                                                 bool& fail) {
-  // the data value for the FP32 terms, rounded from its fixed-point copy
-  // (one load less per pixel than reading the float copy)
-  const float vx = fx_to_float(v.X);
+  // f0 = rho + x with the data's float-float copy: two int64 conversions
+  // fewer per pixel than converting f as well
+  const float vx = v.x.x;
   const ff bgc = ff_div(ff_from_fixed(v.B), ff{(float)v.C, 0.0f});
   const ff rho = ff_add(ff_from_fixed(v.F - v.X), bgc);
-  const ff f0 = ff_add(ff_from_fixed(v.F), bgc);
+  const ff f0 = ff_add(rho, ff{v.x.x, v.x.y});
   if (!(f0.h > 0.0f)) fail = true;
   else devf += dev_res(rho.h, vx);
   const ff t1 = ff_div(ff{2.0f * rho.h, 2.0f * rho.l}, f0);
@@ -212,8 +214,10 @@ __device__ __forceinline__ void g32_pixel_state(const G32Pix& v, int p, WarpWS<f
 
 // Pass 1a: the ROI's pixels are loaded G32_GROUP per lane at a time (all
 // loads of a group in flight together) and their start state goes to the
-// warp workspace; returns the lane's start error terms.
-constexpr int G32_GROUP = 2;
+// warp workspace; returns the lane's start error terms.  One pixel at a time
+// measured best: larger groups hold more loaded values in registers than
+// the 80-register budget of six CTAs per SM allows, and spill.
+constexpr int G32_GROUP = 1;
 
 template <typename T>
 __device__ inline void g32_gather(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,

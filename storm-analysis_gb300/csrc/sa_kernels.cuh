@@ -823,7 +823,14 @@ __global__ void k_new_image(FrameSet<T> fs, const I* img, int frame0, int nframe
     const long long g = (long long)frame0 * fs.npix + i;
     const double v = (double)img[i] * (double)fs.rqe[k] + (double)fs.scmos[k];
     const_cast<T*>(fs.x)[g] = (T)v;
-    if (fs.xq) const_cast<long long*>(fs.xq)[g] = __double2ll_rn(v * 68719476736.0);
+    if (fs.xq) {
+      const long long q = __double2ll_rn(v * 68719476736.0);
+      const_cast<long long*>(fs.xq)[g] = q;
+      // q 2^-36 is exact in double for |v| < 2^17; its float-float pair
+      const double d = (double)q * 1.4551915228366852e-11;
+      const float h = __double2float_rn(d);
+      const_cast<float2*>(fs.xff)[g] = make_float2(h, __double2float_rn(d - (double)h));
+    }
     for (int w = 0; w < AccW<T>::W; w++) {
       fs.f[g * AccW<T>::W + w] = 0;
       fs.bg[g * AccW<T>::W + w] = 0;
