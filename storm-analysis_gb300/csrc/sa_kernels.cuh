@@ -444,6 +444,21 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
 // k_sweep: persistent warps over the run ranks of all frames in IN_SWEEP
 // ---------------------------------------------------------------------------
 
+// Can the steps of two peaks whose ROI anchors differ by (dx, dy) touch a
+// common pixel, when each may move its anchor by up to dil in x and y?  A
+// ROI pixel's centre lies within roi/2 of the ROI centre (the circular ROI,
+// multi_fit.c:1031-1060), so two ROIs share no pixel when their centres are
+// more than roi apart; the moves widen that by the distance between the two
+// squares of reachable anchors.  The bounding-box test is kept as well.
+__device__ __forceinline__ bool footprints_overlap(int dx, int dy, int roi, int dil) {
+  const int span = roi + 2 * dil;
+  dx = abs(dx);
+  dy = abs(dy);
+  if (dx >= span || dy >= span) return false;
+  const int ex = max(dx - 2 * dil, 0), ey = max(dy - 2 * dil, 0);
+  return ex * ex + ey * ey <= roi * roi;
+}
+
 // G32 >= 0: the FP32 Gaussian step (lm_step_g32) of model G32 (one
 // instantiation per model); G32 < 0: lm_step.
 template <typename T, int G32>
@@ -476,7 +491,6 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
     const int base = fs.pk_off[f];
     const int start = c->start;
     const int dil = c->dil;
-    const int span = cfg.roi + 2 * dil;   // anchors closer than this: dilated footprints overlap
     const unsigned a0 = fs.anchor0[base + r];
     const int ax = a0 & 0xffff, ay = a0 >> 16;
     const int li = fs.run[base + r];
@@ -513,7 +527,7 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
                 if (cand < r && cand >= start) {
                   const unsigned b0 = fs.anchor0[base + cand];
                   const int bx = b0 & 0xffff, by = b0 >> 16;
-                  if (abs(bx - ax) < span && abs(by - ay) < span) q = cand;
+                  if (footprints_overlap(bx - ax, by - ay, cfg.roi, dil)) q = cand;
                 }
               }
               unsigned m = __ballot_sync(0xffffffffu, q >= 0);
