@@ -473,7 +473,8 @@ def run_serving(args, local_rank):
         reqs.append({"model": model, "image": wl["images"][0], "background": wl["backgrounds"][0],
                      "peaks": wl["guesses"][0], "ptype": "hdf5", "fitter": wl["fitter"], "rqe": wl["rqe"],
                      "scmos_cal": wl["scmos_cal"], "camera": (model, size), "max_iterations": MAX_IT})
-    server = FitServer(mem_cap_bytes=40e9, slots=args.slots, precision=args.precision)
+    server = FitServer(mem_cap_bytes=40e9, slots=args.slots, precision=args.precision,
+                       ticks_per_launch=args.ticks_per_launch, ctas_per_slot=args.ctas_per_slot)
     warm = reqs[:args.warmup]
     if warm:
         server.run(warm)
@@ -501,7 +502,8 @@ def run_serving(args, local_rank):
         "data": "synthetic (seeded, benchmark configuration 4 shapes, sizes %s)" % (sizes,),
         "config": {"workload": "cfg4 serving: %d requests Poisson at %.0f frames/s, models 2d/3d/Z/spline3D, "
                                "density log-U(0.05, 2) /um^2" % (len(timed), args.rate),
-                   "slots_per_lane": args.slots, "memory_cap_gb": 40,
+                   "slots_per_lane": args.slots, "ticks_per_launch": args.ticks_per_launch,
+                   "ctas_per_slot": args.ctas_per_slot, "memory_cap_gb": 40,
                    "lanes": len(server.lanes), "localizations": int(locs)},
         "latency_ms": {"p50": float(numpy.percentile(lat, 50)), "p99": float(numpy.percentile(lat, 99)),
                        "max": float(lat.max()),
@@ -531,7 +533,9 @@ def main():
     ap.add_argument("--serving", action="store_true", help="run the serving stream instead")
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rate", type=float, default=2000.0)
-    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--slots", type=int, default=32)
+    ap.add_argument("--ticks-per-launch", type=int, default=4)
+    ap.add_argument("--ctas-per-slot", type=int, default=12)
     ap.add_argument("--serving-sizes", default="128,256,512")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
