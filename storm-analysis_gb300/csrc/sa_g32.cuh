@@ -1,7 +1,7 @@
 // sa_g32.cuh -- the LM step of one peak in the FP32 engine for the Gaussian
 // models (2dfixed, 2d, 3d, Z); one warp per peak.
 //
-// Precision plan.  The step's Hessian, its FP32 Cholesky factor and the
+// Precision plan.  The step's Hessian, its FP32 LDL^T factor and the
 // per-pixel model shape are FP32; what decides the step -- the gradient and
 // the change of the MLE error between the start of the step and a trial --
 // is carried in float-float ("ff", ~48 bits) from exact inputs:
@@ -78,92 +78,96 @@ static __device__ __noinline__ int solve_g32_fallback(const float* jh, int k, do
 }
 
 // Damped solve (H + lam diag H) d = b of the FP32 Gaussian step
-// (multi_fit.c:1174-1203 with dposv :1839-1883), warp-collective, FP32
-// instructions only: lane i holds row i, Jacobi-scaled and eliminated in
-// FP32 (lu_substitute), then two refinements with the residual in
-// float-float.  A pivot <= 0 hands the system to the FP64 Cholesky on
-// lane 0, which decides failure as dposv does.  Solution on lane 0.
-__device__ inline int solve_g32(WarpWS<float>& ws, int k, double lam, double* out, int lane) {
+// (multi_fit.c:1174-1203 with dposv :1839-1883), FP32 instructions only.
+// Every lane factors the Jacobi-scaled matrix (LDL^T) and substitutes on its
+// own, so the factorisation needs no shuffles; the two refinements compute
+// the residual in float-float a row per lane and gather it to every lane.
+// A pivot <= 0 hands the system to the FP64 Cholesky on lane 0, which
+// decides failure as dposv does.  Solution on lane 0.
+template <int K>
+__device__ inline int solve_g32(WarpWS<float>& ws, double lam, double* out, int lane) {
   const float* jh = g32_jh(ws);
-  const bool act = lane < k;
   const ff L1 = ff_from_double(1.0 + lam);
-  ff Ai[MAX_JAC];
-  float r[MAX_JAC];
-  ff bi{0.0f, 0.0f}, dii{1.0f, 0.0f};
+  float sc[K], D[K], L[K][K], c[K];
+  int status = 0;
 #pragma unroll
-  for (int j = 0; j < MAX_JAC; j++) {
-    Ai[j] = ff{0.0f, 0.0f};
-    if (act && j < k) {
-      const int id = hes_index(k, lane, j);
-      const ff a{jh[id], jh[36 + id]};
-      Ai[j] = (j == lane) ? ff_mul(L1, a) : a;
-      if (j == lane) dii = Ai[j];
-    }
+  for (int i = 0; i < K; i++) {
+    const int id = hes_index(K, i, i);
+    const float d = ff_mul(L1, ff{jh[id], jh[36 + id]}).h;
+    if (!(d > 1.0e-30f && d < 1.0e30f)) status = 2;
+    sc[i] = rsqrtf(d);
   }
-  if (act) bi = ff{jh[lane], jh[36 + lane]};
-  const bool bad = act && !(dii.h > 1.0e-30f && dii.h < 1.0e30f);
-  int status = __any_sync(0xffffffffu, bad) ? 2 : 0;
-  const float si = act && !bad ? rsqrtf(dii.h) : 0.0f;
   if (status == 0) {
 #pragma unroll
-    for (int j = 0; j < MAX_JAC; j++) {
-      const float sj = __shfl_sync(0xffffffffu, si, j);
-      r[j] = (act && j < k) ? (Ai[j].h * si) * sj : 0.0f;
-    }
+    for (int j = 0; j < K; j++) {
+      const int idj = hes_index(K, j, j);
+      float dj = (ff_mul(L1, ff{jh[idj], jh[36 + idj]}).h * sc[j]) * sc[j];
 #pragma unroll
-    for (int j = 0; j < MAX_JAC; j++) {
-      if (j < k && status == 0) {
-        const float piv = __shfl_sync(0xffffffffu, r[j], j);
-        if (!(piv > 0.0f)) {
-          status = 2;
-        } else {
-          const bool below = act && lane > j;
-          const float m = below ? __fdiv_rn(r[j], piv) : 0.0f;
+      for (int m = 0; m < j; m++) dj = fmaf(-L[j][m] * L[j][m], D[m], dj);
+      if (!(dj > 0.0f)) status = 2;
+      D[j] = dj;
 #pragma unroll
-          for (int l = j + 1; l < MAX_JAC; l++) {
-            if (l < k) {
-              const float pl = __shfl_sync(0xffffffffu, r[l], j);
-              if (below) r[l] = fmaf(-m, pl, r[l]);
-            }
-          }
-          if (below) r[j] = m;
-        }
+      for (int i = j + 1; i < K; i++) {
+        float t = (jh[hes_index(K, i, j)] * sc[i]) * sc[j];
+#pragma unroll
+        for (int m = 0; m < j; m++) t = fmaf(-L[i][m] * L[j][m], D[m], t);
+        L[i][j] = __fdiv_rn(t, dj);
       }
     }
   }
   if (status == 0) {
-    float c = act ? bi.h * si : 0.0f;
-    c = lu_substitute(r, c, k, lane);
-    ff xs = act ? two_prod(c, si) : ff{0.0f, 0.0f};
+    // L D L^T x = c, c = scaled right-hand side; d = x * scale
+    auto substitute = [&](float (&v)[K]) {
+#pragma unroll
+      for (int i = 0; i < K; i++) {
+#pragma unroll
+        for (int m = 0; m < i; m++) v[i] = fmaf(-L[i][m], v[m], v[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < K; i++) v[i] = __fdiv_rn(v[i], D[i]);
+#pragma unroll
+      for (int i = K - 1; i >= 0; i--) {
+#pragma unroll
+        for (int m = i + 1; m < K; m++) v[i] = fmaf(-L[m][i], v[m], v[i]);
+      }
+    };
+    ff x[K];
+#pragma unroll
+    for (int i = 0; i < K; i++) c[i] = jh[i] * sc[i];
+    substitute(c);
+#pragma unroll
+    for (int i = 0; i < K; i++) x[i] = two_prod(c[i], sc[i]);
     for (int it = 0; it < 2; it++) {
-      ff res = bi;
+      // residual of row `lane` in float-float, then every row to every lane
+      ff res{0.0f, 0.0f};
+      if (lane < K) {
+        res = ff{jh[lane], jh[36 + lane]};
 #pragma unroll
-      for (int j = 0; j < MAX_JAC; j++) {
-        if (j < k) {
-          const ff dj = shfl_ff(xs, j);
-          if (act) res = ff_sub(res, ff_mul(Ai[j], dj));
+        for (int j = 0; j < K; j++) {
+          const int id = hes_index(K, lane, j);
+          const ff a{jh[id], jh[36 + id]};
+          res = ff_sub(res, ff_mul(j == lane ? ff_mul(L1, a) : a, x[j]));
         }
       }
-      c = act ? res.h * si : 0.0f;
-      c = lu_substitute(r, c, k, lane);
-      if (act) xs = ff_add(xs, two_prod(c, si));
-    }
 #pragma unroll
-    for (int j = 0; j < MAX_JAC; j++) {
-      if (j < k) {
-        const ff v = shfl_ff(xs, j);
-        if (lane == 0) {
-          out[j] = ff_to_double(v);
-          if (isnan(v.h)) status = 1;   // multi_fit.c:1857-1863
-        }
+      for (int i = 0; i < K; i++) c[i] = __shfl_sync(0xffffffffu, res.h, i) * sc[i];
+      substitute(c);
+#pragma unroll
+      for (int i = 0; i < K; i++) x[i] = ff_add(x[i], two_prod(c[i], sc[i]));
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < K; j++) {
+        out[j] = ff_to_double(x[j]);
+        if (isnan(x[j].h)) status = 1;   // multi_fit.c:1857-1863
       }
     }
   }
   if (lane == 0 && status == 2) {
     double o[MAX_JAC];
-    status = solve_g32_fallback(jh, k, lam, o);
+    status = solve_g32_fallback(jh, K, lam, o);
 #pragma unroll
-    for (int j = 0; j < MAX_JAC; j++) out[j] = o[j];
+    for (int j = 0; j < K; j++) out[j] = o[j];
   }
   return status;
 }
@@ -422,10 +426,13 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     fail = __any_sync(0xffffffffu, fail);
     {
       float* jh = g32_jh(ws);
-      const ff hv = warp_transpose_sum32_ff(acc, lane);
+      // the Hessian is FP32 throughout (a 1e-7 relative error in it moves
+      // no decision of configuration 1 and 0.1-0.2 % of configuration 2's
+      // iteration counts); its lo words stay zero
+      const float hv = warp_transpose_sum32(acc, lane);
       if (lane < nhes) {
-        jh[k + lane] = hv.h;
-        jh[36 + k + lane] = hv.l;
+        jh[k + lane] = hv;
+        jh[36 + k + lane] = 0.0f;
       }
       const ff gv = warp_reduce8_ff(g, lane);
       const int gi = reduce8_index(lane);
@@ -470,7 +477,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
       // damped solve (multi_fit.c:1174-1203), warp-collective
       const double lam = __shfl_sync(0xffffffffu, w.lambda, 0);
       double b[MAX_JAC];
-      const int info = solve_g32(ws, k, lam, b, lane);
+      const int info = solve_g32<k>(ws, lam, b, lane);
       if (lane == 0) {
         if (info != 0) {
           ctr[C_DPOSV]++;
