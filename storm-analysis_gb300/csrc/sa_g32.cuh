@@ -244,7 +244,9 @@ __device__ inline void g32_gather(const ModelCfg& cfg, const FrameSet<T>& fs, lo
 }
 
 // Pass 1b over the ROI for model M: ff gradient and FP32 Hessian partial
-// sums of this lane, from the start state in the warp workspace.
+// sums of this lane, from the start state in the warp workspace.  Two
+// loops: the Hessian's FP32 products do not hold registers across the
+// float-float gradient's chains.
 template <int M, typename T>
 __device__ inline void g32_pass1(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
                                  const PeakRec& o, WarpWS<T>& ws, int lane, ff (&g)[8],
@@ -253,40 +255,48 @@ __device__ inline void g32_pass1(const ModelCfg& cfg, const FrameSet<T>& fs, lon
   const int ts = ws.ts;
   const float* t0 = ws.tab0;
   const float* gt = ws.tab1;
+  // gradient (float-float)
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
     roi_rc(fs.roi_xy, p, rx, ry);
     const ff t1{ws.t1h[p], ws.t1l[p]};
-    const float f0h = ws.f0g[p], xv = ws.Xs[p], rq = ws.Rs[p];
-    const float t2 = __fdiv_rn(2.0f * xv, f0h * f0h);
-    const ff ps = ff_mul_f(g32_psf(t0, ts, rx, ry), rq);
-    const ff u = ff_mul(t1, ps);
+    const float rq = ws.Rs[p];
+    const ff u = ff_mul(t1, ff_mul_f(g32_psf(t0, ts, rx, ry), rq));
     const ff A1{gt[rx], gt[ts + rx]}, A2{gt[2 * ts + rx], gt[3 * ts + rx]};
     const ff B1{gt[4 * ts + ry], gt[5 * ts + ry]}, B2{gt[6 * ts + ry], gt[7 * ts + ry]};
-    float jf[K];
-    jf[0] = ps.h;
     g[0] = ff_add(g[0], u);
     if constexpr (M == M_3D) {
       g[1] = ff_add(g[1], ff_mul(u, A1));
       g[2] = ff_add(g[2], ff_mul(u, A2));
       g[3] = ff_add(g[3], ff_mul(u, B1));
       g[4] = ff_add(g[4], ff_mul(u, B2));
-      jf[1] = ps.h * A1.h;
-      jf[2] = ps.h * A2.h;
-      jf[3] = ps.h * B1.h;
-      jf[4] = ps.h * B2.h;
     } else {
       g[1] = ff_add(g[1], ff_mul(u, A1));
       g[2] = ff_add(g[2], ff_mul(u, B1));
-      jf[1] = ps.h * A1.h;
-      jf[2] = ps.h * B1.h;
-      if constexpr (M != M_2DFIXED) {
-        const ff W = ff_add(A2, B2);
-        g[3] = ff_add(g[3], ff_mul(u, W));
-        jf[3] = ps.h * W.h;
-      }
+      if constexpr (M != M_2DFIXED) g[3] = ff_add(g[3], ff_mul(u, ff_add(A2, B2)));
     }
     g[K - 1] = ff_add(g[K - 1], ff_mul_f(t1, rq));
+  }
+  // Hessian (FP32)
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(fs.roi_xy, p, rx, ry);
+    const float f0h = ws.f0g[p], xv = ws.Xs[p], rq = ws.Rs[p];
+    const float t2 = __fdiv_rn(2.0f * xv, f0h * f0h);
+    const float ps = t0[rx] * t0[2 * ts + ry] * rq;
+    const float a1 = gt[rx], a2 = gt[2 * ts + rx], b1 = gt[4 * ts + ry], b2 = gt[6 * ts + ry];
+    float jf[K];
+    jf[0] = ps;
+    if constexpr (M == M_3D) {
+      jf[1] = ps * a1;
+      jf[2] = ps * a2;
+      jf[3] = ps * b1;
+      jf[4] = ps * b2;
+    } else {
+      jf[1] = ps * a1;
+      jf[2] = ps * b1;
+      if constexpr (M != M_2DFIXED) jf[3] = ps * (a2 + b2);
+    }
     jf[K - 1] = rq;
 #pragma unroll
     for (int l = 0; l < K; l++) {
