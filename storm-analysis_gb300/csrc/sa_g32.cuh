@@ -552,8 +552,13 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
         } else {
           w.error = is_delta ? se + dev : dev;
           const double change = is_delta ? dev : w.error - se;
+          // |change| / se < tol as a product for a positive start error (no
+          // FP64 division on the step's critical path; the two forms differ
+          // only within 1e-16 of the threshold, far below the engine's
+          // float-float error change)
+          const bool small = (se > 0.0) ? (fabs(change) < cfg.tol * se) : (fabs(change) / se < cfg.tol);
           if (change > 0.0) {
-            if ((change / se) < cfg.tol) {
+            if (small) {
               w.status = CONVERGED;
               act = ACT_BREAK_ADDED;
             } else {
@@ -564,7 +569,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
               act = ACT_CONTINUE;
             }
           } else {
-            if ((-change / se) < cfg.tol) {
+            if (small) {
               w.status = CONVERGED;
             } else if (w.lambda > LAMBDA_MIN) {
               w.lambda = LAMBDA_DOWN * w.lambda;

@@ -551,7 +551,9 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
       if (lane == 0) st_release(fs.done + base + r, epoch);
       continue;
     }
-    __threadfence();
+    // No fence before the step: every lane made its own acquire load of each
+    // dependency's done flag, which orders the step's reads after the
+    // predecessors' writes (released after their own fence below).
     // -- the step
     bool esc;
     if constexpr (G32 >= 0)
