@@ -88,7 +88,7 @@ template <int K>
 __device__ inline int solve_g32(WarpWS<float>& ws, double lam, double* out, int lane) {
   const float* jh = g32_jh(ws);
   const ff L1 = ff_from_double(1.0 + lam);
-  float sc[K], D[K], L[K][K], c[K];
+  float sc[K], D[K], R[K], L[K][K], c[K];
   int status = 0;
 #pragma unroll
   for (int i = 0; i < K; i++) {
@@ -106,12 +106,14 @@ __device__ inline int solve_g32(WarpWS<float>& ws, double lam, double* out, int 
       for (int m = 0; m < j; m++) dj = fmaf(-L[j][m] * L[j][m], D[m], dj);
       if (!(dj > 0.0f)) status = 2;
       D[j] = dj;
+      const float inv = __frcp_rn(dj);
+      R[j] = inv;
 #pragma unroll
       for (int i = j + 1; i < K; i++) {
         float t = (jh[hes_index(K, i, j)] * sc[i]) * sc[j];
 #pragma unroll
         for (int m = 0; m < j; m++) t = fmaf(-L[i][m] * L[j][m], D[m], t);
-        L[i][j] = __fdiv_rn(t, dj);
+        L[i][j] = t * inv;
       }
     }
   }
@@ -124,7 +126,7 @@ __device__ inline int solve_g32(WarpWS<float>& ws, double lam, double* out, int 
         for (int m = 0; m < i; m++) v[i] = fmaf(-L[i][m], v[m], v[i]);
       }
 #pragma unroll
-      for (int i = 0; i < K; i++) v[i] = __fdiv_rn(v[i], D[i]);
+      for (int i = 0; i < K; i++) v[i] = v[i] * R[i];
 #pragma unroll
       for (int i = K - 1; i >= 0; i--) {
 #pragma unroll
