@@ -209,7 +209,7 @@ def peaks_rows(wl):
 
 def run_ours(args, rank, world, local_rank):
     import torch
-    from sa_gb300 import engine, loadclib, synth
+    from sa_gb300 import engine, loadclib, replicas, synth
 
     lib = loadclib.load()
     lib.saSetDevice(local_rank)
@@ -220,7 +220,7 @@ def run_ours(args, rank, world, local_rank):
         dist.init_process_group("nccl")
 
     cfg = args.config
-    wl = synth.make_workload(cfg, frames=args.frames, seed=cfg + 1000 * rank)
+    wl = synth.make_workload(cfg, frames=args.frames, seed=replicas.replica_seed(cfg, rank))
     kw = dict(wl["fitter"])
     model = kw.pop("model")
     kw.pop("spline", None)
@@ -269,12 +269,7 @@ def run_ours(args, rank, world, local_rank):
             fn()
         e1.record()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / k
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return replicas.max_over_ranks(e0.elapsed_time(e1) / k, dist, device="cuda")
 
     for _ in range(args.warmup):
         step_resident()
@@ -327,8 +322,8 @@ def run_ours(args, rank, world, local_rank):
         plain = {"value": n / (time.perf_counter() - t0), "frames": nplain}
         pf.cleanup(verbose=False)
 
-    value = units * world / (ms_value / 1e3)
-    e2e = units * world / (ms_e2e / 1e3)
+    value = replicas.job_throughput(units, world, ms_value)
+    e2e = replicas.job_throughput(units, world, ms_e2e)
     props = torch.cuda.get_device_properties(local_rank)
     nsm = props.multi_processor_count
     mx = clk["sm_max_mhz"] or 2070.0
@@ -538,9 +533,8 @@ def main():
     ap.add_argument("--ctas-per-slot", type=int, default=12)
     ap.add_argument("--serving-sizes", default="128,256,512")
     args = ap.parse_args()
-    rank = int(os.environ.get("RANK", 0))
-    world = int(os.environ.get("WORLD_SIZE", 1))
-    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    from sa_gb300.replicas import rank_env
+    rank, world, local_rank = rank_env()
     if args.serving and args.impl == "ours":
         if rank == 0:
             run_serving(args, local_rank)
