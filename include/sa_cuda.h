@@ -184,7 +184,7 @@ int saDeviceCount(void);
  * decisions) or 64 (FP64 throughout).  Call before the first image. */
 int saSetPrecision(saFitData *fit, int bits);
 /* Footprint dilation (pixels) used by the dependency scheduler in the first
- * 20 sweeps of a fit (default 3); later sweeps use 0. */
+ * 10 sweeps of a fit (default 3); later sweeps use 0. */
 int saSetDilation(saFitData *fit, int pixels);
 /* At most `ctas` CTAs (4 warps each) for the handle's sweep kernel; 0 (the
  * default) uses the full persistent grid.  A small cap lets the sweeps of

@@ -536,10 +536,12 @@ saFitData* new_handle(const double* rqe, const double* scmos, double tol, int nx
   e->cfg.tol = tol;
   e->cfg.min_height = -1.0;   // multi_fit.c:965
   e->cfg.dil = -1;                // 3 pixels (finish_geometry) unless set
-  // After 20 sweeps most peaks have converged and the rest move little:
+  // After 10 sweeps peaks move by hundredths of a pixel per sweep:
   // dependencies then use the undilated footprint (an anchor move escapes).
+  // Measured on the 64-frame 3d workload: switching after 5, 10 or 20
+  // sweeps is within 1 %, a late dilation of 1 costs 3 %.
   e->cfg.dil_late = 0;
-  e->cfg.dil_switch = 20;
+  e->cfg.dil_switch = 10;
   e->npix = (long long)nx * ny;
   e->rqe_h.assign(rqe, rqe + e->npix);
   e->scmos_h.assign(scmos, scmos + e->npix);
