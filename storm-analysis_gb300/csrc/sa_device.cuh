@@ -452,6 +452,7 @@ struct WarpWS {
   float* tab0;  // shape tables of the step's start: ex hi, ex lo, ey hi, ey lo, xt, yt
   float* tab1;  // trial tables (same layout) / pass-1 gradient tables / solve scratch
   int ts;       // table stride (ROI size rounded up to 32)
+  const unsigned short* roi;   // ROI pixel table (packed rx | ry << 8)
 };
 
 template <typename T>
@@ -495,6 +496,7 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
     ws.tab0 = t + 6 * n;
     ws.tab1 = ws.tab0 + 6 * ts;
     ws.ts = ts;
+    ws.roi = nullptr;
     // generic views used by the auxiliary kernels (jt_row reads xt / yt)
     ws.Fb = ws.Bs = ws.R = ws.X = ws.IC = ws.psf = ws.psf0 = ws.f0 = ws.rho = nullptr;
     ws.ext = reinterpret_cast<T*>(ws.tab0);

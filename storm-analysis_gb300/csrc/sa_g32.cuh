@@ -183,9 +183,9 @@ struct G32Pix {
 
 template <typename T>
 __device__ __forceinline__ void g32_load(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
-                                         int ax, int ay, int p, G32Pix& v) {
+                                         const unsigned short* roi, int ax, int ay, int p, G32Pix& v) {
   int rx, ry;
-  roi_rc(fs.roi_xy, p, rx, ry);
+  roi_rc(roi, p, rx, ry);
   const long long k = pix_index(cfg, ax, ay, rx, ry);
   v.F = __ldcg(fs.f + fbase + k);
   v.B = __ldcg(fs.bg + fbase + k);
@@ -234,7 +234,7 @@ __device__ inline void g32_gather(const ModelCfg& cfg, const FrameSet<T>& fs, lo
 #pragma unroll
       for (int j = 0; j < G32_GROUP; j++) {
         const int p = p0 + 32 * j;
-        if (p < cfg.nroi) g32_load(cfg, fs, fbase, o.xi, o.yi, p, v[j]);
+        if (p < cfg.nroi) g32_load(cfg, fs, fbase, ws.roi, o.xi, o.yi, p, v[j]);
       }
 #pragma unroll
       for (int j = 0; j < G32_GROUP; j++) {
@@ -260,7 +260,7 @@ __device__ inline void g32_pass1(const ModelCfg& cfg, const FrameSet<T>& fs, lon
   // gradient (float-float)
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
-    roi_rc(fs.roi_xy, p, rx, ry);
+    roi_rc(ws.roi, p, rx, ry);
     const ff t1{ws.t1h[p], ws.t1l[p]};
     const float rq = ws.Rs[p];
     const ff u = ff_mul(t1, ff_mul_f(g32_psf(t0, ts, rx, ry), rq));
@@ -282,7 +282,7 @@ __device__ inline void g32_pass1(const ModelCfg& cfg, const FrameSet<T>& fs, lon
   // Hessian (FP32)
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
-    roi_rc(fs.roi_xy, p, rx, ry);
+    roi_rc(ws.roi, p, rx, ry);
     const float f0h = ws.f0g[p], xv = ws.Xs[p], rq = ws.Rs[p];
     const float t2 = __fdiv_rn(2.0f * xv, f0h * f0h);
     const float ps = t0[rx] * t0[2 * ts + ry] * rq;
@@ -320,7 +320,7 @@ __device__ inline void g32_delta(const ModelCfg& cfg, const FrameSet<T>& fs, lon
   const ff DBG = ff_from_double(t.p[PBG] - o.p[PBG]);
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
-    roi_rc(fs.roi_xy, p, rx, ry);
+    roi_rc(ws.roi, p, rx, ry);
     const float xv = ws.Xs[p], rq = ws.Rs[p];
     const ff d = ff_mul_f(ff_sub(ff_mul(H1, g32_psf(ws.tab1, ts, rx, ry)), ff_mul(H0, g32_psf(ws.tab0, ts, rx, ry))), rq);
     const ff bgd = ff_div(ff_mul_f(DBG, rq), ff{ws.Cs[p], 0.0f});
@@ -359,7 +359,7 @@ __device__ inline float g32_absolute(const ModelCfg& cfg, const FrameSet<T>& fs,
   float devf = 0.0f;
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
-    roi_rc(fs.roi_xy, p, rx, ry);
+    roi_rc(ws.roi, p, rx, ry);
     const long long k = pix_index(cfg, t.xi, t.yi, rx, ry);
     long long F = __ldcg(fs.f + fbase + k), B = __ldcg(fs.bg + fbase + k);
     int C = __ldcg(fs.cnt + fbase + k);
@@ -597,7 +597,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     if (added_end && wl.xi == orig.xi && wl.yi == orig.yi) {
       for (int p = lane; p < cfg.nroi; p += 32) {
         int rx, ry;
-        roi_rc(fs.roi_xy, p, rx, ry);
+        roi_rc(ws.roi, p, rx, ry);
         const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
         const float rq = ws.Rs[p], sc = (float)__ldg(fs.scmos + kk);
         Q2 q0f, q0b, q1f, q1b;
@@ -609,7 +609,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     } else {
       for (int p = lane; p < cfg.nroi; p += 32) {
         int rx, ry;
-        roi_rc(fs.roi_xy, p, rx, ry);
+        roi_rc(ws.roi, p, rx, ry);
         const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
         Q2 qf, qb;
         g32_contrib(ws.tab0, ts, H0, BG0, rx, ry, ws.Rs[p], (float)__ldg(fs.scmos + kk), qf, qb);
@@ -621,7 +621,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     if (added_end && (wl.xi != orig.xi || wl.yi != orig.yi)) {
       for (int p = lane; p < cfg.nroi; p += 32) {
         int rx, ry;
-        roi_rc(fs.roi_xy, p, rx, ry);
+        roi_rc(ws.roi, p, rx, ry);
         const long long kk = pix_index(cfg, wl.xi, wl.yi, rx, ry);
         Q2 qf, qb;
         g32_contrib(ws.tab1, ts, H1, BG1, rx, ry, (float)__ldg(fs.rqe + kk), (float)__ldg(fs.scmos + kk), qf, qb);

@@ -468,6 +468,13 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(cfg, cfg.nroi), cfg, cfg.nroi);
+  if constexpr (G32 >= 0) {
+    // the ROI pixel table, shared by the CTA's warps, after their workspaces
+    unsigned short* roi = reinterpret_cast<unsigned short*>(smem + (size_t)wpb * warp_ws_bytes<T>(cfg, cfg.nroi));
+    for (int i = threadIdx.x; i < cfg.nroi; i += blockDim.x) roi[i] = fs.roi_xy[i];
+    __syncthreads();
+    ws.roi = roi;
+  }
   const int gwarp = blockIdx.x * wpb + wib;
   int f = gwarp % fs.F;
   int misses = 0;
