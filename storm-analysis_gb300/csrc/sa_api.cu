@@ -128,7 +128,7 @@ struct Engine {
   int* d_run = nullptr;
   unsigned* d_anchor = nullptr;
   int* d_done = nullptr;
-  int* d_cellitems = nullptr;
+  int2* d_cellitems = nullptr;
   int* d_stepctr = nullptr;
 
   // scheduling
@@ -318,7 +318,7 @@ struct Engine {
     CK(cudaMalloc(&d_run, c * sizeof(int)));
     CK(cudaMalloc(&d_anchor, c * sizeof(unsigned)));
     CK(cudaMalloc(&d_done, c * sizeof(int)));
-    CK(cudaMalloc(&d_cellitems, c * sizeof(int)));
+    CK(cudaMalloc(&d_cellitems, c * sizeof(int2)));
     CK(cudaMalloc(&d_stepctr, c * NCOUNTERS * sizeof(int)));
     CK(cudaMemset(d_pk, 0, c * sizeof(PeakRec)));
     CK(cudaMemset(d_done, 0xff, c * sizeof(int)));

@@ -131,7 +131,7 @@ struct FrameSet {
   unsigned* anchor0;     // packed (xi | yi << 16) per run rank at sweep start
   int* done;             // epoch per run rank
   int* cell_start;       // [F][gx*gy+1]
-  int* cell_items;       // run ranks grouped by cell
+  int2* cell_items;      // run ranks grouped by cell, each with its packed anchor
   int* stepctr;          // [peaks][NCOUNTERS] counters of the latest step of each peak
   FrameCtl* ctl;
   unsigned* err_flag;    // bit 0: wait timeout, bit 1: ROI too large

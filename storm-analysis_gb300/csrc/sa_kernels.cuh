@@ -520,31 +520,53 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
           const int b = c->barrier[bi];
           if (b < r && b >= start) ok = wait_epoch(fs.done + base + b, epoch, fs.err_flag);
         }
-        // lower-index RUNNING neighbours whose dilated footprints overlap
+        // lower-index RUNNING neighbours whose dilated footprints overlap:
+        // lane l < 9 reads the range of neighbouring cell l, then the
+        // candidates of all nine cells are checked 32 at a time
         const int cw = cfg.cell;
         const int cx = ax / cw, cy = ay / cw;
         const int* cs = fs.cell_start + (size_t)f * (cfg.gx * cfg.gy + 1);
-        for (int yy = max(cy - 1, 0); yy <= min(cy + 1, cfg.gy - 1) && ok; yy++) {
-          for (int xx = max(cx - 1, 0); xx <= min(cx + 1, cfg.gx - 1) && ok; xx++) {
-            const int c0 = cs[yy * cfg.gx + xx], c1 = cs[yy * cfg.gx + xx + 1];
-            for (int j0 = c0; j0 < c1 && ok; j0 += 32) {
-              int q = -1;
-              if (j0 + lane < c1) {
-                const int cand = fs.cell_items[base + j0 + lane];
-                if (cand < r && cand >= start) {
-                  const unsigned b0 = fs.anchor0[base + cand];
-                  const int bx = b0 & 0xffff, by = b0 >> 16;
-                  if (footprints_overlap(bx - ax, by - ay, cfg.roi, dil)) q = cand;
-                }
-              }
-              unsigned m = __ballot_sync(0xffffffffu, q >= 0);
-              while (m && ok) {
-                const int src = __ffs(m) - 1;
-                m &= m - 1;
-                const int qq = __shfl_sync(0xffffffffu, q, src);
-                ok = wait_epoch(fs.done + base + qq, epoch, fs.err_flag);
-              }
+        int c0 = 0, cnt = 0;
+        if (lane < 9) {
+          const int yy = cy - 1 + lane / 3, xx = cx - 1 + lane % 3;
+          if (yy >= 0 && yy < cfg.gy && xx >= 0 && xx < cfg.gx) {
+            c0 = cs[yy * cfg.gx + xx];
+            cnt = cs[yy * cfg.gx + xx + 1] - c0;
+          }
+        }
+        int off = cnt;   // inclusive prefix sum over the nine cells
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, off, o);
+          if (lane >= o) off += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, off, 8);
+        off -= cnt;      // exclusive
+        for (int j0 = 0; j0 < total && ok; j0 += 32) {
+          const int j = j0 + lane;
+          // the cell holding candidate j: the last cell whose offset is <= j
+          int idx = -1;
+#pragma unroll
+          for (int k = 0; k < 9; k++) {
+            const int ok_ = __shfl_sync(0xffffffffu, off, k);
+            const int ck = __shfl_sync(0xffffffffu, c0, k);
+            if (j < total && j >= ok_) idx = ck + (j - ok_);
+          }
+          int q = -1;
+          if (idx >= 0) {
+            const int2 e = fs.cell_items[base + idx];
+            if (e.x < r && e.x >= start) {
+              const unsigned b0 = (unsigned)e.y;
+              const int bx = b0 & 0xffff, by = b0 >> 16;
+              if (footprints_overlap(bx - ax, by - ay, cfg.roi, dil)) q = e.x;
             }
+          }
+          unsigned m = __ballot_sync(0xffffffffu, q >= 0);
+          while (m && ok) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const int qq = __shfl_sync(0xffffffffu, q, src);
+            ok = wait_epoch(fs.done + base + qq, epoch, fs.err_flag);
           }
         }
       }
@@ -651,7 +673,7 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
       const unsigned a = fs.anchor0[base + r];
       const int cell = ((a >> 16) / cfg.cell) * cfg.gx + (a & 0xffff) / cfg.cell;
       const int slot = atomicAdd(&cntc[cell], 1);
-      fs.cell_items[base + slot] = r;
+      fs.cell_items[base + slot] = make_int2(r, (int)a);
     }
     if (tid == 0) {
       c->nrun = nrun;
