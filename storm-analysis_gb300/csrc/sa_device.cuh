@@ -141,6 +141,24 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
   return fast_two_sum(p, e);
 }
 
+// a * b as an unnormalised pair (p, e) with p + e = a * b to ~2^-48.
+__device__ __forceinline__ ff ff_mul_raw(ff a, ff b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return ff{p, e};
+}
+
+// Cascaded summation: acc += x with the rounding error of the high parts
+// kept exactly and the low parts summed in FP32; acc is renormalised by the
+// caller (fast_two_sum) once the sum is complete.
+__device__ __forceinline__ void ff_acc(ff& acc, ff x) {
+  const ff s = two_sum(acc.h, x.h);
+  acc.h = s.h;
+  acc.l = __fadd_rn(acc.l, __fadd_rn(s.l, x.l));
+}
+
 __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
   const float p = __fmul_rn(a.h, b);
   const float e = __fmaf_rn(a.h, b, -p);

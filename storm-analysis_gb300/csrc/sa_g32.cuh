@@ -266,19 +266,21 @@ __device__ inline void g32_pass1(const ModelCfg& cfg, const FrameSet<T>& fs, lon
     const ff u = ff_mul(t1, ff_mul_f(g32_psf(t0, ts, rx, ry), rq));
     const ff A1{gt[rx], gt[ts + rx]}, A2{gt[2 * ts + rx], gt[3 * ts + rx]};
     const ff B1{gt[4 * ts + ry], gt[5 * ts + ry]}, B2{gt[6 * ts + ry], gt[7 * ts + ry]};
-    g[0] = ff_add(g[0], u);
+    ff_acc(g[0], u);
     if constexpr (M == M_3D) {
-      g[1] = ff_add(g[1], ff_mul(u, A1));
-      g[2] = ff_add(g[2], ff_mul(u, A2));
-      g[3] = ff_add(g[3], ff_mul(u, B1));
-      g[4] = ff_add(g[4], ff_mul(u, B2));
+      ff_acc(g[1], ff_mul_raw(u, A1));
+      ff_acc(g[2], ff_mul_raw(u, A2));
+      ff_acc(g[3], ff_mul_raw(u, B1));
+      ff_acc(g[4], ff_mul_raw(u, B2));
     } else {
-      g[1] = ff_add(g[1], ff_mul(u, A1));
-      g[2] = ff_add(g[2], ff_mul(u, B1));
-      if constexpr (M != M_2DFIXED) g[3] = ff_add(g[3], ff_mul(u, ff_add(A2, B2)));
+      ff_acc(g[1], ff_mul_raw(u, A1));
+      ff_acc(g[2], ff_mul_raw(u, B1));
+      if constexpr (M != M_2DFIXED) ff_acc(g[3], ff_mul_raw(u, ff_add(A2, B2)));
     }
-    g[K - 1] = ff_add(g[K - 1], ff_mul_f(t1, rq));
+    ff_acc(g[K - 1], ff_mul_f(t1, rq));
   }
+#pragma unroll
+  for (int l = 0; l < K; l++) g[l] = fast_two_sum(g[l].h, g[l].l);
   // Hessian (FP32)
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
@@ -329,7 +331,7 @@ __device__ inline void g32_delta(const ModelCfg& cfg, const FrameSet<T>& fs, lon
     if (!(f0 + df.h > 0.0f)) {
       fail = true;
     } else {
-      s1 = ff_add(s1, ff_mul(df, ff{ws.t1h[p], ws.t1l[p]}));
+      ff_acc(s1, ff_mul_raw(df, ff{ws.t1h[p], ws.t1l[p]}));
       s2 += 2.0f * xv * r_minus_log1p(__fdiv_rn(df.h, f0));
     }
   }
@@ -535,6 +537,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
         ff s1{0.0f, 0.0f};
         float s2 = 0.0f;
         g32_delta(cfg, fs, fbase, orig, wl, ws, lane, s1, s2, fail);
+        s1 = fast_two_sum(s1.h, s1.l);
         dev = ff_to_double(warp_sum_ffv(s1)) + warp_sum_ff(s2);
       } else {
         dev = warp_sum_ff(g32_absolute(cfg, fs, fbase, orig, wl, ws, lane, fail));
