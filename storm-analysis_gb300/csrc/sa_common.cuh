@@ -82,6 +82,8 @@ struct ModelCfg {
   double zmin, zmax;
   double min_height;
   int force_serial;      // 1: every frame runs its peaks strictly in index order
+  int rqe_one;           // 1: rqe is 1 at every pixel (no per-pixel loads)
+  int scmos_zero;        // 1: the sCMOS term is 0 at every pixel
   int dil_late;          // dilation from sweep dil_switch on (<= dil)
   int dil_switch;
 };

@@ -192,7 +192,7 @@ __device__ __forceinline__ void g32_load(const ModelCfg& cfg, const FrameSet<T>&
   v.C = __ldcg(fs.cnt + fbase + k);
   v.X = __ldg(fs.xq + fbase + k);
   v.x = __ldg(fs.xff + fbase + k);
-  v.rq = (float)__ldg(fs.rqe + k);
+  v.rq = cfg.rqe_one ? 1.0f : (float)__ldg(fs.rqe + k);
 }
 
 // Per-pixel state of the step's start, from the loaded pixel: f0 = f + bg /
@@ -366,7 +366,8 @@ __device__ inline float g32_absolute(const ModelCfg& cfg, const FrameSet<T>& fs,
     long long F = __ldcg(fs.f + fbase + k), B = __ldcg(fs.bg + fbase + k);
     int C = __ldcg(fs.cnt + fbase + k);
     const float xv = (float)__ldg(fs.x + fbase + k);
-    const float rq = (float)__ldg(fs.rqe + k), sc = (float)__ldg(fs.scmos + k);
+    const float rq = cfg.rqe_one ? 1.0f : (float)__ldg(fs.rqe + k);
+    const float sc = cfg.scmos_zero ? 0.0f : (float)__ldg(fs.scmos + k);
     const long long Xq = __ldg(fs.xq + fbase + k);
     const int ox = rx + dx, oy = ry + dy;   // the same image pixel in the start ROI
     if (in_roi(ox, oy, cfg.roi)) {
@@ -597,12 +598,31 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     __syncwarp();
     const PeakRec& wl = *ws.w;
     const ff H1 = ff_from_double(wl.p[PH]), BG1 = ff_from_double(wl.p[PBG]);
-    if (added_end && wl.xi == orig.xi && wl.yi == orig.yi) {
+    if (added_end && wl.xi == orig.xi && wl.yi == orig.yi && cfg.rqe_one && cfg.scmos_zero) {
+      // uniform calibration: BG * 1 + 0 at every pixel, quantised once
+      // (bit-identical to g32_contrib with rqe 1 and sCMOS 0)
+      Q2 b0, b1;
+      b0.h = fixed_from_ff(BG0);
+      b1.h = fixed_from_ff(BG1);
+      b0.l = b1.l = 0;
+      const Q2 db = q_sub(b1, b0);
       for (int p = lane; p < cfg.nroi; p += 32) {
         int rx, ry;
         roi_rc(ws.roi, p, rx, ry);
         const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
-        const float rq = ws.Rs[p], sc = (float)__ldg(fs.scmos + kk);
+        Q2 q0f, q1f;
+        q0f.h = fixed_from_ff(ff_mul(H0, g32_psf(ws.tab0, ts, rx, ry)));
+        q1f.h = fixed_from_ff(ff_mul(H1, g32_psf(ws.tab1, ts, rx, ry)));
+        q0f.l = q1f.l = 0;
+        acc_red<1>(fs.f, fbase + kk, q_sub(q1f, q0f), +1);
+        acc_red<1>(fs.bg, fbase + kk, db, +1);
+      }
+    } else if (added_end && wl.xi == orig.xi && wl.yi == orig.yi) {
+      for (int p = lane; p < cfg.nroi; p += 32) {
+        int rx, ry;
+        roi_rc(ws.roi, p, rx, ry);
+        const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
+        const float rq = ws.Rs[p], sc = cfg.scmos_zero ? 0.0f : (float)__ldg(fs.scmos + kk);
         Q2 q0f, q0b, q1f, q1b;
         g32_contrib(ws.tab0, ts, H0, BG0, rx, ry, rq, sc, q0f, q0b);
         g32_contrib(ws.tab1, ts, H1, BG1, rx, ry, rq, sc, q1f, q1b);
@@ -615,7 +635,8 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
         roi_rc(ws.roi, p, rx, ry);
         const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
         Q2 qf, qb;
-        g32_contrib(ws.tab0, ts, H0, BG0, rx, ry, ws.Rs[p], (float)__ldg(fs.scmos + kk), qf, qb);
+        g32_contrib(ws.tab0, ts, H0, BG0, rx, ry, ws.Rs[p], cfg.scmos_zero ? 0.0f : (float)__ldg(fs.scmos + kk),
+                    qf, qb);
         acc_red<1>(fs.f, fbase + kk, qf, -1);
         acc_red<1>(fs.bg, fbase + kk, qb, -1);
         atomicAdd(fs.cnt + fbase + kk, -1);
@@ -627,7 +648,8 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
         roi_rc(ws.roi, p, rx, ry);
         const long long kk = pix_index(cfg, wl.xi, wl.yi, rx, ry);
         Q2 qf, qb;
-        g32_contrib(ws.tab1, ts, H1, BG1, rx, ry, (float)__ldg(fs.rqe + kk), (float)__ldg(fs.scmos + kk), qf, qb);
+        g32_contrib(ws.tab1, ts, H1, BG1, rx, ry, cfg.rqe_one ? 1.0f : (float)__ldg(fs.rqe + kk),
+                    cfg.scmos_zero ? 0.0f : (float)__ldg(fs.scmos + kk), qf, qb);
         acc_red<1>(fs.f, fbase + kk, qf, +1);
         acc_red<1>(fs.bg, fbase + kk, qb, +1);
         atomicAdd(fs.cnt + fbase + kk, 1);
