@@ -164,6 +164,7 @@ struct Engine {
 
   ~Engine() {
     release();
+    release_poll_buffers();
     if (h_ctl) cudaFreeHost(h_ctl);
     if (ev_poll) cudaEventDestroy(ev_poll);
   }
@@ -405,19 +406,82 @@ struct Engine {
 
   // Run ticks until no frame is pending.  Frames start in SWEEP_PENDING
   // with max_sweeps set by the caller.
-  int run_until_done(std::vector<FrameCtl>& ctl) {
+  // Two bursts are kept in flight: the next two ticks are queued before the
+  // host reads the frame control blocks of the previous burst, so the
+  // device never idles on the host's poll.  Ticks queued after the last
+  // frame has finished change nothing (every kernel skips DONE frames).
+  // Fits of one or two sweeps (a host-driven sweep loop) keep one burst in
+  // flight, so that no tick is launched past their end.
+  int run_until_done(std::vector<FrameCtl>& ctl, int max_sweeps) {
+    if (ensure_poll_buffers()) return -1;
+    const bool ahead = max_sweeps > 2;
+    if (burst_poll(0)) return -1;
+    int cur = 0;
     for (;;) {
-      const int burst = 2;
-      for (int i = 0; i < burst; i++)
-        if (tick()) return -1;
-      CK(cudaMemcpyAsync(ctl.data(), d_ctl, sizeof(FrameCtl) * F, cudaMemcpyDeviceToHost, stream));
-      CK(cudaStreamSynchronize(stream));
-      if (check_err_flag()) return -1;
+      if (ahead && burst_poll(1 - cur)) return -1;
+      CK(cudaEventSynchronize(ev_pb[cur]));
+      if (h_perr[cur]) {
+        CK(cudaStreamSynchronize(stream));
+        return check_err_flag() ? -1 : 0;
+      }
       bool active = false;
       for (int f = 0; f < F; f++)
-        if (ctl[f].phase != PH_DONE && ctl[f].phase != PH_IDLE) active = true;
-      if (!active) break;
+        if (h_pctl[cur][f].phase != PH_DONE && h_pctl[cur][f].phase != PH_IDLE) active = true;
+      if (!active) {
+        for (int f = 0; f < F; f++) ctl[f] = h_pctl[cur][f];
+        CK(cudaStreamSynchronize(stream));
+        return check_err_flag() ? -1 : 0;
+      }
+      if (ahead) {
+        cur = 1 - cur;
+      } else if (burst_poll(cur)) {
+        return -1;
+      }
     }
+  }
+
+  // Pinned buffers and events of the two bursts in flight.
+  FrameCtl* h_pctl[2] = {nullptr, nullptr};
+  unsigned* h_perr = nullptr;
+  cudaEvent_t ev_pb[2] = {nullptr, nullptr};
+  int pctl_n = 0;
+
+  int ensure_poll_buffers() {
+    if (!h_perr) {
+      CK(cudaMallocHost((void**)&h_perr, 2 * sizeof(unsigned)));
+      for (int b = 0; b < 2; b++) CK(cudaEventCreateWithFlags(&ev_pb[b], cudaEventDisableTiming));
+    }
+    if (pctl_n < F) {
+      for (int b = 0; b < 2; b++) {
+        if (h_pctl[b]) cudaFreeHost(h_pctl[b]);
+        h_pctl[b] = nullptr;
+        CK(cudaMallocHost((void**)&h_pctl[b], sizeof(FrameCtl) * F));
+      }
+      pctl_n = F;
+    }
+    return 0;
+  }
+
+  void release_poll_buffers() {
+    for (int b = 0; b < 2; b++) {
+      if (h_pctl[b]) cudaFreeHost(h_pctl[b]);
+      if (ev_pb[b]) cudaEventDestroy(ev_pb[b]);
+      h_pctl[b] = nullptr;
+      ev_pb[b] = nullptr;
+    }
+    if (h_perr) cudaFreeHost(h_perr);
+    h_perr = nullptr;
+    pctl_n = 0;
+  }
+
+  // Two ticks, then the frame control blocks and the error flag into
+  // pinned buffer b, then its event.
+  int burst_poll(int b) {
+    for (int i = 0; i < 2; i++)
+      if (tick()) return -1;
+    CK(cudaMemcpyAsync(h_pctl[b], d_ctl, sizeof(FrameCtl) * F, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h_perr + b, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+    CK(cudaEventRecord(ev_pb[b], stream));
     return 0;
   }
 
@@ -435,7 +499,7 @@ struct Engine {
       ctl[f].max_sweeps = max_sweeps;
     }
     CK(cudaMemcpy(d_ctl, ctl.data(), sizeof(FrameCtl) * F, cudaMemcpyHostToDevice));
-    if (run_until_done(ctl)) return -1;
+    if (run_until_done(ctl, max_sweeps)) return -1;
     int sw = 0;
     for (int f = 0; f < F; f++) sw = std::max(sw, ctl[f].sweeps);
     unconv_cache = (F == 1) ? ctl[0].unconverged : -1;
