@@ -503,7 +503,10 @@ def run_serving(args, local_rank):
         "latency_ms": {"p50": float(numpy.percentile(lat, 50)), "p99": float(numpy.percentile(lat, 99)),
                        "max": float(lat.max()),
                        "p50_512": float(numpy.percentile(lat[big], 50)) if big else None,
-                       "p99_512": float(numpy.percentile(lat[big], 99)) if big else None},
+                       "p99_512": float(numpy.percentile(lat[big], 99)) if big else None,
+                       "p50_by_model": {m: float(numpy.percentile(lat[[j for j, r in enumerate(timed)
+                                                                       if r["model"] == m]], 50))
+                                        for m in sorted({r["model"] for r in timed})}},
         "e2e": {"value": locs / wall, "unit": "localizations/s", "note": "host frames in, results out"},
         "gpu_launches": int(launches),
         "clocks": clk,

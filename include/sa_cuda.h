@@ -250,6 +250,9 @@ int saSlotLoad(saFitData *fit, int slot, const void *image, const void *backgrou
                const double *peaks, int n_peaks, const char *p_type, int max_iterations);
 int saSlotLaunch(saFitData *fit, int n_ticks);
 int saSlotPoll(saFitData *fit, int32_t *phases, int32_t *sweeps);
+/* 1 when the read-back of the last saSlotLaunch has completed (saSlotPoll
+ * will not block), 0 while it is in flight, < 0 on error. */
+int saSlotReady(saFitData *fit);
 int saSlotResults(saFitData *fit, int slot, double *values, int32_t *ints);
 
 /* No reference counterpart.  Fit image (residual = 0, as mFitGetFitImage) or

@@ -1582,6 +1582,16 @@ int saSlotLaunch(saFitData* h, int n_ticks) {
   return 0;
 }
 
+int saSlotReady(saFitData* h) {
+  Engine* e = E(h);
+  if (!e || !e->ev_poll) return -1;
+  const cudaError_t q = cudaEventQuery(e->ev_poll);
+  if (q == cudaSuccess) return 1;
+  if (q == cudaErrorNotReady) return 0;
+  set_error("CUDA error: %s", cudaGetErrorString(q));
+  return -1;
+}
+
 int saSlotPoll(saFitData* h, int32_t* phases, int32_t* sweeps) {
   Engine* e = E(h);
   if (!e || !e->h_ctl || !e->ev_poll) return -1;

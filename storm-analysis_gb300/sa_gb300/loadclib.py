@@ -148,6 +148,8 @@ def _declare(lib):
     lib.saSlotLaunch.restype = ci
     lib.saSlotPoll.argtypes = [hp, i32, i32]
     lib.saSlotPoll.restype = ci
+    lib.saSlotReady.argtypes = [hp]
+    lib.saSlotReady.restype = ci
     lib.saSlotResults.argtypes = [hp, ci, f64, i32]
     lib.saSlotResults.restype = ci
 
@@ -168,5 +170,5 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "saNewBackgrounds", "saNewPeaksBatch", "saNewPeaksBatchDevice", "saDoFitBatch", "saGetNFitBatch",
            "saGetPeakPropertyBatch", "saGetPeakPropertyIntBatch", "saSetTiming", "saGetTiming",
            "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice", "saGetSweepTimes",
-           "saGetFitImageNoAlloc", "saSlotLoad", "saSlotLaunch", "saSlotPoll", "saSlotResults",
+           "saGetFitImageNoAlloc", "saSlotLoad", "saSlotLaunch", "saSlotPoll", "saSlotReady", "saSlotResults",
            "saSetSweepCTAs"]

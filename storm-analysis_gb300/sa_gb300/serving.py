@@ -14,7 +14,9 @@ independent slots (saSlotLoad / saSlotLaunch / saSlotPoll / saSlotResults).
 * Continuous batching: a slot starts fitting while the lane's other slots
   are mid-fit (the device state machine runs every loaded slot's sweeps, a
   slot finishes independently of the others), and each lane runs on its own
-  CUDA stream, so the sweeps of different lanes overlap on the device.
+  CUDA stream, so the sweeps of different lanes overlap on the device.  The
+  host never waits on one lane: a lane gets its next burst of sweep ticks
+  as soon as its previous burst has completed, whatever the others do.
 * State stays resident: a frame's fit image and peak records live in its
   slot from admission to completion.
 
@@ -112,6 +114,15 @@ class Lane(object):
             raise MultiFitterException("saSlotLaunch: " + loadclib.last_error())
         self.launched = True
 
+    def ready(self):
+        """True when the last launch's read-back has completed."""
+        if not self.launched:
+            return True
+        r = self.lib.saSlotReady(self.fitter.h)
+        if r < 0:
+            raise MultiFitterException("saSlotReady: " + loadclib.last_error())
+        return r == 1
+
     def poll(self):
         """Wait for the last launch; return the slots that finished."""
         if not self.launched:
@@ -208,34 +219,38 @@ class FitServer(object):
         return lane
 
     def _retire_idle(self):
-        for key in [k for k, l in self.lanes.items() if not l.active()]:
+        for key in [k for k, l in self.lanes.items() if not l.active() and not l.launched]:
             self.lanes.pop(key).close()
 
     def step(self):
-        """Admit queued requests into free slots, launch a burst of sweep ticks
-        on every lane with work (all lanes before any wait, so they overlap),
-        then collect the finished requests.  Returns the finished ids."""
+        """One pass over the lanes without waiting on any of them: collect
+        the lanes whose burst of sweep ticks has completed, admit queued
+        requests into the free slots of lanes that are not running, and
+        give every idle lane with work its next burst.  A lane whose frames
+        take long sweeps does not hold the others back.  Returns the
+        finished ids."""
+        finished = []
+        for lane in self.lanes.values():
+            if lane.launched and lane.ready():
+                for slot in lane.poll():
+                    rid = lane.busy[slot]
+                    self.done[rid] = lane.results(slot)
+                    self.t_done[rid] = time.perf_counter()
+                    lane.busy[slot] = None
+                    finished.append(rid)
         waiting = []
         for rid in self.queue:
             req = self.reqs[rid]
             lane = self._lane_for(req)
-            slot = lane.free_slot() if lane is not None else -1
+            slot = lane.free_slot() if (lane is not None and not lane.launched) else -1
             if slot < 0:
                 waiting.append(rid)
                 continue
             lane.load(slot, rid, req)
         self.queue = waiting
-        busy = [l for l in self.lanes.values() if l.active()]
-        for lane in busy:
-            lane.launch(self.ticks)
-        finished = []
-        for lane in busy:
-            for slot in lane.poll():
-                rid = lane.busy[slot]
-                self.done[rid] = lane.results(slot)
-                self.t_done[rid] = time.perf_counter()
-                lane.busy[slot] = None
-                finished.append(rid)
+        for lane in self.lanes.values():
+            if not lane.launched and lane.active():
+                lane.launch(self.ticks)
         return finished
 
     def pending(self):
@@ -256,7 +271,8 @@ class FitServer(object):
                 ids[i] = self.submit(requests[i], t=t0 + (0.0 if arrival_s is None else arrival_s[i]))
                 k += 1
             if self.pending():
-                self.step()
+                if not self.step():
+                    time.sleep(2e-5)   # every lane mid-burst
             elif k < len(order):
                 time.sleep(max(0.0, min(0.001, arrival_s[order[k]] - now)))
         return ids
