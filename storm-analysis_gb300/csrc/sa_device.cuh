@@ -541,6 +541,7 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
     ws.yt = tab + 384;
     ws.t1h = ws.t1l = ws.f0g = ws.Xs = ws.Rs = ws.Cs = ws.tab0 = ws.tab1 = nullptr;
     ws.ts = 0;
+    ws.roi = nullptr;
     off = ws_pixel_arrays<T>() * n * sizeof(T) + 4 * 64 * sizeof(T) * 2;
   }
   off = (off + 15) & ~(size_t)15;

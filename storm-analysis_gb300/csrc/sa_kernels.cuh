@@ -87,7 +87,7 @@ __device__ inline void load_base(const ModelCfg& cfg, const FrameSet<T>& fs, lon
   constexpr int W = AccW<T>::W;
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
-    roi_rc(fs.roi_xy, p, rx, ry);
+    roi_rc(ws.roi, p, rx, ry);
     const long long k = pix_index(cfg, ax, ay, rx, ry);
     const Q2 Fq = acc_load<W>(fs.f, fbase + k);
     const Q2 Bq = acc_load<W>(fs.bg, fbase + k);
@@ -134,7 +134,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
   bool fail = false;
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
-    roi_rc(fs.roi_xy, p, rx, ry);
+    roi_rc(ws.roi, p, rx, ry);
     const long long kk = pix_index(cfg, orig.xi, orig.yi, rx, ry);
     const Q2 Fq = acc_load<AccW<T>::W>(fs.f, fbase + kk);
     const Q2 Bq = acc_load<AccW<T>::W>(fs.bg, fbase + kk);
@@ -334,7 +334,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
         const float dbg = (float)(bgv - orig.p[PBG]);
         for (int p = lane; p < cfg.nroi; p += 32) {
           int rx, ry;
-          roi_rc(fs.roi_xy, p, rx, ry);
+          roi_rc(ws.roi, p, rx, ry);
           float psf, dpsf;
           psf_and_delta(cfg, fs.aij, ws, s, rx, ry, psf, dpsf);
           ws.psf[p] = psf;
@@ -347,7 +347,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
       } else {
         for (int p = lane; p < cfg.nroi; p += 32) {
           int rx, ry;
-          roi_rc(fs.roi_xy, p, rx, ry);
+          roi_rc(ws.roi, p, rx, ry);
           const T psf = psf_at(cfg, fs.aij, ws, s, rx, ry);
           ws.psf[p] = psf;
           const T rq = ws.R[p];
@@ -359,7 +359,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     } else {
       for (int p = lane; p < cfg.nroi; p += 32) {
         int rx, ry;
-        roi_rc(fs.roi_xy, p, rx, ry);
+        roi_rc(ws.roi, p, rx, ry);
         const T psf = psf_at(cfg, fs.aij, ws, s, rx, ry);
         ws.psf[p] = psf;
         const T rq = ws.R[p];
@@ -424,7 +424,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     const PeakRec& wl = *ws.w;
     for (int p = lane; p < cfg.nroi; p += 32) {
       int rx, ry;
-      roi_rc(fs.roi_xy, p, rx, ry);
+      roi_rc(ws.roi, p, rx, ry);
       const long long kk = pix_index(cfg, wl.xi, wl.yi, rx, ry);
       const T rq = ws.R[p];
       const T sc = __ldg(fs.scmos + kk);
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   WarpWS<T> ws = warp_ws<T>(smem + (size_t)wib * warp_ws_bytes<T>(cfg, cfg.nroi), cfg, cfg.nroi);
-  if constexpr (G32 >= 0) {
+  {
     // the ROI pixel table, shared by the CTA's warps, after their workspaces
     unsigned short* roi = reinterpret_cast<unsigned short*>(smem + (size_t)wpb * warp_ws_bytes<T>(cfg, cfg.nroi));
     for (int i = threadIdx.x; i < cfg.nroi; i += blockDim.x) roi[i] = fs.roi_xy[i];

@@ -38,7 +38,7 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t ws = warp_ws_bytes<T>(cfg, cfg.nroi);
-  const size_t s_sweep = ws * (SWEEP_BLOCK / 32) + (gauss32<T>(cfg) ? (((size_t)cfg.nroi * 2 + 15) & ~(size_t)15) : 0);
+  const size_t s_sweep = ws * (SWEEP_BLOCK / 32) + (((size_t)cfg.nroi * 2 + 15) & ~(size_t)15);
   const size_t ws0 = warp_ws_bytes<T>(cfg, 0);
   const size_t grid_bytes = (size_t)(cfg.gx * cfg.gy + 1) * sizeof(int);
   const size_t s_cta = ws0 * (CTA_BLOCK / 32) > grid_bytes ? ws0 * (CTA_BLOCK / 32) : grid_bytes;
