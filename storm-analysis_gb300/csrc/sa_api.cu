@@ -609,8 +609,13 @@ saFitData* new_handle(const double* rqe, const double* scmos, double tol, int nx
   e->npix = (long long)nx * ny;
   e->rqe_h.assign(rqe, rqe + e->npix);
   e->scmos_h.assign(scmos, scmos + e->npix);
-  e->cfg.rqe_one = std::all_of(e->rqe_h.begin(), e->rqe_h.end(), [](double v) { return v == 1.0; }) ? 1 : 0;
-  e->cfg.scmos_zero = std::all_of(e->scmos_h.begin(), e->scmos_h.end(), [](double v) { return v == 0.0; }) ? 1 : 0;
+  // uniform calibration (rqe 1, sCMOS 0 everywhere) enables the FP32 step's
+  // per-peak background quantisation; SA_CUDA_CAL_FAST=0 keeps the
+  // per-pixel form (the results are the same)
+  const char* pc = getenv("SA_CUDA_CAL_FAST");
+  const bool cal_fast = !(pc && atoi(pc) == 0);
+  e->cfg.rqe_one = cal_fast && std::all_of(e->rqe_h.begin(), e->rqe_h.end(), [](double v) { return v == 1.0; }) ? 1 : 0;
+  e->cfg.scmos_zero = cal_fast && std::all_of(e->scmos_h.begin(), e->scmos_h.end(), [](double v) { return v == 0.0; }) ? 1 : 0;
   const char* pe = getenv("SA_CUDA_PRECISION");
   if (pe && atoi(pe) == 64) e->prec = 64;
   const char* ps = getenv("SA_CUDA_SERIAL");

@@ -178,6 +178,27 @@ def test_batch_equals_single_frames():
         assert numpy.array_equal(res[p], single[p]), p
 
 
+def test_uniform_calibration_path_is_exact(monkeypatch):
+    """With rqe 1 and no sCMOS term the FP32 write-back quantises a peak's
+    background contribution once per step; the per-pixel form gives the
+    same bits."""
+    from sa_gb300 import engine, synth
+    wl = synth.make_workload(1, frames=3, nx=192, ny=192)
+    kw = dict(wl["fitter"])
+    kw.pop("model")
+    outs = []
+    for fast in ("0", "1"):
+        monkeypatch.setenv("SA_CUDA_CAL_FAST", fast)
+        b = engine.BatchFitter("3d", (192, 192), 3, precision=32, **kw)
+        b.load(numpy.stack(wl["images"]), numpy.stack(wl["backgrounds"]), wl["guesses"], "hdf5")
+        sweeps = b.fit(200)
+        outs.append((b.results(), sweeps))
+        b.close()
+    assert outs[0][1] == outs[1][1]
+    for p in ["x", "y", "z", "height", "background", "status", "iterations", "error"]:
+        assert numpy.array_equal(outs[0][0][p], outs[1][0][p]), p
+
+
 def test_escape_rollback_path_is_exact():
     """With no footprint dilation almost every anchor move escapes; the
     rollback / barrier re-run must still reproduce the normal schedule."""
