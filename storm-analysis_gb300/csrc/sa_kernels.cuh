@@ -617,12 +617,19 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
   const int base = fs.pk_off[f];
   const int tid = threadIdx.x;
   if (phase == PH_SWEEP_PENDING) {
-    const int n = fs.nfit[f];
+    // Within a fit a peak only leaves RUNNING, so after the first sweep the
+    // candidates are the previous sweep's run list (compacted in place:
+    // every kept entry moves to a lower or equal position, and a chunk is
+    // read before any of it is written).
+    const bool from_run = c->sweeps > 0;
+    const int n = from_run ? c->nrun : fs.nfit[f];
     int nrun = 0;
     for (int c0 = 0; c0 < n; c0 += 1024) {
-      const int i = c0 + tid;
+      const int k = c0 + tid;
+      const int i = (k < n) ? (from_run ? fs.run[base + k] : k) : -1;
+      __syncthreads();
       int flag = 0;
-      if (i < n && fs.pk[base + i].status == RUNNING) {
+      if (i >= 0 && fs.pk[base + i].status == RUNNING) {
         // A RUNNING peak always has an in-image ROI, except one re-marked
         // RUNNING by the caller after a failed placement; it cannot be
         // fitted (its ROI is outside the image) and is set to ERROR.
