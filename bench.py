@@ -18,6 +18,8 @@ step fits all 64 frames to termination through the batched engine.
           reference's host-driven sweep loop), for comparison
   cpu_baseline  the FP64 CPU oracle (our C restatement of the reference's
           fitter) on the host cores, one process per core, a bounded sample
+  finder  the GPU peak finder (matched filters + local maxima) on the same
+          frames, mirror-padded, with its own CPU baseline (the oracle)
 
 `python bench.py --impl reference` times the CPU oracle on all host cores on
 the same workload and prints the same JSON line with "impl": "reference".
@@ -404,11 +406,101 @@ def run_ours(args, rank, world, local_rank):
         line["cpu_baseline"] = {"value": n_cpu / wall, "unit": "localizations/s", "cores": cores,
                                 "kind": "port", "sample": "%d frames of the step's workload, one "
                                 "process per core, %.1f s wall" % (min(cores, F), wall)}
+    if rank == 0 and not args.no_finder:
+        line["finder"] = run_finder(args, wl, torch)
     if dist is not None:
         dist.destroy_process_group()
     fit.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+FINDER_PARAMS = dict(background_sigma=8.0, foreground_sigma=1.0, find_max_radius=5, iterations=20,
+                     sigma=1.5, threshold=6.0, roi_size=18)
+
+
+def run_finder(args, wl, torch):
+    """The GPU peak finder (PeakFinderGaussian.peakFinder with background
+    estimation) over the step's frames, mirror-padded by the finder margin
+    (11 px for roi 18): one finder step = newImages + estimateBackground +
+    findPeaks for all frames.  Two frame sets alternate between steps (the
+    second is each frame flipped top to bottom) so that the memoised
+    matched filters convolve every step, as they do on a movie."""
+    from sa_gb300 import fitting
+    margin = int(FINDER_PARAMS["roi_size"] / 2 + 2)
+    frames = numpy.ascontiguousarray(numpy.stack([fitting.padArray(im, margin) for im in wl["images"]]))
+    alt = numpy.ascontiguousarray(frames[:, ::-1, :])
+    F = frames.shape[0]
+    shape = frames.shape[1:]
+    d_sets = [torch.from_numpy(frames).cuda(), torch.from_numpy(alt).cuda()]
+    p_sets = [torch.from_numpy(frames).pin_memory().numpy(), torch.from_numpy(alt).pin_memory().numpy()]
+    torch.cuda.synchronize()
+    bf = fitting.BatchPeakFinder(FINDER_PARAMS, shape, F)
+    found = []
+
+    def step(i, host=False):
+        bf.newImages(p_sets[i % 2] if host else d_sets[i % 2])
+        bf.estimateBackground()
+        bf.findPeaks()
+        found.append(bf.total)
+        if host:
+            bf.peaks()
+
+    def timed(k, host=False):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(k):
+            step(i, host)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    for i in range(max(args.warmup, 3)):
+        step(i)
+    l0 = bf.kernel_launches()
+    del found[:]
+    ms = timed(args.steps)
+    launches = (bf.kernel_launches() - l0) // max(args.steps, 1)
+    mean_found = float(numpy.mean(found))
+    ms_e2e = timed(args.steps, host=True)
+    taps = 0
+    for f in (bf.bg_filter, bf.fg_mfilter, bf.fg_vfilter):
+        if f is not None:
+            info = f.info()
+            taps += (info[1] + info[2]) if info[0] else info[1] * info[2]
+    flops = 2.0 * taps * F * shape[0] * shape[1]
+    achieved = flops / (ms / 1e3) / 1e12
+    out = {"metric": "frames/s (peak finding: background + matched filters + local maxima)",
+           "value": F / (ms / 1e3), "unit": "frames/s", "ms_per_step": ms,
+           "frames_per_step": F, "frame": "%dx%d padded (margin %d)" % (shape[1], shape[0], margin),
+           "peaks_found_per_step": mean_found,
+           "params": FINDER_PARAMS,
+           "gpu_launches_per_step": int(launches),
+           "e2e": {"value": F / (ms_e2e / 1e3), "unit": "frames/s", "ms_per_step": ms_e2e,
+                   "h2d_bytes_per_step": int(frames.nbytes), "d2h_bytes_per_step": int(mean_found * 32)},
+           "roofline": {"bound": "fp64", "kernel": "k_conv_fast + k_conv_slow (separable FP64 convolution)",
+                        "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s", "frac": achieved / 1.25,
+                        "peak_source": "nominal FP64 (no measured FP64 peak on this pool)",
+                        "flops_per_pixel": 2 * taps,
+                        "note": "whole finder step time (all kernels) in the denominator"}}
+    if not args.no_cpu:
+        from oracle import finder as ofinder
+        n_cpu = min(F, 4)
+        t0 = time.perf_counter()
+        of = ofinder.PeakFinderGaussian(FINDER_PARAMS)
+        for i in range(n_cpu):
+            of.newImage(frames[i])
+            z = numpy.zeros(shape)
+            of.estimateBackground(z)
+            of.findPeaks(z)
+        wall = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n_cpu / wall, "unit": "frames/s", "cores": 1, "kind": "port",
+                               "sample": "%d frames, numpy FFT matched filters + the local-maxima loop, "
+                               "%.1f s" % (n_cpu, wall)}
+    bf.cleanUp()
+    return out
 
 
 def run_reference(args, rank, world):
@@ -527,6 +619,7 @@ def main():
     ap.add_argument("--plain-frames", type=int, default=2)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-finder", action="store_true", help="skip the peak-finder measurement")
     ap.add_argument("--cpu-cores", type=int, default=None)
     ap.add_argument("--serving", action="store_true", help="run the serving stream instead")
     ap.add_argument("--requests", type=int, default=200)

@@ -887,6 +887,9 @@ int get_double_props(Engine* e, int frame0, int nframes, double* values, const c
 
 }  // namespace
 
+// Error recorder shared with the peak finder's translation unit.
+void sa::record_error(const char* msg) { set_error("%s", msg); }
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

@@ -1,0 +1,1294 @@
+// sa_finder.cu -- the peak finder of libsa_cuda.so (include/sa_finder.h):
+// matched filters (circular convolution with a PSF, the job of
+// sa_library/matched_filter.c), the local-maxima finder
+// (sa_library/ia_utilities.c:58-210) and the fused Gaussian peak-finding pass
+// of PeakFinderGaussian.peakFinder (sa_library/fitting.py:444-501), batched
+// over frames of one size.
+//
+// The reference convolves through FFTW.  Here the PSFs the finder uses are
+// small-support Gaussians, so the convolution is computed directly in FP64:
+// two 1D passes for a separable PSF (81 + 81 taps for the background filter
+// of sigma 8), a 2D sum over the support otherwise.  Each pass stages its
+// rows (with the circular halo) in shared memory; the FP64 FMA pipe bounds
+// it.  The local-maxima finder marks candidates one warp per image row
+// (ballot bit masks), scans the row counts in one block and emits the peaks
+// in the reference's plane, row, column order, so the lists are identical.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "sa_finder.h"
+#include "sa_launch.h"
+
+namespace {
+
+void ferr(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  sa::record_error(buf);
+}
+
+#define FCK(call)                                                             \
+  do {                                                                        \
+    cudaError_t e__ = (call);                                                 \
+    if (e__ != cudaSuccess) {                                                 \
+      ferr("%s failed: %s", #call, cudaGetErrorString(e__));                  \
+      return -1;                                                              \
+    }                                                                         \
+  } while (0)
+
+constexpr int kThreads = 256;
+constexpr int kSlowTR = 64;   // output rows per block of the slow-axis pass
+constexpr int kTC = 32;       // columns per block of the slow-axis and 2D passes
+constexpr int k2dTR = 16;     // output rows per block of the 2D pass
+constexpr size_t kSmemMax = 200 * 1024;
+
+template <typename P>
+void dfree(P*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+// flag[f] = 1 when some pixel of frame f differs from the image of its last
+// convolution by more than max_diff (matched_filter.c:118-133).
+__global__ void k_memo_diff(const double* __restrict__ in, const double* __restrict__ old,
+                            int npix, double max_diff, int* __restrict__ flag) {
+  const int f = blockIdx.y;
+  const size_t base = (size_t)f * npix;
+  int hit = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x) {
+    if (fabs(in[base + i] - old[base + i]) > max_diff) {
+      hit = 1;
+      break;
+    }
+  }
+  if (__syncthreads_or(hit) && threadIdx.x == 0) flag[f] = 1;
+}
+
+// old = in for the frames that will be convolved (matched_filter.c:135-139).
+__global__ void k_memo_copy(const double* __restrict__ in, double* __restrict__ old, int npix,
+                            const int* __restrict__ flag) {
+  const int f = blockIdx.y;
+  if (!flag[f]) return;
+  const size_t base = (size_t)f * npix;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x)
+    old[base + i] = in[base + i];
+}
+
+// Pass along the fast axis: out[r][c] = sum_j w[j] in[r][(c - b0 - j) mod C].
+// One block per (row, frame); the row and its circular halo are staged as
+// ext[t] = in[r][(t - b0 - nb + 1) mod C], so that the tap j of output c is
+// ext[c + nb - 1 - j].
+__global__ void __launch_bounds__(kThreads)
+k_conv_fast(const double* __restrict__ in, double* __restrict__ out, int R, int C,
+            const double* __restrict__ w, int b0, int nb, const int* __restrict__ flag) {
+  extern __shared__ double sm[];
+  const int r = blockIdx.x, f = blockIdx.y;
+  if (!flag[f]) return;
+  double* ws = sm;
+  double* ext = sm + nb;
+  const size_t row = ((size_t)f * R + r) * C;
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) ws[j] = w[j];
+  int base = (-b0 - nb + 1) % C;
+  if (base < 0) base += C;
+  const int next = C + nb - 1;
+  for (int t = threadIdx.x; t < next; t += blockDim.x) ext[t] = in[row + (t + base) % C];
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) {
+    const double* e = ext + c + nb - 1;
+    double s = 0.0;
+    for (int j = 0; j < nb; ++j) s = fma(ws[j], e[-j], s);
+    out[row + c] = s;
+  }
+}
+
+// Pass along the slow axis: out[r][c] = sum_i w[i] in[(r - a0 - i) mod R][c].
+// Block (32, 8) covers 32 columns x kSlowTR output rows; ext row t holds input
+// row (r0 - a0 - na + 1 + t) mod R.
+__global__ void __launch_bounds__(kThreads)
+k_conv_slow(const double* __restrict__ in, double* __restrict__ out, int R, int C,
+            const double* __restrict__ w, int a0, int na, const int* __restrict__ flag) {
+  extern __shared__ double sm[];
+  const int f = blockIdx.z;
+  if (!flag[f]) return;
+  const int c0 = blockIdx.x * kTC, r0 = blockIdx.y * kSlowTR;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTC + tx;
+  double* ws = sm;
+  double* ext = sm + na;
+  const size_t fb = (size_t)f * R * C;
+  for (int j = tid; j < na; j += kThreads) ws[j] = w[j];
+  int base = (r0 - a0 - na + 1) % R;
+  if (base < 0) base += R;
+  const int nrows = kSlowTR + na - 1;
+  const int c = c0 + tx;
+  for (int t = ty; t < nrows; t += kThreads / kTC)
+    ext[t * kTC + tx] = (c < C) ? in[fb + (size_t)((base + t) % R) * C + c] : 0.0;
+  __syncthreads();
+  if (c >= C) return;
+  for (int q = ty; q < kSlowTR; q += kThreads / kTC) {
+    const int r = r0 + q;
+    if (r >= R) break;
+    const double* e = ext + (q + na - 1) * kTC + tx;
+    double s = 0.0;
+    for (int i = 0; i < na; ++i) s = fma(ws[i], e[-i * kTC], s);
+    out[fb + (size_t)r * C + c] = s;
+  }
+}
+
+// Direct 2D circular convolution over the PSF's support (na x nb taps,
+// w[i * nb + j] = psf[(a0 + i) mod R][(b0 + j) mod C]).  Block (32, 8) covers
+// 32 columns x k2dTR rows; ext holds the input tile with its halo.
+__global__ void __launch_bounds__(kThreads)
+k_conv_2d(const double* __restrict__ in, double* __restrict__ out, int R, int C,
+          const double* __restrict__ w, int a0, int na, int b0, int nb,
+          const int* __restrict__ flag) {
+  extern __shared__ double sm[];
+  const int f = blockIdx.z;
+  if (!flag[f]) return;
+  const int c0 = blockIdx.x * kTC, r0 = blockIdx.y * k2dTR;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTC + tx;
+  const int er = k2dTR + na - 1, ec = kTC + nb - 1;
+  double* ws = sm;
+  double* ext = sm + na * nb;
+  const size_t fb = (size_t)f * R * C;
+  for (int k = tid; k < na * nb; k += kThreads) ws[k] = w[k];
+  int rb = (r0 - a0 - na + 1) % R;
+  if (rb < 0) rb += R;
+  int cb = (c0 - b0 - nb + 1) % C;
+  if (cb < 0) cb += C;
+  for (int k = tid; k < er * ec; k += kThreads) {
+    const int t = k / ec, u = k - t * ec;
+    ext[k] = in[fb + (size_t)((rb + t) % R) * C + (cb + u) % C];
+  }
+  __syncthreads();
+  const int c = c0 + tx;
+  if (c >= C) return;
+  for (int q = ty; q < k2dTR; q += kThreads / kTC) {
+    const int r = r0 + q;
+    if (r >= R) break;
+    double s = 0.0;
+    for (int i = 0; i < na; ++i) {
+      const double* e = ext + (q + na - 1 - i) * ec + tx + nb - 1;
+      const double* wr = ws + i * nb;
+      for (int j = 0; j < nb; ++j) s = fma(wr[j], e[-j], s);
+    }
+    out[fb + (size_t)r * C + c] = s;
+  }
+}
+
+// Local maxima (ia_utilities.c:105-210).
+struct LMax {
+  const double* img;   // F x Z x R x C
+  int32_t* taken;      // F x Z x R x C
+  uint32_t* bits;      // F x Z x R x W candidate masks
+  int32_t* rowcnt;     // F x Z x R
+  int R, C, Z, W, nrows;
+  int margin, z_range, rr, cr;
+  double radius, threshold;
+};
+
+// isLocalMaxima (ia_utilities.c:177-210): the search box uses the C
+// conversions of the reference (y: truncation of yi -/+ radius; x: ceil
+// radius; radius**2 truncated to int).  Ties go to the pixel with the larger
+// row and column.
+__device__ bool is_local_max(const LMax& a, const double* fimg, int zi, int yi, int xi, double cur) {
+  const int sz = max(zi - a.z_range, 0), ez = min(zi + a.z_range, a.Z - 1);
+  const int sy = max((int)(yi - a.radius), 0), ey = min((int)(yi + a.radius), a.R - 1);
+  const int sx = max(xi - a.cr, 0), ex = min(xi + a.cr, a.C - 1);
+  for (int z = sz; z <= ez; ++z) {
+    const double* p = fimg + (size_t)z * a.R * a.C;
+    for (int y = sy; y <= ey; ++y) {
+      const int dy = (y - yi) * (y - yi);
+      const double* row = p + (size_t)y * a.C;
+      for (int x = sx; x <= ex; ++x) {
+        const int dx = (x - xi) * (x - xi);
+        if (dx + dy > a.rr) continue;
+        const double v = row[x];
+        if (y <= yi && x <= xi) {
+          if (v > cur) return false;
+        } else if (v >= cur) {
+          return false;
+        }
+      }
+    }
+  }
+  return true;
+}
+
+// One warp per (frame, plane, row): candidate bits by ballot, row count.
+__global__ void k_lmax_mark(LMax a) {
+  const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (warp >= a.nrows) return;
+  const int y = warp % a.R, fz = warp / a.R, zi = fz % a.Z, f = fz / a.Z;
+  const double* fimg = a.img + (size_t)f * a.Z * a.R * a.C;
+  const double* row = fimg + ((size_t)zi * a.R + y) * a.C;
+  const int32_t* tk = a.taken + (size_t)warp * a.C;
+  uint32_t* bits = a.bits + (size_t)warp * a.W;
+  const bool row_in = y >= a.margin && y < a.R - a.margin;
+  int cnt = 0;
+  for (int w = 0; w < a.W; ++w) {
+    const int x = w * 32 + lane;
+    bool flag = false;
+    if (row_in && x >= a.margin && x < a.C - a.margin) {
+      const double cur = row[x];
+      if (cur > a.threshold && tk[x] < 1) flag = is_local_max(a, fimg, zi, y, x, cur);
+    }
+    const uint32_t b = __ballot_sync(0xffffffffu, flag);
+    if (lane == 0) bits[w] = b;
+    cnt += __popc(b);
+  }
+  if (lane == 0) a.rowcnt[warp] = cnt;
+}
+
+// Exclusive scan of the row counts in one block of 1024 threads; fcount[f]
+// is frame f's total and fcount[F] the grand total.
+__global__ void __launch_bounds__(1024)
+k_lmax_scan(const int32_t* __restrict__ rowcnt, int32_t* __restrict__ rowoff, int nrows,
+            int rows_per_frame, int F, int32_t* __restrict__ fcount) {
+  __shared__ int32_t wsum[32];
+  __shared__ int32_t carry_s;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  for (int base = 0; base < nrows; base += 1024) {
+    const int i = base + threadIdx.x;
+    const int v = i < nrows ? rowcnt[i] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int s = wsum[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += y;
+      }
+      wsum[lane] = s;
+    }
+    __syncthreads();
+    const int incl = x + (wid ? wsum[wid - 1] : 0);
+    const int carry = carry_s;
+    if (i < nrows) rowoff[i] = carry + incl - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry_s = carry + incl;
+    __syncthreads();
+  }
+  for (int f = threadIdx.x; f < F; f += 1024) {
+    const int s = rowoff[f * rows_per_frame];
+    const int e = (f + 1 < F) ? rowoff[(f + 1) * rows_per_frame] : carry_s;
+    fcount[f] = e - s;
+  }
+  if (threadIdx.x == 0) fcount[F] = carry_s;
+}
+
+// One warp per row with candidates: write the peaks at their scanned
+// positions (plane, row, column order) and advance taken.  Peaks at or past
+// cap are dropped, as findLocalMaxima stops at n_peaks.
+__global__ void k_lmax_emit(LMax a, const int32_t* __restrict__ rowoff,
+                            const double* __restrict__ zvalues, double* __restrict__ out, int cap,
+                            double sigma) {
+  const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (warp >= a.nrows) return;
+  if (a.rowcnt[warp] == 0) return;
+  const int y = warp % a.R, fz = warp / a.R, zi = fz % a.Z;
+  const double* row = a.img + (size_t)warp * a.C;
+  int32_t* tk = a.taken + (size_t)warp * a.C;
+  const uint32_t* bits = a.bits + (size_t)warp * a.W;
+  int pos = rowoff[warp];
+  for (int w = 0; w < a.W; ++w) {
+    const uint32_t b = bits[w];
+    if (b == 0) continue;
+    if ((b >> lane) & 1u) {
+      const int p = pos + __popc(b & ((1u << lane) - 1u));
+      if (p < cap) {
+        const int x = w * 32 + lane;
+        double* o = out + (size_t)p * 4;
+        o[0] = (double)x;
+        o[1] = (double)y;
+        o[2] = zvalues[zi];
+        o[3] = sigma > 0.0 ? sigma : row[x];
+        tk[x] += 1;
+      }
+    }
+    pos += __popc(b);
+  }
+}
+
+// calcMaxPeaks (ia_utilities.c:58-75): candidates inside the margin.
+__global__ void k_lmax_count(LMax a, int32_t* __restrict__ count) {
+  int n = 0;
+  const size_t total = (size_t)a.nrows * a.C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % a.C);
+    const int y = (int)((i / a.C) % a.R);
+    if (y >= a.margin && y < a.R - a.margin && x >= a.margin && x < a.C - a.margin &&
+        a.img[i] > a.threshold && a.taken[i] < 1)
+      ++n;
+  }
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(count, n);
+}
+
+__global__ void k_fill_i32(int32_t* __restrict__ p, size_t n, int32_t v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+// Finder arithmetic of fitting.py:257 and :454-470, in the reference's order:
+// bgv = (background + fit) + camera_variance; fgr = (image - background) - fit.
+__global__ void k_find_prep(const double* __restrict__ image, const double* __restrict__ bg,
+                            const double* __restrict__ fit, const double* __restrict__ camvar,
+                            double* __restrict__ bgv, double* __restrict__ fgr, int npix,
+                            size_t total) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double b = bg[i];
+    const double ft = fit ? fit[i] : 0.0;
+    double v = b + ft;
+    if (camvar) v += camvar[i % npix];
+    bgv[i] = v;
+    fgr[i] = (image[i] - b) - ft;
+  }
+}
+
+// image - fit, the input of the background filter (fitting.py:268).
+__global__ void k_sub(const double* __restrict__ a, const double* __restrict__ b,
+                      double* __restrict__ out, size_t total) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = b ? a[i] - b[i] : a[i];
+}
+
+// masked = (fg / sqrt(bgv <= 0.1 ? 0.1 : bgv)) * mask (fitting.py:476-497).
+__global__ void k_find_ratio(const double* __restrict__ fg, const double* __restrict__ bgv,
+                             const double* __restrict__ mask, double* __restrict__ out, int npix,
+                             size_t total) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    double v = bgv[i];
+    if (v <= 0.1) v = 0.1;
+    double r = fg[i] / sqrt(v);
+    if (mask) r = r * mask[i % npix];
+    out[i] = r;
+  }
+}
+
+int grid_for(size_t n) {
+  size_t g = (n + kThreads - 1) / kThreads;
+  return (int)std::min<size_t>(std::max<size_t>(g, 1), 152 * 16);
+}
+
+// ---------------------------------------------------------------------------
+// Matched filter
+// ---------------------------------------------------------------------------
+
+// The smallest circular arc [start, start + len) of 0..n-1 holding every
+// index with nz set; start in (-n, n).  No nonzero index: len 0.
+void circular_support(const std::vector<char>& nz, int n, int* start, int* len) {
+  int count = 0;
+  for (char v : nz) count += v ? 1 : 0;
+  if (count == 0) {
+    *start = 0;
+    *len = 0;
+    return;
+  }
+  if (count == n) {
+    *start = -(n / 2);
+    *len = n;
+    return;
+  }
+  // the longest circular run of zeros; the support is its complement
+  int best = -1, best_at = 0;
+  for (int i = 0; i < n; ++i) {
+    if (nz[i] || !nz[(i + n - 1) % n]) continue;   // runs start after a nonzero
+    int k = 0;
+    while (k < n && !nz[(i + k) % n]) ++k;
+    if (k > best) {
+      best = k;
+      best_at = i;
+    }
+  }
+  int s = (best_at + best) % n;
+  *len = n - best;
+  if (s > n / 2) s -= n;
+  *start = s;
+}
+
+struct MFilter {
+  int R = 0, C = 0;
+  int separable = 1;
+  int a0 = 0, na = 1, b0 = 0, nb = 1;
+  double* d_wa = nullptr;   // separable: taps along rows (slow axis)
+  double* d_wb = nullptr;   // separable: taps along columns (fast axis)
+  double* d_w2 = nullptr;   // 2D: na x nb
+  double max_diff = 0.0;
+  std::vector<double> h_rc;   // the recentred PSF, first content of every frame's result
+  int F = 0;
+  double* d_last = nullptr;   // F x R x C: each frame's last result
+  double* d_old = nullptr;    // F x R x C: each frame's last convolved image (memo)
+  double* d_tmp = nullptr;    // F x R x C: fast-axis pass output
+  int* d_flag = nullptr;      // F
+  double* d_io = nullptr;     // R x C staging of the host entry points
+  double* d_io2 = nullptr;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  size_t smem_fast = 0, smem_slow = 0, smem_2d = 0;
+};
+
+void filter_free(MFilter* m) {
+  dfree(m->d_wa);
+  dfree(m->d_wb);
+  dfree(m->d_w2);
+  dfree(m->d_last);
+  dfree(m->d_old);
+  dfree(m->d_tmp);
+  dfree(m->d_flag);
+  dfree(m->d_io);
+  dfree(m->d_io2);
+}
+
+int filter_frames(MFilter* m, int F, cudaStream_t s) {
+  if (F <= m->F) return 0;
+  const size_t npix = (size_t)m->R * m->C;
+  double *last = nullptr, *old = nullptr, *tmp = nullptr;
+  int* flag = nullptr;
+  FCK(cudaMalloc(&last, sizeof(double) * npix * F));
+  FCK(cudaMalloc(&old, sizeof(double) * npix * F));
+  FCK(cudaMalloc(&tmp, sizeof(double) * npix * F));
+  FCK(cudaMalloc(&flag, sizeof(int) * F));
+  FCK(cudaStreamSynchronize(s));
+  if (m->F > 0) {
+    FCK(cudaMemcpy(last, m->d_last, sizeof(double) * npix * m->F, cudaMemcpyDeviceToDevice));
+    FCK(cudaMemcpy(old, m->d_old, sizeof(double) * npix * m->F, cudaMemcpyDeviceToDevice));
+  }
+  for (int f = m->F; f < F; ++f)
+    FCK(cudaMemcpy(last + npix * f, m->h_rc.data(), sizeof(double) * npix, cudaMemcpyHostToDevice));
+  FCK(cudaMemset(old + npix * m->F, 0, sizeof(double) * npix * (F - m->F)));
+  dfree(m->d_last);
+  dfree(m->d_old);
+  dfree(m->d_tmp);
+  dfree(m->d_flag);
+  m->d_last = last;
+  m->d_old = old;
+  m->d_tmp = tmp;
+  m->d_flag = flag;
+  m->F = F;
+  return 0;
+}
+
+// Convolve n frames of d_in (device) into the handle's results; memo as
+// convolveMemo, else every frame.
+int filter_run(MFilter* m, const double* d_in, int n, int memo, cudaStream_t s) {
+  if (n < 1) return 0;
+  if (filter_frames(m, n, s)) return -1;
+  const int npix = m->R * m->C;
+  if (memo) {
+    if (m->max_diff <= 0.0) {
+      ferr("convolveMemo: the filter was created without memoisation (max_diff 0)");
+      return -1;
+    }
+    FCK(cudaMemsetAsync(m->d_flag, 0, sizeof(int) * n, s));
+    const dim3 g(std::min(64, (npix + kThreads - 1) / kThreads), n);
+    k_memo_diff<<<g, kThreads, 0, s>>>(d_in, m->d_old, npix, m->max_diff, m->d_flag);
+    k_memo_copy<<<g, kThreads, 0, s>>>(d_in, m->d_old, npix, m->d_flag);
+    m->launches += 2;
+  } else {
+    FCK(cudaMemsetAsync(m->d_flag, 0x01, sizeof(int) * n, s));
+  }
+  if (m->separable) {
+    k_conv_fast<<<dim3(m->R, n), kThreads, m->smem_fast, s>>>(d_in, m->d_tmp, m->R, m->C, m->d_wb,
+                                                             m->b0, m->nb, m->d_flag);
+    const dim3 g((m->C + kTC - 1) / kTC, (m->R + kSlowTR - 1) / kSlowTR, n);
+    k_conv_slow<<<g, dim3(kTC, kThreads / kTC), m->smem_slow, s>>>(m->d_tmp, m->d_last, m->R, m->C,
+                                                                    m->d_wa, m->a0, m->na, m->d_flag);
+    m->launches += 2;
+  } else {
+    const dim3 g((m->C + kTC - 1) / kTC, (m->R + k2dTR - 1) / k2dTR, n);
+    k_conv_2d<<<g, dim3(kTC, kThreads / kTC), m->smem_2d, s>>>(d_in, m->d_last, m->R, m->C, m->d_w2,
+                                                                m->a0, m->na, m->b0, m->nb, m->d_flag);
+    m->launches += 1;
+  }
+  FCK(cudaGetLastError());
+  return 0;
+}
+
+MFilter* filter_create(const double* psf, double max_diff, int R, int C) {
+  if (!psf || R < 1 || C < 1) {
+    ferr("saFilterCreate: bad arguments (psf %p, %d x %d)", (const void*)psf, R, C);
+    return nullptr;
+  }
+  MFilter* m = new MFilter();
+  m->R = R;
+  m->C = C;
+  m->max_diff = max_diff > 0.0 ? max_diff : 0.0;
+  m->h_rc.assign(psf, psf + (size_t)R * C);
+  const std::vector<double>& p = m->h_rc;
+  std::vector<char> rnz(R, 0), cnz(C, 0);
+  double pmax = 0.0;
+  int pr = 0, pc = 0;
+  for (int r = 0; r < R; ++r)
+    for (int c = 0; c < C; ++c) {
+      const double v = p[(size_t)r * C + c];
+      if (v != 0.0) {
+        rnz[r] = 1;
+        cnz[c] = 1;
+      }
+      if (std::fabs(v) > pmax) {
+        pmax = std::fabs(v);
+        pr = r;
+        pc = c;
+      }
+    }
+  int a0, na, b0, nb;
+  circular_support(rnz, R, &a0, &na);
+  circular_support(cnz, C, &b0, &nb);
+  if (na == 0) {   // an all-zero PSF: one zero tap
+    a0 = b0 = 0;
+    na = nb = 1;
+  }
+  auto at = [&](int a, int b) { return p[(size_t)(((a % R) + R) % R) * C + ((b % C) + C) % C]; };
+  // rank-1 test against the pivot row and column
+  std::vector<double> u(na), v(nb);
+  const double piv = at(pr, pc);
+  for (int i = 0; i < na; ++i) u[i] = at(a0 + i, pc);
+  for (int j = 0; j < nb; ++j) v[j] = piv != 0.0 ? at(pr, b0 + j) / piv : 0.0;
+  double resid = 0.0;
+  for (int i = 0; i < na; ++i)
+    for (int j = 0; j < nb; ++j) resid = std::max(resid, std::fabs(at(a0 + i, b0 + j) - u[i] * v[j]));
+  m->separable = resid <= 1e-12 * pmax;
+  m->a0 = a0;
+  m->na = na;
+  m->b0 = b0;
+  m->nb = nb;
+  bool ok = true, reported = false;
+  if (m->separable) {
+    m->smem_fast = sizeof(double) * (size_t)(2 * nb + C - 1);
+    m->smem_slow = sizeof(double) * (size_t)(na + (kSlowTR + na - 1) * kTC);
+    if (m->smem_fast > kSmemMax || m->smem_slow > kSmemMax) {
+      ferr("saFilterCreate: a %d x %d image with a %d x %d tap PSF exceeds the shared-memory tile", R, C,
+           na, nb);
+      ok = false;
+      reported = true;
+    }
+    ok = ok && cudaMalloc(&m->d_wa, sizeof(double) * na) == cudaSuccess &&
+         cudaMalloc(&m->d_wb, sizeof(double) * nb) == cudaSuccess &&
+         cudaMemcpy(m->d_wa, u.data(), sizeof(double) * na, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(m->d_wb, v.data(), sizeof(double) * nb, cudaMemcpyHostToDevice) == cudaSuccess;
+  } else {
+    m->smem_2d = sizeof(double) * (size_t)(na * nb + (k2dTR + na - 1) * (kTC + nb - 1));
+    if (m->smem_2d > kSmemMax) {
+      ferr("saFilterCreate: the PSF is not separable and its support (%d x %d) is too large for "
+           "direct convolution", na, nb);
+      ok = false;
+      reported = true;
+    }
+    std::vector<double> w((size_t)na * nb);
+    for (int i = 0; i < na; ++i)
+      for (int j = 0; j < nb; ++j) w[(size_t)i * nb + j] = at(a0 + i, b0 + j);
+    ok = ok && cudaMalloc(&m->d_w2, sizeof(double) * w.size()) == cudaSuccess &&
+         cudaMemcpy(m->d_w2, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  }
+  ok = ok && cudaFuncSetAttribute(k_conv_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax) == cudaSuccess &&
+       cudaFuncSetAttribute(k_conv_slow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax) == cudaSuccess &&
+       cudaFuncSetAttribute(k_conv_2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax) == cudaSuccess &&
+       cudaMalloc(&m->d_io, sizeof(double) * (size_t)R * C) == cudaSuccess &&
+       cudaMalloc(&m->d_io2, sizeof(double) * (size_t)R * C) == cudaSuccess;
+  if (!ok) {
+    if (!reported) ferr("saFilterCreate: device set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
+    filter_free(m);
+    delete m;
+    return nullptr;
+  }
+  return m;
+}
+
+int filter_host(MFilter* m, const double* image, double* result, int memo) {
+  if (!m || !image || !result) {
+    ferr("convolve: NULL argument");
+    return -1;
+  }
+  const size_t bytes = sizeof(double) * (size_t)m->R * m->C;
+  FCK(cudaMemcpyAsync(m->d_io, image, bytes, cudaMemcpyHostToDevice, m->stream));
+  if (filter_run(m, m->d_io, 1, memo, m->stream)) return -1;
+  FCK(cudaMemcpyAsync(result, m->d_last, bytes, cudaMemcpyDeviceToHost, m->stream));
+  FCK(cudaStreamSynchronize(m->stream));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Local maxima
+// ---------------------------------------------------------------------------
+
+struct Maxima {
+  int margin = 0, z_range = 0, Z = 1, n_dup = 1;
+  double radius = 0.0, threshold = 0.0;
+  double* d_zvalues = nullptr;
+  int R = 0, C = 0, W = 0, F = 0;
+  int32_t* d_taken = nullptr;
+  uint32_t* d_bits = nullptr;
+  int32_t* d_rowcnt = nullptr;
+  int32_t* d_rowoff = nullptr;
+  int32_t* d_fcount = nullptr;
+  int32_t* h_fcount = nullptr;   // pinned, F + 1
+  double* d_out = nullptr;
+  int out_cap = 0, n_out = 0;
+  double* d_stage = nullptr;   // host images staged for saMaximaFind
+  size_t stage_bytes = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+};
+
+void maxima_free(Maxima* h) {
+  dfree(h->d_stage);
+  dfree(h->d_zvalues);
+  dfree(h->d_taken);
+  dfree(h->d_bits);
+  dfree(h->d_rowcnt);
+  dfree(h->d_rowoff);
+  dfree(h->d_fcount);
+  dfree(h->d_out);
+  if (h->h_fcount) cudaFreeHost(h->h_fcount);
+  h->h_fcount = nullptr;
+}
+
+LMax lmax_args(const Maxima* h, const double* d_img, int n) {
+  LMax a;
+  a.img = d_img;
+  a.taken = h->d_taken;
+  a.bits = h->d_bits;
+  a.rowcnt = h->d_rowcnt;
+  a.R = h->R;
+  a.C = h->C;
+  a.Z = h->Z;
+  a.W = h->W;
+  a.nrows = n * h->Z * h->R;
+  a.margin = h->margin;
+  a.z_range = h->z_range;
+  a.rr = (int)(h->radius * h->radius);
+  a.cr = (int)std::ceil(h->radius);
+  a.radius = h->radius;
+  a.threshold = h->threshold;
+  return a;
+}
+
+int maxima_reset(Maxima* h, cudaStream_t s) {
+  if (h->F < 1) return 0;
+  const size_t n = (size_t)h->F * h->Z * h->R * h->C;
+  k_fill_i32<<<grid_for(n), kThreads, 0, s>>>(h->d_taken, n, 1 - h->n_dup);
+  h->launches += 1;
+  FCK(cudaGetLastError());
+  return 0;
+}
+
+// Size the per-frame state for n frames of R x C (taken starts at
+// 1 - n_duplicates; frames keep their counts when the set grows).
+int maxima_frames(Maxima* h, int R, int C, int n, cudaStream_t s) {
+  if (h->F > 0 && (R != h->R || C != h->C)) {
+    ferr("maxima finder: image size changed from %d x %d to %d x %d", h->R, h->C, R, C);
+    return -1;
+  }
+  if (n <= h->F) return 0;
+  const int W = (C + 31) / 32;
+  const size_t per = (size_t)h->Z * R;
+  int32_t *taken = nullptr, *rowcnt = nullptr, *rowoff = nullptr, *fcount = nullptr, *hf = nullptr;
+  uint32_t* bits = nullptr;
+  FCK(cudaMalloc(&taken, sizeof(int32_t) * per * C * n));
+  FCK(cudaMalloc(&bits, sizeof(uint32_t) * per * W * n));
+  FCK(cudaMalloc(&rowcnt, sizeof(int32_t) * per * n));
+  FCK(cudaMalloc(&rowoff, sizeof(int32_t) * per * n));
+  FCK(cudaMalloc(&fcount, sizeof(int32_t) * (n + 1)));
+  FCK(cudaMallocHost(&hf, sizeof(int32_t) * (n + 1)));
+  FCK(cudaStreamSynchronize(s));
+  const size_t old = (size_t)h->F * per * C;
+  if (h->F > 0) FCK(cudaMemcpy(taken, h->d_taken, sizeof(int32_t) * old, cudaMemcpyDeviceToDevice));
+  const size_t fresh = per * C * n - old;
+  k_fill_i32<<<grid_for(fresh), kThreads, 0, s>>>(taken + old, fresh, 1 - h->n_dup);
+  h->launches += 1;
+  FCK(cudaGetLastError());
+  dfree(h->d_taken);
+  dfree(h->d_bits);
+  dfree(h->d_rowcnt);
+  dfree(h->d_rowoff);
+  dfree(h->d_fcount);
+  if (h->h_fcount) cudaFreeHost(h->h_fcount);
+  h->d_taken = taken;
+  h->d_bits = bits;
+  h->d_rowcnt = rowcnt;
+  h->d_rowoff = rowoff;
+  h->d_fcount = fcount;
+  h->h_fcount = hf;
+  h->R = R;
+  h->C = C;
+  h->W = W;
+  h->F = n;
+  return 0;
+}
+
+// Mark, scan and read back the counts of n frames; returns the total.
+int maxima_mark(Maxima* h, const double* d_img, int n, cudaStream_t s) {
+  const LMax a = lmax_args(h, d_img, n);
+  const int warps_per_block = kThreads / 32;
+  const int blocks = (a.nrows + warps_per_block - 1) / warps_per_block;
+  k_lmax_mark<<<blocks, kThreads, 0, s>>>(a);
+  k_lmax_scan<<<1, 1024, 0, s>>>(h->d_rowcnt, h->d_rowoff, a.nrows, h->Z * h->R, n, h->d_fcount);
+  h->launches += 2;
+  FCK(cudaGetLastError());
+  FCK(cudaMemcpyAsync(h->h_fcount, h->d_fcount, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s));
+  FCK(cudaStreamSynchronize(s));
+  return h->h_fcount[n];
+}
+
+int maxima_emit(Maxima* h, const double* d_img, int n, int cap, double sigma, cudaStream_t s) {
+  if (cap > h->out_cap) {
+    dfree(h->d_out);
+    const int want = std::max(cap, 1024);
+    FCK(cudaMalloc(&h->d_out, sizeof(double) * 4 * (size_t)want));
+    h->out_cap = want;
+  }
+  const LMax a = lmax_args(h, d_img, n);
+  const int warps_per_block = kThreads / 32;
+  const int blocks = (a.nrows + warps_per_block - 1) / warps_per_block;
+  k_lmax_emit<<<blocks, kThreads, 0, s>>>(a, h->d_rowoff, h->d_zvalues, h->d_out, cap, sigma);
+  h->launches += 1;
+  FCK(cudaGetLastError());
+  h->n_out = cap;
+  return 0;
+}
+
+// Find: mark + scan + emit every found peak; counts per frame to host.
+int maxima_find(Maxima* h, const double* d_img, int R, int C, int n, int32_t* counts, double sigma,
+                cudaStream_t s) {
+  if (maxima_frames(h, R, C, n, s)) return -1;
+  const int total = maxima_mark(h, d_img, n, s);
+  if (total < 0) return -1;
+  if (counts)
+    for (int f = 0; f < n; ++f) counts[f] = h->h_fcount[f];
+  if (maxima_emit(h, d_img, n, total, sigma, s)) return -1;
+  // the peak rows are complete when this returns: callers hand them to work
+  // on other streams (the fitter's)
+  FCK(cudaStreamSynchronize(s));
+  return total;
+}
+
+Maxima* maxima_create(int margin, int z_range, double radius, double threshold, const double* z_values,
+                      int n_planes, int n_dup) {
+  if (n_planes < 1 || !z_values) {
+    ferr("saMaximaCreate: need at least one plane and its z value");
+    return nullptr;
+  }
+  Maxima* h = new Maxima();
+  h->margin = margin;
+  h->z_range = z_range;
+  h->radius = radius;
+  h->threshold = threshold;
+  h->Z = n_planes;
+  h->n_dup = n_dup;
+  if (cudaMalloc(&h->d_zvalues, sizeof(double) * n_planes) != cudaSuccess ||
+      cudaMemcpy(h->d_zvalues, z_values, sizeof(double) * n_planes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    ferr("saMaximaCreate: device allocation failed");
+    maxima_free(h);
+    delete h;
+    return nullptr;
+  }
+  return h;
+}
+
+// ---------------------------------------------------------------------------
+// Fused Gaussian finder
+// ---------------------------------------------------------------------------
+
+struct Finder {
+  int R = 0, C = 0, F = 0;
+  MFilter *bg = nullptr, *fm = nullptr, *fv = nullptr;
+  Maxima* mx = nullptr;
+  double sigma = 1.0;
+  double* d_image = nullptr;    // F x R x C
+  double* d_bgest = nullptr;    // F x R x C: a given background (bg_estimate)
+  const double* d_background = nullptr;   // the current background (bg->d_last or d_bgest)
+  double* d_a = nullptr;        // F x R x C scratch (bg_var / image - fit)
+  double* d_b = nullptr;        // F x R x C scratch (foreground)
+  double* d_ratio = nullptr;    // F x R x C: masked foreground / noise
+  double* d_fit = nullptr;      // F x R x C staging of a host fit image
+  double* d_camvar = nullptr;   // R x C
+  double* d_mask = nullptr;     // R x C
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  int n_peaks = 0;
+};
+
+void finder_free_frames(Finder* h) {
+  dfree(h->d_image);
+  dfree(h->d_bgest);
+  dfree(h->d_a);
+  dfree(h->d_b);
+  dfree(h->d_ratio);
+  dfree(h->d_fit);
+}
+
+int finder_frames(Finder* h, int n) {
+  if (n <= h->F) return 0;
+  FCK(cudaStreamSynchronize(h->stream));
+  finder_free_frames(h);
+  const size_t bytes = sizeof(double) * (size_t)h->R * h->C * n;
+  FCK(cudaMalloc(&h->d_image, bytes));
+  FCK(cudaMalloc(&h->d_a, bytes));
+  FCK(cudaMalloc(&h->d_b, bytes));
+  FCK(cudaMalloc(&h->d_ratio, bytes));
+  h->d_background = nullptr;
+  h->F = n;
+  return 0;
+}
+
+// A per-frame array argument: device pointers are used as they are, host
+// arrays are staged into dst.
+const double* finder_input(Finder* h, const double* p, int on_device, double** dst, int n) {
+  if (!p || on_device) return p;
+  const size_t bytes = sizeof(double) * (size_t)h->R * h->C * n;
+  if (!*dst && cudaMalloc(dst, sizeof(double) * (size_t)h->R * h->C * h->F) != cudaSuccess) {
+    ferr("peak finder: device allocation failed");
+    return nullptr;
+  }
+  if (cudaMemcpyAsync(*dst, p, bytes, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) {
+    ferr("peak finder: host-to-device copy failed");
+    return nullptr;
+  }
+  return *dst;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+void* saFilterCreate(const double* psf, double max_diff, int x_size, int y_size, int estimate) {
+  (void)estimate;
+  return filter_create(psf, max_diff, x_size, y_size);
+}
+
+int saFilterConvolve(void* flt, const double* image, double* result) {
+  return filter_host(static_cast<MFilter*>(flt), image, result, 0);
+}
+
+int saFilterConvolveMemo(void* flt, const double* image, double* result) {
+  return filter_host(static_cast<MFilter*>(flt), image, result, 1);
+}
+
+void saFilterCleanup(void* flt) {
+  MFilter* m = static_cast<MFilter*>(flt);
+  if (!m) return;
+  cudaStreamSynchronize(m->stream);
+  filter_free(m);
+  delete m;
+}
+
+int saFilterConvolveDevice(void* flt, const double* d_images, int n_frames, int memo, double* d_result) {
+  MFilter* m = static_cast<MFilter*>(flt);
+  if (!m || !d_images || n_frames < 1) {
+    ferr("saFilterConvolveDevice: bad arguments");
+    return -1;
+  }
+  if (filter_run(m, d_images, n_frames, memo, m->stream)) return -1;
+  if (d_result)
+    FCK(cudaMemcpyAsync(d_result, m->d_last, sizeof(double) * (size_t)m->R * m->C * n_frames,
+                        cudaMemcpyDeviceToDevice, m->stream));
+  return 0;
+}
+
+const double* saFilterResultDevice(void* flt) {
+  MFilter* m = static_cast<MFilter*>(flt);
+  return m ? m->d_last : nullptr;
+}
+
+int saFilterInfo(void* flt, int32_t* out6) {
+  MFilter* m = static_cast<MFilter*>(flt);
+  if (!m || !out6) return -1;
+  out6[0] = m->separable;
+  out6[1] = m->na;
+  out6[2] = m->nb;
+  out6[3] = m->a0;
+  out6[4] = m->b0;
+  out6[5] = m->F;
+  return 0;
+}
+
+int saFilterSetStream(void* flt, void* stream) {
+  MFilter* m = static_cast<MFilter*>(flt);
+  if (!m) return -1;
+  m->stream = static_cast<cudaStream_t>(stream);
+  return 0;
+}
+
+int saCalcMaxPeaks(saFlmData* flm) {
+  if (!flm || !flm->images || !flm->taken || flm->zsize < 1) {
+    ferr("calcMaxPeaks: bad flmData");
+    return -1;
+  }
+  const int Z = flm->zsize, R = flm->ysize, C = flm->xsize;
+  const size_t plane = (size_t)R * C;
+  double* d_img = nullptr;
+  int32_t *d_taken = nullptr, *d_count = nullptr;
+  int n = -1;
+  if (cudaMalloc(&d_img, sizeof(double) * plane * Z) == cudaSuccess &&
+      cudaMalloc(&d_taken, sizeof(int32_t) * plane * Z) == cudaSuccess &&
+      cudaMalloc(&d_count, sizeof(int32_t)) == cudaSuccess) {
+    bool ok = cudaMemset(d_count, 0, sizeof(int32_t)) == cudaSuccess;
+    for (int z = 0; ok && z < Z; ++z)
+      ok = cudaMemcpy(d_img + plane * z, flm->images[z], sizeof(double) * plane, cudaMemcpyHostToDevice) ==
+               cudaSuccess &&
+           cudaMemcpy(d_taken + plane * z, flm->taken[z], sizeof(int32_t) * plane,
+                      cudaMemcpyHostToDevice) == cudaSuccess;
+    if (ok) {
+      LMax a{};
+      a.img = d_img;
+      a.taken = d_taken;
+      a.R = R;
+      a.C = C;
+      a.Z = Z;
+      a.nrows = Z * R;
+      a.margin = flm->margin;
+      a.threshold = flm->threshold;
+      k_lmax_count<<<grid_for(plane * Z), kThreads>>>(a, d_count);
+      int32_t hc = 0;
+      if (cudaGetLastError() == cudaSuccess &&
+          cudaMemcpy(&hc, d_count, sizeof(int32_t), cudaMemcpyDeviceToHost) == cudaSuccess)
+        n = hc;
+    }
+  }
+  if (n < 0) ferr("calcMaxPeaks: device step failed: %s", cudaGetErrorString(cudaGetLastError()));
+  dfree(d_img);
+  dfree(d_taken);
+  dfree(d_count);
+  return n;
+}
+
+void saFindLocalMaxima(saFlmData* flm, double* z, double* y, double* x, double* h) {
+  if (!flm || !flm->images || !flm->taken || !flm->z_values || flm->zsize < 1 || !z || !y || !x || !h) {
+    ferr("findLocalMaxima: bad flmData");
+    return;
+  }
+  const int Z = flm->zsize, R = flm->ysize, C = flm->xsize;
+  const size_t plane = (size_t)R * C;
+  Maxima* mh = maxima_create(flm->margin, flm->z_range, flm->radius, flm->threshold, flm->z_values, Z, 1);
+  if (!mh) return;
+  double* d_img = nullptr;
+  bool ok = cudaMalloc(&d_img, sizeof(double) * plane * Z) == cudaSuccess && maxima_frames(mh, R, C, 1, 0) == 0;
+  for (int k = 0; ok && k < Z; ++k)
+    ok = cudaMemcpy(d_img + plane * k, flm->images[k], sizeof(double) * plane, cudaMemcpyHostToDevice) ==
+             cudaSuccess &&
+         cudaMemcpy(mh->d_taken + plane * k, flm->taken[k], sizeof(int32_t) * plane,
+                    cudaMemcpyHostToDevice) == cudaSuccess;
+  int total = ok ? maxima_mark(mh, d_img, 1, 0) : -1;
+  ok = total >= 0;
+  const int cap = ok ? std::min(total, std::max(flm->n_peaks, 0)) : 0;
+  if (ok && flm->n_peaks > 0 && total >= flm->n_peaks) printf("Warning! Found maximum number of peaks!\n");
+  ok = ok && maxima_emit(mh, d_img, 1, cap, 0.0, 0) == 0;
+  std::vector<double> rows((size_t)cap * 4);
+  if (ok && cap > 0)
+    ok = cudaMemcpy(rows.data(), mh->d_out, sizeof(double) * rows.size(), cudaMemcpyDeviceToHost) == cudaSuccess;
+  for (int k = 0; ok && k < Z; ++k)
+    ok = cudaMemcpy(flm->taken[k], mh->d_taken + plane * k, sizeof(int32_t) * plane,
+                    cudaMemcpyDeviceToHost) == cudaSuccess;
+  if (ok) {
+    for (int i = 0; i < cap; ++i) {
+      x[i] = rows[4 * i];
+      y[i] = rows[4 * i + 1];
+      z[i] = rows[4 * i + 2];
+      h[i] = rows[4 * i + 3];
+    }
+    flm->n_peaks = cap;
+  } else {
+    ferr("findLocalMaxima: device step failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  dfree(d_img);
+  maxima_free(mh);
+  delete mh;
+}
+
+void* saMaximaCreate(int margin, int z_range, double radius, double threshold, const double* z_values,
+                     int n_planes, int n_duplicates) {
+  return maxima_create(margin, z_range, radius, threshold, z_values, n_planes, n_duplicates);
+}
+
+int saMaximaFind(void* mh, const double* images, int on_device, int rows, int cols, int n_frames,
+                 int32_t* counts, double sigma) {
+  Maxima* h = static_cast<Maxima*>(mh);
+  if (!h || !images || rows < 1 || cols < 1 || n_frames < 1) {
+    ferr("saMaximaFind: bad arguments");
+    return -1;
+  }
+  const double* d_img = images;
+  if (!on_device) {
+    const size_t bytes = sizeof(double) * (size_t)n_frames * h->Z * rows * cols;
+    if (bytes > h->stage_bytes) {
+      dfree(h->d_stage);
+      FCK(cudaMalloc(&h->d_stage, bytes));
+      h->stage_bytes = bytes;
+    }
+    FCK(cudaMemcpyAsync(h->d_stage, images, bytes, cudaMemcpyHostToDevice, h->stream));
+    d_img = h->d_stage;
+  }
+  return maxima_find(h, d_img, rows, cols, n_frames, counts, sigma, h->stream);
+}
+
+const double* saMaximaPeaksDevice(void* mh) {
+  Maxima* h = static_cast<Maxima*>(mh);
+  return h ? h->d_out : nullptr;
+}
+
+int saMaximaGetPeaks(void* mh, double* rows) {
+  Maxima* h = static_cast<Maxima*>(mh);
+  if (!h || !rows) return -1;
+  if (h->n_out > 0) {
+    FCK(cudaMemcpyAsync(rows, h->d_out, sizeof(double) * 4 * (size_t)h->n_out, cudaMemcpyDeviceToHost,
+                        h->stream));
+    FCK(cudaStreamSynchronize(h->stream));
+  }
+  return h->n_out;
+}
+
+int saMaximaResetTaken(void* mh) {
+  Maxima* h = static_cast<Maxima*>(mh);
+  if (!h) return -1;
+  return maxima_reset(h, h->stream);
+}
+
+int saMaximaGetTaken(void* mh, int32_t* taken) {
+  Maxima* h = static_cast<Maxima*>(mh);
+  if (!h || !taken) return -1;
+  if (h->F > 0) {
+    FCK(cudaMemcpyAsync(taken, h->d_taken, sizeof(int32_t) * (size_t)h->F * h->Z * h->R * h->C,
+                        cudaMemcpyDeviceToHost, h->stream));
+    FCK(cudaStreamSynchronize(h->stream));
+  }
+  return h->F;
+}
+
+int saMaximaSetStream(void* mh, void* stream) {
+  Maxima* h = static_cast<Maxima*>(mh);
+  if (!h) return -1;
+  h->stream = static_cast<cudaStream_t>(stream);
+  return 0;
+}
+
+void saMaximaCleanup(void* mh) {
+  Maxima* h = static_cast<Maxima*>(mh);
+  if (!h) return;
+  cudaStreamSynchronize(h->stream);
+  maxima_free(h);
+  delete h;
+}
+
+void* saFinderCreate(int rows, int cols, void* bg_filter, void* fg_filter, void* fv_filter, int margin,
+                     double radius, double threshold, double z_value, double sigma) {
+  MFilter* bg = static_cast<MFilter*>(bg_filter);
+  MFilter* fm = static_cast<MFilter*>(fg_filter);
+  MFilter* fv = static_cast<MFilter*>(fv_filter);
+  if (rows < 1 || cols < 1 || !bg || (!fm) != (!fv)) {
+    ferr("saFinderCreate: need a background filter and both or neither foreground filters");
+    return nullptr;
+  }
+  for (MFilter* m : {bg, fm, fv})
+    if (m && (m->R != rows || m->C != cols)) {
+      ferr("saFinderCreate: a filter is %d x %d, the frames %d x %d", m->R, m->C, rows, cols);
+      return nullptr;
+    }
+  Maxima* mx = maxima_create(margin + 1, 1, radius, threshold, &z_value, 1, 1);
+  if (!mx) return nullptr;
+  Finder* h = new Finder();
+  h->R = rows;
+  h->C = cols;
+  h->bg = bg;
+  h->fm = fm;
+  h->fv = fv;
+  h->mx = mx;
+  h->sigma = sigma;
+  return h;
+}
+
+int saFinderSetVariance(void* fh, const double* camera_variance) {
+  Finder* h = static_cast<Finder*>(fh);
+  if (!h) return -1;
+  if (!camera_variance) {
+    dfree(h->d_camvar);
+    return 0;
+  }
+  const size_t bytes = sizeof(double) * (size_t)h->R * h->C;
+  if (!h->d_camvar) FCK(cudaMalloc(&h->d_camvar, bytes));
+  FCK(cudaMemcpyAsync(h->d_camvar, camera_variance, bytes, cudaMemcpyHostToDevice, h->stream));
+  FCK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int saFinderSetMask(void* fh, const double* peak_mask) {
+  Finder* h = static_cast<Finder*>(fh);
+  if (!h) return -1;
+  if (!peak_mask) {
+    dfree(h->d_mask);
+    return 0;
+  }
+  const size_t bytes = sizeof(double) * (size_t)h->R * h->C;
+  if (!h->d_mask) FCK(cudaMalloc(&h->d_mask, bytes));
+  FCK(cudaMemcpyAsync(h->d_mask, peak_mask, bytes, cudaMemcpyHostToDevice, h->stream));
+  FCK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int saFinderNewImages(void* fh, const double* images, int n_frames, int on_device) {
+  Finder* h = static_cast<Finder*>(fh);
+  if (!h || !images || n_frames < 1) {
+    ferr("saFinderNewImages: bad arguments");
+    return -1;
+  }
+  if (h->F > 0 && n_frames != h->F) {
+    ferr("saFinderNewImages: the handle holds %d frames, got %d", h->F, n_frames);
+    return -1;
+  }
+  if (finder_frames(h, n_frames)) return -1;
+  const size_t bytes = sizeof(double) * (size_t)h->R * h->C * n_frames;
+  FCK(cudaMemcpyAsync(h->d_image, images, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                      h->stream));
+  if (maxima_frames(h->mx, h->R, h->C, n_frames, h->stream)) return -1;
+  if (maxima_reset(h->mx, h->stream)) return -1;
+  h->d_background = nullptr;
+  return 0;
+}
+
+int saFinderEstimateBackground(void* fh, const double* fit, const double* bg_estimate, int on_device) {
+  Finder* h = static_cast<Finder*>(fh);
+  if (!h || h->F < 1) {
+    ferr("saFinderEstimateBackground: no images");
+    return -1;
+  }
+  const int n = h->F;
+  const size_t total = (size_t)h->R * h->C * n;
+  if (bg_estimate) {
+    const double* b = finder_input(h, bg_estimate, on_device, &h->d_bgest, n);
+    if (!b) return -1;
+    h->d_background = b;
+    return 0;
+  }
+  const double* f = finder_input(h, fit, on_device, &h->d_fit, n);
+  if (fit && !f) return -1;
+  k_sub<<<grid_for(total), kThreads, 0, h->stream>>>(h->d_image, f, h->d_a, total);
+  h->launches += 1;
+  FCK(cudaGetLastError());
+  const int64_t l0 = h->bg->launches;
+  if (filter_run(h->bg, h->d_a, n, 1, h->stream)) return -1;
+  h->launches += h->bg->launches - l0;
+  h->d_background = h->bg->d_last;
+  return 0;
+}
+
+int saFinderFindPeaks(void* fh, const double* fit, int on_device, int32_t* counts) {
+  Finder* h = static_cast<Finder*>(fh);
+  if (!h || h->F < 1 || !h->d_background) {
+    ferr("saFinderFindPeaks: call saFinderNewImages and saFinderEstimateBackground first");
+    return -1;
+  }
+  const int n = h->F, npix = h->R * h->C;
+  const size_t total = (size_t)npix * n;
+  const double* f = finder_input(h, fit, on_device, &h->d_fit, n);
+  if (fit && !f) return -1;
+  k_find_prep<<<grid_for(total), kThreads, 0, h->stream>>>(h->d_image, h->d_background, f, h->d_camvar, h->d_a,
+                                                           h->d_b, npix, total);
+  h->launches += 1;
+  FCK(cudaGetLastError());
+  const double* bgv = h->d_a;
+  const double* fg = h->d_b;
+  if (h->fv) {
+    const int64_t l0 = h->fv->launches + h->fm->launches;
+    if (filter_run(h->fv, h->d_a, n, 1, h->stream)) return -1;
+    if (filter_run(h->fm, h->d_b, n, 1, h->stream)) return -1;
+    h->launches += h->fv->launches + h->fm->launches - l0;
+    bgv = h->fv->d_last;
+    fg = h->fm->d_last;
+  }
+  k_find_ratio<<<grid_for(total), kThreads, 0, h->stream>>>(fg, bgv, h->d_mask, h->d_ratio, npix, total);
+  h->launches += 1;
+  FCK(cudaGetLastError());
+  const int64_t l0 = h->mx->launches;
+  const int found = maxima_find(h->mx, h->d_ratio, h->R, h->C, n, counts, h->sigma, h->stream);
+  h->launches += h->mx->launches - l0;
+  if (found < 0) return -1;
+  h->n_peaks = found;
+  return found;
+}
+
+const double* saFinderBackgroundDevice(void* fh) {
+  Finder* h = static_cast<Finder*>(fh);
+  return h ? h->d_background : nullptr;
+}
+
+const double* saFinderPeaksDevice(void* fh) {
+  Finder* h = static_cast<Finder*>(fh);
+  return h ? h->mx->d_out : nullptr;
+}
+
+int saFinderGetPeaks(void* fh, double* rows) {
+  Finder* h = static_cast<Finder*>(fh);
+  if (!h) return -1;
+  return saMaximaGetPeaks(h->mx, rows);
+}
+
+int saFinderGetArray(void* fh, int which, double* out) {
+  Finder* h = static_cast<Finder*>(fh);
+  if (!h || !out || h->F < 1) return -1;
+  const double* src = which == 0 ? h->d_background : which == 1 ? h->d_ratio : nullptr;
+  if (!src) {
+    ferr("saFinderGetArray: nothing to return for %d", which);
+    return -1;
+  }
+  FCK(cudaMemcpyAsync(out, src, sizeof(double) * (size_t)h->R * h->C * h->F, cudaMemcpyDeviceToHost,
+                      h->stream));
+  FCK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int saFinderSetStream(void* fh, void* stream) {
+  Finder* h = static_cast<Finder*>(fh);
+  if (!h) return -1;
+  h->stream = static_cast<cudaStream_t>(stream);
+  h->mx->stream = h->stream;
+  return 0;
+}
+
+int64_t saFinderKernelLaunches(void* fh) {
+  Finder* h = static_cast<Finder*>(fh);
+  return h ? h->launches : -1;
+}
+
+void saFinderCleanup(void* fh) {
+  Finder* h = static_cast<Finder*>(fh);
+  if (!h) return;
+  cudaStreamSynchronize(h->stream);
+  finder_free_frames(h);
+  dfree(h->d_camvar);
+  dfree(h->d_mask);
+  maxima_free(h->mx);
+  delete h->mx;
+  delete h;
+}
+
+}  // extern "C"

@@ -7,6 +7,9 @@
 
 namespace sa {
 
+// Print msg and keep it for saGetLastError (defined in sa_api.cu).
+void record_error(const char* msg);
+
 template <typename T>
 struct Launch {
   // Set shared-memory limits of the kernels; returns the sweep CTA count

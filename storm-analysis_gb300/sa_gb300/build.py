@@ -1,8 +1,11 @@
 """
 Build libsa_cuda.so (the engine) from storm-analysis_gb300/csrc for sm_103a.
 
-The three translation units are compiled in parallel with nvcc and linked
-into sa_gb300/libsa_cuda.so; only the CUDA runtime is linked (no torch).
+The four translation units (the fitter for float and double pixels, the
+fitter's host API and the peak finder) are compiled in parallel with nvcc
+and linked into sa_gb300/libsa_cuda.so; only the CUDA runtime is linked (no
+torch).  libsa_matched_filter.so, the reference-named matched-filter entry
+points, is linked against it.
 """
 import concurrent.futures
 import os
@@ -15,9 +18,10 @@ REPO = os.path.dirname(PKG_ROOT)
 CSRC = os.path.join(PKG_ROOT, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIB = os.path.join(HERE, "libsa_cuda.so")
+MF_LIB = os.path.join(HERE, "libsa_matched_filter.so")
 BUILD_DIR = os.path.join(PKG_ROOT, "_build")
 
-SOURCES = ["sa_launch_f32.cu", "sa_launch_f64.cu", "sa_api.cu"]
+SOURCES = ["sa_launch_f32.cu", "sa_launch_f64.cu", "sa_api.cu", "sa_finder.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
 
@@ -39,9 +43,9 @@ def _compile(src, verbose):
 
 
 def _stale():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(MF_LIB):
         return True
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(MF_LIB))
     for d in (CSRC, INCLUDE):
         for f in os.listdir(d):
             if os.path.getmtime(os.path.join(d, f)) > t:
@@ -66,6 +70,14 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    tmp = MF_LIB + ".tmp"
+    cmd = [nvcc(), "-shared", "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE, "-o", tmp,
+           os.path.join(CSRC, "sa_matched_filter.cpp"), "-L", HERE, "-lsa_cuda",
+           "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link of libsa_matched_filter.so failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, MF_LIB)
     return LIB
 
 

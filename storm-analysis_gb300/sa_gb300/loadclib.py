@@ -153,6 +153,44 @@ def _declare(lib):
     lib.saSlotResults.argtypes = [hp, ci, f64, i32]
     lib.saSlotResults.restype = ci
 
+    # peak finder (include/sa_finder.h)
+    i64r = ctypes.c_int64
+    for name, args, res in [
+            ("saFilterCreate", [f64, cd, ci, ci, ci], vp),
+            ("saFilterConvolve", [vp, f64, f64], ci),
+            ("saFilterConvolveMemo", [vp, f64, f64], ci),
+            ("saFilterCleanup", [vp], None),
+            ("saFilterConvolveDevice", [vp, vp, ci, ci, vp], ci),
+            ("saFilterResultDevice", [vp], vp),
+            ("saFilterInfo", [vp, i32], ci),
+            ("saFilterSetStream", [vp, vp], ci),
+            ("saCalcMaxPeaks", [vp], ci),
+            ("saFindLocalMaxima", [vp, f64, f64, f64, f64], None),
+            ("saMaximaCreate", [ci, ci, cd, cd, f64, ci, ci], vp),
+            ("saMaximaFind", [vp, vp, ci, ci, ci, ci, i32, cd], ci),
+            ("saMaximaPeaksDevice", [vp], vp),
+            ("saMaximaGetPeaks", [vp, f64], ci),
+            ("saMaximaResetTaken", [vp], ci),
+            ("saMaximaGetTaken", [vp, i32], ci),
+            ("saMaximaSetStream", [vp, vp], ci),
+            ("saMaximaCleanup", [vp], None),
+            ("saFinderCreate", [ci, ci, vp, vp, vp, ci, cd, cd, cd, cd], vp),
+            ("saFinderSetVariance", [vp, vp], ci),
+            ("saFinderSetMask", [vp, vp], ci),
+            ("saFinderNewImages", [vp, vp, ci, ci], ci),
+            ("saFinderEstimateBackground", [vp, vp, vp, ci], ci),
+            ("saFinderFindPeaks", [vp, vp, ci, i32], ci),
+            ("saFinderBackgroundDevice", [vp], vp),
+            ("saFinderPeaksDevice", [vp], vp),
+            ("saFinderGetPeaks", [vp, f64], ci),
+            ("saFinderGetArray", [vp, ci, f64], ci),
+            ("saFinderSetStream", [vp, vp], ci),
+            ("saFinderKernelLaunches", [vp], i64r),
+            ("saFinderCleanup", [vp], None)]:
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+
 
 EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoInitialize3D",
            "daoInitializeZ", "daoNewPeaks", "daoCleanup", "daoInitialize2DFixedALS",
@@ -172,3 +210,17 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice", "saGetSweepTimes",
            "saGetFitImageNoAlloc", "saSlotLoad", "saSlotLaunch", "saSlotPoll", "saSlotReady", "saSlotResults",
            "saSetSweepCTAs"]
+
+FINDER_EXPORTS = ["saFilterCreate", "saFilterConvolve", "saFilterConvolveMemo", "saFilterCleanup",
+                  "saFilterConvolveDevice", "saFilterResultDevice", "saFilterInfo", "saFilterSetStream",
+                  "saCalcMaxPeaks", "saFindLocalMaxima", "saMaximaCreate", "saMaximaFind",
+                  "saMaximaPeaksDevice", "saMaximaGetPeaks", "saMaximaResetTaken", "saMaximaGetTaken",
+                  "saMaximaSetStream", "saMaximaCleanup", "saFinderCreate", "saFinderSetVariance",
+                  "saFinderSetMask", "saFinderNewImages", "saFinderEstimateBackground",
+                  "saFinderFindPeaks", "saFinderBackgroundDevice", "saFinderPeaksDevice",
+                  "saFinderGetPeaks", "saFinderGetArray", "saFinderSetStream", "saFinderKernelLaunches",
+                  "saFinderCleanup"]
+
+# libsa_matched_filter.so: the reference's matched-filter names
+MATCHED_FILTER_EXPORTS = ["cleanup", "convolve", "convolveMemo", "initialize"]
+MF_LIB_PATH = os.path.join(HERE, "libsa_matched_filter.so")

@@ -135,3 +135,49 @@ def test_spline_handle_from_reference_library(lib):
         geo.append((c.roi_n_index, c.fit_size_x, c.jac_size, c.xoff))
         lib.cfCleanup(h)
     assert geo[0] == geo[1] and geo[0][1] == 8 and geo[0][2] == 5
+
+
+def _declared(header):
+    src = open(os.path.join(ROOT, "include", header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", src)
+    return sorted(set(names) - {"if", "for", "while", "return", "sizeof"})
+
+
+def _exported(path):
+    nm = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True,
+                        check=True).stdout
+    return set(line.split()[-1] for line in nm.splitlines() if " T " in line)
+
+
+def test_finder_exports_header(lib):
+    """The peak finder's entry points (include/sa_finder.h) are exported by
+    libsa_cuda.so, and libsa_matched_filter.so exports the reference's
+    matched-filter names (include/sa_matched_filter.h)."""
+    from sa_gb300 import loadclib
+    declared = _declared("sa_finder.h")
+    assert len(declared) >= 30
+    assert [n for n in declared if n not in _exported(loadclib.LIB_PATH)] == []
+    assert sorted(loadclib.FINDER_EXPORTS) == declared
+    mf = _declared("sa_matched_filter.h")
+    assert mf == ["cleanup", "convolve", "convolveMemo", "initialize"]
+    assert sorted(loadclib.MATCHED_FILTER_EXPORTS) == mf
+    assert set(mf) <= _exported(loadclib.MF_LIB_PATH)
+
+
+def test_finder_without_device_fails_loudly(lib):
+    """No CUDA device: the finder classes raise and the C entry points
+    return NULL with a recorded message -- there is no CPU fallback."""
+    from sa_gb300 import fitting, loadclib, matched_filter_c
+    if lib.saDeviceCount() > 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(loadclib.EngineUnavailable):
+        matched_filter_c.MatchedFilter(numpy.ones((8, 8)))
+    with pytest.raises(loadclib.EngineUnavailable):
+        fitting.PeakFinderGaussian({"find_max_radius": 5, "iterations": 1, "sigma": 1.5, "threshold": 6.0,
+                                    "background_sigma": 8.0, "roi_size": 18})
+    psf = numpy.zeros((16, 16))
+    psf[0, 0] = 1.0
+    lib.saClearLastError()
+    assert not lib.saFilterCreate(psf, 0.0, 16, 16, 0)
+    assert "saFilterCreate" in loadclib.last_error() or "failed" in loadclib.last_error()

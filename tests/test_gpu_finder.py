@@ -1,0 +1,295 @@
+"""The GPU peak finder against the CPU oracle (oracle/finder.py) and the
+golden fixture of the reference's own local-maxima C:
+
+  * matched filters (separable and 2D paths, even / odd / clamped sizes,
+    memoisation, the reference-named libsa_matched_filter.so);
+  * the local-maxima finder, bit-exact (peak lists and taken counts) on the
+    reference's outputs, through the handle and the flmData entry points;
+  * PeakFinderGaussian.peakFinder on synthetic 512 x 512 frames (with and
+    without the foreground filter, camera variance and an AOI mask), and
+    the batched finder with its device hand-off to the fitter.
+
+Tolerances: convolutions agree with numpy's FFT convolution to 1e-12 of the
+result's magnitude (the two sum in different orders); the found peak lists
+are compared exactly.
+"""
+import ctypes
+import os
+
+import numpy
+import pytest
+
+from oracle import finder as F
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "g_finder.npz")
+CONV_RTOL = 1e-12
+
+PARAMS = dict(background_sigma=8.0, foreground_sigma=1.0, find_max_radius=5, iterations=20, sigma=1.5,
+              threshold=6.0, roi_size=18)
+
+
+def conv_close(got, ref):
+    return numpy.abs(got - ref).max() <= CONV_RTOL * max(numpy.abs(ref).max(), 1.0)
+
+
+@pytest.mark.parametrize("shape,sigma", [((80, 90), 1.0), ((41, 53), 2.0), ((41, 53), 8.0),
+                                         ((534, 534), 8.0), ((75, 64), 1.5)])
+def test_matched_filter_separable(shape, sigma):
+    from sa_gb300 import matched_filter_c
+    rng = numpy.random.default_rng(int(sigma * 10) + shape[0])
+    psf = F.gaussian_psf(shape, sigma)
+    g = matched_filter_c.MatchedFilter(psf)
+    assert g.info()[0] == 1
+    o = F.MatchedFilter(psf)
+    for _ in range(2):
+        img = rng.uniform(0.0, 200.0, shape)
+        assert conv_close(g.convolve(img), o.convolve(img))
+    g.cleanup()
+
+
+def test_matched_filter_psf_squared_and_2d_path():
+    from sa_gb300 import matched_filter_c
+    rng = numpy.random.default_rng(8)
+    psf = F.gaussian_psf((64, 48), 1.0)
+    sq = psf * psf
+    g = matched_filter_c.MatchedFilter(sq)
+    img = rng.uniform(0.0, 50.0, (64, 48))
+    assert conv_close(g.convolve(img), F.MatchedFilter(sq).convolve(img))
+    g.cleanup()
+    # a PSF that is not rank 1: the direct 2D path, support straddling the wrap
+    blob = numpy.zeros((37, 45))
+    blob[14:23, 17:28] = rng.uniform(0.0, 1.0, (9, 11))
+    g = matched_filter_c.MatchedFilter(blob)
+    info = g.info()
+    assert info[0] == 0 and info[1] == 9 and info[2] == 11
+    for _ in range(2):
+        img = rng.uniform(-5.0, 50.0, (37, 45))
+        assert conv_close(g.convolve(img), F.MatchedFilter(blob).convolve(img))
+    g.cleanup()
+
+
+def test_matched_filter_memo_and_normalisation():
+    """The reference's matched-filter tests: unit-sum PSF keeps the sum;
+    memoisation returns the previous result while no pixel moved more than
+    max_diff and recomputes after."""
+    from sa_gb300 import matched_filter_c
+    psf = F.gaussian_psf((80, 90), 1.0)
+    g = matched_filter_c.MatchedFilter(psf)
+    for i in range(1, 5):
+        img = numpy.zeros((80, 90))
+        img[40, 45] = float(i)
+        assert abs(img.sum() - g.convolve(img).sum()) < 1e-6
+    g.cleanup()
+    psf = F.gaussian_psf((40, 50), 2.0)
+    g = matched_filter_c.MatchedFilter(psf, memoize=True, max_diff=0.1)
+    o = F.MatchedFilter(psf, memoize=True, max_diff=0.1)
+    assert numpy.array_equal(g.convolve(numpy.zeros((40, 50))), o.convolve(numpy.zeros((40, 50))))
+    seq = [1.0, 1.05, 1.1, 1.0, 1.0]
+    prev = None
+    for v in seq:
+        img = numpy.zeros((40, 50))
+        img[20, 25] = v
+        r, ro = g.convolve(img), o.convolve(img)
+        assert conv_close(r, ro)
+        if prev is not None and v in (1.05,):
+            assert numpy.abs(r - prev).max() < 1e-12
+        prev = r
+    g.cleanup()
+
+
+def test_reference_named_matched_filter_library():
+    """libsa_matched_filter.so answers the reference binding's calls
+    (matched_filter_c.py:17-34): initialize / convolve / convolveMemo /
+    cleanup with host arrays."""
+    from numpy.ctypeslib import ndpointer
+    from sa_gb300 import loadclib
+    loadclib.load()
+    mf = ctypes.CDLL(loadclib.MF_LIB_PATH)
+    f64 = ndpointer(dtype=numpy.float64)
+    mf.initialize.argtypes = [f64, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    mf.initialize.restype = ctypes.c_void_p
+    mf.convolve.argtypes = [ctypes.c_void_p, f64, f64]
+    mf.convolveMemo.argtypes = [ctypes.c_void_p, f64, f64]
+    mf.cleanup.argtypes = [ctypes.c_void_p]
+    psf = F.gaussian_psf((60, 70), 2.0)
+    rc = numpy.ascontiguousarray(F.recenter_psf(psf))
+    h = mf.initialize(rc, 1.0e-3, 60, 70, 1)
+    img = numpy.random.default_rng(2).uniform(0, 10, (60, 70))
+    out = numpy.zeros((60, 70))
+    mf.convolve(h, img, out)
+    assert conv_close(out, F.MatchedFilter(psf).convolve(img))
+    out2 = numpy.zeros((60, 70))
+    mf.convolveMemo(h, img, out2)
+    assert conv_close(out2, out)
+    mf.cleanup(h)
+
+
+def _lm_cases(g):
+    i = 0
+    while "lm%d_images" % i in g:
+        yield i
+        i += 1
+
+
+def test_local_maxima_match_reference_golden():
+    """MaximaFinder on the GPU returns the reference's peaks and taken
+    counts exactly, call after call (ties, planes, fractional radii)."""
+    from sa_gb300 import ia_utilities_c
+    g = numpy.load(GOLDEN)
+    for i in _lm_cases(g):
+        imgs = [numpy.ascontiguousarray(a) for a in g["lm%d_images" % i]]
+        m, r, thr, zr, calls, nd = g["lm%d_params" % i]
+        zv = list(g["lm%d_zvalues" % i])
+        mx = ia_utilities_c.MaximaFinder(margin=int(m) - 1, n_duplicates=int(nd), radius=float(r),
+                                         threshold=float(thr), z_range=int(zr), z_values=zv)
+        for c in range(int(calls)):
+            x, y, z, h = mx.findMaxima(imgs, want_height=True)
+            got = numpy.stack([x, y, z, h]) if x.size else numpy.zeros((4, 0))
+            assert numpy.array_equal(got, g["lm%d_c%d_xyzh" % (i, c)]), (i, c)
+            assert numpy.array_equal(mx.getTaken(), g["lm%d_c%d_taken" % (i, c)]), (i, c)
+        mx.resetTaken()
+        assert numpy.all(mx.getTaken() == 1 - int(nd))
+        mx.cleanup()
+
+
+def test_flmdata_entry_points_match_reference_golden():
+    """saCalcMaxPeaks / saFindLocalMaxima with the reference's flmData and
+    host arrays (the calls ia_utilities_c.py:214-225 makes)."""
+    from sa_gb300 import ia_utilities_c
+    g = numpy.load(GOLDEN)
+    for i in _lm_cases(g):
+        imgs = [numpy.ascontiguousarray(a) for a in g["lm%d_images" % i]]
+        m, r, thr, zr, calls, nd = g["lm%d_params" % i]
+        zv = numpy.ascontiguousarray(g["lm%d_zvalues" % i], dtype=numpy.float64)
+        taken = [numpy.ascontiguousarray(numpy.ones(imgs[0].shape, numpy.int32) - int(nd)) for _ in imgs]
+        P = ctypes.c_void_p * len(imgs)
+        c_img = P(*[a.ctypes.data for a in imgs])
+        c_tk = P(*[t.ctypes.data for t in taken])
+        flm = ia_utilities_c.FlmData(margin=int(m), n_peaks=0, z_range=int(zr), xsize=imgs[0].shape[1],
+                                     ysize=imgs[0].shape[0], zsize=len(imgs), radius=float(r),
+                                     threshold=float(thr), z_values=zv.ctypes.data,
+                                     taken=ctypes.addressof(c_tk), images=ctypes.addressof(c_img))
+        for c in range(int(calls)):
+            n = ia_utilities_c.calc_max_peaks(flm)
+            assert n == int(g["lm%d_c%d_max" % (i, c)])
+            out = [numpy.zeros(n + 1) for _ in range(4)]
+            flm.n_peaks = n + 1
+            k = ia_utilities_c.find_local_maxima(flm, *out)
+            z, y, x, h = (a[:k] for a in out)
+            got = numpy.stack([x, y, z, h]) if k else numpy.zeros((4, 0))
+            assert numpy.array_equal(got, g["lm%d_c%d_xyzh" % (i, c)]), (i, c)
+            assert numpy.array_equal(numpy.stack(taken), g["lm%d_c%d_taken" % (i, c)]), (i, c)
+    # the n_peaks cap: the first n_peaks maxima, taken advanced for those only
+    imgs = [numpy.ascontiguousarray(a) for a in g["lm0_images"]]
+    m, r, thr, zr, calls, nd = g["lm0_params"]
+    full = g["lm0_c0_xyzh"]
+    taken = [numpy.zeros(imgs[0].shape, numpy.int32)]
+    c_img = (ctypes.c_void_p * 1)(imgs[0].ctypes.data)
+    c_tk = (ctypes.c_void_p * 1)(taken[0].ctypes.data)
+    zv = numpy.ascontiguousarray(g["lm0_zvalues"])
+    flm = ia_utilities_c.FlmData(margin=int(m), n_peaks=10, z_range=int(zr), xsize=imgs[0].shape[1],
+                                 ysize=imgs[0].shape[0], zsize=1, radius=float(r), threshold=float(thr),
+                                 z_values=zv.ctypes.data, taken=ctypes.addressof(c_tk),
+                                 images=ctypes.addressof(c_img))
+    out = [numpy.zeros(10) for _ in range(4)]
+    assert ia_utilities_c.find_local_maxima(flm, *out) == 10
+    assert numpy.array_equal(out[2], full[0, :10]) and numpy.array_equal(out[1], full[1, :10])
+    assert int(taken[0].sum()) == 10
+
+
+def _frames(n, size=512, seed=3):
+    from sa_gb300 import synth
+    wl = synth.make_workload(1, frames=n, nx=size, ny=size, seed=seed)
+    return wl
+
+
+def _compare_finder(params, frames, camvar=None, fit_images=None, iterations=1):
+    from sa_gb300 import fitting
+    gf = fitting.PeakFinderGaussian(params)
+    of = F.PeakFinderGaussian(params)
+    if camvar is not None:
+        gf.setVariance(camvar)
+        of.setVariance(camvar)
+    n_peaks = 0
+    for k, img in enumerate(frames):
+        img = gf.padArray(img)
+        gf.newImage(img)
+        of.newImage(img)
+        fit = numpy.zeros(img.shape) if fit_images is None else gf.padArray(fit_images[k])
+        for it in range(iterations):
+            bg_g = gf.estimateBackground(fit)
+            bg_o = of.estimateBackground(fit)
+            assert conv_close(bg_g, bg_o)
+            pg, tg, dg = gf.findPeaks(fit)
+            po, to, do = of.findPeaks(fit)
+            assert (tg, dg) == (to, do)
+            for key in ("x", "y", "z", "sigma"):
+                assert numpy.array_equal(pg[key], po[key]), (k, it, key)
+            sg = gf.significance()
+            assert conv_close(sg, of.last_masked)
+            n_peaks += pg["x"].size
+    launches = gf.kernel_launches()
+    gf.cleanUp()
+    assert n_peaks > 0
+    return n_peaks, launches
+
+
+def test_peak_finder_matches_oracle_512():
+    wl = _frames(2)
+    n, launches = _compare_finder(PARAMS, wl["images"], iterations=2)
+    assert launches > 0
+
+
+def test_peak_finder_variants():
+    """No foreground filter; camera variance; an AOI box; a fit image."""
+    wl = _frames(1, size=256, seed=5)
+    p = dict(PARAMS)
+    p.pop("foreground_sigma")
+    _compare_finder(p, wl["images"])
+    cam = numpy.random.default_rng(1).gamma(2.0, 2.0, size=(256, 256))
+    _compare_finder(PARAMS, wl["images"], camvar=cam)
+    p = dict(PARAMS, x_start=20, x_stop=200, y_start=30, y_stop=220)
+    _compare_finder(p, wl["images"])
+    fit = [0.5 * numpy.asarray(wl["images"][0]) - 10.0]
+    _compare_finder(PARAMS, wl["images"], fit_images=fit, iterations=3)
+
+
+def test_batch_finder_matches_single_frames_and_hands_off():
+    """Four frames at once equal four single-frame runs; the device
+    hand-off to BatchFitter fits the same as loading the peaks from the
+    host."""
+    from sa_gb300 import engine, fitting
+    wl = _frames(4, size=256, seed=9)
+    pad = fitting.PeakFinderGaussian(PARAMS).margin
+    frames = numpy.stack([fitting.padArray(im, pad) for im in wl["images"]])
+    bf = fitting.BatchPeakFinder(PARAMS, frames.shape[1:], 4)
+    bf.newImages(frames)
+    bf.estimateBackground()
+    counts, done = bf.findPeaks()
+    peaks = bf.peaks()
+    bgs = bf.background()
+    for k in range(4):
+        of = F.PeakFinderGaussian(PARAMS)
+        of.newImage(frames[k])
+        bo = of.estimateBackground(numpy.zeros(frames[k].shape))
+        po, _, _ = of.findPeaks(numpy.zeros(frames[k].shape))
+        assert conv_close(bgs[k], bo)
+        assert counts[k] == po["x"].size
+        for key in ("x", "y", "z", "sigma"):
+            assert numpy.array_equal(peaks[k][key], po[key])
+    kw = dict(roi_size=18, sigma_range=[0.5, 4.0])
+    a = engine.BatchFitter("3d", frames.shape[1:], 4, precision=64, **kw)
+    bf.handoff(a)
+    a.fit(200)
+    ra = a.results()
+    b = engine.BatchFitter("3d", frames.shape[1:], 4, precision=64, **kw)
+    b.load(frames, bgs, peaks, "finder")
+    b.fit(200)
+    rb = b.results()
+    for key in ("x", "y", "height", "status"):
+        assert numpy.array_equal(ra[key], rb[key]), key
+    a.close()
+    b.close()
+    bf.cleanUp()

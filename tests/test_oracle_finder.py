@@ -1,0 +1,96 @@
+"""The CPU oracle of the peak finder (oracle/finder.py) against the golden
+fixture made from the reference's own C (tests/golden/make_golden_finder.py:
+draw_gaussians.c PSFs; ia_utilities.c calcMaxPeaks / findLocalMaxima with
+ties, several planes, fractional radii and repeated calls), and against the
+reference's own matched-filter test criteria (test/test_matched_filter.py)."""
+import os
+
+import numpy
+import pytest
+
+from oracle import finder as F
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "g_finder.npz")
+
+
+@pytest.fixture(scope="module")
+def g():
+    return numpy.load(GOLDEN)
+
+
+def test_psf_matches_reference_drawing(g):
+    for i in range(5):
+        shape = tuple(int(v) for v in g["psf%d_shape" % i])
+        psf = F.gaussian_psf(shape, float(g["psf%d_sigma" % i]))
+        assert numpy.abs(psf - g["psf%d" % i]).max() <= 1e-15 * g["psf%d" % i].max()
+
+
+def lm_cases(g):
+    i = 0
+    while "lm%d_images" % i in g:
+        yield i
+        i += 1
+
+
+def test_local_maxima_match_reference_exactly(g):
+    n_cases = 0
+    for i in lm_cases(g):
+        imgs = list(g["lm%d_images" % i])
+        m, r, thr, zr, calls, nd = g["lm%d_params" % i]
+        zv = list(g["lm%d_zvalues" % i])
+        taken = [numpy.ones(imgs[0].shape, numpy.int32) - int(nd) for _ in imgs]
+        for c in range(int(calls)):
+            n = F.calc_max_peaks(imgs, taken, int(m), thr)
+            x, y, z, h = F.find_local_maxima(imgs, taken, int(m), r, thr, int(zr), zv)
+            got = numpy.stack([x, y, z, h]) if x.size else numpy.zeros((4, 0))
+            assert n == int(g["lm%d_c%d_max" % (i, c)])
+            assert numpy.array_equal(got, g["lm%d_c%d_xyzh" % (i, c)])
+            assert numpy.array_equal(numpy.stack(taken), g["lm%d_c%d_taken" % (i, c)])
+            n_cases += 1
+    assert n_cases >= 9
+
+
+def _psf(shape, s):
+    return F.gaussian_psf(shape, s)
+
+
+def test_matched_filter_normalisation_and_numpy_fft():
+    """Unit-sum PSF keeps the image sum; the result is numpy's FFT
+    convolution with the recentred PSF."""
+    psf = _psf((80, 90), 1.0)
+    flt = F.MatchedFilter(psf)
+    for i in range(1, 5):
+        img = numpy.zeros((80, 90))
+        img[40, 45] = float(i)
+        conv = flt.convolve(img)
+        assert abs(img.sum() - conv.sum()) < 1e-6
+    img = numpy.zeros((80, 90))
+    img[40, 45] = 100.0
+    t = numpy.real(numpy.fft.ifft2(numpy.fft.fft2(F.recenter_psf(psf)) * numpy.fft.fft2(img)))
+    assert numpy.allclose(flt.convolve(img), t)
+
+
+def test_matched_filter_memo():
+    psf = _psf((40, 50), 2.0)
+    flt = F.MatchedFilter(psf, memoize=True, max_diff=0.1)
+    img = numpy.zeros((40, 50))
+    img[20, 25] = 1.0
+    r1 = flt.convolve(img)
+    img2 = img.copy()
+    img2[20, 25] = 1.05
+    assert numpy.abs(flt.convolve(img2) - r1).max() < 1e-12
+    img3 = img.copy()
+    img3[20, 25] = 1.1
+    assert numpy.abs(flt.convolve(img3) - r1).max() > 1e-12
+    # before any convolution a memo filter returns the recentred PSF
+    f2 = F.MatchedFilter(psf, memoize=True, max_diff=0.1)
+    assert numpy.array_equal(f2.convolve(numpy.zeros((40, 50))), F.recenter_psf(psf))
+
+
+def test_pad_array_mirrors_edges():
+    a = numpy.arange(20.0).reshape(4, 5)
+    p = F.pad_array(a, 2)
+    assert p.shape == (8, 9)
+    assert numpy.array_equal(p[2:6, 2:7], a)
+    assert numpy.array_equal(p[0:2, 2:7], numpy.flipud(a[0:2]))
+    assert numpy.array_equal(p[2:6, 0:2], numpy.fliplr(a[:, 0:2]))
