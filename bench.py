@@ -437,8 +437,13 @@ def run_finder(args, wl, torch):
     torch.cuda.synchronize()
     bf = fitting.BatchPeakFinder(FINDER_PARAMS, shape, F)
     found = []
+    count = [0]
 
-    def step(i, host=False):
+    def step(host=False):
+        # strictly alternating frame sets, across warm-up and timed steps:
+        # a repeated set would let the memoised filters skip their work
+        i = count[0]
+        count[0] += 1
         bf.newImages(p_sets[i % 2] if host else d_sets[i % 2])
         bf.estimateBackground()
         bf.findPeaks()
@@ -451,14 +456,14 @@ def run_finder(args, wl, torch):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        for i in range(k):
-            step(i, host)
+        for _ in range(k):
+            step(host)
         e1.record()
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / k
 
-    for i in range(max(args.warmup, 3)):
-        step(i)
+    for _ in range(max(args.warmup, 3)):
+        step()
     l0 = bf.kernel_launches()
     del found[:]
     ms = timed(args.steps)
