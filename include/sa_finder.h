@@ -103,6 +103,58 @@ int saMaximaGetTaken(void *mh, int32_t *taken);
 int saMaximaSetStream(void *mh, void *stream);
 void saMaximaCleanup(void *mh);
 
+/* ---- Post-fit culling ---------------------------------------------------- */
+
+/* The neighbour queries of the find / fit loop (sa_library/fitting.py:
+ * 716-782), on host arrays as the reference binds them.  The reference
+ * searches a kd-tree (dbscan/kdtree.c) per call; here a uniform grid of
+ * cells at least the radius wide is built on the GPU.  A point is a
+ * neighbour when dx*dx + dy*dy <= r*r.  Statuses: 0 RUNNING, 1 CONVERGED,
+ * 2 ERROR. */
+/* ia_utilities.c:221 markDimmerPeaks: non-ERROR peaks with a brighter peak
+ * within r_removal become ERROR, and CONVERGED peaks within r_neighbors of
+ * one become RUNNING; returns the number marked. */
+int saMarkDimmerPeaks(double *x, double *y, double *h, int32_t *status, double r_removal, double r_neighbors,
+                      int np);
+/* ia_utilities.c:292 markLowSignificancePeaks: non-ERROR peaks whose
+ * significance is not above min_sig become ERROR, with the same neighbour
+ * rule; returns the number marked. */
+int saMarkLowSignificancePeaks(double *x, double *y, double *sig, int32_t *status, double min_sig,
+                               double r_neighbors, int np);
+/* ia_utilities.c:401 runningIfHasNeighbors: current peaks that are neither
+ * RUNNING nor ERROR become RUNNING when a new peak is within radius. */
+void saRunningIfHasNeighbors(double *c_x, double *c_y, double *n_x, double *n_y, int32_t *status, double radius,
+                             int nc, int nn);
+/* ia_utilities.c:82 createKDTree / :166 freeKDTree / :347 nearestKDTree:
+ * distance to and index of the nearest point within radius (-1 / -1 when
+ * none); points at equal distance go to the lower index (the reference
+ * takes the first its tree returns). */
+void *saCreateKDTree(double *x, double *y, int n);
+void saFreeKDTree(void *kd);
+void saNearestKDTree(void *kd, double *x, double *y, double *dist, int32_t *index, double radius, int n);
+
+/* ---- Frame ingest -------------------------------------------------------- */
+
+/* FrameReader.loadAFrame (sa_library/analysis_io.py:243-260) fused with
+ * padArray (sa_library/fitting.py:112-132): each raw rows x cols frame
+ * becomes (frame - offset) * scale (offset and scale per pixel, host arrays,
+ * or NULL for the scalars offset0 / scale0; scale is the reference's
+ * gain * rqe product), values below 1 set to 1 when clip, mirror-padded by
+ * pad pixels (pad <= rows, cols) into doubles.  Raw pixels: dtype_bits 16
+ * (uint16; big_endian swaps the bytes as DaxReader.loadAFrame does,
+ * sa_library/datareader.py:232-243), 32 (float) or 64 (double), host or
+ * device.  The padded frames go to d_out (device) or, when it is NULL, to a
+ * buffer of the handle (saIngestResultDevice). */
+void *saIngestCreate(int rows, int cols, int pad, const double *offset, const double *scale, double offset0,
+                     double scale0, int clip);
+int saIngestFrames(void *ih, const void *frames, int n_frames, int dtype_bits, int big_endian, int on_device,
+                   double *d_out);
+const double *saIngestResultDevice(void *ih);
+int saIngestGetFrames(void *ih, double *out);
+int saIngestSetStream(void *ih, void *stream);
+int64_t saIngestKernelLaunches(void *ih);
+void saIngestCleanup(void *ih);
+
 /* ---- Gaussian peak finder ------------------------------------------------ */
 
 /* PeakFinderGaussian (sa_library/fitting.py:361-501) on n_frames padded

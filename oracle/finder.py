@@ -23,6 +23,10 @@ Followed, function by function:
                       the search box and of radius**2
   MaximaFinder        sa_library/ia_utilities_c.py:132-250 (margin + 1,
                       taken initialised to 1 - n_duplicates)
+  mark_dimmer_peaks,  sa_library/ia_utilities.c:221-430 (the post-fit
+  mark_low_significance_peaks, running_if_has_neighbors, nearest
+                      culling; brute-force neighbour search with the
+                      kd-tree's membership test)
   pad_array           sa_library/fitting.py:112-132
   peak_mask           sa_library/fitting.py:134-176
   PeakFinderGaussian  sa_library/fitting.py:185-501 (newImage,
@@ -179,6 +183,80 @@ class MaximaFinder:
         if self.taken is not None:
             for t in self.taken:
                 t[:, :] = 1 - self.n_duplicates
+
+
+RUNNING, CONVERGED, ERROR = 0, 1, 2
+
+
+def _within(x, y, qx, qy, r):
+    """Indices within r of (qx, qy): dx*dx + dy*dy <= r*r, as
+    kd_nearest_range tests it (dbscan/kdtree.c:262-293)."""
+    dx = x - qx
+    dy = y - qy
+    return numpy.nonzero(dx * dx + dy * dy <= r * r)[0]
+
+
+def mark_dimmer_peaks(x, y, h, status, r_removal, r_neighbors):
+    """sa_library/ia_utilities.c:221-283, in the reference's peak order."""
+    removed = 0
+    for i in range(x.size):
+        if status[i] == ERROR:
+            continue
+        nb = _within(x, y, x[i], y[i], r_removal)
+        if nb.size < 2:
+            continue
+        if numpy.any(h[nb] > h[i]):
+            removed += 1
+            status[i] = ERROR
+            for k in _within(x, y, x[i], y[i], r_neighbors):
+                if status[k] == CONVERGED:
+                    status[k] = RUNNING
+    return removed
+
+
+def mark_low_significance_peaks(x, y, sig, status, min_sig, r_neighbors):
+    """sa_library/ia_utilities.c:292-340."""
+    removed = 0
+    for i in range(x.size):
+        if status[i] == ERROR:
+            continue
+        if sig[i] > min_sig:
+            continue
+        status[i] = ERROR
+        removed += 1
+        for k in _within(x, y, x[i], y[i], r_neighbors):
+            if status[k] == CONVERGED:
+                status[k] = RUNNING
+    return removed
+
+
+def running_if_has_neighbors(c_x, c_y, n_x, n_y, status, radius):
+    """sa_library/ia_utilities.c:401-430."""
+    for i in range(c_x.size):
+        if status[i] == RUNNING or status[i] == ERROR:
+            continue
+        if _within(n_x, n_y, c_x[i], c_y[i], radius).size > 0:
+            status[i] = RUNNING
+    return status
+
+
+def nearest(px, py, qx, qy, radius):
+    """sa_library/ia_utilities.c:347-391: distance to and index of the
+    nearest point within radius, -1 / -1 when there is none."""
+    dist = numpy.full(qx.size, -1.0)
+    index = numpy.full(qx.size, -1, dtype=numpy.int32)
+    for i in range(qx.size):
+        nb = _within(px, py, qx[i], qy[i], radius)
+        if nb.size == 0:
+            continue
+        dx = px[nb] - qx[i]
+        dy = py[nb] - qy[i]
+        dd = dx * dx + dy * dy
+        j = int(numpy.argmin(dd))
+        if dd[j] < radius * radius + 0.1:
+            dist[i] = math.sqrt(dd[j])
+            index[i] = nb[j]
+    return dist, index
 
 
 def pad_array(a, pad):

@@ -392,6 +392,193 @@ __global__ void k_find_ratio(const double* __restrict__ fg, const double* __rest
   }
 }
 
+// Frame ingest: FrameReader.loadAFrame (sa_library/analysis_io.py:243-260:
+// (frame - offset) * (gain * rqe), values below 1 set to 1) and padArray
+// (sa_library/fitting.py:112-132: mirror padding that repeats the edge
+// pixel), one block per padded output row.  Raw pixels are uint16 (byte
+// swapped for big-endian .dax data), float32 or float64.
+__device__ __forceinline__ int mirror_index(int i, int n) {
+  return i < 0 ? -1 - i : (i >= n ? 2 * n - 1 - i : i);
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_ingest(const void* __restrict__ raw, int bits, int swap, int rows, int cols, int pad,
+         const double* __restrict__ offset, const double* __restrict__ scale, double off0, double sc0,
+         int clip, double* __restrict__ out) {
+  const int prow = rows + 2 * pad, pcol = cols + 2 * pad;
+  const int y = blockIdx.x % prow, f = blockIdx.x / prow;
+  const int sy = mirror_index(y - pad, rows);
+  const size_t src_row = ((size_t)f * rows + sy) * cols;
+  double* o = out + ((size_t)f * prow + y) * pcol;
+  for (int x = threadIdx.x; x < pcol; x += blockDim.x) {
+    const int sx = mirror_index(x - pad, cols);
+    double v;
+    if (bits == 16) {
+      unsigned int u = static_cast<const uint16_t*>(raw)[src_row + sx];
+      if (swap) u = ((u >> 8) | (u << 8)) & 0xffffu;
+      v = (double)u;
+    } else if (bits == 32) {
+      v = (double)static_cast<const float*>(raw)[src_row + sx];
+    } else {
+      v = static_cast<const double*>(raw)[src_row + sx];
+    }
+    const int p = sy * cols + sx;
+    v = (v - (offset ? offset[p] : off0)) * (scale ? scale[p] : sc0);
+    if (clip && v < 1.0) v = 1.0;
+    o[x] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour queries of the post-fit culling (sa_library/ia_utilities.c:221-430)
+// ---------------------------------------------------------------------------
+// The reference builds a kd-tree per call; here points are hashed into a
+// uniform grid of cells at least the query radius wide, so every point
+// within the radius lies in the 3 x 3 cells around the query.  Cells hash
+// into a power-of-two table (a bucket may hold several cells; the distance
+// test decides).  Membership follows kd_nearest_range (dbscan/kdtree.c:
+// 262-293): dx*dx + dy*dy <= r*r, in that order.
+
+struct PointGrid {
+  const double* x;
+  const double* y;
+  const int32_t* start;   // T bucket starts (exclusive scan of the counts)
+  const int32_t* total;   // total points (end of the last bucket)
+  const int32_t* items;   // point indices by bucket
+  int T;
+  double cs;
+};
+
+__device__ __forceinline__ long long cell_of(double v, double cs) { return (long long)floor(v / cs); }
+
+__device__ __forceinline__ int bucket_of(long long cx, long long cy, int T) {
+  const unsigned long long h = (unsigned long long)cx * 0x9E3779B97F4A7C15ull ^
+                               ((unsigned long long)cy * 0xC2B2AE3D27D4EB4Full + 0x165667B19E3779F9ull);
+  return (int)((h ^ (h >> 29)) & (unsigned long long)(T - 1));
+}
+
+__global__ void k_grid_count(const double* __restrict__ x, const double* __restrict__ y, int n, double cs, int T,
+                             int32_t* __restrict__ counts) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    atomicAdd(&counts[bucket_of(cell_of(x[i], cs), cell_of(y[i], cs), T)], 1);
+}
+
+__global__ void k_grid_fill(const double* __restrict__ x, const double* __restrict__ y, int n, double cs, int T,
+                            const int32_t* __restrict__ start, int32_t* __restrict__ cursor,
+                            int32_t* __restrict__ items) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int b = bucket_of(cell_of(x[i], cs), cell_of(y[i], cs), T);
+    items[start[b] + atomicAdd(&cursor[b], 1)] = i;
+  }
+}
+
+// Visit every grid point within r of (qx, qy); fn(k, dd) returns true to stop.
+template <typename Fn>
+__device__ void grid_visit(const PointGrid& g, double qx, double qy, double r, Fn fn) {
+  const long long cx = cell_of(qx, g.cs), cy = cell_of(qy, g.cs);
+  const double rr = __dmul_rn(r, r);
+  for (int dy = -1; dy <= 1; ++dy)
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int b = bucket_of(cx + dx, cy + dy, g.T);
+      const int s = g.start[b], e = (b + 1 < g.T) ? g.start[b + 1] : *g.total;
+      for (int j = s; j < e; ++j) {
+        const int k = g.items[j];
+        const double ex = g.x[k] - qx, ey = g.y[k] - qy;
+        // unfused, as the reference's host build evaluates it
+        const double dd = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+        if (dd <= rr && fn(k, dd)) return;
+      }
+    }
+}
+
+constexpr int32_t kRunning = 0, kConverged = 1, kError = 2;
+
+// markDimmerPeaks, first half: a non-ERROR peak with a brighter peak within
+// r_removal is marked (ia_utilities.c:236-268).
+__global__ void k_mark_dimmer(PointGrid g, const double* __restrict__ h, const int32_t* __restrict__ status,
+                              int n, double r, int32_t* __restrict__ marked, int32_t* __restrict__ n_marked) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int m = 0;
+    if (status[i] != kError) {
+      const double hi = h[i];
+      grid_visit(g, g.x[i], g.y[i], r, [&](int k, double) {
+        if (h[k] > hi) m = 1;
+        return m != 0;
+      });
+    }
+    marked[i] = m;
+    if (m) atomicAdd(n_marked, 1);
+  }
+}
+
+// markLowSignificancePeaks, first half: a non-ERROR peak whose significance
+// is not above the minimum is marked (ia_utilities.c:305-315).
+__global__ void k_mark_low_sig(const double* __restrict__ sig, const int32_t* __restrict__ status, int n,
+                               double min_sig, int32_t* __restrict__ marked, int32_t* __restrict__ n_marked) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int m = (status[i] != kError && !(sig[i] > min_sig)) ? 1 : 0;
+    marked[i] = m;
+    if (m) atomicAdd(n_marked, 1);
+  }
+}
+
+// Second half of both: marked peaks become ERROR; a CONVERGED peak within
+// r_neighbors of a marked peak becomes RUNNING.  In the reference's loop a
+// peak is marked from its own brightness / significance alone, so the
+// result does not depend on the order the peaks are visited in.
+__global__ void k_mark_apply(PointGrid g, const int32_t* __restrict__ marked, const int32_t* __restrict__ in,
+                             int32_t* __restrict__ out, int n, double r) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int32_t st = in[i];
+    if (marked[i]) {
+      st = kError;
+    } else if (st == kConverged) {
+      bool near = false;
+      grid_visit(g, g.x[i], g.y[i], r, [&](int k, double) {
+        near = marked[k] != 0;
+        return near;
+      });
+      if (near) st = kRunning;
+    }
+    out[i] = st;
+  }
+}
+
+// runningIfHasNeighbors (ia_utilities.c:401-430): a peak that is neither
+// RUNNING nor ERROR becomes RUNNING when a new peak is within radius.
+__global__ void k_running_if_neighbors(PointGrid g, const double* __restrict__ cx, const double* __restrict__ cy,
+                                       int32_t* __restrict__ status, int nc, double r) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    if (status[i] == kRunning || status[i] == kError) continue;
+    bool near = false;
+    grid_visit(g, cx[i], cy[i], r, [&](int, double) {
+      near = true;
+      return true;
+    });
+    if (near) status[i] = kRunning;
+  }
+}
+
+// nearestKDTree (ia_utilities.c:347-391): the nearest point within radius
+// (distance and index), -1 / -1 when there is none.  Equal distances go to
+// the lower index.
+__global__ void k_nearest(PointGrid g, const double* __restrict__ qx, const double* __restrict__ qy, int n,
+                          double r, double* __restrict__ dist, int32_t* __restrict__ index) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double best = __dadd_rn(__dmul_rn(r, r), 0.1);
+    int bi = -1;
+    grid_visit(g, qx[i], qy[i], r, [&](int k, double dd) {
+      if (dd < best || (dd == best && k < bi)) {
+        best = dd;
+        bi = k;
+      }
+      return false;
+    });
+    dist[i] = bi >= 0 ? sqrt(best) : -1.0;
+    index[i] = bi;
+  }
+}
+
 int grid_for(size_t n) {
   size_t g = (n + kThreads - 1) / kThreads;
   return (int)std::min<size_t>(std::max<size_t>(g, 1), 152 * 16);
@@ -874,6 +1061,96 @@ const double* finder_input(Finder* h, const double* p, int on_device, double** d
   return *dst;
 }
 
+// Device arrays of one culling call (host-array entry points).
+struct CullBuf {
+  double* d = nullptr;    // x, y, value (3 n) + query x, y (2 nq)
+  int32_t* i = nullptr;   // status in/out (2 n), marked (n), items (n), counts/starts/cursor (3 T), misc (4)
+  int n = 0, nq = 0, T = 0;
+  ~CullBuf() {
+    dfree(d);
+    dfree(i);
+  }
+};
+
+int table_size(int n) {
+  int T = 1024;
+  while (T < 2 * n && T < (1 << 26)) T <<= 1;
+  return T;
+}
+
+// Build the bucket grid of points (x, y) (device) with cells of width >= r.
+int build_grid(const double* x, const double* y, int n, double r, int T, int32_t* counts, int32_t* starts,
+               int32_t* cursor, int32_t* items, int32_t* total2, PointGrid* g) {
+  const double cs = std::max(r * (1.0 + 1e-9), 1e-6);
+  FCK(cudaMemsetAsync(counts, 0, sizeof(int32_t) * T, 0));
+  FCK(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * T, 0));
+  if (n > 0) k_grid_count<<<grid_for(n), kThreads>>>(x, y, n, cs, T, counts);
+  k_lmax_scan<<<1, 1024>>>(counts, starts, T, T, 1, total2);
+  if (n > 0) k_grid_fill<<<grid_for(n), kThreads>>>(x, y, n, cs, T, starts, cursor, items);
+  FCK(cudaGetLastError());
+  g->x = x;
+  g->y = y;
+  g->start = starts;
+  g->total = total2 + 1;
+  g->items = items;
+  g->T = T;
+  g->cs = cs;
+  return 0;
+}
+
+// Points + values + statuses to the device, grid built, for the host-array
+// culling entry points.
+int cull_setup(CullBuf& b, int n, int nq, const double* x, const double* y, const double* v, const int32_t* status,
+               const double* qx, const double* qy, double r, PointGrid* g) {
+  b.n = n;
+  b.nq = nq;
+  b.T = table_size(n);
+  const size_t nd = 3 * (size_t)n + 2 * (size_t)nq + 2, ni = 4 * (size_t)std::max(n, nq) + 3 * (size_t)b.T + 8;
+  FCK(cudaMalloc(&b.d, sizeof(double) * nd));
+  FCK(cudaMalloc(&b.i, sizeof(int32_t) * ni));
+  double *dx = b.d, *dy = b.d + n, *dv = b.d + 2 * n, *qxd = b.d + 3 * n, *qyd = qxd + nq;
+  if (n > 0) {
+    FCK(cudaMemcpy(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice));
+    FCK(cudaMemcpy(dy, y, sizeof(double) * n, cudaMemcpyHostToDevice));
+    if (v) FCK(cudaMemcpy(dv, v, sizeof(double) * n, cudaMemcpyHostToDevice));
+  }
+  if (nq > 0) {
+    FCK(cudaMemcpy(qxd, qx, sizeof(double) * nq, cudaMemcpyHostToDevice));
+    FCK(cudaMemcpy(qyd, qy, sizeof(double) * nq, cudaMemcpyHostToDevice));
+  }
+  const int m = std::max(n, nq);
+  int32_t* st_in = b.i;
+  if (status && m > 0) FCK(cudaMemcpy(st_in, status, sizeof(int32_t) * m, cudaMemcpyHostToDevice));
+  int32_t* items = b.i + 3 * (size_t)m;
+  int32_t* counts = b.i + 4 * (size_t)m;
+  int32_t* starts = counts + b.T;
+  int32_t* cursor = starts + b.T;
+  int32_t* misc = cursor + b.T;
+  FCK(cudaMemset(misc, 0, sizeof(int32_t) * 8));
+  return build_grid(dx, dy, n, r, b.T, counts, starts, cursor, items, misc, g);
+}
+
+struct Ingest {
+  int rows = 0, cols = 0, pad = 0, clip = 1;
+  double off0 = 0.0, sc0 = 1.0;
+  double* d_offset = nullptr;   // rows x cols, or none
+  double* d_scale = nullptr;    // rows x cols, or none
+  void* d_raw = nullptr;        // staging of host frames
+  size_t raw_bytes = 0;
+  double* d_out = nullptr;      // frames x (rows + 2 pad) x (cols + 2 pad)
+  size_t out_bytes = 0;
+  int n_frames = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+};
+
+void ingest_free(Ingest* h) {
+  dfree(h->d_offset);
+  dfree(h->d_scale);
+  dfree(h->d_raw);
+  dfree(h->d_out);
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1097,6 +1374,229 @@ void saMaximaCleanup(void* mh) {
   if (!h) return;
   cudaStreamSynchronize(h->stream);
   maxima_free(h);
+  delete h;
+}
+
+int saMarkDimmerPeaks(double* x, double* y, double* h, int32_t* status, double r_removal, double r_neighbors,
+                      int np) {
+  if (np <= 0) return 0;
+  if (!x || !y || !h || !status) {
+    ferr("markDimmerPeaks: NULL argument");
+    return -1;
+  }
+  CullBuf b;
+  PointGrid g;
+  if (cull_setup(b, np, 0, x, y, h, status, nullptr, nullptr, std::max(r_removal, r_neighbors), &g)) return -1;
+  int32_t* st_in = b.i;
+  int32_t* st_out = b.i + np;
+  int32_t* marked = b.i + 2 * (size_t)np;
+  int32_t* misc = b.i + 4 * (size_t)np + 3 * (size_t)b.T;
+  k_mark_dimmer<<<grid_for(np), kThreads>>>(g, b.d + 2 * np, st_in, np, r_removal, marked, misc + 4);
+  k_mark_apply<<<grid_for(np), kThreads>>>(g, marked, st_in, st_out, np, r_neighbors);
+  FCK(cudaGetLastError());
+  int32_t removed = 0;
+  FCK(cudaMemcpy(status, st_out, sizeof(int32_t) * np, cudaMemcpyDeviceToHost));
+  FCK(cudaMemcpy(&removed, misc + 4, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return removed;
+}
+
+int saMarkLowSignificancePeaks(double* x, double* y, double* sig, int32_t* status, double min_sig,
+                               double r_neighbors, int np) {
+  if (np <= 0) return 0;
+  if (!x || !y || !sig || !status) {
+    ferr("markLowSignificancePeaks: NULL argument");
+    return -1;
+  }
+  CullBuf b;
+  PointGrid g;
+  if (cull_setup(b, np, 0, x, y, sig, status, nullptr, nullptr, r_neighbors, &g)) return -1;
+  int32_t* st_in = b.i;
+  int32_t* st_out = b.i + np;
+  int32_t* marked = b.i + 2 * (size_t)np;
+  int32_t* misc = b.i + 4 * (size_t)np + 3 * (size_t)b.T;
+  k_mark_low_sig<<<grid_for(np), kThreads>>>(b.d + 2 * np, st_in, np, min_sig, marked, misc + 4);
+  k_mark_apply<<<grid_for(np), kThreads>>>(g, marked, st_in, st_out, np, r_neighbors);
+  FCK(cudaGetLastError());
+  int32_t removed = 0;
+  FCK(cudaMemcpy(status, st_out, sizeof(int32_t) * np, cudaMemcpyDeviceToHost));
+  FCK(cudaMemcpy(&removed, misc + 4, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return removed;
+}
+
+void saRunningIfHasNeighbors(double* c_x, double* c_y, double* n_x, double* n_y, int32_t* status, double radius,
+                             int nc, int nn) {
+  if (nc <= 0 || nn <= 0) return;
+  if (!c_x || !c_y || !n_x || !n_y || !status) {
+    ferr("runningIfHasNeighbors: NULL argument");
+    return;
+  }
+  CullBuf b;
+  PointGrid g;
+  // grid over the new peaks, queries are the current peaks
+  if (cull_setup(b, nn, nc, n_x, n_y, nullptr, nullptr, c_x, c_y, radius, &g)) return;
+  int32_t* st = b.i;
+  if (cudaMemcpy(st, status, sizeof(int32_t) * nc, cudaMemcpyHostToDevice) != cudaSuccess) {
+    ferr("runningIfHasNeighbors: copy failed");
+    return;
+  }
+  k_running_if_neighbors<<<grid_for(nc), kThreads>>>(g, b.d + 3 * nn, b.d + 3 * nn + nc, st, nc, radius);
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpy(status, st, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost) != cudaSuccess)
+    ferr("runningIfHasNeighbors: device step failed");
+}
+
+// The "kd-tree" of createKDTree / nearestKDTree is the point set itself;
+// the grid is built per query radius.
+struct PointSet {
+  int n = 0;
+  std::vector<double> x, y;
+};
+
+void* saCreateKDTree(double* x, double* y, int n) {
+  if (n < 0 || (n > 0 && (!x || !y))) {
+    ferr("createKDTree: bad arguments");
+    return nullptr;
+  }
+  PointSet* p = new PointSet();
+  p->n = n;
+  p->x.assign(x, x + n);
+  p->y.assign(y, y + n);
+  return p;
+}
+
+void saFreeKDTree(void* kd) { delete static_cast<PointSet*>(kd); }
+
+void saNearestKDTree(void* kd, double* x, double* y, double* dist, int32_t* index, double radius, int n) {
+  PointSet* p = static_cast<PointSet*>(kd);
+  if (!p || n <= 0) return;
+  if (p->n == 0) {
+    for (int i = 0; i < n; ++i) {
+      dist[i] = -1.0;
+      index[i] = -1;
+    }
+    return;
+  }
+  CullBuf b;
+  PointGrid g;
+  if (cull_setup(b, p->n, n, p->x.data(), p->y.data(), nullptr, nullptr, x, y, radius, &g)) return;
+  double* qx = b.d + 3 * (size_t)p->n;
+  double* qy = qx + n;
+  double* dd = nullptr;
+  int32_t* di = b.i + 2 * (size_t)std::max(p->n, n);
+  if (cudaMalloc(&dd, sizeof(double) * n) != cudaSuccess) {
+    ferr("nearestKDTree: device allocation failed");
+    return;
+  }
+  k_nearest<<<grid_for(n), kThreads>>>(g, qx, qy, n, radius, dd, di);
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpy(dist, dd, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(index, di, sizeof(int32_t) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+    ferr("nearestKDTree: device step failed");
+  cudaFree(dd);
+}
+
+void* saIngestCreate(int rows, int cols, int pad, const double* offset, const double* scale, double offset0,
+                     double scale0, int clip) {
+  if (rows < 1 || cols < 1 || pad < 0 || pad > rows || pad > cols) {
+    ferr("saIngestCreate: bad frame size %d x %d or padding %d (padding must not exceed the frame)", rows, cols,
+         pad);
+    return nullptr;
+  }
+  Ingest* h = new Ingest();
+  h->rows = rows;
+  h->cols = cols;
+  h->pad = pad;
+  h->clip = clip ? 1 : 0;
+  h->off0 = offset0;
+  h->sc0 = scale0;
+  const size_t bytes = sizeof(double) * (size_t)rows * cols;
+  bool ok = true;
+  if (offset)
+    ok = ok && cudaMalloc(&h->d_offset, bytes) == cudaSuccess &&
+         cudaMemcpy(h->d_offset, offset, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  if (scale)
+    ok = ok && cudaMalloc(&h->d_scale, bytes) == cudaSuccess &&
+         cudaMemcpy(h->d_scale, scale, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  if (!ok) {
+    ferr("saIngestCreate: device set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
+    ingest_free(h);
+    delete h;
+    return nullptr;
+  }
+  return h;
+}
+
+int saIngestFrames(void* ih, const void* frames, int n_frames, int dtype_bits, int big_endian, int on_device,
+                   double* d_out) {
+  Ingest* h = static_cast<Ingest*>(ih);
+  if (!h || !frames || n_frames < 1 || (dtype_bits != 16 && dtype_bits != 32 && dtype_bits != 64)) {
+    ferr("saIngestFrames: bad arguments (dtype bits must be 16, 32 or 64)");
+    return -1;
+  }
+  const size_t raw_bytes = (size_t)n_frames * h->rows * h->cols * (dtype_bits / 8);
+  const void* src = frames;
+  if (!on_device) {
+    if (raw_bytes > h->raw_bytes) {
+      FCK(cudaStreamSynchronize(h->stream));
+      dfree(h->d_raw);
+      FCK(cudaMalloc(&h->d_raw, raw_bytes));
+      h->raw_bytes = raw_bytes;
+    }
+    FCK(cudaMemcpyAsync(h->d_raw, frames, raw_bytes, cudaMemcpyHostToDevice, h->stream));
+    src = h->d_raw;
+  }
+  const int prow = h->rows + 2 * h->pad, pcol = h->cols + 2 * h->pad;
+  double* out = d_out;
+  if (!out) {
+    const size_t ob = sizeof(double) * (size_t)n_frames * prow * pcol;
+    if (ob > h->out_bytes) {
+      FCK(cudaStreamSynchronize(h->stream));
+      dfree(h->d_out);
+      FCK(cudaMalloc(&h->d_out, ob));
+      h->out_bytes = ob;
+    }
+    out = h->d_out;
+  }
+  k_ingest<<<n_frames * prow, kThreads, 0, h->stream>>>(src, dtype_bits, big_endian && dtype_bits == 16,
+                                                        h->rows, h->cols, h->pad, h->d_offset, h->d_scale,
+                                                        h->off0, h->sc0, h->clip, out);
+  h->launches += 1;
+  FCK(cudaGetLastError());
+  h->n_frames = n_frames;
+  return 0;
+}
+
+const double* saIngestResultDevice(void* ih) {
+  Ingest* h = static_cast<Ingest*>(ih);
+  return h ? h->d_out : nullptr;
+}
+
+int saIngestGetFrames(void* ih, double* out) {
+  Ingest* h = static_cast<Ingest*>(ih);
+  if (!h || !out || !h->d_out) return -1;
+  const size_t n = (size_t)h->n_frames * (h->rows + 2 * h->pad) * (h->cols + 2 * h->pad);
+  FCK(cudaMemcpyAsync(out, h->d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+  FCK(cudaStreamSynchronize(h->stream));
+  return h->n_frames;
+}
+
+int saIngestSetStream(void* ih, void* stream) {
+  Ingest* h = static_cast<Ingest*>(ih);
+  if (!h) return -1;
+  h->stream = static_cast<cudaStream_t>(stream);
+  return 0;
+}
+
+int64_t saIngestKernelLaunches(void* ih) {
+  Ingest* h = static_cast<Ingest*>(ih);
+  return h ? h->launches : -1;
+}
+
+void saIngestCleanup(void* ih) {
+  Ingest* h = static_cast<Ingest*>(ih);
+  if (!h) return;
+  cudaStreamSynchronize(h->stream);
+  ingest_free(h);
   delete h;
 }
 

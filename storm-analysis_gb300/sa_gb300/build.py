@@ -4,8 +4,9 @@ Build libsa_cuda.so (the engine) from storm-analysis_gb300/csrc for sm_103a.
 The four translation units (the fitter for float and double pixels, the
 fitter's host API and the peak finder) are compiled in parallel with nvcc
 and linked into sa_gb300/libsa_cuda.so; only the CUDA runtime is linked (no
-torch).  libsa_matched_filter.so, the reference-named matched-filter entry
-points, is linked against it.
+torch).  libsa_matched_filter.so and libsa_ia_utilities.so, the
+reference-named matched-filter and image-analysis entry points, are linked
+against it.
 """
 import concurrent.futures
 import os
@@ -19,6 +20,9 @@ CSRC = os.path.join(PKG_ROOT, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 LIB = os.path.join(HERE, "libsa_cuda.so")
 MF_LIB = os.path.join(HERE, "libsa_matched_filter.so")
+IA_LIB = os.path.join(HERE, "libsa_ia_utilities.so")
+# reference-named forwarding libraries linked against libsa_cuda.so
+SHIMS = [(MF_LIB, "sa_matched_filter.cpp"), (IA_LIB, "sa_ia_utilities.cpp")]
 BUILD_DIR = os.path.join(PKG_ROOT, "_build")
 
 SOURCES = ["sa_launch_f32.cu", "sa_launch_f64.cu", "sa_api.cu", "sa_finder.cu"]
@@ -43,9 +47,10 @@ def _compile(src, verbose):
 
 
 def _stale():
-    if not os.path.exists(LIB) or not os.path.exists(MF_LIB):
+    outs = [LIB] + [lib for lib, _ in SHIMS]
+    if not all(os.path.exists(p) for p in outs):
         return True
-    t = min(os.path.getmtime(LIB), os.path.getmtime(MF_LIB))
+    t = min(os.path.getmtime(p) for p in outs)
     for d in (CSRC, INCLUDE):
         for f in os.listdir(d):
             if os.path.getmtime(os.path.join(d, f)) > t:
@@ -70,14 +75,14 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
-    tmp = MF_LIB + ".tmp"
-    cmd = [nvcc(), "-shared", "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE, "-o", tmp,
-           os.path.join(CSRC, "sa_matched_filter.cpp"), "-L", HERE, "-lsa_cuda",
-           "-Xlinker", "-rpath,$ORIGIN"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("link of libsa_matched_filter.so failed:\n%s\n%s" % (r.stdout, r.stderr))
-    os.replace(tmp, MF_LIB)
+    for lib, src in SHIMS:
+        tmp = lib + ".tmp"
+        cmd = [nvcc(), "-shared", "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE, "-o", tmp,
+               os.path.join(CSRC, src), "-L", HERE, "-lsa_cuda", "-Xlinker", "-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link of %s failed:\n%s\n%s" % (os.path.basename(lib), r.stdout, r.stderr))
+        os.replace(tmp, lib)
     return LIB
 
 

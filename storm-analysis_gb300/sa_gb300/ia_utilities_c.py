@@ -1,8 +1,13 @@
 """
-GPU local-maxima finder behind the reference's MaximaFinder class
-(sa_library/ia_utilities_c.py:132-250): same constructor arguments,
-findMaxima(images, want_height) and resetTaken().  The taken counts live on
-the GPU (saMaxima* in include/sa_finder.h); getTaken() copies them back.
+GPU image-analysis utilities behind the reference's
+sa_library/ia_utilities_c.py:
+
+  MaximaFinder (:132-250): same constructor arguments, findMaxima(images,
+      want_height) and resetTaken(); the taken counts live on the GPU
+      (saMaxima* in include/sa_finder.h), getTaken() copies them back;
+  markDimmerPeaks, markLowSignificancePeaks, runningIfHasNeighbors and
+      KDTree.nearest (:252-465): the post-fit culling, same arguments and
+      in-place status updates, neighbour queries on the GPU.
 
 The reference-layout entry points saCalcMaxPeaks / saFindLocalMaxima
 (flmData, host arrays) are reached through FlmData below.
@@ -12,6 +17,11 @@ import ctypes
 import numpy
 
 from . import loadclib
+
+
+RUNNING = 0
+CONVERGED = 1
+ERROR = 2
 
 
 class FlmData(ctypes.Structure):
@@ -94,3 +104,62 @@ def find_local_maxima(flm, z, y, x, h):
     """saFindLocalMaxima on a filled FlmData (reference argument order)."""
     loadclib.load().saFindLocalMaxima(ctypes.byref(flm), z, y, x, h)
     return flm.n_peaks
+
+
+def _c(a, dtype):
+    assert a.flags["C_CONTIGUOUS"], "array is not C contiguous!"
+    assert a.dtype == dtype, "expected %s" % numpy.dtype(dtype)
+    return a
+
+
+def markDimmerPeaks(x, y, h, status, r_removal, r_neighbors):
+    """Non-ERROR peaks with a brighter peak within r_removal become ERROR,
+    CONVERGED peaks within r_neighbors of one become RUNNING (status is
+    updated in place); returns the number removed."""
+    lib = loadclib.load()
+    n = lib.saMarkDimmerPeaks(_c(x, numpy.float64), _c(y, numpy.float64), _c(h, numpy.float64),
+                              _c(status, numpy.int32), float(r_removal), float(r_neighbors), x.size)
+    if n < 0:
+        raise MaximaFinderException(loadclib.last_error())
+    return n
+
+
+def markLowSignificancePeaks(x, y, significance, status, minimum_significance, r_neighbors):
+    lib = loadclib.load()
+    n = lib.saMarkLowSignificancePeaks(_c(x, numpy.float64), _c(y, numpy.float64),
+                                       _c(significance, numpy.float64), _c(status, numpy.int32),
+                                       float(minimum_significance), float(r_neighbors), x.size)
+    if n < 0:
+        raise MaximaFinderException(loadclib.last_error())
+    return n
+
+
+def runningIfHasNeighbors(status, c_x, c_y, n_x, n_y, radius):
+    lib = loadclib.load()
+    lib.saRunningIfHasNeighbors(_c(c_x, numpy.float64), _c(c_y, numpy.float64), _c(n_x, numpy.float64),
+                                _c(n_y, numpy.float64), _c(status, numpy.int32), float(radius), c_x.size, n_x.size)
+    return status
+
+
+class KDTree(object):
+    """Nearest-point queries within a radius (the reference's C kd-tree
+    wrapper); equal distances go to the lower index."""
+
+    def __init__(self, x=None, y=None, **kwds):
+        super(KDTree, self).__init__(**kwds)
+        self.clib = loadclib.load()
+        x = numpy.ascontiguousarray(x, dtype=numpy.float64)
+        y = numpy.ascontiguousarray(y, dtype=numpy.float64)
+        self.kd_tree = self.clib.saCreateKDTree(x, y, x.size)
+
+    def cleanup(self):
+        self.clib.saFreeKDTree(self.kd_tree)
+        self.kd_tree = None
+
+    def nearest(self, x, y, max_dist):
+        x = numpy.ascontiguousarray(x, dtype=numpy.float64)
+        y = numpy.ascontiguousarray(y, dtype=numpy.float64)
+        dist = numpy.zeros(x.size, dtype=numpy.float64) - 1.0
+        index = numpy.zeros(x.size, dtype=numpy.int32) - 1
+        self.clib.saNearestKDTree(self.kd_tree, x, y, dist, index, float(max_dist), x.size)
+        return [dist, index]

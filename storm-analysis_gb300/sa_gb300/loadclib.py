@@ -174,6 +174,19 @@ def _declare(lib):
             ("saMaximaGetTaken", [vp, i32], ci),
             ("saMaximaSetStream", [vp, vp], ci),
             ("saMaximaCleanup", [vp], None),
+            ("saMarkDimmerPeaks", [f64, f64, f64, i32, cd, cd, ci], ci),
+            ("saMarkLowSignificancePeaks", [f64, f64, f64, i32, cd, cd, ci], ci),
+            ("saRunningIfHasNeighbors", [f64, f64, f64, f64, i32, cd, ci, ci], None),
+            ("saCreateKDTree", [f64, f64, ci], vp),
+            ("saFreeKDTree", [vp], None),
+            ("saNearestKDTree", [vp, f64, f64, f64, i32, cd, ci], None),
+            ("saIngestCreate", [ci, ci, ci, vp, vp, cd, cd, ci], vp),
+            ("saIngestFrames", [vp, vp, ci, ci, ci, ci, vp], ci),
+            ("saIngestResultDevice", [vp], vp),
+            ("saIngestGetFrames", [vp, f64], ci),
+            ("saIngestSetStream", [vp, vp], ci),
+            ("saIngestKernelLaunches", [vp], i64r),
+            ("saIngestCleanup", [vp], None),
             ("saFinderCreate", [ci, ci, vp, vp, vp, ci, cd, cd, cd, cd], vp),
             ("saFinderSetVariance", [vp, vp], ci),
             ("saFinderSetMask", [vp, vp], ci),
@@ -215,7 +228,11 @@ FINDER_EXPORTS = ["saFilterCreate", "saFilterConvolve", "saFilterConvolveMemo", 
                   "saFilterConvolveDevice", "saFilterResultDevice", "saFilterInfo", "saFilterSetStream",
                   "saCalcMaxPeaks", "saFindLocalMaxima", "saMaximaCreate", "saMaximaFind",
                   "saMaximaPeaksDevice", "saMaximaGetPeaks", "saMaximaResetTaken", "saMaximaGetTaken",
-                  "saMaximaSetStream", "saMaximaCleanup", "saFinderCreate", "saFinderSetVariance",
+                  "saMaximaSetStream", "saMaximaCleanup", "saMarkDimmerPeaks", "saMarkLowSignificancePeaks",
+                  "saRunningIfHasNeighbors", "saCreateKDTree", "saFreeKDTree", "saNearestKDTree",
+                  "saIngestCreate", "saIngestFrames",
+                  "saIngestResultDevice", "saIngestGetFrames", "saIngestSetStream", "saIngestKernelLaunches",
+                  "saIngestCleanup", "saFinderCreate", "saFinderSetVariance",
                   "saFinderSetMask", "saFinderNewImages", "saFinderEstimateBackground",
                   "saFinderFindPeaks", "saFinderBackgroundDevice", "saFinderPeaksDevice",
                   "saFinderGetPeaks", "saFinderGetArray", "saFinderSetStream", "saFinderKernelLaunches",
@@ -224,3 +241,8 @@ FINDER_EXPORTS = ["saFilterCreate", "saFilterConvolve", "saFilterConvolveMemo", 
 # libsa_matched_filter.so: the reference's matched-filter names
 MATCHED_FILTER_EXPORTS = ["cleanup", "convolve", "convolveMemo", "initialize"]
 MF_LIB_PATH = os.path.join(HERE, "libsa_matched_filter.so")
+
+# libsa_ia_utilities.so: the reference's image-analysis utility names
+IA_UTILITIES_EXPORTS = ["calcMaxPeaks", "createKDTree", "findLocalMaxima", "freeKDTree", "markDimmerPeaks",
+                        "markLowSignificancePeaks", "nearestKDTree", "runningIfHasNeighbors"]
+IA_LIB_PATH = os.path.join(HERE, "libsa_ia_utilities.so")

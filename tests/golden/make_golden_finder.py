@@ -7,7 +7,10 @@ code, compiled from its sources by ``make -C oracle ref``:
     draws them, for even, odd and clamped image sizes;
   * libia_utilities.so (sa_library/ia_utilities.c): calcMaxPeaks and
     findLocalMaxima on seeded images with many exact ties, several z planes,
-    fractional radii and repeated calls that advance the taken counts.
+    fractional radii and repeated calls that advance the taken counts; and
+    the post-fit culling (markDimmerPeaks, markLowSignificancePeaks,
+    runningIfHasNeighbors, createKDTree / nearestKDTree) on clustered
+    peaks with mixed statuses.
 
 Run here, where the reference tree exists:
 
@@ -24,7 +27,7 @@ REF = os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle", "_ref")
 
 
 class FlmData(ctypes.Structure):
-    """The field order of flmData in sa_library/ia_utilities.c:19-35."""
+    """The field order of flmData in sa_library/ia_utilities.c:20-36."""
     _fields_ = [("margin", ctypes.c_int), ("n_peaks", ctypes.c_int), ("z_range", ctypes.c_int),
                 ("xsize", ctypes.c_int), ("ysize", ctypes.c_int), ("zsize", ctypes.c_int),
                 ("radius", ctypes.c_double), ("threshold", ctypes.c_double),
@@ -98,6 +101,44 @@ def main():
             out["lm%d_c%d_max" % (i, c)] = numpy.array(n)
             out["lm%d_c%d_xyzh" % (i, c)] = numpy.stack([x, y, z, h]) if x.size else numpy.zeros((4, 0))
             out["lm%d_c%d_taken" % (i, c)] = numpy.stack(taken).copy()
+    # post-fit culling (ia_utilities.c:221-430): clustered peaks, mixed statuses
+    f64 = ctypes.c_double
+    dp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    ia.markDimmerPeaks.restype = ctypes.c_int
+    ia.markLowSignificancePeaks.restype = ctypes.c_int
+    ia.createKDTree.restype = ctypes.c_void_p
+    for i, (n, r1, r2) in enumerate([(300, 1.5, 7.5), (60, 2.0, 5.0), (1000, 1.0, 5.0)]):
+        centres = rng.uniform(10, 90, (n // 3, 2))
+        pts = numpy.concatenate([centres + rng.normal(0, 0.8, centres.shape) for _ in range(3)])[:n]
+        x = numpy.ascontiguousarray(pts[:, 0])
+        y = numpy.ascontiguousarray(pts[:, 1])
+        h = numpy.ascontiguousarray(rng.uniform(100, 1000, x.size))
+        sig = numpy.ascontiguousarray(rng.uniform(0, 12, x.size))
+        st = numpy.ascontiguousarray(rng.choice([0, 1, 1, 1, 2], x.size).astype(numpy.int32))
+        out["cull%d_xyhs" % i] = numpy.stack([x, y, h, sig])
+        out["cull%d_status" % i] = st.copy()
+        out["cull%d_r" % i] = numpy.array([r1, r2])
+        s1 = st.copy()
+        n1 = ia.markDimmerPeaks(dp(x), dp(y), dp(h), dp(s1), f64(r1), f64(r2), x.size)
+        out["cull%d_dimmer" % i] = s1
+        out["cull%d_dimmer_n" % i] = numpy.array(n1)
+        s2 = st.copy()
+        n2 = ia.markLowSignificancePeaks(dp(x), dp(y), dp(sig), dp(s2), f64(6.0), f64(r2), x.size)
+        out["cull%d_lowsig" % i] = s2
+        out["cull%d_lowsig_n" % i] = numpy.array(n2)
+        nx = numpy.ascontiguousarray(rng.uniform(10, 90, n // 10 + 1))
+        ny = numpy.ascontiguousarray(rng.uniform(10, 90, n // 10 + 1))
+        s3 = st.copy()
+        ia.runningIfHasNeighbors(dp(x), dp(y), dp(nx), dp(ny), dp(s3), f64(r2), x.size, nx.size)
+        out["cull%d_new" % i] = numpy.stack([nx, ny])
+        out["cull%d_running" % i] = s3
+        kd = ia.createKDTree(dp(nx), dp(ny), nx.size)
+        dist = numpy.zeros(x.size)
+        idx = numpy.zeros(x.size, dtype=numpy.int32)
+        ia.nearestKDTree(ctypes.c_void_p(kd), dp(x), dp(y), dp(dist), dp(idx), f64(r2), x.size)
+        ia.freeKDTree(ctypes.c_void_p(kd))
+        out["cull%d_nearest_d" % i] = dist
+        out["cull%d_nearest_i" % i] = idx
     numpy.savez_compressed(os.path.join(HERE, "g_finder.npz"), **out)
     print("wrote g_finder.npz:", len(out), "arrays")
 

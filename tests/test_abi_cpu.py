@@ -163,6 +163,9 @@ def test_finder_exports_header(lib):
     assert mf == ["cleanup", "convolve", "convolveMemo", "initialize"]
     assert sorted(loadclib.MATCHED_FILTER_EXPORTS) == mf
     assert set(mf) <= _exported(loadclib.MF_LIB_PATH)
+    ia = _declared("sa_ia_utilities.h")
+    assert sorted(loadclib.IA_UTILITIES_EXPORTS) == ia and len(ia) == 8
+    assert set(ia) <= _exported(loadclib.IA_LIB_PATH)
 
 
 def test_finder_without_device_fails_loudly(lib):

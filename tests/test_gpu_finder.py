@@ -293,3 +293,119 @@ def test_batch_finder_matches_single_frames_and_hands_off():
     a.close()
     b.close()
     bf.cleanUp()
+
+
+def test_frame_ingest_matches_reference_readers(tmp_path):
+    """FrameReaderStd / FrameReaderSCMOS on the GPU return the reference
+    readers' frames bit for bit (golden fixture), and the fused mirror
+    padding equals padArray; float inputs go through the same kernel."""
+    import ctypes
+    from sa_gb300 import analysis_io, loadclib
+    from test_oracle_ingest import write_dax
+    g = numpy.load(os.path.join(os.path.dirname(GOLDEN), "g_ingest.npz"))
+    n, h, w = g["frames"].shape
+    for tag, big in (("big", 1), ("little", 0)):
+        path = str(tmp_path / ("m_%s.dax" % tag))
+        write_dax(path, g["raw_" + tag], big)
+        rd = analysis_io.FrameReaderStd(movie_file=path, camera_gain=2.5, camera_offset=100.0)
+        for i in range(n):
+            assert numpy.array_equal(rd.loadAFrame(i), g["std_" + tag][i])
+        ptr = rd.loadFramesPadded(0, n, 7)
+        out = numpy.zeros((n, h + 14, w + 14))
+        ih = rd._handle(7)
+        rd.clib.saIngestGetFrames(ih, out)
+        assert ptr and numpy.array_equal(out, g["std_%s_pad7" % tag])
+        rd.close()
+    cal = str(tmp_path / "calib.npy")
+    numpy.save(cal, numpy.array([g["offset"], g["variance"], g["gain"], g["rqe"], 2], dtype=object),
+               allow_pickle=True)
+    rd = analysis_io.FrameReaderSCMOS(movie_file=str(tmp_path / "m_big.dax"), calibration_file=cal)
+    for i in range(n):
+        assert numpy.array_equal(rd.loadAFrame(i), g["scmos_big"][i])
+    rd.loadFramesPadded(0, n, 11)
+    out = numpy.zeros((n, h + 22, w + 22))
+    rd.clib.saIngestGetFrames(rd._handle(11), out)
+    assert numpy.array_equal(out, g["scmos_big_pad11"])
+    rd.close()
+    # float32 / float64 frames: conversion and padding only
+    lib = loadclib.load()
+    f64 = g["frames"].astype(numpy.float64) * 1.25
+    for arr, bits in ((f64.astype(numpy.float32), 32), (f64, 64)):
+        ih = lib.saIngestCreate(h, w, 5, None, None, 3.0, 0.5, 1)
+        a = numpy.ascontiguousarray(arr)
+        assert lib.saIngestFrames(ih, a.ctypes.data_as(ctypes.c_void_p), n, bits, 0, 0, None) == 0
+        out = numpy.zeros((n, h + 10, w + 10))
+        lib.saIngestGetFrames(ih, out)
+        exp = numpy.stack([F.pad_array(numpy.maximum((a[i].astype(numpy.float64) - 3.0) * 0.5, 1.0), 5)
+                           for i in range(n)])
+        assert numpy.array_equal(out, exp)
+        lib.saIngestCleanup(ih)
+
+
+def _cull_cases(g):
+    i = 0
+    while "cull%d_xyhs" % i in g:
+        yield i
+        i += 1
+
+
+def test_culling_matches_reference_golden():
+    """The post-fit culling on the GPU returns the reference's statuses,
+    counts and nearest-neighbour answers exactly (sa_gb300.ia_utilities_c
+    mirror of the reference's Python functions)."""
+    from sa_gb300 import ia_utilities_c as U
+    g = numpy.load(GOLDEN)
+    for i in _cull_cases(g):
+        x, y, h, sig = (numpy.ascontiguousarray(a) for a in g["cull%d_xyhs" % i])
+        st = numpy.ascontiguousarray(g["cull%d_status" % i])
+        r1, r2 = (float(v) for v in g["cull%d_r" % i])
+        s1 = st.copy()
+        assert U.markDimmerPeaks(x, y, h, s1, r1, r2) == int(g["cull%d_dimmer_n" % i])
+        assert numpy.array_equal(s1, g["cull%d_dimmer" % i])
+        s2 = st.copy()
+        assert U.markLowSignificancePeaks(x, y, sig, s2, 6.0, r2) == int(g["cull%d_lowsig_n" % i])
+        assert numpy.array_equal(s2, g["cull%d_lowsig" % i])
+        nx, ny = (numpy.ascontiguousarray(a) for a in g["cull%d_new" % i])
+        assert numpy.array_equal(U.runningIfHasNeighbors(st.copy(), x, y, nx, ny, r2), g["cull%d_running" % i])
+        kd = U.KDTree(x=nx, y=ny)
+        d, ix = kd.nearest(x, y, r2)
+        kd.cleanup()
+        assert numpy.array_equal(d, g["cull%d_nearest_d" % i])
+        assert numpy.array_equal(ix, g["cull%d_nearest_i" % i])
+    # empty and degenerate inputs
+    e = numpy.zeros(0)
+    es = numpy.zeros(0, dtype=numpy.int32)
+    assert U.markDimmerPeaks(e, e, e, es, 1.0, 5.0) == 0
+    one = numpy.array([5.0])
+    s = numpy.array([1], dtype=numpy.int32)
+    assert U.markDimmerPeaks(one, one, one, s, 1.0, 5.0) == 0 and s[0] == 1
+
+
+def test_reference_named_ia_utilities_library():
+    """libsa_ia_utilities.so answers the reference binding's calls
+    (ia_utilities_c.py:16-87) under the reference's names."""
+    from numpy.ctypeslib import ndpointer
+    from sa_gb300 import loadclib
+    loadclib.load()
+    ia = ctypes.CDLL(loadclib.IA_LIB_PATH)
+    f64 = ndpointer(dtype=numpy.float64)
+    i32 = ndpointer(dtype=numpy.int32)
+    ia.markDimmerPeaks.argtypes = [f64, f64, f64, i32, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+    ia.markDimmerPeaks.restype = ctypes.c_int
+    ia.createKDTree.argtypes = [f64, f64, ctypes.c_int]
+    ia.createKDTree.restype = ctypes.c_void_p
+    ia.nearestKDTree.argtypes = [ctypes.c_void_p, f64, f64, f64, i32, ctypes.c_double, ctypes.c_int]
+    ia.freeKDTree.argtypes = [ctypes.c_void_p]
+    g = numpy.load(GOLDEN)
+    x, y, h, sig = (numpy.ascontiguousarray(a) for a in g["cull0_xyhs"])
+    st = numpy.ascontiguousarray(g["cull0_status"]).copy()
+    r1, r2 = (float(v) for v in g["cull0_r"])
+    assert ia.markDimmerPeaks(x, y, h, st, r1, r2, x.size) == int(g["cull0_dimmer_n"])
+    assert numpy.array_equal(st, g["cull0_dimmer"])
+    nx, ny = (numpy.ascontiguousarray(a) for a in g["cull0_new"])
+    kd = ia.createKDTree(nx, ny, nx.size)
+    d = numpy.zeros(x.size)
+    ix = numpy.zeros(x.size, dtype=numpy.int32)
+    ia.nearestKDTree(kd, x, y, d, ix, r2, x.size)
+    ia.freeKDTree(kd)
+    assert numpy.array_equal(d, g["cull0_nearest_d"]) and numpy.array_equal(ix, g["cull0_nearest_i"])

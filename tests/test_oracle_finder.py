@@ -94,3 +94,25 @@ def test_pad_array_mirrors_edges():
     assert numpy.array_equal(p[2:6, 2:7], a)
     assert numpy.array_equal(p[0:2, 2:7], numpy.flipud(a[0:2]))
     assert numpy.array_equal(p[2:6, 0:2], numpy.fliplr(a[:, 0:2]))
+
+
+def test_culling_matches_reference_exactly(g):
+    """markDimmerPeaks, markLowSignificancePeaks, runningIfHasNeighbors and
+    the kd-tree nearest query of the oracle equal the reference's C."""
+    i = 0
+    while "cull%d_xyhs" % i in g:
+        x, y, h, sig = g["cull%d_xyhs" % i]
+        st = g["cull%d_status" % i]
+        r1, r2 = g["cull%d_r" % i]
+        s1 = st.copy()
+        assert F.mark_dimmer_peaks(x, y, h, s1, r1, r2) == int(g["cull%d_dimmer_n" % i])
+        assert numpy.array_equal(s1, g["cull%d_dimmer" % i])
+        s2 = st.copy()
+        assert F.mark_low_significance_peaks(x, y, sig, s2, 6.0, r2) == int(g["cull%d_lowsig_n" % i])
+        assert numpy.array_equal(s2, g["cull%d_lowsig" % i])
+        nx, ny = g["cull%d_new" % i]
+        assert numpy.array_equal(F.running_if_has_neighbors(x, y, nx, ny, st.copy(), r2), g["cull%d_running" % i])
+        d, ix = F.nearest(nx, ny, x, y, r2)
+        assert numpy.array_equal(d, g["cull%d_nearest_d" % i]) and numpy.array_equal(ix, g["cull%d_nearest_i" % i])
+        i += 1
+    assert i == 3
