@@ -50,8 +50,10 @@ void saFilterCleanup(void *flt);
  * (saFilterResultDevice) and are copied to d_result when it is not NULL. */
 int saFilterConvolveDevice(void *flt, const double *d_images, int n_frames, int memo, double *d_result);
 const double *saFilterResultDevice(void *flt);
-/* [separable, taps along rows, taps along cols, first row offset, first
- * col offset, frames allocated] */
+/* [separable (2: separable passes in double-float on the FP32 pipe, the
+ * default; 1: FP64 passes, with SA_FINDER_FP64=1 set when the filter is
+ * created; 0: the FP64 2D path), taps along rows, taps along cols, first row
+ * offset, first col offset, frames allocated] */
 int saFilterInfo(void *flt, int32_t *out6);
 int saFilterSetStream(void *flt, void *stream);
 

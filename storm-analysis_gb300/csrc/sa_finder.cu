@@ -6,17 +6,18 @@
 // over frames of one size.
 //
 // The reference convolves through FFTW.  Here the PSFs the finder uses are
-// small-support Gaussians, so the convolution is computed directly in FP64:
-// two 1D passes for a separable PSF (81 + 81 taps for the background filter
-// of sigma 8), a 2D sum over the support otherwise.  Each pass stages its
-// rows (with the circular halo) in shared memory; the FP64 FMA pipe bounds
-// it.  The local-maxima finder marks candidates one warp per image row
+// small-support Gaussians, so the convolution is computed directly: two 1D
+// passes for a separable PSF (81 + 81 taps for the background filter of
+// sigma 8) in double-float arithmetic on the FP32 pipe (FP64 passes with
+// SA_FINDER_FP64=1), a 2D FP64 sum over the support otherwise.  Each pass
+// stages its rows (with the circular halo) in shared memory.  The local-maxima finder marks candidates one warp per image row
 // (ballot bit masks), scans the row counts in one block and emits the peaks
 // in the reference's plane, row, column order, so the lists are identical.
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -144,6 +145,86 @@ k_conv_slow(const double* __restrict__ in, double* __restrict__ out, int R, int 
     double s = 0.0;
     for (int i = 0; i < na; ++i) s = fma(ws[i], e[-i * kTC], s);
     out[fb + (size_t)r * C + c] = s;
+  }
+}
+
+// The same two passes on the FP32 pipe in double-float arithmetic: GB300
+// issues FP32 FMAs at many times its FP64 rate, so each tap is computed as a
+// float pair.  A double input x is split as x = xh + xl (floats, exact to
+// 2^-48 |x|); a tap adds w * x with the exact product wh*xh (p + e by FMA)
+// plus the cross terms wh*xl + wl*xh, and the running sum is kept as a
+// normalised float pair (Knuth two-sum, then fast two-sum).  Per tap about
+// 2^-48 of the running sum is lost: the result agrees with the FP64 sum to
+// ~1e-14 of its magnitude.  The explicit-rounding intrinsics keep the
+// compiler from fusing the two-sum steps.
+__device__ __forceinline__ float2 ff_split(double v) {
+  const float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(v - (double)h));
+}
+
+__device__ __forceinline__ void ff_tap(float2 w, float2 x, float& sh, float& sl) {
+  const float p = __fmul_rn(w.x, x.x);
+  float e = fmaf(w.x, x.x, -p);
+  e = fmaf(w.x, x.y, e);
+  e = fmaf(w.y, x.x, e);
+  const float s = __fadd_rn(sh, p);
+  const float v = __fsub_rn(s, sh);
+  float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(p, v));
+  t = __fadd_rn(__fadd_rn(t, sl), e);
+  sh = __fadd_rn(s, t);
+  sl = __fsub_rn(t, __fsub_rn(sh, s));
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_conv_fast_ff(const double* __restrict__ in, double* __restrict__ out, int R, int C,
+               const float2* __restrict__ w, int b0, int nb, const int* __restrict__ flag) {
+  extern __shared__ float2 smf[];
+  const int r = blockIdx.x, f = blockIdx.y;
+  if (!flag[f]) return;
+  float2* ws = smf;
+  float2* ext = smf + nb;
+  const size_t row = ((size_t)f * R + r) * C;
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) ws[j] = w[j];
+  int base = (-b0 - nb + 1) % C;
+  if (base < 0) base += C;
+  const int next = C + nb - 1;
+  for (int t = threadIdx.x; t < next; t += blockDim.x) ext[t] = ff_split(in[row + (t + base) % C]);
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) {
+    const float2* e = ext + c + nb - 1;
+    float sh = 0.0f, sl = 0.0f;
+    for (int j = 0; j < nb; ++j) ff_tap(ws[j], e[-j], sh, sl);
+    out[row + c] = (double)sh + (double)sl;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_conv_slow_ff(const double* __restrict__ in, double* __restrict__ out, int R, int C,
+               const float2* __restrict__ w, int a0, int na, const int* __restrict__ flag) {
+  extern __shared__ float2 smf[];
+  const int f = blockIdx.z;
+  if (!flag[f]) return;
+  const int c0 = blockIdx.x * kTC, r0 = blockIdx.y * kSlowTR;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTC + tx;
+  float2* ws = smf;
+  float2* ext = smf + na;
+  const size_t fb = (size_t)f * R * C;
+  for (int j = tid; j < na; j += kThreads) ws[j] = w[j];
+  int base = (r0 - a0 - na + 1) % R;
+  if (base < 0) base += R;
+  const int nrows = kSlowTR + na - 1;
+  const int c = c0 + tx;
+  for (int t = ty; t < nrows; t += kThreads / kTC)
+    ext[t * kTC + tx] = (c < C) ? ff_split(in[fb + (size_t)((base + t) % R) * C + c]) : make_float2(0.0f, 0.0f);
+  __syncthreads();
+  if (c >= C) return;
+  for (int q = ty; q < kSlowTR; q += kThreads / kTC) {
+    const int r = r0 + q;
+    if (r >= R) break;
+    const float2* e = ext + (q + na - 1) * kTC + tx;
+    float sh = 0.0f, sl = 0.0f;
+    for (int i = 0; i < na; ++i) ff_tap(ws[i], e[-i * kTC], sh, sl);
+    out[fb + (size_t)r * C + c] = (double)sh + (double)sl;
   }
 }
 
@@ -626,6 +707,9 @@ struct MFilter {
   int a0 = 0, na = 1, b0 = 0, nb = 1;
   double* d_wa = nullptr;   // separable: taps along rows (slow axis)
   double* d_wb = nullptr;   // separable: taps along columns (fast axis)
+  float2* d_wa_ff = nullptr;   // the same taps as float pairs
+  float2* d_wb_ff = nullptr;
+  int ff = 1;                  // separable passes in double-float (FP32 pipe)
   double* d_w2 = nullptr;   // 2D: na x nb
   double max_diff = 0.0;
   std::vector<double> h_rc;   // the recentred PSF, first content of every frame's result
@@ -644,6 +728,8 @@ struct MFilter {
 void filter_free(MFilter* m) {
   dfree(m->d_wa);
   dfree(m->d_wb);
+  dfree(m->d_wa_ff);
+  dfree(m->d_wb_ff);
   dfree(m->d_w2);
   dfree(m->d_last);
   dfree(m->d_old);
@@ -702,11 +788,18 @@ int filter_run(MFilter* m, const double* d_in, int n, int memo, cudaStream_t s) 
     FCK(cudaMemsetAsync(m->d_flag, 0x01, sizeof(int) * n, s));
   }
   if (m->separable) {
-    k_conv_fast<<<dim3(m->R, n), kThreads, m->smem_fast, s>>>(d_in, m->d_tmp, m->R, m->C, m->d_wb,
-                                                             m->b0, m->nb, m->d_flag);
     const dim3 g((m->C + kTC - 1) / kTC, (m->R + kSlowTR - 1) / kSlowTR, n);
-    k_conv_slow<<<g, dim3(kTC, kThreads / kTC), m->smem_slow, s>>>(m->d_tmp, m->d_last, m->R, m->C,
-                                                                    m->d_wa, m->a0, m->na, m->d_flag);
+    if (m->ff) {
+      k_conv_fast_ff<<<dim3(m->R, n), kThreads, m->smem_fast, s>>>(d_in, m->d_tmp, m->R, m->C, m->d_wb_ff,
+                                                                  m->b0, m->nb, m->d_flag);
+      k_conv_slow_ff<<<g, dim3(kTC, kThreads / kTC), m->smem_slow, s>>>(m->d_tmp, m->d_last, m->R, m->C,
+                                                                         m->d_wa_ff, m->a0, m->na, m->d_flag);
+    } else {
+      k_conv_fast<<<dim3(m->R, n), kThreads, m->smem_fast, s>>>(d_in, m->d_tmp, m->R, m->C, m->d_wb,
+                                                               m->b0, m->nb, m->d_flag);
+      k_conv_slow<<<g, dim3(kTC, kThreads / kTC), m->smem_slow, s>>>(m->d_tmp, m->d_last, m->R, m->C,
+                                                                      m->d_wa, m->a0, m->na, m->d_flag);
+    }
     m->launches += 2;
   } else {
     const dim3 g((m->C + kTC - 1) / kTC, (m->R + k2dTR - 1) / k2dTR, n);
@@ -776,10 +869,27 @@ MFilter* filter_create(const double* psf, double max_diff, int R, int C) {
       ok = false;
       reported = true;
     }
+    // float-pair copies of the taps (hi = nearest float, lo = nearest float
+    // of the remainder)
+    auto split = [](const std::vector<double>& a) {
+      std::vector<float2> o(a.size());
+      for (size_t k = 0; k < a.size(); ++k) {
+        const float h = (float)a[k];
+        o[k] = make_float2(h, (float)(a[k] - (double)h));
+      }
+      return o;
+    };
+    const std::vector<float2> uf = split(u), vf = split(v);
+    const char* env = getenv("SA_FINDER_FP64");
+    m->ff = !(env && env[0] == '1');
     ok = ok && cudaMalloc(&m->d_wa, sizeof(double) * na) == cudaSuccess &&
          cudaMalloc(&m->d_wb, sizeof(double) * nb) == cudaSuccess &&
+         cudaMalloc(&m->d_wa_ff, sizeof(float2) * na) == cudaSuccess &&
+         cudaMalloc(&m->d_wb_ff, sizeof(float2) * nb) == cudaSuccess &&
          cudaMemcpy(m->d_wa, u.data(), sizeof(double) * na, cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(m->d_wb, v.data(), sizeof(double) * nb, cudaMemcpyHostToDevice) == cudaSuccess;
+         cudaMemcpy(m->d_wb, v.data(), sizeof(double) * nb, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(m->d_wa_ff, uf.data(), sizeof(float2) * na, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(m->d_wb_ff, vf.data(), sizeof(float2) * nb, cudaMemcpyHostToDevice) == cudaSuccess;
   } else {
     m->smem_2d = sizeof(double) * (size_t)(na * nb + (k2dTR + na - 1) * (kTC + nb - 1));
     if (m->smem_2d > kSmemMax) {
@@ -795,6 +905,8 @@ MFilter* filter_create(const double* psf, double max_diff, int R, int C) {
          cudaMemcpy(m->d_w2, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice) == cudaSuccess;
   }
   ok = ok && cudaFuncSetAttribute(k_conv_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax) == cudaSuccess &&
+       cudaFuncSetAttribute(k_conv_fast_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax) == cudaSuccess &&
+       cudaFuncSetAttribute(k_conv_slow_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax) == cudaSuccess &&
        cudaFuncSetAttribute(k_conv_slow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax) == cudaSuccess &&
        cudaFuncSetAttribute(k_conv_2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax) == cudaSuccess &&
        cudaMalloc(&m->d_io, sizeof(double) * (size_t)R * C) == cudaSuccess &&
@@ -1061,16 +1173,30 @@ const double* finder_input(Finder* h, const double* p, int on_device, double** d
   return *dst;
 }
 
-// Device arrays of one culling call (host-array entry points).
+// Device arrays of the culling entry points (host arrays in and out),
+// kept per thread and grown on demand so that a call allocates nothing in
+// the steady state.
 struct CullBuf {
   double* d = nullptr;    // x, y, value (3 n) + query x, y (2 nq)
-  int32_t* i = nullptr;   // status in/out (2 n), marked (n), items (n), counts/starts/cursor (3 T), misc (4)
+  int32_t* i = nullptr;   // status in/out (2 n), marked (n), items (n), counts/starts/cursor (3 T), misc (8)
+  double* dq = nullptr;   // nearest distances (nq)
+  size_t cap_d = 0, cap_i = 0, cap_q = 0;
   int n = 0, nq = 0, T = 0;
-  ~CullBuf() {
-    dfree(d);
-    dfree(i);
-  }
 };
+
+CullBuf& cull_buf() {
+  static thread_local CullBuf b;
+  return b;
+}
+
+template <typename P>
+int grow(P*& p, size_t* cap, size_t want) {
+  if (want <= *cap) return 0;
+  dfree(p);
+  FCK(cudaMalloc(&p, sizeof(P) * want));
+  *cap = want;
+  return 0;
+}
 
 int table_size(int n) {
   int T = 1024;
@@ -1106,8 +1232,7 @@ int cull_setup(CullBuf& b, int n, int nq, const double* x, const double* y, cons
   b.nq = nq;
   b.T = table_size(n);
   const size_t nd = 3 * (size_t)n + 2 * (size_t)nq + 2, ni = 4 * (size_t)std::max(n, nq) + 3 * (size_t)b.T + 8;
-  FCK(cudaMalloc(&b.d, sizeof(double) * nd));
-  FCK(cudaMalloc(&b.i, sizeof(int32_t) * ni));
+  if (grow(b.d, &b.cap_d, nd) || grow(b.i, &b.cap_i, ni) || grow(b.dq, &b.cap_q, (size_t)nq + 1)) return -1;
   double *dx = b.d, *dy = b.d + n, *dv = b.d + 2 * n, *qxd = b.d + 3 * n, *qyd = qxd + nq;
   if (n > 0) {
     FCK(cudaMemcpy(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice));
@@ -1201,7 +1326,7 @@ const double* saFilterResultDevice(void* flt) {
 int saFilterInfo(void* flt, int32_t* out6) {
   MFilter* m = static_cast<MFilter*>(flt);
   if (!m || !out6) return -1;
-  out6[0] = m->separable;
+  out6[0] = m->separable ? (m->ff ? 2 : 1) : 0;
   out6[1] = m->na;
   out6[2] = m->nb;
   out6[3] = m->a0;
@@ -1384,7 +1509,7 @@ int saMarkDimmerPeaks(double* x, double* y, double* h, int32_t* status, double r
     ferr("markDimmerPeaks: NULL argument");
     return -1;
   }
-  CullBuf b;
+  CullBuf& b = cull_buf();
   PointGrid g;
   if (cull_setup(b, np, 0, x, y, h, status, nullptr, nullptr, std::max(r_removal, r_neighbors), &g)) return -1;
   int32_t* st_in = b.i;
@@ -1407,7 +1532,7 @@ int saMarkLowSignificancePeaks(double* x, double* y, double* sig, int32_t* statu
     ferr("markLowSignificancePeaks: NULL argument");
     return -1;
   }
-  CullBuf b;
+  CullBuf& b = cull_buf();
   PointGrid g;
   if (cull_setup(b, np, 0, x, y, sig, status, nullptr, nullptr, r_neighbors, &g)) return -1;
   int32_t* st_in = b.i;
@@ -1430,7 +1555,7 @@ void saRunningIfHasNeighbors(double* c_x, double* c_y, double* n_x, double* n_y,
     ferr("runningIfHasNeighbors: NULL argument");
     return;
   }
-  CullBuf b;
+  CullBuf& b = cull_buf();
   PointGrid g;
   // grid over the new peaks, queries are the current peaks
   if (cull_setup(b, nn, nc, n_x, n_y, nullptr, nullptr, c_x, c_y, radius, &g)) return;
@@ -1476,23 +1601,17 @@ void saNearestKDTree(void* kd, double* x, double* y, double* dist, int32_t* inde
     }
     return;
   }
-  CullBuf b;
+  CullBuf& b = cull_buf();
   PointGrid g;
   if (cull_setup(b, p->n, n, p->x.data(), p->y.data(), nullptr, nullptr, x, y, radius, &g)) return;
   double* qx = b.d + 3 * (size_t)p->n;
   double* qy = qx + n;
-  double* dd = nullptr;
   int32_t* di = b.i + 2 * (size_t)std::max(p->n, n);
-  if (cudaMalloc(&dd, sizeof(double) * n) != cudaSuccess) {
-    ferr("nearestKDTree: device allocation failed");
-    return;
-  }
-  k_nearest<<<grid_for(n), kThreads>>>(g, qx, qy, n, radius, dd, di);
+  k_nearest<<<grid_for(n), kThreads>>>(g, qx, qy, n, radius, b.dq, di);
   if (cudaGetLastError() != cudaSuccess ||
-      cudaMemcpy(dist, dd, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(dist, b.dq, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(index, di, sizeof(int32_t) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
     ferr("nearestKDTree: device step failed");
-  cudaFree(dd);
 }
 
 void* saIngestCreate(int rows, int cols, int pad, const double* offset, const double* scale, double offset0,

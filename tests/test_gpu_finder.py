@@ -41,12 +41,34 @@ def test_matched_filter_separable(shape, sigma):
     rng = numpy.random.default_rng(int(sigma * 10) + shape[0])
     psf = F.gaussian_psf(shape, sigma)
     g = matched_filter_c.MatchedFilter(psf)
-    assert g.info()[0] == 1
+    assert g.info()[0] == 2        # separable, double-float passes
     o = F.MatchedFilter(psf)
     for _ in range(2):
         img = rng.uniform(0.0, 200.0, shape)
         assert conv_close(g.convolve(img), o.convolve(img))
     g.cleanup()
+
+
+def test_double_float_passes_match_fp64_passes(monkeypatch):
+    """The default separable passes (double-float on the FP32 pipe) agree
+    with the FP64 passes (SA_FINDER_FP64=1) to 1e-13 of the magnitude, on
+    the background (81 taps) and PSF-squared filters."""
+    from sa_gb300 import matched_filter_c
+    rng = numpy.random.default_rng(12)
+    for sigma, square in ((8.0, False), (1.0, True)):
+        psf = F.gaussian_psf((534, 534), sigma)
+        if square:
+            psf = psf * psf
+        g_ff = matched_filter_c.MatchedFilter(psf)
+        monkeypatch.setenv("SA_FINDER_FP64", "1")
+        g_64 = matched_filter_c.MatchedFilter(psf)
+        monkeypatch.delenv("SA_FINDER_FP64")
+        assert g_ff.info()[0] == 2 and g_64.info()[0] == 1
+        img = rng.uniform(1.0, 5000.0, (534, 534))
+        a, b = g_ff.convolve(img), g_64.convolve(img)
+        assert numpy.abs(a - b).max() <= 1e-13 * numpy.abs(b).max()
+        g_ff.cleanup()
+        g_64.cleanup()
 
 
 def test_matched_filter_psf_squared_and_2d_path():
