@@ -288,6 +288,23 @@ __device__ bool is_local_max(const LMax& a, const double* fimg, int zi, int yi, 
   const int sz = max(zi - a.z_range, 0), ez = min(zi + a.z_range, a.Z - 1);
   const int sy = max((int)(yi - a.radius), 0), ey = min((int)(yi + a.radius), a.R - 1);
   const int sx = max(xi - a.cr, 0), ex = min(xi + a.cr, a.C - 1);
+  // A necessary condition first: the 3 x 3 neighbourhood in the candidate's
+  // own plane (part of the search below).  Most candidates sit on the slope
+  // of a peak and fail here after a few reads; the outcome is the same
+  // since the test is a conjunction over the search region.
+  {
+    const double* p = fimg + (size_t)zi * a.R * a.C;
+    for (int y = max(yi - 1, sy); y <= min(yi + 1, ey); ++y)
+      for (int x = max(xi - 1, sx); x <= min(xi + 1, ex); ++x) {
+        if ((x - xi) * (x - xi) + (y - yi) * (y - yi) > a.rr) continue;
+        const double v = p[(size_t)y * a.C + x];
+        if (y <= yi && x <= xi) {
+          if (v > cur) return false;
+        } else if (v >= cur) {
+          return false;
+        }
+      }
+  }
   for (int z = sz; z <= ez; ++z) {
     const double* p = fimg + (size_t)z * a.R * a.C;
     for (int y = sy; y <= ey; ++y) {
@@ -476,8 +493,9 @@ __global__ void k_find_ratio(const double* __restrict__ fg, const double* __rest
 // Frame ingest: FrameReader.loadAFrame (sa_library/analysis_io.py:243-260:
 // (frame - offset) * (gain * rqe), values below 1 set to 1) and padArray
 // (sa_library/fitting.py:112-132: mirror padding that repeats the edge
-// pixel), one block per padded output row.  Raw pixels are uint16 (byte
-// swapped for big-endian .dax data), float32 or float64.
+// pixel).  Raw pixels are uint16 (byte swapped for big-endian .dax data),
+// float32 or float64.  One thread per padded output pixel: coalesced
+// writes, reads from the mirrored source.
 __device__ __forceinline__ int mirror_index(int i, int n) {
   return i < 0 ? -1 - i : (i >= n ? 2 * n - 1 - i : i);
 }
@@ -486,28 +504,28 @@ __global__ void __launch_bounds__(kThreads)
 k_ingest(const void* __restrict__ raw, int bits, int swap, int rows, int cols, int pad,
          const double* __restrict__ offset, const double* __restrict__ scale, double off0, double sc0,
          int clip, double* __restrict__ out) {
+  // one thread per padded output pixel of frame blockIdx.y
   const int prow = rows + 2 * pad, pcol = cols + 2 * pad;
-  const int y = blockIdx.x % prow, f = blockIdx.x / prow;
-  const int sy = mirror_index(y - pad, rows);
-  const size_t src_row = ((size_t)f * rows + sy) * cols;
-  double* o = out + ((size_t)f * prow + y) * pcol;
-  for (int x = threadIdx.x; x < pcol; x += blockDim.x) {
-    const int sx = mirror_index(x - pad, cols);
-    double v;
-    if (bits == 16) {
-      unsigned int u = static_cast<const uint16_t*>(raw)[src_row + sx];
-      if (swap) u = ((u >> 8) | (u << 8)) & 0xffffu;
-      v = (double)u;
-    } else if (bits == 32) {
-      v = (double)static_cast<const float*>(raw)[src_row + sx];
-    } else {
-      v = static_cast<const double*>(raw)[src_row + sx];
-    }
-    const int p = sy * cols + sx;
-    v = (v - (offset ? offset[p] : off0)) * (scale ? scale[p] : sc0);
-    if (clip && v < 1.0) v = 1.0;
-    o[x] = v;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= prow * pcol) return;
+  const int f = blockIdx.y;
+  const int y = i / pcol, x = i - y * pcol;
+  const int sy = mirror_index(y - pad, rows), sx = mirror_index(x - pad, cols);
+  const int p = sy * cols + sx;
+  const size_t src = (size_t)f * rows * cols + p;
+  double v;
+  if (bits == 16) {
+    unsigned int u = static_cast<const uint16_t*>(raw)[src];
+    if (swap) u = ((u >> 8) | (u << 8)) & 0xffffu;
+    v = (double)u;
+  } else if (bits == 32) {
+    v = (double)static_cast<const float*>(raw)[src];
+  } else {
+    v = static_cast<const double*>(raw)[src];
   }
+  v = (v - (offset ? offset[p] : off0)) * (scale ? scale[p] : sc0);
+  if (clip && v < 1.0) v = 1.0;
+  out[(size_t)f * prow * pcol + i] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -1676,7 +1694,8 @@ int saIngestFrames(void* ih, const void* frames, int n_frames, int dtype_bits, i
     }
     out = h->d_out;
   }
-  k_ingest<<<n_frames * prow, kThreads, 0, h->stream>>>(src, dtype_bits, big_endian && dtype_bits == 16,
+  const dim3 grid((unsigned)(((size_t)prow * pcol + kThreads - 1) / kThreads), n_frames);
+  k_ingest<<<grid, kThreads, 0, h->stream>>>(src, dtype_bits, big_endian && dtype_bits == 16,
                                                         h->rows, h->cols, h->pad, h->d_offset, h->d_scale,
                                                         h->off0, h->sc0, h->clip, out);
   h->launches += 1;
