@@ -500,6 +500,23 @@ __device__ __forceinline__ int mirror_index(int i, int n) {
   return i < 0 ? -1 - i : (i >= n ? 2 * n - 1 - i : i);
 }
 
+// GB300 issues few FP64 instructions per clock, so the exact parts of the
+// conversion run on the integer pipe: a uint16 becomes a double by building
+// its bits (exponent from the leading one, the rest as mantissa), and
+// "v < 1.0" is decided on the bit pattern.
+__device__ __forceinline__ double u16_to_double(unsigned int u) {
+  if (u == 0) return 0.0;
+  const int e = 31 - __clz(u);
+  const unsigned long long m = ((unsigned long long)u << (52 - e)) & 0xFFFFFFFFFFFFFull;
+  return __longlong_as_double((long long)(((unsigned long long)(1023 + e) << 52) | m));
+}
+
+__device__ __forceinline__ bool less_than_one(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  if ((b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return false;   // NaN
+  return (b >> 63) ? true : b < 0x3FF0000000000000ull;
+}
+
 __global__ void __launch_bounds__(kThreads)
 k_ingest(const void* __restrict__ raw, int bits, int swap, int rows, int cols, int pad,
          const double* __restrict__ offset, const double* __restrict__ scale, double off0, double sc0,
@@ -517,14 +534,14 @@ k_ingest(const void* __restrict__ raw, int bits, int swap, int rows, int cols, i
   if (bits == 16) {
     unsigned int u = static_cast<const uint16_t*>(raw)[src];
     if (swap) u = ((u >> 8) | (u << 8)) & 0xffffu;
-    v = (double)u;
+    v = u16_to_double(u);
   } else if (bits == 32) {
     v = (double)static_cast<const float*>(raw)[src];
   } else {
     v = static_cast<const double*>(raw)[src];
   }
   v = (v - (offset ? offset[p] : off0)) * (scale ? scale[p] : sc0);
-  if (clip && v < 1.0) v = 1.0;
+  if (clip && less_than_one(v)) v = 1.0;
   out[(size_t)f * prow * pcol + i] = v;
 }
 
