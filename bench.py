@@ -24,6 +24,8 @@ step fits all 64 frames to termination through the batched engine.
           clip, mirror pad), and "ingest" times that kernel alone
   culling the post-fit culling (markDimmerPeaks, markLowSignificancePeaks)
           on the step's fitted peaks, per frame, reference call shape
+  analysis  the whole per-frame find / fit loop (sa_gb300.find_peaks) on two
+          of the frames, with the oracle's loop on one frame beside it
 
 `python bench.py --impl reference` times the CPU oracle on all host cores on
 the same workload and prints the same JSON line with "impl": "reference".
@@ -414,6 +416,7 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0 and not args.no_finder:
         line["finder"] = run_finder(args, wl, torch)
         line["culling"] = run_culling(args, fit)
+        line["analysis"] = run_analysis(args, wl)
     if dist is not None:
         dist.destroy_process_group()
     fit.close()
@@ -604,6 +607,38 @@ def run_culling(args, fit):
         w = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": nk / w, "unit": "peaks/s", "cores": 1, "kind": "port",
                                "sample": "%d frames, brute-force neighbour search in numpy, %.3f s" % (k, w)}
+    return out
+
+
+def run_analysis(args, wl):
+    """The whole 3D-DAOSTORM frame analysis (PeakFinderFitter.analyzeImage:
+    finder passes with the threshold count-down, fits, culling, removal of
+    unconverged peaks) through sa_gb300.find_peaks on two of the step's
+    512 x 512 frames, one frame at a time as the reference analyses a
+    movie; the CPU baseline runs the oracle's loop on the first frame."""
+    from sa_gb300 import find_peaks
+    params = dict(FINDER_PARAMS, model="3d")
+    n = 2
+    ff = find_peaks.initFindAndFit(params, precision=args.precision)
+    ff.analyzeFrame(wl["images"][0])    # warm-up: filters, handles, first launches
+    t0 = time.perf_counter()
+    found = [ff.analyzeFrame(wl["images"][i])["x"].size for i in range(n)]
+    wall = time.perf_counter() - t0
+    ff.peak_fitter.mfitter.cleanup(verbose=False)
+    ff.peak_finder.cleanUp()
+    out = {"metric": "frames/s (find / fit loop per frame, host-driven as the reference)",
+           "value": n / wall, "unit": "frames/s", "frames": n, "localizations": int(sum(found)),
+           "localizations_per_s": sum(found) / wall}
+    if not args.no_cpu:
+        from oracle import analysis
+        t0 = time.perf_counter()
+        ref = analysis.analyze_frame(params, wl["images"][0], [0.75, 7.5])
+        w = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / w, "unit": "frames/s", "cores": 1, "kind": "port",
+                               "sample": "1 frame through the oracle's loop (FP64 C fitter, numpy finder "
+                                         "and culling), %.1f s" % w}
+        out["oracle_localizations_frame0"] = int(ref["x"].size)
+        out["gpu_localizations_frame0"] = int(found[0])
     return out
 
 
