@@ -25,7 +25,8 @@ step fits all 64 frames to termination through the batched engine.
   culling the post-fit culling (markDimmerPeaks, markLowSignificancePeaks)
           on the step's fitted peaks, per frame, reference call shape
   analysis  the whole per-frame find / fit loop (sa_gb300.find_peaks) on two
-          of the frames, with the oracle's loop on one frame beside it
+          of the frames, with the oracle's loop on one frame beside it;
+          analysis_batch the same loop for all frames at once (BatchFindFit)
 
 `python bench.py --impl reference` times the CPU oracle on all host cores on
 the same workload and prints the same JSON line with "impl": "reference".
@@ -417,6 +418,7 @@ def run_ours(args, rank, world, local_rank):
         line["finder"] = run_finder(args, wl, torch)
         line["culling"] = run_culling(args, fit)
         line["analysis"] = run_analysis(args, wl)
+        line["analysis_batch"] = run_analysis_batch(args, wl)
     if dist is not None:
         dist.destroy_process_group()
     fit.close()
@@ -640,6 +642,26 @@ def run_analysis(args, wl):
         out["oracle_localizations_frame0"] = int(ref["x"].size)
         out["gpu_localizations_frame0"] = int(found[0])
     return out
+
+
+def run_analysis_batch(args, wl):
+    """The same find / fit loop for all of the step's frames at once
+    (sa_gb300.find_peaks.BatchFindFit): finder and fits stay on the GPU
+    across passes, all frames' fits run in one batched sweep loop."""
+    from sa_gb300 import find_peaks
+    params = dict(FINDER_PARAMS, model="3d")
+    frames = numpy.stack(wl["images"])
+    bf = find_peaks.BatchFindFit(params, frames.shape[1:], frames.shape[0], precision=args.precision)
+    bf.analyze(frames[:, ::-1, :].copy())    # warm-up on other frames
+    t0 = time.perf_counter()
+    res = bf.analyze(frames)
+    wall = time.perf_counter() - t0
+    passes = bf.passes
+    bf.cleanUp()
+    n = sum(r["x"].size for r in res)
+    return {"metric": "frames/s (find / fit loop, all frames batched)", "value": frames.shape[0] / wall,
+            "unit": "frames/s", "frames": int(frames.shape[0]), "localizations": int(n),
+            "localizations_per_s": n / wall, "passes": passes, "wall_s": wall}
 
 
 def run_reference(args, rank, world):

@@ -214,6 +214,21 @@ int saNewPeaksBatch(saFitData *fit, const double *peaks, const int32_t *counts, 
 int saNewPeaksBatchDevice(saFitData *fit, const double *d_peaks, const int32_t *counts, int n_frames,
                           const char *p_type);
 int saDoFitBatch(saFitData *fit, int max_iterations);
+/* As saDoFitBatch for the frames with active[f] != 0 only; the others are
+ * left untouched (a frame the find / fit loop gave no new peaks). */
+int saDoFitBatchFrames(saFitData *fit, int max_iterations, const int32_t *active);
+/* mFitSetPeakStatus for every frame: status holds all frames' peaks, frames
+ * in order (multi_fit.c:1809-1831). */
+int saSetPeakStatusBatch(saFitData *fit, const int32_t *status);
+/* mFitRemoveErrorPeaks (status 2) / mFitRemoveRunningPeaks (status 0) for
+ * every frame (multi_fit.c:1704-1779). */
+int saRemovePeaksBatch(saFitData *fit, int status);
+/* Grow every frame's peak storage to at least capacity_per_frame, keeping
+ * the peaks (saSetFrames drops them). */
+int saReservePeaksBatch(saFitData *fit, int capacity_per_frame);
+/* mFitGetFitImage (residual 0) / mFitGetResidual (1) of every frame into
+ * device memory d_out (n_frames x image_size_y x image_size_x doubles). */
+int saGetFitImagesDevice(saFitData *fit, double *d_out, int residual);
 int saGetNFitBatch(saFitData *fit, int32_t *counts);
 int saGetPeakPropertyBatch(saFitData *fit, double *values, const char *what);
 int saGetPeakPropertyIntBatch(saFitData *fit, int32_t *values, const char *what);

@@ -485,8 +485,10 @@ struct Engine {
     return 0;
   }
 
-  // Start a fit (max_sweeps sweeps at most) on all frames and run it.
-  int fit(int max_sweeps, int* sweeps_out) {
+  // Start a fit (max_sweeps sweeps at most) on all frames, or on the frames
+  // with active[f] != 0, and run it.  Inactive frames stay DONE: every
+  // kernel skips them.
+  int fit(int max_sweeps, int* sweeps_out, const int32_t* active = nullptr) {
     if (!d_pk) {
       if (sweeps_out) *sweeps_out = 0;
       return 0;
@@ -494,7 +496,7 @@ struct Engine {
     std::vector<FrameCtl> ctl(F);
     CK(cudaMemcpy(ctl.data(), d_ctl, sizeof(FrameCtl) * F, cudaMemcpyDeviceToHost));
     for (int f = 0; f < F; f++) {
-      ctl[f].phase = PH_SWEEP_PENDING;
+      ctl[f].phase = (active && !active[f]) ? PH_DONE : PH_SWEEP_PENDING;
       ctl[f].sweeps = 0;
       ctl[f].max_sweeps = max_sweeps;
     }
@@ -1422,6 +1424,117 @@ int saDoFitBatch(saFitData* h, int max_iterations) {
   if (e->fit(max_iterations + 1, &sw)) return -1;
   sync_counters(h);
   return sw;
+}
+
+int saDoFitBatchFrames(saFitData* h, int max_iterations, const int32_t* active) {
+  Engine* e = E(h);
+  if (!e || !active) return -1;
+  int sw = 0;
+  if (e->fit(max_iterations + 1, &sw, active)) return -1;
+  sync_counters(h);
+  return sw;
+}
+
+// All frames' peak records to the host (frame-major, nfit[f] each).
+static int pull_all(Engine* e, std::vector<std::vector<PeakRec>>& out) {
+  out.assign(e->F, {});
+  for (int f = 0; f < e->F; f++) {
+    out[f].resize(e->nfit[f]);
+    if (e->nfit[f] > 0)
+      CK(cudaMemcpy(out[f].data(), e->d_pk + e->pk_off[f], sizeof(PeakRec) * e->nfit[f], cudaMemcpyDeviceToHost));
+  }
+  return 0;
+}
+
+static int push_all(Engine* e, const std::vector<std::vector<PeakRec>>& in) {
+  for (int f = 0; f < e->F; f++) {
+    if (!in[f].empty())
+      CK(cudaMemcpy(e->d_pk + e->pk_off[f], in[f].data(), sizeof(PeakRec) * in[f].size(), cudaMemcpyHostToDevice));
+    e->nfit[f] = (int)in[f].size();
+  }
+  if (e->sync_nfit()) return -1;
+  CK(cudaStreamSynchronize(e->stream));
+  e->host_valid = false;
+  e->unconv_cache = -1;
+  return 0;
+}
+
+int saSetPeakStatusBatch(saFitData* h, const int32_t* status) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk || !status) return -1;
+  std::vector<int> slots, frames;
+  for (int f = 0; f < e->F; f++)
+    for (int i = 0; i < e->nfit[f]; i++) {
+      slots.push_back(e->pk_off[f] + i);
+      frames.push_back(f);
+    }
+  const int n = (int)slots.size();
+  if (n == 0) return 0;
+  const size_t ib = (size_t)n * sizeof(int);
+  if (e->stage(3 * ib)) return -1;
+  int* d_slots = (int*)e->d_stage;
+  int* d_frames = d_slots + n;
+  int* d_status = d_frames + n;
+  CK(cudaMemcpyAsync(d_slots, slots.data(), ib, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(d_frames, frames.data(), ib, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(d_status, status, ib, cudaMemcpyHostToDevice, e->stream));
+  CK((e->prec == 32)
+         ? Launch<float>::set_status(e->cfg, e->fs<float>(), d_slots, d_frames, d_status, n, e->warp_smem, e->stream)
+         : Launch<double>::set_status(e->cfg, e->fs<double>(), d_slots, d_frames, d_status, n, e->warp_smem,
+                                      e->stream));
+  e->launches += 1;
+  CK(cudaStreamSynchronize(e->stream));
+  e->host_valid = false;
+  e->unconv_cache = -1;
+  return 0;
+}
+
+int saRemovePeaksBatch(saFitData* h, int status) {
+  Engine* e = E(h);
+  if (!e || !e->d_pk) return -1;
+  std::vector<std::vector<PeakRec>> recs;
+  if (pull_all(e, recs)) return -1;
+  for (auto& v : recs) {
+    std::vector<PeakRec> keep;
+    keep.reserve(v.size());
+    for (const PeakRec& r : v) {
+      if (r.status != status) keep.push_back(r);
+      else if (status == RUNNING) h->n_non_converged++;
+    }
+    v.swap(keep);
+  }
+  if (push_all(e, recs)) return -1;
+  h->nfit = e->nfit[0];
+  return 0;
+}
+
+int saReservePeaksBatch(saFitData* h, int capacity_per_frame) {
+  Engine* e = E(h);
+  if (!e || e->F < 1) return -1;
+  bool need = !e->d_pk;
+  for (int f = 0; f < e->F && !need; f++) need = e->cap_f[f] < capacity_per_frame;
+  if (!need) return 0;
+  std::vector<std::vector<PeakRec>> recs;
+  if (e->d_pk && pull_all(e, recs)) return -1;
+  std::vector<int> caps(e->F);
+  for (int f = 0; f < e->F; f++) caps[f] = std::max(capacity_per_frame, e->d_pk ? e->cap_f[f] : 0);
+  if (e->set_peak_caps(caps)) return -1;
+  if (!recs.empty() && push_all(e, recs)) return -1;
+  h->max_nfit = e->cap_f[0];
+  return 0;
+}
+
+int saGetFitImagesDevice(saFitData* h, double* d_out, int residual) {
+  Engine* e = E(h);
+  if (!e || !d_out || !e->d_x) return -1;
+  for (int f = 0; f < e->F; f++) {
+    CK((e->prec == 32) ? Launch<float>::fit_image(e->fs<float>(), f, d_out + (size_t)f * e->npix, residual, e->stream)
+                       : Launch<double>::fit_image(e->fs<double>(), f, d_out + (size_t)f * e->npix, residual,
+                                                   e->stream));
+    e->launches += 1;
+  }
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
 }
 
 int saGetNFitBatch(saFitData* h, int32_t* counts) {

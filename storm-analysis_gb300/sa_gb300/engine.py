@@ -131,6 +131,33 @@ class BatchFitter(object):
                                                         ctypes.c_char_p(peaks_type.encode())),
                         "saNewPeaksBatchDevice")
 
+    def reserve(self, capacity_per_frame):
+        """Grow each frame's peak storage, keeping its peaks."""
+        if not self._framed:
+            return self.ensure_frames(capacity_per_frame)
+        if capacity_per_frame > (self.capacity or 0):
+            self._ok(self.clib.saReservePeaksBatch(self.h, int(capacity_per_frame)), "saReservePeaksBatch")
+            self.capacity = int(capacity_per_frame)
+
+    def fit_frames(self, active, max_iterations=2000):
+        """Fit only the frames with active[f] true."""
+        a = numpy.ascontiguousarray(numpy.asarray(active, dtype=numpy.int32))
+        return self._ok(self.clib.saDoFitBatchFrames(self.h, int(max_iterations), a), "saDoFitBatchFrames")
+
+    def set_status(self, status):
+        """Statuses of all frames' peaks (frames in order), as mFitSetPeakStatus."""
+        st = numpy.ascontiguousarray(status, dtype=numpy.int32)
+        return self._ok(self.clib.saSetPeakStatusBatch(self.h, st), "saSetPeakStatusBatch")
+
+    def remove(self, status):
+        """Drop every frame's peaks with this status (2 ERROR, 0 RUNNING)."""
+        return self._ok(self.clib.saRemovePeaksBatch(self.h, int(status)), "saRemovePeaksBatch")
+
+    def fit_images_device(self, d_out, residual=False):
+        """Every frame's fit image into device memory d_out (address)."""
+        return self._ok(self.clib.saGetFitImagesDevice(self.h, ctypes.c_void_p(d_out), 1 if residual else 0),
+                        "saGetFitImagesDevice")
+
     def results_fast(self):
         """All results with one device-to-host copy: (values[n, 8], ints[n, 2]) with
         columns x, y, z, height, background, xsigma, ysigma, error / status, iterations."""

@@ -6,12 +6,19 @@ GPU finder (fitting.PeakFinderGaussian), culling (ia_utilities_c) and
 fitter (dao_fit_c).  Same control flow as the reference: per frame, up to
 `iterations` passes of background estimate -> new peaks -> fit -> culling,
 then the unconverged peaks are removed.
+
+BatchFindFit runs the same loop for n frames at once: frames, backgrounds,
+new peaks, fit images and the fits stay on the GPU across passes, the fits
+of all frames run in one batched sweep loop, and only the per-frame peak
+lists that the culling reads travel to the host.
 """
 import numpy
 
-from . import dao_fit_c
+from . import dao_fit_c, engine
 from . import ia_utilities_c as iaUtilsC
-from .fitting import PeakFinderGaussian, _Params, padArray
+from .fitting import BatchPeakFinder, PeakFinderGaussian, _Params, padArray
+
+RUNNING, CONVERGED, ERROR = 0, 1, 2
 
 
 class PeakFitter(object):
@@ -178,3 +185,146 @@ def initFindAndFit(parameters, precision=32):
     elif fmodel == "Z":
         properties += ["xsigma", "ysigma", "z"]
     return PeakFinderFitter(peak_finder=finder, peak_fitter=fitter, properties=properties)
+
+
+class BatchFindFit(object):
+    """PeakFinderFitter.analyzeImage for n_frames frames of one shape at
+    once (Gaussian models, MLE).  Frames that a pass leaves without new
+    peaks are not refitted, as the reference's per-frame loop stops there;
+    the loop ends when every frame is done or after `iterations` passes."""
+
+    def __init__(self, parameters, shape, n_frames, precision=32, max_iterations=2000):
+        import torch
+        self.torch = torch
+        p = _Params(parameters)
+        self.model = p.getAttr("model")
+        self.n_frames = int(n_frames)
+        # the finder's ROI and margin (fitting.py:376-386)
+        roi = p.getAttr("roi_size", -1)
+        if roi == -1:
+            roi = int(8.0 * p.getAttr("sigma"))
+            if self.model != "2dfixed":
+                roi = int(1.5 * roi)
+        self.margin = int(roi / 2 + 2)
+        self.shape = tuple(shape)
+        self.pshape = (self.shape[0] + 2 * self.margin, self.shape[1] + 2 * self.margin)
+        self.finder = BatchPeakFinder(parameters, self.pshape, self.n_frames)
+        sigma = p.getAttr("sigma")
+        kw = dict(roi_size=roi, precision=precision)
+        if self.model in ("2d", "3d"):
+            kw["sigma_range"] = p.getAttr("sigma_range") if p.hasAttr("sigma_range") else [0.5 * sigma, 5.0 * sigma]
+        if self.model == "Z":
+            kw.update(wx_params=p.getAttr("wx_params"), wy_params=p.getAttr("wy_params"),
+                      min_z=p.getAttr("min_z"), max_z=p.getAttr("max_z"))
+        self.fitter = engine.BatchFitter(self.model, self.pshape, self.n_frames, **kw)
+        self.sigma = sigma
+        self.neighborhood = sigma * PeakFinderFitter.unconverged_dist
+        self.threshold = p.getAttr("threshold")
+        self.max_iterations = max_iterations
+        self.d_fit = torch.zeros(self.n_frames * self.pshape[0] * self.pshape[1], dtype=torch.float64,
+                                 device="cuda")
+        self.passes = 0
+
+    def _frames_of(self, a):
+        edges = numpy.concatenate([[0], numpy.cumsum(self.fitter.counts())])
+        return [numpy.ascontiguousarray(a[edges[f]:edges[f + 1]]) for f in range(self.n_frames)], edges
+
+    def analyze(self, frames):
+        """frames: (n_frames, ny, nx) photo-electrons.  Returns one dict of
+        peak properties per frame (x, y without the margin)."""
+        f = self.finder
+        fit = self.fitter
+        padded = numpy.ascontiguousarray(numpy.stack([padArray(im, self.margin) for im in frames]))
+        f.newImages(padded)
+        fit.ensure_frames(1)
+        fit.load_images(padded)
+        self.d_fit.zero_()
+        self.torch.cuda.synchronize()
+        done = numpy.zeros(self.n_frames, dtype=bool)
+        for it in range(f.iterations):
+            self.passes = it + 1
+            first = it == 0
+            f.estimateBackground(None if first else self.d_fit)
+            counting_down = f.cur_threshold > f.threshold
+            counts, _ = f.findPeaks(None if first else self.d_fit)
+            fit.load_backgrounds(self.fitter.clib.saFinderBackgroundDevice(f.fh), on_device=True, dtype_bits=64)
+            active = (counts > 0) & ~done
+            if active.any():
+                self._fit_pass(active, counts)
+            fit.fit_images_device(self.d_fit.data_ptr())
+            if not counting_down:
+                done |= counts == 0
+            if done.all():
+                break
+        fit.remove(RUNNING)
+        props = ["background", "error", "height", "iterations", "significance", "sum", "x", "y", "xsigma",
+                 "ysigma", "status"]
+        vals = {}
+        for pname in props:
+            if pname == "significance":
+                v = fit.prop("fg_sum") / numpy.sqrt(fit.prop("bg_sum"))
+            else:
+                v = fit.prop(pname)
+            vals[pname] = v
+        per, _ = zip(*[self._frames_of(vals[p]) for p in props])
+        out = []
+        for fr in range(self.n_frames):
+            d = {p: per[k][fr] for k, p in enumerate(props)}
+            d["x"] = d["x"] - float(self.margin)
+            d["y"] = d["y"] - float(self.margin)
+            out.append(d)
+        return out
+
+    def _fit_pass(self, active, counts):
+        """PeakFitter.fitPeaks (fitting.py:701-782) for the active frames."""
+        fit = self.fitter
+        nfit = fit.counts()
+        new = self.finder.peaks()
+        if (nfit[active] > 0).any():
+            status = fit.prop("status")
+            xs, edges = self._frames_of(fit.prop("x"))
+            ys, _ = self._frames_of(fit.prop("y"))
+            for fr in numpy.nonzero(active & (nfit > 0))[0]:
+                st = numpy.ascontiguousarray(status[edges[fr]:edges[fr + 1]])
+                iaUtilsC.runningIfHasNeighbors(st, xs[fr], ys[fr], numpy.ascontiguousarray(new[fr]["x"]),
+                                               numpy.ascontiguousarray(new[fr]["y"]), self.neighborhood)
+                status[edges[fr]:edges[fr + 1]] = st
+            fit.set_status(status)
+        # new peaks of inactive frames are not added (counts 0 there)
+        add = numpy.where(active, counts, 0).astype(numpy.int32)
+        fit.reserve(int((nfit + add).max()) + 1)
+        if (add != counts).any():
+            rows = numpy.concatenate([numpy.stack([new[fr]["x"], new[fr]["y"], new[fr]["z"], new[fr]["sigma"]], axis=1)
+                                      for fr in range(self.n_frames) if add[fr] > 0] or [numpy.zeros((0, 4))])
+            self.fitter.clib.saNewPeaksBatch(fit.h, numpy.ascontiguousarray(rows), add, self.n_frames, b"finder")
+        else:
+            fit.load_peaks_device(self.fitter.clib.saFinderPeaksDevice(self.finder.fh), add, "finder")
+        fit.fit_frames(active, self.max_iterations)
+        fit.remove(ERROR)
+        status = fit.prop("status")
+        xs, edges = self._frames_of(fit.prop("x"))
+        ys, _ = self._frames_of(fit.prop("y"))
+        hs, _ = self._frames_of(fit.prop("height"))
+        sig = fit.prop("fg_sum") / numpy.sqrt(fit.prop("bg_sum"))
+        ss, _ = self._frames_of(sig)
+        changed = False
+        for fr in numpy.nonzero(active)[0]:
+            st = numpy.ascontiguousarray(status[edges[fr]:edges[fr + 1]])
+            n_p = iaUtilsC.markDimmerPeaks(xs[fr], ys[fr], hs[fr], st, self.sigma, self.neighborhood)
+            n_s = iaUtilsC.markLowSignificancePeaks(xs[fr], ys[fr], ss[fr], st, self.threshold, self.neighborhood)
+            if n_p + n_s > 0:
+                status[edges[fr]:edges[fr + 1]] = st
+                changed = True
+        if changed:
+            fit.set_status(status)
+            fit.remove(ERROR)
+        status = fit.prop("status")
+        sts, _ = self._frames_of(status)
+        again = numpy.array([active[fr] and bool((sts[fr] == RUNNING).any()) for fr in range(self.n_frames)])
+        if again.any():
+            fit.fit_frames(again, self.max_iterations)
+            fit.remove(ERROR)
+
+    def cleanUp(self):
+        self.finder.cleanUp()
+        self.fitter.close()

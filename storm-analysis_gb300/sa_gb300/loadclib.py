@@ -123,6 +123,9 @@ def _declare(lib):
                        ("saNewBackgrounds", [hp, vp, ci, ci, ci]),
                        ("saNewPeaksBatch", [hp, f64, i32, ci, cs]), ("saDoFitBatch", [hp, ci]),
                        ("saNewPeaksBatchDevice", [hp, vp, i32, ci, cs]),
+                       ("saDoFitBatchFrames", [hp, ci, i32]), ("saSetPeakStatusBatch", [hp, i32]),
+                       ("saRemovePeaksBatch", [hp, ci]), ("saReservePeaksBatch", [hp, ci]),
+                       ("saGetFitImagesDevice", [hp, vp, ci]),
                        ("saGetNFitBatch", [hp, i32]), ("saGetPeakPropertyBatch", [hp, f64, cs]),
                        ("saGetPeakPropertyIntBatch", [hp, i32, cs]), ("saSetTiming", [hp, ci]),
                        ("saGetTiming", [hp, ctypes.POINTER(ctypes.c_double),
@@ -219,6 +222,8 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "saGetLastError", "saClearLastError", "saDeviceCount", "saSetPrecision", "saSetDilation", "saSetStream",
            "saDoFit", "saGetCounters", "saGetSchedStats", "saSetFrames", "saNewImages",
            "saNewBackgrounds", "saNewPeaksBatch", "saNewPeaksBatchDevice", "saDoFitBatch", "saGetNFitBatch",
+           "saDoFitBatchFrames", "saSetPeakStatusBatch", "saRemovePeaksBatch", "saReservePeaksBatch",
+           "saGetFitImagesDevice",
            "saGetPeakPropertyBatch", "saGetPeakPropertyIntBatch", "saSetTiming", "saGetTiming",
            "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice", "saGetSweepTimes",
            "saGetFitImageNoAlloc", "saSlotLoad", "saSlotLaunch", "saSlotPoll", "saSlotReady", "saSlotResults",

@@ -458,3 +458,23 @@ def test_find_fit_loop_matches_oracle():
     d2 = (got["x"][:, None] - ref["x"][None, :]) ** 2 + (got["y"][:, None] - ref["y"][None, :]) ** 2
     near = numpy.sqrt(d2.min(axis=1))
     assert numpy.mean(near < 1e-3) >= 0.99
+
+
+def test_batched_find_fit_loop_matches_oracle():
+    """BatchFindFit (three frames at once, fits and finder state on the GPU
+    across passes) returns, frame by frame, the oracle loop's peaks (FP64
+    engine: same count, positions within 1e-6 px)."""
+    from sa_gb300 import find_peaks, synth
+    from oracle import analysis
+    P = dict(PARAMS, model="3d")
+    wl = synth.make_workload(1, frames=3, nx=128, ny=128, seed=31)
+    frames = numpy.stack(wl["images"])
+    bf = find_peaks.BatchFindFit(P, frames.shape[1:], 3, precision=64)
+    got = bf.analyze(frames)
+    bf.cleanUp()
+    for k in range(3):
+        ref = analysis.analyze_frame(P, frames[k], [0.75, 7.5])
+        assert got[k]["x"].size == ref["x"].size > 50, k
+        assert numpy.abs(got[k]["x"] - ref["x"]).max() < 1e-6
+        assert numpy.abs(got[k]["y"] - ref["y"]).max() < 1e-6
+        assert numpy.abs(got[k]["height"] / ref["height"] - 1.0).max() < 1e-6
