@@ -236,6 +236,10 @@ class BatchFindFit(object):
         fit = self.fitter
         padded = numpy.ascontiguousarray(numpy.stack([padArray(im, self.margin) for im in frames]))
         f.newImages(padded)
+        # a new frame set: drop the previous analysis's peaks (mFitNewImage
+        # starts every frame empty, multi_fit.c:1407)
+        fit._framed = False
+        fit.capacity = None
         fit.ensure_frames(1)
         fit.load_images(padded)
         self.d_fit.zero_()
