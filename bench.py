@@ -786,6 +786,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-finder", action="store_true", help="skip the peak-finder measurement")
     ap.add_argument("--finder-only", action="store_true", help="measure the peak finder alone")
+    ap.add_argument("--loop-only", action="store_true", help="measure the batched find / fit loop alone")
+    ap.add_argument("--size", type=int, default=None, help="frame size for --finder-only / --loop-only")
     ap.add_argument("--cpu-cores", type=int, default=None)
     ap.add_argument("--serving", action="store_true", help="run the serving stream instead")
     ap.add_argument("--requests", type=int, default=200)
@@ -797,13 +799,21 @@ def main():
     args = ap.parse_args()
     from sa_gb300.replicas import rank_env
     rank, world, local_rank = rank_env()
-    if args.finder_only and args.impl == "ours":
+    if args.loop_only and args.impl == "ours":
         if rank == 0:
             import torch
             from sa_gb300 import loadclib, synth
             loadclib.load().saSetDevice(local_rank)
             torch.cuda.set_device(local_rank)
-            wl = synth.make_workload(args.config, frames=args.frames, seed=args.config)
+            wl = synth.make_workload(args.config, frames=args.frames, seed=args.config, nx=args.size, ny=args.size)
+            print(json.dumps(run_analysis_batch(args, wl)), flush=True)
+    elif args.finder_only and args.impl == "ours":
+        if rank == 0:
+            import torch
+            from sa_gb300 import loadclib, synth
+            loadclib.load().saSetDevice(local_rank)
+            torch.cuda.set_device(local_rank)
+            wl = synth.make_workload(args.config, frames=args.frames, seed=args.config, nx=args.size, ny=args.size)
             print(json.dumps(run_finder(args, wl, torch)), flush=True)
     elif args.serving and args.impl == "ours":
         if rank == 0:
