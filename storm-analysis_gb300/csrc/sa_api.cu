@@ -415,7 +415,6 @@ struct Engine {
   int run_until_done(std::vector<FrameCtl>& ctl, int max_sweeps) {
     if (ensure_poll_buffers()) return -1;
     const bool ahead = max_sweeps > 2;
-    burst_ticks = 2;
     if (burst_poll(0)) return -1;
     int cur = 0;
     for (;;) {
@@ -426,15 +425,8 @@ struct Engine {
         return check_err_flag() ? -1 : 0;
       }
       bool active = false;
-      int done_sweeps = 0;
-      for (int f = 0; f < F; f++) {
+      for (int f = 0; f < F; f++)
         if (h_pctl[cur][f].phase != PH_DONE && h_pctl[cur][f].phase != PH_IDLE) active = true;
-        done_sweeps = std::max(done_sweeps, h_pctl[cur][f].sweeps);
-      }
-      // A fit's tail (a few peaks that keep iterating, up to max_sweeps)
-      // runs sweeps of little work; longer bursts there keep the host's
-      // poll off the device's path.  Ticks past the end change nothing.
-      burst_ticks = done_sweeps >= 32 ? 8 : (done_sweeps >= 8 ? 4 : 2);
       if (!active) {
         for (int f = 0; f < F; f++) ctl[f] = h_pctl[cur][f];
         CK(cudaStreamSynchronize(stream));
@@ -482,11 +474,10 @@ struct Engine {
     pctl_n = 0;
   }
 
-  // burst_ticks ticks, then the frame control blocks and the error flag
-  // into pinned buffer b, then its event.
-  int burst_ticks = 2;
+  // Two ticks, then the frame control blocks and the error flag into
+  // pinned buffer b, then its event.
   int burst_poll(int b) {
-    for (int i = 0; i < burst_ticks; i++)
+    for (int i = 0; i < 2; i++)
       if (tick()) return -1;
     CK(cudaMemcpyAsync(h_pctl[b], d_ctl, sizeof(FrameCtl) * F, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(h_perr + b, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
