@@ -451,7 +451,7 @@ __global__ void k_fill_i32(int32_t* __restrict__ p, size_t n, int32_t v) {
     p[i] = v;
 }
 
-// Finder arithmetic of fitting.py:257 and :454-470, in the reference's order:
+// Finder arithmetic of fitting.py:453-457 and :479, in the reference's order:
 // bgv = (background + fit) + camera_variance; fgr = (image - background) - fit.
 __global__ void k_find_prep(const double* __restrict__ image, const double* __restrict__ bg,
                             const double* __restrict__ fit, const double* __restrict__ camvar,
@@ -468,7 +468,7 @@ __global__ void k_find_prep(const double* __restrict__ image, const double* __re
   }
 }
 
-// image - fit, the input of the background filter (fitting.py:268).
+// image - fit, the input of the background filter (fitting.py:265).
 __global__ void k_sub(const double* __restrict__ a, const double* __restrict__ b,
                       double* __restrict__ out, size_t total) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
@@ -476,7 +476,7 @@ __global__ void k_sub(const double* __restrict__ a, const double* __restrict__ b
     out[i] = b ? a[i] - b[i] : a[i];
 }
 
-// masked = (fg / sqrt(bgv <= 0.1 ? 0.1 : bgv)) * mask (fitting.py:476-497).
+// masked = (fg / sqrt(bgv <= 0.1 ? 0.1 : bgv)) * mask (fitting.py:470-497).
 __global__ void k_find_ratio(const double* __restrict__ fg, const double* __restrict__ bgv,
                              const double* __restrict__ mask, double* __restrict__ out, int npix,
                              size_t total) {
