@@ -169,6 +169,15 @@ void saIngestCleanup(void *ih);
  * sigma of the "finder" rows. */
 void *saFinderCreate(int rows, int cols, void *bg_filter, void *fg_filter, void *fv_filter,
                      int margin, double radius, double threshold, double z_value, double sigma);
+/* PeakFinderArbitraryPSF (sa_library/fitting.py:504-672): the finder of
+ * Spliner / pupil-function / PSF-FFT analysis.  Per plane z (n_planes z
+ * values): the foreground filter fg_filters[z] (the PSF at that z) and the
+ * PSF-squared filter fv_filters[z], the variance taking |fit| (:618); the
+ * maxima are searched over all planes (z_range = n_planes) and each peak's
+ * z is z_values of its plane.  Peak rows are (x, y, z, height). */
+void *saFinderCreateArbitrary(int rows, int cols, void *bg_filter, int n_planes, void **fg_filters,
+                              void **fv_filters, const double *z_values, int margin, double radius,
+                              double threshold);
 /* setVariance (fitting.py:353-359): the padded camera variance, host. */
 int saFinderSetVariance(void *fh, const double *camera_variance);
 /* The peak mask (fitting.py:134-176), host; NULL for none. */
@@ -189,7 +198,8 @@ const double *saFinderBackgroundDevice(void *fh);
 const double *saFinderPeaksDevice(void *fh);
 int saFinderGetPeaks(void *fh, double *rows);
 /* Host copy of a per-frame array (all frames): 0 background, 1 the masked
- * foreground / noise ratio of the last saFinderFindPeaks. */
+ * foreground / noise ratio of the last saFinderFindPeaks (all planes of a
+ * frame together). */
 int saFinderGetArray(void *fh, int which, double *out);
 int saFinderSetStream(void *fh, void *stream);
 /* Kernels the finder has launched (its filters' and maxima finder's

@@ -31,6 +31,7 @@ Followed, function by function:
   peak_mask           sa_library/fitting.py:134-176
   PeakFinderGaussian  sa_library/fitting.py:185-501 (newImage,
                       estimateBackground, findPeaks, peakFinder)
+  PeakFinderArbitraryPSF  sa_library/fitting.py:504-672
 
 Pinned by tests/golden/g_finder.npz, made by tests/golden/make_golden_finder.py
 from the reference's own ia_utilities.c and draw_gaussians.c compiled from
@@ -380,3 +381,64 @@ class PeakFinderGaussian:
             self.cur_threshold -= 1.0
             return [new_peaks, "finder", False]
         return [new_peaks, "finder", new_peaks["x"].size == 0]
+
+
+class PeakFinderArbitraryPSF(PeakFinderGaussian):
+    """sa_library/fitting.py:504-672: per z plane a foreground filter (the
+    PSF at that z, unit sum) and its square; the variance takes |fit|; the
+    maxima are searched over all planes."""
+
+    def __init__(self, params, psf_object):
+        self.p = dict(params)
+        self.find_max_radius = self.p["find_max_radius"]
+        self.iterations = self.p["iterations"]
+        self.sigma = self.p["sigma"]
+        self.threshold = self.p["threshold"]
+        self.psf_object = psf_object
+        self.margin = psf_object.getMargin()
+        self.fg_mfilter_zval = [z * 1.0e3 for z in self.p.get("z_value", [0.0])]
+        self.z_values = [psf_object.getScaledZ(z) for z in self.fg_mfilter_zval]
+        self.mfinder = MaximaFinder(self.margin, self.find_max_radius, self.threshold, self.z_values)
+        self.bg_filter = None
+        self.fg_mfilter, self.fg_vfilter = [], []
+        self.camera_variance = None
+        self.peak_mask = None
+        self.background = None
+        self.pf_iterations = 0
+
+    def newImage(self, new_image):
+        self.image = numpy.copy(new_image)
+        if self.iterations > 4:
+            self.cur_threshold = self.threshold + 4.0
+        else:
+            self.cur_threshold = self.threshold + float(self.iterations)
+        if self.peak_mask is None:
+            self.peak_mask = peak_mask(new_image.shape, self.p, self.margin)
+        if self.bg_filter is None:
+            self.bg_filter = MatchedFilter(gaussian_psf(new_image.shape, self.p["background_sigma"]),
+                                           memoize=True, max_diff=1.0e-3)
+        self.mfinder.resetTaken()
+        if not self.fg_mfilter:
+            for zval in self.fg_mfilter_zval:
+                psf = self.psf_object.getPSF(zval, shape=new_image.shape, normalize=False)
+                psf_norm = psf / numpy.sum(psf)
+                self.fg_mfilter.append(MatchedFilter(psf_norm, memoize=True, max_diff=1.0e-3))
+                self.fg_vfilter.append(MatchedFilter(psf_norm * psf_norm, memoize=True, max_diff=1.0e-3))
+
+    def peakFinder(self, fit_peaks_image):
+        bg_var = self.background + numpy.abs(fit_peaks_image)
+        if self.camera_variance is not None:
+            bg_var += self.camera_variance
+        masked = []
+        for fm, fv in zip(self.fg_mfilter, self.fg_vfilter):
+            background = fv.convolve(bg_var)
+            mask = background <= 0.1
+            if numpy.sum(mask) > 0:
+                background[mask] = 0.1
+            bg_std = numpy.sqrt(background)
+            foreground = self.image - self.background - fit_peaks_image
+            foreground = fm.convolve(foreground)
+            masked.append((foreground / bg_std) * self.peak_mask)
+        self.last_masked = masked
+        x, y, z = self.mfinder.findMaxima(masked)
+        return {"x": x, "y": y, "z": z}

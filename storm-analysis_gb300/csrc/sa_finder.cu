@@ -453,15 +453,16 @@ __global__ void k_fill_i32(int32_t* __restrict__ p, size_t n, int32_t v) {
 
 // Finder arithmetic of fitting.py:453-457 and :479, in the reference's order:
 // bgv = (background + fit) + camera_variance; fgr = (image - background) - fit.
+// The arbitrary-PSF finder takes |fit| in the variance (fitting.py:618).
 __global__ void k_find_prep(const double* __restrict__ image, const double* __restrict__ bg,
                             const double* __restrict__ fit, const double* __restrict__ camvar,
                             double* __restrict__ bgv, double* __restrict__ fgr, int npix,
-                            size_t total) {
+                            size_t total, int abs_fit) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     const double b = bg[i];
     const double ft = fit ? fit[i] : 0.0;
-    double v = b + ft;
+    double v = b + (abs_fit ? fabs(ft) : ft);
     if (camvar) v += camvar[i % npix];
     bgv[i] = v;
     fgr[i] = (image[i] - b) - ft;
@@ -477,16 +478,18 @@ __global__ void k_sub(const double* __restrict__ a, const double* __restrict__ b
 }
 
 // masked = (fg / sqrt(bgv <= 0.1 ? 0.1 : bgv)) * mask (fitting.py:470-497).
+// out holds n_planes planes per frame; this call writes plane z.
 __global__ void k_find_ratio(const double* __restrict__ fg, const double* __restrict__ bgv,
                              const double* __restrict__ mask, double* __restrict__ out, int npix,
-                             size_t total) {
+                             size_t total, int z, int n_planes) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     double v = bgv[i];
     if (v <= 0.1) v = 0.1;
     double r = fg[i] / sqrt(v);
     if (mask) r = r * mask[i % npix];
-    out[i] = r;
+    const size_t o = n_planes == 1 ? i : ((i / npix) * n_planes + z) * npix + i % npix;
+    out[o] = r;
   }
 }
 
@@ -1152,7 +1155,10 @@ Maxima* maxima_create(int margin, int z_range, double radius, double threshold, 
 
 struct Finder {
   int R = 0, C = 0, F = 0;
-  MFilter *bg = nullptr, *fm = nullptr, *fv = nullptr;
+  MFilter* bg = nullptr;
+  std::vector<MFilter*> fms, fvs;   // per plane: foreground filter and PSF-squared filter (may be empty)
+  int Z = 1;                        // planes (z values) of the maxima search
+  int abs_fit = 0;                  // |fit| in the variance (arbitrary-PSF finder)
   Maxima* mx = nullptr;
   double sigma = 1.0;
   double* d_image = nullptr;    // F x R x C
@@ -1160,7 +1166,7 @@ struct Finder {
   const double* d_background = nullptr;   // the current background (bg->d_last or d_bgest)
   double* d_a = nullptr;        // F x R x C scratch (bg_var / image - fit)
   double* d_b = nullptr;        // F x R x C scratch (foreground)
-  double* d_ratio = nullptr;    // F x R x C: masked foreground / noise
+  double* d_ratio = nullptr;    // F x Z x R x C: masked foreground / noise per plane
   double* d_fit = nullptr;      // F x R x C staging of a host fit image
   double* d_camvar = nullptr;   // R x C
   double* d_mask = nullptr;     // R x C
@@ -1186,7 +1192,7 @@ int finder_frames(Finder* h, int n) {
   FCK(cudaMalloc(&h->d_image, bytes));
   FCK(cudaMalloc(&h->d_a, bytes));
   FCK(cudaMalloc(&h->d_b, bytes));
-  FCK(cudaMalloc(&h->d_ratio, bytes));
+  FCK(cudaMalloc(&h->d_ratio, bytes * h->Z));
   h->d_background = nullptr;
   h->F = n;
   return 0;
@@ -1775,10 +1781,46 @@ void* saFinderCreate(int rows, int cols, void* bg_filter, void* fg_filter, void*
   h->R = rows;
   h->C = cols;
   h->bg = bg;
-  h->fm = fm;
-  h->fv = fv;
+  if (fm) {
+    h->fms.push_back(fm);
+    h->fvs.push_back(fv);
+  }
   h->mx = mx;
   h->sigma = sigma;
+  return h;
+}
+
+void* saFinderCreateArbitrary(int rows, int cols, void* bg_filter, int n_planes, void** fg_filters,
+                              void** fv_filters, const double* z_values, int margin, double radius,
+                              double threshold) {
+  MFilter* bg = static_cast<MFilter*>(bg_filter);
+  if (rows < 1 || cols < 1 || !bg || n_planes < 1 || !fg_filters || !fv_filters || !z_values) {
+    ferr("saFinderCreateArbitrary: need a background filter and a foreground and PSF-squared filter per plane");
+    return nullptr;
+  }
+  std::vector<MFilter*> fms(n_planes), fvs(n_planes);
+  for (int z = 0; z < n_planes; ++z) {
+    fms[z] = static_cast<MFilter*>(fg_filters[z]);
+    fvs[z] = static_cast<MFilter*>(fv_filters[z]);
+    for (MFilter* m : {fms[z], fvs[z], bg})
+      if (!m || m->R != rows || m->C != cols) {
+        ferr("saFinderCreateArbitrary: filter of plane %d missing or not %d x %d", z, rows, cols);
+        return nullptr;
+      }
+  }
+  // MaximaFinder(margin, radius, threshold, z_values): z_range = n_planes
+  Maxima* mx = maxima_create(margin + 1, n_planes, radius, threshold, z_values, n_planes, 1);
+  if (!mx) return nullptr;
+  Finder* h = new Finder();
+  h->R = rows;
+  h->C = cols;
+  h->bg = bg;
+  h->fms = fms;
+  h->fvs = fvs;
+  h->Z = n_planes;
+  h->abs_fit = 1;
+  h->mx = mx;
+  h->sigma = 0.0;
   return h;
 }
 
@@ -1867,22 +1909,26 @@ int saFinderFindPeaks(void* fh, const double* fit, int on_device, int32_t* count
   const double* f = finder_input(h, fit, on_device, &h->d_fit, n);
   if (fit && !f) return -1;
   k_find_prep<<<grid_for(total), kThreads, 0, h->stream>>>(h->d_image, h->d_background, f, h->d_camvar, h->d_a,
-                                                           h->d_b, npix, total);
+                                                           h->d_b, npix, total, h->abs_fit);
   h->launches += 1;
   FCK(cudaGetLastError());
-  const double* bgv = h->d_a;
-  const double* fg = h->d_b;
-  if (h->fv) {
-    const int64_t l0 = h->fv->launches + h->fm->launches;
-    if (filter_run(h->fv, h->d_a, n, 1, h->stream)) return -1;
-    if (filter_run(h->fm, h->d_b, n, 1, h->stream)) return -1;
-    h->launches += h->fv->launches + h->fm->launches - l0;
-    bgv = h->fv->d_last;
-    fg = h->fm->d_last;
+  for (int z = 0; z < h->Z; ++z) {
+    const double* bgv = h->d_a;
+    const double* fg = h->d_b;
+    if (!h->fvs.empty()) {
+      MFilter* fv = h->fvs[z];
+      MFilter* fm = h->fms[z];
+      const int64_t l0 = fv->launches + fm->launches;
+      if (filter_run(fv, h->d_a, n, 1, h->stream)) return -1;
+      if (filter_run(fm, h->d_b, n, 1, h->stream)) return -1;
+      h->launches += fv->launches + fm->launches - l0;
+      bgv = fv->d_last;
+      fg = fm->d_last;
+    }
+    k_find_ratio<<<grid_for(total), kThreads, 0, h->stream>>>(fg, bgv, h->d_mask, h->d_ratio, npix, total, z, h->Z);
+    h->launches += 1;
+    FCK(cudaGetLastError());
   }
-  k_find_ratio<<<grid_for(total), kThreads, 0, h->stream>>>(fg, bgv, h->d_mask, h->d_ratio, npix, total);
-  h->launches += 1;
-  FCK(cudaGetLastError());
   const int64_t l0 = h->mx->launches;
   const int found = maxima_find(h->mx, h->d_ratio, h->R, h->C, n, counts, h->sigma, h->stream);
   h->launches += h->mx->launches - l0;
@@ -1915,7 +1961,8 @@ int saFinderGetArray(void* fh, int which, double* out) {
     ferr("saFinderGetArray: nothing to return for %d", which);
     return -1;
   }
-  FCK(cudaMemcpyAsync(out, src, sizeof(double) * (size_t)h->R * h->C * h->F, cudaMemcpyDeviceToHost,
+  const size_t planes = which == 1 ? (size_t)h->Z : 1;
+  FCK(cudaMemcpyAsync(out, src, sizeof(double) * (size_t)h->R * h->C * h->F * planes, cudaMemcpyDeviceToHost,
                       h->stream));
   FCK(cudaStreamSynchronize(h->stream));
   return 0;

@@ -353,3 +353,103 @@ class BatchPeakFinder(_FinderCore):
             fitter.load_images(self._images)
         fitter.load_backgrounds(self.clib.saFinderBackgroundDevice(self.fh), on_device=True, dtype_bits=64)
         fitter.load_peaks_device(self.clib.saFinderPeaksDevice(self.fh), self.counts, "finder")
+
+
+class PeakFinderArbitraryPSF(_FinderCore):
+    """The reference's PeakFinderArbitraryPSF (sa_library/fitting.py:504-672),
+    the finder of Spliner / pupil-function / PSF-FFT analysis, on the GPU.
+    psf_object is the reference's PSF object (getMargin, getScaledZ,
+    isValidZ, getPSF(z, shape=..., normalize=False)); parameters may hold
+    z_value, a list of z (um) at which foreground filters are made.  One
+    frame at a time with host arrays; peaks come back as x, y, z."""
+
+    def __init__(self, parameters=None, psf_object=None):
+        self.parameters = _Params(parameters)
+        p = self.parameters
+        self.clib = loadclib.load()
+        self.find_max_radius = p.getAttr("find_max_radius")
+        self.iterations = p.getAttr("iterations")
+        self.sigma = p.getAttr("sigma")
+        self.threshold = p.getAttr("threshold")
+        if p.hasAttr("peak_locations"):
+            raise FittingException("peak_locations files are not read by the GPU finder")
+        self.psf_object = psf_object
+        self.margin = psf_object.getMargin()
+        zv = p.getAttr("z_value", [0.0])
+        self.fg_mfilter_zval = [z * 1.0e3 for z in (zv if numpy.ndim(zv) else [zv])]
+        self.z_values = []
+        for zval in self.fg_mfilter_zval:
+            assert psf_object.isValidZ(zval)
+            self.z_values.append(psf_object.getScaledZ(zval))
+        self.bg_filter = None
+        self.fg_mfilter, self.fg_vfilter = [], []
+        self.camera_variance = None
+        self.peak_mask = None
+        self.fh = None
+        self.pf_iterations = 0
+        self.cur_threshold = None
+        self.shape = None
+
+    def _setup(self, shape):
+        if self.fh is not None:
+            if tuple(shape) != self.shape:
+                raise FittingException("frame shape changed from %s to %s" % (self.shape, tuple(shape)))
+            return
+        self.shape = tuple(shape)
+        p = self.parameters
+        self.peak_mask = peakMask(shape, p.p, self.margin)
+        self.bg_filter = MatchedFilter(gaussianPSF(shape, p.getAttr("background_sigma")), memoize=True,
+                                       max_diff=1.0e-3)
+        for zval in self.fg_mfilter_zval:
+            psf = self.psf_object.getPSF(zval, shape=shape, normalize=False)
+            psf_norm = psf / numpy.sum(psf)
+            self.fg_mfilter.append(MatchedFilter(psf_norm, memoize=True, max_diff=1.0e-3))
+            self.fg_vfilter.append(MatchedFilter(psf_norm * psf_norm, memoize=True, max_diff=1.0e-3))
+        n = len(self.fg_mfilter)
+        fms = (ctypes.c_void_p * n)(*[f.handle() for f in self.fg_mfilter])
+        fvs = (ctypes.c_void_p * n)(*[f.handle() for f in self.fg_vfilter])
+        zv = numpy.ascontiguousarray(self.z_values, dtype=numpy.float64)
+        self.fh = self.clib.saFinderCreateArbitrary(shape[0], shape[1], self.bg_filter.handle(), n, fms, fvs, zv,
+                                                    self.margin, float(self.find_max_radius),
+                                                    float(self.threshold))
+        if not self.fh:
+            raise FittingException(loadclib.last_error())
+        mask = numpy.ascontiguousarray(self.peak_mask, dtype=numpy.float64)
+        if not numpy.all(mask == 1.0):
+            self._ok(self.clib.saFinderSetMask(self.fh, mask.ctypes.data_as(ctypes.c_void_p)))
+        if self.camera_variance is not None:
+            self._upload_variance()
+
+    def cleanUp(self):
+        if self.fh:
+            self.clib.saFinderCleanup(self.fh)
+        self.fh = None
+        for f in [self.bg_filter] + self.fg_mfilter + self.fg_vfilter:
+            if f is not None:
+                f.cleanup()
+        self.bg_filter = None
+        self.fg_mfilter, self.fg_vfilter = [], []
+
+    newImage = PeakFinderGaussian.newImage
+    estimateBackground = PeakFinderGaussian.estimateBackground
+
+    def peakFinder(self, fit_peaks_image):
+        fit, _ = _ptr(fit_peaks_image)
+        counts = numpy.zeros(1, dtype=numpy.int32)
+        n = self._ok(self.clib.saFinderFindPeaks(
+            self.fh, None if fit is None else fit.ctypes.data_as(ctypes.c_void_p), 0, counts))
+        rows = numpy.zeros((max(n, 1), 4))
+        self.clib.saFinderGetPeaks(self.fh, rows)
+        rows = rows[:n]
+        return {"x": numpy.ascontiguousarray(rows[:, 0]), "y": numpy.ascontiguousarray(rows[:, 1]),
+                "z": numpy.ascontiguousarray(rows[:, 2])}
+
+    def findPeaks(self, fit_peaks_image):
+        self.pf_iterations += 1
+        new_peaks = self.peakFinder(fit_peaks_image)
+        return [new_peaks, "finder", self._after_find(new_peaks["x"].size)]
+
+    def significance(self):
+        out = numpy.zeros((len(self.z_values),) + self.shape)
+        self._ok(self.clib.saFinderGetArray(self.fh, 1, out))
+        return out

@@ -191,6 +191,7 @@ def _declare(lib):
             ("saIngestKernelLaunches", [vp], i64r),
             ("saIngestCleanup", [vp], None),
             ("saFinderCreate", [ci, ci, vp, vp, vp, ci, cd, cd, cd, cd], vp),
+            ("saFinderCreateArbitrary", [ci, ci, vp, ci, vp, vp, f64, ci, cd, cd], vp),
             ("saFinderSetVariance", [vp, vp], ci),
             ("saFinderSetMask", [vp, vp], ci),
             ("saFinderNewImages", [vp, vp, ci, ci], ci),
@@ -237,7 +238,7 @@ FINDER_EXPORTS = ["saFilterCreate", "saFilterConvolve", "saFilterConvolveMemo", 
                   "saRunningIfHasNeighbors", "saCreateKDTree", "saFreeKDTree", "saNearestKDTree",
                   "saIngestCreate", "saIngestFrames",
                   "saIngestResultDevice", "saIngestGetFrames", "saIngestSetStream", "saIngestKernelLaunches",
-                  "saIngestCleanup", "saFinderCreate", "saFinderSetVariance",
+                  "saIngestCleanup", "saFinderCreate", "saFinderCreateArbitrary", "saFinderSetVariance",
                   "saFinderSetMask", "saFinderNewImages", "saFinderEstimateBackground",
                   "saFinderFindPeaks", "saFinderBackgroundDevice", "saFinderPeaksDevice",
                   "saFinderGetPeaks", "saFinderGetArray", "saFinderSetStream", "saFinderKernelLaunches",

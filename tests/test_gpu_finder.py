@@ -491,3 +491,62 @@ def test_batched_find_fit_loop_matches_single_frames_and_oracle():
         d2 = (ref["x"][:, None] - got[k]["x"][None, :]) ** 2 + (ref["y"][:, None] - got[k]["y"][None, :]) ** 2
         near = numpy.sqrt(d2.min(axis=1))
         assert numpy.mean(near < 1e-3) >= 0.5 and numpy.mean(near < 0.5) >= 0.9, (k, numpy.mean(near < 1e-3))
+
+
+class RotatedGaussianPSF(object):
+    """A PSF object with the reference's interface (getMargin, isValidZ,
+    getScaledZ, getPSF): an elliptical Gaussian rotated by 30 degrees whose
+    widths change with z, cut to 17 x 17 pixels -- not separable, so the
+    matched filters take the direct 2D path."""
+
+    def getMargin(self):
+        return 10
+
+    def isValidZ(self, z):
+        return -500.0 <= z <= 500.0
+
+    def getScaledZ(self, z):
+        return (z + 500.0) / 100.0
+
+    def getPSF(self, z, shape=None, normalize=False):
+        sx, sy = 1.2 + 0.002 * abs(z), 1.8 - 0.001 * z
+        yy, xx = numpy.mgrid[0:shape[0], 0:shape[1]]
+        dx, dy = xx - 0.5 * shape[1], yy - 0.5 * shape[0]
+        c, s = numpy.cos(numpy.pi / 6), numpy.sin(numpy.pi / 6)
+        u, v = c * dx + s * dy, -s * dx + c * dy
+        psf = numpy.exp(-(u * u / (2 * sx * sx) + v * v / (2 * sy * sy)))
+        psf[(numpy.abs(dx) > 8) | (numpy.abs(dy) > 8)] = 0.0
+        return psf / psf.sum() if normalize else psf
+
+
+def test_arbitrary_psf_finder_matches_oracle():
+    """PeakFinderArbitraryPSF (three z planes, non-separable PSFs, |fit| in
+    the variance, maxima over the planes) returns the oracle's peaks."""
+    from sa_gb300 import fitting, matched_filter_c
+    params = dict(PARAMS, z_value=[-0.2, 0.0, 0.2])
+    params.pop("foreground_sigma")
+    psf = RotatedGaussianPSF()
+    wl = _frames(1, size=128, seed=17)
+    gf = fitting.PeakFinderArbitraryPSF(params, psf)
+    of = F.PeakFinderArbitraryPSF(params, psf)
+    img = gf.padArray(wl["images"][0])
+    fit = [numpy.zeros(img.shape), 0.3 * img - 20.0]
+    total = 0
+    for f in (gf, of):
+        f.newImage(img)
+    for k in range(2):
+        bg_g = gf.estimateBackground(fit[k])
+        bg_o = of.estimateBackground(fit[k])
+        assert conv_close(bg_g, bg_o)
+        pg, tg, dg = gf.findPeaks(fit[k])
+        po, to, do = of.findPeaks(fit[k])
+        assert dg == do
+        for key in ("x", "y", "z"):
+            assert numpy.array_equal(pg[key], po[key]), (k, key)
+        sg = gf.significance()
+        for z in range(3):
+            assert conv_close(sg[z], of.last_masked[z])
+        total += pg["x"].size
+    assert gf.fg_mfilter[0].info()[0] == 0 and total > 10
+    assert set(numpy.unique(pg["z"])) <= set(of.z_values)
+    gf.cleanUp()
