@@ -184,3 +184,15 @@ def test_finder_without_device_fails_loudly(lib):
     lib.saClearLastError()
     assert not lib.saFilterCreate(psf, 0.0, 16, 16, 0)
     assert "saFilterCreate" in loadclib.last_error() or "failed" in loadclib.last_error()
+
+
+def test_find_fit_loop_without_device_fails_loudly(lib):
+    """The find / fit loop and the frame readers need the GPU: without one
+    they raise instead of running anything on the host."""
+    from sa_gb300 import find_peaks, loadclib
+    if lib.saDeviceCount() > 0:
+        pytest.skip("a GPU is visible")
+    params = {"find_max_radius": 5, "iterations": 1, "sigma": 1.5, "threshold": 6.0, "background_sigma": 8.0,
+              "roi_size": 18, "model": "3d"}
+    with pytest.raises(loadclib.EngineUnavailable):
+        find_peaks.initFindAndFit(params)
