@@ -52,6 +52,68 @@ class SplinePSF(object):
     def getMargin(self):
         return int(self.getSize() / 2 + 2)
 
+    def getZMin(self):
+        return self.zmin
+
+    def getZMax(self):
+        return self.zmax
+
+    def isValidZ(self, z):
+        """fitting.py:996-1006: strictly inside the spline's z range (nm)."""
+        return self.zmin < z < self.zmax
+
+    def _f3d(self, z, y, x):
+        """Spline3D.f (spliner/spline3D.py:150-163) for arrays of y, x at
+        one z: cell by floor (the last knot belongs to the last cell),
+        sum of coeff * dx^i dy^j dz^k; 0 outside [0, cells]."""
+        n = self.spline_size
+
+        def cell(v):
+            v = numpy.asarray(v, dtype=numpy.float64)
+            i = numpy.floor(v).astype(numpy.int64)
+            d = v - numpy.floor(v)
+            last = v == n
+            i = numpy.where(last, n - 1, i)
+            d = numpy.where(last, 1.0, d)
+            bad = (v < 0.0) | (v > n)
+            return numpy.clip(i, 0, n - 1), d, bad
+
+        ix, dx, bx = cell(x)
+        iy, dy, by = cell(y)
+        iz, dz, bz = cell(numpy.full(numpy.shape(x), z))
+        c = self.coeff[ix, iy, iz]                       # (..., 64)
+        pw = lambda d: numpy.stack([numpy.ones_like(d), d, d * d, d * d * d], axis=-1)
+        px, py, pz = pw(dx), pw(dy), pw(dz)
+        mono = px[..., :, None, None] * py[..., None, :, None] * pz[..., None, None, :]
+        val = numpy.sum(c * mono.reshape(mono.shape[:-3] + (64,)), axis=-1)
+        return numpy.where(bx | by | bz, 0.0, val)
+
+    def getPSF(self, z_value, shape=None, up_sample=1, normalize=True):
+        """SplineToPSF3D.getPSF (spliner/spline_to_psf.py:162-200) with
+        upsize (:49-73): the spline sampled at pixel centres around the
+        middle, drawn into a `shape` array; z in nm."""
+        assert isinstance(up_sample, int), "up_sample must be an integer."
+        psf_size = up_sample * (self.spline_size - 1)
+        off = 0.5 if psf_size % 2 == 0 else 1.0
+        grid = numpy.arange(psf_size, dtype=numpy.float64) / float(up_sample) + off
+        yy, xx = numpy.meshgrid(grid, grid, indexing="ij")
+        if self.is3d:
+            psf = self._f3d(self.getScaledZ(z_value), yy, xx)
+        else:
+            raise NotImplementedError("getPSF for 2D splines")
+        if shape is not None:
+            im_x, im_y = shape[0] * up_sample, shape[1] * up_sample
+            if psf_size % 2 == 0:
+                sx, sy = int(im_x / 2 - psf_size / 2), int(im_y / 2 - psf_size / 2)
+            else:
+                sx, sy = int(im_x / 2 - psf_size / 2) + 1, int(im_y / 2 - psf_size / 2) + 1
+            big = numpy.zeros((im_x, im_y))
+            big[sx:sx + psf_size, sy:sy + psf_size] = psf
+            psf = big
+        if normalize:
+            psf = psf / numpy.sum(psf)
+        return psf
+
     def getSize(self):
         return self.spline_size
 

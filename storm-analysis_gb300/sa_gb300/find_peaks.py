@@ -90,6 +90,14 @@ class PeakFitter(object):
         return self.mfitter.rescaleZ(z)
 
 
+class PeakFitterArbitraryPSF(PeakFitter):
+    """fitting.py:808-818: the neighbourhood is half the PSF size + 1."""
+
+    def __init__(self, **kwds):
+        super(PeakFitterArbitraryPSF, self).__init__(**kwds)
+        self.neighborhood = int(0.5 * self.mfitter.getSize()) + 1
+
+
 class PeakFinderFitter(object):
     """fitting.py:832-935."""
     unconverged_dist = 5.0
@@ -184,6 +192,32 @@ def initFindAndFit(parameters, precision=32):
         properties += ["xsigma", "ysigma"]
     elif fmodel == "Z":
         properties += ["xsigma", "ysigma", "z"]
+    return PeakFinderFitter(peak_finder=finder, peak_fitter=fitter, properties=properties)
+
+
+def initFindAndFitSpline(parameters, spline_fn=None, precision=32):
+    """Spliner's finder + fitter (spliner/find_peaks_std.py:52-135): the
+    arbitrary-PSF finder with the spline as its PSF object, the cubic spline
+    fitter (MLE), properties with z in microns.  spline_fn defaults to the
+    parameters' "spline" file."""
+    from . import cubic_fit_c
+    from .analysis_io import loadCMOSCalibration
+    from .fitting import PeakFinderArbitraryPSF
+    p = _Params(parameters)
+    if p.getAttr("fit_error_model", "MLE") != "MLE":
+        raise dao_fit_c.MultiFitterException("only the MLE error model is implemented by this engine")
+    if spline_fn is None:
+        spline_fn = cubic_fit_c.SplinePSF(spline_data=p.getAttr("spline"))
+    finder = PeakFinderArbitraryPSF(parameters=parameters, psf_object=spline_fn)
+    rqe = variance = None
+    if p.hasAttr("camera_calibration"):
+        [offset, variance, gain, rqe] = loadCMOSCalibration(p.getAttr("camera_calibration"))
+        variance = finder.setVariance(variance / (gain * gain))
+        rqe = finder.padArray(rqe)
+    cls = cubic_fit_c.CSpline3DFit if spline_fn.getType() == "3D" else cubic_fit_c.CSpline2DFit
+    mfitter = cls(spline_fn=spline_fn, rqe=rqe, scmos_cal=variance, precision=precision)
+    fitter = PeakFitterArbitraryPSF(mfitter=mfitter, parameters=parameters)
+    properties = ["background", "error", "height", "iterations", "significance", "sum", "x", "y", "z"]
     return PeakFinderFitter(peak_finder=finder, peak_fitter=fitter, properties=properties)
 
 

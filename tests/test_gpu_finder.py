@@ -550,3 +550,29 @@ def test_arbitrary_psf_finder_matches_oracle():
     assert gf.fg_mfilter[0].info()[0] == 0 and total > 10
     assert set(numpy.unique(pg["z"])) <= set(of.z_values)
     gf.cleanUp()
+
+
+def test_spliner_find_fit_loop_matches_oracle():
+    """Spliner's whole frame analysis (arbitrary-PSF finder on three z
+    planes of the spline PSF, cubic spline fitter, culling with the PSF-size
+    neighbourhood) on the GPU against the oracle's loop: same peak count
+    within 2 and 90 % of the peaks within 1e-4 px (x, y) and 1e-3 (z)."""
+    from sa_gb300 import cubic_fit_c, find_peaks, synth
+    from oracle import analysis
+    wl = synth.make_workload(3, frames=1, nx=128, ny=128, seed=5, n_emitters=60)
+    sp = wl["spline"]
+    spline = cubic_fit_c.SplinePSF(coeff=sp["coeff"], zmin=synth.SPLINE_ZMIN_NM, zmax=synth.SPLINE_ZMAX_NM)
+    P = dict(background_sigma=8.0, find_max_radius=5, iterations=20, sigma=1.5, threshold=6.0,
+             z_value=[-0.2, 0.0, 0.2])
+    ref = analysis.analyze_frame(P, wl["images"][0], None, psf_object=spline, spline=sp["coeff"])
+    ff = find_peaks.initFindAndFitSpline(P, spline_fn=spline, precision=64)
+    got = ff.analyzeFrame(wl["images"][0])
+    ff.peak_fitter.mfitter.cleanup(verbose=False)
+    ff.peak_finder.cleanUp()
+    assert ref["x"].size > 40 and abs(got["x"].size - ref["x"].size) <= 2
+    d2 = (ref["x"][:, None] - got["x"][None, :]) ** 2 + (ref["y"][:, None] - got["y"][None, :]) ** 2
+    j = d2.argmin(axis=1)
+    near = numpy.sqrt(d2[numpy.arange(ref["x"].size), j])
+    zr = numpy.array([spline.rescaleZ(z) for z in ref["z"]])
+    ok = (near < 1e-4) & (numpy.abs(got["z"][j] - zr) < 1e-3)
+    assert numpy.mean(ok) >= 0.9

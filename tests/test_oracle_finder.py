@@ -116,3 +116,40 @@ def test_culling_matches_reference_exactly(g):
         assert numpy.array_equal(d, g["cull%d_nearest_d" % i]) and numpy.array_equal(ix, g["cull%d_nearest_i" % i])
         i += 1
     assert i == 3
+
+
+def test_spline_psf_matches_spline3d_evaluation():
+    """SplinePSF.getPSF (the PSF object Spliner's finder draws its filters
+    from) samples the spline as Spline3D.f does (spliner/spline3D.py:150-163,
+    spliner/spline1D.py:12-28), restated point by point here."""
+    import math
+    from sa_gb300 import cubic_fit_c, synth
+    sp = synth.make_spline(3)
+    S = cubic_fit_c.SplinePSF(coeff=sp["coeff"], zmin=synth.SPLINE_ZMIN_NM, zmax=synth.SPLINE_ZMAX_NM)
+    n = S.getSize()
+
+    def rc(v):
+        if v < 0 or v > n:
+            return -1, -1.0
+        fl = math.floor(v)
+        i, d = int(fl), v - fl
+        if v == n:
+            i, d = i - 1, 1.0
+        return i, d
+
+    def f(z, y, x):
+        (ix, dx), (iy, dy), (iz, dz) = rc(x), rc(y), rc(z)
+        if -1 in (ix, iy, iz):
+            return 0.0
+        return sum(S.coeff[ix, iy, iz, i * 16 + j * 4 + k] * dx ** i * dy ** j * dz ** k
+                   for i in range(4) for j in range(4) for k in range(4))
+
+    for zval in (-300.0, 0.0, 250.0):
+        psf = S.getPSF(zval, normalize=False)
+        sz = S.getScaledZ(zval)
+        off = 0.5 if (n - 1) % 2 == 0 else 1.0
+        ref = numpy.array([[f(sz, y + off, x + off) for x in range(n - 1)] for y in range(n - 1)])
+        assert numpy.abs(psf - ref).max() <= 1e-12 * numpy.abs(ref).max()
+    big = S.getPSF(0.0, shape=(64, 64), normalize=True)
+    assert big.shape == (64, 64) and abs(big.sum() - 1.0) < 1e-12
+    assert S.isValidZ(0.0) and not S.isValidZ(S.getZMax())
