@@ -37,6 +37,12 @@ extern "C" {
  * true of every Gaussian the finder draws), else as a 2D sum over the PSF's
  * support (at most about 60 x 60 pixels).  Returns NULL on failure. */
 void *saFilterCreate(const double *psf, double max_diff, int x_size, int y_size, int estimate);
+/* No reference counterpart; host only, no device needed: how saFilterCreate
+ * will convolve with this recentred PSF.  out5 = [separable, taps along
+ * rows (na), taps along cols (nb), first row offset (a0), first col offset
+ * (b0)]; when separable, u (na) and v (nb), if not NULL, receive the 1D taps
+ * with psf[(a0 + i) mod x_size][(b0 + j) mod y_size] = u[i] * v[j]. */
+int saFilterAnalyze(const double *psf, int x_size, int y_size, int32_t *out5, double *u, double *v);
 /* matched_filter.c:93 convolve: result = image (*) psf, circular. */
 int saFilterConvolve(void *flt, const double *image, double *result);
 /* matched_filter.c:118 convolveMemo: as convolve when some pixel differs

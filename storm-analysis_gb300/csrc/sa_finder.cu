@@ -849,17 +849,17 @@ int filter_run(MFilter* m, const double* d_in, int n, int memo, cudaStream_t s) 
   return 0;
 }
 
-MFilter* filter_create(const double* psf, double max_diff, int R, int C) {
-  if (!psf || R < 1 || C < 1) {
-    ferr("saFilterCreate: bad arguments (psf %p, %d x %d)", (const void*)psf, R, C);
-    return nullptr;
-  }
-  MFilter* m = new MFilter();
-  m->R = R;
-  m->C = C;
-  m->max_diff = max_diff > 0.0 ? max_diff : 0.0;
-  m->h_rc.assign(psf, psf + (size_t)R * C);
-  const std::vector<double>& p = m->h_rc;
+// Host analysis of a recentred PSF (R x C): the smallest circular support
+// along each axis (offsets a0 .. a0 + na - 1 along rows, b0 .. b0 + nb - 1
+// along columns) and whether the PSF is rank 1 to 1e-12 of its maximum
+// (then psf[a][b] = u[a - a0] * v[b - b0], from its pivot row and column).
+struct PsfTaps {
+  int a0 = 0, na = 1, b0 = 0, nb = 1, separable = 1;
+  std::vector<double> u, v;
+};
+
+PsfTaps analyze_psf(const std::vector<double>& p, int R, int C) {
+  PsfTaps t;
   std::vector<char> rnz(R, 0), cnz(C, 0);
   double pmax = 0.0;
   int pr = 0, pc = 0;
@@ -885,14 +885,39 @@ MFilter* filter_create(const double* psf, double max_diff, int R, int C) {
   }
   auto at = [&](int a, int b) { return p[(size_t)(((a % R) + R) % R) * C + ((b % C) + C) % C]; };
   // rank-1 test against the pivot row and column
-  std::vector<double> u(na), v(nb);
+  t.u.assign(na, 0.0);
+  t.v.assign(nb, 0.0);
   const double piv = at(pr, pc);
-  for (int i = 0; i < na; ++i) u[i] = at(a0 + i, pc);
-  for (int j = 0; j < nb; ++j) v[j] = piv != 0.0 ? at(pr, b0 + j) / piv : 0.0;
+  for (int i = 0; i < na; ++i) t.u[i] = at(a0 + i, pc);
+  for (int j = 0; j < nb; ++j) t.v[j] = piv != 0.0 ? at(pr, b0 + j) / piv : 0.0;
   double resid = 0.0;
   for (int i = 0; i < na; ++i)
-    for (int j = 0; j < nb; ++j) resid = std::max(resid, std::fabs(at(a0 + i, b0 + j) - u[i] * v[j]));
-  m->separable = resid <= 1e-12 * pmax;
+    for (int j = 0; j < nb; ++j) resid = std::max(resid, std::fabs(at(a0 + i, b0 + j) - t.u[i] * t.v[j]));
+  t.separable = resid <= 1e-12 * pmax;
+  t.a0 = a0;
+  t.na = na;
+  t.b0 = b0;
+  t.nb = nb;
+  return t;
+}
+
+MFilter* filter_create(const double* psf, double max_diff, int R, int C) {
+  if (!psf || R < 1 || C < 1) {
+    ferr("saFilterCreate: bad arguments (psf %p, %d x %d)", (const void*)psf, R, C);
+    return nullptr;
+  }
+  MFilter* m = new MFilter();
+  m->R = R;
+  m->C = C;
+  m->max_diff = max_diff > 0.0 ? max_diff : 0.0;
+  m->h_rc.assign(psf, psf + (size_t)R * C);
+  const std::vector<double>& p = m->h_rc;
+  const PsfTaps taps = analyze_psf(p, R, C);
+  const std::vector<double>& u = taps.u;
+  const std::vector<double>& v = taps.v;
+  const int a0 = taps.a0, na = taps.na, b0 = taps.b0, nb = taps.nb;
+  auto at = [&](int a, int b) { return p[(size_t)(((a % R) + R) % R) * C + ((b % C) + C) % C]; };
+  m->separable = taps.separable;
   m->a0 = a0;
   m->na = na;
   m->b0 = b0;
@@ -1324,6 +1349,23 @@ void ingest_free(Ingest* h) {
 // ===========================================================================
 
 extern "C" {
+
+int saFilterAnalyze(const double* psf, int x_size, int y_size, int32_t* out5, double* u, double* v) {
+  if (!psf || !out5 || x_size < 1 || y_size < 1) {
+    ferr("saFilterAnalyze: bad arguments");
+    return -1;
+  }
+  const std::vector<double> p(psf, psf + (size_t)x_size * y_size);
+  const PsfTaps t = analyze_psf(p, x_size, y_size);
+  out5[0] = t.separable;
+  out5[1] = t.na;
+  out5[2] = t.nb;
+  out5[3] = t.a0;
+  out5[4] = t.b0;
+  if (u) std::copy(t.u.begin(), t.u.end(), u);
+  if (v) std::copy(t.v.begin(), t.v.end(), v);
+  return 0;
+}
 
 void* saFilterCreate(const double* psf, double max_diff, int x_size, int y_size, int estimate) {
   (void)estimate;

@@ -160,6 +160,7 @@ def _declare(lib):
     i64r = ctypes.c_int64
     for name, args, res in [
             ("saFilterCreate", [f64, cd, ci, ci, ci], vp),
+            ("saFilterAnalyze", [f64, ci, ci, i32, vp, vp], ci),
             ("saFilterConvolve", [vp, f64, f64], ci),
             ("saFilterConvolveMemo", [vp, f64, f64], ci),
             ("saFilterCleanup", [vp], None),
@@ -230,7 +231,7 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "saGetFitImageNoAlloc", "saSlotLoad", "saSlotLaunch", "saSlotPoll", "saSlotReady", "saSlotResults",
            "saSetSweepCTAs"]
 
-FINDER_EXPORTS = ["saFilterCreate", "saFilterConvolve", "saFilterConvolveMemo", "saFilterCleanup",
+FINDER_EXPORTS = ["saFilterCreate", "saFilterAnalyze", "saFilterConvolve", "saFilterConvolveMemo", "saFilterCleanup",
                   "saFilterConvolveDevice", "saFilterResultDevice", "saFilterInfo", "saFilterSetStream",
                   "saCalcMaxPeaks", "saFindLocalMaxima", "saMaximaCreate", "saMaximaFind",
                   "saMaximaPeaksDevice", "saMaximaGetPeaks", "saMaximaResetTaken", "saMaximaGetTaken",
