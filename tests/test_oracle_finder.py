@@ -153,3 +153,46 @@ def test_spline_psf_matches_spline3d_evaluation():
     big = S.getPSF(0.0, shape=(64, 64), normalize=True)
     assert big.shape == (64, 64) and abs(big.sum() - 1.0) < 1e-12
     assert S.isValidZ(0.0) and not S.isValidZ(S.getZMax())
+
+
+def _two_phase(x, y, status, marked, r_neighbors):
+    """The GPU kernels' formulation (k_mark_* then k_mark_apply): marked
+    peaks become ERROR; a CONVERGED peak within r_neighbors of a marked one
+    becomes RUNNING; every peak decided from the statuses on entry."""
+    out = status.copy()
+    out[marked] = F.ERROR
+    for i in numpy.nonzero(~marked & (status == F.CONVERGED))[0]:
+        nb = F._within(x, y, x[i], y[i], r_neighbors)
+        if marked[nb].any():
+            out[i] = F.RUNNING
+    return out
+
+
+def test_culling_does_not_depend_on_visiting_order():
+    """The parallel culling rests on this: in the reference's sequential
+    loops (ia_utilities.c:221-340) a peak's mark depends only on its own
+    height / significance and its status on entry, so marking all peaks
+    first and applying after gives the sequential result."""
+    rng = numpy.random.default_rng(21)
+    for trial in range(40):
+        n = int(rng.integers(5, 400))
+        centres = rng.uniform(5, 60, (max(n // 3, 1), 2))
+        pts = numpy.concatenate([centres + rng.normal(0, 0.9, centres.shape) for _ in range(3)])[:n]
+        x, y = numpy.ascontiguousarray(pts[:, 0]), numpy.ascontiguousarray(pts[:, 1])
+        n = x.size
+        h = rng.uniform(100, 1000, n)
+        h[rng.integers(0, n, n // 10)] = 500.0          # exact height ties
+        sig = rng.uniform(0, 12, n)
+        st = rng.choice([0, 1, 1, 1, 2], n).astype(numpy.int32)
+        r1, r2 = rng.uniform(0.5, 2.0), rng.uniform(2.0, 8.0)
+        s_seq = st.copy()
+        n_seq = F.mark_dimmer_peaks(x, y, h, s_seq, r1, r2)
+        marked = numpy.array([st[i] != F.ERROR and (h[F._within(x, y, x[i], y[i], r1)] > h[i]).any()
+                              for i in range(n)])
+        assert marked.sum() == n_seq
+        assert numpy.array_equal(_two_phase(x, y, st, marked, r2), s_seq)
+        s_seq = st.copy()
+        n_seq = F.mark_low_significance_peaks(x, y, sig, s_seq, 6.0, r2)
+        marked = (st != F.ERROR) & ~(sig > 6.0)
+        assert marked.sum() == n_seq
+        assert numpy.array_equal(_two_phase(x, y, st, marked, r2), s_seq)
