@@ -21,7 +21,7 @@ def analyze_frame(params, frame, sigma_range, model="3d", max_iterations=2000, p
     """Found and fitted peaks of one frame (x, y without the margin).  With
     psf_object and spline (the coefficients) the frame is analysed as
     Spliner does: the arbitrary-PSF finder, the cubic spline fitter and the
-    neighbourhood int(spline size / 2) + 1 (fitting.py:808-818)."""
+    neighbourhood int(spline size / 2) + 1 (fitting.py:826-834)."""
     sigma = params["sigma"]
     if psf_object is not None:
         finder = F.PeakFinderArbitraryPSF(params, psf_object)

@@ -131,6 +131,12 @@ class BatchFitter(object):
                                                         ctypes.c_char_p(peaks_type.encode())),
                         "saNewPeaksBatchDevice")
 
+    def reset(self):
+        """Start over: the next load re-creates the frame set, dropping every
+        frame's peaks (as mFitNewImage starts a frame empty)."""
+        self._framed = False
+        self.capacity = None
+
     def reserve(self, capacity_per_frame):
         """Grow each frame's peak storage, keeping its peaks."""
         if not self._framed:

@@ -22,7 +22,7 @@ RUNNING, CONVERGED, ERROR = 0, 1, 2
 
 
 class PeakFitter(object):
-    """fitting.py:674-806."""
+    """fitting.py:674-823."""
 
     def __init__(self, mfitter=None, parameters=None, **kwds):
         super(PeakFitter, self).__init__(**kwds)
@@ -91,7 +91,7 @@ class PeakFitter(object):
 
 
 class PeakFitterArbitraryPSF(PeakFitter):
-    """fitting.py:808-818: the neighbourhood is half the PSF size + 1."""
+    """fitting.py:826-834: the neighbourhood is half the PSF size + 1."""
 
     def __init__(self, **kwds):
         super(PeakFitterArbitraryPSF, self).__init__(**kwds)
@@ -99,7 +99,7 @@ class PeakFitterArbitraryPSF(PeakFitter):
 
 
 class PeakFinderFitter(object):
-    """fitting.py:832-935."""
+    """fitting.py:837-935."""
     unconverged_dist = 5.0
 
     def __init__(self, peak_finder=None, peak_fitter=None, properties=None, **kwds):
@@ -272,8 +272,7 @@ class BatchFindFit(object):
         f.newImages(padded)
         # a new frame set: drop the previous analysis's peaks (mFitNewImage
         # starts every frame empty, multi_fit.c:1407)
-        fit._framed = False
-        fit.capacity = None
+        fit.reset()
         fit.ensure_frames(1)
         fit.load_images(padded)
         self.d_fit.zero_()
