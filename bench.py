@@ -644,6 +644,26 @@ def run_analysis(args, wl):
     return out
 
 
+def _loop_worker(frame):
+    """One frame through the oracle's find / fit loop (CPU baseline)."""
+    from oracle import analysis
+    t0 = time.perf_counter()
+    r = analysis.analyze_frame(dict(FINDER_PARAMS, model="3d"), frame, [0.75, 7.5])
+    return int(r["x"].size), time.perf_counter() - t0
+
+
+def loop_cpu_sample(frames, cores):
+    """The oracle's loop on min(cores, frames) frames, one process per core
+    (spawned: this process already holds a CUDA context)."""
+    n = min(cores, len(frames))
+    ctx = multiprocessing.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(n) as pool:
+        res = pool.map(_loop_worker, [numpy.ascontiguousarray(frames[i]) for i in range(n)])
+    wall = time.perf_counter() - t0
+    return n, sum(r[0] for r in res), wall
+
+
 def run_analysis_batch(args, wl):
     """The same find / fit loop for all of the step's frames at once
     (sa_gb300.find_peaks.BatchFindFit): finder and fits stay on the GPU
@@ -660,12 +680,19 @@ def run_analysis_batch(args, wl):
     passes = bf.passes
     bf.cleanUp()
     n = sum(r["x"].size for r in res)
-    return {"metric": "frames/s (find / fit loop, all frames batched)", "value": frames.shape[0] / wall,
+    out = {"metric": "frames/s (find / fit loop, all frames batched)", "value": frames.shape[0] / wall,
             "unit": "frames/s", "frames": int(frames.shape[0]), "localizations": int(n),
             "localizations_per_s": n / wall, "passes": passes, "wall_s": wall,
             "note": "each doFit runs up to 2000 sweeps as the reference's does; a few oscillating "
                     "peaks keep every fit to that limit, and a sweep of a handful of peaks costs "
                     "~0.24 ms (the latency of one LM step), so the fits' tails set this number"}
+    if not args.no_cpu:
+        cores = args.cpu_cores or os.cpu_count()
+        nf, nloc, w = loop_cpu_sample(frames, cores)
+        out["cpu_baseline"] = {"value": nf / w, "unit": "frames/s", "cores": nf, "kind": "port",
+                               "sample": "%d frames through the oracle's loop, one process per core, %.1f s "
+                                         "wall (%d localizations)" % (nf, w, nloc)}
+    return out
 
 
 def run_reference(args, rank, world):
