@@ -1,7 +1,8 @@
 """
-Reader of the Zhuang lab .dax movie format, as the reference's DaxReader
-(sa_library/datareader.py:156-243): the .inf side file gives the frame
-size, frame count and byte order; frames are uint16.
+Reader of the Zhuang lab .dax movie format (the reference's DaxReader,
+sa_library/datareader.py:156-243, is the reader this replaces): the .inf
+side file gives the frame size, frame count and byte order; frames are
+uint16.
 
 loadAFrame returns one frame in native byte order, as the reference does.
 loadRaw returns consecutive frames exactly as stored (no byte swap), for
@@ -13,38 +14,40 @@ import re
 import numpy
 
 
+def read_inf(inf_filename):
+    """The fields of a .inf side file as a dict of stripped strings: one
+    "key = value" pair per line (lines without " = " are skipped)."""
+    fields = {}
+    with open(inf_filename, "r") as inf:
+        for line in inf:
+            key, sep, value = line.partition(" = ")
+            if sep:
+                fields[key.strip()] = value.strip()
+    return fields
+
+
+_DIMS = re.compile(r"^\s*(\d+)\s*x\s*(\d+)\s*$")
+
+
 class DaxReader(object):
+    """A .dax movie: frames of uint16 pixels, row-major, in the byte order
+    the .inf file names ("... big endian" or "... little endian" in its
+    data type; little endian when it names none).  The .inf's "frame
+    dimensions = W x H" gives the width W (pixels per row) and height H, and
+    "number of frames" the length."""
 
     def __init__(self, filename, verbose=False):
         self.filename = filename
         self.verbose = verbose
-        dirname = os.path.dirname(filename)
-        if len(dirname) > 0:
-            dirname = dirname + "/"
-        self.inf_filename = dirname + os.path.splitext(os.path.basename(filename))[0] + ".inf"
-        self.image_height = None
-        self.image_width = None
-        self.number_frames = 0
-        self.bigendian = 0
-        size_re = re.compile(r'frame dimensions = ([\d]+) x ([\d]+)')
-        length_re = re.compile(r'number of frames = ([\d]+)')
-        endian_re = re.compile(r' (big|little) endian')
-        with open(self.inf_filename, "r") as inf:
-            for line in inf:
-                m = size_re.match(line)
-                if m:
-                    self.image_height = int(m.group(2))
-                    self.image_width = int(m.group(1))
-                m = length_re.match(line)
-                if m:
-                    self.number_frames = int(m.group(1))
-                m = endian_re.search(line)
-                if m:
-                    self.bigendian = 1 if m.group(1) == "big" else 0
-        if not self.image_height:
-            print("Could not determine image size, assuming 256x256.")
-            self.image_height = 256
-            self.image_width = 256
+        self.inf_filename = os.path.splitext(filename)[0] + ".inf"
+        fields = read_inf(self.inf_filename)
+        dims = _DIMS.match(fields.get("frame dimensions", ""))
+        if dims is None:
+            raise IOError("%s: no 'frame dimensions = W x H' line" % self.inf_filename)
+        self.image_width, self.image_height = int(dims.group(1)), int(dims.group(2))
+        self.number_frames = int(fields.get("number of frames", "0"))
+        order = " ".join(fields.values())
+        self.bigendian = 1 if "big endian" in order else 0
         self.fileptr = open(filename, "rb") if os.path.exists(filename) else None
 
     def close(self):

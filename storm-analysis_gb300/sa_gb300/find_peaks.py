@@ -1,16 +1,33 @@
 """
-The find / fit loop of 3D-DAOSTORM and sCMOS analysis on the GPU: the
-reference's PeakFitter, PeakFinderFitter (sa_library/fitting.py:674-935)
-and initFindAndFit (daostorm_3d/find_peaks.py:16-135) over this package's
-GPU finder (fitting.PeakFinderGaussian), culling (ia_utilities_c) and
-fitter (dao_fit_c).  Same control flow as the reference: per frame, up to
-`iterations` passes of background estimate -> new peaks -> fit -> culling,
-then the unconverged peaks are removed.
+The find / fit loop of 3D-DAOSTORM, sCMOS and Spliner analysis, over this
+package's GPU finder (fitting.PeakFinderGaussian / PeakFinderArbitraryPSF /
+BatchPeakFinder), culling (ia_utilities_c) and fitter (dao_fit_c,
+cubic_fit_c, engine.BatchFitter).
 
-BatchFindFit runs the same loop for n frames at once: frames, backgrounds,
-new peaks, fit images and the fits stay on the GPU across passes, the fits
-of all frames run in one batched sweep loop, and only the per-frame peak
+Design.  A frame's analysis is a sequence of finder passes; each pass that
+found new peaks runs one *fit pass* over the frame's fitted peaks.  The fit
+pass is written once (`fit_pass`) for a set of frames and a mask of the
+frames it applies to, over a small "frame set" interface:
+
+    FitterFrames   one MultiFitter per frame (the reference's one-frame
+                   objects: dao_fit_c / cubic_fit_c, or anything with the
+                   same methods);
+    BatchFrames    one engine.BatchFitter holding every frame on the GPU.
+
+`FindFitLoop` drives host-side finders and a FitterFrames set; with one
+frame it is the reference's per-frame analysis (initFindAndFit(...)
+.analyzeImage / analyzeFrame, the entry points std_analysis calls,
+sa_utilities/std_analysis.py:84-105).  `BatchFindFit` drives the batched
+finder and a BatchFrames set: frames, backgrounds, new peaks, fit images
+and peak records stay on the GPU across passes, and only the per-frame peak
 lists that the culling reads travel to the host.
+
+What a fit pass does (the reference's PeakFitter.fitPeaks,
+sa_library/fitting.py:701-782, whose order decides the results): peaks near
+a new peak go back to RUNNING; the new peaks are added; the frame is fitted
+and its ERROR peaks dropped; dimmer neighbours and low-significance peaks are
+marked ERROR and dropped; a frame that still has RUNNING peaks is fitted
+again.
 """
 import numpy
 
@@ -20,212 +37,366 @@ from .fitting import BatchPeakFinder, PeakFinderGaussian, _Params, padArray
 
 RUNNING, CONVERGED, ERROR = 0, 1, 2
 
+# Radius of "near a new peak", in units of the PSF sigma (fitting.py:839).
+UNCONVERGED_DIST = 5.0
 
-class PeakFitter(object):
-    """fitting.py:674-823."""
 
-    def __init__(self, mfitter=None, parameters=None, **kwds):
-        super(PeakFitter, self).__init__(**kwds)
-        parameters = _Params(parameters)
-        self.no_fitting = parameters.getAttr("no_fitting", 0)
+class GpuCulling(object):
+    """The three culling steps of a fit pass on the GPU (ia_utilities_c).
+    Each works on one frame's arrays; statuses are edited in place."""
+
+    @staticmethod
+    def wake(status, x, y, new_x, new_y, radius):
+        return iaUtilsC.runningIfHasNeighbors(status, x, y, numpy.ascontiguousarray(new_x),
+                                              numpy.ascontiguousarray(new_y), radius)
+
+    @staticmethod
+    def dimmer(x, y, height, status, sigma, radius):
+        return iaUtilsC.markDimmerPeaks(x, y, height, status, sigma, radius)
+
+    @staticmethod
+    def faint(x, y, significance, status, threshold, radius):
+        return iaUtilsC.markLowSignificancePeaks(x, y, significance, status, threshold, radius)
+
+
+# ---------------------------------------------------------------------------
+# frame sets
+# ---------------------------------------------------------------------------
+
+class FitterFrames(object):
+    """A frame set of MultiFitter objects, one per frame."""
+
+    def __init__(self, fitters, max_iterations=2000):
+        self.fitters = list(fitters)
+        self.max_iterations = max_iterations
+
+    def __len__(self):
+        return len(self.fitters)
+
+    def nfit(self):
+        return numpy.array([f.getNFit() for f in self.fitters])
+
+    def column(self, k, name):
+        return self.fitters[k].getPeakProperty(name)
+
+    def set_status(self, statuses, frames):
+        for k in frames:
+            self.fitters[k].setPeakStatus(statuses[k])
+
+    def add(self, new_peaks, peaks_type, frames):
+        for k in frames:
+            self.fitters[k].newPeaks(new_peaks[k], peaks_type)
+
+    def fit(self, frames):
+        for k in frames:
+            self.fitters[k].doFit(self.max_iterations)
+
+    def drop(self, status, frames):
+        for k in frames:
+            if status == ERROR:
+                self.fitters[k].removeErrorPeaks()
+            else:
+                self.fitters[k].removeRunningPeaks()
+
+    def running(self, frames):
+        return [k for k in frames if self.fitters[k].getUnconverged() > 0]
+
+    def count_culled(self, k, n_dimmer, n_faint):
+        f = self.fitters[k]
+        if hasattr(f, "incProximityCounter"):
+            f.incProximityCounter(n_dimmer)
+            f.incSignificanceCounter(n_faint)
+
+
+class BatchFrames(object):
+    """A frame set that is one engine.BatchFitter: per-frame columns are
+    slices of the batch's property arrays (read once per pass and name)."""
+
+    def __init__(self, fitter, max_iterations=2000):
+        self.fitter = fitter
+        self.max_iterations = max_iterations
+        self._cache = {}
+
+    def __len__(self):
+        return self.fitter.n_frames
+
+    def _invalidate(self):
+        self._cache = {}
+
+    def nfit(self):
+        if "_n" not in self._cache:
+            self._cache["_n"] = self.fitter.counts()
+        return self._cache["_n"]
+
+    def _edges(self):
+        return numpy.concatenate([[0], numpy.cumsum(self.nfit())])
+
+    def _all(self, name):
+        if name not in self._cache:
+            if name == "significance":
+                v = self.fitter.prop("fg_sum") / numpy.sqrt(self.fitter.prop("bg_sum"))
+            else:
+                v = self.fitter.prop(name)
+            self._cache[name] = v
+        return self._cache[name]
+
+    def column(self, k, name):
+        e = self._edges()
+        return numpy.ascontiguousarray(self._all(name)[e[k]:e[k + 1]])
+
+    def set_status(self, statuses, frames):
+        full = self._all("status").copy()
+        e = self._edges()
+        for k in frames:
+            full[e[k]:e[k + 1]] = statuses[k]
+        self.fitter.set_status(full)
+        self._invalidate()
+
+    def add(self, new_peaks, peaks_type, frames, device_rows=None):
+        counts = numpy.zeros(len(self), dtype=numpy.int32)
+        for k in frames:
+            counts[k] = new_peaks[k]["x"].size
+        self.fitter.reserve(int((self.nfit() + counts).max()) + 1)
+        if device_rows is not None:
+            # every frame's finder rows are used: the device hand-off
+            self.fitter.load_peaks_device(device_rows, counts, peaks_type)
+        else:
+            rows = [numpy.stack([new_peaks[k][c] for c in ("x", "y", "z", "sigma")], axis=1)
+                    for k in range(len(self)) if counts[k] > 0]
+            rows = numpy.ascontiguousarray(numpy.concatenate(rows) if rows else numpy.zeros((0, 4)))
+            self.fitter.clib.saNewPeaksBatch(self.fitter.h, rows, counts, len(self), peaks_type.encode())
+        self._invalidate()
+
+    def fit(self, frames):
+        mask = numpy.zeros(len(self), dtype=bool)
+        mask[list(frames)] = True
+        self.fitter.fit_frames(mask, self.max_iterations)
+        self._invalidate()
+
+    def drop(self, status, frames):
+        # ERROR / RUNNING peaks only exist in the frames being worked on
+        self.fitter.remove(status)
+        self._invalidate()
+
+    def running(self, frames):
+        st = self._all("status")
+        e = self._edges()
+        return [k for k in frames if (st[e[k]:e[k + 1]] == RUNNING).any()]
+
+    def count_culled(self, k, n_dimmer, n_faint):
+        pass
+
+
+# ---------------------------------------------------------------------------
+# one fit pass over a set of frames
+# ---------------------------------------------------------------------------
+
+def fit_pass(fs, frames, new_peaks, peaks_type, sigma, threshold, neighborhood, culling=GpuCulling,
+             fitting=True, add_kw=None):
+    """One pass of PeakFitter.fitPeaks (sa_library/fitting.py:701-782) for
+    the frames listed in `frames`, each of which has new peaks
+    (new_peaks[k], a dict of x, y, ...).  fs is a frame set."""
+    frames = [int(k) for k in frames]
+    if not frames:
+        return
+    nfit = fs.nfit()
+    # 1. a fitted peak near a new one must be refitted
+    woken = [k for k in frames if nfit[k] > 0]
+    if woken:
+        st = {}
+        for k in woken:
+            s = numpy.ascontiguousarray(fs.column(k, "status"), dtype=numpy.int32)
+            st[k] = culling.wake(s, fs.column(k, "x"), fs.column(k, "y"), new_peaks[k]["x"], new_peaks[k]["y"],
+                                 neighborhood)
+        fs.set_status(st, woken)
+    # 2. add and fit
+    fs.add(new_peaks, peaks_type, frames, **(add_kw or {}))
+    if fitting:
+        fs.fit(frames)
+        fs.drop(ERROR, frames)
+    # 3. culling: dimmer neighbours, then low significance
+    culled, st = [], {}
+    for k in frames:
+        s = numpy.ascontiguousarray(fs.column(k, "status"), dtype=numpy.int32)
+        x, y = fs.column(k, "x"), fs.column(k, "y")
+        n_dim = culling.dimmer(x, y, fs.column(k, "height"), s, sigma, neighborhood)
+        n_sig = culling.faint(x, y, fs.column(k, "significance"), s, threshold, neighborhood)
+        if n_dim + n_sig > 0:
+            st[k] = s
+            culled.append(k)
+            fs.count_culled(k, n_dim, n_sig)
+    if culled:
+        fs.set_status(st, culled)
+        fs.drop(ERROR, culled)
+    # 4. refit the frames whose culling left peaks RUNNING
+    if fitting:
+        again = fs.running(frames)
+        if again:
+            fs.fit(again)
+            fs.drop(ERROR, again)
+
+
+# ---------------------------------------------------------------------------
+# host-driven loop (the reference's per-frame analysis)
+# ---------------------------------------------------------------------------
+
+class FindFitLoop(object):
+    """Find / fit analysis of frames one at a time with a host-side finder
+    and a MultiFitter (PeakFinderFitter.analyzeImage, fitting.py:867-935).
+
+    finder      PeakFinderGaussian / PeakFinderArbitraryPSF (or an object
+                with their methods)
+    mfitter     the frame's MultiFitter
+    properties  the peak properties analyzeImage returns
+    neighborhood  radius (pixels) of the culling's neighbour queries
+    """
+
+    def __init__(self, finder, mfitter, properties, neighborhood, sigma, threshold, no_fitting=False,
+                 culling=GpuCulling):
+        assert "x" in properties and "y" in properties, "'x' and 'y' are required properties."
+        self.peak_finder = finder
         self.mfitter = mfitter
-        self.minimum_significance = parameters.getAttr("threshold")
-        self.sigma = parameters.getAttr("sigma")
-        self.neighborhood = self.sigma * PeakFinderFitter.unconverged_dist
-
-    def cleanUp(self):
-        self.mfitter.cleanup()
-
-    def fitPeaks(self, new_peaks, peaks_type):
-        """One fitting pass; returns the current fit image."""
-        if new_peaks["x"].size > 0:
-            if self.mfitter.getNFit() > 0:
-                c_x = self.mfitter.getPeakProperty("x")
-                c_y = self.mfitter.getPeakProperty("y")
-                status = self.mfitter.getPeakProperty("status")
-                new_status = iaUtilsC.runningIfHasNeighbors(status, c_x, c_y,
-                                                            numpy.ascontiguousarray(new_peaks["x"]),
-                                                            numpy.ascontiguousarray(new_peaks["y"]),
-                                                            self.neighborhood)
-                self.mfitter.setPeakStatus(new_status)
-            self.mfitter.newPeaks(new_peaks, peaks_type)
-            if not self.no_fitting:
-                self.mfitter.doFit()
-                self.mfitter.removeErrorPeaks()
-            status = self.mfitter.getPeakProperty("status")
-            px = self.mfitter.getPeakProperty("x")
-            py = self.mfitter.getPeakProperty("y")
-            n_proximity = iaUtilsC.markDimmerPeaks(px, py, self.mfitter.getPeakProperty("height"), status,
-                                                   self.sigma, self.neighborhood)
-            n_significance = iaUtilsC.markLowSignificancePeaks(px, py,
-                                                               self.mfitter.getPeakProperty("significance"),
-                                                               status, self.minimum_significance,
-                                                               self.neighborhood)
-            if (n_proximity + n_significance) > 0:
-                self.mfitter.setPeakStatus(status)
-                self.mfitter.removeErrorPeaks()
-                self.mfitter.incProximityCounter(n_proximity)
-                self.mfitter.incSignificanceCounter(n_significance)
-            if (self.mfitter.getUnconverged() > 0) and (not self.no_fitting):
-                self.mfitter.doFit()
-                self.mfitter.removeErrorPeaks()
-        return self.mfitter.getFitImage()
-
-    def getPeakProperty(self, pname):
-        return self.mfitter.getPeakProperty(pname)
-
-    def newBackground(self, new_background):
-        self.mfitter.newBackground(new_background)
-
-    def newImage(self, new_image):
-        if not self.mfitter.isInitialized():
-            self.mfitter.initializeC(new_image)
-        self.mfitter.newImage(new_image)
-
-    def removeRunningPeaks(self):
-        if not self.no_fitting:
-            self.mfitter.removeRunningPeaks()
-
-    def rescaleZ(self, z):
-        return self.mfitter.rescaleZ(z)
-
-
-class PeakFitterArbitraryPSF(PeakFitter):
-    """fitting.py:826-834: the neighbourhood is half the PSF size + 1."""
-
-    def __init__(self, **kwds):
-        super(PeakFitterArbitraryPSF, self).__init__(**kwds)
-        self.neighborhood = int(0.5 * self.mfitter.getSize()) + 1
-
-
-class PeakFinderFitter(object):
-    """fitting.py:837-935."""
-    unconverged_dist = 5.0
-
-    def __init__(self, peak_finder=None, peak_fitter=None, properties=None, **kwds):
-        super(PeakFinderFitter, self).__init__(**kwds)
-        self.peak_finder = peak_finder
-        self.peak_fitter = peak_fitter
-        self.properties = properties
-        assert ("x" in self.properties), "'x' is a required property."
-        assert ("y" in self.properties), "'y' is a required property."
+        self.properties = list(properties)
+        self.neighborhood = neighborhood
+        self.sigma = sigma
+        self.threshold = threshold
+        self.no_fitting = bool(no_fitting)
+        self.culling = culling
+        self.frames = FitterFrames([mfitter])
 
     def analyzeImage(self, movie_reader):
-        """As the reference: movie_reader.getFrame() (photo-electrons) and
-        movie_reader.getBackground() (an estimate or None)."""
-        bg = movie_reader.getBackground()
-        return self.analyzeFrame(movie_reader.getFrame(), bg)
+        """movie_reader.getFrame() (photo-electrons) and getBackground()."""
+        return self.analyzeFrame(movie_reader.getFrame(), movie_reader.getBackground())
 
     def analyzeFrame(self, frame, bg_estimate=None):
-        image = padArray(frame, self.peak_finder.margin)
-        fit_peaks_image = numpy.zeros(image.shape)
+        margin = self.peak_finder.margin
+        image = padArray(frame, margin)
         if bg_estimate is not None:
-            bg_estimate = padArray(bg_estimate, self.peak_finder.margin)
+            bg_estimate = padArray(bg_estimate, margin)
+        if not self.mfitter.isInitialized():
+            self.mfitter.initializeC(image)
         self.peak_finder.newImage(image)
-        self.peak_fitter.newImage(image)
-        for i in range(self.peak_finder.iterations):
-            background = self.peak_finder.estimateBackground(fit_peaks_image, bg_estimate)
-            [new_peaks, peaks_type, done] = self.peak_finder.findPeaks(fit_peaks_image)
-            self.peak_fitter.newBackground(background)
-            fit_peaks_image = self.peak_fitter.fitPeaks(new_peaks, peaks_type)
+        self.mfitter.newImage(image)
+        fit_image = numpy.zeros(image.shape)
+        for _ in range(self.peak_finder.iterations):
+            background = self.peak_finder.estimateBackground(fit_image, bg_estimate)
+            new_peaks, peaks_type, done = self.peak_finder.findPeaks(fit_image)
+            self.mfitter.newBackground(background)
+            if new_peaks["x"].size > 0:
+                fit_pass(self.frames, [0], [new_peaks], peaks_type, self.sigma, self.threshold,
+                         self.neighborhood, culling=self.culling, fitting=not self.no_fitting)
+            fit_image = self.mfitter.getFitImage()
             if done:
                 break
-        self.peak_fitter.removeRunningPeaks()
+        if not self.no_fitting:
+            self.mfitter.removeRunningPeaks()
         return self.getPeakProperties()
 
-    def cleanUp(self):
-        self.peak_finder.cleanUp()
-        self.peak_fitter.cleanUp()
-
     def getPeakProperties(self):
-        peaks = {}
-        for pname in self.properties:
-            peaks[pname] = self.peak_fitter.getPeakProperty(pname)
-            if pname in ("x", "y"):
-                peaks[pname] -= float(self.peak_finder.margin)
-            elif pname == "z":
-                peaks[pname] = self.peak_fitter.rescaleZ(peaks[pname])
-        return peaks
+        out = {}
+        margin = float(self.peak_finder.margin)
+        for name in self.properties:
+            v = self.mfitter.getPeakProperty(name)
+            if name in ("x", "y"):
+                v = v - margin
+            elif name == "z":
+                v = self.mfitter.rescaleZ(v)
+            out[name] = v
+        return out
+
+    def cleanUp(self, verbose=False):
+        self.peak_finder.cleanUp()
+        self.mfitter.cleanup(verbose=verbose)
+
+
+def _camera(finder, parameters):
+    """sCMOS calibration of the analysis, padded like the frames: (rqe,
+    variance / gain^2) or (None, None) (daostorm_3d/find_peaks.py:31-40)."""
+    from .analysis_io import loadCMOSCalibration
+    p = _Params(parameters)
+    if not p.hasAttr("camera_calibration"):
+        return None, None
+    offset, variance, gain, rqe = loadCMOSCalibration(p.getAttr("camera_calibration"))
+    variance = finder.setVariance(variance / (gain * gain))
+    return finder.padArray(rqe), variance
+
+
+_GAUSSIAN_FITTERS = {"2dfixed": dao_fit_c.MultiFitter2DFixed, "2d": dao_fit_c.MultiFitter2D,
+                     "3d": dao_fit_c.MultiFitter3D, "Z": dao_fit_c.MultiFitterZ}
+
+_GAUSSIAN_PROPS = {"2dfixed": ["xsigma"], "2d": ["xsigma"], "3d": ["xsigma", "ysigma"],
+                   "Z": ["xsigma", "ysigma", "z"]}
+
+
+def _check_mle(p):
+    if p.getAttr("fit_error_model", "MLE") != "MLE":
+        raise dao_fit_c.MultiFitterException("only the MLE error model is implemented by this engine")
+
+
+def _sigma_range(p):
+    if p.hasAttr("sigma_range"):
+        return p.getAttr("sigma_range")
+    s = p.getAttr("sigma")
+    return [0.5 * s, 5.0 * s]
 
 
 def initFindAndFit(parameters, precision=32):
-    """Finder + fitter for the MLE Gaussian models ('2dfixed', '2d', '3d';
-    'Z' takes wx_params / wy_params / min_z / max_z from the parameters).
-    A sCMOS camera_calibration file sets the camera variance and RQE as in
-    daostorm_3d/find_peaks.py:31-40."""
-    from .analysis_io import loadCMOSCalibration
+    """3D-DAOSTORM / sCMOS analysis of one frame at a time
+    (daostorm_3d/find_peaks.py:16-135): the Gaussian finder and the MLE
+    Gaussian fitter of the parameters' model ('2dfixed', '2d', '3d', 'Z';
+    'Z' reads wx_params / wy_params / min_z / max_z)."""
     p = _Params(parameters)
-    fmodel = p.getAttr("model")
-    emodel = p.getAttr("fit_error_model", "MLE")
-    if emodel != "MLE":
-        raise dao_fit_c.MultiFitterException("only the MLE error model is implemented by this engine")
+    _check_mle(p)
+    model = p.getAttr("model")
+    if model not in _GAUSSIAN_FITTERS:
+        raise dao_fit_c.MultiFitterException("unknown model '%s'" % model)
     finder = PeakFinderGaussian(parameters)
-    rqe = variance = None
-    if p.hasAttr("camera_calibration"):
-        [offset, variance, gain, rqe] = loadCMOSCalibration(p.getAttr("camera_calibration"))
-        variance = variance / (gain * gain)
-        variance = finder.setVariance(variance)
-        rqe = finder.padArray(rqe)
-    kwds = {"roi_size": finder.getROISize(), "rqe": rqe, "scmos_cal": variance, "precision": precision}
-    if fmodel in ("2d", "3d"):
-        if p.hasAttr("sigma_range"):
-            kwds["sigma_range"] = p.getAttr("sigma_range")
-        else:
-            sigma = p.getAttr("sigma")
-            kwds["sigma_range"] = [0.5 * sigma, 5.0 * sigma]
-    if fmodel == "2dfixed":
-        mfitter = dao_fit_c.MultiFitter2DFixed(**kwds)
-    elif fmodel == "2d":
-        mfitter = dao_fit_c.MultiFitter2D(**kwds)
-    elif fmodel == "3d":
-        mfitter = dao_fit_c.MultiFitter3D(**kwds)
-    elif fmodel == "Z":
-        mfitter = dao_fit_c.MultiFitterZ(wx_params=p.getAttr("wx_params"), wy_params=p.getAttr("wy_params"),
-                                         min_z=p.getAttr("min_z"), max_z=p.getAttr("max_z"), **kwds)
-    else:
-        raise dao_fit_c.MultiFitterException("unknown model '%s'" % fmodel)
-    fitter = PeakFitter(mfitter=mfitter, parameters=parameters)
-    properties = ["background", "error", "height", "iterations", "significance", "sum", "x", "y"]
-    if fmodel in ("2dfixed", "2d"):
-        properties.append("xsigma")
-    elif fmodel == "3d":
-        properties += ["xsigma", "ysigma"]
-    elif fmodel == "Z":
-        properties += ["xsigma", "ysigma", "z"]
-    return PeakFinderFitter(peak_finder=finder, peak_fitter=fitter, properties=properties)
+    rqe, variance = _camera(finder, parameters)
+    kw = dict(roi_size=finder.getROISize(), rqe=rqe, scmos_cal=variance, precision=precision)
+    if model in ("2d", "3d"):
+        kw["sigma_range"] = _sigma_range(p)
+    if model == "Z":
+        kw.update(wx_params=p.getAttr("wx_params"), wy_params=p.getAttr("wy_params"), min_z=p.getAttr("min_z"),
+                  max_z=p.getAttr("max_z"))
+    mfitter = _GAUSSIAN_FITTERS[model](**kw)
+    props = ["background", "error", "height", "iterations", "significance", "sum", "x", "y"] + _GAUSSIAN_PROPS[model]
+    sigma = p.getAttr("sigma")
+    return FindFitLoop(finder, mfitter, props, sigma * UNCONVERGED_DIST, sigma, p.getAttr("threshold"),
+                       no_fitting=p.getAttr("no_fitting", 0))
 
 
 def initFindAndFitSpline(parameters, spline_fn=None, precision=32):
-    """Spliner's finder + fitter (spliner/find_peaks_std.py:52-135): the
-    arbitrary-PSF finder with the spline as its PSF object, the cubic spline
-    fitter (MLE), properties with z in microns.  spline_fn defaults to the
-    parameters' "spline" file."""
+    """Spliner's analysis (spliner/find_peaks_std.py:52-135): the
+    arbitrary-PSF finder with the spline as its PSF object and the cubic
+    spline fitter (MLE); z comes back in microns.  The culling's neighbour
+    radius is half the spline's size plus one pixel (fitting.py:826-834).
+    spline_fn defaults to the parameters' "spline" file."""
     from . import cubic_fit_c
-    from .analysis_io import loadCMOSCalibration
     from .fitting import PeakFinderArbitraryPSF
     p = _Params(parameters)
-    if p.getAttr("fit_error_model", "MLE") != "MLE":
-        raise dao_fit_c.MultiFitterException("only the MLE error model is implemented by this engine")
+    _check_mle(p)
     if spline_fn is None:
         spline_fn = cubic_fit_c.SplinePSF(spline_data=p.getAttr("spline"))
     finder = PeakFinderArbitraryPSF(parameters=parameters, psf_object=spline_fn)
-    rqe = variance = None
-    if p.hasAttr("camera_calibration"):
-        [offset, variance, gain, rqe] = loadCMOSCalibration(p.getAttr("camera_calibration"))
-        variance = finder.setVariance(variance / (gain * gain))
-        rqe = finder.padArray(rqe)
+    rqe, variance = _camera(finder, parameters)
     cls = cubic_fit_c.CSpline3DFit if spline_fn.getType() == "3D" else cubic_fit_c.CSpline2DFit
     mfitter = cls(spline_fn=spline_fn, rqe=rqe, scmos_cal=variance, precision=precision)
-    fitter = PeakFitterArbitraryPSF(mfitter=mfitter, parameters=parameters)
-    properties = ["background", "error", "height", "iterations", "significance", "sum", "x", "y", "z"]
-    return PeakFinderFitter(peak_finder=finder, peak_fitter=fitter, properties=properties)
+    props = ["background", "error", "height", "iterations", "significance", "sum", "x", "y", "z"]
+    return FindFitLoop(finder, mfitter, props, int(0.5 * mfitter.getSize()) + 1, p.getAttr("sigma"),
+                       p.getAttr("threshold"), no_fitting=p.getAttr("no_fitting", 0))
 
+
+# ---------------------------------------------------------------------------
+# batched loop: n frames at once, state on the GPU
+# ---------------------------------------------------------------------------
 
 class BatchFindFit(object):
-    """PeakFinderFitter.analyzeImage for n_frames frames of one shape at
-    once (Gaussian models, MLE).  Frames that a pass leaves without new
-    peaks are not refitted, as the reference's per-frame loop stops there;
-    the loop ends when every frame is done or after `iterations` passes."""
+    """FindFitLoop.analyzeFrame for n_frames frames of one shape at once
+    (Gaussian models, MLE).  All frames advance pass by pass together: a
+    frame whose pass found no new peaks is not refitted (the per-frame loop
+    skips the fit pass there), and a frame that is done keeps taking finder
+    passes, which change nothing, until every frame is done or after
+    `iterations` passes."""
 
     def __init__(self, parameters, shape, n_frames, precision=32, max_iterations=2000):
         import torch
@@ -233,7 +404,7 @@ class BatchFindFit(object):
         p = _Params(parameters)
         self.model = p.getAttr("model")
         self.n_frames = int(n_frames)
-        # the finder's ROI and margin (fitting.py:376-386)
+        # the finder's ROI decides the margin (fitting.py:376-386)
         roi = p.getAttr("roi_size", -1)
         if roi == -1:
             roi = int(8.0 * p.getAttr("sigma"))
@@ -243,35 +414,28 @@ class BatchFindFit(object):
         self.shape = tuple(shape)
         self.pshape = (self.shape[0] + 2 * self.margin, self.shape[1] + 2 * self.margin)
         self.finder = BatchPeakFinder(parameters, self.pshape, self.n_frames)
-        sigma = p.getAttr("sigma")
         kw = dict(roi_size=roi, precision=precision)
         if self.model in ("2d", "3d"):
-            kw["sigma_range"] = p.getAttr("sigma_range") if p.hasAttr("sigma_range") else [0.5 * sigma, 5.0 * sigma]
+            kw["sigma_range"] = _sigma_range(p)
         if self.model == "Z":
             kw.update(wx_params=p.getAttr("wx_params"), wy_params=p.getAttr("wy_params"),
                       min_z=p.getAttr("min_z"), max_z=p.getAttr("max_z"))
         self.fitter = engine.BatchFitter(self.model, self.pshape, self.n_frames, **kw)
-        self.sigma = sigma
-        self.neighborhood = sigma * PeakFinderFitter.unconverged_dist
+        self.frames = BatchFrames(self.fitter, max_iterations)
+        self.sigma = p.getAttr("sigma")
+        self.neighborhood = self.sigma * UNCONVERGED_DIST
         self.threshold = p.getAttr("threshold")
-        self.max_iterations = max_iterations
         self.d_fit = torch.zeros(self.n_frames * self.pshape[0] * self.pshape[1], dtype=torch.float64,
                                  device="cuda")
         self.passes = 0
 
-    def _frames_of(self, a):
-        edges = numpy.concatenate([[0], numpy.cumsum(self.fitter.counts())])
-        return [numpy.ascontiguousarray(a[edges[f]:edges[f + 1]]) for f in range(self.n_frames)], edges
-
     def analyze(self, frames):
         """frames: (n_frames, ny, nx) photo-electrons.  Returns one dict of
         peak properties per frame (x, y without the margin)."""
-        f = self.finder
-        fit = self.fitter
+        f, fit = self.finder, self.fitter
         padded = numpy.ascontiguousarray(numpy.stack([padArray(im, self.margin) for im in frames]))
         f.newImages(padded)
-        # a new frame set: drop the previous analysis's peaks (mFitNewImage
-        # starts every frame empty, multi_fit.c:1407)
+        # a new frame set: every frame starts empty (mFitNewImage, multi_fit.c:1407)
         fit.reset()
         fit.ensure_frames(1)
         fit.load_images(padded)
@@ -280,87 +444,35 @@ class BatchFindFit(object):
         done = numpy.zeros(self.n_frames, dtype=bool)
         for it in range(f.iterations):
             self.passes = it + 1
-            first = it == 0
-            f.estimateBackground(None if first else self.d_fit)
+            fit_images = None if it == 0 else self.d_fit
+            f.estimateBackground(fit_images)
             counting_down = f.cur_threshold > f.threshold
-            counts, _ = f.findPeaks(None if first else self.d_fit)
+            counts, _ = f.findPeaks(fit_images)
             fit.load_backgrounds(self.fitter.clib.saFinderBackgroundDevice(f.fh), on_device=True, dtype_bits=64)
-            active = (counts > 0) & ~done
-            if active.any():
-                self._fit_pass(active, counts)
+            active = numpy.nonzero((counts > 0) & ~done)[0]
+            if active.size:
+                new = f.peaks()
+                # rows of frames that are done stay on the host path (they are skipped)
+                every = active.size == int((counts > 0).sum())
+                add_kw = {"device_rows": self.fitter.clib.saFinderPeaksDevice(f.fh)} if every else None
+                fit_pass(self.frames, active, new, "finder", self.sigma, self.threshold, self.neighborhood,
+                         add_kw=add_kw)
             fit.fit_images_device(self.d_fit.data_ptr())
             if not counting_down:
                 done |= counts == 0
             if done.all():
                 break
         fit.remove(RUNNING)
+        self.frames._invalidate()
         props = ["background", "error", "height", "iterations", "significance", "sum", "x", "y", "xsigma",
                  "ysigma", "status"]
-        vals = {}
-        for pname in props:
-            if pname == "significance":
-                v = fit.prop("fg_sum") / numpy.sqrt(fit.prop("bg_sum"))
-            else:
-                v = fit.prop(pname)
-            vals[pname] = v
-        per, _ = zip(*[self._frames_of(vals[p]) for p in props])
         out = []
-        for fr in range(self.n_frames):
-            d = {p: per[k][fr] for k, p in enumerate(props)}
+        for k in range(self.n_frames):
+            d = {name: self.frames.column(k, name) for name in props}
             d["x"] = d["x"] - float(self.margin)
             d["y"] = d["y"] - float(self.margin)
             out.append(d)
         return out
-
-    def _fit_pass(self, active, counts):
-        """PeakFitter.fitPeaks (fitting.py:701-782) for the active frames."""
-        fit = self.fitter
-        nfit = fit.counts()
-        new = self.finder.peaks()
-        if (nfit[active] > 0).any():
-            status = fit.prop("status")
-            xs, edges = self._frames_of(fit.prop("x"))
-            ys, _ = self._frames_of(fit.prop("y"))
-            for fr in numpy.nonzero(active & (nfit > 0))[0]:
-                st = numpy.ascontiguousarray(status[edges[fr]:edges[fr + 1]])
-                iaUtilsC.runningIfHasNeighbors(st, xs[fr], ys[fr], numpy.ascontiguousarray(new[fr]["x"]),
-                                               numpy.ascontiguousarray(new[fr]["y"]), self.neighborhood)
-                status[edges[fr]:edges[fr + 1]] = st
-            fit.set_status(status)
-        # new peaks of inactive frames are not added (counts 0 there)
-        add = numpy.where(active, counts, 0).astype(numpy.int32)
-        fit.reserve(int((nfit + add).max()) + 1)
-        if (add != counts).any():
-            rows = numpy.concatenate([numpy.stack([new[fr]["x"], new[fr]["y"], new[fr]["z"], new[fr]["sigma"]], axis=1)
-                                      for fr in range(self.n_frames) if add[fr] > 0] or [numpy.zeros((0, 4))])
-            self.fitter.clib.saNewPeaksBatch(fit.h, numpy.ascontiguousarray(rows), add, self.n_frames, b"finder")
-        else:
-            fit.load_peaks_device(self.fitter.clib.saFinderPeaksDevice(self.finder.fh), add, "finder")
-        fit.fit_frames(active, self.max_iterations)
-        fit.remove(ERROR)
-        status = fit.prop("status")
-        xs, edges = self._frames_of(fit.prop("x"))
-        ys, _ = self._frames_of(fit.prop("y"))
-        hs, _ = self._frames_of(fit.prop("height"))
-        sig = fit.prop("fg_sum") / numpy.sqrt(fit.prop("bg_sum"))
-        ss, _ = self._frames_of(sig)
-        changed = False
-        for fr in numpy.nonzero(active)[0]:
-            st = numpy.ascontiguousarray(status[edges[fr]:edges[fr + 1]])
-            n_p = iaUtilsC.markDimmerPeaks(xs[fr], ys[fr], hs[fr], st, self.sigma, self.neighborhood)
-            n_s = iaUtilsC.markLowSignificancePeaks(xs[fr], ys[fr], ss[fr], st, self.threshold, self.neighborhood)
-            if n_p + n_s > 0:
-                status[edges[fr]:edges[fr + 1]] = st
-                changed = True
-        if changed:
-            fit.set_status(status)
-            fit.remove(ERROR)
-        status = fit.prop("status")
-        sts, _ = self._frames_of(status)
-        again = numpy.array([active[fr] and bool((sts[fr] == RUNNING).any()) for fr in range(self.n_frames)])
-        if again.any():
-            fit.fit_frames(again, self.max_iterations)
-            fit.remove(ERROR)
 
     def cleanUp(self):
         self.finder.cleanUp()

@@ -9,8 +9,9 @@ include/sa_finder.h).  BatchPeakFinder does the same for n frames of one
 size at once with the frames, backgrounds and found peaks resident on the
 GPU, and hands them to a BatchFitter without a host round trip.
 
-gaussianPSF, padArray and peakMask restate sa_library/fitting.py:38-46,
-:112-132 and :134-176 (host-side set-up).
+gaussianPSF, padArray and peakMask give the finder's host-side set-up
+(the filters' PSF, the mirror padding and the area-of-interest mask of
+sa_library/fitting.py:38-46, :112-132 and :134-176).
 """
 import ctypes
 
@@ -63,50 +64,55 @@ def gaussianPSF(shape, sigma):
 
 
 def padArray(ori_array, pad_size):
-    """Mirror padding by pad_size pixels on every side."""
+    """The frame with pad_size pixels of mirror padding on every side, as
+    float64: the border pixel is repeated (numpy's "symmetric" mode), which
+    is the padding the reference's finder and fitter see
+    (sa_library/fitting.py:112-132).  pad_size must not exceed the frame's
+    size; pad_size <= 0 returns the frame unchanged."""
     if pad_size <= 0:
         return ori_array
-    xs, ys = ori_array.shape
-    lg = numpy.ones((xs + 2 * pad_size, ys + 2 * pad_size))
-    lg[pad_size:xs + pad_size, pad_size:ys + pad_size] = ori_array.astype(numpy.float64)
-    lg[0:pad_size, :] = numpy.flipud(lg[pad_size:2 * pad_size, :])
-    lg[xs + pad_size:xs + 2 * pad_size, :] = numpy.flipud(lg[xs:xs + pad_size, :])
-    lg[:, 0:pad_size] = numpy.fliplr(lg[:, pad_size:2 * pad_size])
-    lg[:, ys + pad_size:ys + 2 * pad_size] = numpy.fliplr(lg[:, ys:ys + pad_size])
-    return lg
+    return numpy.pad(numpy.asarray(ori_array, dtype=numpy.float64), int(pad_size), mode="symmetric")
+
+
+_AOI_CIRCLE = ("x_center", "y_center", "aoi_radius")
 
 
 def peakMask(shape, parameters, margin):
-    """The AOI mask: a circle (x_center, y_center, aoi_radius) or the
-    x_start / x_stop / y_start / y_stop box, with the reference's indexing
-    (its circle uses shape[0] on both axes; its stops end at -1)."""
-    parameters = _Params(parameters)
-    peak_mask = numpy.ones(shape)
-    if parameters.hasAttr("x_center"):
-        assert parameters.hasAttr("y_center"), "Y center must be specified."
-        assert parameters.hasAttr("aoi_radius"), "AOI radius must be specified."
-        rr = parameters.getAttr("aoi_radius")
-        xc = parameters.getAttr("x_center") + margin
-        yc = parameters.getAttr("y_center") + margin
-        rr = rr * rr
-        xr = numpy.arange(peak_mask.shape[0]) - xc
-        yr = numpy.arange(peak_mask.shape[0]) - yc
-        xv, yv = numpy.meshgrid(xr, yr)
-        peak_mask[((xv * xv + yv * yv) > rr)] = 0
-    elif parameters.hasAttr("y_center"):
-        assert parameters.hasAttr("x_center"), "X center must be specified."
-    elif parameters.hasAttr("aoi_radius"):
-        assert parameters.hasAttr("x_center"), "X center must be specified."
-    else:
-        if parameters.hasAttr("x_start"):
-            peak_mask[:, 0:parameters.getAttr("x_start") + margin] = 0.0
-        if parameters.hasAttr("x_stop"):
-            peak_mask[:, parameters.getAttr("x_stop") + margin:-1] = 0.0
-        if parameters.hasAttr("y_start"):
-            peak_mask[0:parameters.getAttr("y_start") + margin, :] = 0.0
-        if parameters.hasAttr("y_stop"):
-            peak_mask[parameters.getAttr("y_stop") + margin:-1, :] = 0.0
-    return peak_mask
+    """The finder's area-of-interest mask on padded frames of this shape: 1
+    where peaks may be found, 0 elsewhere (sa_library/fitting.py:134-176).
+    Parameters are in unpadded pixels.  Two forms:
+
+    circle  x_center, y_center, aoi_radius (all three once any is given): a
+            pixel (column c, row r) is out when (c - xc)^2 + (r - yc)^2 >
+            aoi_radius^2; both coordinates run over shape[0] values, so the
+            circle form needs square frames;
+    box     any of x_start, x_stop (columns) and y_start, y_stop (rows):
+            columns before x_start and from x_stop up to, but not including,
+            the last column are out (rows likewise)."""
+    p = _Params(parameters)
+    mask = numpy.ones(shape)
+    given = [k for k in _AOI_CIRCLE if p.hasAttr(k)]
+    if given:
+        missing = [k for k in _AOI_CIRCLE if k not in given]
+        if missing:
+            raise AssertionError("%s must be specified for a circular AOI." % missing[0])
+        r = float(p.getAttr("aoi_radius"))
+        n = shape[0]
+        dc = numpy.arange(n, dtype=numpy.float64) - (p.getAttr("x_center") + margin)
+        dr = numpy.arange(n, dtype=numpy.float64) - (p.getAttr("y_center") + margin)
+        mask[(dc[None, :] * dc[None, :] + dr[:, None] * dr[:, None]) > r * r] = 0
+        return mask
+    lo = {k: p.getAttr(k) + margin for k in ("x_start", "y_start") if p.hasAttr(k)}
+    hi = {k: p.getAttr(k) + margin for k in ("x_stop", "y_stop") if p.hasAttr(k)}
+    if "x_start" in lo:
+        mask[:, :lo["x_start"]] = 0.0
+    if "x_stop" in hi:
+        mask[:, hi["x_stop"]:-1] = 0.0
+    if "y_start" in lo:
+        mask[:lo["y_start"], :] = 0.0
+    if "y_stop" in hi:
+        mask[hi["y_stop"]:-1, :] = 0.0
+    return mask
 
 
 def _ptr(a):

@@ -567,8 +567,7 @@ def test_spliner_find_fit_loop_matches_oracle():
     ref = analysis.analyze_frame(P, wl["images"][0], None, psf_object=spline, spline=sp["coeff"])
     ff = find_peaks.initFindAndFitSpline(P, spline_fn=spline, precision=64)
     got = ff.analyzeFrame(wl["images"][0])
-    ff.peak_fitter.mfitter.cleanup(verbose=False)
-    ff.peak_finder.cleanUp()
+    ff.cleanUp()
     assert ref["x"].size > 40 and abs(got["x"].size - ref["x"].size) <= 2
     d2 = (ref["x"][:, None] - got["x"][None, :]) ** 2 + (ref["y"][:, None] - got["y"][None, :]) ** 2
     j = d2.argmin(axis=1)
