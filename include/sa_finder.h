@@ -41,7 +41,9 @@ void *saFilterCreate(const double *psf, double max_diff, int x_size, int y_size,
  * will convolve with this recentred PSF.  out5 = [separable, taps along
  * rows (na), taps along cols (nb), first row offset (a0), first col offset
  * (b0)]; when separable, u (na) and v (nb), if not NULL, receive the 1D taps
- * with psf[(a0 + i) mod x_size][(b0 + j) mod y_size] = u[i] * v[j]. */
+ * with psf[(a0 + i) mod x_size][(b0 + j) mod y_size] = u[i] * v[j].  na and
+ * nb are only known after the call, so size u for x_size and v for y_size
+ * entries (na <= x_size, nb <= y_size always hold). */
 int saFilterAnalyze(const double *psf, int x_size, int y_size, int32_t *out5, double *u, double *v);
 /* matched_filter.c:93 convolve: result = image (*) psf, circular. */
 int saFilterConvolve(void *flt, const double *image, double *result);

@@ -19,7 +19,8 @@ import types
 import numpy
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = "/root/reference"
+# the reference tree (a Python package importable from here); SA_REFERENCE overrides
+REFERENCE = os.environ.get("SA_REFERENCE", "/root/reference")
 
 
 def import_reference():
