@@ -270,6 +270,33 @@ int saSlotPoll(saFitData *fit, int32_t *phases, int32_t *sweeps);
 int saSlotReady(saFitData *fit);
 int saSlotResults(saFitData *fit, int slot, double *values, int32_t *ints);
 
+/* No reference counterpart: scheduler parameters.  A peak's step waits for
+ * the lower-index RUNNING peaks whose footprints, dilated by `dil` pixels
+ * (saSetDilation, before the first image), overlap its own; from sweep
+ * dil_switch of a fit on the dilation is dil_late (<= dil).  The results do
+ * not depend on these (the order of every pixel's updates is the
+ * reference's whatever they are), only the time does.  Any time between
+ * fits.  Returns 0, or -1 on error. */
+int saSetSchedule(saFitData *fit, int dil_late, int dil_switch);
+/* No reference counterpart: the CTA count of the persistent sweep grid at
+ * full occupancy (SMs x resident CTAs), once the handle has its first
+ * image; -1 before.  saSetSweepCTAs caps it. */
+int saGetSweepGrid(saFitData *fit);
+
+/* No reference counterpart: the engine's damped solves in checkable form.
+ * mFitSolve (multi_fit.c:1839-1883) solves (H + lam diag H) x = b with
+ * LAPACK dposv("Lower") and reports failure (not positive definite, or a
+ * NaN in x); the engine replaces that call by device solvers, which this
+ * runs on n_sys systems: a holds n_sys row-major k x k matrices H (only
+ * the upper triangle is read), b and x n_sys x k, info n_sys statuses (0 =
+ * solved, nonzero = the failure mFitSolve reports).  engine 0: the FP64
+ * Cholesky (FP64 engine; fallback of both FP32 solvers); 1: the FP32
+ * Gaussian step's solver, given H rounded to FP32 as that step keeps it
+ * (k 4 to 6); 2: the FP32 spline step's solver.  Host arrays; allocates
+ * temporary device memory.  Returns 0, or -1 on error (saGetLastError). */
+int saSolveDamped(const double *a, const double *b, int n_sys, int k, double lam, int engine, double *x,
+                  int32_t *info);
+
 /* No reference counterpart.  Fit image (residual = 0, as mFitGetFitImage) or
  * residual (residual = 1, as mFitGetResidual) of frame `frame` of the frame
  * set, written to the host array out (image_size_x * image_size_y doubles),
@@ -279,10 +306,13 @@ int saSlotResults(saFitData *fit, int slot, double *values, int32_t *ints);
  * must not allocate: cudaMalloc / cudaFree (which the other output paths
  * may call to grow their staging buffer) can synchronise the whole device,
  * and a serving loop with work in flight on other streams, or one that has
- * reserved its device memory up front, cannot afford that.  The first call
- * on each device looks the scratch address up (cudaGetSymbolAddress); make
- * it before any stream capture.  Calls that overlap in time (other threads
- * or streams, any handle) share the one scratch array and race.
+ * reserved its device memory up front, cannot afford that.  The scratch's
+ * address is looked up (cudaGetSymbolAddress, which loads the library's
+ * device module on first use) once per device when a handle is created
+ * (daoInitialize / cfInitialize) with that device current, so this call
+ * itself only launches one kernel and copies.  Calls that overlap in time
+ * (other threads or streams, any handle) share the one scratch array and
+ * race.
  * Returns 0 on success, -1 on error (saGetLastError). */
 int saGetFitImageNoAlloc(saFitData *fit, int frame, double *out, int residual);
 

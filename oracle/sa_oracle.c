@@ -68,12 +68,22 @@ struct oraFit {
 /* small helpers                                                        */
 /* ------------------------------------------------------------------ */
 
+/* A peak's psf buffer holds its roi*roi shape values and, after them, the
+ * Gaussian models' four ROI tables xt, ext, yt, eyt (roi values each), kept
+ * with the peak as the reference's daoPeak keeps them (dao_fit.c:968-998
+ * fills them, the daoCalcJH* functions read them). */
+static double *shape_tabs(const oraFit *fit, const OPeak *pk)
+{
+  return pk->psf + (size_t)fit->roi * fit->roi;
+}
+
 static void peak_copy(const oraFit *fit, OPeak *dst, const OPeak *src)
 {
   double *keep = dst->psf;
   *dst = *src;
   dst->psf = keep;
   memcpy(dst->psf, src->psf, sizeof(double) * fit->nroi);
+  memcpy(shape_tabs(fit, dst), shape_tabs(fit, src), sizeof(double) * 4 * fit->roi);
 }
 
 static int is_spline(const oraFit *fit)
@@ -249,14 +259,15 @@ static void peak_shape(const oraFit *fit, OPeak *pk)
 {
   int i;
   if (!is_spline(fit)) {
-    double ext[64], eyt[64], xo, yo, t;
+    double *xt = shape_tabs(fit, pk), *ext = xt + fit->roi, *yt = xt + 2 * fit->roi, *eyt = xt + 3 * fit->roi;
+    double xo, yo;
     xo = -(pk->p[PX] - (double)pk->xi) - fit->xoff;
     yo = -(pk->p[PY] - (double)pk->yi) - fit->xoff;
     for (i = 0; i < fit->roi; i++) {
-      t = (double)i + xo;
-      ext[i] = exp(-t * t * pk->p[PXW]);
-      t = (double)i + yo;
-      eyt[i] = exp(-t * t * pk->p[PYW]);
+      xt[i] = (double)i + xo;
+      ext[i] = exp(-xt[i] * xt[i] * pk->p[PXW]);
+      yt[i] = (double)i + yo;
+      eyt[i] = exp(-yt[i] * yt[i] * pk->p[PYW]);
     }
     for (i = 0; i < fit->nroi; i++) pk->psf[i] = eyt[fit->ry[i]] * ext[fit->rx[i]];
   } else {
@@ -349,7 +360,7 @@ static void calc_jh(const oraFit *fit, const OPeak *pk, double *jac, double *hes
   int n = fit->jac, j, l, m;
   size_t b = roi_base(fit, pk), k;
   double jt[7], fi, xi, rq, t1, t2, h = pk->p[PH];
-  double ext[64], eyt[64], xt[64], yt[64];
+  const double *xt = shape_tabs(fit, pk), *ext = xt + fit->roi, *yt = xt + 2 * fit->roi, *eyt = xt + 3 * fit->roi;
   double gx = 0.0, gy = 0.0;
   double df3[64], dx3[64], dy3[64], dz3[64];
   double df2[16], dx2[16], dy2[16];
@@ -358,14 +369,7 @@ static void calc_jh(const oraFit *fit, const OPeak *pk, double *jac, double *hes
   for (l = 0; l < n * n; l++) hes[l] = 0.0;
 
   if (!is_spline(fit)) {
-    double xo = -(pk->p[PX] - (double)pk->xi) - fit->xoff;
-    double yo = -(pk->p[PY] - (double)pk->yi) - fit->xoff;
-    for (l = 0; l < fit->roi; l++) {
-      xt[l] = (double)l + xo;
-      ext[l] = exp(-xt[l] * xt[l] * pk->p[PXW]);
-      yt[l] = (double)l + yo;
-      eyt[l] = exp(-yt[l] * yt[l] * pk->p[PYW]);
-    }
+    /* the shape tables of the peak's current state (peak_shape) */
     if (fit->model == ORA_Z) {
       /* d width / d z terms, dao_fit.c:904-916. */
       double z0, z1, z2, zt;
@@ -642,7 +646,7 @@ oraFit *oraCreate(int model, const double *rqe, const double *scmos, double tol,
     }
     roi_index(fit, s);
   }
-  fit->w.psf = (double *)malloc(sizeof(double) * fit->roi * fit->roi);
+  fit->w.psf = (double *)malloc(sizeof(double) * (fit->roi * fit->roi + 4 * fit->roi));
   return fit;
 }
 
@@ -721,7 +725,7 @@ static void grow_peaks(oraFit *fit, int n_new)
   if ((fit->nfit + n_new) <= fit->maxfit) return;
   n_alloc = PEAK_BLOCK * ((fit->nfit + n_new) / PEAK_BLOCK + 1);
   np = (OPeak *)calloc(n_alloc, sizeof(OPeak));
-  for (j = 0; j < n_alloc; j++) np[j].psf = (double *)calloc(fit->roi * fit->roi, sizeof(double));
+  for (j = 0; j < n_alloc; j++) np[j].psf = (double *)calloc(fit->roi * fit->roi + 4 * fit->roi, sizeof(double));
   i = 0;
   for (j = 0; j < fit->nfit; j++) {
     if (fit->pk[j].status != ERROR) {

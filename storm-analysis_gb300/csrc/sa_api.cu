@@ -66,22 +66,20 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocPixels];
 namespace {
 
 // The scratch's device address on the current device, looked up once per
-// device (the first call on a device makes this set-up call).
+// device.  Handle creation (new_handle: daoInitialize / cfInitialize) makes
+// this set-up call with the handle's device current; the lookup loads this
+// file's device module on that device, so saGetFitImageNoAlloc itself only
+// launches a kernel and copies.  Returns nullptr (the caller reports it)
+// when there is no usable device.
 double* noalloc_scratch() {
   static double* addr[64] = {nullptr};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= 64) {
-    set_error("saGetFitImageNoAlloc: no current device (%s)", cudaGetErrorString(e));
-    return nullptr;
-  }
+  if (e != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
   if (!addr[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      set_error("saGetFitImageNoAlloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
-      return nullptr;
-    }
+    if (e != cudaSuccess || !p) return nullptr;
     addr[dev] = static_cast<double*>(p);
   }
   return addr[dev];
@@ -97,6 +95,8 @@ struct Engine {
   std::vector<unsigned short> roi_xy;
   std::vector<int> roi_x, roi_y;
   SplineH* spline = nullptr;
+  // saGetFitImageNoAlloc's scratch on the device current at creation
+  double* noalloc = nullptr;
 
   // frames
   int F = 0;
@@ -597,6 +597,12 @@ saFitData* new_handle(const double* rqe, const double* scmos, double tol, int nx
   saFitData* h = (saFitData*)calloc(1, sizeof(saFitData));
   Engine* e = new Engine();
   h->engine = e;
+  {
+    // set-up of saGetFitImageNoAlloc (no device: the entry point reports it)
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0) e->noalloc = noalloc_scratch();
+    cudaGetLastError();
+  }
   e->cfg.nx = nx;
   e->cfg.ny = ny;
   e->cfg.tol = tol;
@@ -1186,8 +1192,11 @@ int saGetFitImageNoAlloc(saFitData* h, int frame, double* out, int residual) {
     set_error("saGetFitImageNoAlloc: no image or frame %d out of range", frame);
     return -1;
   }
-  double* scratch = noalloc_scratch();
-  if (!scratch) return -1;
+  double* scratch = e->noalloc;
+  if (!scratch) {
+    set_error("saGetFitImageNoAlloc: the device scratch was not found when the handle was created");
+    return -1;
+  }
   // The kernel writes every element that is copied out: nothing in the
   // scratch has to start at zero.
   cudaError_t err = (e->prec == 32)
@@ -1245,6 +1254,36 @@ static void remove_peaks(saFitData* h, int drop_status) {
 void mFitRemoveErrorPeaks(saFitData* h) { remove_peaks(h, ERROR); }
 void mFitRemoveRunningPeaks(saFitData* h) { remove_peaks(h, RUNNING); }
 
+int saSolveDamped(const double* a, const double* b, int n_sys, int k, double lam, int engine, double* x,
+                  int32_t* info) {
+  if (n_sys < 0 || k < 1 || k > MAX_JAC || engine < 0 || engine > 2 || (engine == 1 && (k < 4 || k > 6))) {
+    set_error("saSolveDamped: unsupported n_sys %d, k %d, engine %d", n_sys, k, engine);
+    return -1;
+  }
+  if (n_sys == 0) return 0;
+  const size_t na = (size_t)n_sys * k * k, nb = (size_t)n_sys * k;
+  double *da = nullptr, *db = nullptr, *dx = nullptr;
+  int* di = nullptr;
+  cudaError_t err = cudaMalloc(&da, na * sizeof(double));
+  if (err == cudaSuccess) err = cudaMalloc(&db, nb * sizeof(double));
+  if (err == cudaSuccess) err = cudaMalloc(&dx, nb * sizeof(double));
+  if (err == cudaSuccess) err = cudaMalloc(&di, (size_t)n_sys * sizeof(int));
+  if (err == cudaSuccess) err = cudaMemcpy(da, a, na * sizeof(double), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(db, b, nb * sizeof(double), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = solve_batch(da, db, n_sys, k, lam, engine, dx, di, 0);
+  if (err == cudaSuccess) err = cudaMemcpy(x, dx, nb * sizeof(double), cudaMemcpyDeviceToHost);
+  if (err == cudaSuccess) err = cudaMemcpy(info, di, (size_t)n_sys * sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(da);
+  cudaFree(db);
+  cudaFree(dx);
+  cudaFree(di);
+  if (err != cudaSuccess) {
+    set_error("saSolveDamped: %s", cudaGetErrorString(err));
+    return -1;
+  }
+  return 0;
+}
+
 int saSetPrecision(saFitData* h, int bits) {
   Engine* e = E(h);
   if (!e) return -1;
@@ -1270,6 +1309,25 @@ int saSetDilation(saFitData* h, int pixels) {
   e->cfg.dil = pixels;
   if (e->model_set) finish_geometry(e);
   return 0;
+}
+
+int saSetSchedule(saFitData* h, int dil_late, int dil_switch) {
+  Engine* e = E(h);
+  if (!e) return -1;
+  const int dil = e->cfg.dil < 0 ? 3 : e->cfg.dil;
+  if (dil_late < 0 || dil_late > dil || dil_switch < 0) {
+    set_error("saSetSchedule: late dilation must be 0..%d and the switch sweep >= 0", dil);
+    return -1;
+  }
+  e->cfg.dil_late = dil_late;
+  e->cfg.dil_switch = dil_switch;
+  return 0;
+}
+
+int saGetSweepGrid(saFitData* h) {
+  Engine* e = E(h);
+  if (!e || !e->configured) return -1;
+  return e->sweep_grid;
 }
 
 int saSetSweepCTAs(saFitData* h, int ctas) {

@@ -392,17 +392,6 @@ __device__ __forceinline__ float dev_res(float res, float x) {
 
 __device__ __forceinline__ float deviance(float fi, float x) { return dev_res(fi - x, x); }
 
-// Change of the deviance when the model value f0 (residual rho0 = f0 - x)
-// changes by df: 2[df - x log1p(df/f0)] = 2[df rho0/f0 + x (r - log1p(r))],
-// r = df/f0.  Both terms are accurate relative to the change itself, so an
-// FP32 evaluation decides "error went up / down / by less than tol" as an
-// FP64 evaluation of the two absolute errors would.
-__device__ __forceinline__ float dev_delta(float df, float f0, float rho0, float x) {
-  const float r = __fdiv_rn(df, f0);
-  if (fabsf(r) < 0.5f) return 2.0f * (__fdiv_rn(df * rho0, f0) + x * r_minus_log1p(r));
-  return 2.0f * (df - x * log1pf(r));
-}
-
 // Explicitly rounded products so that a contribution computed in one
 // kernel is bit-identical to the one recomputed in another.
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
@@ -444,12 +433,12 @@ struct WarpWS {
   T* Fb;      // base fit image (without this peak) at the cached anchor
   T* Bs;      // base background sum + this pixel's sCMOS term
   T* R;       // rqe
-  T* X;       // data
+  T* X;       // data (FP32 splines: the low word of t1 until a trial reloads)
   T* IC;      // 1 / (base count + 1)
   T* psf;     // current peak shape
   T* psf0;    // FP32 only: shape at the start of the step
   T* f0;      // FP32 only: model value at the start of the step
-  T* rho;     // FP32 only: residual f0 - x, computed in FP64
+  T* rho;     // FP32 only: t1 = 2 (f0 - x) / f0, high word
   T* ext;     // Gaussian x factors / spline deltas (4*64)
   T* eyt;
   T* xt;
@@ -464,8 +453,8 @@ struct WarpWS {
   float* t1h;   // t1 = 2 (f0 - x) / f0 at the start of the step, float-float
   float* t1l;
   float* f0g;   // f0 (float)
-  float* Xs;    // data, rqe and peak count (with this peak) at the start anchor
-  float* Rs;
+  float* T2s;   // Hessian weight 2 x / f0^2, rqe and peak count (with this
+  float* Rs;    // peak) at the start anchor
   float* Cs;
   float* tab0;  // shape tables of the step's start: ex hi, ex lo, ey hi, ey lo, xt, yt
   float* tab1;  // trial tables (same layout) / pass-1 gradient tables / solve scratch
@@ -508,7 +497,7 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
     ws.t1h = t;
     ws.t1l = t + n;
     ws.f0g = t + 2 * n;
-    ws.Xs = t + 3 * n;
+    ws.T2s = t + 3 * n;
     ws.Rs = t + 4 * n;
     ws.Cs = t + 5 * n;
     ws.tab0 = t + 6 * n;
@@ -539,7 +528,7 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
     ws.eyt = tab + 128;
     ws.xt = tab + 256;
     ws.yt = tab + 384;
-    ws.t1h = ws.t1l = ws.f0g = ws.Xs = ws.Rs = ws.Cs = ws.tab0 = ws.tab1 = nullptr;
+    ws.t1h = ws.t1l = ws.f0g = ws.T2s = ws.Rs = ws.Cs = ws.tab0 = ws.tab1 = nullptr;
     ws.ts = 0;
     ws.roi = nullptr;
     off = ws_pixel_arrays<T>() * n * sizeof(T) + 4 * 64 * sizeof(T) * 2;
@@ -668,6 +657,35 @@ __device__ __forceinline__ T pw(T v, int e) {
 // Monomial tables for value / d/dx / d/dy / d/dz (computeDelta3D,
 // cubic_spline.c:105-138; computeDelta2D :66-91).  Deltas are clamped to
 // [0, 1] as rangeCheckD does (:798-826).
+__device__ __forceinline__ ff ff_pow(ff v, int e) {
+  ff r{1.0f, 0.0f};
+  for (int i = 0; i < e; i++) r = ff_mul(r, v);
+  return r;
+}
+
+// FP32 engine: the value monomials x^a y^b z^c as float-float (hi words in
+// ext[0, 64), lo words in yt[0, 64)), from the FP64 deltas.  The spline's
+// model value is evaluated from them with a compensated dot
+// (spline_value_ff): FP32 rounding noise in the model value, which the fit
+// image carries from one step to the next, moves the converged background
+// of ~1 % of the peaks of the spline workload by more than 1e-4 relative
+// (FP64 oracle with 1e-8 relative noise on the value; 1e-9: 0.1 %).
+template <typename T>
+__device__ inline void spline_value_monomials(const ModelCfg& cfg, const SplinePos& s, WarpWS<T>& ws,
+                                              int lane) {
+  const bool three = (cfg.model == M_SPLINE3D);
+  const ff x = ff_from_double(clamp01(s.xd)), y = ff_from_double(clamp01(s.yd));
+  const ff z = ff_from_double(three ? clamp01(s.zd) : 0.0);
+  for (int id = lane; id < (three ? 64 : 16); id += 32) {
+    const int a = three ? (id >> 4) : (id >> 2);
+    const int b = three ? ((id >> 2) & 3) : (id & 3);
+    const int c = three ? (id & 3) : 0;
+    const ff m = ff_mul(ff_mul(ff_pow(x, a), ff_pow(y, b)), ff_pow(z, c));
+    ws.ext[id] = (T)m.h;
+    ws.yt[id] = (T)m.l;
+  }
+}
+
 template <typename T>
 __device__ inline void spline_tables(const ModelCfg& cfg, const SplinePos& s, WarpWS<T>& ws,
                                      int lane) {
@@ -677,7 +695,7 @@ __device__ inline void spline_tables(const ModelCfg& cfg, const SplinePos& s, Wa
     for (int id = lane; id < 64; id += 32) {
       const int a = id >> 4, b = (id >> 2) & 3, c = id & 3;
       const T px = pw(x, a), py = pw(y, b), pz = pw(z, c);
-      ws.ext[id] = mul_rn(mul_rn(px, py), pz);
+      if (sizeof(T) != 4) ws.ext[id] = mul_rn(mul_rn(px, py), pz);
       // derivative tables are indexed by the coefficient they multiply
       ws.ext[64 + id] = (a > 0) ? mul_rn(mul_rn(mul_rn((T)a, pw(x, a - 1)), py), pz) : (T)0;
       ws.eyt[id] = (b > 0) ? mul_rn(mul_rn(px, mul_rn((T)b, pw(y, b - 1))), pz) : (T)0;
@@ -687,11 +705,12 @@ __device__ inline void spline_tables(const ModelCfg& cfg, const SplinePos& s, Wa
     for (int id = lane; id < 16; id += 32) {
       const int a = id >> 2, b = id & 3;
       const T px = pw(x, a), py = pw(y, b);
-      ws.ext[id] = mul_rn(px, py);
+      if (sizeof(T) != 4) ws.ext[id] = mul_rn(px, py);
       ws.ext[64 + id] = (a > 0) ? mul_rn(mul_rn((T)a, pw(x, a - 1)), py) : (T)0;
       ws.eyt[id] = (b > 0) ? mul_rn(px, mul_rn((T)b, pw(y, b - 1))) : (T)0;
     }
   }
+  if constexpr (sizeof(T) == 4) spline_value_monomials(cfg, s, ws, lane);
 }
 
 __device__ __forceinline__ int clampi(int v, int hi_excl) {
@@ -720,6 +739,38 @@ __device__ __forceinline__ T spline_dot(const T* c, const T* tab, int n) {
   return acc;
 }
 
+// FP32 engine: the spline's value at ROI pixel (rx, ry) as float-float: a
+// compensated dot (Ogita, Rump and Oishi's Dot2, with the float-float
+// monomials' lo words folded into the error sum) of the cell's FP32
+// coefficients with the value monomials of spline_value_monomials.
+__device__ __forceinline__ ff spline_value_ff(const ModelCfg& cfg, const float* aij, const WarpWS<float>& ws,
+                                              const SplinePos& s, int rx, int ry) {
+  const int nc = (cfg.model == M_SPLINE3D) ? 64 : 16;
+  const float* c = spline_cell(cfg, aij, s.zi, ry + s.ys, rx + s.xs);
+  float hi = 0.0f, err = 0.0f;
+#pragma unroll 8
+  for (int i = 0; i < nc; i++) {
+    const float ci = __ldg(c + i);
+    const float p = __fmul_rn(ci, ws.ext[i]);
+    const float pe = __fmaf_rn(ci, ws.ext[i], -p);
+    const ff t = two_sum(hi, p);
+    hi = t.h;
+    err = __fmaf_rn(ci, ws.yt[i], __fadd_rn(err, __fadd_rn(t.l, pe)));
+  }
+  return fast_two_sum(hi, err);
+}
+
+// FP32 spline contributions at one pixel, quantised from float-float
+// values: f: h * (psf * rqe), bg: bg * rqe + scmos (multi_fit.c:52-54).
+// Every add and subtract of a spline peak in the FP32 engine goes through
+// this function, so they cancel exactly.
+__device__ __forceinline__ void spl32_contrib(ff psf, ff H, ff BG, float rq, float sc, Q2& qf, Q2& qb) {
+  qf.h = fixed_from_ff(ff_mul(H, ff_mul_f(psf, rq)));
+  qf.l = 0;
+  qb.h = fixed_from_ff(ff_add_f(ff_mul_f(BG, rq), sc));
+  qb.l = 0;
+}
+
 // Peak shape at ROI pixel p for the tables currently in the workspace.
 template <typename T>
 __device__ __forceinline__ T psf_at(const ModelCfg& cfg, const T* aij, const WarpWS<T>& ws,
@@ -728,9 +779,13 @@ __device__ __forceinline__ T psf_at(const ModelCfg& cfg, const T* aij, const War
     if constexpr (sizeof(T) == 4) return g32_psf(ws.tab0, ws.ts, rx, ry).h;
     else return mul_rn(ws.eyt[ry], ws.ext[rx]);
   }
-  const int nc = (cfg.model == M_SPLINE3D) ? 64 : 16;
-  const T* c = spline_cell(cfg, aij, s.zi, ry + s.ys, rx + s.xs);
-  return spline_dot(c, ws.ext, nc);
+  if constexpr (sizeof(T) == 4) {
+    return spline_value_ff(cfg, aij, ws, s, rx, ry).h;
+  } else {
+    const int nc = (cfg.model == M_SPLINE3D) ? 64 : 16;
+    const T* c = spline_cell(cfg, aij, s.zi, ry + s.ys, rx + s.xs);
+    return spline_dot(c, ws.ext, nc);
+  }
 }
 
 // Widths from z for the Z model, daoCalcWidthsFromZ dao_fit.c:1009-1035.
@@ -1221,6 +1276,22 @@ __device__ inline void add_peak(const ModelCfg& cfg, const FrameSet<T>& fs, long
       }
       return;
     }
+  }
+  if constexpr (sizeof(T) == 4) {
+    // FP32 splines
+    const ff H = ff_from_double(w.p[PH]), BG = ff_from_double(w.p[PBG]);
+    for (int p = lane; p < cfg.nroi; p += 32) {
+      int rx, ry;
+      roi_rc(fs.roi_xy, p, rx, ry);
+      const long long k = pix_index(cfg, w.xi, w.yi, rx, ry);
+      Q2 qf, qb;
+      spl32_contrib(spline_value_ff(cfg, fs.aij, ws, s, rx, ry), H, BG, __ldg(fs.rqe + k), __ldg(fs.scmos + k),
+                    qf, qb);
+      acc_red<1>(fs.f, fbase + k, qf, sign);
+      acc_red<1>(fs.bg, fbase + k, qb, sign);
+      atomicAdd(fs.cnt + fbase + k, sign);
+    }
+    return;
   }
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;

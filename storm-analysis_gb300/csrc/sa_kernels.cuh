@@ -129,6 +129,9 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
   T acc[32];
 #pragma unroll
   for (int i = 0; i < 32; i++) acc[i] = (T)0;
+  ff g[MAX_JAC];   // FP32 engine: per-lane float-float gradient
+#pragma unroll
+  for (int i = 0; i < MAX_JAC; i++) g[i] = ff{0.0f, 0.0f};
   double dev = 0.0;
   float devf = 0.0f;   // FP32 engine: per-lane partial sum
   bool fail = false;
@@ -142,23 +145,36 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     const T xv = __ldg(fs.x + fbase + kk);
     const T rq = __ldg(fs.rqe + kk);
     const T sc = __ldg(fs.scmos + kk);
-    const T psf = psf_at(cfg, fs.aij, ws, s0, rx, ry);
-    T t1, t2;
+    T psf;
+    ff psf_ff{0.0f, 0.0f};   // FP32: the model value as float-float
     if constexpr (sizeof(T) == 4) {
-      // FP32 engine, float and integer instructions only.  The residual
-      // rho = f + bg/cnt - x keeps f - x exact by subtracting in fixed point
-      // (x * 2^36 is an exact integer for data >= 2^-12).
-      const long long Xq = __float2ll_rn(xv * 68719476736.0f);
-      const float rho = fx_to_float(Fq.h - Xq) + __fdiv_rn(fx_to_float(Bq.h), (float)Cg);
-      const float f0 = xv + rho;
+      psf_ff = spline_value_ff(cfg, fs.aij, ws, s0, rx, ry);
+      psf = psf_ff.h;
+    } else {
+      psf = psf_at(cfg, fs.aij, ws, s0, rx, ry);
+    }
+    T t1, t2;
+    float t1lo = 0.0f;
+    if constexpr (sizeof(T) == 4) {
+      // FP32 engine (spline models), float and integer instructions only.
+      // The residual rho = f + bg/cnt - x is float-float: f - x is exact in
+      // fixed point (the data's fixed-point copy), so t1 = 2 rho / f0 and
+      // the Hessian weight t2 = 2 x / f0^2 = (2 - t1) / f0 are accurate to
+      // ~1e-14 before their final rounding; t1 stays float-float for the
+      // gradient and for the first-order error change of the trials.
+      const long long Xq = __ldg(fs.xq + fbase + kk);
+      const float2 xd = __ldg(fs.xff + fbase + kk);
+      const ff rh = ff_add(ff_from_fixed(Fq.h - Xq), ff_div(ff_from_fixed(Bq.h), ff{(float)Cg, 0.0f}));
+      const ff f0 = ff_add(rh, ff{xd.x, xd.y});
+      const ff t1f = ff_div(ff{2.0f * rh.h, 2.0f * rh.l}, f0);
       ws.psf0[p] = psf;
-      ws.f0[p] = f0;
-      ws.rho[p] = rho;
-      if (!(f0 > 0.0f)) fail = true;
-      else devf += dev_res(rho, xv);
-      // t1 = 2(1 - x/f) = 2 rho / f without cancellation, t2 = 2x/f^2
-      t1 = __fdiv_rn(2.0f * rho, f0);
-      t2 = __fdiv_rn(2.0f * xv, f0 * f0);
+      ws.f0[p] = f0.h;
+      ws.rho[p] = t1f.h;   // the FP32 engine keeps t1 here (hi word)
+      t1lo = t1f.l;
+      if (!(f0.h > 0.0f)) fail = true;
+      else devf += dev_res(rh.h, xd.x);
+      t1 = t1f.h;
+      t2 = ff_div(ff_sub(ff{2.0f, 0.0f}, t1f), f0).h;
     } else {
       const double fi0 = acc_value<AccW<T>::W>(Fq) + acc_value<AccW<T>::W>(Bq) / (double)Cg;
       if (!(fi0 > 0.0)) fail = true;
@@ -172,7 +188,11 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     int idx = 0;
 #pragma unroll
     for (int l = 0; l < MAX_JAC; l++) {
-      if (l < k) acc[l] += t1 * jt[l];
+      if constexpr (sizeof(T) == 4) {
+        if (l < k) ff_acc(g[l], ff_mul_raw(ff{(float)t1, t1lo}, ff{(float)jt[l], 0.0f}));
+      } else {
+        if (l < k) acc[l] += t1 * jt[l];
+      }
     }
     idx = k;
 #pragma unroll
@@ -188,8 +208,13 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     }
     (void)idx;
     // subtract this peak (multi_fit.c:1141) and keep the base state
-    const Q2 cf = quant_t<T>(contrib_f(orig.p[PH], psf, rq));
-    const Q2 cb = quant_t<T>(contrib_bg(orig.p[PBG], rq, sc));
+    Q2 cf, cb;
+    if constexpr (sizeof(T) == 4) {
+      spl32_contrib(psf_ff, ff_from_double(orig.p[PH]), ff_from_double(orig.p[PBG]), rq, sc, cf, cb);
+    } else {
+      cf = quant_t<T>(contrib_f(orig.p[PH], psf, rq));
+      cb = quant_t<T>(contrib_bg(orig.p[PBG], rq, sc));
+    }
     acc_red<AccW<T>::W>(fs.f, fbase + kk, cf, -1);
     acc_red<AccW<T>::W>(fs.bg, fbase + kk, cb, -1);
     atomicAdd(fs.cnt + fbase + kk, -1);
@@ -201,7 +226,10 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
       ws.Bs[p] = (T)(acc_value<AccW<T>::W>(q_sub(Bq, cb)) + (double)sc);
     }
     ws.R[p] = rq;
-    ws.X[p] = xv;
+    // FP32: the low word of t1 until a trial reloads the base state (the
+    // trials then take the absolute path, which reloads the data here)
+    if constexpr (sizeof(T) == 4) ws.X[p] = t1lo;
+    else ws.X[p] = xv;
     ws.IC[p] = ic_store<T>(Cg);   // (Cg - 1) + 1 once the peak is re-added
   }
   if constexpr (sizeof(T) == 4) dev = warp_sum_ff(devf);
@@ -211,14 +239,24 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     // Per-lane partial sums (a few pixels each) are summed across the warp
     // in float-float arithmetic: the cross-lane sums are where the gradient
     // cancels.
+    // The gradient's lo words go to columns nh .. nh + k - 1 (nh + k <= 25).
     float* red = ws.red;
 #pragma unroll
-    for (int i = 0; i < 32; i++)
-      if (i < nh) red[lane * 33 + i] = acc[i];
+    for (int i = 0; i < 32; i++) {
+      if (i < k) {
+        const ff gi = fast_two_sum(g[i < MAX_JAC ? i : 0].h, g[i < MAX_JAC ? i : 0].l);
+        red[lane * 33 + i] = gi.h;
+        red[lane * 33 + nh + i] = gi.l;
+      } else if (i < nh) {
+        red[lane * 33 + i] = acc[i];
+      }
+    }
     __syncwarp();
     if (lane < nh) {
       float hi = 0.0f, lo = 0.0f;
       for (int j = 0; j < 32; j++) ff_add(hi, lo, red[j * 33 + lane]);
+      if (lane < k)
+        for (int j = 0; j < 32; j++) ff_add(hi, lo, red[j * 33 + nh + lane]);
       ws.jh[lane] = (double)hi + (double)lo;
     }
   } else {
@@ -249,6 +287,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     se = w.error;
   }
   int cax = orig.xi, cay = orig.yi;   // anchor of the cached base arrays
+  bool reloaded = false;              // base arrays reloaded by a trial
   bool added_end = false, escaped = false;
   for (;;) {
     int act = ACT_EVAL;
@@ -307,31 +346,40 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     // -- trial evaluation: shape, add, error (multi_fit.c:1229-1256)
     const PeakRec& wl = *ws.w;
     SplinePos s = shape_tables(cfg, wl, ws, lane);
-    if (wl.xi != cax || wl.yi != cay) {
+    bool is_delta = false;
+    if constexpr (sizeof(T) == 4) {
+      // FP32: evaluate the change of the error from the start of the step
+      // when the ROI and the spline cell are unchanged and the start state
+      // is still in the workspace.
+      is_delta = !reloaded && (wl.xi == orig.xi) && (wl.yi == orig.yi) &&
+                 (!is_spline(cfg.model) || (s.xs == s0.xs && s.ys == s0.ys && s.zi == s0.zi));
+    }
+    if (sizeof(T) == 4 ? (!is_delta && (!reloaded || wl.xi != cax || wl.yi != cay))
+                       : (wl.xi != cax || wl.yi != cay)) {
       __threadfence();
       __syncwarp();
       load_base(cfg, fs, fbase, wl.xi, wl.yi, ws, lane);
       __syncwarp();
       cax = wl.xi;
       cay = wl.yi;
+      reloaded = true;
     }
     dev = 0.0;
     devf = 0.0f;
     fail = false;
-    bool is_delta = false;
     const double hh = wl.p[PH], bgv = wl.p[PBG];
     const T bgT = (T)bgv;
     if constexpr (sizeof(T) == 4) {
-      // FP32: evaluate the change of the error from the start of the step
-      // when the ROI and (for splines) the spline cell are unchanged.
-      is_delta = (wl.xi == orig.xi) && (wl.yi == orig.yi) &&
-                 (!is_spline(cfg.model) || (s.xs == s0.xs && s.ys == s0.ys && s.zi == s0.zi));
       if (is_delta) {
         diff_tables(cfg, orig, wl, s0, s, ws, lane);
         __syncwarp();
         const float h1 = (float)hh;
         const float dh = (float)(hh - orig.p[PH]);
         const float dbg = (float)(bgv - orig.p[PBG]);
+        // first-order term df * t1 in float-float (its pixel sum cancels
+        // near convergence), second-order term 2 x (r - log1p r) in FP32
+        ff s1{0.0f, 0.0f};
+        float s2 = 0.0f;
         for (int p = lane; p < cfg.nroi; p += 32) {
           int rx, ry;
           roi_rc(ws.roi, p, rx, ry);
@@ -340,10 +388,19 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
           ws.psf[p] = psf;
           const float rq = ws.R[p];
           const float df = rq * fmaf(h1, dpsf, dh * ws.psf0[p]) + dbg * rq * ws.IC[p];
-          const float f1 = ws.f0[p] + df;
-          if (!(f1 > 0.0f)) fail = true;
-          else devf += dev_delta(df, ws.f0[p], ws.rho[p], ws.X[p]);
+          const float f0 = ws.f0[p];
+          if (!(f0 + df > 0.0f)) {
+            fail = true;
+          } else {
+            const float t1h = ws.rho[p];
+            ff_acc(s1, ff_mul_raw(ff{df, 0.0f}, ff{t1h, ws.X[p]}));
+            const float xv = fmaf(-0.5f * t1h, f0, f0);
+            s2 += 2.0f * xv * r_minus_log1p(__fdiv_rn(df, f0));
+          }
         }
+        s1 = fast_two_sum(s1.h, s1.l);
+        devf = 0.0f;
+        dev = ff_to_double(warp_sum_ffv(s1)) + warp_sum_ff(s2);
       } else {
         for (int p = lane; p < cfg.nroi; p += 32) {
           int rx, ry;
@@ -368,8 +425,11 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
         else dev += (double)deviance(fi, ws.X[p]);
       }
     }
-    if constexpr (sizeof(T) == 4) dev = warp_sum_ff(devf);
-    else dev = warp_sum(dev);
+    if constexpr (sizeof(T) == 4) {
+      if (!is_delta) dev = warp_sum_ff(devf);
+    } else {
+      dev = warp_sum(dev);
+    }
     fail = __any_sync(0xffffffffu, fail);
     if (lane == 0) {
       if (fail) {
@@ -422,15 +482,32 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
   __syncwarp();
   if (added_end) {
     const PeakRec& wl = *ws.w;
-    for (int p = lane; p < cfg.nroi; p += 32) {
-      int rx, ry;
-      roi_rc(ws.roi, p, rx, ry);
-      const long long kk = pix_index(cfg, wl.xi, wl.yi, rx, ry);
-      const T rq = ws.R[p];
-      const T sc = __ldg(fs.scmos + kk);
-      acc_red<AccW<T>::W>(fs.f, fbase + kk, quant_t<T>(contrib_f(wl.p[PH], ws.psf[p], rq)), +1);
-      acc_red<AccW<T>::W>(fs.bg, fbase + kk, quant_t<T>(contrib_bg(wl.p[PBG], rq, sc)), +1);
-      atomicAdd(fs.cnt + fbase + kk, 1);
+    if constexpr (sizeof(T) == 4) {
+      // the tables in the workspace are the accepted trial's
+      const SplinePos sw = spline_pos(wl.p, wl.xi, wl.yi, wl.zi);
+      const ff H = ff_from_double(wl.p[PH]), BG = ff_from_double(wl.p[PBG]);
+      for (int p = lane; p < cfg.nroi; p += 32) {
+        int rx, ry;
+        roi_rc(ws.roi, p, rx, ry);
+        const long long kk = pix_index(cfg, wl.xi, wl.yi, rx, ry);
+        Q2 qf, qb;
+        spl32_contrib(spline_value_ff(cfg, fs.aij, ws, sw, rx, ry), H, BG, __ldg(fs.rqe + kk),
+                      __ldg(fs.scmos + kk), qf, qb);
+        acc_red<1>(fs.f, fbase + kk, qf, +1);
+        acc_red<1>(fs.bg, fbase + kk, qb, +1);
+        atomicAdd(fs.cnt + fbase + kk, 1);
+      }
+    } else {
+      for (int p = lane; p < cfg.nroi; p += 32) {
+        int rx, ry;
+        roi_rc(ws.roi, p, rx, ry);
+        const long long kk = pix_index(cfg, wl.xi, wl.yi, rx, ry);
+        const T rq = ws.R[p];
+        const T sc = __ldg(fs.scmos + kk);
+        acc_red<AccW<T>::W>(fs.f, fbase + kk, quant_t<T>(contrib_f(wl.p[PH], ws.psf[p], rq)), +1);
+        acc_red<AccW<T>::W>(fs.bg, fbase + kk, quant_t<T>(contrib_bg(wl.p[PBG], rq, sc)), +1);
+        atomicAdd(fs.cnt + fbase + kk, 1);
+      }
     }
   }
   if (lane == 0) {

@@ -10,6 +10,14 @@ namespace sa {
 // Print msg and keep it for saGetLastError (defined in sa_api.cu).
 void record_error(const char* msg);
 
+// The engine's damped solves (H + lam diag H) x = b on n_sys systems of
+// size k (a: n_sys row-major k x k matrices, upper triangle read; b, x:
+// n_sys x k; info: 0 or the solver's failure code).  engine 0: FP64
+// Cholesky; 1: FP32 Gaussian step solver (k 4-6); 2: FP32 spline step
+// solver.  Device pointers (sa_solve.cu).
+cudaError_t solve_batch(const double* a, const double* b, int n_sys, int k, double lam, int engine,
+                        double* x, int* info, cudaStream_t s);
+
 template <typename T>
 struct Launch {
   // Set shared-memory limits of the kernels; returns the sweep CTA count

@@ -1,8 +1,8 @@
 """
 Build libsa_cuda.so (the engine) from storm-analysis_gb300/csrc for sm_103a.
 
-The four translation units (the fitter for float and double pixels, the
-fitter's host API and the peak finder) are compiled in parallel with nvcc
+The five translation units (the fitter for float and double pixels, the
+fitter's host API, the peak finder and the batched solver check) are compiled in parallel with nvcc
 and linked into sa_gb300/libsa_cuda.so; only the CUDA runtime is linked (no
 torch).  libsa_matched_filter.so and libsa_ia_utilities.so, the
 reference-named matched-filter and image-analysis entry points, are linked
@@ -25,7 +25,7 @@ IA_LIB = os.path.join(HERE, "libsa_ia_utilities.so")
 SHIMS = [(MF_LIB, "sa_matched_filter.cpp"), (IA_LIB, "sa_ia_utilities.cpp")]
 BUILD_DIR = os.path.join(PKG_ROOT, "_build")
 
-SOURCES = ["sa_launch_f32.cu", "sa_launch_f64.cu", "sa_api.cu", "sa_finder.cu"]
+SOURCES = ["sa_launch_f32.cu", "sa_launch_f64.cu", "sa_api.cu", "sa_finder.cu", "sa_solve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
 

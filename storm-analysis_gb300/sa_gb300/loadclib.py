@@ -143,6 +143,12 @@ def _declare(lib):
     lib.saGetSweepTimes.restype = ci
     lib.saGetFitImageNoAlloc.argtypes = [hp, ci, f64, ci]
     lib.saGetFitImageNoAlloc.restype = ci
+    lib.saSolveDamped.argtypes = [f64, f64, ci, ci, ctypes.c_double, ci, f64, i32]
+    lib.saSolveDamped.restype = ci
+    lib.saSetSchedule.argtypes = [hp, ci, ci]
+    lib.saSetSchedule.restype = ci
+    lib.saGetSweepGrid.argtypes = [hp]
+    lib.saGetSweepGrid.restype = ci
     lib.saSetSweepCTAs.argtypes = [hp, ci]
     lib.saSetSweepCTAs.restype = ci
     lib.saSlotLoad.argtypes = [hp, ci, vp, vp, ci, f64, ci, cs, ci]
@@ -229,7 +235,7 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "saGetPeakPropertyBatch", "saGetPeakPropertyIntBatch", "saSetTiming", "saGetTiming",
            "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice", "saGetSweepTimes",
            "saGetFitImageNoAlloc", "saSlotLoad", "saSlotLaunch", "saSlotPoll", "saSlotReady", "saSlotResults",
-           "saSetSweepCTAs"]
+           "saSetSweepCTAs", "saSolveDamped", "saSetSchedule", "saGetSweepGrid"]
 
 FINDER_EXPORTS = ["saFilterCreate", "saFilterAnalyze", "saFilterConvolve", "saFilterConvolveMemo", "saFilterCleanup",
                   "saFilterConvolveDevice", "saFilterResultDevice", "saFilterInfo", "saFilterSetStream",

@@ -1,7 +1,8 @@
 """saGetFitImageNoAlloc: the fit image / residual through the library's
-static device scratch, compared with mFitGetFitImage / mFitGetResidual
-through the C ABI, two calls in a row.  Collected last (file name) so that
-it also runs after every other test has used the device."""
+static device scratch, for callers that cannot allocate device memory,
+compared with mFitGetFitImage / mFitGetResidual through the C ABI, two
+calls in a row.  Collected last (file name) so that it also runs after
+every other test has used the device."""
 import numpy
 import pytest
 
@@ -13,6 +14,11 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("precision", [32, 64])
 def test_no_alloc_fit_image_matches(precision):
+    """On a handle that has never used the allocating output path: one
+    warm-up call, then two calls of each kind leave the device's free memory
+    unchanged, and their outputs equal what mFitGetFitImage /
+    mFitGetResidual return afterwards (bit for bit)."""
+    import torch
     from sa_gb300 import loadclib
     case = load_case("g_3d_dense")
     f = make_gpu_fitter(case["model"], case["image"], rqe=case["rqe"], scmos=case["scmos"],
@@ -20,13 +26,23 @@ def test_no_alloc_fit_image_matches(precision):
     run_fitter(f, case)
     lib = loadclib.load()
     shape = case["image"].shape
+    warm = numpy.zeros(shape)
+    assert lib.saGetFitImageNoAlloc(f.mfit, 0, warm, 0) == 0, loadclib.last_error()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    got = {}
+    for residual in (0, 1):
+        got[residual] = []
+        for _ in range(2):
+            out = numpy.full(shape, numpy.nan)
+            assert lib.saGetFitImageNoAlloc(f.mfit, 0, out, residual) == 0, loadclib.last_error()
+            got[residual].append(out)
+    assert torch.cuda.mem_get_info()[0] == free0
     for residual, ref_fn in ((0, lib.mFitGetFitImage), (1, lib.mFitGetResidual)):
         ref = numpy.zeros(shape)
         ref_fn(f.mfit, ref)
-        for _ in range(2):
-            got = numpy.full(shape, numpy.nan)
-            assert lib.saGetFitImageNoAlloc(f.mfit, 0, got, residual) == 0, loadclib.last_error()
-            assert numpy.array_equal(got, ref)
+        for out in got[residual]:
+            assert numpy.array_equal(out, ref)
     f.cleanup(verbose=False)
 
 
