@@ -61,7 +61,7 @@ MAX_IT = 200
 # CPU side (oracle); workers are spawned, never forked from a CUDA process
 # ----------------------------------------------------------------------------
 
-PARITY_PROPS = ("x", "y", "z", "height", "background", "status", "iterations")
+PARITY_PROPS = ("x", "y", "z", "height", "background", "xsigma", "ysigma", "status", "iterations")
 
 
 def _cpu_worker(args):
@@ -119,7 +119,7 @@ def parity_block(vals, ints, counts, oracle_frames):
     relative height / background <= 1e-4 for >= 99.9 % of them)."""
     from sa_gb300 import parity
     edges = numpy.concatenate([[0], numpy.cumsum(counts)])
-    cols = {"x": 0, "y": 1, "z": 2, "height": 3, "background": 4}
+    cols = {"x": 0, "y": 1, "z": 2, "height": 3, "background": 4, "xsigma": 5, "ysigma": 6}
     got = {k: [] for k in PARITY_PROPS}
     ref = {k: [] for k in PARITY_PROPS}
     for f in sorted(oracle_frames):
@@ -471,6 +471,8 @@ def run_ours(args, rank, world, local_rank):
             # parity oracle (no floating-point contraction) on the same frames
             n_cpu, wall, _ = cpu_sample(wl, nf, cores, pool, lib="liboracle_timing.so")
             _, wall_p, ora = cpu_sample(wl, nf, cores, pool)
+            if not args.no_configs:
+                line["configs"] = run_config_reports(args, pool, cores)
         line["cpu_baseline"] = {"value": n_cpu / wall, "unit": "localizations/s", "cores": cores,
                                 "kind": "port", "sample": "%d frames of the step's workload, one "
                                 "process per core, %.1f s wall" % (nf, wall),
@@ -613,21 +615,56 @@ def run_finder(args, wl, torch):
                         "note": "whole finder step time (all kernels) in the denominator; each tap is ~15 "
                                 "FP32-pipe instructions (exact product + two-sum), ncu issue ~80 %"}}
     if not args.no_cpu:
-        from oracle import finder as ofinder
-        n_cpu = min(F, 4)
-        t0 = time.perf_counter()
-        of = ofinder.PeakFinderGaussian(FINDER_PARAMS)
-        for i in range(n_cpu):
-            of.newImage(frames[i])
-            z = numpy.zeros(shape)
-            of.estimateBackground(z)
-            of.findPeaks(z)
-        wall = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": n_cpu / wall, "unit": "frames/s", "cores": 1, "kind": "port",
-                               "sample": "%d frames, numpy FFT matched filters + the local-maxima loop, "
-                               "%.1f s" % (n_cpu, wall)}
+        cores = args.cpu_cores or os.cpu_count() or 1
+        per = max(1, min(F, 2 * cores) // cores)
+        ctx = multiprocessing.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            pool.map(_finder_warm, range(cores), chunksize=1)
+            work = [frames[i::cores][:per] for i in range(cores)]
+            t0 = time.perf_counter()
+            done = sum(pool.map(_finder_worker, work, chunksize=1))
+            wall = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": done / wall, "unit": "frames/s", "cores": cores, "kind": "port",
+                               "sample": "%d frames, one process per core: numpy FFT matched filters (the "
+                               "reference uses FFTW) + the local-maxima loop, %.1f s" % (done, wall)}
     bf.cleanUp()
     return out
+
+
+def _finder_warm(_):
+    from oracle import finder  # noqa: F401
+    return 0
+
+
+def _finder_worker(frames):
+    """The oracle's finder (background, foreground, maxima) on some frames."""
+    from oracle import finder as ofinder
+    of = ofinder.PeakFinderGaussian(FINDER_PARAMS)
+    for im in frames:
+        of.newImage(im)
+        z = numpy.zeros(im.shape)
+        of.estimateBackground(z)
+        of.findPeaks(z)
+    return len(frames)
+
+
+def _cull_warm(_):
+    from oracle import finder  # noqa: F401
+    import scipy.spatial  # noqa: F401
+    return 0
+
+
+def _cull_worker(args):
+    """The reference's two culling loops on some frames (CPU baseline)."""
+    from oracle import finder as ofinder
+    frames, sigma, nbhd, thr = args
+    n = 0
+    for fx, fy, fh, fs, fst in frames:
+        s = fst.copy()
+        ofinder.mark_dimmer_peaks_kd(fx, fy, fh, s, sigma, nbhd)
+        ofinder.mark_low_significance_peaks_kd(fx, fy, fs, s, thr, nbhd)
+        n += fx.size
+    return n
 
 
 def run_culling(args, fit):
@@ -662,20 +699,17 @@ def run_culling(args, fit):
            "unit": "peaks/s", "ms_per_step": wall * 1e3, "frames": len(frames), "peaks": n,
            "removed": int(removed), "api": "host arrays per frame (reference call shape)"}
     if not args.no_cpu:
-        from oracle import finder as ofinder
-
-        class O(object):
-            markDimmerPeaks = staticmethod(ofinder.mark_dimmer_peaks)
-            markLowSignificancePeaks = staticmethod(ofinder.mark_low_significance_peaks)
-        k = 2
-        t0 = time.perf_counter()
-        nk = 0
-        for fr in frames[:k]:
-            one(fr, O)
-            nk += fr[0].size
-        w = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": nk / w, "unit": "peaks/s", "cores": 1, "kind": "port",
-                               "sample": "%d frames, brute-force neighbour search in numpy, %.3f s" % (k, w)}
+        cores = min(args.cpu_cores or os.cpu_count() or 1, len(frames))
+        ctx = multiprocessing.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            pool.map(_cull_warm, range(cores), chunksize=1)
+            chunks = [frames[i::cores] for i in range(cores)]
+            t0 = time.perf_counter()
+            nk = sum(pool.map(_cull_worker, [(c, sigma, nbhd, thr) for c in chunks], chunksize=1))
+            w = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": nk / w, "unit": "peaks/s", "cores": cores, "kind": "port",
+                               "sample": "all %d frames, one process per core, kd-tree neighbour queries (scipy "
+                                         "cKDTree, as the reference's C builds one per call), %.3f s" % (len(frames), w)}
     return out
 
 
@@ -807,6 +841,62 @@ def run_reference(args, rank, world):
             "e2e": {"value": value, "unit": "localizations/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+CONFIG_SAMPLES = {0: 1, 2: 16, 3: 8}   # frames per configuration in the per-configuration report
+
+
+def run_config_reports(args, pool, cores):
+    """Benchmark configurations 0, 2 and 3 (2d; Z with sCMOS; 3D spline) on
+    a sample of frames each: the batched engine's localizations/s on the
+    sample, and the errors of x, y, z, height, widths and background against
+    the FP64 oracle's fits of the same (float32-rounded) frames."""
+    import torch
+    from sa_gb300 import cubic_fit_c, engine, parity, synth
+    out = {}
+    for cfg, nf in CONFIG_SAMPLES.items():
+        wl = synth.make_workload(cfg, frames=nf)
+        kw = dict(wl["fitter"])
+        model = kw.pop("model")
+        spl = kw.pop("spline", None)
+        if spl is not None:
+            kw["spline"] = cubic_fit_c.SplinePSF(coeff=spl["coeff"])
+        F = len(wl["images"])
+        shape = (wl["ny"], wl["nx"])
+        images = numpy.ascontiguousarray(numpy.stack(wl["images"]).astype(numpy.float32))
+        bgs = numpy.ascontiguousarray(numpy.stack(wl["backgrounds"]).astype(numpy.float32))
+        fit = engine.BatchFitter(model, shape, F, rqe=wl["rqe"], scmos_cal=wl["scmos_cal"],
+                                 precision=args.precision, **kw)
+        fit.load(images, bgs, wl["guesses"], "hdf5")
+        fit.fit(MAX_IT)   # warm-up
+        ms = []
+        for _ in range(2):
+            fit.load(images, bgs, wl["guesses"], "hdf5")
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fit.fit(MAX_IT)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        got = fit.results(props=("x", "y", "z", "height", "background", "xsigma", "ysigma"))
+        units = int(fit.counts().sum())
+        fit.close()
+        _, _, ora = cpu_sample(wl, F, cores, pool)
+        ref = {k: numpy.concatenate([ora[f][k] for f in range(F)]) for k in ora[0]}
+        st = parity.compare(got, ref)
+        conv = (got["status"] == ref["status"]) & (ref["status"] == 1)
+        rec = {"workload": "cfg%d: %s model, %d frames %dx%d, %d emitters" % (cfg, model, F, shape[1], shape[0], units),
+               "localizations_per_s": units / (min(ms) / 1e3), "ms_per_fit": min(ms),
+               "peaks": st["n"], "status_agree": st["status_agree"],
+               "frac_within": min([st[k] for k in st if k.startswith("frac_ok")] or [1.0]),
+               "max_dx": st.get("max_dx"), "max_dy": st.get("max_dy"), "max_dz": st.get("max_dz"),
+               "max_rel_height": st.get("max_rel_h"), "max_rel_background": st.get("max_rel_bg")}
+        if not model.startswith("spline") and conv.any():
+            for w in ("xsigma", "ysigma"):
+                rec["max_rel_" + w] = float(numpy.max(numpy.abs(got[w][conv] - ref[w][conv]) / numpy.abs(ref[w][conv])))
+        out["cfg%d" % cfg] = rec
+    return out
 
 
 DENSITY_BINS = 6   # log-spaced density bins of the serving stream's frame cache
@@ -1000,6 +1090,7 @@ def main():
     ap.add_argument("--serving", action="store_true", help="run the serving stream instead")
     ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving block of the default run")
+    ap.add_argument("--no-configs", action="store_true", help="skip the per-configuration error report")
     ap.add_argument("--latency-frames", type=int, default=20)
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--slots", type=int, default=32)

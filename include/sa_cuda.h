@@ -273,11 +273,18 @@ int saSlotResults(saFitData *fit, int slot, double *values, int32_t *ints);
 /* No reference counterpart: scheduler parameters.  A peak's step waits for
  * the lower-index RUNNING peaks whose footprints, dilated by `dil` pixels
  * (saSetDilation, before the first image), overlap its own; from sweep
- * dil_switch of a fit on the dilation is dil_late (<= dil).  The results do
+ * dil_switch of a fit on the dilation is dil_late (<= dil), except in a
+ * frame whose previous sweep re-ran more than once.  The results do
  * not depend on these (the order of every pixel's updates is the
  * reference's whatever they are), only the time does.  Any time between
  * fits.  Returns 0, or -1 on error. */
 int saSetSchedule(saFitData *fit, int dil_late, int dil_switch);
+/* No reference counterpart: when every frame still fitting has at most
+ * `peaks` RUNNING peaks left, their remaining sweeps run in one launch, the
+ * steps of a frame one after another in index order, instead of three
+ * launches and a host poll per sweep (default 4; 0 never).  The results do
+ * not change.  Returns 0, or -1 on error. */
+int saSetTailPeaks(saFitData *fit, int peaks);
 /* No reference counterpart: the CTA count of the persistent sweep grid at
  * full occupancy (SMs x resident CTAs), once the handle has its first
  * image; -1 before.  saSetSweepCTAs caps it. */

@@ -231,6 +231,46 @@ def mark_low_significance_peaks(x, y, sig, status, min_sig, r_neighbors):
     return removed
 
 
+def mark_dimmer_peaks_kd(x, y, h, status, r_removal, r_neighbors):
+    """mark_dimmer_peaks with the neighbour lists from a kd-tree (scipy's
+    cKDTree), as the reference's C builds one per call
+    (sa_library/ia_utilities.c:221-283); same visiting order and status
+    rules.  For the timed CPU baseline."""
+    from scipy.spatial import cKDTree
+    pts = numpy.stack([x, y], axis=1)
+    tree = cKDTree(pts)
+    near = tree.query_ball_point(pts, r_removal)
+    removed = 0
+    for i in range(x.size):
+        if status[i] == ERROR or len(near[i]) < 2:
+            continue
+        if numpy.any(h[near[i]] > h[i]):
+            removed += 1
+            status[i] = ERROR
+            for k in tree.query_ball_point(pts[i], r_neighbors):
+                if status[k] == CONVERGED:
+                    status[k] = RUNNING
+    return removed
+
+
+def mark_low_significance_peaks_kd(x, y, sig, status, min_sig, r_neighbors):
+    """mark_low_significance_peaks with kd-tree neighbour queries
+    (sa_library/ia_utilities.c:292-340).  For the timed CPU baseline."""
+    from scipy.spatial import cKDTree
+    pts = numpy.stack([x, y], axis=1)
+    tree = cKDTree(pts)
+    removed = 0
+    for i in range(x.size):
+        if status[i] == ERROR or sig[i] > min_sig:
+            continue
+        status[i] = ERROR
+        removed += 1
+        for k in tree.query_ball_point(pts[i], r_neighbors):
+            if status[k] == CONVERGED:
+                status[k] = RUNNING
+    return removed
+
+
 def running_if_has_neighbors(c_x, c_y, n_x, n_y, status, radius):
     """sa_library/ia_utilities.c:401-430."""
     for i in range(c_x.size):

@@ -2,6 +2,7 @@
 // device-driven sweep loop and the reference-named C ABI (include/sa_cuda.h).
 #include <algorithm>
 #include <climits>
+#include <cstddef>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -136,6 +137,7 @@ struct Engine {
   int epoch = 0;
   int sweep_grid = 0;
   int sweep_ctas_cap = 0;   // 0: the full persistent grid
+  int tail_peaks = 4;       // k_tail for frames with at most this many RUNNING peaks (0: never)
   size_t sweep_smem = 0, cta_smem = 0, warp_smem = 0;
   bool configured = false;
 
@@ -414,6 +416,7 @@ struct Engine {
   // flight, so that no tick is launched past their end.
   int run_until_done(std::vector<FrameCtl>& ctl, int max_sweeps) {
     if (ensure_poll_buffers()) return -1;
+    bool tail_queued = false;
     const bool ahead = max_sweeps > 2;
     if (burst_poll(0)) return -1;
     int cur = 0;
@@ -431,6 +434,25 @@ struct Engine {
         for (int f = 0; f < F; f++) ctl[f] = h_pctl[cur][f];
         CK(cudaStreamSynchronize(stream));
         return check_err_flag() ? -1 : 0;
+      }
+      // Once every frame still fitting has at most tail_peaks RUNNING peaks
+      // (a count that only falls during a fit), their remaining sweeps run
+      // in one launch after the ticks already queued; a frame that is not
+      // ready for it when it runs is left to the ticks.
+      if (ahead && tail_peaks > 0 && !tail_queued) {
+        bool all = true, any = false;
+        for (int f = 0; f < F && all; f++) {
+          const FrameCtl& c = h_pctl[cur][f];
+          if (c.phase == PH_DONE || c.phase == PH_IDLE) continue;
+          if (c.phase == PH_SWEEP_PENDING && c.sweeps > 0 && c.unconverged <= tail_peaks) any = true;
+          else all = false;
+        }
+        if (all && any) {
+          if (prec == 32) CK(Launch<float>::tail(cfg, fs<float>(), tail_peaks, stream));
+          else CK(Launch<double>::tail(cfg, fs<double>(), tail_peaks, stream));
+          launches += 1;
+          tail_queued = true;
+        }
       }
       if (ahead) {
         cur = 1 - cur;
@@ -479,7 +501,9 @@ struct Engine {
   int burst_poll(int b) {
     for (int i = 0; i < 2; i++)
       if (tick()) return -1;
-    CK(cudaMemcpyAsync(h_pctl[b], d_ctl, sizeof(FrameCtl) * F, cudaMemcpyDeviceToHost, stream));
+    // the fields before the device-only lists of every frame's block
+    CK(cudaMemcpy2DAsync(h_pctl[b], sizeof(FrameCtl), d_ctl, sizeof(FrameCtl), offsetof(FrameCtl, escaped), F,
+                         cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(h_perr + b, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
     CK(cudaEventRecord(ev_pb[b], stream));
     return 0;
@@ -1330,6 +1354,13 @@ int saGetSweepGrid(saFitData* h) {
   return e->sweep_grid;
 }
 
+int saSetTailPeaks(saFitData* h, int peaks) {
+  Engine* e = E(h);
+  if (!e || peaks < 0) return -1;
+  e->tail_peaks = peaks;
+  return 0;
+}
+
 int saSetSweepCTAs(saFitData* h, int ctas) {
   Engine* e = E(h);
   if (!e || ctas < 0) return -1;
@@ -1756,7 +1787,8 @@ int saSlotLaunch(saFitData* h, int n_ticks) {
   if (!e->ev_poll) CK(cudaEventCreateWithFlags(&e->ev_poll, cudaEventDisableTiming));
   for (int i = 0; i < n_ticks; i++)
     if (e->tick()) return -1;
-  CK(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(FrameCtl) * e->F, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaMemcpy2DAsync(e->h_ctl, sizeof(FrameCtl), e->d_ctl, sizeof(FrameCtl), offsetof(FrameCtl, escaped), e->F,
+                       cudaMemcpyDeviceToHost, e->stream));
   CK(cudaEventRecord(e->ev_poll, e->stream));
   return 0;
 }

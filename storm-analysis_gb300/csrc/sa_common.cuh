@@ -49,8 +49,8 @@ enum { PT_FINDER = 0, PT_TESTING = 1, PT_TEXT = 2 };
 // Frame phases of the device-side doFit state machine.
 enum { PH_IDLE = 0, PH_SWEEP_PENDING = 1, PH_IN_SWEEP = 2, PH_RERUN_PENDING = 3, PH_DONE = 4 };
 
-constexpr int MAX_BARRIERS = 48;      // per frame; beyond this the frame runs in index order
-constexpr int MAX_ESCAPES = 48;
+constexpr int MAX_BARRIERS = 256;     // per frame; beyond this the frame runs in index order
+constexpr int MAX_ESCAPES = 128;      // per sweep attempt; beyond this likewise
 constexpr int MAX_ROI = 64;           // ROI edge limit (ext/eyt tables)
 constexpr int MAX_JAC = 7;
 
@@ -97,9 +97,8 @@ struct FrameCtl {
   int grab;              // next run rank to hand out
   int escaped_min;       // lowest escaped run rank of this attempt (INT_MAX: none)
   int n_escaped;
-  int escaped[MAX_ESCAPES];
   int n_barrier;
-  int barrier[MAX_BARRIERS];
+  int frontier;          // every run rank in [start, frontier) is done (kept when n_barrier > 0)
   int serial;            // 1: every peak waits for its predecessor (index order)
   int unconverged;
   int nrun;
@@ -108,6 +107,9 @@ struct FrameCtl {
   int barriers_total;    // escaped peaks made barriers, all sweeps
   int dil;               // footprint dilation of the current sweep
   long long ctr[NCOUNTERS];
+  // device-only lists (the host's polls copy the fields above them)
+  int escaped[MAX_ESCAPES];
+  int barrier[MAX_BARRIERS];   // ascending
 };
 
 // Device pointers of a frame set.  T is the pixel arithmetic type.

@@ -42,6 +42,51 @@ __device__ __forceinline__ bool wait_epoch(const int* done, int epoch, unsigned*
   return true;
 }
 
+// The completed prefix of a frame's sweep attempt: every run rank in
+// [start, *frontier) is done.  advance_prefix (all lanes, warp-uniform)
+// moves it over the done ranks at its end, 32 done flags per round trip
+// (one per lane); any warp may move it, so a rank that completes while
+// another warp is moving the prefix past it is never missed (that warp, or
+// this one, sees its flag).  The warp barrier and the fence before each
+// move order the writes of the ranks it moves over (seen by the lanes'
+// acquire loads of their flags) before the move, so a waiter that acquires
+// the prefix sees them.  Returns the prefix.
+__device__ __forceinline__ int advance_prefix(int* frontier, const int* done, int nrun, int epoch, int lane) {
+  int fr = __shfl_sync(0xffffffffu, lane == 0 ? ld_acquire(frontier) : 0, 0);
+  while (fr < nrun) {
+    const int q = fr + lane;
+    const bool d = (q < nrun) && (ld_acquire(done + q) == epoch);
+    const unsigned m = __ballot_sync(0xffffffffu, d);
+    const int k = (~m != 0u) ? (__ffs(~m) - 1) : 32;
+    if (k == 0) break;
+    __syncwarp();
+    int seen = 0;
+    if (lane == 0) {
+      __threadfence();
+      seen = atomicCAS(frontier, fr, fr + k);
+    }
+    seen = __shfl_sync(0xffffffffu, seen, 0);
+    fr = (seen == fr) ? fr + k : seen;
+  }
+  return fr;
+}
+
+// Wait (all lanes, warp-uniform) until the completed prefix reaches target,
+// moving it along meanwhile.  Bounded like wait_epoch.
+__device__ __forceinline__ bool wait_prefix(int* frontier, int target, const int* done, int nrun, int epoch,
+                                            unsigned* err_flag, int lane) {
+  if (advance_prefix(frontier, done, nrun, epoch, lane) >= target) return true;
+  unsigned long long t0 = global_ns();
+  while (advance_prefix(frontier, done, nrun, epoch, lane) < target) {
+    __nanosleep(200);
+    if (global_ns() - t0 > 4000000000ull) {
+      if (lane == 0) atomicOr(err_flag, 1u);
+      return false;
+    }
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // warp reductions
 // ---------------------------------------------------------------------------

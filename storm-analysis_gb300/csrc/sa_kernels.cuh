@@ -581,22 +581,28 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
     if constexpr (G32 >= 0) g32_prologue<G32>(cfg, fs.pk + base + li, ws, lane);
     bool barrier = c->serial != 0;
     bool ok = true;
+    const int nb = c->n_barrier;
     // -- dependencies
     if (c->serial) {
       if (r - 1 >= start) ok = wait_epoch(fs.done + base + r - 1, epoch, fs.err_flag);
     } else {
-      const int nb = c->n_barrier;
-      for (int bi = 0; bi < nb && ok; bi++) {
-        const int b = c->barrier[bi];
-        if (b == r) barrier = true;
+      // Barriers (escaped peaks of earlier attempts, unbounded steps) are
+      // ascending: the last one <= r decides.  A barrier waits until the
+      // completed prefix reaches it (every lower rank done); a later rank
+      // waits for the last barrier below it, which is done only after
+      // every rank below that barrier.
+      int lo = 0, hi = nb;   // first barrier index with barrier > r
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (c->barrier[mid] <= r) lo = mid + 1;
+        else hi = mid;
       }
+      const int bprev = lo > 0 ? c->barrier[lo - 1] : -1;
+      if (bprev == r) barrier = true;
       if (barrier) {
-        for (int q = start; q < r && ok; q++) ok = wait_epoch(fs.done + base + q, epoch, fs.err_flag);
+        ok = wait_prefix(&c->frontier, r, fs.done + base, c->nrun, epoch, fs.err_flag, lane);
       } else {
-        for (int bi = 0; bi < nb && ok; bi++) {
-          const int b = c->barrier[bi];
-          if (b < r && b >= start) ok = wait_epoch(fs.done + base + b, epoch, fs.err_flag);
-        }
+        if (bprev >= start) ok = wait_epoch(fs.done + base + bprev, epoch, fs.err_flag);
         // lower-index RUNNING neighbours whose dilated footprints overlap:
         // lane l < 9 reads the range of neighbouring cell l, then the
         // candidates of all nine cells are checked 32 at a time
@@ -655,6 +661,7 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
     if (*((volatile int*)&c->escaped_min) < r) {
       __syncwarp();
       if (lane == 0) st_release(fs.done + base + r, epoch);
+      if (nb > 0) advance_prefix(&c->frontier, fs.done + base, c->nrun, epoch, lane);
       continue;
     }
     // No fence before the step: every lane made its own acquire load of each
@@ -676,6 +683,7 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
     __threadfence();
     __syncwarp();
     if (lane == 0) st_release(fs.done + base + r, epoch);
+    if (nb > 0) advance_prefix(&c->frontier, fs.done + base, c->nrun, epoch, lane);
   }
 }
 
@@ -763,11 +771,16 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
       c->nrun = nrun;
       c->start = 0;
       c->grab = 0;
+      c->frontier = 0;
       c->escaped_min = INT_MAX;
       c->n_escaped = 0;
       c->n_barrier = 0;
       c->serial = cfg.force_serial;
-      c->dil = (c->sweeps >= cfg.dil_switch) ? cfg.dil_late : cfg.dil;
+      // the late dilation from sweep dil_switch on, unless the previous
+      // sweep of this frame re-ran more than once (anchors still moving
+      // in many places: a dense frame then spends more on re-runs than
+      // the wider footprints cost)
+      c->dil = (c->sweeps >= cfg.dil_switch && c->attempts <= 2) ? cfg.dil_late : cfg.dil;
       c->attempts = 1;
       c->phase = nrun > 0 ? PH_IN_SWEEP : PH_IN_SWEEP;
     }
@@ -776,15 +789,20 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
     const int nrun = c->nrun;
     // barriers: merge the escaped run ranks
     if (tid == 0) {
+      // merge the escaped run ranks into the ascending barrier list
       const int ne = min(c->n_escaped, MAX_ESCAPES);
       for (int e = 0; e < ne; e++) {
         const int r = c->escaped[e];
-        bool have = false;
-        for (int q = 0; q < c->n_barrier; q++) have |= (c->barrier[q] == r);
-        if (!have) {
-          if (c->n_barrier < MAX_BARRIERS) c->barrier[c->n_barrier++] = r;
-          else c->serial = 1;
+        int pos = 0;
+        while (pos < c->n_barrier && c->barrier[pos] < r) pos++;
+        if (pos < c->n_barrier && c->barrier[pos] == r) continue;
+        if (c->n_barrier >= MAX_BARRIERS) {
+          c->serial = 1;
+          continue;
         }
+        for (int q = c->n_barrier; q > pos; q--) c->barrier[q] = c->barrier[q - 1];
+        c->barrier[pos] = r;
+        c->n_barrier++;
       }
       if (c->n_escaped > MAX_ESCAPES) c->serial = 1;
       s_total = 0;
@@ -823,6 +841,7 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
     if (tid == 0) {
       c->start = b;
       c->grab = b;
+      c->frontier = b;
       c->escaped_min = INT_MAX;
       c->n_escaped = 0;
       c->attempts += 1;
@@ -935,6 +954,126 @@ __global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
     c->unconverged = s_unconv;
     c->sweeps += 1;
     c->phase = (s_unconv == 0 || c->sweeps >= c->max_sweeps) ? PH_DONE : PH_SWEEP_PENDING;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_tail: the remaining sweeps of frames with few RUNNING peaks, one launch
+// ---------------------------------------------------------------------------
+
+// One warp (a 32-thread CTA) per frame.  A frame whose fit has made at least
+// one sweep and has at most tail_peaks RUNNING peaks left runs all of its
+// remaining sweeps here, each as k_prepare + k_sweep + k_post would: the
+// RUNNING peaks of the previous sweep's run list, in index order, take their
+// LM steps one after another -- the reference's own sequential order
+// (mFitIterateLM multi_fit.c:1072-1349), so every step is unbounded and
+// needs no dependency wait or escape -- then the moved peaks are recentered
+// (mFitRecenterPeaks :1644-1690), the counters summed and the frame's
+// next phase decided (dao_fit_c.py:332-356).  The results are the ones the
+// normal ticks give; what goes is two launches and a host poll per sweep.
+template <typename T, int G32>
+__global__ void __launch_bounds__(32) k_tail(ModelCfg cfg, FrameSet<T> fs, int tail_peaks) {
+  extern __shared__ __align__(16) char smem[];
+  const int lane = threadIdx.x;
+  const int f = blockIdx.x;
+  FrameCtl* c = fs.ctl + f;
+  if (c->phase != PH_SWEEP_PENDING || c->sweeps == 0 || c->unconverged > tail_peaks) return;
+  WarpWS<T> ws = warp_ws<T>(smem, cfg, cfg.nroi);
+  {
+    unsigned short* roi = reinterpret_cast<unsigned short*>(smem + warp_ws_bytes<T>(cfg, cfg.nroi));
+    for (int i = lane; i < cfg.nroi; i += 32) roi[i] = fs.roi_xy[i];
+    __syncwarp();
+    ws.roi = roi;
+  }
+  const int base = fs.pk_off[f];
+  const long long fbase = (long long)f * fs.npix;
+  int nrun = c->nrun;
+  for (;;) {
+    // run list: the previous run list's RUNNING peaks, in order (k_prepare)
+    int m = 0;
+    for (int k0 = 0; k0 < nrun; k0 += 32) {
+      const int k = k0 + lane;
+      const int i = (k < nrun) ? fs.run[base + k] : -1;
+      bool flag = false;
+      if (i >= 0 && fs.pk[base + i].status == RUNNING) {
+        const PeakRec& q = fs.pk[base + i];
+        if (q.xi < 0 || q.yi < 0 || q.xi >= cfg.nx - cfg.roi || q.yi >= cfg.ny - cfg.roi)
+          fs.pk[base + i].status = ERROR;
+        else
+          flag = true;
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, flag);
+      __syncwarp();
+      if (flag) fs.run[base + m + __popc(bal & ((1u << lane) - 1u))] = i;
+      m += __popc(bal);
+      __syncwarp();
+    }
+    nrun = m;
+    // the steps, one after another in index order (k_sweep)
+    long long loc[NCOUNTERS];
+#pragma unroll
+    for (int i = 0; i < NCOUNTERS; i++) loc[i] = 0;
+    for (int r = 0; r < nrun; r++) {
+      const int li = fs.run[base + r];
+      int* sc = fs.stepctr + (size_t)(base + li) * NCOUNTERS;
+      if constexpr (G32 >= 0) {
+        g32_prologue<G32>(cfg, fs.pk + base + li, ws, lane);
+        lm_step_g32<G32>(cfg, fs, fbase, fs.pk + base + li, true, 0, ws, sc, lane);
+      } else {
+        lm_step(cfg, fs, fbase, fs.pk + base + li, true, 0, ws, sc, lane);
+      }
+      __threadfence();
+      __syncwarp();
+      if (lane == 0)
+        for (int i = 0; i < NCOUNTERS; i++) loc[i] += sc[i];
+      __syncwarp();
+    }
+    // recenter, count (k_post)
+    int unconv = 0;
+    for (int r = 0; r < nrun; r++) {
+      const int li = fs.run[base + r];
+      PeakRec rec;
+      load_rec(fs.pk + base + li, rec);
+      if (rec.status != RUNNING) continue;
+      const double dx = rec.p[PX] - rec.xi, dy = rec.p[PY] - rec.yi;
+      if (!((dx < -0.25) || (dx > 1.25) || (dy < -0.25) || (dy > 1.25))) {
+        unconv++;
+        continue;
+      }
+      SplinePos sp = shape_tables(cfg, rec, ws, lane);
+      add_peak(cfg, fs, fbase, rec, sp, ws, -1, lane);
+      __syncwarp();
+      rec.added -= 1;
+      rec.xi = (int)floor(rec.p[PX]);
+      rec.yi = (int)floor(rec.p[PY]);
+      const int chk = base_check(cfg, rec);
+      if (chk) {
+        if (lane == 0) {
+          loc[C_LOST]++;
+          loc[chk == 1 ? C_MARGIN : C_NEGH]++;
+        }
+        rec.status = ERROR;
+      } else {
+        SplinePos s2 = shape_tables(cfg, rec, ws, lane);
+        add_peak(cfg, fs, fbase, rec, s2, ws, +1, lane);
+        rec.added += 1;
+        unconv++;
+      }
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) fs.pk[base + li] = rec;
+      __syncwarp();
+    }
+    if (lane == 0) {
+      for (int i = 0; i < NCOUNTERS; i++) c->ctr[i] += loc[i];
+      c->unconverged = unconv;
+      c->sweeps += 1;
+      c->nrun = nrun;
+      c->attempts = 1;
+      c->phase = (unconv == 0 || c->sweeps >= c->max_sweeps) ? PH_DONE : PH_SWEEP_PENDING;
+    }
+    __syncwarp();
+    if (unconv == 0 || *((volatile int*)&c->sweeps) >= c->max_sweeps) break;
   }
 }
 

@@ -28,6 +28,9 @@ struct Launch {
   static cudaError_t sweep(const ModelCfg& cfg, const FrameSet<T>& fs, int epoch, int grid,
                            size_t smem, cudaStream_t s);
   static cudaError_t post(const ModelCfg& cfg, const FrameSet<T>& fs, size_t smem, cudaStream_t s);
+  // The remaining sweeps of every frame with at most tail_peaks RUNNING
+  // peaks left, one warp per frame, in one launch (k_tail).
+  static cudaError_t tail(const ModelCfg& cfg, const FrameSet<T>& fs, int tail_peaks, cudaStream_t s);
   static cudaError_t new_image(const FrameSet<T>& fs, const void* img, int bits, int frame0,
                                int nframes, cudaStream_t s);
   static cudaError_t new_background(const FrameSet<T>& fs, const void* bg, int bits, int frame0,

@@ -29,6 +29,21 @@ void (*sweep_kernel(const ModelCfg& cfg))(ModelCfg, FrameSet<T>, int) {
 }
 
 template <typename T>
+void (*tail_kernel(const ModelCfg& cfg))(ModelCfg, FrameSet<T>, int) {
+  if constexpr (sizeof(T) == 4) {
+    if (gauss32<T>(cfg)) {
+      switch (cfg.model) {
+        case M_2DFIXED: return k_tail<T, M_2DFIXED>;
+        case M_2D: return k_tail<T, M_2D>;
+        case M_3D: return k_tail<T, M_3D>;
+        default: return k_tail<T, M_Z>;
+      }
+    }
+  }
+  return k_tail<T, -1>;
+}
+
+template <typename T>
 cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* sweep_smem,
                                  size_t* cta_smem, size_t* warp_smem) {
   int dev = 0;
@@ -61,6 +76,8 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
   if (e != cudaSuccess) return e;
   e = raise_limit((const void*)k_post<T>);
   if (e != cudaSuccess) return e;
+  e = raise_limit((const void*)tail_kernel<T>(cfg));
+  if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T>(cfg), SWEEP_BLOCK, s_sweep);
   if (e != cudaSuccess) return e;
@@ -88,6 +105,13 @@ cudaError_t Launch<T>::sweep(const ModelCfg& cfg, const FrameSet<T>& fs, int epo
 template <typename T>
 cudaError_t Launch<T>::post(const ModelCfg& cfg, const FrameSet<T>& fs, size_t smem, cudaStream_t s) {
   k_post<T><<<fs.F, CTA_BLOCK, smem, s>>>(cfg, fs);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::tail(const ModelCfg& cfg, const FrameSet<T>& fs, int tail_peaks, cudaStream_t s) {
+  const size_t smem = warp_ws_bytes<T>(cfg, cfg.nroi) + (((size_t)cfg.nroi * 2 + 15) & ~(size_t)15);
+  tail_kernel<T>(cfg)<<<fs.F, 32, smem, s>>>(cfg, fs, tail_peaks);
   return cudaGetLastError();
 }
 

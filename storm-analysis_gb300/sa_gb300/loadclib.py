@@ -149,6 +149,8 @@ def _declare(lib):
     lib.saSetSchedule.restype = ci
     lib.saGetSweepGrid.argtypes = [hp]
     lib.saGetSweepGrid.restype = ci
+    lib.saSetTailPeaks.argtypes = [hp, ci]
+    lib.saSetTailPeaks.restype = ci
     lib.saSetSweepCTAs.argtypes = [hp, ci]
     lib.saSetSweepCTAs.restype = ci
     lib.saSlotLoad.argtypes = [hp, ci, vp, vp, ci, f64, ci, cs, ci]
@@ -235,7 +237,7 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "saGetPeakPropertyBatch", "saGetPeakPropertyIntBatch", "saSetTiming", "saGetTiming",
            "saGetKernelLaunches", "saGetResultsBatch", "saSetDevice", "saGetSweepTimes",
            "saGetFitImageNoAlloc", "saSlotLoad", "saSlotLaunch", "saSlotPoll", "saSlotReady", "saSlotResults",
-           "saSetSweepCTAs", "saSolveDamped", "saSetSchedule", "saGetSweepGrid"]
+           "saSetSweepCTAs", "saSolveDamped", "saSetSchedule", "saGetSweepGrid", "saSetTailPeaks"]
 
 FINDER_EXPORTS = ["saFilterCreate", "saFilterAnalyze", "saFilterConvolve", "saFilterConvolveMemo", "saFilterCleanup",
                   "saFilterConvolveDevice", "saFilterResultDevice", "saFilterInfo", "saFilterSetStream",
