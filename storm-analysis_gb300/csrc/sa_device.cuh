@@ -21,25 +21,47 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Polling load: no ordering, and unlike an acquire load it does not
+// invalidate the SM's L1 on every poll.  A wait polls with it and acquires
+// once, when it has seen what it waits for.
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
 
-// Wait (all lanes, warp-uniform) until done[idx] == epoch.  Bounded: after
-// ~4 s the wait gives up, raises bit 0 of err_flag and returns false.
+// Sleep between polls: 32 ns doubling to 512 ns.  A waiter wakes at most
+// about half a microsecond after its predecessor is done (an LM step takes
+// tens of microseconds), and sleeping waiters leave the issue slots to the
+// warps that are stepping.
+__device__ __forceinline__ void poll_backoff(unsigned& ns) {
+  __nanosleep(ns);
+  if (ns < 512) ns <<= 1;
+}
+
+constexpr unsigned long long WAIT_LIMIT_NS = 4000000000ull;
+
+// Wait (all lanes, warp-uniform) until done[idx] == epoch, with an acquire
+// load at the end.  Bounded: after ~4 s the wait gives up, raises bit 0 of
+// err_flag and returns false.
 __device__ __forceinline__ bool wait_epoch(const int* done, int epoch, unsigned* err_flag) {
   if (ld_acquire(done) == epoch) return true;
-  unsigned long long t0 = global_ns();
-  while (ld_acquire(done) != epoch) {
-    __nanosleep(100);
-    if (global_ns() - t0 > 4000000000ull) {
+  const unsigned long long t0 = global_ns();
+  unsigned ns = 32;
+  for (unsigned it = 1;; it++) {
+    poll_backoff(ns);
+    if (ld_relaxed(done) == epoch) return ld_acquire(done) == epoch;
+    if ((it & 31) == 0 && global_ns() - t0 > WAIT_LIMIT_NS) {
       atomicOr(err_flag, 1u);
       return false;
     }
   }
-  return true;
 }
 
 // The completed prefix of a frame's sweep attempt: every run rank in
@@ -47,24 +69,23 @@ __device__ __forceinline__ bool wait_epoch(const int* done, int epoch, unsigned*
 // moves it over the done ranks at its end, 32 done flags per round trip
 // (one per lane); any warp may move it, so a rank that completes while
 // another warp is moving the prefix past it is never missed (that warp, or
-// this one, sees its flag).  The warp barrier and the fence before each
-// move order the writes of the ranks it moves over (seen by the lanes'
-// acquire loads of their flags) before the move, so a waiter that acquires
-// the prefix sees them.  Returns the prefix.
+// this one, sees its flag).  Before each move every lane fences (its
+// relaxed observation of a done flag followed by the fence acquires that
+// rank's writes, and the fence releases them again with the move), so a
+// waiter that acquires the prefix sees the writes of every rank below it.
+// Returns the prefix (a relaxed read: wait_prefix acquires it).
 __device__ __forceinline__ int advance_prefix(int* frontier, const int* done, int nrun, int epoch, int lane) {
-  int fr = __shfl_sync(0xffffffffu, lane == 0 ? ld_acquire(frontier) : 0, 0);
+  int fr = __shfl_sync(0xffffffffu, lane == 0 ? ld_relaxed(frontier) : 0, 0);
   while (fr < nrun) {
     const int q = fr + lane;
-    const bool d = (q < nrun) && (ld_acquire(done + q) == epoch);
+    const bool d = (q < nrun) && (ld_relaxed(done + q) == epoch);
     const unsigned m = __ballot_sync(0xffffffffu, d);
     const int k = (~m != 0u) ? (__ffs(~m) - 1) : 32;
     if (k == 0) break;
+    __threadfence();
     __syncwarp();
     int seen = 0;
-    if (lane == 0) {
-      __threadfence();
-      seen = atomicCAS(frontier, fr, fr + k);
-    }
+    if (lane == 0) seen = atomicCAS(frontier, fr, fr + k);
     seen = __shfl_sync(0xffffffffu, seen, 0);
     fr = (seen == fr) ? fr + k : seen;
   }
@@ -72,19 +93,23 @@ __device__ __forceinline__ int advance_prefix(int* frontier, const int* done, in
 }
 
 // Wait (all lanes, warp-uniform) until the completed prefix reaches target,
-// moving it along meanwhile.  Bounded like wait_epoch.
+// moving it along meanwhile; acquires the prefix at the end.  Bounded like
+// wait_epoch.
 __device__ __forceinline__ bool wait_prefix(int* frontier, int target, const int* done, int nrun, int epoch,
                                             unsigned* err_flag, int lane) {
-  if (advance_prefix(frontier, done, nrun, epoch, lane) >= target) return true;
-  unsigned long long t0 = global_ns();
-  while (advance_prefix(frontier, done, nrun, epoch, lane) < target) {
-    __nanosleep(200);
-    if (global_ns() - t0 > 4000000000ull) {
-      if (lane == 0) atomicOr(err_flag, 1u);
-      return false;
+  if (advance_prefix(frontier, done, nrun, epoch, lane) < target) {
+    const unsigned long long t0 = global_ns();
+    unsigned ns = 32;
+    for (unsigned it = 1;; it++) {
+      poll_backoff(ns);
+      if (advance_prefix(frontier, done, nrun, epoch, lane) >= target) break;
+      if ((it & 31) == 0 && global_ns() - t0 > WAIT_LIMIT_NS) {
+        if (lane == 0) atomicOr(err_flag, 1u);
+        return false;
+      }
     }
   }
-  return true;
+  return ld_acquire(frontier) >= target;
 }
 
 // ---------------------------------------------------------------------------
@@ -225,16 +250,61 @@ __device__ __forceinline__ ff ff_from_double(double d) {
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.h + (double)a.l; }
 
-// One-word fixed-point value q * 2^-36 as an exact float-float pair.
+// Fixed-point words (q * 2^-36) to and from FP32 with 32-bit instructions.
+// The 64-bit integer <-> float conversions issue on the FP64 pipe, which
+// runs at a small fraction of the FP32 rate on this part.  A word splits
+// into its signed high word and the low word's bits 31..9 and 8..0; each
+// piece converts exactly by the exponent-bias trick (an integer below 2^23
+// placed in the mantissa of 2^23, or of 1.5 * 2^23 for a signed one).
+// Words beyond the fast range (|q * 2^-36| >= 2^17) take the 64-bit
+// conversions.
+
+__device__ __forceinline__ float fx_u23(unsigned u) {   // 0 <= u < 2^23: exact
+  return __fsub_rn(__int_as_float(0x4B000000u | u), 8388608.0f);
+}
+
+__device__ __forceinline__ float fx_s22(int s) {   // |s| < 2^22: exact
+  return __fsub_rn(__int_as_float(0x4B400000 + s), 12582912.0f);
+}
+
+// q * 2^-36 = a + b + c exactly; false outside the fast range.
+__device__ __forceinline__ bool fx_split(long long q, float& a, float& b, float& c) {
+  const int hi = (int)(q >> 32);
+  const unsigned lo = (unsigned)q;
+  a = __fmul_rn(fx_s22(hi), 0.0625f);                           // hi * 2^-4
+  b = __fmul_rn(fx_u23(lo >> 9), 7.450580596923828125e-9f);     // 2^-27
+  c = __fmul_rn(fx_u23(lo & 511u), 1.4551915228366852e-11f);    // 2^-36
+  return (unsigned)(hi + (1 << 21)) < (1u << 22);
+}
+
+// One-word fixed-point value q * 2^-36 as a float-float pair (~2^-48).
 __device__ __forceinline__ ff ff_from_fixed(long long q) {
+  float a, b, c;
+  if (fx_split(q, a, b, c)) {
+    // a + b is a multiple of 2^-27 and c < 2^-27: the renormalisation's
+    // ordering condition holds
+    const ff s = two_sum(a, b);
+    return fast_two_sum(s.h, __fadd_rn(s.l, c));
+  }
   const float h = __ll2float_rn(q);
   const long long r = q - __float2ll_rn(h);
   return ff{__fmul_rn(h, 1.4551915228366852e-11f), __fmul_rn(__ll2float_rn(r), 1.4551915228366852e-11f)};
 }
 
+// y rounded to the nearest integer (ties to even), as __float2ll_rn: y is
+// split at a multiple of 2^31 (t, exact) and the remainder y - t (exact,
+// |y - t| <= 2^30) rounded on its own.
+__device__ __forceinline__ long long fx_round(float y) {
+  if (!(fabsf(y) < 6.755399441055744e15f)) return __float2ll_rn(y);   // 1.5 * 2^52 (and NaN)
+  const float t = __fsub_rn(__fadd_rn(y, 2.7021597764222976e16f), 2.7021597764222976e16f);   // 1.5 * 2^54
+  const int hi = __float_as_int(__fadd_rn(__fmul_rn(t, 4.656612873077393e-10f), 12582912.0f)) - 0x4B400000;
+  const int lo = __float2int_rn(__fsub_rn(y, t));
+  return (long long)hi * 2147483648LL + (long long)lo;
+}
+
 // Float-float value rounded to the one-word fixed-point grid (2^-36).
 __device__ __forceinline__ long long fixed_from_ff(ff a) {
-  return __float2ll_rn(__fmul_rn(a.h, 68719476736.0f)) + __float2ll_rn(__fmul_rn(a.l, 68719476736.0f));
+  return fx_round(__fmul_rn(a.h, 68719476736.0f)) + fx_round(__fmul_rn(a.l, 68719476736.0f));
 }
 
 __device__ __forceinline__ ff two_prod(float a, float b) {
@@ -503,6 +573,8 @@ struct WarpWS {
   float* Cs;
   float* tab0;  // shape tables of the step's start: ex hi, ex lo, ey hi, ey lo, xt, yt
   float* tab1;  // trial tables (same layout) / pass-1 gradient tables / solve scratch
+  float* par0;  // float-float parameter slots (g32_params) of the step's start record
+  float* par1;  // ... and of the current trial
   int ts;       // table stride (ROI size rounded up to 32)
   const unsigned short* roi;   // ROI pixel table (packed rx | ry << 8)
 };
@@ -519,7 +591,7 @@ __host__ __device__ inline size_t warp_ws_bytes(const ModelCfg& cfg, int nroi) {
   size_t n = (size_t)((nroi + 31) / 32) * 32;
   size_t b;
   if (gauss32<T>(cfg)) {
-    b = 6 * n * sizeof(float) + 14 * (size_t)table_stride(cfg.roi) * sizeof(float);
+    b = 6 * n * sizeof(float) + 14 * (size_t)table_stride(cfg.roi) * sizeof(float) + 2 * 20 * sizeof(float);
   } else {
     b = ws_pixel_arrays<T>() * n * sizeof(T);
     b += 4 * 64 * sizeof(T) * 2;   // ext/eyt/xt/yt (Gaussian) or 4 delta tables (spline)
@@ -556,7 +628,9 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
     ws.xt = reinterpret_cast<T*>(ws.tab0 + 4 * ts);
     ws.yt = reinterpret_cast<T*>(ws.tab0 + 5 * ts);
     ws.red = ws.tab1;
-    off = 6 * n * sizeof(float) + 14 * (size_t)ts * sizeof(float);
+    ws.par0 = ws.tab0 + 14 * ts;
+    ws.par1 = ws.par0 + 20;
+    off = 6 * n * sizeof(float) + 14 * (size_t)ts * sizeof(float) + 2 * 20 * sizeof(float);
   } else {
     T* t = reinterpret_cast<T*>(base);
     ws.Fb = t;
@@ -573,7 +647,7 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
     ws.eyt = tab + 128;
     ws.xt = tab + 256;
     ws.yt = tab + 384;
-    ws.t1h = ws.t1l = ws.f0g = ws.T2s = ws.Rs = ws.Cs = ws.tab0 = ws.tab1 = nullptr;
+    ws.t1h = ws.t1l = ws.f0g = ws.T2s = ws.Rs = ws.Cs = ws.tab0 = ws.tab1 = ws.par0 = ws.par1 = nullptr;
     ws.ts = 0;
     ws.roi = nullptr;
     off = ws_pixel_arrays<T>() * n * sizeof(T) + 4 * 64 * sizeof(T) * 2;
@@ -595,7 +669,7 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
 
 // Offsets of the first ROI column / row from the peak centre
 // (daoCalcPeakShape dao_fit.c:968-998; the y offset uses xoff, :979) and
-// the widths, as float-float values (a few FP64 instructions per table).
+// the widths, as float-float values.
 struct G32Axes {
   ff xo, yo, wx, wy;
 };
@@ -608,6 +682,53 @@ __device__ __forceinline__ G32Axes g32_axes(const ModelCfg& cfg, const PeakRec& 
   return a;
 }
 
+// The float-float parameters of a Gaussian record that the FP32 step uses,
+// converted lane-parallel into a shared slot table (two floats per slot):
+// lane i computes slot i, so the set costs one pass of FP64 instructions
+// instead of one per value.  An FP64 instruction takes 64 cycles of this
+// part's FP64 pipe whether one lane or 32 execute it.  The values equal
+// g32_axes' and ff_from_double's bit for bit (the same double operations).
+enum { GP_XO = 0, GP_YO, GP_WX, GP_WY, GP_H, GP_BG, GP_GX, GP_GY, GP_DBG, GP_N };
+
+// z_factors' gx (side 0) or gy (side 1), one lane each.
+__device__ __forceinline__ double z_factor_side(const ModelCfg& cfg, const PeakRec& w, int side) {
+  const double c0 = side ? cfg.wy[0] : cfg.wx[0], c1 = side ? cfg.wy[1] : cfg.wx[1];
+  const double c2 = side ? cfg.wy[2] : cfg.wx[2], c3 = side ? cfg.wy[3] : cfg.wx[3];
+  const double c4 = side ? cfg.wy[4] : cfg.wx[4];
+  const double z0 = (w.p[PZ] - c1) / c2;
+  const double z1 = z0 * z0, z2 = z1 * z0;
+  const double zt = 2.0 * z0 + 3.0 * c3 * z1 + 4.0 * c4 * z2;
+  return -2.0 * zt / (c0 * (side ? w.wyt : w.wxt));
+}
+
+// Slots of record w into par[2 * GP_N] (all lanes, warp-uniform).  ref is
+// the record the background change GP_DBG is taken against (nullptr: no
+// GP_DBG); zf: also the Z model's width derivatives GP_GX / GP_GY.
+__device__ inline void g32_params(const ModelCfg& cfg, const PeakRec& w, const PeakRec* ref, bool zf,
+                                  float* par, int lane) {
+  const int sl = lane < GP_N ? lane : GP_H;
+  const int pi = (sl == GP_XO) ? PX : (sl == GP_YO) ? PY : (sl == GP_WX) ? PXW : (sl == GP_WY) ? PYW
+               : (sl == GP_BG || sl == GP_DBG) ? PBG : PH;
+  double v = w.p[pi];
+  double b = 0.0;   // v - 0 is v (a -0.0 stays -0.0)
+  if (sl <= GP_YO) b = (double)(sl == GP_XO ? w.xi : w.yi);
+  else if (sl == GP_DBG && ref) b = ref->p[PBG];
+  v = v - b;
+  if (sl <= GP_YO) v = -v - cfg.xoff;
+  if (zf) {
+    const double g = z_factor_side(cfg, w, sl == GP_GY ? 1 : 0);
+    if (sl == GP_GX || sl == GP_GY) v = g;
+  }
+  const ff f = ff_from_double(v);
+  if (lane < GP_N) {
+    par[2 * lane] = f.h;
+    par[2 * lane + 1] = f.l;
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ ff gpar(const float* par, int slot) { return ff{par[2 * slot], par[2 * slot + 1]}; }
+
 // FP32 Gaussian shape tables: per axis the factor exp(-t^2 w) as a
 // float-float pair and the offset t as a float, all in FP32 instructions.
 // dst layout (stride ts): ex hi, ex lo, ey hi, ey lo, xt, yt.
@@ -616,8 +737,7 @@ __device__ __forceinline__ G32Axes g32_axes(const ModelCfg& cfg, const PeakRec& 
 // above e^30 are taken as e^30: a trial with such a factor has a model value
 // of 1e13 or more at that pixel, an error far above any start error, and is
 // rejected whatever the exact value (as the reference rejects it).
-__device__ inline void g32_tables(const ModelCfg& cfg, const PeakRec& w, float* dst, int ts, int lane) {
-  const G32Axes ax = g32_axes(cfg, w);
+__device__ inline void g32_tables_ax(const ModelCfg& cfg, const G32Axes& ax, float* dst, int ts, int lane) {
   for (int i = lane; i < cfg.roi; i += 32) {
     const ff tx = ff_add_f(ax.xo, (float)i), ty = ff_add_f(ax.yo, (float)i);
     ff argx = ff_neg(ff_mul(ff_mul(tx, tx), ax.wx)), argy = ff_neg(ff_mul(ff_mul(ty, ty), ax.wy));
@@ -632,6 +752,20 @@ __device__ inline void g32_tables(const ModelCfg& cfg, const PeakRec& w, float* 
     dst[4 * ts + i] = tx.h;
     dst[5 * ts + i] = ty.h;
   }
+}
+
+__device__ inline void g32_tables(const ModelCfg& cfg, const PeakRec& w, float* dst, int ts, int lane) {
+  g32_tables_ax(cfg, g32_axes(cfg, w), dst, ts, lane);
+}
+
+// The same tables from a slot table of g32_params.
+__device__ inline void g32_tables_p(const ModelCfg& cfg, const float* par, float* dst, int ts, int lane) {
+  G32Axes ax;
+  ax.xo = gpar(par, GP_XO);
+  ax.yo = gpar(par, GP_YO);
+  ax.wx = gpar(par, GP_WX);
+  ax.wy = gpar(par, GP_WY);
+  g32_tables_ax(cfg, ax, dst, ts, lane);
 }
 
 __device__ __forceinline__ ff g32_psf(const float* tab, int ts, int rx, int ry) {
@@ -1261,7 +1395,7 @@ __device__ __forceinline__ Q2 quant_t(T v);
 template <>
 __device__ __forceinline__ Q2 quant_t<float>(float v) {
   Q2 q;
-  q.h = __float2ll_rn(v * 68719476736.0f);
+  q.h = fx_round(v * 68719476736.0f);
   q.l = 0;
   return q;
 }
@@ -1272,6 +1406,8 @@ __device__ __forceinline__ Q2 quant_t<double>(double v) {
 
 // One-word accumulator value as float (FP32 engine).
 __device__ __forceinline__ float fx_to_float(long long q) {
+  float a, b, c;
+  if (fx_split(q, a, b, c)) return __fadd_rn(a, __fadd_rn(b, c));
   return __ll2float_rn(q) * 1.4551915228366852e-11f;   // 2^-36
 }
 

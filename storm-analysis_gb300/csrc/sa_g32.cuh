@@ -33,15 +33,18 @@ enum { ACT_EVAL = 0, ACT_CONTINUE = 1, ACT_BREAK = 2, ACT_BREAK_ADDED = 3, ACT_E
 //   3d      [ps, ps a1, ps a2, ps b1, ps b2, rqe] (:811-871)
 //   Z       [ps, ps a1, ps b1, ps (a2+b2), rqe] (:883-958)
 template <int M>
-__device__ inline void g32_grad_tables(const ModelCfg& cfg, const PeakRec& w, double gx, double gy,
-                                       float* g, int ts, int lane) {
-  const G32Axes ax = g32_axes(cfg, w);
+__device__ inline void g32_grad_tables(const ModelCfg& cfg, const float* par, float* g, int ts, int lane) {
+  G32Axes ax;
+  ax.xo = gpar(par, GP_XO);
+  ax.yo = gpar(par, GP_YO);
+  ax.wx = gpar(par, GP_WX);
+  ax.wy = gpar(par, GP_WY);
   constexpr bool one_width = (M == M_2DFIXED) || (M == M_2D);
-  const ff H = ff_from_double(w.p[PH]);
+  const ff H = gpar(par, GP_H);
   const ff H2 = ff{2.0f * H.h, 2.0f * H.l};
   const ff HX = ff_mul(H2, ax.wx), HY = ff_mul(H2, one_width ? ax.wx : ax.wy);   // 2 h w
-  const ff NX = (M == M_Z) ? ff_neg(ff_mul(H, ff_from_double(gx))) : ff_neg(H);
-  const ff NY = (M == M_Z) ? ff_neg(ff_mul(H, ff_from_double(gy))) : ff_neg(H);
+  const ff NX = (M == M_Z) ? ff_neg(ff_mul(H, gpar(par, GP_GX))) : ff_neg(H);
+  const ff NY = (M == M_Z) ? ff_neg(ff_mul(H, gpar(par, GP_GY))) : ff_neg(H);
   for (int i = lane; i < cfg.roi; i += 32) {
     const ff tx = ff_add_f(ax.xo, (float)i), ty = ff_add_f(ax.yo, (float)i);
     ff v = ff_mul(HX, tx);
@@ -68,13 +71,63 @@ __device__ __forceinline__ ff shfl_ff(ff v, int src) {
   return ff{__shfl_sync(0xffffffffu, v.h, src), __shfl_sync(0xffffffffu, v.l, src)};
 }
 
-// The FP64 Cholesky of the ff normal equations (lane 0).  Kept out of line:
-// it is the rare path, and its arrays would otherwise weigh on the register
-// allocation of the whole step.
-static __device__ __noinline__ int solve_g32_fallback(const float* jh, int k, double lam, double* out) {
-  double jd[36];
-  for (int i = 0; i < 36; i++) jd[i] = (double)jh[i] + (double)jh[36 + i];
-  return solve_fp64_lane0(jd, k, lam, out);
+// The FP64 Cholesky of the ff normal equations (lane 0), the rare path of
+// solve_g32 (an FP32 pivot <= 0), with the arithmetic of solve_fp64_lane0 /
+// chol_solve.  Its matrix lives in shared scratch s (MAX_JAC^2 + MAX_JAC
+// doubles; the factor overwrites the lower triangle) and its loops are not
+// unrolled, so it adds no registers to the step; an out-of-line call would
+// make the compiler save the step's live registers to the stack around it.
+__device__ inline int solve_g32_fallback(const float* jh, int k, double lam, double* s, double* out) {
+  double* A = s;
+  double* b = s + MAX_JAC * MAX_JAC;
+  int id = k;
+#pragma unroll 1
+  for (int l = 0; l < k; l++) {
+    b[l] = (double)jh[l] + (double)jh[36 + l];
+#pragma unroll 1
+    for (int m = l; m < k; m++) {
+      const double v = (double)jh[id] + (double)jh[36 + id];
+      A[l * MAX_JAC + m] = (l == m) ? (1.0 + lam) * v : v;
+      id++;
+    }
+  }
+#pragma unroll 1
+  for (int j = 0; j < k; j++) {
+    double d = A[j * MAX_JAC + j];
+#pragma unroll 1
+    for (int q = 0; q < j; q++) d = __dsub_rn(d, __dmul_rn(A[j * MAX_JAC + q], A[j * MAX_JAC + q]));
+    if (!(d > 0.0)) return j + 1;
+    d = sqrt(d);
+    A[j * MAX_JAC + j] = d;
+#pragma unroll 1
+    for (int i = j + 1; i < k; i++) {
+      double t = A[j * MAX_JAC + i];
+#pragma unroll 1
+      for (int q = 0; q < j; q++) t = __dsub_rn(t, __dmul_rn(A[i * MAX_JAC + q], A[j * MAX_JAC + q]));
+      A[i * MAX_JAC + j] = t / d;
+    }
+  }
+#pragma unroll 1
+  for (int i = 0; i < k; i++) {
+    double t = b[i];
+#pragma unroll 1
+    for (int q = 0; q < i; q++) t = __dsub_rn(t, __dmul_rn(A[i * MAX_JAC + q], b[q]));
+    b[i] = t / A[i * MAX_JAC + i];
+  }
+#pragma unroll 1
+  for (int i = k - 1; i >= 0; i--) {
+    double t = b[i];
+#pragma unroll 1
+    for (int q = i + 1; q < k; q++) t = __dsub_rn(t, __dmul_rn(A[q * MAX_JAC + i], b[q]));
+    b[i] = t / A[i * MAX_JAC + i];
+  }
+  int st = 0;
+#pragma unroll 1
+  for (int i = 0; i < k; i++) {
+    out[i] = b[i];
+    if (isnan(b[i])) st = 1;
+  }
+  return st;
 }
 
 // Damped solve (H + lam diag H) d = b of the FP32 Gaussian step
@@ -83,13 +136,16 @@ static __device__ __noinline__ int solve_g32_fallback(const float* jh, int k, do
 // own, so the factorisation needs no shuffles; the two refinements compute
 // the residual in float-float a row per lane and gather it to every lane.
 // A pivot <= 0 hands the system to the FP64 Cholesky on lane 0, which
-// decides failure as dposv does.  Solution on lane 0.
+// decides failure as dposv does.  Lane j < K returns component j of the
+// solution in dl (the K conversions to double run lane-parallel); the
+// status is returned on every lane.
 template <int K>
-__device__ inline int solve_g32(WarpWS<float>& ws, double lam, double* out, int lane) {
+__device__ inline int solve_g32(WarpWS<float>& ws, double lam, double& dl, int lane) {
   const float* jh = g32_jh(ws);
   const ff L1 = ff_from_double(1.0 + lam);
   float sc[K], D[K], R[K], L[K][K], c[K];
   int status = 0;
+  dl = 0.0;
 #pragma unroll
   for (int i = 0; i < K; i++) {
     const int id = hes_index(K, i, i);
@@ -157,19 +213,22 @@ __device__ inline int solve_g32(WarpWS<float>& ws, double lam, double* out, int 
 #pragma unroll
       for (int i = 0; i < K; i++) x[i] = ff_add(x[i], two_prod(c[i], sc[i]));
     }
-    if (lane == 0) {
+    ff xl = x[0];
 #pragma unroll
-      for (int j = 0; j < K; j++) {
-        out[j] = ff_to_double(x[j]);
-        if (isnan(x[j].h)) status = 1;   // multi_fit.c:1857-1863
-      }
-    }
+    for (int j = 1; j < K; j++)
+      if (lane == j) xl = x[j];
+    dl = ff_to_double(xl);
+    if (__any_sync(0xffffffffu, lane < K && isnan(xl.h))) status = 1;   // multi_fit.c:1857-1863
   }
-  if (lane == 0 && status == 2) {
-    double o[MAX_JAC];
-    status = solve_g32_fallback(jh, K, lam, o);
-#pragma unroll
-    for (int j = 0; j < K; j++) out[j] = o[j];
+  if (status == 2) {   // the same on every lane (the factorisation is)
+    // scratch: the trial tables, rebuilt after every solve
+    double* scr = reinterpret_cast<double*>(ws.tab1);
+    int st = 0;
+    if (lane == 0) st = solve_g32_fallback(jh, K, lam, scr, scr + MAX_JAC * MAX_JAC + MAX_JAC);
+    __syncwarp();
+    status = __shfl_sync(0xffffffffu, st, 0);
+    dl = scr[MAX_JAC * MAX_JAC + MAX_JAC + (lane < K ? lane : 0)];
+    __syncwarp();
   }
   return status;
 }
@@ -213,7 +272,8 @@ __device__ __forceinline__ void g32_pixel_state(const G32Pix& v, int p, WarpWS<f
   // f0 = rho + x with the data's float-float copy: two int64 conversions
   // fewer per pixel than converting f as well
   const float vx = v.x.x;
-  const ff bgc = ff_div(ff_from_fixed(v.B), ff{(float)v.C, 0.0f});
+  const float cf = fx_s22(v.C);
+  const ff bgc = ff_div(ff_from_fixed(v.B), ff{cf, 0.0f});
   const ff rho = ff_add(ff_from_fixed(v.F - v.X), bgc);
   const ff f0 = ff_add(rho, ff{v.x.x, v.x.y});
   if (!(f0.h > 0.0f)) fail = true;
@@ -225,7 +285,7 @@ __device__ __forceinline__ void g32_pixel_state(const G32Pix& v, int p, WarpWS<f
   if constexpr (M == M_Z) ws.T2s[p] = ff_div(ff_sub(ff{2.0f, 0.0f}, t1), f0).h;
   else ws.T2s[p] = __fdiv_rn(2.0f * vx, f0.h * f0.h);
   ws.Rs[p] = v.rq;
-  ws.Cs[p] = (float)v.C;
+  ws.Cs[p] = cf;
 }
 
 // Pass 1a: the ROI's pixels are loaded G32_GROUP per lane at a time (all
@@ -364,8 +424,8 @@ __device__ inline void g32_delta(const ModelCfg& cfg, const FrameSet<T>& fs, lon
                                  const PeakRec& o, const PeakRec& t, WarpWS<T>& ws, int lane, ff& s1,
                                  float& s2, bool& fail) {
   const int ts = ws.ts;
-  const ff H0 = ff_from_double(o.p[PH]), H1 = ff_from_double(t.p[PH]);
-  const ff DBG = ff_from_double(t.p[PBG] - o.p[PBG]);
+  const ff H0 = gpar(ws.par0, GP_H), H1 = gpar(ws.par1, GP_H);
+  const ff DBG = gpar(ws.par1, GP_DBG);
   for (int p = lane; p < cfg.nroi; p += 32) {
     int rx, ry;
     roi_rc(ws.roi, p, rx, ry);
@@ -404,8 +464,8 @@ __device__ inline float g32_absolute(const ModelCfg& cfg, const FrameSet<T>& fs,
                                      const PeakRec& o, const PeakRec& t, WarpWS<T>& ws, int lane,
                                      bool& fail) {
   const int ts = ws.ts;
-  const float h1 = (float)t.p[PH], bg1 = (float)t.p[PBG];
-  const ff H0 = ff_from_double(o.p[PH]), BG0 = ff_from_double(o.p[PBG]);
+  const float h1 = ws.par1[2 * GP_H], bg1 = ws.par1[2 * GP_BG];   // (float) of the doubles
+  const ff H0 = gpar(ws.par0, GP_H), BG0 = gpar(ws.par0, GP_BG);
   const int dx = t.xi - o.xi, dy = t.yi - o.yi;
   float devf = 0.0f;
   for (int p = lane; p < cfg.nroi; p += 32) {
@@ -428,11 +488,93 @@ __device__ inline float g32_absolute(const ModelCfg& cfg, const FrameSet<T>& fs,
     }
     const float psf = g32_psf(ws.tab1, ts, rx, ry).h;
     const float res = fx_to_float(F - Xq) + h1 * psf * rq +
-                      __fdiv_rn(fx_to_float(B) + bg1 * rq + sc, (float)(C + 1));
+                      __fdiv_rn(fx_to_float(B) + bg1 * rq + sc, fx_s22(C + 1));
     if (!(xv + res > 0.0f)) fail = true;
     else devf += dev_res(res, xv);
   }
   return devf;
+}
+
+// Delta slot j of model M -> its parameter (apply_update's order,
+// dao_fit.c:1777-1880).
+template <int M>
+__device__ __forceinline__ int g32_delta_param(int j) {
+  if constexpr (M == M_3D) return j == 0 ? PH : j == 1 ? PX : j == 2 ? PXW : j == 3 ? PY : j == 4 ? PYW : PBG;
+  if constexpr (M == M_Z) return j == 0 ? PH : j == 1 ? PX : j == 2 ? PY : j == 3 ? PZ : PBG;
+  if constexpr (M == M_2D) return j == 0 ? PH : j == 1 ? PX : j == 2 ? PY : j == 3 ? PXW : PBG;
+  return j == 0 ? PH : j == 1 ? PX : j == 2 ? PY : PBG;
+}
+
+// apply_update + check_for of model M on the trial record t (a copy of
+// the working record, in the warp workspace), one parameter per lane:
+// lane j < K applies delta j (dl) to its parameter with the same double
+// operations -- the Z range clamp and widths from z (dao_fit.c:1828-1880),
+// the ROI re-anchor (mFitUpdate multi_fit.c:1933-1946), mFitCheck and the
+// width clamps of daoCheck2D / daoCheck3D (:1061-1119).  Each FP64
+// instruction then runs once for all parameters.  Returns check_for's code
+// (0 ok, 1 margin, 2 negative height) on every lane.
+template <int M>
+__device__ inline int g32_update(const ModelCfg& cfg, PeakRec& t, double dl, int lane) {
+  constexpr int K = (M == M_2DFIXED) ? 4 : ((M == M_3D) ? 6 : 5);
+  const bool act = lane < K;
+  const int pi = g32_delta_param<M>(act ? lane : 0);
+  double nv = t.p[pi] - dl;
+  if constexpr (M == M_Z) {
+    if (pi == PZ) {
+      if (nv < cfg.zmin) nv = cfg.zmin;
+      if (nv > cfg.zmax) nv = cfg.zmax;
+    }
+  }
+  // re-anchor on the PX and PY lanes
+  const bool axis = act && (pi == PX || pi == PY);
+  int ai = (pi == PY) ? t.yi : t.xi;
+  {
+    const double d = nv - (double)ai;
+    if (axis && ((d < -0.5) || (d > 1.5))) ai = (int)floor(nv);
+  }
+  // widths from the new z: wx on lane 0, wy on lane 1 (widths_from_z)
+  double wt = 0.0, wv = 0.0;
+  if constexpr (M == M_Z) {
+    const double z = __shfl_sync(0xffffffffu, nv, 3);   // delta 3 is PZ
+    const bool sy = (lane == 1);
+    const double c0 = sy ? cfg.wy[0] : cfg.wx[0], c1 = sy ? cfg.wy[1] : cfg.wx[1];
+    const double c2 = sy ? cfg.wy[2] : cfg.wx[2], c3 = sy ? cfg.wy[3] : cfg.wx[3];
+    const double c4 = sy ? cfg.wy[4] : cfg.wx[4];
+    const double z0 = (z - c1) / c2;
+    const double z1 = z0 * z0, z2 = z1 * z0, z3 = z2 * z0;
+    const double tt = 1.0 + z1 + c3 * z2 + c4 * z3;
+    wt = tt * tt;
+    wv = 2.0 / (c0 * tt);
+  }
+  // mFitCheck: the anchors in the image, a non-negative height
+  const int lim = (pi == PY) ? (cfg.ny - cfg.roi) : (cfg.nx - cfg.roi);
+  const bool margin = __any_sync(0xffffffffu, axis && ((ai < 0) || (ai >= lim)));
+  const bool negh = __any_sync(0xffffffffu, act && pi == PH && (nv < 0.0));
+  // width clamps (used only when the check passes; the record is dropped otherwise)
+  double cv = nv;
+  if constexpr (M == M_2D || M == M_3D) {
+    if (pi == PXW || (M == M_3D && pi == PYW)) {
+      if (cv < cfg.wmin) cv = cfg.wmin;
+      else if (cv > cfg.wmax) cv = cfg.wmax;
+    }
+  }
+  if (act) {
+    t.p[pi] = cv;
+    if (M == M_2D && pi == PXW) t.p[PYW] = nv;   // the unclamped x width
+    if (pi == PX) t.xi = ai;
+    if (pi == PY) t.yi = ai;
+  }
+  if constexpr (M == M_Z) {
+    if (lane == 0) {
+      t.wxt = wt;
+      t.p[PXW] = wv;
+    } else if (lane == 1) {
+      t.wyt = wt;
+      t.p[PYW] = wv;
+    }
+  }
+  __syncwarp();
+  return margin ? 1 : (negh ? 2 : 0);
 }
 
 // What the step of a peak needs before it reads the fit image: its record
@@ -447,10 +589,9 @@ __device__ inline void g32_prologue(const ModelCfg& cfg, const PeakRec* recp, Wa
     }
     __syncwarp();
     const PeakRec& orig = *ws.orig;
-    g32_tables(cfg, orig, ws.tab0, ws.ts, lane);
-    double gxd, gyd;
-    z_factors(cfg, M, orig, gxd, gyd);
-    g32_grad_tables<M>(cfg, orig, gxd, gyd, ws.tab1, ws.ts, lane);
+    g32_params(cfg, orig, nullptr, M == M_Z, ws.par0, lane);
+    g32_tables_p(cfg, ws.par0, ws.tab0, ws.ts, lane);
+    g32_grad_tables<M>(cfg, ws.par0, ws.tab1, ws.ts, lane);
     __syncwarp();
   }
 }
@@ -485,7 +626,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     // accepted trial back.  No other warp touches this ROI during the step,
     // so the subtraction is deferred to the write-back, which applies the
     // net change once; the trial evaluations account for it.
-    const ff H0 = ff_from_double(orig.p[PH]), BG0 = ff_from_double(orig.p[PBG]);
+    const ff H0 = gpar(ws.par0, GP_H), BG0 = gpar(ws.par0, GP_BG);
     const double dev0 = warp_sum_ff(devf);
     fail = __any_sync(0xffffffffu, fail);
     {
@@ -550,8 +691,15 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
       if (act == ACT_BREAK) break;
       // damped solve (multi_fit.c:1174-1203), warp-collective
       const double lam = __shfl_sync(0xffffffffu, w.lambda, 0);
-      double b[MAX_JAC];
-      const int info = solve_g32<k>(ws, lam, b, lane);
+      double dl;
+      const int info = solve_g32<k>(ws, lam, dl, lane);
+      int c = 0;
+      if (info == 0) {
+        PeakRec& t = *ws.t;
+        if (lane == 0) t = w;
+        __syncwarp();
+        c = g32_update<M>(cfg, t, dl, lane);
+      }
       if (lane == 0) {
         if (info != 0) {
           ctr[C_DPOSV]++;
@@ -559,10 +707,7 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
           w.lambda = w.lambda * LAMBDA_UP;
           act = ACT_CONTINUE;
         } else {
-          PeakRec& t = *ws.t;
-          t = w;
-          apply_update(cfg, M, t, b);
-          const int c = check_for(cfg, M, t);
+          const PeakRec& t = *ws.t;
           if (c) {
             if (c == 1) ctr[C_MARGIN]++;
             else ctr[C_NEGH]++;
@@ -588,7 +733,8 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
       }
       // -- trial evaluation: shape, add, error (multi_fit.c:1229-1256)
       const PeakRec& wl = *ws.w;
-      g32_tables(cfg, wl, ws.tab1, ts, lane);
+      g32_params(cfg, wl, &orig, false, ws.par1, lane);
+      g32_tables_p(cfg, ws.par1, ws.tab1, ts, lane);
       __syncwarp();
       const bool is_delta = (wl.xi == orig.xi) && (wl.yi == orig.yi);
       double dev;
@@ -656,7 +802,9 @@ __device__ bool lm_step_g32(const ModelCfg& cfg, const FrameSet<T>& fs, long lon
     if (lane == 0) w.added = orig.added - 1 + (added_end ? 1 : 0);
     __syncwarp();
     const PeakRec& wl = *ws.w;
-    const ff H1 = ff_from_double(wl.p[PH]), BG1 = ff_from_double(wl.p[PBG]);
+    // the accepted trial's slots (par1 is the last trial's, and a step
+    // that adds back ends on an accepted trial)
+    const ff H1 = gpar(ws.par1, GP_H), BG1 = gpar(ws.par1, GP_BG);
     if (added_end && wl.xi == orig.xi && wl.yi == orig.yi && cfg.rqe_one && cfg.scmos_zero) {
       // uniform calibration: BG * 1 + 0 at every pixel, quantised once
       // (bit-identical to g32_contrib with rqe 1 and sCMOS 0)

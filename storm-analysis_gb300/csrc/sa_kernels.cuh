@@ -644,13 +644,19 @@ __global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, F
               if (footprints_overlap(bx - ax, by - ay, cfg.roi, dil)) q = e.x;
             }
           }
-          unsigned m = __ballot_sync(0xffffffffu, q >= 0);
+          // each lane reads its own candidate's done flag (one round trip
+          // for all of them); only the ranks not yet done are waited for,
+          // one at a time by the whole warp.  The __syncwarp orders every
+          // lane's later reads after the lanes' acquire loads.
+          const bool pend = (q >= 0) && (ld_acquire(fs.done + base + q) != epoch);
+          unsigned m = __ballot_sync(0xffffffffu, pend);
           while (m && ok) {
             const int src = __ffs(m) - 1;
             m &= m - 1;
             const int qq = __shfl_sync(0xffffffffu, q, src);
             ok = wait_epoch(fs.done + base + qq, epoch, fs.err_flag);
           }
+          __syncwarp();
         }
       }
     }

@@ -9,14 +9,26 @@ namespace sa {
 namespace {
 
 // Workspace of one warp: room for either solver's view of the normal
-// equations (36 doubles, or 72 floats of float-float hi / lo words).
+// equations (36 doubles, or 72 floats of float-float hi / lo words), and the
+// shared scratch of the FP32 Gaussian solver's FP64 fallback (which the LM
+// step lends from its trial tables).
 struct SolveWS {
   double jh[36];
+  double scr[MAX_JAC * MAX_JAC + 2 * MAX_JAC];
 };
 
+// The FP32 Gaussian solver returns component j on lane j: gather it into
+// out on lane 0.
 template <int K>
 __device__ int solve_g32_k(WarpWS<float>& ws, double lam, double* out, int lane) {
-  return solve_g32<K>(ws, lam, out, lane);
+  double dl;
+  const int st = solve_g32<K>(ws, lam, dl, lane);
+#pragma unroll
+  for (int j = 0; j < K; j++) {
+    const double v = __shfl_sync(0xffffffffu, dl, j);
+    if (lane == 0) out[j] = v;
+  }
+  return st;
 }
 
 // engine 0: FP64 Cholesky (the FP64 engine and the fallback of both FP32
@@ -58,6 +70,7 @@ __global__ void k_solve_batch(const double* a, const double* b, int n_sys, int k
   } else if (engine == 1) {
     WarpWS<float> ws{};
     ws.jh = w.jh;
+    ws.tab1 = reinterpret_cast<float*>(w.scr);
     switch (k) {
       case 4: st = solve_g32_k<4>(ws, lam, out, lane); break;
       case 5: st = solve_g32_k<5>(ws, lam, out, lane); break;
