@@ -235,9 +235,20 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
   return fast_two_sum(p, __fmaf_rn(a.l, b, e));
 }
 
-// a / b: one correction of the FP32 quotient (relative error ~1e-14).
+// Hardware reciprocal approximation (rcp.approx, about 1 ulp).  Where its
+// result is corrected afterwards (ff_div) or only scales an FP32 term it
+// replaces the correctly rounded reciprocal, whose slow-path check makes it
+// several times longer on the dependency chain.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// a / b: one correction of the FP32 quotient q1 = a.h / b.h (relative error
+// ~1e-14; the correction absorbs the approximate reciprocal's error).
 __device__ __forceinline__ ff ff_div(ff a, ff b) {
-  const float inv = __frcp_rn(b.h);
+  const float inv = rcp_approx(b.h);
   const float q1 = __fmul_rn(a.h, inv);
   const ff r = ff_sub(a, ff_mul_f(b, q1));
   return fast_two_sum(q1, __fmul_rn(r.h, inv));

@@ -283,34 +283,36 @@ __device__ __forceinline__ void g32_pixel_state(const G32Pix& v, int p, WarpWS<f
   ws.t1l[p] = t1.l;
   ws.f0g[p] = f0.h;
   if constexpr (M == M_Z) ws.T2s[p] = ff_div(ff_sub(ff{2.0f, 0.0f}, t1), f0).h;
-  else ws.T2s[p] = __fdiv_rn(2.0f * vx, f0.h * f0.h);
+  else {
+    const float iv = rcp_approx(f0.h);
+    ws.T2s[p] = (2.0f * vx) * (iv * iv);
+  }
   ws.Rs[p] = v.rq;
   ws.Cs[p] = cf;
 }
 
-// Pass 1a: the ROI's pixels are loaded G32_GROUP per lane at a time (all
-// loads of a group in flight together) and their start state goes to the
-// warp workspace; returns the lane's start error terms.  One pixel at a time
-// measured best: larger groups hold more loaded values in registers than
-// the 80-register budget of six CTAs per SM allows, and spill.
-constexpr int G32_GROUP = 1;
-
+// Pass 1a: the start state of the ROI's pixels into the warp workspace;
+// returns the lane's start error terms.  Software-pipelined: the loads of
+// the lane's next pixel are in flight while this one is computed, which
+// hides one L2 round trip per pixel at the cost of one pixel's loaded
+// values in registers.
 template <int M, typename T>
 __device__ inline void g32_gather(const ModelCfg& cfg, const FrameSet<T>& fs, long long fbase,
                                   const PeakRec& o, WarpWS<T>& ws, int lane, float& devf, bool& fail) {
   if constexpr (sizeof(T) == 4) {
-    for (int p0 = lane; p0 < cfg.nroi; p0 += 32 * G32_GROUP) {
-      G32Pix v[G32_GROUP];
-#pragma unroll
-      for (int j = 0; j < G32_GROUP; j++) {
-        const int p = p0 + 32 * j;
-        if (p < cfg.nroi) g32_load(cfg, fs, fbase, ws.roi, o.xi, o.yi, p, v[j]);
-      }
-#pragma unroll
-      for (int j = 0; j < G32_GROUP; j++) {
-        const int p = p0 + 32 * j;
-        if (p < cfg.nroi) g32_pixel_state<M>(v[j], p, ws, devf, fail);
-      }
+    int p = lane;
+    if (p >= cfg.nroi) return;
+    G32Pix cur;
+    g32_load(cfg, fs, fbase, ws.roi, o.xi, o.yi, p, cur);
+    for (;;) {
+      const int pn = p + 32;
+      const bool more = pn < cfg.nroi;
+      G32Pix nxt;
+      if (more) g32_load(cfg, fs, fbase, ws.roi, o.xi, o.yi, pn, nxt);
+      g32_pixel_state<M>(cur, p, ws, devf, fail);
+      if (!more) break;
+      cur = nxt;
+      p = pn;
     }
   }
 }

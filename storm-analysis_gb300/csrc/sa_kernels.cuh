@@ -539,7 +539,7 @@ __device__ __forceinline__ bool footprints_overlap(int dx, int dy, int roi, int 
 // G32 >= 0: the FP32 Gaussian step (lm_step_g32) of model G32 (one
 // instantiation per model); G32 < 0: lm_step.
 template <typename T, int G32>
-__global__ void __launch_bounds__(128, G32 >= 0 ? 6 : 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
+__global__ void __launch_bounds__(128, 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
   extern __shared__ __align__(16) char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
