@@ -494,7 +494,7 @@ __device__ __forceinline__ double deviance(double fi, double x) {
 // conditioned.
 __device__ __forceinline__ float r_minus_log1p(float r) {
   if (fabsf(r) < 0.5f) {
-    const float u = __fdiv_rn(r, 2.0f + r);
+    const float u = r * rcp_approx(2.0f + r);
     const float u2 = u * u;
     float s = 1.0f / 19.0f;
     s = fmaf(u2, s, 1.0f / 17.0f);
@@ -513,7 +513,7 @@ __device__ __forceinline__ float r_minus_log1p(float r) {
 // Deviance from the residual res = f - x, which the caller computes
 // accurately: 2 x (r - log1p(r)) with r = res / x.
 __device__ __forceinline__ float dev_res(float res, float x) {
-  return 2.0f * x * r_minus_log1p(__fdiv_rn(res, x));
+  return 2.0f * x * r_minus_log1p(res * rcp_approx(x));
 }
 
 __device__ __forceinline__ float deviance(float fi, float x) { return dev_res(fi - x, x); }

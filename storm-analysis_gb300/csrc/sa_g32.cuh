@@ -443,7 +443,7 @@ __device__ inline void g32_delta(const ModelCfg& cfg, const FrameSet<T>& fs, lon
       ff_acc(s1, ff_mul_raw(df, ff{t1h, ws.t1l[p]}));
       // x = f0 (1 - t1 / 2); the second-order term is FP32 anyway
       const float xv = fmaf(-0.5f * t1h, f0, f0);
-      s2 += 2.0f * xv * r_minus_log1p(__fdiv_rn(df.h, f0));
+      s2 += 2.0f * xv * r_minus_log1p(df.h * rcp_approx(f0));
     }
   }
 }
@@ -490,7 +490,7 @@ __device__ inline float g32_absolute(const ModelCfg& cfg, const FrameSet<T>& fs,
     }
     const float psf = g32_psf(ws.tab1, ts, rx, ry).h;
     const float res = fx_to_float(F - Xq) + h1 * psf * rq +
-                      __fdiv_rn(fx_to_float(B) + bg1 * rq + sc, fx_s22(C + 1));
+                      (fx_to_float(B) + bg1 * rq + sc) * rcp_approx(fx_s22(C + 1));
     if (!(xv + res > 0.0f)) fail = true;
     else devf += dev_res(res, xv);
   }
