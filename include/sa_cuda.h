@@ -143,6 +143,36 @@ void cfNewPeaks(saFitData *fit, double *peak_params, char *p_type, int n_peaks);
 /* cubic_fit.c:511 cfCleanup (also frees the spline) */
 void cfCleanup(saFitData *fit);
 
+/* The FFT PSF model.  psf_fft/psf_fft.c (bound by psf_fft/psf_fft_c.py):
+ * a 3D PSF (z_size x y_size x x_size doubles, x fastest), its spectrum and
+ * the middle z plane of the translated PSF, host-side. */
+/* psf_fft.c:310 pFTInitialize */
+void *pFTInitialize(double *psf, int z_size, int y_size, int x_size);
+/* psf_fft.c:89 pFTCleanup */
+void pFTCleanup(void *pfft);
+/* psf_fft.c:372 pFTTranslate */
+void pFTTranslate(void *pfft, double dx, double dy, double dz);
+/* psf_fft.c:116 pFTGetPSF, :147 pFTGetPSFdx, :191 pFTGetPSFdy, :235 pFTGetPSFdz
+ * (y_size x x_size doubles each) */
+void pFTGetPSF(void *pfft, double *psf);
+void pFTGetPSFdx(void *pfft, double *dx);
+void pFTGetPSFdy(void *pfft, double *dy);
+void pFTGetPSFdz(void *pfft, double *dz);
+/* psf_fft.c:274 pFTGetXSize, :282 pFTGetYSize, :290 pFTGetZSize */
+int pFTGetXSize(void *pfft);
+int pFTGetYSize(void *pfft);
+int pFTGetZSize(void *pfft);
+
+/* psf_fft/fft_fit.c (bound by psf_fft/fft_fit_c.py).  The FFT PSF model runs
+ * in the FP64 engine whatever saSetPrecision asked for. */
+/* fft_fit.c:254 ftFitInitialize (psf_fft from pFTInitialize) */
+saFitData *ftFitInitialize(void *psf_fft, double *rqe, double *scmos_calibration, double tol, int im_size_x,
+                           int im_size_y);
+/* fft_fit.c:318 ftFitNewPeaks */
+void ftFitNewPeaks(saFitData *fit, double *peak_params, char *p_type, int n_peaks);
+/* fft_fit.c:165 ftFitCleanup (the PSF object stays the caller's) */
+void ftFitCleanup(saFitData *fit);
+
 /* ---- shared LM core (sa_library/multi_fit.c) ----------------------------- */
 
 /* multi_fit.c:90 mFitAnscombeTransformImage (ALS only; reports an error) */
@@ -282,7 +312,7 @@ int saSetSchedule(saFitData *fit, int dil_late, int dil_switch);
 /* No reference counterpart: when every frame still fitting has at most
  * `peaks` RUNNING peaks left, their remaining sweeps run in one launch, the
  * steps of a frame one after another in index order, instead of three
- * launches and a host poll per sweep (default 4; 0 never).  The results do
+ * launches and a host poll per sweep (default 8; 0 never).  The results do
  * not change.  Returns 0, or -1 on error. */
 int saSetTailPeaks(saFitData *fit, int peaks);
 /* No reference counterpart: the CTA count of the persistent sweep grid at

@@ -19,7 +19,7 @@ from numpy.ctypeslib import ndpointer
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 
-MODELS = {"2dfixed": 0, "2d": 1, "3d": 2, "Z": 3, "spline2D": 4, "spline3D": 5}
+MODELS = {"2dfixed": 0, "2d": 1, "3d": 2, "Z": 3, "spline2D": 4, "spline3D": 5, "fft": 6}
 PEAK_TYPES = {"finder": 0, "testing": 1, "text": 2, "hdf5": 2}
 DPROPS = {"background": 0, "bg_sum": 1, "error": 2, "fg_sum": 3, "height": 4, "sum": 5,
           "x": 6, "xsigma": 7, "y": 8, "ysigma": 9, "z": 10, "jacobian": 11}
@@ -78,6 +78,7 @@ def load():
     lib.oraSplineEval3D.restype = ctypes.c_double
     lib.oraSolve.argtypes = [f64, f64, ctypes.c_int]
     lib.oraSolve.restype = ctypes.c_int
+    lib.oraFFTEval.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, f64, f64, f64, f64]
     _lib = lib
     return lib
 
@@ -100,11 +101,11 @@ class OracleFitter(object):
 
     def __init__(self, model, shape, rqe=None, scmos_cal=None, roi_size=10, sigma_range=None,
                  wx_params=None, wy_params=None, min_z=None, max_z=None, spline=None,
-                 tol=1.0e-6):
+                 tol=1.0e-6, psf=None):
         lib = load()
         self.lib = lib
         self.model = model
-        self.spline = model.startswith("spline")
+        self.spline = model.startswith("spline") or model == "fft"
         ny, nx = shape
         self.shape = (ny, nx)
         rqe = numpy.ones(shape) if rqe is None else rqe
@@ -121,7 +122,14 @@ class OracleFitter(object):
                                      dtype=numpy.float64)
         zmin = 0.0 if min_z is None else float(min_z)
         zmax = 0.0 if max_z is None else float(max_z)
-        if self.spline:
+        if model == "fft":
+            # the PSF's spectrum as pFTInitialize computes it (oracle/psf_fft.py)
+            from . import psf_fft
+            psf = numpy.ascontiguousarray(psf, dtype=numpy.float64)
+            sz, sy, sx = psf.shape
+            spec = psf_fft.PSFFFT(psf).psf_fft
+            aij = numpy.ascontiguousarray(numpy.stack([spec.real, spec.imag], axis=-1)).ravel()
+        elif self.spline:
             coeff = numpy.ascontiguousarray(spline, dtype=numpy.float64)
             sx, sy = coeff.shape[0], coeff.shape[1]
             sz = coeff.shape[2] if coeff.ndim == 4 else 0
@@ -132,6 +140,7 @@ class OracleFitter(object):
         self.h = lib.oraCreate(MODELS[model], rqe, scmos_cal, tol, nx, ny, roi_size, wmin, wmax,
                                wx, wy, zmin, zmax, numpy.ascontiguousarray(aij), sx, sy, sz)
         self.iterations = 0
+        self.psf_shape = None if psf is None else numpy.asarray(psf).shape
 
     def cleanup(self, verbose=False):
         if self.h:
@@ -241,3 +250,12 @@ def fit_frames(workload, indices, max_iterations=200, props=("x", "y", "z", "hei
         results.append({p: fitter.getPeakProperty(p) for p in props})
     fitter.cleanup()
     return results
+
+
+def fft_eval(fitter, dx, dy, dz):
+    """The FFT PSF model's PSF and x, y, z derivatives on the PSF grid for a
+    translation, as the oracle's fitter evaluates them."""
+    ny, nx = fitter.psf_shape[1], fitter.psf_shape[2]
+    out = [numpy.zeros(ny * nx) for _ in range(4)]
+    fitter.lib.oraFFTEval(fitter.h, dx, dy, dz, *out)
+    return [o.reshape(ny, nx) for o in out]

@@ -20,6 +20,9 @@
 
 #include "sa_oracle.h"
 
+/* pi as the reference's M_PI (not defined under -std=c99) */
+#define ORA_PI 3.14159265358979323846
+
 /* Parameter slots (multi_fit.h:20-26). */
 enum { PH = 0, PX = 1, PXW = 2, PY = 3, PYW = 4, PBG = 5, PZ = 6 };
 
@@ -55,7 +58,8 @@ struct oraFit {
   double xoff, yoff, zoff, tol, min_height;
   double wmin, wmax, zmin, zmax, wx[5], wy[5];
   int sx, sy, sz;
-  double *aij;
+  double *aij;            /* spline coefficients; ORA_FFT: the PSF spectrum (re, im) */
+  double *fft_tw;         /* ORA_FFT: twiddle tables, see fft_eval */
   double *rqe, *scmos, *x, *f, *bg, *bgest, *err, *tfi;
   int *cnt, *stale;
   OPeak *pk;
@@ -85,6 +89,8 @@ static void peak_copy(const oraFit *fit, OPeak *dst, const OPeak *src)
   memcpy(dst->psf, src->psf, sizeof(double) * fit->nroi);
   memcpy(shape_tabs(fit, dst), shape_tabs(fit, src), sizeof(double) * 4 * fit->roi);
 }
+
+static int is_fft(const oraFit *fit) { return fit->model == ORA_FFT; }
 
 static int is_spline(const oraFit *fit)
 {
@@ -253,11 +259,159 @@ static void widths_from_z(const oraFit *fit, OPeak *pk)
   pk->p[PYW] = 2.0 / (fit->wy[0] * t);
 }
 
+/* ORA_FFT: the translated PSF and its x, y, z derivatives on the PSF's
+ * x-y grid, the middle z plane of the c2r inverse of the translated
+ * spectrum (pFTTranslate psf_fft.c:372-420, pFTGetPSF :116-137,
+ * pFTGetPSFdx/dy/dz :147-272).  Evaluated separably: for each (ky, kx) the
+ * z sum, then for each (y, kx) the y sum, then for each (y, x) the x sum
+ * with the c2r weights (1 for the DC and Nyquist bins of x, whose
+ * imaginary parts the c2r drops, 2 otherwise).  Shift vectors as
+ * pFTCalcShiftVector :43-60 (the z shift with -dz), derivative factors as
+ * pFTCalcShiftVectorDerivative :70-84 (the spectrum times -i d). */
+static void shift_vec(double dx, int size, double *re, double *im)
+{
+  int i;
+  double t1 = -ORA_PI * 2.0 * dx / ((double)size);
+  re[0] = 1.0;
+  im[0] = 0.0;
+  for (i = 1; i < (size / 2 + 1); i++) {
+    double t2 = t1 * (double)i;
+    double tr = cos(t2), tc = sin(t2);
+    re[size - i] = tr;
+    re[i] = tr;
+    im[size - i] = -tc;
+    im[i] = tc;
+  }
+}
+
+static void shift_deriv(int size, double *d)
+{
+  int i;
+  double t1 = -ORA_PI * 2.0 / ((double)size);
+  d[0] = 0.0;
+  for (i = 1; i < (size / 2 + 1); i++) {
+    double t2 = t1 * (double)i;
+    d[size - i] = t2;
+    d[i] = -t2;
+  }
+}
+
+/* e^{2 pi i k n / N} with k n reduced mod N first */
+static void twiddle(long k, long n, long N, double *re, double *im)
+{
+  double a = 2.0 * ORA_PI * (double)((k * n) % N) / (double)N;
+  *re = cos(a);
+  *im = sin(a);
+}
+
+static void fft_eval(const oraFit *fit, double dx, double dy, double dz,
+                     double *psf, double *gx, double *gy, double *gz)
+{
+  int nx = fit->sx, ny = fit->sy, nz = fit->sz, nk = nx / 2 + 1, zm = nz / 2;
+  int kz, ky, kx, y, x;
+  double *sxr = malloc(sizeof(double) * 6 * 64), *sxi = sxr + 64, *syr = sxr + 128, *syi = sxr + 192,
+         *szr = sxr + 256, *szi = sxr + 320;
+  double dkx[64], dky[64], dkz[64];
+  double *Cr = calloc((size_t)ny * nk * 10, sizeof(double));
+  double *Ci = Cr + ny * nk, *Czr = Ci + ny * nk, *Czi = Czr + ny * nk;
+  double *Dr = Czi + ny * nk, *Di = Dr + ny * nk, *Dyr = Di + ny * nk, *Dyi = Dyr + ny * nk;
+  double *Dzr = Dyi + ny * nk, *Dzi = Dzr + ny * nk;
+  shift_vec(dx, nx, sxr, sxi);
+  shift_vec(dy, ny, syr, syi);
+  shift_vec(-dz, nz, szr, szi);
+  shift_deriv(nx, dkx);
+  shift_deriv(ny, dky);
+  shift_deriv(nz, dkz);
+  for (ky = 0; ky < ny; ky++) {
+    for (kx = 0; kx < nk; kx++) {
+      double cr = 0.0, ci = 0.0, czr = 0.0, czi = 0.0;
+      for (kz = 0; kz < nz; kz++) {
+        const double *w = fit->aij + 2 * (((size_t)kz * ny + ky) * nk + kx);
+        double r1 = w[0], c1 = w[1], r2, c2, er, ei, pr, pi;
+        /* z, y, x shifts in the reference's order */
+        r2 = r1 * szr[kz] - c1 * szi[kz];
+        c2 = r1 * szi[kz] + c1 * szr[kz];
+        r1 = r2 * syr[ky] - c2 * syi[ky];
+        c1 = r2 * syi[ky] + c2 * syr[ky];
+        r2 = r1 * sxr[kx] - c1 * sxi[kx];
+        c2 = r1 * sxi[kx] + c1 * sxr[kx];
+        twiddle(kz, zm, nz, &er, &ei);
+        pr = r2 * er - c2 * ei;
+        pi = r2 * ei + c2 * er;
+        cr += pr;
+        ci += pi;
+        /* times -i dkz: (pr, pi) -> (pi dkz, -pr dkz) */
+        czr += pi * dkz[kz];
+        czi -= pr * dkz[kz];
+      }
+      Cr[ky * nk + kx] = cr; Ci[ky * nk + kx] = ci;
+      Czr[ky * nk + kx] = czr; Czi[ky * nk + kx] = czi;
+    }
+  }
+  for (y = 0; y < ny; y++) {
+    for (kx = 0; kx < nk; kx++) {
+      double dr = 0.0, di = 0.0, dyr = 0.0, dyi = 0.0, dzr = 0.0, dzi = 0.0;
+      for (ky = 0; ky < ny; ky++) {
+        double er, ei, ar = Cr[ky * nk + kx], ai = Ci[ky * nk + kx], pr, pi;
+        twiddle(ky, y, ny, &er, &ei);
+        pr = ar * er - ai * ei;
+        pi = ar * ei + ai * er;
+        dr += pr;
+        di += pi;
+        dyr += pi * dky[ky];
+        dyi -= pr * dky[ky];
+        ar = Czr[ky * nk + kx]; ai = Czi[ky * nk + kx];
+        dzr += ar * er - ai * ei;
+        dzi += ar * ei + ai * er;
+      }
+      Dr[y * nk + kx] = dr; Di[y * nk + kx] = di;
+      Dyr[y * nk + kx] = dyr; Dyi[y * nk + kx] = dyi;
+      Dzr[y * nk + kx] = dzr; Dzi[y * nk + kx] = dzi;
+    }
+  }
+  for (y = 0; y < ny; y++) {
+    for (x = 0; x < nx; x++) {
+      double vp = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+      for (kx = 0; kx < nk; kx++) {
+        double er, ei, c = ((kx == 0) || (2 * kx == nx)) ? 1.0 : 2.0;
+        double pr, pi;
+        twiddle(kx, x, nx, &er, &ei);
+        pr = Dr[y * nk + kx] * er - Di[y * nk + kx] * ei;
+        pi = Dr[y * nk + kx] * ei + Di[y * nk + kx] * er;
+        vp += c * pr;
+        vx += c * pi * dkx[kx];   /* Re((pr + i pi)(-i dkx)) */
+        vy += c * (Dyr[y * nk + kx] * er - Dyi[y * nk + kx] * ei);
+        vz += c * (Dzr[y * nk + kx] * er - Dzi[y * nk + kx] * ei);
+      }
+      if (psf) psf[y * nx + x] = vp;
+      if (gx) gx[y * nx + x] = vx;
+      if (gy) gy[y * nx + x] = vy;
+      if (gz) gz[y * nx + x] = -vz;
+    }
+  }
+  free(Cr);
+  free(sxr);
+}
+
+/* Exported for the tests of the evaluation itself. */
+void oraFFTEval(const oraFit *fit, double dx, double dy, double dz, double *psf, double *gx, double *gy, double *gz)
+{
+  fft_eval(fit, dx, dy, dz, psf, gx, gy, gz);
+}
+
 /* Peak shape into pk->psf: daoCalcPeakShape dao_fit.c:968-998 (note the
  * y offset also uses xoff, :979), cfCalcPeakShape cubic_fit.c:435-502. */
 static void peak_shape(const oraFit *fit, OPeak *pk)
 {
   int i;
+  if (is_fft(fit)) {
+    /* ftFitCalcPeakShape fft_fit.c:127-155 */
+    double *grid = malloc(sizeof(double) * fit->sx * fit->sy);
+    fft_eval(fit, pk->p[PX] - (double)pk->xi, pk->p[PY] - (double)pk->yi, pk->p[PZ], grid, NULL, NULL, NULL);
+    for (i = 0; i < fit->nroi; i++) pk->psf[i] = grid[fit->ry[i] * fit->sx + fit->rx[i]];
+    free(grid);
+    return;
+  }
   if (!is_spline(fit)) {
     double *xt = shape_tabs(fit, pk), *ext = xt + fit->roi, *yt = xt + 2 * fit->roi, *eyt = xt + 3 * fit->roi;
     double xo, yo;
@@ -365,10 +519,18 @@ static void calc_jh(const oraFit *fit, const OPeak *pk, double *jac, double *hes
   double df3[64], dx3[64], dy3[64], dz3[64];
   double df2[16], dx2[16], dy2[16];
 
+  double *fg = NULL;   /* ORA_FFT: x, y, z derivative grids */
+
   for (l = 0; l < n; l++) jac[l] = 0.0;
   for (l = 0; l < n * n; l++) hes[l] = 0.0;
 
-  if (!is_spline(fit)) {
+  if (is_fft(fit)) {
+    /* ftFitCalcJH3D fft_fit.c:43-117: translate, then the derivatives */
+    size_t ng = (size_t)fit->sx * fit->sy;
+    fg = malloc(sizeof(double) * 3 * ng);
+    fft_eval(fit, pk->p[PX] - (double)pk->xi, pk->p[PY] - (double)pk->yi, pk->p[PZ], NULL, fg, fg + ng,
+             fg + 2 * ng);
+  } else if (!is_spline(fit)) {
     /* the shape tables of the peak's current state (peak_shape) */
     if (fit->model == ORA_Z) {
       /* d width / d z terms, dao_fit.c:904-916. */
@@ -431,6 +593,15 @@ static void calc_jh(const oraFit *fit, const OPeak *pk, double *jac, double *hes
       jt[4] = rq;
       break;
     }
+    case ORA_FFT: {
+      size_t ng = (size_t)fit->sx * fit->sy, g = (size_t)ry * fit->sx + rx;
+      jt[0] = rq * pk->psf[j];
+      jt[1] = rq * h * fg[g];
+      jt[2] = rq * h * fg[ng + g];
+      jt[3] = rq * h * fg[2 * ng + g];
+      jt[4] = rq;
+      break;
+    }
     case ORA_SPLINE3D: {
       const double *c = cell3d(fit, pk->zi, ry + pk->ys, rx + pk->xs);
       jt[0] = rq * pk->psf[j];
@@ -455,6 +626,7 @@ static void calc_jh(const oraFit *fit, const OPeak *pk, double *jac, double *hes
     for (l = 0; l < n; l++)
       for (m = l; m < n; m++) hes[l * n + m] += t2 * jt[l] * jt[m];
   }
+  free(fg);
 }
 
 /* Parameter update from the solved step, in each model's delta order:
@@ -495,6 +667,15 @@ static void apply_update(const oraFit *fit, OPeak *pk, const double *d)
     anchor_update(pk);
     widths_from_z(fit, pk);
     break;
+  case ORA_FFT: {
+    /* ftFitUpdate3D fft_fit.c:481-497, ftFitZRangeCheck :506-524 */
+    double max_z = ((double)fit->sz) * 0.5 - 1.0e-12;
+    pk->p[PH] -= d[0]; pk->p[PX] -= d[1]; pk->p[PY] -= d[2]; pk->p[PZ] -= d[3]; pk->p[PBG] -= d[4];
+    anchor_update(pk);
+    if (pk->p[PZ] < -max_z) pk->p[PZ] = -max_z;
+    if (pk->p[PZ] > max_z) pk->p[PZ] = max_z;
+    break;
+  }
   default: { /* ORA_SPLINE3D */
     double zmax;
     pk->p[PH] -= d[0]; pk->p[PX] -= d[1]; pk->p[PY] -= d[2]; pk->p[PZ] -= d[3]; pk->p[PBG] -= d[4];
@@ -615,7 +796,16 @@ oraFit *oraCreate(int model, const double *rqe, const double *scmos, double tol,
   case ORA_SPLINE2D: fit->jac = 4; break;
   default: fit->jac = 5; break;
   }
-  if (!is_spline(fit)) {
+  if (is_fft(fit)) {
+    /* ftFitInitialize fft_fit.c:254-310: ROI = PSF x size */
+    size_t nc = (size_t)sz * sy * (sx / 2 + 1) * 2;
+    fit->sx = sx; fit->sy = sy; fit->sz = sz;
+    fit->aij = (double *)malloc(sizeof(double) * nc);
+    memcpy(fit->aij, aij, sizeof(double) * nc);
+    fit->xoff = 0.5 * ((double)sx) - 1.0;
+    fit->yoff = 0.5 * ((double)sy) - 1.0;
+    roi_index(fit, sx);
+  } else if (!is_spline(fit)) {
     /* daoInitialize dao_fit.c:1251-1309 */
     roi_index(fit, roi_size);
     fit->xoff = 0.5 * ((double)roi_size) - 1.0;
@@ -743,7 +933,9 @@ static void grow_peaks(oraFit *fit, int n_new)
 /* daoNewPeaks dao_fit.c:1582-1766 and cfNewPeaks cubic_fit.c:758-928. */
 void oraNewPeaks(oraFit *fit, const double *peaks, int ptype, int n_peaks)
 {
-  int i, start, stop, spline = is_spline(fit);
+  /* arbitrary-PSF input formats (x, y, z [, background, height]) for the
+   * splines and the FFT PSF (cubic_fit.c:776-914, fft_fit.c:318-470) */
+  int i, start, stop, spline = is_spline(fit) || is_fft(fit);
   int ncol;
   grow_peaks(fit, n_peaks);
   start = fit->nfit;
@@ -786,7 +978,7 @@ void oraNewPeaks(oraFit *fit, const double *peaks, int ptype, int n_peaks)
     }
     pk->xi = (int)floor(pk->p[PX]);
     pk->yi = (int)floor(pk->p[PY]);
-    if (spline) pk->zi = (int)pk->p[PZ];
+    if (is_spline(fit)) pk->zi = (int)pk->p[PZ];
     if (ptype != ORA_PEAKS_TEXT) {
       pk->p[PBG] = 1.0;
       pk->p[PH] = 1.0;
@@ -896,7 +1088,7 @@ void oraIterate(oraFit *fit)
         continue;
       }
       apply_update(fit, w, wjac);
-      if (is_spline(fit) ? base_check(fit, w) : model_check(fit, w)) {
+      if ((is_spline(fit) || is_fft(fit)) ? base_check(fit, w) : model_check(fit, w)) {
         reset_working(fit, i);
         w->status = ERROR;
         continue;

@@ -23,6 +23,7 @@
 #define ORA_Z         3   /* dao_fit.c daoInitializeZ       */
 #define ORA_SPLINE2D  4   /* cubic_fit.c cfInitialize2D     */
 #define ORA_SPLINE3D  5   /* cubic_fit.c cfInitialize3D     */
+#define ORA_FFT       6   /* psf_fft/fft_fit.c ftFitInitialize: FFT-translated 3D PSF */
 
 /* Peak input formats (dao_fit.c:1603-1753, cubic_fit.c:776-914). */
 #define ORA_PEAKS_FINDER   0
@@ -54,7 +55,11 @@ typedef struct oraFit oraFit;
  *   roi_size      Gaussian ROI size (ignored for splines: ROI = spline size - 1).
  *   wmin, wmax    width clamp for 2D/3D (width = 1/(2 sigma^2)).
  *   wx, wy        5 defocus-curve parameters [w0, c, d, A, B] for Z.
- *   aij, sx..sz   spline coefficients (sx*sy*sz*64 for 3D, sx*sy*16 for 2D).
+ *   aij, sx..sz   spline coefficients (sx*sy*sz*64 for 3D, sx*sy*16 for 2D);
+ *                 for ORA_FFT the PSF's r2c spectrum (pFTInitialize
+ *                 psf_fft.c:253-318: the transform of psf / (sz*sy*sx)) as
+ *                 (re, im) pairs, sz x sy x (sx/2 + 1), and the PSF's x, y,
+ *                 z sizes in sx, sy, sz.
  */
 oraFit *oraCreate(int model, const double *rqe, const double *scmos, double tol,
                   int nx, int ny, int roi_size,

@@ -6,11 +6,13 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "sa_launch.h"
+#include "sa_psf_fft.h"
 #include "sa_cuda.h"
 
 using namespace sa;
@@ -115,6 +117,7 @@ struct Engine {
   FrameCtl* d_ctl = nullptr;
   int* d_cellstart = nullptr;
   unsigned* d_err = nullptr;
+  int* d_epoch = nullptr;   // the sweep epoch, advanced on the device by k_post
   unsigned short* d_roi = nullptr;
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
@@ -134,10 +137,10 @@ struct Engine {
 
   // scheduling
   cudaStream_t stream = 0;
-  int epoch = 0;
+  cudaStream_t own_stream = nullptr;   // created for graph capture when no stream was set
   int sweep_grid = 0;
   int sweep_ctas_cap = 0;   // 0: the full persistent grid
-  int tail_peaks = 4;       // k_tail for frames with at most this many RUNNING peaks (0: never)
+  int tail_peaks = 8;       // k_tail for frames with at most this many RUNNING peaks (0: never)
   size_t sweep_smem = 0, cta_smem = 0, warp_smem = 0;
   bool configured = false;
 
@@ -167,6 +170,10 @@ struct Engine {
   ~Engine() {
     release();
     release_poll_buffers();
+    if (own_stream) {
+      cudaStreamSynchronize(own_stream);
+      cudaStreamDestroy(own_stream);
+    }
     if (h_ctl) cudaFreeHost(h_ctl);
     if (ev_poll) cudaEventDestroy(ev_poll);
   }
@@ -179,7 +186,8 @@ struct Engine {
   void release() {
     release_peaks();
     dfree(d_x); dfree(d_xq); dfree(d_xff); dfree(d_rqe); dfree(d_scmos); dfree(d_aij); dfree(d_f); dfree(d_bg); dfree(d_cnt);
-    dfree(d_bgest); dfree(d_ctl); dfree(d_cellstart); dfree(d_err); dfree(d_roi); dfree(d_stage);
+    dfree(d_bgest); dfree(d_ctl); dfree(d_cellstart); dfree(d_err); dfree(d_epoch); dfree(d_roi); dfree(d_stage);
+    release_graphs();
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     ev0 = ev1 = nullptr;
@@ -193,7 +201,7 @@ struct Engine {
 
   template <typename T>
   FrameSet<T> fs() const {
-    FrameSet<T> s;
+    FrameSet<T> s{};   // zeroed padding: the burst graphs compare it bytewise
     s.F = F;
     s.npix = npix;
     s.x = (const T*)d_x;
@@ -213,6 +221,7 @@ struct Engine {
     s.run = d_run;
     s.anchor0 = d_anchor;
     s.done = d_done;
+    s.epoch = d_epoch;
     s.cell_start = d_cellstart;
     s.cell_items = d_cellitems;
     s.stepctr = d_stepctr;
@@ -249,6 +258,8 @@ struct Engine {
       set_error("the fitting model has not been initialised");
       return -1;
     }
+    // the FFT PSF model runs in the FP64 engine only
+    if (cfg.model == M_FFT) prec = 64;
     cudaError_t e = (prec == 32) ? Launch<float>::configure(cfg, &sweep_grid, &sweep_smem, &cta_smem, &warp_smem)
                                  : Launch<double>::configure(cfg, &sweep_grid, &sweep_smem, &cta_smem, &warp_smem);
     if (e != cudaSuccess) {
@@ -288,10 +299,18 @@ struct Engine {
       CK(cudaMalloc(&d_err, sizeof(unsigned)));
       CK(cudaMemset(d_err, 0, sizeof(unsigned)));
     }
+    if (!d_epoch) {
+      // done flags start at -1 (d_done is memset to 0xff), epochs at 1
+      const int one = 1;
+      CK(cudaMalloc(&d_epoch, sizeof(int)));
+      CK(cudaMemcpy(d_epoch, &one, sizeof(int), cudaMemcpyHostToDevice));
+    }
     if (!d_rqe) {
       if (upload_t(&d_rqe, rqe_h.data(), npix)) return -1;
       if (upload_t(&d_scmos, scmos_h.data(), npix)) return -1;
       if (!aij_h.empty() && upload_t(&d_aij, aij_h.data(), aij_h.size())) return -1;
+      // the FFT model's tables (FP64: d_aij holds them as doubles)
+      if (cfg.model == M_FFT) cfg.fft = static_cast<const double*>(d_aij);
       CK(cudaMalloc(&d_roi, roi_xy.size() * sizeof(unsigned short)));
       CK(cudaMemcpy(d_roi, roi_xy.data(), roi_xy.size() * sizeof(unsigned short), cudaMemcpyHostToDevice));
     }
@@ -389,17 +408,15 @@ struct Engine {
     if (prec == 32) {
       FrameSet<float> s = fs<float>();
       CK(Launch<float>::prepare(cfg, s, cta_smem, stream));
-      epoch++;
       if (timing) CK(cudaEventRecord(ta, stream));
-      CK(Launch<float>::sweep(cfg, s, epoch, grid(), sweep_smem, stream));
+      CK(Launch<float>::sweep(cfg, s, grid(), sweep_smem, stream));
       if (timing) CK(cudaEventRecord(tb, stream));
       CK(Launch<float>::post(cfg, s, cta_smem, stream));
     } else {
       FrameSet<double> s = fs<double>();
       CK(Launch<double>::prepare(cfg, s, cta_smem, stream));
-      epoch++;
       if (timing) CK(cudaEventRecord(ta, stream));
-      CK(Launch<double>::sweep(cfg, s, epoch, grid(), sweep_smem, stream));
+      CK(Launch<double>::sweep(cfg, s, grid(), sweep_smem, stream));
       if (timing) CK(cudaEventRecord(tb, stream));
       CK(Launch<double>::post(cfg, s, cta_smem, stream));
     }
@@ -485,6 +502,7 @@ struct Engine {
   }
 
   void release_poll_buffers() {
+    release_graphs();
     for (int b = 0; b < 2; b++) {
       if (h_pctl[b]) cudaFreeHost(h_pctl[b]);
       if (ev_pb[b]) cudaEventDestroy(ev_pb[b]);
@@ -496,9 +514,130 @@ struct Engine {
     pctl_n = 0;
   }
 
+  // Bursts as CUDA graphs: the two ticks, the poll copies and the event of
+  // poll buffer b are captured once and relaunched as one graph while
+  // nothing they were captured with changes (model configuration, the frame
+  // set's device arrays, launch shapes, poll buffers); anything else
+  // re-captures.  The sweep epoch lives on the device (k_post advances
+  // it), so the captured launches need no per-tick arguments.  With timing
+  // on, or SA_CUDA_GRAPHS=0 in the environment, bursts are launched
+  // kernel by kernel.
+  cudaGraphExec_t burst_exec[2] = {nullptr, nullptr};
+  std::vector<unsigned char> burst_sig[2];
+  bool use_graphs = !(getenv("SA_CUDA_GRAPHS") && getenv("SA_CUDA_GRAPHS")[0] == '0');
+
+  void release_graphs() {
+    for (int b = 0; b < 2; b++) {
+      if (burst_exec[b]) cudaGraphExecDestroy(burst_exec[b]);
+      burst_exec[b] = nullptr;
+      burst_sig[b].clear();
+    }
+  }
+
+  std::vector<unsigned char> burst_signature(int b) const {
+    std::vector<unsigned char> v;
+    auto put = [&v](const void* p, size_t n) {
+      const unsigned char* c = static_cast<const unsigned char*>(p);
+      v.insert(v.end(), c, c + n);
+    };
+    put(&cfg, sizeof(cfg));
+    if (prec == 32) {
+      const FrameSet<float> s = fs<float>();
+      put(&s, sizeof(s));
+    } else {
+      const FrameSet<double> s = fs<double>();
+      put(&s, sizeof(s));
+    }
+    const int g = grid();
+    put(&g, sizeof(g));
+    put(&prec, sizeof(prec));
+    put(&sweep_smem, sizeof(sweep_smem));
+    put(&cta_smem, sizeof(cta_smem));
+    put(&h_pctl[b], sizeof(h_pctl[b]));
+    put(&h_perr, sizeof(h_perr));
+    put(&ev_pb[b], sizeof(ev_pb[b]));
+    put(&stream, sizeof(stream));
+    return v;
+  }
+
+  // The stream work of one burst (captured; no early return, so that the
+  // capture is always ended).
+  cudaError_t enqueue_burst(int b) {
+    cudaError_t err = cudaSuccess;
+    auto keep = [&err](cudaError_t e) {
+      if (err == cudaSuccess) err = e;
+    };
+    for (int i = 0; i < 2; i++) {
+      if (prec == 32) {
+        const FrameSet<float> s = fs<float>();
+        keep(Launch<float>::prepare(cfg, s, cta_smem, stream));
+        keep(Launch<float>::sweep(cfg, s, grid(), sweep_smem, stream));
+        keep(Launch<float>::post(cfg, s, cta_smem, stream));
+      } else {
+        const FrameSet<double> s = fs<double>();
+        keep(Launch<double>::prepare(cfg, s, cta_smem, stream));
+        keep(Launch<double>::sweep(cfg, s, grid(), sweep_smem, stream));
+        keep(Launch<double>::post(cfg, s, cta_smem, stream));
+      }
+    }
+    keep(cudaMemcpy2DAsync(h_pctl[b], sizeof(FrameCtl), d_ctl, sizeof(FrameCtl), offsetof(FrameCtl, escaped), F,
+                           cudaMemcpyDeviceToHost, stream));
+    keep(cudaMemcpyAsync(h_perr + b, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+    // an event record node (a plain record under capture only marks the
+    // capture's dependencies and cannot be waited on afterwards)
+    keep(cudaEventRecordWithFlags(ev_pb[b], stream, cudaEventRecordExternal));
+    return err;
+  }
+
+  // Launch burst b as a graph; 1 when graphs are not available here (the
+  // caller launches kernel by kernel), -1 on error.
+  int burst_graph(int b) {
+    if (stream == 0) {
+      // the legacy default stream cannot be captured: a blocking stream of
+      // our own keeps the same ordering with work on the legacy stream
+      if (!own_stream && cudaStreamCreate(&own_stream) != cudaSuccess) {
+        cudaGetLastError();
+        use_graphs = false;
+        return 1;
+      }
+      stream = own_stream;
+    }
+    std::vector<unsigned char> sig = burst_signature(b);
+    if (!burst_exec[b] || sig != burst_sig[b]) {
+      if (burst_exec[b]) cudaGraphExecDestroy(burst_exec[b]);
+      burst_exec[b] = nullptr;
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        use_graphs = false;
+        return 1;
+      }
+      cudaError_t err = enqueue_burst(b);
+      const cudaError_t e2 = cudaStreamEndCapture(stream, &g);
+      if (err == cudaSuccess) err = e2;
+      if (err == cudaSuccess) err = cudaGraphInstantiate(&burst_exec[b], g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (err != cudaSuccess) {
+        cudaGetLastError();
+        burst_exec[b] = nullptr;
+        use_graphs = false;
+        return 1;
+      }
+      burst_sig[b] = sig;
+    }
+    CK(cudaGraphLaunch(burst_exec[b], stream));
+    ticks += 2;
+    launches += 6;
+    return 0;
+  }
+
   // Two ticks, then the frame control blocks and the error flag into
   // pinned buffer b, then its event.
   int burst_poll(int b) {
+    if (use_graphs && !timing) {
+      const int r = burst_graph(b);
+      if (r <= 0) return r;
+    }
     for (int i = 0; i < 2; i++)
       if (tick()) return -1;
     // the fields before the device-only lists of every frame's block
@@ -1121,6 +1260,51 @@ void cfCleanup(saFitData* h) {
   }
   daoCleanup(h);
 }
+
+// ---- the FFT PSF fitter (psf_fft/fft_fit.c; psf_fft/fft_fit_c.py binds it) ----
+
+// ftFitInitialize fft_fit.c:254-310: the ROI is the PSF's x size (square in
+// x / y), xoff = x_size / 2 - 1, yoff = y_size / 2 - 1, five parameters
+// (height, x, y, z, background).  The handle keeps the PSF's device tables;
+// the FFT model runs in the FP64 engine.
+saFitData* ftFitInitialize(void* psf_fft, double* rqe, double* scmos, double tol, int nx, int ny) {
+  const PsfFFTH* p = reinterpret_cast<const PsfFFTH*>(psf_fft);
+  if (!p) {
+    set_error("ftFitInitialize: NULL psf_fft");
+    return nullptr;
+  }
+  if (p->nx != p->ny) {
+    // The reference exits the process here (fft_fit.c:283-286).
+    set_error("PSF must be square in X/Y!");
+    return nullptr;
+  }
+  if (p->nx < 2 || p->nx > MAX_ROI || p->nz < 1 || p->nz > 64) {
+    set_error("unsupported PSF size %d x %d x %d", p->nz, p->ny, p->nx);
+    return nullptr;
+  }
+  saFitData* h = new_handle(rqe, scmos, tol, nx, ny);
+  if (!h) return nullptr;
+  Engine* e = E(h);
+  e->prec = 64;
+  e->cfg.sx = p->nx;
+  e->cfg.sy = p->ny;
+  e->cfg.sz = p->nz;
+  psf_fft_tables(*p, e->aij_h);
+  e->cfg.xoff = 0.5 * (double)p->nx - 1.0;
+  e->cfg.yoff = 0.5 * (double)p->ny - 1.0;
+  roi_index(e, p->nx);
+  publish_geometry(h);
+  set_model(h, M_FFT, 5);
+  return h;
+}
+
+// ftFitNewPeaks fft_fit.c:318-470 ("finder" / "testing": x, y, z;
+// "text" / "hdf5": x, y, z, background, height).
+void ftFitNewPeaks(saFitData* h, double* peaks, char* p_type, int n) { new_peaks_single(h, peaks, p_type, n); }
+
+// ftFitCleanup fft_fit.c:165-192 (the PSF object is the caller's, freed by
+// pFTCleanup).
+void ftFitCleanup(saFitData* h) { daoCleanup(h); }
 
 void mFitNewImage(saFitData* h, double* img) { image_single(h, img, false); }
 void mFitNewBackground(saFitData* h, double* bg) { image_single(h, bg, true); }

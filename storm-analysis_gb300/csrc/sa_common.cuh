@@ -26,7 +26,7 @@ enum { PH = 0, PX = 1, PXW = 2, PY = 3, PYW = 4, PBG = 5, PZ = 6 };
 // Peak status (multi_fit.h:33-35).
 enum { RUNNING = 0, CONVERGED = 1, ERROR = 2 };
 // Models.
-enum { M_2DFIXED = 0, M_2D = 1, M_3D = 2, M_Z = 3, M_SPLINE2D = 4, M_SPLINE3D = 5 };
+enum { M_2DFIXED = 0, M_2D = 1, M_3D = 2, M_Z = 3, M_SPLINE2D = 4, M_SPLINE3D = 5, M_FFT = 6 };
 // Counter slots in the reference's fitData order (multi_fit.h:87-94), plus
 // one diagnostic slot of our own: starting-error evaluations that met fi <= 0.
 enum { C_DPOSV = 0, C_ITER, C_LOST, C_MARGIN, C_NEGFI, C_NEGH, C_NONCONV, C_NONDECR, C_STARTFAIL,
@@ -71,7 +71,7 @@ struct ModelCfg {
   int jac;
   int nx, ny;
   int roi, nroi;
-  int sx, sy, sz;        // spline cells (x, y, z)
+  int sx, sy, sz;        // spline cells (x, y, z); M_FFT: the PSF's x, y, z sizes
   int dil;               // footprint dilation (pixels)
   int cell;              // scheduling grid cell (pixels)
   int gx, gy;            // grid cells per frame
@@ -86,6 +86,7 @@ struct ModelCfg {
   int scmos_zero;        // 1: the sCMOS term is 0 at every pixel
   int dil_late;          // dilation from sweep dil_switch on (<= dil)
   int dil_switch;
+  const double* fft;     // M_FFT: the PSF's spectrum and twiddle tables on the device (fft_layout)
 };
 
 // Per-frame control block of the device state machine.
@@ -134,6 +135,7 @@ struct FrameSet {
   int* run;              // run list: local peak index per run rank
   unsigned* anchor0;     // packed (xi | yi << 16) per run rank at sweep start
   int* done;             // epoch per run rank
+  int* epoch;            // epoch of the current tick (one int; k_post advances it)
   int* cell_start;       // [F][gx*gy+1]
   int2* cell_items;      // run ranks grouped by cell, each with its packed anchor
   int* stepctr;          // [peaks][NCOUNTERS] counters of the latest step of each peak

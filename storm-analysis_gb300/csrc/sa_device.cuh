@@ -544,14 +544,53 @@ __device__ __forceinline__ T contrib_bg(double bg, T rqe, T scmos) {
 // per-warp workspace in shared memory
 // ---------------------------------------------------------------------------
 
-__host__ __device__ __forceinline__ bool is_spline(int model) { return model >= M_SPLINE2D; }
+__host__ __device__ __forceinline__ bool is_spline(int model) { return model == M_SPLINE2D || model == M_SPLINE3D; }
+__host__ __device__ __forceinline__ bool is_fft(int model) { return model == M_FFT; }
+// an arbitrary-PSF model: input formats (x, y, z [, background, height]) and
+// mFitCheck alone as the check (cubic_fit.c:660, fft_fit.c:303)
+__host__ __device__ __forceinline__ bool is_arb(int model) { return model >= M_SPLINE2D; }
+
+// The FFT PSF model's device tables (doubles), for a PSF of nz x ny x nx
+// (x fastest) and nk = nx/2 + 1 spectrum columns:
+//   W  [nz][ny][nk] (re, im)  the spectrum, pFTInitialize psf_fft.c:310-365
+//   Ex [nx][nk]     (re, im)  e^{2 pi i kx x / nx}
+//   Ey [ny][ny]     (re, im)  e^{2 pi i ky y / ny}   (index [y][ky])
+//   Ez [nz]         (re, im)  e^{2 pi i kz (nz/2) / nz}: the middle z plane
+//   dkx [nk], dky [ny], dkz [nz]  pFTCalcShiftVectorDerivative :70-84
+struct FFTLayout {
+  int nk, w, ex, ey, ez, dkx, dky, dkz, total;
+};
+__host__ __device__ __forceinline__ FFTLayout fft_layout(int nx, int ny, int nz) {
+  FFTLayout L;
+  L.nk = nx / 2 + 1;
+  L.w = 0;
+  L.ex = L.w + 2 * nz * ny * L.nk;
+  L.ey = L.ex + 2 * nx * L.nk;
+  L.ez = L.ey + 2 * ny * ny;
+  L.dkx = L.ez + 2 * nz;
+  L.dky = L.dkx + L.nk;
+  L.dkz = L.dky + ny;
+  L.total = L.dkz + nz;
+  return L;
+}
+// Warps of a 1024-thread per-frame CTA (k_prepare, k_post) that carry a
+// workspace: all 32, or 8 for the FFT PSF model, whose shape scratch is
+// ~20 KB per warp.
+__host__ __device__ __forceinline__ int cta_ws_warps(int model) { return model == M_FFT ? 8 : 32; }
+
+// Doubles of a warp's FFT scratch: C, Cz [ny][nk], D, Dy, Dz [ny][nk]
+// (complex), the shift vectors sx [nk], sy [ny], sz [nz] (complex).
+__host__ __device__ __forceinline__ int fft_scratch_doubles(int nx, int ny, int nz) {
+  const int nk = nx / 2 + 1;
+  return 2 * (5 * ny * nk + nk + ny + nz);
+}
 
 // The FP32 engine fits the Gaussian models with compensated (float-float)
 // arithmetic on the quantities that decide steps; it has its own, smaller
 // workspace layout.
 template <typename T>
 __host__ __device__ __forceinline__ bool gauss32(const ModelCfg& cfg) {
-  return sizeof(T) == 4 && !is_spline(cfg.model);
+  return sizeof(T) == 4 && !is_arb(cfg.model);
 }
 
 template <typename T>
@@ -584,6 +623,7 @@ struct WarpWS {
   float* Cs;
   float* tab0;  // shape tables of the step's start: ex hi, ex lo, ey hi, ey lo, xt, yt
   float* tab1;  // trial tables (same layout) / pass-1 gradient tables / solve scratch
+  double* fw;   // M_FFT: the shape evaluation's scratch (fft_scratch_doubles)
   float* par0;  // float-float parameter slots (g32_params) of the step's start record
   float* par1;  // ... and of the current trial
   int ts;       // table stride (ROI size rounded up to 32)
@@ -611,6 +651,7 @@ __host__ __device__ inline size_t warp_ws_bytes(const ModelCfg& cfg, int nroi) {
   b += 36 * sizeof(double) + 16 * sizeof(double);
   b += 3 * sizeof(PeakRec);
   if (sizeof(T) == 4 && !gauss32<T>(cfg) && nroi > 0) b += 32 * 33 * sizeof(float);
+  if (is_fft(cfg.model)) b = ((b + 15) & ~(size_t)15) + fft_scratch_doubles(cfg.sx, cfg.sy, cfg.sz) * sizeof(double);
   return (b + 127) & ~(size_t)127;
 }
 
@@ -671,6 +712,12 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
   ws.t = ws.w + 2;
   if (!gauss32<T>(cfg))
     ws.red = reinterpret_cast<float*>(base + off + 52 * sizeof(double) + 3 * sizeof(PeakRec));
+  ws.fw = nullptr;
+  if (is_fft(cfg.model)) {
+    size_t o = off + 52 * sizeof(double) + 3 * sizeof(PeakRec);
+    if (sizeof(T) == 4 && nroi > 0) o += 32 * 33 * sizeof(float);
+    ws.fw = reinterpret_cast<double*>(base + ((o + 15) & ~(size_t)15));
+  }
   return ws;
 }
 
@@ -961,10 +1008,158 @@ __device__ __forceinline__ void spl32_contrib(ff psf, ff H, ff BG, float rq, flo
   qb.l = 0;
 }
 
+// ---------------------------------------------------------------------------
+// FFT PSF model (M_FFT, the FP64 engine): ftFitCalcPeakShape fft_fit.c:127-155
+// and ftFitCalcJH3D :43-117 through pFTTranslate / pFTGetPSF* (psf_fft.c).
+// The PSF at the peak's offset (dx, dy, dz) is the middle z plane of the c2r
+// inverse of the spectrum times the shift vectors, evaluated separably: for
+// each (ky, kx) the z sum C of the shifted spectrum times the middle-plane
+// twiddle (and Cz, the same times -i dkz); for each (y, kx) the y sums D of
+// C, Dy of C times -i dky and Dz of Cz; a pixel (x, y) is then the c2r x sum
+// of D[y] (weights 1 for the x DC and Nyquist bins, whose imaginary parts
+// the c2r drops, 2 otherwise), and of D[y] times -i dkx, Dy[y], Dz[y] for
+// the derivatives (dz negated, as pFTGetPSFdz).
+// ---------------------------------------------------------------------------
+
+constexpr double SA_PI = 3.14159265358979323846;   // the reference's M_PI
+
+template <typename T>
+__device__ inline void fft_tables(const ModelCfg& cfg, const PeakRec& w, WarpWS<T>& ws, int lane) {
+  const int nx = cfg.sx, ny = cfg.sy, nz = cfg.sz;
+  const FFTLayout L = fft_layout(nx, ny, nz);
+  const int nk = L.nk;
+  double* C = ws.fw;
+  double* Cz = C + 2 * ny * nk;
+  double* Dm = Cz + 2 * ny * nk;
+  double* Dy = Dm + 2 * ny * nk;
+  double* Dz = Dy + 2 * ny * nk;
+  double* sxv = Dz + 2 * ny * nk;
+  double* syv = sxv + 2 * nk;
+  double* szv = syv + 2 * ny;
+  const double ox = w.p[PX] - (double)w.xi, oy = w.p[PY] - (double)w.yi, oz = w.p[PZ];
+  // shift vectors, pFTCalcShiftVector psf_fft.c:43-60 (the z one with -dz):
+  // entry k is cos / sin of t1 * m with m = k up to size/2 (the sine kept
+  // positive at size/2, the reference loop's second write) and m = size - k
+  // with the sine negated above it
+  for (int i = lane; i < nk + ny + nz; i += 32) {
+    int size, k;
+    double d;
+    double* out;
+    if (i < nk) {
+      size = nx; k = i; d = ox; out = sxv + 2 * k;
+    } else if (i < nk + ny) {
+      size = ny; k = i - nk; d = oy; out = syv + 2 * k;
+    } else {
+      size = nz; k = i - nk - ny; d = -oz; out = szv + 2 * k;
+    }
+    double re = 1.0, im = 0.0;
+    if (k > 0) {
+      const double t1 = -SA_PI * 2.0 * d / ((double)size);
+      const bool low = k <= size / 2;
+      const double t2 = t1 * (double)(low ? k : size - k);
+      re = cos(t2);
+      im = low ? sin(t2) : -sin(t2);
+    }
+    out[0] = re;
+    out[1] = im;
+  }
+  __syncwarp();
+  const double* Wt = cfg.fft + L.w;
+  const double* Ez = cfg.fft + L.ez;
+  const double* dkz = cfg.fft + L.dkz;
+  for (int q = lane; q < ny * nk; q += 32) {
+    const int ky = q / nk, kx = q - ky * nk;
+    const double syr = syv[2 * ky], syi = syv[2 * ky + 1], sxr = sxv[2 * kx], sxi = sxv[2 * kx + 1];
+    double cr = 0.0, ci = 0.0, czr = 0.0, czi = 0.0;
+    for (int kz = 0; kz < nz; kz++) {
+      const double* wp = Wt + 2 * (((size_t)kz * ny + ky) * nk + kx);
+      double r1 = __ldg(wp), c1 = __ldg(wp + 1), r2, c2;
+      // z, y, x shifts in the reference's order (pFTTranslate :395-418)
+      r2 = r1 * szv[2 * kz] - c1 * szv[2 * kz + 1];
+      c2 = r1 * szv[2 * kz + 1] + c1 * szv[2 * kz];
+      r1 = r2 * syr - c2 * syi;
+      c1 = r2 * syi + c2 * syr;
+      r2 = r1 * sxr - c1 * sxi;
+      c2 = r1 * sxi + c1 * sxr;
+      const double er = __ldg(Ez + 2 * kz), ei = __ldg(Ez + 2 * kz + 1);
+      const double pr = r2 * er - c2 * ei, pi = r2 * ei + c2 * er;
+      cr += pr;
+      ci += pi;
+      const double dk = __ldg(dkz + kz);
+      czr += pi * dk;
+      czi -= pr * dk;
+    }
+    C[2 * q] = cr;
+    C[2 * q + 1] = ci;
+    Cz[2 * q] = czr;
+    Cz[2 * q + 1] = czi;
+  }
+  __syncwarp();
+  const double* Ey = cfg.fft + L.ey;
+  const double* dky = cfg.fft + L.dky;
+  for (int q = lane; q < ny * nk; q += 32) {
+    const int y = q / nk, kx = q - y * nk;
+    double dr = 0.0, di = 0.0, dyr = 0.0, dyi = 0.0, dzr = 0.0, dzi = 0.0;
+    for (int ky = 0; ky < ny; ky++) {
+      const double er = __ldg(Ey + 2 * (y * ny + ky)), ei = __ldg(Ey + 2 * (y * ny + ky) + 1);
+      const int c = 2 * (ky * nk + kx);
+      const double ar = C[c], ai = C[c + 1];
+      const double pr = ar * er - ai * ei, pi = ar * ei + ai * er;
+      dr += pr;
+      di += pi;
+      const double dk = __ldg(dky + ky);
+      dyr += pi * dk;
+      dyi -= pr * dk;
+      const double zr = Cz[c], zi = Cz[c + 1];
+      dzr += zr * er - zi * ei;
+      dzi += zr * ei + zi * er;
+    }
+    Dm[2 * q] = dr;
+    Dm[2 * q + 1] = di;
+    Dy[2 * q] = dyr;
+    Dy[2 * q + 1] = dyi;
+    Dz[2 * q] = dzr;
+    Dz[2 * q + 1] = dzi;
+  }
+}
+
+// The PSF at ROI pixel (rx, ry) from fft_tables' D arrays; with g non-null
+// also its x, y and z derivatives (pFTGetPSFdx / dy / dz) in g[0..2].
+__device__ inline double fft_pixel(const ModelCfg& cfg, const double* fw, int rx, int ry, double* g) {
+  const int nx = cfg.sx, ny = cfg.sy;
+  const FFTLayout L = fft_layout(nx, ny, cfg.sz);
+  const int nk = L.nk;
+  const double* Dm = fw + 4 * ny * nk;
+  const double* Dy = Dm + 2 * ny * nk;
+  const double* Dz = Dy + 2 * ny * nk;
+  const double* Ex = cfg.fft + L.ex + 2 * rx * nk;
+  const double* dkx = cfg.fft + L.dkx;
+  double vp = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+  for (int kx = 0; kx < nk; kx++) {
+    const double er = __ldg(Ex + 2 * kx), ei = __ldg(Ex + 2 * kx + 1);
+    const double c = ((kx == 0) || (2 * kx == nx)) ? 1.0 : 2.0;
+    const int o = 2 * (ry * nk + kx);
+    const double pr = Dm[o] * er - Dm[o + 1] * ei, pi = Dm[o] * ei + Dm[o + 1] * er;
+    vp += c * pr;
+    if (g) {
+      vx += c * pi * __ldg(dkx + kx);
+      vy += c * (Dy[o] * er - Dy[o + 1] * ei);
+      vz += c * (Dz[o] * er - Dz[o + 1] * ei);
+    }
+  }
+  if (g) {
+    g[0] = vx;
+    g[1] = vy;
+    g[2] = -vz;
+  }
+  return vp;
+}
+
 // Peak shape at ROI pixel p for the tables currently in the workspace.
 template <typename T>
 __device__ __forceinline__ T psf_at(const ModelCfg& cfg, const T* aij, const WarpWS<T>& ws,
                                     const SplinePos& s, int rx, int ry) {
+  if (is_fft(cfg.model)) return (T)fft_pixel(cfg, ws.fw, rx, ry, nullptr);
   if (!is_spline(cfg.model)) {
     if constexpr (sizeof(T) == 4) return g32_psf(ws.tab0, ws.ts, rx, ry).h;
     else return mul_rn(ws.eyt[ry], ws.ext[rx]);
@@ -1029,6 +1224,15 @@ __device__ inline void apply_update(const ModelCfg& cfg, int model, PeakRec& w, 
       anchor_update(w);
       widths_from_z(cfg, w);
       break;
+    case M_FFT: {
+      // ftFitUpdate3D fft_fit.c:481-497 with ftFitZRangeCheck :506-524
+      w.p[PH] -= d[0]; w.p[PX] -= d[1]; w.p[PY] -= d[2]; w.p[PZ] -= d[3]; w.p[PBG] -= d[4];
+      anchor_update(w);
+      const double max_z = ((double)cfg.sz) * 0.5 - 1.0e-12;
+      if (w.p[PZ] < -max_z) w.p[PZ] = -max_z;
+      if (w.p[PZ] > max_z) w.p[PZ] = max_z;
+      break;
+    }
     default: {  // M_SPLINE3D, with cfZRangeCheck
       w.p[PH] -= d[0]; w.p[PX] -= d[1]; w.p[PY] -= d[2]; w.p[PZ] -= d[3]; w.p[PBG] -= d[4];
       anchor_update(w);
@@ -1066,7 +1270,7 @@ __device__ inline int model_check(const ModelCfg& cfg, int model, PeakRec& w) {
 }
 
 __device__ __forceinline__ int check_for(const ModelCfg& cfg, int model, PeakRec& w) {
-  return is_spline(model) ? base_check(cfg, w) : model_check(cfg, model, w);
+  return is_arb(model) ? base_check(cfg, w) : model_check(cfg, model, w);
 }
 
 // Prepare the shape tables of peak w (all lanes) and return its spline
@@ -1075,7 +1279,11 @@ template <typename T>
 __device__ inline SplinePos shape_tables(const ModelCfg& cfg, const PeakRec& w, WarpWS<T>& ws,
                                          int lane) {
   SplinePos s;
-  if (is_spline(cfg.model)) {
+  if (is_fft(cfg.model)) {
+    s.xs = s.ys = s.zi = 0;
+    s.xd = s.yd = s.zd = 0.0;
+    fft_tables(cfg, w, ws, lane);
+  } else if (is_spline(cfg.model)) {
     s = spline_pos(w.p, w.xi, w.yi, w.zi);
     spline_tables(cfg, s, ws, lane);
   } else {
@@ -1136,6 +1344,17 @@ __device__ __forceinline__ void jt_row(const ModelCfg& cfg, const T* aij, const 
       jt[1] = rq * (T)2 * h * (T)w.p[PXW] * xt * e_t;
       jt[2] = rq * (T)2 * h * (T)w.p[PYW] * yt * e_t;
       jt[3] = rq * (-h * xt * xt * gx * e_t - h * yt * yt * gy * e_t);
+      jt[4] = rq;
+      break;
+    }
+    case M_FFT: {
+      // ftFitCalcJH3D fft_fit.c:90-100
+      double g[3];
+      fft_pixel(cfg, ws.fw, rx, ry, g);
+      jt[0] = rq * psf;
+      jt[1] = rq * h * (T)g[0];
+      jt[2] = rq * h * (T)g[1];
+      jt[3] = rq * h * (T)g[2];
       jt[4] = rq;
       break;
     }

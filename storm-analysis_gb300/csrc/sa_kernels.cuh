@@ -539,8 +539,11 @@ __device__ __forceinline__ bool footprints_overlap(int dx, int dy, int roi, int 
 // G32 >= 0: the FP32 Gaussian step (lm_step_g32) of model G32 (one
 // instantiation per model); G32 < 0: lm_step.
 template <typename T, int G32>
-__global__ void __launch_bounds__(128, 5) k_sweep(ModelCfg cfg, FrameSet<T> fs, int epoch) {
+__global__ void __launch_bounds__(128, 5) k_sweep(ModelCfg cfg, FrameSet<T> fs) {
   extern __shared__ __align__(16) char smem[];
+  // the tick's epoch: a done flag equal to it marks a rank done in this
+  // launch (k_post of the previous tick advanced it)
+  const int epoch = __ldcg(fs.epoch);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
@@ -816,9 +819,10 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
     __syncthreads();
     // roll back run ranks > b: remove the current contribution, restore the snapshot
     const int lane = tid & 31, wid = tid >> 5;
-    WarpWS<T> ws = warp_ws<T>(smem + (size_t)wid * warp_ws_bytes<T>(cfg, 0), cfg, 0);
+    const int nws = cta_ws_warps(cfg.model);
+    WarpWS<T> ws = warp_ws<T>(smem + (size_t)(wid < nws ? wid : 0) * warp_ws_bytes<T>(cfg, 0), cfg, 0);
     const long long fbase = (long long)f * fs.npix;
-    for (int r = b + 1 + wid; r < nrun; r += 32) {
+    for (int r = b + 1 + wid; wid < nws && r < nrun; r += nws) {
       const int li = fs.run[base + r];
       PeakRec cur, sn;
       load_rec(fs.pk + base + li, cur);
@@ -871,6 +875,8 @@ __global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
   __shared__ int s_move[1024];
   const int f = blockIdx.x;
   FrameCtl* c = fs.ctl + f;
+  // the next tick's epoch (every k_sweep of this tick has finished)
+  if (f == 0 && threadIdx.x == 0) *fs.epoch += 1;
   if (c->phase != PH_IN_SWEEP) return;
   const int tid = threadIdx.x;
   if (c->escaped_min != INT_MAX) {
@@ -884,7 +890,8 @@ __global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
   const int base = fs.pk_off[f];
   const int nrun = c->nrun;
   const int lane = tid & 31, wid = tid >> 5;
-  WarpWS<T> ws = warp_ws<T>(smem + (size_t)wid * warp_ws_bytes<T>(cfg, 0), cfg, 0);
+  const int nws = cta_ws_warps(cfg.model);
+  WarpWS<T> ws = warp_ws<T>(smem + (size_t)(wid < nws ? wid : 0) * warp_ws_bytes<T>(cfg, 0), cfg, 0);
   const long long fbase = (long long)f * fs.npix;
   // recenter (mFitRecenterPeaks multi_fit.c:1644-1690); order-free with
   // fixed-point accumulation.  The run ranks are scanned a thread each; the
@@ -904,7 +911,7 @@ __global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
     }
     __syncthreads();
     const int nmove = s_nmove;
-    for (int m = wid; m < nmove; m += 32) {
+    for (int m = wid; wid < nws && m < nmove; m += nws) {
       const int li = fs.run[base + s_move[m]];
       PeakRec rec;
       load_rec(fs.pk + base + li, rec);
@@ -1141,7 +1148,7 @@ __device__ inline PeakRec new_peak_rec(const ModelCfg& cfg, const double* q, int
   w.status = RUNNING;
   w.zi = 0;
   for (int i = 0; i < 4; i++) w.pad[i] = 0;
-  const bool spl = is_spline(cfg.model);
+  const bool spl = is_arb(cfg.model);   // the arbitrary-PSF input formats
   w.p[PX] = q[0] - cfg.xoff;
   w.p[PY] = q[1] - cfg.yoff;
   w.p[PZ] = q[2] - cfg.zoff;
@@ -1164,7 +1171,7 @@ __device__ inline PeakRec new_peak_rec(const ModelCfg& cfg, const double* q, int
   }
   w.xi = (int)floor(w.p[PX]);
   w.yi = (int)floor(w.p[PY]);
-  if (spl) w.zi = (int)w.p[PZ];
+  if (is_spline(cfg.model)) w.zi = (int)w.p[PZ];
   if (ptype != PT_TEXT) {
     w.p[PBG] = 1.0;
     w.p[PH] = 1.0;

@@ -25,7 +25,7 @@ struct Launch {
   static cudaError_t configure(const ModelCfg& cfg, int* sweep_grid, size_t* sweep_smem,
                                size_t* cta_smem, size_t* warp_smem);
   static cudaError_t prepare(const ModelCfg& cfg, const FrameSet<T>& fs, size_t smem, cudaStream_t s);
-  static cudaError_t sweep(const ModelCfg& cfg, const FrameSet<T>& fs, int epoch, int grid,
+  static cudaError_t sweep(const ModelCfg& cfg, const FrameSet<T>& fs, int grid,
                            size_t smem, cudaStream_t s);
   static cudaError_t post(const ModelCfg& cfg, const FrameSet<T>& fs, size_t smem, cudaStream_t s);
   // The remaining sweeps of every frame with at most tail_peaks RUNNING

@@ -14,7 +14,7 @@ constexpr int AUX_BLOCK = 256;      // warp-per-peak auxiliary kernels
 // The sweep kernel of a configuration: the FP32 Gaussian models have one
 // instantiation each, everything else shares the generic step.
 template <typename T>
-void (*sweep_kernel(const ModelCfg& cfg))(ModelCfg, FrameSet<T>, int) {
+void (*sweep_kernel(const ModelCfg& cfg))(ModelCfg, FrameSet<T>) {
   if constexpr (sizeof(T) == 4) {
     if (gauss32<T>(cfg)) {
       switch (cfg.model) {
@@ -56,7 +56,8 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
   const size_t s_sweep = ws * (SWEEP_BLOCK / 32) + (((size_t)cfg.nroi * 2 + 15) & ~(size_t)15);
   const size_t ws0 = warp_ws_bytes<T>(cfg, 0);
   const size_t grid_bytes = (size_t)(cfg.gx * cfg.gy + 1) * sizeof(int);
-  const size_t s_cta = ws0 * (CTA_BLOCK / 32) > grid_bytes ? ws0 * (CTA_BLOCK / 32) : grid_bytes;
+  const size_t s_cta_ws = ws0 * (size_t)cta_ws_warps(cfg.model);
+  const size_t s_cta = s_cta_ws > grid_bytes ? s_cta_ws : grid_bytes;
   const size_t s_aux = ws0 * (AUX_BLOCK / 32);
   if (s_sweep > (size_t)max_smem || s_cta > (size_t)max_smem) return cudaErrorInvalidConfiguration;
   // The limit is a property of the kernel, shared by every handle of the
@@ -96,9 +97,9 @@ cudaError_t Launch<T>::prepare(const ModelCfg& cfg, const FrameSet<T>& fs, size_
 }
 
 template <typename T>
-cudaError_t Launch<T>::sweep(const ModelCfg& cfg, const FrameSet<T>& fs, int epoch, int grid,
-                             size_t smem, cudaStream_t s) {
-  sweep_kernel<T>(cfg)<<<grid, SWEEP_BLOCK, smem, s>>>(cfg, fs, epoch);
+cudaError_t Launch<T>::sweep(const ModelCfg& cfg, const FrameSet<T>& fs, int grid, size_t smem,
+                             cudaStream_t s) {
+  sweep_kernel<T>(cfg)<<<grid, SWEEP_BLOCK, smem, s>>>(cfg, fs);
   return cudaGetLastError();
 }
 

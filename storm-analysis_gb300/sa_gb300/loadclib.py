@@ -95,6 +95,25 @@ def _declare(lib):
     lib.initSpline3D.argtypes = [f64, ci, ci, ci]
     lib.initSpline3D.restype = vp
     lib.splineCleanup.argtypes = [vp]
+    # the FFT PSF model (psf_fft.c / fft_fit.c names)
+    lib.pFTInitialize.argtypes = [f64, ci, ci, ci]
+    lib.pFTInitialize.restype = vp
+    lib.pFTCleanup.argtypes = [vp]
+    lib.pFTCleanup.restype = None
+    lib.pFTTranslate.argtypes = [vp, cd, cd, cd]
+    lib.pFTTranslate.restype = None
+    for name in ["pFTGetPSF", "pFTGetPSFdx", "pFTGetPSFdy", "pFTGetPSFdz"]:
+        getattr(lib, name).argtypes = [vp, f64]
+        getattr(lib, name).restype = None
+    for name in ["pFTGetXSize", "pFTGetYSize", "pFTGetZSize"]:
+        getattr(lib, name).argtypes = [vp]
+        getattr(lib, name).restype = ci
+    lib.ftFitInitialize.argtypes = [vp, f64, f64, cd, ci, ci]
+    lib.ftFitInitialize.restype = hp
+    lib.ftFitNewPeaks.argtypes = [hp, f64, cs, ci]
+    lib.ftFitNewPeaks.restype = None
+    lib.ftFitCleanup.argtypes = [hp]
+    lib.ftFitCleanup.restype = None
     for name in ["getXSize", "getYSize", "getZSize"]:
         getattr(lib, name).argtypes = [vp]
         getattr(lib, name).restype = ci
@@ -225,6 +244,9 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "initSpline2D", "initSpline3D", "splineCleanup", "getXSize", "getYSize", "getZSize",
            "cfInitialize", "cfInitialize2D", "cfInitialize3D", "cfInitialize3DALS",
            "cfInitialize3DLS", "cfInitialize3DFWLS", "cfNewPeaks", "cfCleanup",
+           "pFTInitialize", "pFTCleanup", "pFTTranslate", "pFTGetPSF", "pFTGetPSFdx", "pFTGetPSFdy",
+           "pFTGetPSFdz", "pFTGetXSize", "pFTGetYSize", "pFTGetZSize", "ftFitInitialize", "ftFitNewPeaks",
+           "ftFitCleanup",
            "mFitAnscombeTransformImage", "mFitGetFitImage", "mFitGetNError",
            "mFitGetPeakPropertyDouble", "mFitGetPeakPropertyInt", "mFitGetResidual",
            "mFitGetUnconverged", "mFitIterateLM", "mFitNewBackground", "mFitNewImage",
