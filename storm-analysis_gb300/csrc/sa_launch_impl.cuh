@@ -59,7 +59,8 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
   const size_t s_cta_ws = ws0 * (size_t)cta_ws_warps(cfg.model);
   const size_t s_cta = s_cta_ws > grid_bytes ? s_cta_ws : grid_bytes;
   const size_t s_aux = ws0 * (AUX_BLOCK / 32);
-  if (s_sweep > (size_t)max_smem || s_cta > (size_t)max_smem) return cudaErrorInvalidConfiguration;
+  if (s_sweep > (size_t)max_smem || s_cta > (size_t)max_smem || s_aux > (size_t)max_smem)
+    return cudaErrorInvalidConfiguration;
   // The limit is a property of the kernel, shared by every handle of the
   // process (handles of different models and ROI sizes may run side by
   // side), so it is raised to the device maximum rather than to this
@@ -79,6 +80,13 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
   if (e != cudaSuccess) return e;
   e = raise_limit((const void*)tail_kernel<T>(cfg));
   if (e != cudaSuccess) return e;
+  // the warp-per-peak auxiliary kernels (their workspace is above the
+  // default 48 KB for the FFT PSF model)
+  for (const void* fn : {(const void*)k_newpeaks<T>, (const void*)k_newpeaks_finder<T>, (const void*)k_peak_props<T>,
+                         (const void*)k_set_status<T>}) {
+    e = raise_limit(fn);
+    if (e != cudaSuccess) return e;
+  }
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T>(cfg), SWEEP_BLOCK, s_sweep);
   if (e != cudaSuccess) return e;
