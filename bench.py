@@ -896,7 +896,54 @@ def run_config_reports(args, pool, cores):
             for w in ("xsigma", "ysigma"):
                 rec["max_rel_" + w] = float(numpy.max(numpy.abs(got[w][conv] - ref[w][conv]) / numpy.abs(ref[w][conv])))
         out["cfg%d" % cfg] = rec
+    out["fft"] = run_fft_report(args, pool, cores)
     return out
+
+
+FFT_FRAMES = 4
+
+
+def run_fft_report(args, pool, cores):
+    """The FFT PSF model (psf_fft / fft_fit, FP64 engine) on synthetic
+    frames drawn with the model itself: localizations/s of the batched
+    engine and the errors against the oracle's fits of the same frames."""
+    import torch
+    from sa_gb300 import engine, parity, psf_fft_c, synth
+    wl = synth.fft_workload(frames=FFT_FRAMES)
+    F = len(wl["images"])
+    shape = (wl["ny"], wl["nx"])
+    images = numpy.ascontiguousarray(numpy.stack(wl["images"]).astype(numpy.float32))
+    bgs = numpy.ascontiguousarray(numpy.stack(wl["backgrounds"]).astype(numpy.float32))
+    pf = psf_fft_c.PSFFFT(wl["fitter"]["psf"])
+    fit = engine.BatchFitter("fft", shape, F, psf_fft=pf, precision=64)
+    fit.load(images, bgs, wl["guesses"], "hdf5")
+    fit.fit(MAX_IT)   # warm-up
+    ms = []
+    for _ in range(2):
+        fit.load(images, bgs, wl["guesses"], "hdf5")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fit.fit(MAX_IT)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    got = fit.results(props=("x", "y", "z", "height", "background"))
+    units = int(fit.counts().sum())
+    fit.close()
+    pf.cleanup()
+    n_cpu, wall_cpu, ora = cpu_sample(wl, F, cores, pool)
+    ref = {k: numpy.concatenate([ora[f][k] for f in range(F)]) for k in ora[0]}
+    st = parity.compare(got, ref)
+    psf = wl["fitter"]["psf"]
+    return {"workload": "FFT PSF model (%dx%dx%d stack), %d frames %dx%d, %d emitters, FP64 engine"
+                        % (psf.shape[0], psf.shape[1], psf.shape[2], F, shape[1], shape[0], units),
+            "localizations_per_s": units / (min(ms) / 1e3), "ms_per_fit": min(ms),
+            "cpu_localizations_per_s": n_cpu / wall_cpu if wall_cpu > 0 else None, "cpu_cores": cores,
+            "peaks": st["n"], "status_agree": st["status_agree"],
+            "frac_within": min([st[k] for k in st if k.startswith("frac_ok")] or [1.0]),
+            "max_dx": st.get("max_dx"), "max_dy": st.get("max_dy"), "max_dz": st.get("max_dz"),
+            "max_rel_height": st.get("max_rel_h"), "max_rel_background": st.get("max_rel_bg")}
 
 
 DENSITY_BINS = 6   # log-spaced density bins of the serving stream's frame cache

@@ -19,7 +19,7 @@ import numpy
 from . import loadclib
 from .dao_fit_c import MultiFitterException, formatPeaksArbitraryPSF, formatPeaksGaussianPSF
 
-MODEL_INIT = {"2dfixed", "2d", "3d", "Z", "spline2D", "spline3D"}
+MODEL_INIT = {"2dfixed", "2d", "3d", "Z", "spline2D", "spline3D", "fft"}
 
 RESULT_PROPS = ("x", "y", "z", "height", "background", "xsigma", "ysigma", "error")
 
@@ -28,7 +28,7 @@ class BatchFitter(object):
     def __init__(self, model, shape, n_frames, roi_size=10, sigma_range=None, rqe=None,
                  scmos_cal=None, wx_params=None, wy_params=None, min_z=None, max_z=None,
                  spline=None, precision=32, peaks_capacity=None, tol=1.0e-6, dilation=None,
-                 stream=None):
+                 stream=None, psf_fft=None):
         if model not in MODEL_INIT:
             raise MultiFitterException("unknown model '%s'" % model)
         self.clib = loadclib.load()
@@ -42,9 +42,14 @@ class BatchFitter(object):
         self.scmos_cal = numpy.ascontiguousarray(scmos_cal, dtype=numpy.float64)
         self.spline = spline
         lib = self.clib
+        self.psf_fft = psf_fft
         if model.startswith("spline"):
             sp = spline.getCPointer()
             self.h = lib.cfInitialize(sp, self.rqe, self.scmos_cal, tol, nx, ny)
+        elif model == "fft":
+            # psf_fft: a psf_fft_c.PSFFFT (or anything with getCPointer()); the
+            # FFT PSF model runs in the FP64 engine
+            self.h = lib.ftFitInitialize(psf_fft.getCPointer(), self.rqe, self.scmos_cal, tol, nx, ny)
         else:
             self.h = lib.daoInitialize(self.rqe, self.scmos_cal, tol, nx, ny, roi_size)
         if not self.h:
@@ -67,7 +72,7 @@ class BatchFitter(object):
                                float(min_z), float(max_z))
         elif model == "spline3D":
             lib.cfInitialize3D(self.h)
-        else:
+        elif model == "spline2D":
             lib.cfInitialize2D(self.h)
         self.capacity = None
         self._framed = False
@@ -87,7 +92,7 @@ class BatchFitter(object):
             self._framed = True
 
     def format(self, peaks, peaks_type):
-        if self.model.startswith("spline"):
+        if self.model.startswith("spline") or self.model == "fft":
             return formatPeaksArbitraryPSF(peaks, peaks_type)
         return formatPeaksGaussianPSF(peaks, peaks_type)
 
@@ -240,6 +245,8 @@ class BatchFitter(object):
         if self.h:
             if self.model.startswith("spline"):
                 self.clib.cfCleanup(self.h)
+            elif self.model == "fft":
+                self.clib.ftFitCleanup(self.h)
             else:
                 self.clib.daoCleanup(self.h)
             self.h = None

@@ -349,3 +349,56 @@ def serving_frame(model, size, density, seed):
     n = max(1, int(round(density * (size * PIXEL_UM) ** 2)))
     return make_workload(cfg, frames=1, nx=size, ny=size, seed=seed, n_emitters=n,
                          camera_seed=10000 + 97 * cfg + size, min_sep=0.0)
+
+
+# ---------------------------------------------------------------------------
+# FFT PSF model workload (psf_fft / fft_fit)
+# ---------------------------------------------------------------------------
+
+def fft_psf_stack(z_size=17, size=20, seed=3):
+    """A measured-PSF stand-in for the FFT PSF model: an astigmatic stack
+    of z_size planes on a size x size grid (x fastest), widths 1.6 px at the
+    middle plane changing +-35 % across the stack, a 2 % per-plane ripple,
+    the middle plane summing to 1."""
+    rng = numpy.random.default_rng(seed)
+    zz = numpy.linspace(-1.0, 1.0, z_size)[:, None, None]
+    yy = (numpy.arange(size) - size / 2.0)[None, :, None]
+    xx = (numpy.arange(size) - size / 2.0)[None, None, :]
+    sx = 1.6 * (1.0 + 0.35 * zz + 0.2 * zz * zz)
+    sy = 1.6 * (1.0 - 0.35 * zz + 0.2 * zz * zz)
+    psf = numpy.exp(-xx * xx / (2 * sx * sx) - yy * yy / (2 * sy * sy))
+    psf = psf * (1.0 + 0.02 * rng.standard_normal((z_size, 1, 1)))
+    return psf / psf[z_size // 2].sum()
+
+
+def fft_workload(frames=4, nx=256, ny=256, n_emitters=300, seed=21, background=10.0):
+    """Frames of emitters drawn with the FFT PSF model itself (the PSF
+    translated by its spectrum, psf_fft_c.PSFFFT; Poisson noise) and
+    "hdf5" starting peaks: the truth perturbed by 0.3 px in x / y, half its
+    z, 80 % of its height.  z in z pixels of the stack, within +-3."""
+    from . import psf_fft_c
+    psf = fft_psf_stack()
+    pf = psf_fft_c.PSFFFT(psf)
+    size = psf.shape[1]
+    xoff, yoff = 0.5 * size - 1.0, 0.5 * psf.shape[1] - 1.0
+    rng = numpy.random.default_rng(seed)
+    out = dict(model="fft", nx=nx, ny=ny, images=[], backgrounds=[], truth=[], guesses=[],
+               rqe=numpy.ones((ny, nx)), scmos_cal=numpy.zeros((ny, nx)), fitter={"model": "fft", "psf": psf})
+    for _ in range(frames):
+        img = numpy.full((ny, nx), background)
+        x = rng.uniform(size, nx - size, n_emitters)
+        y = rng.uniform(size, ny - size, n_emitters)
+        z = rng.uniform(-3.0, 3.0, n_emitters)
+        h = rng.uniform(3000.0, 20000.0, n_emitters)
+        for i in range(n_emitters):
+            px, py = x[i] - xoff, y[i] - yoff
+            xi, yi = int(math.floor(px)), int(math.floor(py))
+            pf.translate(px - xi, py - yi, z[i])
+            img[yi:yi + size, xi:xi + size] += h[i] * pf.getPSF()
+        out["images"].append(rng.poisson(img).astype(numpy.float64))
+        out["backgrounds"].append(numpy.full((ny, nx), background))
+        out["truth"].append(dict(x=x, y=y, z=z, height=h))
+        out["guesses"].append(dict(x=x + rng.normal(0.0, 0.3, n_emitters), y=y + rng.normal(0.0, 0.3, n_emitters),
+                                   z=0.5 * z, background=numpy.full(n_emitters, background), height=0.8 * h))
+    pf.cleanup()
+    return out

@@ -16,6 +16,9 @@ pytestmark = pytest.mark.gpu
 
 
 def make_case(seed, n_peaks, shape=(96, 104), psf_shape=(17, 20), ptype="hdf5", background=10.0):
+    """An image of n_peaks FFT-PSF emitters (the oracle's model, Poisson
+    noise) and starting peaks: for "hdf5" perturbed truth, for "finder" /
+    "testing" rounded positions at z = 0."""
     from oracle import oracle, psf_fft as opf
     psf = opf.test_psf(psf_shape[0], psf_shape[1], seed=3)
     rng = numpy.random.default_rng(seed)
@@ -46,16 +49,16 @@ def make_case(seed, n_peaks, shape=(96, 104), psf_shape=(17, 20), ptype="hdf5", 
     return psf, img, bg, peaks
 
 
-def fit_both(psf, img, bg, peaks, ptype, max_iterations=200):
+def fit_both(psf, img, bg, peaks, ptype, max_iterations=200, rqe=None, scmos=None, precision=64):
     from oracle import oracle
     from sa_gb300 import fft_fit_c, psf_fft_c
-    ref = oracle.OracleFitter("fft", img.shape, psf=psf)
+    ref = oracle.OracleFitter("fft", img.shape, psf=psf, rqe=rqe, scmos_cal=scmos)
     ref.newImage(img)
     ref.newBackground(bg)
     ref.newPeaks(peaks, ptype)
     ref.doFit(max_iterations)
     fn = psf_fft_c.PSFFnBase(psf_data={"psf": psf, "pixel_size": 100.0, "zmin": -800.0, "zmax": 800.0})
-    gpu = fft_fit_c.CFFTFit(psf_fn=fn)
+    gpu = fft_fit_c.CFFTFit(psf_fn=fn, rqe=rqe, scmos_cal=scmos, precision=precision)
     gpu.initializeC(img)
     gpu.newImage(img)
     gpu.newBackground(bg)
@@ -70,10 +73,32 @@ def fit_both(psf, img, bg, peaks, ptype, max_iterations=200):
     return out
 
 
-@pytest.mark.parametrize("seed,n_peaks,ptype", [(1, 12, "hdf5"), (2, 30, "hdf5"), (3, 16, "finder")])
-def test_fft_fit_matches_oracle(seed, n_peaks, ptype):
-    psf, img, bg, peaks = make_case(seed, n_peaks, ptype=ptype)
-    out = fit_both(psf, img, bg, peaks, ptype)
+CASES = [
+    dict(seed=1, n_peaks=12, ptype="hdf5"),
+    dict(seed=2, n_peaks=30, ptype="hdf5"),
+    dict(seed=3, n_peaks=16, ptype="finder"),
+    dict(seed=4, n_peaks=16, ptype="testing"),
+    # a PSF of even x / y size 16 and 21 planes, sCMOS calibration and RQE
+    dict(seed=5, n_peaks=20, ptype="hdf5", psf_shape=(21, 16), calibration=True),
+    # a handle asked for the FP32 engine runs the FFT model in FP64 all the same
+    dict(seed=6, n_peaks=12, ptype="hdf5", precision=32),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: "seed%d-%s" % (c["seed"], c["ptype"]))
+def test_fft_fit_matches_oracle(case):
+    case = dict(case)
+    ptype = case["ptype"]
+    calibration = case.pop("calibration", False)
+    precision = case.pop("precision", 64)
+    psf, img, bg, peaks = make_case(case["seed"], case["n_peaks"], ptype=ptype,
+                                    psf_shape=case.get("psf_shape", (17, 20)))
+    rqe = scmos = None
+    if calibration:
+        rng = numpy.random.default_rng(case["seed"] + 100)
+        rqe = rng.uniform(0.8, 1.2, img.shape)
+        scmos = rng.uniform(0.5, 3.0, img.shape)
+    out = fit_both(psf, img, bg, peaks, ptype, rqe=rqe, scmos=scmos, precision=precision)
     st_ref, st_gpu = out["status"]
     assert numpy.array_equal(st_ref, st_gpu)
     assert numpy.array_equal(out["iterations"][0], out["iterations"][1])
