@@ -73,6 +73,15 @@ def _cpu_worker(args):
     kw = dict(fitter_kw)
     model = kw.pop("model")
     spline = kw.pop("spline", None)
+    if model == "pupil":
+        # the oracle takes the pupil function as pfnInitialize / pfnSetPF do
+        from sa_gb300 import pupil_math
+        pf_data = kw.pop("pf_data")
+        cls = pupil_math.GeometrySim if pf_data["geo_sim_pf"] else pupil_math.Geometry
+        geo = cls(pf_data["pf"].shape[0], pf_data["pixel_size"], pf_data["wavelength"],
+                  pf_data["immersion_index"], pf_data["numerical_aperture"])
+        kw = {"pupil": (geo.kx, geo.ky, numpy.real(geo.kz), pf_data["pf"]),
+              "min_z": kw.pop("zmin"), "max_z": kw.pop("zmax")}
     f = O.OracleFitter(model, shape, rqe=rqe, scmos_cal=scmos,
                        spline=(spline["coeff"] if spline is not None else None), **kw)
     n = 0
@@ -897,25 +906,32 @@ def run_config_reports(args, pool, cores):
                 rec["max_rel_" + w] = float(numpy.max(numpy.abs(got[w][conv] - ref[w][conv]) / numpy.abs(ref[w][conv])))
         out["cfg%d" % cfg] = rec
     out["fft"] = run_fft_report(args, pool, cores)
+    out["pupil"] = run_fft_report(args, pool, cores, model="pupil")
     return out
 
 
 FFT_FRAMES = 4
 
 
-def run_fft_report(args, pool, cores):
-    """The FFT PSF model (psf_fft / fft_fit, FP64 engine) on synthetic
+def run_fft_report(args, pool, cores, model="fft"):
+    """An arbitrary-PSF model in the FP64 engine -- the FFT PSF (psf_fft /
+    fft_fit) or the pupil function (pupilfn / pupil_fit) -- on synthetic
     frames drawn with the model itself: localizations/s of the batched
     engine and the errors against the oracle's fits of the same frames."""
     import torch
-    from sa_gb300 import engine, parity, psf_fft_c, synth
-    wl = synth.fft_workload(frames=FFT_FRAMES)
+    from sa_gb300 import engine, parity, psf_fft_c, pupil_fn, synth
+    wl = synth.fft_workload(frames=FFT_FRAMES) if model == "fft" else synth.pupil_workload(frames=FFT_FRAMES)
     F = len(wl["images"])
     shape = (wl["ny"], wl["nx"])
     images = numpy.ascontiguousarray(numpy.stack(wl["images"]).astype(numpy.float32))
     bgs = numpy.ascontiguousarray(numpy.stack(wl["backgrounds"]).astype(numpy.float32))
-    pf = psf_fft_c.PSFFFT(wl["fitter"]["psf"])
-    fit = engine.BatchFitter("fft", shape, F, psf_fft=pf, precision=64)
+    if model == "fft":
+        obj = psf_fft_c.PSFFFT(wl["fitter"]["psf"])
+        fit = engine.BatchFitter("fft", shape, F, psf_fft=obj, precision=64)
+    else:
+        obj = pupil_fn.PupilFunction(pf_data=wl["fitter"]["pf_data"], zmin=wl["fitter"]["zmin"],
+                                     zmax=wl["fitter"]["zmax"])
+        fit = engine.BatchFitter("pupil", shape, F, pupil_fn=obj, precision=64)
     fit.load(images, bgs, wl["guesses"], "hdf5")
     fit.fit(MAX_IT)   # warm-up
     ms = []
@@ -931,15 +947,20 @@ def run_fft_report(args, pool, cores):
     got = fit.results(props=("x", "y", "z", "height", "background"))
     units = int(fit.counts().sum())
     fit.close()
-    pf.cleanup()
+    obj.cleanup()
     n_cpu, wall_cpu, ora = cpu_sample(wl, F, cores, pool)
     ref = {k: numpy.concatenate([ora[f][k] for f in range(F)]) for k in ora[0]}
     st = parity.compare(got, ref)
-    psf = wl["fitter"]["psf"]
-    return {"workload": "FFT PSF model (%dx%dx%d stack), %d frames %dx%d, %d emitters, FP64 engine"
-                        % (psf.shape[0], psf.shape[1], psf.shape[2], F, shape[1], shape[0], units),
+    if model == "fft":
+        psf = wl["fitter"]["psf"]
+        what = "FFT PSF model (%dx%dx%d stack)" % psf.shape
+    else:
+        what = "pupil-function model (%d px pupil)" % wl["fitter"]["pf_data"]["pf"].shape[0]
+    return {"workload": "%s, %d frames %dx%d, %d emitters, FP64 engine" % (what, F, shape[1], shape[0], units),
             "localizations_per_s": units / (min(ms) / 1e3), "ms_per_fit": min(ms),
             "cpu_localizations_per_s": n_cpu / wall_cpu if wall_cpu > 0 else None, "cpu_cores": cores,
+            "cpu_kind": "port (the oracle: direct separable DFTs; the reference's C transforms with FFTW, "
+                        "which is not installed, so it cannot be built or timed here)",
             "peaks": st["n"], "status_agree": st["status_agree"],
             "frac_within": min([st[k] for k in st if k.startswith("frac_ok")] or [1.0]),
             "max_dx": st.get("max_dx"), "max_dy": st.get("max_dy"), "max_dz": st.get("max_dz"),

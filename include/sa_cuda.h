@@ -173,6 +173,55 @@ void ftFitNewPeaks(saFitData *fit, double *peak_params, char *p_type, int n_peak
 /* fft_fit.c:165 ftFitCleanup (the PSF object stays the caller's) */
 void ftFitCleanup(saFitData *fit);
 
+/* The pupil-function PSF model.  pupilfn/pupil_function.c (bound by
+ * pupilfn/pupil_function_c.py): a complex pupil function of size x size
+ * samples (size even) with the geometry's kx, ky, kz (size x size doubles
+ * each), translated, and its PSF and derivatives as complex size x size
+ * arrays (real and imaginary parts), host-side. */
+/* pupil_function.c:321 pfnInitialize */
+void *pfnInitialize(double *kx, double *ky, double *kz, int size);
+/* pupil_function.c:42 pfnCleanup */
+void pfnCleanup(void *pupil_data);
+/* pupil_function.c:370 pfnSetPF */
+void pfnSetPF(void *pupil_data, double *r_pf, double *c_pf);
+/* pupil_function.c:419 pfnSetPNEN (dipole patterns of a vectorial PSF) */
+void pfnSetPNEN(void *pupil_data, double *px_ex, double *px_ey, double *py_ex, double *py_ey, double *pz_ex,
+                double *pz_ey);
+/* pupil_function.c:448 pfnTranslate (x, y in pixels, z in microns), :515 pfnTranslateZ */
+void pfnTranslate(void *pupil_data, double dx, double dy, double dz);
+void pfnTranslateZ(void *pupil_data, double dz);
+/* pupil_function.c:80 pfnGetPSF, :135 pfnGetPSFdx, :160 pfnGetPSFdy, :185 pfnGetPSFdz */
+void pfnGetPSF(void *pupil_data, double *psf_r, double *psf_c);
+void pfnGetPSFdx(void *pupil_data, double *psf_dx_r, double *psf_dx_c);
+void pfnGetPSFdy(void *pupil_data, double *psf_dy_r, double *psf_dy_c);
+void pfnGetPSFdz(void *pupil_data, double *psf_dz_r, double *psf_dz_c);
+/* pupil_function.c:108 pfnGetPSFIntensity */
+void pfnGetPSFIntensity(void *pupil_data, double *psf_r);
+/* pupil_function.c:239-302 pfnGetPXEX .. pfnGetPZEY (after pfnSetPNEN) */
+void pfnGetPXEX(void *pupil_data, double *psf_r, double *psf_c);
+void pfnGetPXEY(void *pupil_data, double *psf_r, double *psf_c);
+void pfnGetPYEX(void *pupil_data, double *psf_r, double *psf_c);
+void pfnGetPYEY(void *pupil_data, double *psf_r, double *psf_c);
+void pfnGetPZEX(void *pupil_data, double *psf_r, double *psf_c);
+void pfnGetPZEY(void *pupil_data, double *psf_r, double *psf_c);
+/* pupil_function.c:309 pfnGetSize */
+int pfnGetSize(void *pupil_data);
+
+/* pupilfn/pupil_fit.c (bound by pupilfn/pupil_fit_c.py).  The pupil model
+ * runs in the FP64 engine whatever saSetPrecision asked for; the handle
+ * keeps the pupil function's tables as they are at pfitInitialize.  kx
+ * must be constant along the pupil function's rows (pfnTranslate takes the
+ * x shift from its first column); pfitInitialize returns NULL otherwise. */
+/* pupil_fit.c:288 pfitInitialize (pupil_data from pfnInitialize) */
+saFitData *pfitInitialize(void *pupil_data, double *rqe, double *scmos_calibration, double tol, int im_size_x,
+                          int im_size_y);
+/* pupil_fit.c:342 pfitNewPeaks */
+void pfitNewPeaks(saFitData *fit, double *peak_params, char *p_type, int n_peaks);
+/* pupil_fit.c:511 pfitSetZRange (the z clamp; open until called) */
+void pfitSetZRange(saFitData *fit, double min_z, double max_z);
+/* pupil_fit.c:180 pfitCleanup (the pupil data stays the caller's) */
+void pfitCleanup(saFitData *fit);
+
 /* ---- shared LM core (sa_library/multi_fit.c) ----------------------------- */
 
 /* multi_fit.c:90 mFitAnscombeTransformImage (ALS only; reports an error) */

@@ -19,7 +19,7 @@ from numpy.ctypeslib import ndpointer
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 
-MODELS = {"2dfixed": 0, "2d": 1, "3d": 2, "Z": 3, "spline2D": 4, "spline3D": 5, "fft": 6}
+MODELS = {"2dfixed": 0, "2d": 1, "3d": 2, "Z": 3, "spline2D": 4, "spline3D": 5, "fft": 6, "pupil": 7}
 PEAK_TYPES = {"finder": 0, "testing": 1, "text": 2, "hdf5": 2}
 DPROPS = {"background": 0, "bg_sum": 1, "error": 2, "fg_sum": 3, "height": 4, "sum": 5,
           "x": 6, "xsigma": 7, "y": 8, "ysigma": 9, "z": 10, "jacobian": 11}
@@ -79,6 +79,7 @@ def load():
     lib.oraSolve.argtypes = [f64, f64, ctypes.c_int]
     lib.oraSolve.restype = ctypes.c_int
     lib.oraFFTEval.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, f64, f64, f64, f64]
+    lib.oraPupilEval.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double] + [f64] * 8
     _lib = lib
     return lib
 
@@ -101,11 +102,11 @@ class OracleFitter(object):
 
     def __init__(self, model, shape, rqe=None, scmos_cal=None, roi_size=10, sigma_range=None,
                  wx_params=None, wy_params=None, min_z=None, max_z=None, spline=None,
-                 tol=1.0e-6, psf=None):
+                 tol=1.0e-6, psf=None, pupil=None):
         lib = load()
         self.lib = lib
         self.model = model
-        self.spline = model.startswith("spline") or model == "fft"
+        self.spline = model.startswith("spline") or model in ("fft", "pupil")
         ny, nx = shape
         self.shape = (ny, nx)
         rqe = numpy.ones(shape) if rqe is None else rqe
@@ -122,7 +123,18 @@ class OracleFitter(object):
                                      dtype=numpy.float64)
         zmin = 0.0 if min_z is None else float(min_z)
         zmax = 0.0 if max_z is None else float(max_z)
-        if model == "fft":
+        if model == "pupil":
+            # pfnInitialize / pfnSetPF inputs: the geometry's kx, ky, kz and
+            # the pupil function (pupil = (kx, ky, kz, pf)); the z clamp of
+            # pfitSetZRange, open when not given
+            kx, ky, kz, pf = pupil
+            n = numpy.asarray(kx).shape[0]
+            aij = numpy.concatenate([numpy.ascontiguousarray(a, dtype=numpy.float64).ravel()
+                                     for a in (kx, ky, numpy.real(kz), numpy.real(pf), numpy.imag(pf))])
+            sx, sy, sz = n, n, 0
+            zmin = -1.0e300 if min_z is None else float(min_z)
+            zmax = 1.0e300 if max_z is None else float(max_z)
+        elif model == "fft":
             # the PSF's spectrum as pFTInitialize computes it (oracle/psf_fft.py)
             from . import psf_fft
             psf = numpy.ascontiguousarray(psf, dtype=numpy.float64)
@@ -141,6 +153,7 @@ class OracleFitter(object):
                                wx, wy, zmin, zmax, numpy.ascontiguousarray(aij), sx, sy, sz)
         self.iterations = 0
         self.psf_shape = None if psf is None else numpy.asarray(psf).shape
+        self.pupil_size = None if pupil is None else numpy.asarray(pupil[0]).shape[0]
 
     def cleanup(self, verbose=False):
         if self.h:
@@ -250,6 +263,16 @@ def fit_frames(workload, indices, max_iterations=200, props=("x", "y", "z", "hei
         results.append({p: fitter.getPeakProperty(p) for p in props})
     fitter.cleanup()
     return results
+
+
+def pupil_eval(fitter, dx, dy, dz):
+    """The pupil model's complex PSF and its x, y, z derivatives on the
+    pupil grid (index [u, v], u along the pupil's first index) for a
+    translation (dx, dy, dz): oraPupilEval."""
+    n = fitter.pupil_size
+    out = [numpy.zeros((n, n)) for _ in range(8)]
+    fitter.lib.oraPupilEval(fitter.h, dx, dy, dz, *out)
+    return [out[2 * i] + 1j * out[2 * i + 1] for i in range(4)]
 
 
 def fft_eval(fitter, dx, dy, dz):

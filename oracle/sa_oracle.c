@@ -58,7 +58,9 @@ struct oraFit {
   double xoff, yoff, zoff, tol, min_height;
   double wmin, wmax, zmin, zmax, wx[5], wy[5];
   int sx, sy, sz;
-  double *aij;            /* spline coefficients; ORA_FFT: the PSF spectrum (re, im) */
+  double *aij;            /* spline coefficients; ORA_FFT: the PSF spectrum (re, im);
+                             ORA_PUPIL: 2 pi kx, 2 pi ky, 2 pi kz, then the pupil
+                             function as pfnSetPF stores it (re, im), see pupil_eval */
   double *fft_tw;         /* ORA_FFT: twiddle tables, see fft_eval */
   double *rqe, *scmos, *x, *f, *bg, *bgest, *err, *tfi;
   int *cnt, *stale;
@@ -91,6 +93,7 @@ static void peak_copy(const oraFit *fit, OPeak *dst, const OPeak *src)
 }
 
 static int is_fft(const oraFit *fit) { return fit->model == ORA_FFT; }
+static int is_pupil(const oraFit *fit) { return fit->model == ORA_PUPIL; }
 
 static int is_spline(const oraFit *fit)
 {
@@ -399,11 +402,131 @@ void oraFFTEval(const oraFit *fit, double dx, double dy, double dz, double *psf,
   fft_eval(fit, dx, dy, dz, psf, gx, gy, gz);
 }
 
+/* ORA_PUPIL: the complex PSF of the translated pupil function and its x, y,
+ * z derivatives on the pupil grid, index u * N + v with u along the pupil's
+ * first index (pfnTranslate pupil_function.c:448-506, pfnGetPSF :80-98,
+ * pfnGetPSFdx / dy / dz :135-203: FFTW's unnormalised backward 2D DFT of
+ * the translated pupil function, times -i kx, -i ky, -i kz for the
+ * derivatives, dz negated).  The DFT is evaluated directly: sums over the
+ * second index, then over the first.  Any output may be NULL. */
+static void pupil_eval(const oraFit *fit, double dx, double dy, double dz, double *pr, double *pc,
+                       double *xr, double *xc, double *yr, double *yc, double *zr, double *zc)
+{
+  int n = fit->sx, m = n / 2, m1 = m + 1, i, j, k, u, v, f;
+  size_t nn = (size_t)n * n;
+  const double *kx = fit->aij, *ky = kx + nn, *kz = ky + nn, *pf = kz + nn;
+  double *sx = malloc(sizeof(double) * 4 * n), *szt = malloc(sizeof(double) * 2 * m1 * m1);
+  double *ws = malloc(sizeof(double) * 2 * nn), *in = malloc(sizeof(double) * 2 * nn);
+  double *mid = malloc(sizeof(double) * 2 * nn), *tw = malloc(sizeof(double) * 2 * nn);
+  double *sy = sx + 2 * n;
+  double *outs[4][2];
+  outs[0][0] = pr; outs[0][1] = pc;
+  outs[1][0] = xr; outs[1][1] = xc;
+  outs[2][0] = yr; outs[2][1] = yc;
+  outs[3][0] = zr; outs[3][1] = zc;
+  /* pfnTranslate: x and y multipliers from kx's first column, z over the
+   * pie slice with -dz */
+  for (i = 0; i < n; i++) {
+    double dd = kx[(size_t)i * n] * dx;
+    sx[2 * i] = cos(dd);
+    sx[2 * i + 1] = -sin(dd);
+    dd = kx[(size_t)i * n] * dy;
+    sy[2 * i] = cos(dd);
+    sy[2 * i + 1] = -sin(dd);
+  }
+  for (i = 0; i <= m; i++) {
+    for (j = i; j <= m; j++) {
+      double dd = -kz[(size_t)(m - i) * n + (m - j)] * dz;
+      szt[2 * (i * m1 + j)] = cos(dd);
+      szt[2 * (i * m1 + j) + 1] = -sin(dd);
+      szt[2 * (j * m1 + i)] = szt[2 * (i * m1 + j)];
+      szt[2 * (j * m1 + i) + 1] = szt[2 * (i * m1 + j) + 1];
+    }
+  }
+  for (i = 0; i < n; i++) {
+    for (j = 0; j < n; j++) {
+      size_t l = (size_t)i * n + j;
+      int o = abs(i - m) * m1 + abs(j - m);
+      double r2 = sx[2 * i] * sy[2 * j] - sx[2 * i + 1] * sy[2 * j + 1];
+      double c2 = sx[2 * i] * sy[2 * j + 1] + sx[2 * i + 1] * sy[2 * j];
+      double r1 = r2 * szt[2 * o] - c2 * szt[2 * o + 1];
+      double c1 = r2 * szt[2 * o + 1] + c2 * szt[2 * o];
+      ws[2 * l] = r1 * pf[2 * l] - c1 * pf[2 * l + 1];
+      ws[2 * l + 1] = r1 * pf[2 * l + 1] + c1 * pf[2 * l];
+    }
+  }
+  for (u = 0; u < n; u++) {
+    for (v = 0; v < n; v++) {
+      double a = 2.0 * ORA_PI * (double)(((long)u * v) % n) / (double)n;
+      tw[2 * ((size_t)u * n + v)] = cos(a);
+      tw[2 * ((size_t)u * n + v) + 1] = sin(a);
+    }
+  }
+  for (f = 0; f < 4; f++) {
+    const double *km = (f == 1) ? kx : ((f == 2) ? ky : kz);
+    if (!outs[f][0] && !outs[f][1]) continue;
+    for (i = 0; i < (int)nn; i++) {
+      if (f == 0) {
+        in[2 * i] = ws[2 * i];
+        in[2 * i + 1] = ws[2 * i + 1];
+      } else {
+        in[2 * i] = ws[2 * i + 1] * km[i];
+        in[2 * i + 1] = -ws[2 * i] * km[i];
+      }
+    }
+    for (i = 0; i < n; i++) {
+      for (v = 0; v < n; v++) {
+        double sr = 0.0, si = 0.0;
+        for (k = 0; k < n; k++) {
+          const double *a = in + 2 * ((size_t)i * n + k), *t = tw + 2 * ((size_t)k * n + v);
+          sr += a[0] * t[0] - a[1] * t[1];
+          si += a[0] * t[1] + a[1] * t[0];
+        }
+        mid[2 * ((size_t)i * n + v)] = sr;
+        mid[2 * ((size_t)i * n + v) + 1] = si;
+      }
+    }
+    for (u = 0; u < n; u++) {
+      for (v = 0; v < n; v++) {
+        double sr = 0.0, si = 0.0, sg = (f == 3) ? -1.0 : 1.0;
+        for (i = 0; i < n; i++) {
+          const double *a = mid + 2 * ((size_t)i * n + v), *t = tw + 2 * ((size_t)i * n + u);
+          sr += a[0] * t[0] - a[1] * t[1];
+          si += a[0] * t[1] + a[1] * t[0];
+        }
+        if (outs[f][0]) outs[f][0][(size_t)u * n + v] = sg * sr;
+        if (outs[f][1]) outs[f][1][(size_t)u * n + v] = sg * si;
+      }
+    }
+  }
+  free(sx); free(szt); free(ws); free(in); free(mid); free(tw);
+}
+
+/* Exported for the tests of the evaluation itself. */
+void oraPupilEval(const oraFit *fit, double dx, double dy, double dz, double *pr, double *pc, double *xr,
+                  double *xc, double *yr, double *yc, double *zr, double *zc)
+{
+  pupil_eval(fit, dx, dy, dz, pr, pc, xr, xc, yr, yc, zr, zc);
+}
+
 /* Peak shape into pk->psf: daoCalcPeakShape dao_fit.c:968-998 (note the
  * y offset also uses xoff, :979), cfCalcPeakShape cubic_fit.c:435-502. */
 static void peak_shape(const oraFit *fit, OPeak *pk)
 {
   int i;
+  if (is_pupil(fit)) {
+    /* pfitCalcPeakShape pupil_fit.c:133-170: |psf|^2 at psf[roi_x * N + roi_y] */
+    size_t ng = (size_t)fit->sx * fit->sx;
+    double *gr = malloc(sizeof(double) * 2 * ng), *gc = gr + ng;
+    pupil_eval(fit, pk->p[PX] - (double)pk->xi, pk->p[PY] - (double)pk->yi, pk->p[PZ], gr, gc, NULL, NULL, NULL,
+               NULL, NULL, NULL);
+    for (i = 0; i < fit->nroi; i++) {
+      size_t g = (size_t)fit->rx[i] * fit->sx + fit->ry[i];
+      pk->psf[i] = gr[g] * gr[g] + gc[g] * gc[g];
+    }
+    free(gr);
+    return;
+  }
   if (is_fft(fit)) {
     /* ftFitCalcPeakShape fft_fit.c:127-155 */
     double *grid = malloc(sizeof(double) * fit->sx * fit->sy);
@@ -524,7 +647,13 @@ static void calc_jh(const oraFit *fit, const OPeak *pk, double *jac, double *hes
   for (l = 0; l < n; l++) jac[l] = 0.0;
   for (l = 0; l < n * n; l++) hes[l] = 0.0;
 
-  if (is_fft(fit)) {
+  if (is_pupil(fit)) {
+    /* pfitCalcJH3D pupil_fit.c:45-123: translate, then the derivatives */
+    size_t ng = (size_t)fit->sx * fit->sx;
+    fg = malloc(sizeof(double) * 8 * ng);
+    pupil_eval(fit, pk->p[PX] - (double)pk->xi, pk->p[PY] - (double)pk->yi, pk->p[PZ], fg, fg + ng, fg + 2 * ng,
+               fg + 3 * ng, fg + 4 * ng, fg + 5 * ng, fg + 6 * ng, fg + 7 * ng);
+  } else if (is_fft(fit)) {
     /* ftFitCalcJH3D fft_fit.c:43-117: translate, then the derivatives */
     size_t ng = (size_t)fit->sx * fit->sy;
     fg = malloc(sizeof(double) * 3 * ng);
@@ -602,6 +731,17 @@ static void calc_jh(const oraFit *fit, const OPeak *pk, double *jac, double *hes
       jt[4] = rq;
       break;
     }
+    case ORA_PUPIL: {
+      /* pupil_fit.c:103-107 */
+      size_t ng = (size_t)fit->sx * fit->sx, g = (size_t)rx * fit->sx + ry;
+      double ar = fg[g], ac = fg[ng + g];
+      jt[0] = rq * (ar * ar + ac * ac);
+      jt[1] = rq * 2.0 * h * (ar * fg[2 * ng + g] + ac * fg[3 * ng + g]);
+      jt[2] = rq * 2.0 * h * (ar * fg[4 * ng + g] + ac * fg[5 * ng + g]);
+      jt[3] = rq * 2.0 * h * (ar * fg[6 * ng + g] + ac * fg[7 * ng + g]);
+      jt[4] = rq;
+      break;
+    }
     case ORA_SPLINE3D: {
       const double *c = cell3d(fit, pk->zi, ry + pk->ys, rx + pk->xs);
       jt[0] = rq * pk->psf[j];
@@ -676,6 +816,13 @@ static void apply_update(const oraFit *fit, OPeak *pk, const double *d)
     if (pk->p[PZ] > max_z) pk->p[PZ] = max_z;
     break;
   }
+  case ORA_PUPIL:
+    /* pfitUpdate3D pupil_fit.c:529-546, pfitZRangeCheck :555-570 */
+    pk->p[PH] -= d[0]; pk->p[PX] -= d[1]; pk->p[PY] -= d[2]; pk->p[PZ] -= d[3]; pk->p[PBG] -= d[4];
+    anchor_update(pk);
+    if (pk->p[PZ] < fit->zmin) pk->p[PZ] = fit->zmin;
+    if (pk->p[PZ] > fit->zmax) pk->p[PZ] = fit->zmax;
+    break;
   default: { /* ORA_SPLINE3D */
     double zmax;
     pk->p[PH] -= d[0]; pk->p[PX] -= d[1]; pk->p[PY] -= d[2]; pk->p[PZ] -= d[3]; pk->p[PBG] -= d[4];
@@ -796,7 +943,30 @@ oraFit *oraCreate(int model, const double *rqe, const double *scmos, double tol,
   case ORA_SPLINE2D: fit->jac = 4; break;
   default: fit->jac = 5; break;
   }
-  if (is_fft(fit)) {
+  if (is_pupil(fit)) {
+    /* pfitInitialize pupil_fit.c:288-332 with pfnInitialize / pfnSetPF
+     * pupil_function.c:321-410: aij holds kx, ky, kz and the pupil
+     * function's real and imaginary parts (sx x sx each); ROI = sx,
+     * xoff = yoff = sx / 2 */
+    size_t nn = (size_t)sx * sx, l;
+    int a, b;
+    fit->sx = sx; fit->sy = sx; fit->sz = 0;
+    fit->aij = (double *)malloc(sizeof(double) * 5 * nn);
+    for (l = 0; l < 3 * nn; l++) fit->aij[l] = 2.0 * ORA_PI * aij[l];
+    for (a = 0; a < sx; a++) {
+      for (b = 0; b < sx; b++) {
+        double sg = (((a + b) % 2) == 0) ? 1.0 : -1.0, nrm = 1.0 / ((double)sx);
+        l = (size_t)a * sx + b;
+        fit->aij[3 * nn + 2 * l] = sg * aij[3 * nn + l] * nrm;
+        fit->aij[3 * nn + 2 * l + 1] = sg * aij[4 * nn + l] * nrm;
+      }
+    }
+    fit->xoff = 0.5 * ((double)sx);
+    fit->yoff = 0.5 * ((double)sx);
+    fit->zmin = zmin;
+    fit->zmax = zmax;
+    roi_index(fit, sx);
+  } else if (is_fft(fit)) {
     /* ftFitInitialize fft_fit.c:254-310: ROI = PSF x size */
     size_t nc = (size_t)sz * sy * (sx / 2 + 1) * 2;
     fit->sx = sx; fit->sy = sy; fit->sz = sz;
@@ -935,7 +1105,7 @@ void oraNewPeaks(oraFit *fit, const double *peaks, int ptype, int n_peaks)
 {
   /* arbitrary-PSF input formats (x, y, z [, background, height]) for the
    * splines and the FFT PSF (cubic_fit.c:776-914, fft_fit.c:318-470) */
-  int i, start, stop, spline = is_spline(fit) || is_fft(fit);
+  int i, start, stop, spline = is_spline(fit) || is_fft(fit) || is_pupil(fit);
   int ncol;
   grow_peaks(fit, n_peaks);
   start = fit->nfit;
@@ -1088,7 +1258,7 @@ void oraIterate(oraFit *fit)
         continue;
       }
       apply_update(fit, w, wjac);
-      if ((is_spline(fit) || is_fft(fit)) ? base_check(fit, w) : model_check(fit, w)) {
+      if ((is_spline(fit) || is_fft(fit) || is_pupil(fit)) ? base_check(fit, w) : model_check(fit, w)) {
         reset_working(fit, i);
         w->status = ERROR;
         continue;

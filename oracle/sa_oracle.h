@@ -24,6 +24,7 @@
 #define ORA_SPLINE2D  4   /* cubic_fit.c cfInitialize2D     */
 #define ORA_SPLINE3D  5   /* cubic_fit.c cfInitialize3D     */
 #define ORA_FFT       6   /* psf_fft/fft_fit.c ftFitInitialize: FFT-translated 3D PSF */
+#define ORA_PUPIL     7   /* pupilfn/pupil_fit.c pfitInitialize: pupil-function PSF */
 
 /* Peak input formats (dao_fit.c:1603-1753, cubic_fit.c:776-914). */
 #define ORA_PEAKS_FINDER   0
@@ -59,7 +60,10 @@ typedef struct oraFit oraFit;
  *                 for ORA_FFT the PSF's r2c spectrum (pFTInitialize
  *                 psf_fft.c:253-318: the transform of psf / (sz*sy*sx)) as
  *                 (re, im) pairs, sz x sy x (sx/2 + 1), and the PSF's x, y,
- *                 z sizes in sx, sy, sz.
+ *                 z sizes in sx, sy, sz; for ORA_PUPIL the geometry's kx,
+ *                 ky, kz and the pupil function's real and imaginary parts
+ *                 (sx x sx doubles each, as pfnInitialize / pfnSetPF take
+ *                 them), the pupil size in sx and the z clamp in zmin, zmax.
  */
 oraFit *oraCreate(int model, const double *rqe, const double *scmos, double tol,
                   int nx, int ny, int roi_size,
@@ -97,6 +101,12 @@ void oraRemoveRunningPeaks(oraFit *fit);
  * which: 0 f, 1 dx, 2 dy, 3 dz. */
 double oraSplineEval3D(const double *aij, int sx, int sy, int sz,
                        double z, double y, double x, int which);
+
+/* ORA_PUPIL: the complex PSF of the pupil function translated by (dx, dy,
+ * dz) and its x, y, z derivatives on the sx x sx pupil grid (index
+ * u * sx + v); any output may be NULL. */
+void oraPupilEval(const oraFit *fit, double dx, double dy, double dz, double *pr, double *pc, double *xr,
+                  double *xc, double *yr, double *yc, double *zr, double *zc);
 
 /* FP64 Cholesky solve of a k x k system given as a row-major upper triangle
  * (the layout dposv("Lower") reads, multi_fit.c:1851).  Returns 0 on success. */

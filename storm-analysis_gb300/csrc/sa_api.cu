@@ -13,6 +13,7 @@
 
 #include "sa_launch.h"
 #include "sa_psf_fft.h"
+#include "sa_pupil_fn.h"
 #include "sa_cuda.h"
 
 using namespace sa;
@@ -258,8 +259,8 @@ struct Engine {
       set_error("the fitting model has not been initialised");
       return -1;
     }
-    // the FFT PSF model runs in the FP64 engine only
-    if (cfg.model == M_FFT) prec = 64;
+    // the FFT PSF and pupil-function models run in the FP64 engine only
+    if (cfg.model == M_FFT || cfg.model == M_PUPIL) prec = 64;
     cudaError_t e = (prec == 32) ? Launch<float>::configure(cfg, &sweep_grid, &sweep_smem, &cta_smem, &warp_smem)
                                  : Launch<double>::configure(cfg, &sweep_grid, &sweep_smem, &cta_smem, &warp_smem);
     if (e != cudaSuccess) {
@@ -309,8 +310,8 @@ struct Engine {
       if (upload_t(&d_rqe, rqe_h.data(), npix)) return -1;
       if (upload_t(&d_scmos, scmos_h.data(), npix)) return -1;
       if (!aij_h.empty() && upload_t(&d_aij, aij_h.data(), aij_h.size())) return -1;
-      // the FFT model's tables (FP64: d_aij holds them as doubles)
-      if (cfg.model == M_FFT) cfg.fft = static_cast<const double*>(d_aij);
+      // the FFT and pupil models' tables (FP64: d_aij holds them as doubles)
+      if (cfg.model == M_FFT || cfg.model == M_PUPIL) cfg.fft = static_cast<const double*>(d_aij);
       CK(cudaMalloc(&d_roi, roi_xy.size() * sizeof(unsigned short)));
       CK(cudaMemcpy(d_roi, roi_xy.data(), roi_xy.size() * sizeof(unsigned short), cudaMemcpyHostToDevice));
     }
@@ -1305,6 +1306,65 @@ void ftFitNewPeaks(saFitData* h, double* peaks, char* p_type, int n) { new_peaks
 // ftFitCleanup fft_fit.c:165-192 (the PSF object is the caller's, freed by
 // pFTCleanup).
 void ftFitCleanup(saFitData* h) { daoCleanup(h); }
+
+// ---- the pupil-function fitter (pupilfn/pupil_fit.c; pupilfn/pupil_fit_c.py binds it) ----
+
+// pfitInitialize pupil_fit.c:288-332: the ROI is the pupil size,
+// xoff = yoff = size / 2, five parameters (height, x, y, z, background).
+// The handle keeps the pupil function's device tables as they are at this
+// call (the reference reads the pupil data at each evaluation; its Python
+// sets the pupil function before creating the fitter and not after); the
+// pupil model runs in the FP64 engine.  The z range is open until
+// pfitSetZRange.
+saFitData* pfitInitialize(void* pupil_data, double* rqe, double* scmos, double tol, int nx, int ny) {
+  const PupilH* p = reinterpret_cast<const PupilH*>(pupil_data);
+  if (!p) {
+    set_error("pfitInitialize: NULL pupil_data");
+    return nullptr;
+  }
+  if (p->n < 2 || p->n > MAX_ROI || (p->n % 2) != 0) {
+    set_error("unsupported pupil function size %d", p->n);
+    return nullptr;
+  }
+  if (!pupil_rows_separable(*p)) {
+    // pfnTranslate takes the x shift from kx's first column; the engine's
+    // x derivative does the same
+    set_error("pfitInitialize: kx must be constant along the pupil function's rows");
+    return nullptr;
+  }
+  saFitData* h = new_handle(rqe, scmos, tol, nx, ny);
+  if (!h) return nullptr;
+  Engine* e = E(h);
+  e->prec = 64;
+  e->cfg.sx = p->n;
+  e->cfg.sy = p->n;
+  e->cfg.sz = 0;
+  e->cfg.zmin = -1.0e300;
+  e->cfg.zmax = 1.0e300;
+  pupil_tables(*p, e->aij_h);
+  e->cfg.xoff = 0.5 * (double)p->n;
+  e->cfg.yoff = 0.5 * (double)p->n;
+  roi_index(e, p->n);
+  publish_geometry(h);
+  set_model(h, M_PUPIL, 5);
+  return h;
+}
+
+// pfitNewPeaks pupil_fit.c:342-503 ("finder" / "testing": x, y, z;
+// "text" / "hdf5": x, y, z, background, height).
+void pfitNewPeaks(saFitData* h, double* peaks, char* p_type, int n) { new_peaks_single(h, peaks, p_type, n); }
+
+// pfitSetZRange pupil_fit.c:511-518: the clamp of pfitZRangeCheck :555-570.
+void pfitSetZRange(saFitData* h, double min_z, double max_z) {
+  Engine* e = E(h);
+  if (!e) return;
+  e->cfg.zmin = min_z;
+  e->cfg.zmax = max_z;
+}
+
+// pfitCleanup pupil_fit.c:180-211 (the pupil data is the caller's, freed by
+// pfnCleanup).
+void pfitCleanup(saFitData* h) { daoCleanup(h); }
 
 void mFitNewImage(saFitData* h, double* img) { image_single(h, img, false); }
 void mFitNewBackground(saFitData* h, double* bg) { image_single(h, bg, true); }

@@ -26,7 +26,7 @@ enum { PH = 0, PX = 1, PXW = 2, PY = 3, PYW = 4, PBG = 5, PZ = 6 };
 // Peak status (multi_fit.h:33-35).
 enum { RUNNING = 0, CONVERGED = 1, ERROR = 2 };
 // Models.
-enum { M_2DFIXED = 0, M_2D = 1, M_3D = 2, M_Z = 3, M_SPLINE2D = 4, M_SPLINE3D = 5, M_FFT = 6 };
+enum { M_2DFIXED = 0, M_2D = 1, M_3D = 2, M_Z = 3, M_SPLINE2D = 4, M_SPLINE3D = 5, M_FFT = 6, M_PUPIL = 7 };
 // Counter slots in the reference's fitData order (multi_fit.h:87-94), plus
 // one diagnostic slot of our own: starting-error evaluations that met fi <= 0.
 enum { C_DPOSV = 0, C_ITER, C_LOST, C_MARGIN, C_NEGFI, C_NEGH, C_NONCONV, C_NONDECR, C_STARTFAIL,
@@ -71,7 +71,7 @@ struct ModelCfg {
   int jac;
   int nx, ny;
   int roi, nroi;
-  int sx, sy, sz;        // spline cells (x, y, z); M_FFT: the PSF's x, y, z sizes
+  int sx, sy, sz;        // spline cells (x, y, z); M_FFT: the PSF's x, y, z sizes; M_PUPIL: sx = sy = pupil size
   int dil;               // footprint dilation (pixels)
   int cell;              // scheduling grid cell (pixels)
   int gx, gy;            // grid cells per frame
@@ -79,14 +79,15 @@ struct ModelCfg {
   double tol;
   double wmin, wmax;
   double wx[5], wy[5];   // w0 stored squared (dao_fit.c:1566-1567)
-  double zmin, zmax;
+  double zmin, zmax;     // M_Z, M_PUPIL: the z clamp
   double min_height;
   int force_serial;      // 1: every frame runs its peaks strictly in index order
   int rqe_one;           // 1: rqe is 1 at every pixel (no per-pixel loads)
   int scmos_zero;        // 1: the sCMOS term is 0 at every pixel
   int dil_late;          // dilation from sweep dil_switch on (<= dil)
   int dil_switch;
-  const double* fft;     // M_FFT: the PSF's spectrum and twiddle tables on the device (fft_layout)
+  const double* fft;     // M_FFT: the PSF's spectrum and twiddle tables on the device (fft_layout);
+                         // M_PUPIL: the pupil function's tables (pupil_layout)
 };
 
 // Per-frame control block of the device state machine.

@@ -573,10 +573,58 @@ __host__ __device__ __forceinline__ FFTLayout fft_layout(int nx, int ny, int nz)
   L.total = L.dkz + nz;
   return L;
 }
+__host__ __device__ __forceinline__ bool is_pupil(int model) { return model == M_PUPIL; }
+
+// The pupil-function model's device tables (doubles), pupil size N (even),
+// m = N / 2:
+//   E   [N][N] (re, im)  e^{2 pi i a b / N}: the backward DFT's twiddles
+//   PF  [N][N] (re, im)  the pupil function / N, negated where i + k is odd
+//                        (pfnSetPF pupil_function.c:370-410)
+//   KX  [N]              2 pi kx[i N]: the x and y shift multipliers of
+//                        pfnTranslate :453-463 and the x derivative's
+//   KY  [N][N]           2 pi ky: the y derivative's multiplier (:160-178)
+//   KZ  [N][N]           2 pi kz: the z derivative's multiplier (:185-203)
+//   KZS [m+1][m+1]       2 pi kz at (m - min(a, b), m - max(a, b)): the z
+//                        shift multiplier of pixel offset (a, b) from the
+//                        centre, pfnTranslate's pie slice :475-486
+struct PupilLayout {
+  int e, pf, kx, ky, kz, kzs, total;
+};
+__host__ __device__ __forceinline__ PupilLayout pupil_layout(int n) {
+  PupilLayout L;
+  const int m1 = n / 2 + 1;
+  L.e = 0;
+  L.pf = L.e + 2 * n * n;
+  L.kx = L.pf + 2 * n * n;
+  L.ky = L.kx + n;
+  L.kz = L.ky + n * n;
+  L.kzs = L.kz + n * n;
+  L.total = L.kzs + m1 * m1;
+  return L;
+}
+// Doubles of a warp's pupil scratch: B, By, Bz [N][N] (complex; the sums
+// over the pupil's second index of the translated pupil function, and of it
+// times -i ky and -i kz), three row buffers [N] (complex), the shift
+// vectors sx, sy [N] (complex) and the z shift table [m+1][m+1] (complex).
+__host__ __device__ __forceinline__ int pupil_scratch_doubles(int n) {
+  const int m1 = n / 2 + 1;
+  return 6 * n * n + 10 * n + 2 * m1 * m1;
+}
+// Warps with a workspace in a per-frame CTA (k_prepare, k_post) and in an
+// auxiliary CTA for the pupil model: its scratch is ~54 KB per warp at a
+// 30-pixel pupil, ~110 KB at 44 pixels.
+__host__ __device__ __forceinline__ int pupil_ws_warps(int n) { return n <= 30 ? 4 : (n <= 44 ? 2 : 1); }
+
 // Warps of a 1024-thread per-frame CTA (k_prepare, k_post) that carry a
-// workspace: all 32, or 8 for the FFT PSF model, whose shape scratch is
-// ~20 KB per warp.
-__host__ __device__ __forceinline__ int cta_ws_warps(int model) { return model == M_FFT ? 8 : 32; }
+// workspace: all 32, 8 for the FFT PSF model, whose shape scratch is
+// ~20 KB per warp, and pupil_ws_warps for the pupil model.
+__host__ __device__ __forceinline__ int cta_ws_warps(const ModelCfg& cfg) {
+  return cfg.model == M_FFT ? 8 : (cfg.model == M_PUPIL ? pupil_ws_warps(cfg.sx) : 32);
+}
+// Warps of the warp-per-peak auxiliary kernels' CTAs.
+__host__ __device__ __forceinline__ int aux_warps(const ModelCfg& cfg) {
+  return cfg.model == M_PUPIL ? pupil_ws_warps(cfg.sx) : 8;
+}
 
 // Doubles of a warp's FFT scratch: C, Cz [ny][nk], D, Dy, Dz [ny][nk]
 // (complex), the shift vectors sx [nk], sy [ny], sz [nz] (complex).
@@ -623,7 +671,8 @@ struct WarpWS {
   float* Cs;
   float* tab0;  // shape tables of the step's start: ex hi, ex lo, ey hi, ey lo, xt, yt
   float* tab1;  // trial tables (same layout) / pass-1 gradient tables / solve scratch
-  double* fw;   // M_FFT: the shape evaluation's scratch (fft_scratch_doubles)
+  double* fw;   // M_FFT / M_PUPIL: the shape evaluation's scratch (fft_scratch_doubles,
+                // pupil_scratch_doubles)
   float* par0;  // float-float parameter slots (g32_params) of the step's start record
   float* par1;  // ... and of the current trial
   int ts;       // table stride (ROI size rounded up to 32)
@@ -652,6 +701,7 @@ __host__ __device__ inline size_t warp_ws_bytes(const ModelCfg& cfg, int nroi) {
   b += 3 * sizeof(PeakRec);
   if (sizeof(T) == 4 && !gauss32<T>(cfg) && nroi > 0) b += 32 * 33 * sizeof(float);
   if (is_fft(cfg.model)) b = ((b + 15) & ~(size_t)15) + fft_scratch_doubles(cfg.sx, cfg.sy, cfg.sz) * sizeof(double);
+  if (is_pupil(cfg.model)) b = ((b + 15) & ~(size_t)15) + pupil_scratch_doubles(cfg.sx) * sizeof(double);
   return (b + 127) & ~(size_t)127;
 }
 
@@ -713,7 +763,7 @@ __device__ inline WarpWS<T> warp_ws(char* base, const ModelCfg& cfg, int nroi) {
   if (!gauss32<T>(cfg))
     ws.red = reinterpret_cast<float*>(base + off + 52 * sizeof(double) + 3 * sizeof(PeakRec));
   ws.fw = nullptr;
-  if (is_fft(cfg.model)) {
+  if (is_fft(cfg.model) || is_pupil(cfg.model)) {
     size_t o = off + 52 * sizeof(double) + 3 * sizeof(PeakRec);
     if (sizeof(T) == 4 && nroi > 0) o += 32 * 33 * sizeof(float);
     ws.fw = reinterpret_cast<double*>(base + ((o + 15) & ~(size_t)15));
@@ -1155,11 +1205,177 @@ __device__ inline double fft_pixel(const ModelCfg& cfg, const double* fw, int rx
   return vp;
 }
 
+// ---------------------------------------------------------------------------
+// Pupil-function model (M_PUPIL, the FP64 engine): pfitCalcPeakShape
+// pupil_fit.c:133-170 and pfitCalcJH3D :45-123 through pfnTranslate /
+// pfnGetPSF / pfnGetPSFdx / dy / dz (pupil_function.c).  The complex PSF at
+// pixel (u, v) -- u along the pupil's first index, which is the ROI's x
+// (pupil_fit.c reads psf_r[roi_x * fit_size_y + roi_y]) -- is FFTW's
+// unnormalised backward 2D transform of the translated pupil function ws,
+//   psf(u, v) = sum_i e^{2 pi i i u / N} sum_k ws[i][k] e^{2 pi i k v / N},
+// evaluated separably: the inner sums B[i][v] (and By, Bz: the same of ws
+// times -i ky and -i kz, for the y and z derivatives) in pupil_tables, the
+// outer sum per pixel in pupil_pixel, where the x derivative is the outer
+// sum of B times -i kx[i] (kx is constant along the pupil's rows, which
+// pfitInitialize checks on the host).
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ inline void pupil_tables(const ModelCfg& cfg, const PeakRec& w, WarpWS<T>& ws, int lane,
+                                    bool deriv) {
+  const int n = cfg.sx, m = n / 2, m1 = m + 1;
+  const PupilLayout L = pupil_layout(n);
+  double* B = ws.fw;
+  double* By = B + 2 * n * n;
+  double* Bz = By + 2 * n * n;
+  double* rw = Bz + 2 * n * n;   // the translated pupil function's row i (complex)
+  double* rwy = rw + 2 * n;      // ... times -i ky
+  double* rwz = rwy + 2 * n;     // ... times -i kz
+  double* sxv = rwz + 2 * n;     // x shift per first index (complex)
+  double* syv = sxv + 2 * n;     // y shift per second index (complex)
+  double* szt = syv + 2 * n;     // z shift per pie-slice offset [m+1][m+1] (complex)
+  const double* E = cfg.fft + L.e;
+  const double* PF = cfg.fft + L.pf;
+  const double* KX = cfg.fft + L.kx;
+  const double* KY = cfg.fft + L.ky;
+  const double* KZ = cfg.fft + L.kz;
+  const double* KZS = cfg.fft + L.kzs;
+  // pfitCalcPeakShape :148-150
+  const double dx = w.p[PX] - (double)w.xi, dy = w.p[PY] - (double)w.yi, dz = w.p[PZ];
+  // shift vectors, pfnTranslate :453-463 (both from kx's first column)
+  for (int i = lane; i < 2 * n; i += 32) {
+    const int j = i < n ? i : i - n;
+    const double dd = __ldg(KX + j) * (i < n ? dx : dy);
+    double sv, cv;
+    sincos(dd, &sv, &cv);
+    double* o = (i < n ? sxv : syv) + 2 * j;
+    o[0] = cv;
+    o[1] = -sv;
+  }
+  // z shift over the pie slice, :475-486 (with -dz); symmetric in (a, b)
+  for (int q = lane; q < m1 * m1; q += 32) {
+    const int a = q / m1, b = q - a * m1;
+    if (a <= b) {
+      const double dd = -__ldg(KZS + q) * dz;
+      double sv, cv;
+      sincos(dd, &sv, &cv);
+      szt[2 * q] = cv;
+      szt[2 * q + 1] = -sv;
+      szt[2 * (b * m1 + a)] = cv;
+      szt[2 * (b * m1 + a) + 1] = -sv;
+    }
+  }
+  __syncwarp();
+  for (int i = 0; i < n; i++) {
+    const double xr = sxv[2 * i], xc = sxv[2 * i + 1];
+    const int oa = abs(i - m) * m1;
+    for (int k = lane; k < n; k += 32) {
+      const int o = oa + abs(k - m);
+      // the reference's products in its order, :488-505
+      const double r2 = xr * syv[2 * k] - xc * syv[2 * k + 1];
+      const double c2 = xr * syv[2 * k + 1] + xc * syv[2 * k];
+      const double r1 = r2 * szt[2 * o] - c2 * szt[2 * o + 1];
+      const double c1 = r2 * szt[2 * o + 1] + c2 * szt[2 * o];
+      const double pr = __ldg(PF + 2 * (i * n + k)), pc = __ldg(PF + 2 * (i * n + k) + 1);
+      const double wr = r1 * pr - c1 * pc, wc = r1 * pc + c1 * pr;
+      rw[2 * k] = wr;
+      rw[2 * k + 1] = wc;
+      if (deriv) {
+        // times -i k: (wr, wc) -> (wc k, -wr k), pfnGetPSFdy / dz :165-168, :190-193
+        const double ky = __ldg(KY + i * n + k), kz = __ldg(KZ + i * n + k);
+        rwy[2 * k] = wc * ky;
+        rwy[2 * k + 1] = -wr * ky;
+        rwz[2 * k] = wc * kz;
+        rwz[2 * k + 1] = -wr * kz;
+      }
+    }
+    __syncwarp();
+    if (deriv) {
+      for (int v = lane; v < n; v += 32) {
+        double br = 0.0, bc = 0.0, yr = 0.0, yc = 0.0, zr = 0.0, zc = 0.0;
+        for (int k = 0; k < n; k++) {
+          const double er = __ldg(E + 2 * (k * n + v)), ei = __ldg(E + 2 * (k * n + v) + 1);
+          br += rw[2 * k] * er - rw[2 * k + 1] * ei;
+          bc += rw[2 * k] * ei + rw[2 * k + 1] * er;
+          yr += rwy[2 * k] * er - rwy[2 * k + 1] * ei;
+          yc += rwy[2 * k] * ei + rwy[2 * k + 1] * er;
+          zr += rwz[2 * k] * er - rwz[2 * k + 1] * ei;
+          zc += rwz[2 * k] * ei + rwz[2 * k + 1] * er;
+        }
+        const int o = 2 * (i * n + v);
+        B[o] = br;
+        B[o + 1] = bc;
+        By[o] = yr;
+        By[o + 1] = yc;
+        Bz[o] = zr;
+        Bz[o + 1] = zc;
+      }
+    } else {
+      for (int v = lane; v < n; v += 32) {
+        double br = 0.0, bc = 0.0;
+        for (int k = 0; k < n; k++) {
+          const double er = __ldg(E + 2 * (k * n + v)), ei = __ldg(E + 2 * (k * n + v) + 1);
+          br += rw[2 * k] * er - rw[2 * k + 1] * ei;
+          bc += rw[2 * k] * ei + rw[2 * k + 1] * er;
+        }
+        B[2 * (i * n + v)] = br;
+        B[2 * (i * n + v) + 1] = bc;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// The PSF |psf|^2 at ROI pixel (rx, ry) from pupil_tables' B arrays
+// (pfitCalcPeakShape :164-169); with g non-null also Re(conj(psf) d) for the
+// x, y and z derivatives d (pfitCalcJH3D :103-106 without the 2 h rqe
+// factor; dz negated as pfnGetPSFdz :199-201).
+__device__ inline double pupil_pixel(const ModelCfg& cfg, const double* fw, int rx, int ry, double* g) {
+  const int n = cfg.sx;
+  const PupilLayout L = pupil_layout(n);
+  const double* B = fw;
+  const double* By = B + 2 * n * n;
+  const double* Bz = By + 2 * n * n;
+  const double* E = cfg.fft + L.e;
+  const double* KX = cfg.fft + L.kx;
+  double pr = 0.0, pc = 0.0;
+  if (!g) {
+    for (int i = 0; i < n; i++) {
+      const double er = __ldg(E + 2 * (i * n + rx)), ei = __ldg(E + 2 * (i * n + rx) + 1);
+      const int o = 2 * (i * n + ry);
+      pr += B[o] * er - B[o + 1] * ei;
+      pc += B[o] * ei + B[o + 1] * er;
+    }
+    return pr * pr + pc * pc;
+  }
+  double xr = 0.0, xc = 0.0, yr = 0.0, yc = 0.0, zr = 0.0, zc = 0.0;
+  for (int i = 0; i < n; i++) {
+    const double er = __ldg(E + 2 * (i * n + rx)), ei = __ldg(E + 2 * (i * n + rx) + 1);
+    const int o = 2 * (i * n + ry);
+    const double tr = B[o] * er - B[o + 1] * ei, tc = B[o] * ei + B[o + 1] * er;
+    pr += tr;
+    pc += tc;
+    // times -i kx[i] (pfnGetPSFdx :140-143)
+    const double kx = __ldg(KX + i);
+    xr += tc * kx;
+    xc -= tr * kx;
+    yr += By[o] * er - By[o + 1] * ei;
+    yc += By[o] * ei + By[o + 1] * er;
+    zr += Bz[o] * er - Bz[o + 1] * ei;
+    zc += Bz[o] * ei + Bz[o + 1] * er;
+  }
+  g[0] = pr * xr + pc * xc;
+  g[1] = pr * yr + pc * yc;
+  g[2] = pr * (-zr) + pc * (-zc);
+  return pr * pr + pc * pc;
+}
+
 // Peak shape at ROI pixel p for the tables currently in the workspace.
 template <typename T>
 __device__ __forceinline__ T psf_at(const ModelCfg& cfg, const T* aij, const WarpWS<T>& ws,
                                     const SplinePos& s, int rx, int ry) {
   if (is_fft(cfg.model)) return (T)fft_pixel(cfg, ws.fw, rx, ry, nullptr);
+  if (is_pupil(cfg.model)) return (T)pupil_pixel(cfg, ws.fw, rx, ry, nullptr);
   if (!is_spline(cfg.model)) {
     if constexpr (sizeof(T) == 4) return g32_psf(ws.tab0, ws.ts, rx, ry).h;
     else return mul_rn(ws.eyt[ry], ws.ext[rx]);
@@ -1233,6 +1449,13 @@ __device__ inline void apply_update(const ModelCfg& cfg, int model, PeakRec& w, 
       if (w.p[PZ] > max_z) w.p[PZ] = max_z;
       break;
     }
+    case M_PUPIL:
+      // pfitUpdate3D pupil_fit.c:529-546 with pfitZRangeCheck :555-570
+      w.p[PH] -= d[0]; w.p[PX] -= d[1]; w.p[PY] -= d[2]; w.p[PZ] -= d[3]; w.p[PBG] -= d[4];
+      anchor_update(w);
+      if (w.p[PZ] < cfg.zmin) w.p[PZ] = cfg.zmin;
+      if (w.p[PZ] > cfg.zmax) w.p[PZ] = cfg.zmax;
+      break;
     default: {  // M_SPLINE3D, with cfZRangeCheck
       w.p[PH] -= d[0]; w.p[PX] -= d[1]; w.p[PY] -= d[2]; w.p[PZ] -= d[3]; w.p[PBG] -= d[4];
       anchor_update(w);
@@ -1274,15 +1497,20 @@ __device__ __forceinline__ int check_for(const ModelCfg& cfg, int model, PeakRec
 }
 
 // Prepare the shape tables of peak w (all lanes) and return its spline
-// position (unused for Gaussians).
+// position (unused for Gaussians).  deriv false: only the shape will be
+// read (the pupil model then skips its derivative sums).
 template <typename T>
 __device__ inline SplinePos shape_tables(const ModelCfg& cfg, const PeakRec& w, WarpWS<T>& ws,
-                                         int lane) {
+                                         int lane, bool deriv = true) {
   SplinePos s;
   if (is_fft(cfg.model)) {
     s.xs = s.ys = s.zi = 0;
     s.xd = s.yd = s.zd = 0.0;
     fft_tables(cfg, w, ws, lane);
+  } else if (is_pupil(cfg.model)) {
+    s.xs = s.ys = s.zi = 0;
+    s.xd = s.yd = s.zd = 0.0;
+    pupil_tables(cfg, w, ws, lane, deriv);
   } else if (is_spline(cfg.model)) {
     s = spline_pos(w.p, w.xi, w.yi, w.zi);
     spline_tables(cfg, s, ws, lane);
@@ -1355,6 +1583,17 @@ __device__ __forceinline__ void jt_row(const ModelCfg& cfg, const T* aij, const 
       jt[1] = rq * h * (T)g[0];
       jt[2] = rq * h * (T)g[1];
       jt[3] = rq * h * (T)g[2];
+      jt[4] = rq;
+      break;
+    }
+    case M_PUPIL: {
+      // pfitCalcJH3D pupil_fit.c:103-107
+      double g[3];
+      pupil_pixel(cfg, ws.fw, rx, ry, g);
+      jt[0] = rq * psf;
+      jt[1] = rq * (T)2 * h * (T)g[0];
+      jt[2] = rq * (T)2 * h * (T)g[1];
+      jt[3] = rq * (T)2 * h * (T)g[2];
       jt[4] = rq;
       break;
     }

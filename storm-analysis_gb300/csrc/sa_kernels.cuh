@@ -345,7 +345,7 @@ __device__ bool lm_step(const ModelCfg& cfg, const FrameSet<T>& fs, long long fb
     }
     // -- trial evaluation: shape, add, error (multi_fit.c:1229-1256)
     const PeakRec& wl = *ws.w;
-    SplinePos s = shape_tables(cfg, wl, ws, lane);
+    SplinePos s = shape_tables(cfg, wl, ws, lane, false);
     bool is_delta = false;
     if constexpr (sizeof(T) == 4) {
       // FP32: evaluate the change of the error from the start of the step
@@ -819,7 +819,7 @@ __global__ void __launch_bounds__(1024) k_prepare(ModelCfg cfg, FrameSet<T> fs) 
     __syncthreads();
     // roll back run ranks > b: remove the current contribution, restore the snapshot
     const int lane = tid & 31, wid = tid >> 5;
-    const int nws = cta_ws_warps(cfg.model);
+    const int nws = cta_ws_warps(cfg);
     WarpWS<T> ws = warp_ws<T>(smem + (size_t)(wid < nws ? wid : 0) * warp_ws_bytes<T>(cfg, 0), cfg, 0);
     const long long fbase = (long long)f * fs.npix;
     for (int r = b + 1 + wid; wid < nws && r < nrun; r += nws) {
@@ -890,7 +890,7 @@ __global__ void __launch_bounds__(1024) k_post(ModelCfg cfg, FrameSet<T> fs) {
   const int base = fs.pk_off[f];
   const int nrun = c->nrun;
   const int lane = tid & 31, wid = tid >> 5;
-  const int nws = cta_ws_warps(cfg.model);
+  const int nws = cta_ws_warps(cfg);
   WarpWS<T> ws = warp_ws<T>(smem + (size_t)(wid < nws ? wid : 0) * warp_ws_bytes<T>(cfg, 0), cfg, 0);
   const long long fbase = (long long)f * fs.npix;
   // recenter (mFitRecenterPeaks multi_fit.c:1644-1690); order-free with

@@ -7,9 +7,24 @@
 
 namespace sa {
 
-constexpr int SWEEP_BLOCK = 128;    // 4 warps, one peak each
+constexpr int SWEEP_BLOCK = 128;    // 4 warps, one peak each (fewer where their workspaces do not fit)
 constexpr int CTA_BLOCK = 1024;     // per-frame kernels
-constexpr int AUX_BLOCK = 256;      // warp-per-peak auxiliary kernels
+constexpr int AUX_BLOCK = 256;      // warp-per-peak auxiliary kernels without a workspace
+
+// Threads of a warp-per-peak auxiliary CTA with a workspace per warp.
+static inline int aux_block(const ModelCfg& cfg) { return 32 * aux_warps(cfg); }
+
+// Shared bytes of the sweep CTA's ROI pixel table (after the workspaces).
+static inline size_t roi_table_bytes(int nroi) { return ((size_t)nroi * 2 + 15) & ~(size_t)15; }
+
+// Warps of a sweep CTA whose dynamic shared memory is smem (configure
+// chooses 4, 2 or 1 so that their workspaces fit).
+template <typename T>
+static inline int sweep_warps(const ModelCfg& cfg, size_t smem) {
+  const size_t ws = warp_ws_bytes<T>(cfg, cfg.nroi);
+  const size_t w = (smem - roi_table_bytes(cfg.nroi)) / ws;
+  return w >= 4 ? 4 : (w >= 2 ? 2 : 1);
+}
 
 // The sweep kernel of a configuration: the FP32 Gaussian models have one
 // instantiation each, everything else shares the generic step.
@@ -53,12 +68,16 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t ws = warp_ws_bytes<T>(cfg, cfg.nroi);
-  const size_t s_sweep = ws * (SWEEP_BLOCK / 32) + (((size_t)cfg.nroi * 2 + 15) & ~(size_t)15);
+  // four warps per sweep CTA, or two or one where their workspaces (large
+  // ROIs in the FP64 engine, the pupil model) do not fit
+  int wpc = SWEEP_BLOCK / 32;
+  while (wpc > 1 && ws * wpc + roi_table_bytes(cfg.nroi) > (size_t)max_smem) wpc /= 2;
+  const size_t s_sweep = ws * wpc + roi_table_bytes(cfg.nroi);
   const size_t ws0 = warp_ws_bytes<T>(cfg, 0);
   const size_t grid_bytes = (size_t)(cfg.gx * cfg.gy + 1) * sizeof(int);
-  const size_t s_cta_ws = ws0 * (size_t)cta_ws_warps(cfg.model);
+  const size_t s_cta_ws = ws0 * (size_t)cta_ws_warps(cfg);
   const size_t s_cta = s_cta_ws > grid_bytes ? s_cta_ws : grid_bytes;
-  const size_t s_aux = ws0 * (AUX_BLOCK / 32);
+  const size_t s_aux = ws0 * (size_t)aux_warps(cfg);
   if (s_sweep > (size_t)max_smem || s_cta > (size_t)max_smem || s_aux > (size_t)max_smem)
     return cudaErrorInvalidConfiguration;
   // The limit is a property of the kernel, shared by every handle of the
@@ -88,7 +107,7 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
     if (e != cudaSuccess) return e;
   }
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T>(cfg), SWEEP_BLOCK, s_sweep);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T>(cfg), 32 * wpc, s_sweep);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   *sweep_grid = nsm * per_sm;
@@ -107,7 +126,7 @@ cudaError_t Launch<T>::prepare(const ModelCfg& cfg, const FrameSet<T>& fs, size_
 template <typename T>
 cudaError_t Launch<T>::sweep(const ModelCfg& cfg, const FrameSet<T>& fs, int grid, size_t smem,
                              cudaStream_t s) {
-  sweep_kernel<T>(cfg)<<<grid, SWEEP_BLOCK, smem, s>>>(cfg, fs);
+  sweep_kernel<T>(cfg)<<<grid, 32 * sweep_warps<T>(cfg, smem), smem, s>>>(cfg, fs);
   return cudaGetLastError();
 }
 
@@ -119,7 +138,7 @@ cudaError_t Launch<T>::post(const ModelCfg& cfg, const FrameSet<T>& fs, size_t s
 
 template <typename T>
 cudaError_t Launch<T>::tail(const ModelCfg& cfg, const FrameSet<T>& fs, int tail_peaks, cudaStream_t s) {
-  const size_t smem = warp_ws_bytes<T>(cfg, cfg.nroi) + (((size_t)cfg.nroi * 2 + 15) & ~(size_t)15);
+  const size_t smem = warp_ws_bytes<T>(cfg, cfg.nroi) + roi_table_bytes(cfg.nroi);
   tail_kernel<T>(cfg)<<<fs.F, 32, smem, s>>>(cfg, fs, tail_peaks);
   return cudaGetLastError();
 }
@@ -155,8 +174,8 @@ cudaError_t Launch<T>::new_peaks(const ModelCfg& cfg, const FrameSet<T>& fs, con
                                  int ncol, int ptype, const int* slots, const int* frames, int n,
                                  int do_add, size_t warp_smem, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  const int g = grid_for((long long)n * 32, AUX_BLOCK);
-  k_newpeaks<T><<<g, AUX_BLOCK, warp_smem, s>>>(cfg, fs, rows, ncol, ptype, slots, frames, n, do_add);
+  const int g = grid_for((long long)n * 32, aux_block(cfg));
+  k_newpeaks<T><<<g, aux_block(cfg), warp_smem, s>>>(cfg, fs, rows, ncol, ptype, slots, frames, n, do_add);
   return cudaGetLastError();
 }
 
@@ -164,8 +183,8 @@ template <typename T>
 cudaError_t Launch<T>::new_peaks_finder(const ModelCfg& cfg, const FrameSet<T>& fs, const int* slots,
                                         const int* frame_first, const int* frame_n, int nframes,
                                         size_t warp_smem, cudaStream_t s) {
-  const int g = (nframes * 32 + AUX_BLOCK - 1) / AUX_BLOCK;
-  k_newpeaks_finder<T><<<g, AUX_BLOCK, warp_smem, s>>>(cfg, fs, slots, frame_first, frame_n, nframes);
+  const int g = (nframes * 32 + aux_block(cfg) - 1) / aux_block(cfg);
+  k_newpeaks_finder<T><<<g, aux_block(cfg), warp_smem, s>>>(cfg, fs, slots, frame_first, frame_n, nframes);
   return cudaGetLastError();
 }
 
@@ -183,8 +202,8 @@ cudaError_t Launch<T>::peak_props(const ModelCfg& cfg, const FrameSet<T>& fs, co
                                   const int* frames, int n, double* sum, double* fg, double* bg,
                                   double* jac, size_t warp_smem, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  const int g = grid_for((long long)n * 32, AUX_BLOCK);
-  k_peak_props<T><<<g, AUX_BLOCK, warp_smem, s>>>(cfg, fs, slots, frames, n, sum, fg, bg, jac);
+  const int g = grid_for((long long)n * 32, aux_block(cfg));
+  k_peak_props<T><<<g, aux_block(cfg), warp_smem, s>>>(cfg, fs, slots, frames, n, sum, fg, bg, jac);
   return cudaGetLastError();
 }
 
@@ -193,8 +212,8 @@ cudaError_t Launch<T>::set_status(const ModelCfg& cfg, const FrameSet<T>& fs, co
                                   const int* frames, const int* status, int n, size_t warp_smem,
                                   cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  const int g = grid_for((long long)n * 32, AUX_BLOCK);
-  k_set_status<T><<<g, AUX_BLOCK, warp_smem, s>>>(cfg, fs, slots, frames, status, n);
+  const int g = grid_for((long long)n * 32, aux_block(cfg));
+  k_set_status<T><<<g, aux_block(cfg), warp_smem, s>>>(cfg, fs, slots, frames, status, n);
   return cudaGetLastError();
 }
 

@@ -19,7 +19,7 @@ import numpy
 from . import loadclib
 from .dao_fit_c import MultiFitterException, formatPeaksArbitraryPSF, formatPeaksGaussianPSF
 
-MODEL_INIT = {"2dfixed", "2d", "3d", "Z", "spline2D", "spline3D", "fft"}
+MODEL_INIT = {"2dfixed", "2d", "3d", "Z", "spline2D", "spline3D", "fft", "pupil"}
 
 RESULT_PROPS = ("x", "y", "z", "height", "background", "xsigma", "ysigma", "error")
 
@@ -28,7 +28,7 @@ class BatchFitter(object):
     def __init__(self, model, shape, n_frames, roi_size=10, sigma_range=None, rqe=None,
                  scmos_cal=None, wx_params=None, wy_params=None, min_z=None, max_z=None,
                  spline=None, precision=32, peaks_capacity=None, tol=1.0e-6, dilation=None,
-                 stream=None, psf_fft=None):
+                 stream=None, psf_fft=None, pupil_fn=None):
         if model not in MODEL_INIT:
             raise MultiFitterException("unknown model '%s'" % model)
         self.clib = loadclib.load()
@@ -43,6 +43,7 @@ class BatchFitter(object):
         self.spline = spline
         lib = self.clib
         self.psf_fft = psf_fft
+        self.pupil_fn = pupil_fn
         if model.startswith("spline"):
             sp = spline.getCPointer()
             self.h = lib.cfInitialize(sp, self.rqe, self.scmos_cal, tol, nx, ny)
@@ -50,6 +51,12 @@ class BatchFitter(object):
             # psf_fft: a psf_fft_c.PSFFFT (or anything with getCPointer()); the
             # FFT PSF model runs in the FP64 engine
             self.h = lib.ftFitInitialize(psf_fft.getCPointer(), self.rqe, self.scmos_cal, tol, nx, ny)
+        elif model == "pupil":
+            # pupil_fn: a pupil_fn.PupilFunction (getCPointer(), getZMin(),
+            # getZMax()); the pupil model runs in the FP64 engine
+            self.h = lib.pfitInitialize(pupil_fn.getCPointer(), self.rqe, self.scmos_cal, tol, nx, ny)
+            if self.h:
+                lib.pfitSetZRange(self.h, pupil_fn.getZMin(), pupil_fn.getZMax())
         else:
             self.h = lib.daoInitialize(self.rqe, self.scmos_cal, tol, nx, ny, roi_size)
         if not self.h:
@@ -92,7 +99,7 @@ class BatchFitter(object):
             self._framed = True
 
     def format(self, peaks, peaks_type):
-        if self.model.startswith("spline") or self.model == "fft":
+        if self.model.startswith("spline") or self.model in ("fft", "pupil"):
             return formatPeaksArbitraryPSF(peaks, peaks_type)
         return formatPeaksGaussianPSF(peaks, peaks_type)
 
@@ -247,6 +254,8 @@ class BatchFitter(object):
                 self.clib.cfCleanup(self.h)
             elif self.model == "fft":
                 self.clib.ftFitCleanup(self.h)
+            elif self.model == "pupil":
+                self.clib.pfitCleanup(self.h)
             else:
                 self.clib.daoCleanup(self.h)
             self.h = None

@@ -114,6 +114,35 @@ def _declare(lib):
     lib.ftFitNewPeaks.restype = None
     lib.ftFitCleanup.argtypes = [hp]
     lib.ftFitCleanup.restype = None
+    # the pupil-function model (pupil_function.c / pupil_fit.c names)
+    lib.pfnInitialize.argtypes = [f64, f64, f64, ci]
+    lib.pfnInitialize.restype = vp
+    lib.pfnCleanup.argtypes = [vp]
+    lib.pfnCleanup.restype = None
+    lib.pfnSetPF.argtypes = [vp, f64, f64]
+    lib.pfnSetPF.restype = None
+    lib.pfnSetPNEN.argtypes = [vp, f64, f64, f64, f64, f64, f64]
+    lib.pfnSetPNEN.restype = None
+    lib.pfnTranslate.argtypes = [vp, cd, cd, cd]
+    lib.pfnTranslate.restype = None
+    lib.pfnTranslateZ.argtypes = [vp, cd]
+    lib.pfnTranslateZ.restype = None
+    for name in ["pfnGetPSF", "pfnGetPSFdx", "pfnGetPSFdy", "pfnGetPSFdz", "pfnGetPXEX", "pfnGetPXEY",
+                 "pfnGetPYEX", "pfnGetPYEY", "pfnGetPZEX", "pfnGetPZEY"]:
+        getattr(lib, name).argtypes = [vp, f64, f64]
+        getattr(lib, name).restype = None
+    lib.pfnGetPSFIntensity.argtypes = [vp, f64]
+    lib.pfnGetPSFIntensity.restype = None
+    lib.pfnGetSize.argtypes = [vp]
+    lib.pfnGetSize.restype = ci
+    lib.pfitInitialize.argtypes = [vp, f64, f64, cd, ci, ci]
+    lib.pfitInitialize.restype = hp
+    lib.pfitNewPeaks.argtypes = [hp, f64, cs, ci]
+    lib.pfitNewPeaks.restype = None
+    lib.pfitSetZRange.argtypes = [hp, cd, cd]
+    lib.pfitSetZRange.restype = None
+    lib.pfitCleanup.argtypes = [hp]
+    lib.pfitCleanup.restype = None
     for name in ["getXSize", "getYSize", "getZSize"]:
         getattr(lib, name).argtypes = [vp]
         getattr(lib, name).restype = ci
@@ -247,6 +276,10 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "pFTInitialize", "pFTCleanup", "pFTTranslate", "pFTGetPSF", "pFTGetPSFdx", "pFTGetPSFdy",
            "pFTGetPSFdz", "pFTGetXSize", "pFTGetYSize", "pFTGetZSize", "ftFitInitialize", "ftFitNewPeaks",
            "ftFitCleanup",
+           "pfnInitialize", "pfnCleanup", "pfnSetPF", "pfnSetPNEN", "pfnTranslate", "pfnTranslateZ",
+           "pfnGetPSF", "pfnGetPSFdx", "pfnGetPSFdy", "pfnGetPSFdz", "pfnGetPSFIntensity", "pfnGetPXEX",
+           "pfnGetPXEY", "pfnGetPYEX", "pfnGetPYEY", "pfnGetPZEX", "pfnGetPZEY", "pfnGetSize",
+           "pfitInitialize", "pfitNewPeaks", "pfitSetZRange", "pfitCleanup",
            "mFitAnscombeTransformImage", "mFitGetFitImage", "mFitGetNError",
            "mFitGetPeakPropertyDouble", "mFitGetPeakPropertyInt", "mFitGetResidual",
            "mFitGetUnconverged", "mFitIterateLM", "mFitNewBackground", "mFitNewImage",

@@ -402,3 +402,59 @@ def fft_workload(frames=4, nx=256, ny=256, n_emitters=300, seed=21, background=1
                                    z=0.5 * z, background=numpy.full(n_emitters, background), height=0.8 * h))
     pf.cleanup()
     return out
+
+
+def pupil_function_data(size=30, pixel_size=0.1, seed=5, astigmatism=1.3, coma=0.4, sim=True):
+    """A pupil-function file's contents (the dict a reference .pfn pickle
+    holds) for a size x size pupil at the given camera pixel size (um),
+    emission 0.6 um, oil immersion (1.5), NA 1.4, with astigmatic
+    (r^2 cos 2t) and comatic (r^3 sin t) phase and a 5 % amplitude ripple,
+    normalised to a peak PSF intensity of 1 at focus."""
+    from . import pupil_math
+    rng = numpy.random.default_rng(seed)
+    cls = pupil_math.GeometrySim if sim else pupil_math.Geometry
+    geo = cls(size, pixel_size, 0.6, 1.5, 1.4)
+    t = numpy.arctan2(geo.ky, geo.kx)
+    r = geo.r
+    phase = astigmatism * r * r * numpy.cos(2.0 * t) + coma * r * r * r * numpy.sin(t)
+    pf = geo.createFromPhase(1.0, phase) * (1.0 + 0.05 * rng.standard_normal((size, size)))
+    pf = geo.applyNARestriction(pf)
+    pf = pf / math.sqrt(numpy.max(pupil_math.intensity(pupil_math.toRealSpace(pf))))
+    return {"pf": pf.astype(numpy.complex128), "pixel_size": pixel_size, "geo_sim_pf": sim, "wavelength": 0.6,
+            "immersion_index": 1.5, "numerical_aperture": 1.4}
+
+
+def pupil_workload(frames=4, nx=256, ny=256, n_emitters=300, seed=23, background=10.0, size=30):
+    """Frames of emitters drawn with the pupil-function model itself (the
+    pupil function translated and transformed, pupil_function_c; Poisson
+    noise) and "hdf5" starting peaks: the truth perturbed by 0.3 px in
+    x / y, half its z, 80 % of its height.  z in microns within +-0.4."""
+    from . import pupil_fn
+    pf_data = pupil_function_data(size=size)
+    pfn = pupil_fn.PupilFunction(pf_data=pf_data, zmin=-500.0, zmax=500.0)
+    c = pfn.pupil_fn_c
+    off = 0.5 * size
+    rng = numpy.random.default_rng(seed)
+    out = dict(model="pupil", nx=nx, ny=ny, images=[], backgrounds=[], truth=[], guesses=[],
+               rqe=numpy.ones((ny, nx)), scmos_cal=numpy.zeros((ny, nx)),
+               fitter={"model": "pupil", "pf_data": pf_data, "zmin": -500.0, "zmax": 500.0})
+    for _ in range(frames):
+        img = numpy.full((ny, nx), background)
+        x = rng.uniform(size, nx - size, n_emitters)
+        y = rng.uniform(size, ny - size, n_emitters)
+        z = rng.uniform(-0.4, 0.4, n_emitters)
+        h = rng.uniform(3000.0, 20000.0, n_emitters)
+        for i in range(n_emitters):
+            px, py = x[i] - off, y[i] - off
+            xi, yi = int(math.floor(px)), int(math.floor(py))
+            c.translate(px - xi, py - yi, z[i])
+            p = c.getPSF()
+            # the pupil's first index is the image's x
+            img[yi:yi + size, xi:xi + size] += h[i] * (p.real * p.real + p.imag * p.imag).T
+        out["images"].append(rng.poisson(img).astype(numpy.float64))
+        out["backgrounds"].append(numpy.full((ny, nx), background))
+        out["truth"].append(dict(x=x, y=y, z=z, height=h))
+        out["guesses"].append(dict(x=x + rng.normal(0.0, 0.3, n_emitters), y=y + rng.normal(0.0, 0.3, n_emitters),
+                                   z=0.5 * z, background=numpy.full(n_emitters, background), height=0.8 * h))
+    pfn.cleanup()
+    return out
