@@ -80,6 +80,18 @@ def load():
     lib.oraSolve.restype = ctypes.c_int
     lib.oraFFTEval.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, f64, f64, f64, f64]
     lib.oraPupilEval.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double] + [f64] * 8
+    lib.oraSetMinHeight.argtypes = [vp, ctypes.c_double]
+    lib.oraMPCreate.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+    lib.oraMPCreate.restype = vp
+    lib.oraMPDestroy.argtypes = [vp]
+    lib.oraMPSetChannel.argtypes = [vp, ctypes.c_int, vp]
+    lib.oraMPSetTransforms.argtypes = [vp, f64, f64, f64, f64]
+    lib.oraMPSetWeights.argtypes = [vp, f64, f64, f64, f64, f64, ctypes.c_int]
+    lib.oraMPSetWeightsIndexing.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+    lib.oraMPNewPeaks.argtypes = [vp, f64, ctypes.c_int, ctypes.c_int]
+    lib.oraMPIterate.argtypes = [vp]
+    lib.oraMPGetUnconverged.argtypes = [vp]
+    lib.oraMPGetUnconverged.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -282,3 +294,67 @@ def fft_eval(fitter, dx, dy, dz):
     out = [numpy.zeros(ny * nx) for _ in range(4)]
     fitter.lib.oraFFTEval(fitter.h, dx, dy, dz, *out)
     return [o.reshape(ny, nx) for o in out]
+
+
+class OracleMPFitter(object):
+    """FP64 CPU multi-plane fitter (multi_plane/mp_fit.c with mp_fit_arb.c or
+    mp_fit_dao.c): channels is a list of OracleFitter (one per plane, same
+    image size, created with tol * n_channels as the reference's MPFit
+    does); transforms = (xt_0toN, yt_0toN, xt_Nto0, yt_Nto0), 3 coefficients
+    per channel; weights a dict of (z_size, n_channels) arrays "bg", "h",
+    "x", "y", "z" (None: equal weights, z_size 2, offset 0 and scale 0)."""
+
+    def __init__(self, channels, transforms, kind="arb", independent_heights=0, tol=1.0e-6, weights=None,
+                 z_offset=0.0, z_scale=0.0):
+        self.lib = load()
+        self.channels = channels
+        self.nc = len(channels)
+        self.kind = kind
+        self.h = self.lib.oraMPCreate(self.nc, int(independent_heights), 0 if kind == "arb" else 1,
+                                      tol * self.nc)
+        for c, ch in enumerate(channels):
+            self.lib.oraMPSetChannel(self.h, c, ch.h)
+        self.lib.oraMPSetTransforms(self.h, *[numpy.ascontiguousarray(t, dtype=numpy.float64) for t in transforms])
+        if weights is None:
+            w = numpy.ascontiguousarray(numpy.ones((2, self.nc)) / float(self.nc))
+            weights = {k: w for k in ("bg", "h", "x", "y", "z")}
+        ws = [numpy.ascontiguousarray(weights[k], dtype=numpy.float64) for k in ("bg", "h", "x", "y", "z")]
+        self.lib.oraMPSetWeights(self.h, *ws, ws[0].shape[0])
+        self.lib.oraMPSetWeightsIndexing(self.h, z_offset, z_scale)
+
+    def newImage(self, images):
+        for c, ch in enumerate(self.channels):
+            ch.newImage(images[c])
+
+    def newBackground(self, bgs):
+        for c, ch in enumerate(self.channels):
+            ch.newBackground(bgs[c])
+
+    def newPeaks(self, peaks, peaks_type):
+        rows = format_peaks(peaks, peaks_type, self.kind == "arb")
+        self.lib.oraMPNewPeaks(self.h, rows, PEAK_TYPES[peaks_type], rows.shape[0])
+
+    def iterate(self):
+        self.lib.oraMPIterate(self.h)
+
+    def getUnconverged(self):
+        return self.lib.oraMPGetUnconverged(self.h)
+
+    def doFit(self, max_iterations=200):
+        """MultiFitter.doFit (sa_library/dao_fit_c.py:332-356)."""
+        self.iterate()
+        i = 0
+        while (self.getUnconverged() > 0) and (i < max_iterations):
+            self.iterate()
+            i += 1
+        return i + 1
+
+    def getPeakProperty(self, name, channel=0):
+        return self.channels[channel].getPeakProperty(name)
+
+    def cleanup(self):
+        if self.h:
+            self.lib.oraMPDestroy(self.h)
+            self.h = None
+        for ch in self.channels:
+            ch.cleanup()

@@ -199,3 +199,113 @@ class RefFitter(object):
 
     def removeRunningPeaks(self):
         self.lib.mFitRemoveRunningPeaks(self.mfit)
+
+
+class _MPFitHead(ctypes.Structure):
+    """The leading fields of the reference's mpFit (multi_plane/mp_fit.h:12-44),
+    through the per-channel fitData pointers."""
+    _fields_ = ([(n, ctypes.c_int) for n in ["im_size_x", "im_size_y", "independent_heights", "n_channels",
+                                               "n_weights"]] +
+                [(n, ctypes.c_double) for n in ["tolerance", "w_z_offset", "w_z_scale", "zmin", "zmax"]] +
+                [(n, ctypes.POINTER(ctypes.c_double)) for n in ["xt_0toN", "yt_0toN", "xt_Nto0", "yt_Nto0", "w_bg",
+                                                                 "w_h", "w_x", "w_y", "w_z", "heights"]] +
+                [(n, ctypes.c_void_p) for n in ["jacobian", "w_jacobian", "hessian", "w_hessian"]] +
+                [("fit_data", ctypes.POINTER(ctypes.POINTER(_FitDataHead)))])
+
+
+def mp_available():
+    return os.path.exists(os.path.join(REF_DIR, "libmp_fit_dao.so"))
+
+
+class RefMPDaoFitter(object):
+    """The reference's 2D Gaussian multi-plane fitter (mp_fit.c + mp_fit_dao.c)
+    with the call sequence of multi_plane/mp_fit_dao_c.py MPFitDao2D:
+    mpInitialize(tol * n_channels), mpDaoInitialize2DChannel per channel,
+    mpSetTransforms, mpSetWeights (equal weights, z_size 2), mpDaoNewPeaks,
+    mpIterateLM."""
+
+    PROPS_D = ("x", "y", "height", "background", "xsigma", "ysigma", "error", "z")
+    PROPS_I = ("status", "iterations")
+
+    def __init__(self, shape, n_channels, rqe, variance, sigma_range, roi_size, transforms, tol=1.0e-6):
+        lib = ctypes.CDLL(os.path.join(REF_DIR, "libmp_fit_dao.so"))
+        _declare(lib, False)
+        f64 = ndpointer(dtype=numpy.float64, flags="C_CONTIGUOUS")
+        vp = ctypes.c_void_p
+        lib.mpInitialize.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        lib.mpInitialize.restype = ctypes.POINTER(_MPFitHead)
+        lib.mpDaoInitialize2DChannel.argtypes = [vp, f64, f64, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                                 ctypes.c_int]
+        lib.mpSetTransforms.argtypes = [vp, f64, f64, f64, f64]
+        lib.mpSetWeights.argtypes = [vp, f64, f64, f64, f64, f64, ctypes.c_int]
+        lib.mpSetWeightsIndexing.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        lib.mpDaoNewPeaks.argtypes = [vp, f64, ctypes.c_char_p, ctypes.c_int]
+        lib.mpIterateLM.argtypes = [vp]
+        lib.mpCleanup.argtypes = [vp]
+        self.lib = lib
+        self.nc = n_channels
+        ny, nx = shape
+        self.mp = lib.mpInitialize(tol * n_channels, n_channels, 1, nx, ny)
+        wmax = 1.0 / (2.0 * sigma_range[0] * sigma_range[0])
+        wmin = 1.0 / (2.0 * sigma_range[1] * sigma_range[1])
+        self._keep = []
+        for c in range(n_channels):
+            r = numpy.ascontiguousarray(rqe[c], dtype=numpy.float64)
+            v = numpy.ascontiguousarray(variance[c], dtype=numpy.float64)
+            self._keep += [r, v]
+            lib.mpDaoInitialize2DChannel(self.mp, r, v, wmin, wmax, roi_size, c)
+        lib.mpSetTransforms(self.mp, *[numpy.ascontiguousarray(t, dtype=numpy.float64) for t in transforms])
+        w = numpy.ascontiguousarray(numpy.ones((2, n_channels)) / float(n_channels))
+        lib.mpSetWeights(self.mp, w, w, w, w, w, 2)
+        lib.mpSetWeightsIndexing(self.mp, 0.0, 0.0)
+
+    def channel(self, c):
+        return self.mp.contents.fit_data[c]
+
+    def newImage(self, images):
+        for c in range(self.nc):
+            self.lib.mFitNewImage(self.channel(c), numpy.ascontiguousarray(images[c], dtype=numpy.float64))
+
+    def newBackground(self, bgs):
+        for c in range(self.nc):
+            self.lib.mFitNewBackground(self.channel(c), numpy.ascontiguousarray(bgs[c], dtype=numpy.float64))
+
+    def newPeaks(self, rows, ptype):
+        rows = numpy.ascontiguousarray(rows, dtype=numpy.float64)
+        self.lib.mpDaoNewPeaks(self.mp, rows, ptype.encode(), rows.shape[0])
+
+    def iterate(self):
+        self.lib.mpIterateLM(self.mp)
+
+    def getUnconverged(self):
+        return self.lib.mFitGetUnconverged(self.channel(0))
+
+    def doFit(self, max_iterations=200):
+        """MultiFitter.doFit (sa_library/dao_fit_c.py:332-356)."""
+        self.iterate()
+        i = 0
+        while (self.getUnconverged() > 0) and (i < max_iterations):
+            self.iterate()
+            i += 1
+        return i + 1
+
+    def getPeakProperty(self, name, channel=0):
+        ch = self.channel(channel)
+        n = ch.contents.nfit
+        if name in self.PROPS_I:
+            out = numpy.zeros(n, dtype=numpy.int32)
+            self.lib.mFitGetPeakPropertyInt(ch, out, name.encode())
+        else:
+            out = numpy.zeros(n, dtype=numpy.float64)
+            self.lib.mFitGetPeakPropertyDouble(ch, out, name.encode())
+        return out
+
+    def counters(self, channel=0):
+        h = self.channel(channel).contents
+        return numpy.array([h.n_dposv, h.n_iterations, h.n_lost, h.n_margin, h.n_neg_fi, h.n_neg_height,
+                            h.n_non_converged, h.n_non_decr], dtype=numpy.int64)
+
+    def cleanup(self):
+        if self.mp:
+            self.lib.mpCleanup(self.mp)
+            self.mp = None

@@ -1470,3 +1470,430 @@ void oraRemoveRunningPeaks(oraFit *fit)
   }
   fit->nfit = i;
 }
+
+/* mFitEstimatePeakHeight's lower bound (multi_fit.c:965 sets -1; the
+ * multi-plane channel initialisers set 1, mp_fit_arb.c / mp_fit_dao.c). */
+void oraSetMinHeight(oraFit *fit, double h) { fit->min_height = h; }
+
+/* ------------------------------------------------------------------ */
+/* multi-plane fitting: multi_plane/mp_fit.c (the coupled LM sweep),    */
+/* mp_fit_arb.c (arbitrary PSFs: spline, pupil, FFT) and mp_fit_dao.c   */
+/* (2D Gaussians).  A group is one peak per channel at the same index;  */
+/* its channels share status and lambda, their x / y are tied through   */
+/* the affine maps and their z (and, unless independent, height)        */
+/* through weighted averages of the per-channel LM steps.               */
+/* ------------------------------------------------------------------ */
+
+#define ORA_MP_MAXCH 8
+
+struct oraMP {
+  int nc, indep, kind;          /* kind: ORA_MP_ARB or ORA_MP_DAO */
+  double tol, w_z_offset, w_z_scale;
+  int n_weights;
+  double xt0N[3 * ORA_MP_MAXCH], yt0N[3 * ORA_MP_MAXCH], xtN0[3 * ORA_MP_MAXCH], ytN0[3 * ORA_MP_MAXCH];
+  double *w_bg, *w_h, *w_x, *w_y, *w_z;
+  double heights[ORA_MP_MAXCH];
+  double dl[ORA_MP_MAXCH][7];   /* the per-channel LM steps (w_jacobian after the solve) */
+  oraFit *ch[ORA_MP_MAXCH];
+};
+
+/* mpInitialize mp_fit.c:146-175 (channels are attached with oraMPSetChannel). */
+oraMP *oraMPCreate(int n_channels, int independent_heights, int kind, double tol)
+{
+  oraMP *mp;
+  if (n_channels < 1 || n_channels > ORA_MP_MAXCH) return NULL;
+  mp = (oraMP *)calloc(1, sizeof(oraMP));
+  mp->nc = n_channels;
+  mp->indep = independent_heights;
+  mp->kind = kind;
+  mp->tol = tol;
+  return mp;
+}
+
+void oraMPDestroy(oraMP *mp)
+{
+  if (!mp) return;
+  free(mp->w_bg); free(mp->w_h); free(mp->w_x); free(mp->w_y); free(mp->w_z);
+  free(mp);
+}
+
+/* The channel fitter (created with oraCreate; mpArbInitialize*Channel /
+ * mpDaoInitialize2DChannel set its minimum height to 1). */
+void oraMPSetChannel(oraMP *mp, int channel, oraFit *fit)
+{
+  mp->ch[channel] = fit;
+  fit->min_height = 1.0;
+}
+
+/* mpSetTransforms mp_fit.c:535-548. */
+void oraMPSetTransforms(oraMP *mp, const double *xt_0toN, const double *yt_0toN, const double *xt_Nto0,
+                        const double *yt_Nto0)
+{
+  int i;
+  for (i = 0; i < 3 * mp->nc; i++) {
+    mp->xt0N[i] = xt_0toN[i];
+    mp->yt0N[i] = yt_0toN[i];
+    mp->xtN0[i] = xt_Nto0[i];
+    mp->ytN0[i] = yt_Nto0[i];
+  }
+}
+
+/* mpSetWeights mp_fit.c:561-592 (z the slow index, channel the fast one;
+ * relative heights start at 1). */
+void oraMPSetWeights(oraMP *mp, const double *w_bg, const double *w_h, const double *w_x, const double *w_y,
+                     const double *w_z, int z_size)
+{
+  int i, n = mp->nc * z_size;
+  double **dst[5] = {&mp->w_bg, &mp->w_h, &mp->w_x, &mp->w_y, &mp->w_z};
+  const double *src[5] = {w_bg, w_h, w_x, w_y, w_z};
+  mp->n_weights = z_size;
+  for (i = 0; i < 5; i++) {
+    free(*dst[i]);
+    *dst[i] = (double *)malloc(sizeof(double) * n);
+    memcpy(*dst[i], src[i], sizeof(double) * n);
+  }
+  for (i = 0; i < mp->nc; i++) mp->heights[i] = 1.0;
+}
+
+/* mpSetWeightsIndexing mp_fit.c:600-604. */
+void oraMPSetWeightsIndexing(oraMP *mp, double z_offset, double z_scale)
+{
+  mp->w_z_offset = z_offset;
+  mp->w_z_scale = z_scale;
+}
+
+/* mpWeightIndex mp_fit.c:703-725 (from channel 0's working z). */
+static void mp_weight_index(const oraMP *mp, double *dz, int *zi)
+{
+  double t = mp->w_z_scale * (mp->ch[0]->w.p[PZ] - mp->w_z_offset);
+  *zi = (int)t;
+  *dz = t - (double)*zi;
+  if (*zi < 0) *zi = 0;
+  if (*zi > (mp->n_weights - 2)) *zi = mp->n_weights - 2;
+}
+
+/* mpWeightInterpolate mp_fit.c:732-741. */
+static double mp_weight(const double *w, double dz, int zi, int nc, int c)
+{
+  double w1 = w[nc * zi + c], w2 = w[nc * (zi + 1) + c];
+  return w1 + (w2 - w1) * dz;
+}
+
+/* The z range checks the multi-plane update calls (fn_zrange):
+ * ftFitZRangeCheck fft_fit.c:506-524, pfitZRangeCheck pupil_fit.c:555-570,
+ * cfZRangeCheck cubic_fit.c:987-1005 (which also sets zi). */
+static void mp_z_range(const oraFit *fit, OPeak *pk)
+{
+  if (fit->model == ORA_FFT) {
+    double max_z = ((double)fit->sz) * 0.5 - 1.0e-12;
+    if (pk->p[PZ] < -max_z) pk->p[PZ] = -max_z;
+    if (pk->p[PZ] > max_z) pk->p[PZ] = max_z;
+  } else if (fit->model == ORA_PUPIL) {
+    if (pk->p[PZ] < fit->zmin) pk->p[PZ] = fit->zmin;
+    if (pk->p[PZ] > fit->zmax) pk->p[PZ] = fit->zmax;
+  } else if (fit->model == ORA_SPLINE3D) {
+    double zmax = ((double)fit->sz) - 1.0e-12;
+    if (pk->p[PZ] < 1.0e-12) pk->p[PZ] = 1.0e-12;
+    if (pk->p[PZ] > zmax) pk->p[PZ] = zmax;
+    pk->zi = (int)(pk->p[PZ]);
+  }
+}
+
+/* mpUpdate mp_fit.c:626-696: x and y from the channels' steps mapped back
+ * to channel 0 and averaged with the weights times the relative heights,
+ * mapped out to the other channels; anchors; backgrounds per channel. */
+static void mp_update_xy(oraMP *mp)
+{
+  int i, zi, nc = mp->nc;
+  double dz, p_ave, p_total, w, delta, t;
+  OPeak *w0 = &mp->ch[0]->w;
+  double xoff = mp->ch[0]->xoff, yoff = mp->ch[0]->yoff;
+  mp_weight_index(mp, &dz, &zi);
+  p_ave = 0.0;
+  p_total = 0.0;
+  for (i = 0; i < nc; i++) {
+    w = mp_weight(mp->w_x, dz, zi, nc, i);
+    delta = mp->xtN0[i * 3 + 1] * mp->dl[i][1];
+    delta += mp->xtN0[i * 3 + 2] * mp->dl[i][2];
+    p_ave += delta * w * mp->heights[i];
+    p_total += w * mp->heights[i];
+  }
+  w0->p[PX] -= p_ave / p_total;
+  p_ave = 0.0;
+  p_total = 0.0;
+  for (i = 0; i < nc; i++) {
+    w = mp_weight(mp->w_y, dz, zi, nc, i);
+    delta = mp->ytN0[i * 3 + 1] * mp->dl[i][1];
+    delta += mp->ytN0[i * 3 + 2] * mp->dl[i][2];
+    p_ave += delta * w * mp->heights[i];
+    p_total += w * mp->heights[i];
+  }
+  w0->p[PY] -= p_ave / p_total;
+  for (i = 1; i < nc; i++) {
+    OPeak *pk = &mp->ch[i]->w;
+    t = mp->xt0N[i * 3];
+    t += mp->xt0N[i * 3 + 1] * (w0->p[PX] + xoff);
+    t += mp->xt0N[i * 3 + 2] * (w0->p[PY] + yoff);
+    pk->p[PX] = t - xoff;
+    t = mp->yt0N[i * 3];
+    t += mp->yt0N[i * 3 + 1] * (w0->p[PX] + xoff);
+    t += mp->yt0N[i * 3 + 2] * (w0->p[PY] + yoff);
+    pk->p[PY] = t - yoff;
+  }
+  for (i = 0; i < nc; i++) anchor_update(&mp->ch[i]->w);
+  for (i = 0; i < nc; i++) mp->ch[i]->w.p[PBG] -= mp->dl[i][4];
+}
+
+/* mpArbUpdateZ mp_fit_arb.c:351-384. */
+static void mp_arb_update_z(oraMP *mp)
+{
+  int i, zi, nc = mp->nc;
+  double dz, p_ave = 0.0, p_total = 0.0, w, delta;
+  mp_weight_index(mp, &dz, &zi);
+  for (i = 0; i < nc; i++) {
+    w = mp_weight(mp->w_z, dz, zi, nc, i);
+    p_ave += mp->dl[i][3] * w * mp->heights[i];
+    p_total += w * mp->heights[i];
+  }
+  delta = p_ave / p_total;
+  for (i = 0; i < nc; i++) {
+    mp->ch[i]->w.p[PZ] -= delta;
+    mp_z_range(mp->ch[i], &mp->ch[i]->w);
+  }
+}
+
+/* fn_update: mpArbUpdateFixed mp_fit_arb.c:400-432, mpArbUpdateIndependent
+ * :449-470, mpDaoUpdate mp_fit_dao.c:164-209 (the 2D Gaussian's x width
+ * only -- its y width keeps its value -- and daoCheck2D's clamp, whose
+ * result is not used). */
+static void mp_update(oraMP *mp)
+{
+  int i, zi, nc = mp->nc;
+  double dz, p_ave, p_total, w;
+  if (mp->kind == ORA_MP_DAO) {
+    for (i = 0; i < nc; i++) {
+      OPeak *pk = &mp->ch[i]->w;
+      pk->p[PH] -= mp->dl[i][0];
+      if (pk->p[PH] < 0.01) pk->p[PH] = 0.01;
+      mp->heights[i] = pk->p[PH];
+    }
+    for (i = 0; i < nc; i++) {
+      mp->ch[i]->w.p[PXW] -= mp->dl[i][3];
+      model_check(mp->ch[i], &mp->ch[i]->w);
+    }
+    mp_update_xy(mp);
+    return;
+  }
+  if (mp->indep) {
+    for (i = 0; i < nc; i++) {
+      OPeak *pk = &mp->ch[i]->w;
+      pk->p[PH] -= mp->dl[i][0];
+      if (pk->p[PH] < 0.01) pk->p[PH] = 0.01;
+      mp->heights[i] = pk->p[PH];
+    }
+  } else {
+    mp_weight_index(mp, &dz, &zi);
+    p_ave = 0.0;
+    p_total = 0.0;
+    for (i = 0; i < nc; i++) {
+      w = mp_weight(mp->w_h, dz, zi, nc, i);
+      p_ave += mp->dl[i][0] * w;
+      p_total += w;
+    }
+    mp->ch[0]->w.p[PH] -= p_ave / p_total;
+    for (i = 1; i < nc; i++) mp->ch[i]->w.p[PH] = mp->ch[0]->w.p[PH];
+  }
+  mp_update_xy(mp);
+  mp_arb_update_z(mp);
+}
+
+static int mp_check(oraMP *mp, oraFit *fit, OPeak *pk)
+{
+  (void)mp;
+  return (fit->model == ORA_2D) ? model_check(fit, pk) : base_check(fit, pk);
+}
+
+/* mpResetWorkingPeaks mp_fit.c:500-521. */
+static void mp_reset(oraMP *mp, int i)
+{
+  int c;
+  for (c = 0; c < mp->nc; c++) {
+    reset_working(mp->ch[c], i);
+    mp->ch[c]->w.status = ERROR;
+  }
+}
+
+/* mpCheckError mp_fit.c:43-68. */
+static void mp_check_error(oraMP *mp, int i)
+{
+  int c, bad = 0;
+  for (c = 0; c < mp->nc; c++) {
+    if (mp->ch[c]->pk[i].status == ERROR) {
+      bad = 1;
+      break;
+    }
+  }
+  if (!bad) return;
+  for (c = 0; c < mp->nc; c++) {
+    oraFit *fit = mp->ch[c];
+    if (fit->pk[i].status != ERROR) {
+      peak_copy(fit, &fit->w, &fit->pk[i]);
+      add_peak(fit, &fit->w, -1);
+      peak_copy(fit, &fit->pk[i], &fit->w);
+    }
+    fit->pk[i].status = ERROR;
+  }
+}
+
+/* mpIterateLM mp_fit.c:183-478. */
+void oraMPIterate(oraMP *mp)
+{
+  int i, c, k, l, nc = mp->nc, nfit = mp->ch[0]->nfit;
+  double jac[ORA_MP_MAXCH][7], hes[ORA_MP_MAXCH][49], whes[49], e0, e1;
+  for (i = 0; i < nfit; i++) {
+    int bad;
+    if (mp->ch[0]->pk[i].status != RUNNING) continue;
+    e0 = 0.0;
+    for (c = 0; c < nc; c++) {
+      oraFit *fit = mp->ch[c];
+      peak_copy(fit, &fit->w, &fit->pk[i]);
+      calc_err(fit, &fit->w);          /* return value ignored, mp_fit.c:220 */
+      e0 += fit->w.error;
+      calc_jh(fit, &fit->w, jac[c], hes[c]);
+      add_peak(fit, &fit->w, -1);
+    }
+    for (;;) {
+      bad = 0;
+      if (mp->ch[0]->w.lambda > LAMBDA_MAX) {
+        for (c = 0; c < nc; c++) {
+          mp->ch[c]->ctr[C_LOST]++;
+          mp->ch[c]->w.status = ERROR;
+        }
+        break;
+      }
+      for (c = 0; c < nc; c++) mp->ch[c]->w.status = RUNNING;
+      for (c = 0; c < nc; c++) {
+        oraFit *fit = mp->ch[c];
+        int n = fit->jac;
+        fit->w.iterations++;
+        fit->ctr[C_ITER]++;
+        for (k = 0; k < n; k++) {
+          mp->dl[c][k] = jac[c][k];
+          for (l = 0; l < n; l++)
+            whes[k * n + l] = (k == l) ? (1.0 + fit->w.lambda) * hes[c][k * n + l] : hes[c][k * n + l];
+        }
+        if (oraSolve(whes, mp->dl[c], n) != 0) {
+          bad = 1;
+          fit->ctr[C_DPOSV]++;
+          break;
+        }
+      }
+      if (bad) {
+        for (c = 0; c < nc; c++) {
+          mp->ch[c]->w.status = ERROR;
+          mp->ch[c]->w.lambda = mp->ch[c]->w.lambda * LAMBDA_UP;
+        }
+        continue;
+      }
+      mp_update(mp);
+      for (c = 0; c < nc; c++)
+        if (mp_check(mp, mp->ch[c], &mp->ch[c]->w)) bad = 1;
+      if (bad) {
+        mp_reset(mp, i);
+        continue;
+      }
+      for (c = 0; c < nc; c++) {
+        peak_shape(mp->ch[c], &mp->ch[c]->w);
+        add_peak(mp->ch[c], &mp->ch[c]->w, +1);
+      }
+      e1 = 0.0;
+      for (c = 0; c < nc; c++) {
+        if (calc_err(mp->ch[c], &mp->ch[c]->w)) bad = 1;
+        else e1 += mp->ch[c]->w.error;
+      }
+      if (bad) {
+        for (c = 0; c < nc; c++) add_peak(mp->ch[c], &mp->ch[c]->w, -1);
+        mp_reset(mp, i);
+        continue;
+      }
+      if (e1 > e0) {
+        if (((e1 - e0) / e0) < mp->tol) {
+          for (c = 0; c < nc; c++) mp->ch[c]->w.status = CONVERGED;
+          break;
+        }
+        for (c = 0; c < nc; c++) {
+          mp->ch[c]->ctr[C_NONDECR]++;
+          add_peak(mp->ch[c], &mp->ch[c]->w, -1);
+        }
+        mp_reset(mp, i);
+        continue;
+      }
+      if (((e0 - e1) / e0) < mp->tol) {
+        for (c = 0; c < nc; c++) mp->ch[c]->w.status = CONVERGED;
+      } else if (mp->ch[0]->w.lambda > LAMBDA_MIN) {
+        for (c = 0; c < nc; c++) mp->ch[c]->w.lambda = mp->ch[c]->w.lambda * LAMBDA_DOWN;
+      }
+      break;
+    }
+    /* mpCopyFromWorking mp_fit.c:124-134 (channel 0's status for all) */
+    for (c = 0; c < nc; c++) {
+      mp->ch[c]->w.status = mp->ch[0]->w.status;
+      peak_copy(mp->ch[c], &mp->ch[c]->pk[i], &mp->ch[c]->w);
+    }
+  }
+  for (c = 0; c < nc; c++) recenter(mp->ch[c]);
+  for (i = 0; i < nfit; i++) mp_check_error(mp, i);
+}
+
+/* mpArbNewPeaks mp_fit_arb.c:180-340 and mpDaoNewPeaks mp_fit_dao.c:82-152:
+ * channel 0 takes the peaks as given, the others their positions mapped
+ * through xt_0toN / yt_0toN; with fixed heights the "finder" / "testing"
+ * peaks of a group then take the channels' mean height; groups with an
+ * ERROR peak in any channel are made ERROR in all. */
+void oraMPNewPeaks(oraMP *mp, const double *peaks, int ptype, int n_peaks)
+{
+  int i, j, c, nc = mp->nc, start = mp->ch[0]->nfit, stop = start + n_peaks;
+  int arb = (mp->kind == ORA_MP_ARB);
+  int ncol = (ptype == ORA_PEAKS_TEXT) ? (arb ? 5 : 7) : (arb ? 3 : 4);
+  double *mapped = (double *)malloc(sizeof(double) * ncol * (n_peaks > 0 ? n_peaks : 1));
+  for (c = 0; c < nc; c++) {
+    if (c == 0) {
+      oraNewPeaks(mp->ch[0], peaks, ptype, n_peaks);
+      continue;
+    }
+    for (j = 0; j < n_peaks; j++) {
+      const double *q = peaks + (size_t)ncol * j;
+      double *o = mapped + (size_t)ncol * j, tx = q[0], ty = q[1];
+      memcpy(o, q, sizeof(double) * ncol);
+      o[0] = mp->xt0N[c * 3] + tx * mp->xt0N[c * 3 + 1] + ty * mp->xt0N[c * 3 + 2];
+      o[1] = mp->yt0N[c * 3] + tx * mp->yt0N[c * 3 + 1] + ty * mp->yt0N[c * 3 + 2];
+    }
+    oraNewPeaks(mp->ch[c], mapped, ptype, n_peaks);
+  }
+  free(mapped);
+  if (arb && !mp->indep && (ptype != ORA_PEAKS_TEXT)) {
+    for (i = start; i < stop; i++) {
+      double height = 0.0;
+      for (c = 0; c < nc; c++) {
+        oraFit *fit = mp->ch[c];
+        peak_copy(fit, &fit->w, &fit->pk[i]);
+        height += fit->w.p[PH];
+      }
+      height = height / ((double)nc);
+      for (c = 0; c < nc; c++)
+        if (mp->ch[c]->w.status != ERROR) add_peak(mp->ch[c], &mp->ch[c]->w, -1);
+      for (c = 0; c < nc; c++) {
+        oraFit *fit = mp->ch[c];
+        fit->w.p[PH] = height;
+        if (fit->w.status != ERROR) {
+          add_peak(fit, &fit->w, +1);
+          calc_err(fit, &fit->w);
+        }
+        peak_copy(fit, &fit->pk[i], &fit->w);
+      }
+    }
+  }
+  for (i = start; i < stop; i++) mp_check_error(mp, i);
+}
+
+int oraMPGetUnconverged(oraMP *mp) { return oraGetUnconverged(mp->ch[0]); }

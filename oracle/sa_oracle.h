@@ -108,6 +108,26 @@ double oraSplineEval3D(const double *aij, int sx, int sy, int sz,
 void oraPupilEval(const oraFit *fit, double dx, double dy, double dz, double *pr, double *pc, double *xr,
                   double *xc, double *yr, double *yc, double *zr, double *zc);
 
+/* Multi-plane fitting (multi_plane/mp_fit.c, mp_fit_arb.c, mp_fit_dao.c):
+ * channel fitters made with oraCreate (one per image plane, same size),
+ * coupled by oraMPIterate.  kind: arbitrary PSFs (spline, pupil, FFT) or
+ * 2D Gaussians. */
+#define ORA_MP_ARB 0
+#define ORA_MP_DAO 1
+typedef struct oraMP oraMP;
+oraMP *oraMPCreate(int n_channels, int independent_heights, int kind, double tol);
+void oraMPDestroy(oraMP *mp);
+void oraMPSetChannel(oraMP *mp, int channel, oraFit *fit);
+void oraMPSetTransforms(oraMP *mp, const double *xt_0toN, const double *yt_0toN, const double *xt_Nto0,
+                        const double *yt_Nto0);
+void oraMPSetWeights(oraMP *mp, const double *w_bg, const double *w_h, const double *w_x, const double *w_y,
+                     const double *w_z, int z_size);
+void oraMPSetWeightsIndexing(oraMP *mp, double z_offset, double z_scale);
+void oraMPNewPeaks(oraMP *mp, const double *peaks, int peak_type, int n_peaks);
+void oraMPIterate(oraMP *mp);
+int oraMPGetUnconverged(oraMP *mp);
+void oraSetMinHeight(oraFit *fit, double h);
+
 /* FP64 Cholesky solve of a k x k system given as a row-major upper triangle
  * (the layout dposv("Lower") reads, multi_fit.c:1851).  Returns 0 on success. */
 int oraSolve(double *hessian, double *rhs, int k);

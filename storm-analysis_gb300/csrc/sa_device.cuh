@@ -587,8 +587,14 @@ __host__ __device__ __forceinline__ bool is_pupil(int model) { return model == M
 //   KZS [m+1][m+1]       2 pi kz at (m - min(a, b), m - max(a, b)): the z
 //                        shift multiplier of pixel offset (a, b) from the
 //                        centre, pfnTranslate's pie slice :475-486
+//   RNG [N][2]           per pupil row, the first and last column where the
+//                        pupil function is not zero (first > last: none)
+//   BAND [2]             the first and last row that is not all zero
+// A pupil function is zero outside the objective's NA (a disk of a few
+// pixels' radius in a pupil of tens), so the sums run over its support
+// only; the terms left out are exact zeros.
 struct PupilLayout {
-  int e, pf, kx, ky, kz, kzs, total;
+  int e, pf, kx, ky, kz, kzs, rng, band, total;
 };
 __host__ __device__ __forceinline__ PupilLayout pupil_layout(int n) {
   PupilLayout L;
@@ -599,7 +605,9 @@ __host__ __device__ __forceinline__ PupilLayout pupil_layout(int n) {
   L.ky = L.kx + n;
   L.kz = L.ky + n * n;
   L.kzs = L.kz + n * n;
-  L.total = L.kzs + m1 * m1;
+  L.rng = L.kzs + m1 * m1;
+  L.band = L.rng + 2 * n;
+  L.total = L.band + 2;
   return L;
 }
 // Doubles of a warp's pupil scratch: B, By, Bz [N][N] (complex; the sums
@@ -1266,10 +1274,12 @@ __device__ inline void pupil_tables(const ModelCfg& cfg, const PeakRec& w, WarpW
     }
   }
   __syncwarp();
-  for (int i = 0; i < n; i++) {
+  const int i_lo = (int)__ldg(cfg.fft + L.band), i_hi = (int)__ldg(cfg.fft + L.band + 1);
+  for (int i = i_lo; i <= i_hi; i++) {
     const double xr = sxv[2 * i], xc = sxv[2 * i + 1];
     const int oa = abs(i - m) * m1;
-    for (int k = lane; k < n; k += 32) {
+    const int k_lo = (int)__ldg(cfg.fft + L.rng + 2 * i), k_hi = (int)__ldg(cfg.fft + L.rng + 2 * i + 1);
+    for (int k = k_lo + lane; k <= k_hi; k += 32) {
       const int o = oa + abs(k - m);
       // the reference's products in its order, :488-505
       const double r2 = xr * syv[2 * k] - xc * syv[2 * k + 1];
@@ -1293,7 +1303,7 @@ __device__ inline void pupil_tables(const ModelCfg& cfg, const PeakRec& w, WarpW
     if (deriv) {
       for (int v = lane; v < n; v += 32) {
         double br = 0.0, bc = 0.0, yr = 0.0, yc = 0.0, zr = 0.0, zc = 0.0;
-        for (int k = 0; k < n; k++) {
+        for (int k = k_lo; k <= k_hi; k++) {
           const double er = __ldg(E + 2 * (k * n + v)), ei = __ldg(E + 2 * (k * n + v) + 1);
           br += rw[2 * k] * er - rw[2 * k + 1] * ei;
           bc += rw[2 * k] * ei + rw[2 * k + 1] * er;
@@ -1313,7 +1323,7 @@ __device__ inline void pupil_tables(const ModelCfg& cfg, const PeakRec& w, WarpW
     } else {
       for (int v = lane; v < n; v += 32) {
         double br = 0.0, bc = 0.0;
-        for (int k = 0; k < n; k++) {
+        for (int k = k_lo; k <= k_hi; k++) {
           const double er = __ldg(E + 2 * (k * n + v)), ei = __ldg(E + 2 * (k * n + v) + 1);
           br += rw[2 * k] * er - rw[2 * k + 1] * ei;
           bc += rw[2 * k] * ei + rw[2 * k + 1] * er;
@@ -1338,9 +1348,10 @@ __device__ inline double pupil_pixel(const ModelCfg& cfg, const double* fw, int 
   const double* Bz = By + 2 * n * n;
   const double* E = cfg.fft + L.e;
   const double* KX = cfg.fft + L.kx;
+  const int i_lo = (int)__ldg(cfg.fft + L.band), i_hi = (int)__ldg(cfg.fft + L.band + 1);
   double pr = 0.0, pc = 0.0;
   if (!g) {
-    for (int i = 0; i < n; i++) {
+    for (int i = i_lo; i <= i_hi; i++) {
       const double er = __ldg(E + 2 * (i * n + rx)), ei = __ldg(E + 2 * (i * n + rx) + 1);
       const int o = 2 * (i * n + ry);
       pr += B[o] * er - B[o + 1] * ei;
@@ -1349,7 +1360,7 @@ __device__ inline double pupil_pixel(const ModelCfg& cfg, const double* fw, int 
     return pr * pr + pc * pc;
   }
   double xr = 0.0, xc = 0.0, yr = 0.0, yc = 0.0, zr = 0.0, zc = 0.0;
-  for (int i = 0; i < n; i++) {
+  for (int i = i_lo; i <= i_hi; i++) {
     const double er = __ldg(E + 2 * (i * n + rx)), ei = __ldg(E + 2 * (i * n + rx) + 1);
     const int o = 2 * (i * n + ry);
     const double tr = B[o] * er - B[o + 1] * ei, tc = B[o] * ei + B[o + 1] * er;

@@ -174,6 +174,33 @@ void pupil_tables(const PupilH& p, std::vector<double>& out) {
       const int lo = a < b ? a : b, hi = a < b ? b : a;
       out[L.kzs + a * m1 + b] = p.kz[(size_t)(m - lo) * n + (m - hi)];
     }
+  // the pupil function's support: rows and per-row columns with a non-zero value
+  int i_lo = n, i_hi = -1;
+  for (int i = 0; i < n; i++) {
+    int k_lo = n, k_hi = -1;
+    for (int k = 0; k < n; k++) {
+      const size_t l = (size_t)i * n + k;
+      if (p.pf[2 * l] != 0.0 || p.pf[2 * l + 1] != 0.0) {
+        if (k < k_lo) k_lo = k;
+        k_hi = k;
+      }
+    }
+    if (k_hi < 0) {
+      k_lo = 1;
+      k_hi = 0;
+    } else {
+      if (i < i_lo) i_lo = i;
+      i_hi = i;
+    }
+    out[L.rng + 2 * i] = (double)k_lo;
+    out[L.rng + 2 * i + 1] = (double)k_hi;
+  }
+  if (i_hi < 0) {
+    i_lo = 1;
+    i_hi = 0;
+  }
+  out[L.band] = (double)i_lo;
+  out[L.band + 1] = (double)i_hi;
 }
 
 }  // namespace sa
