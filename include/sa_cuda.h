@@ -222,6 +222,72 @@ void pfitSetZRange(saFitData *fit, double min_z, double max_z);
 /* pupil_fit.c:180 pfitCleanup (the pupil data stays the caller's) */
 void pfitCleanup(saFitData *fit);
 
+/* ---- multi-plane fitting (multi_plane/mp_fit.c, mp_fit_arb.c, mp_fit_dao.c;
+ * bound by multi_plane/mp_fit_c.py, mp_fit_arb_c.py, mp_fit_dao_c.py) -------
+ * The leading fields are the reference's mpFit (mp_fit.h:12-44): its Python
+ * reads n_channels and passes fit_data[i] -- one handle of this library per
+ * image plane -- to the mFit* calls.  The channels run in the FP64 engine;
+ * the coupled sweep runs on the device.  At most 8 channels. */
+typedef struct saMPFit {
+  int im_size_x;
+  int im_size_y;
+  int independent_heights;
+  int n_channels;
+  int n_weights;
+  double tolerance;
+  double w_z_offset;
+  double w_z_scale;
+  double zmin;
+  double zmax;
+  double *xt_0toN;
+  double *yt_0toN;
+  double *xt_Nto0;
+  double *yt_Nto0;
+  double *w_bg;
+  double *w_h;
+  double *w_x;
+  double *w_y;
+  double *w_z;
+  double *heights;
+  void *jacobian;
+  void *w_jacobian;
+  void *hessian;
+  void *w_hessian;
+  saFitData **fit_data;
+  void *fn_cleanup;
+  void *fn_newpeaks;
+  void *fn_peak_xi_yi;
+  void *fn_update;
+  void *fn_zrange;
+  void *engine;  /* private */
+} saMPFit;
+
+/* mp_fit.c:146 mpInitialize */
+saMPFit *mpInitialize(double tolerance, int n_channels, int independent_heights, int im_size_x, int im_size_y);
+/* mp_fit.c:76 mpCleanup (also the channels' fitters) */
+void mpCleanup(saMPFit *mp_fit);
+/* mp_fit.c:183 mpIterateLM */
+void mpIterateLM(saMPFit *mp_fit);
+/* mp_fit.c:535 mpSetTransforms (3 coefficients per channel: offset, x, y) */
+void mpSetTransforms(saMPFit *mp_fit, double *xt_0toN, double *yt_0toN, double *xt_Nto0, double *yt_Nto0);
+/* mp_fit.c:561 mpSetWeights ([z_size][n_channels] each) */
+void mpSetWeights(saMPFit *mp_fit, double *w_bg, double *w_h, double *w_x, double *w_y, double *w_z, int z_size);
+/* mp_fit.c:600 mpSetWeightsIndexing */
+void mpSetWeightsIndexing(saMPFit *mp_fit, double z_offset, double z_scale);
+/* mp_fit_arb.c:36 mpArbInitializePSFFFTChannel, :85 mpArbInitializePupilFnChannel,
+ * :135 mpArbInitializeSplineChannel (a 3D spline) */
+void mpArbInitializePSFFFTChannel(saMPFit *mp_fit, void *psf_fft, double *rqe, double *variance, int channel);
+void mpArbInitializePupilFnChannel(saMPFit *mp_fit, void *pupil_data, double *rqe, double *variance, double zmin,
+                                   double zmax, int channel);
+void mpArbInitializeSplineChannel(saMPFit *mp_fit, void *spline, double *rqe, double *variance, int channel);
+/* mp_fit_arb.c:180 mpArbNewPeaks (n_peaks per channel, channel 0's coordinates) */
+void mpArbNewPeaks(saMPFit *mp_fit, double *peak_params, char *p_type, int n_peaks);
+/* mp_fit_dao.c:28 mpDaoInitialize2DChannel */
+void mpDaoInitialize2DChannel(saMPFit *mp_fit, double *rqe, double *variance, double width_min, double width_max,
+                              int roi_size, int channel);
+/* mp_fit_dao.c:82 mpDaoNewPeaks */
+void mpDaoNewPeaks(saMPFit *mp_fit, double *peak_params, char *p_type, int n_peaks);
+
 /* ---- shared LM core (sa_library/multi_fit.c) ----------------------------- */
 
 /* multi_fit.c:90 mFitAnscombeTransformImage (ALS only; reports an error) */

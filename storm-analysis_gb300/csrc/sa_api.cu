@@ -14,6 +14,7 @@
 #include "sa_launch.h"
 #include "sa_psf_fft.h"
 #include "sa_pupil_fn.h"
+#include "sa_mp.h"
 #include "sa_cuda.h"
 
 using namespace sa;
@@ -2079,6 +2080,315 @@ int saSlotResults(saFitData* h, int slot, double* values, int32_t* ints) {
     ints[j * 2 + 1] = recs[j].iterations;
   }
   return n;
+}
+
+
+// ---- multi-plane fitting (multi_plane/mp_fit.c, mp_fit_arb.c, mp_fit_dao.c;
+// multi_plane/mp_fit_c.py, mp_fit_arb_c.py, mp_fit_dao_c.py bind them) ----
+//
+// The channels are ordinary handles of this library (one image plane
+// each, FP64 engine); the coupled sweep runs on the device (sa_mp.cuh).
+
+struct MPState {
+  int kind = -1;                 // MP_ARB / MP_DAO once a channel is set
+  std::vector<double> xt0N, yt0N, xtN0, ytN0;
+  std::vector<double> w;         // bg, h, x, y, z weights, each [n_weights][nc]
+  double* d_w = nullptr;
+  MPChan* d_chans = nullptr;
+  std::vector<saFitData*> fit;   // the channels (also in saMPFit.fit_data)
+};
+
+static MPState* MPS(saMPFit* mp) { return mp ? reinterpret_cast<MPState*>(mp->engine) : nullptr; }
+
+// A channel's own cleanup (a spline channel frees its spline: cfCleanup).
+static void mp_channel_cleanup(saFitData* h) {
+  Engine* e = E(h);
+  if (e && e->spline) cfCleanup(h);
+  else daoCleanup(h);
+}
+
+// mpInitialize mp_fit.c:146-175.
+saMPFit* mpInitialize(double tolerance, int n_channels, int independent_heights, int im_size_x, int im_size_y) {
+  if (n_channels < 1 || n_channels > MP_MAXCH) {
+    set_error("mpInitialize: %d channels (1..%d)", n_channels, MP_MAXCH);
+    return nullptr;
+  }
+  saMPFit* mp = static_cast<saMPFit*>(calloc(1, sizeof(saMPFit)));
+  MPState* st = new MPState();
+  mp->engine = st;
+  mp->im_size_x = im_size_x;
+  mp->im_size_y = im_size_y;
+  mp->independent_heights = independent_heights;
+  mp->n_channels = n_channels;
+  mp->tolerance = tolerance;
+  const int n3 = 3 * n_channels;
+  st->xt0N.assign(n3, 0.0);
+  st->yt0N.assign(n3, 0.0);
+  st->xtN0.assign(n3, 0.0);
+  st->ytN0.assign(n3, 0.0);
+  mp->xt_0toN = st->xt0N.data();
+  mp->yt_0toN = st->yt0N.data();
+  mp->xt_Nto0 = st->xtN0.data();
+  mp->yt_Nto0 = st->ytN0.data();
+  st->fit.assign(n_channels, nullptr);
+  mp->fit_data = st->fit.data();
+  return mp;
+}
+
+// A channel handle made by one of the fitters' initialisers: the FP64
+// engine, minimum height 1 (mp_fit_arb.c / mp_fit_dao.c set it).
+static int mp_attach(saMPFit* mp, saFitData* h, int channel, int kind) {
+  MPState* st = MPS(mp);
+  if (!h) return -1;
+  if (channel < 0 || channel >= mp->n_channels) {
+    set_error("channel %d out of range (%d channels)", channel, mp->n_channels);
+    mp_channel_cleanup(h);
+    return -1;
+  }
+  if (st->kind >= 0 && st->kind != kind) {
+    set_error("multi-plane channels must all be Gaussian or all arbitrary-PSF");
+    mp_channel_cleanup(h);
+    return -1;
+  }
+  if (st->fit[channel]) mp_channel_cleanup(st->fit[channel]);
+  st->kind = kind;
+  Engine* e = E(h);
+  e->prec = 64;
+  e->cfg.min_height = 1.0;
+  h->minimum_height = 1.0;
+  st->fit[channel] = h;
+  return 0;
+}
+
+// mpArbInitializePSFFFTChannel mp_fit_arb.c:36-77.
+void mpArbInitializePSFFFTChannel(saMPFit* mp, void* psf_fft, double* rqe, double* variance, int channel) {
+  if (!MPS(mp)) return;
+  mp_attach(mp, ftFitInitialize(psf_fft, rqe, variance, mp->tolerance, mp->im_size_x, mp->im_size_y), channel,
+            MP_ARB);
+}
+
+// mpArbInitializePupilFnChannel mp_fit_arb.c:85-128.
+void mpArbInitializePupilFnChannel(saMPFit* mp, void* pupil_data, double* rqe, double* variance, double zmin,
+                                   double zmax, int channel) {
+  if (!MPS(mp)) return;
+  saFitData* h = pfitInitialize(pupil_data, rqe, variance, mp->tolerance, mp->im_size_x, mp->im_size_y);
+  if (mp_attach(mp, h, channel, MP_ARB) == 0) pfitSetZRange(h, zmin, zmax);
+}
+
+// mpArbInitializeSplineChannel mp_fit_arb.c:135-172.
+void mpArbInitializeSplineChannel(saMPFit* mp, void* spline, double* rqe, double* variance, int channel) {
+  if (!MPS(mp)) return;
+  saFitData* h = cfInitialize(spline, rqe, variance, mp->tolerance, mp->im_size_x, mp->im_size_y);
+  if (h) cfInitialize3D(h);
+  mp_attach(mp, h, channel, MP_ARB);
+}
+
+// mpDaoInitialize2DChannel mp_fit_dao.c:28-73.
+void mpDaoInitialize2DChannel(saMPFit* mp, double* rqe, double* variance, double width_min, double width_max,
+                              int roi_size, int channel) {
+  if (!MPS(mp)) return;
+  saFitData* h = daoInitialize(rqe, variance, mp->tolerance, mp->im_size_x, mp->im_size_y, roi_size);
+  if (h) daoInitialize2D(h, width_min, width_max);
+  mp_attach(mp, h, channel, MP_DAO);
+}
+
+// mpSetTransforms mp_fit.c:535-548.
+void mpSetTransforms(saMPFit* mp, double* xt_0toN, double* yt_0toN, double* xt_Nto0, double* yt_Nto0) {
+  MPState* st = MPS(mp);
+  if (!st) return;
+  for (int i = 0; i < 3 * mp->n_channels; i++) {
+    st->xt0N[i] = xt_0toN[i];
+    st->yt0N[i] = yt_0toN[i];
+    st->xtN0[i] = xt_Nto0[i];
+    st->ytN0[i] = yt_Nto0[i];
+  }
+}
+
+// mpSetWeights mp_fit.c:561-592.
+void mpSetWeights(saMPFit* mp, double* w_bg, double* w_h, double* w_x, double* w_y, double* w_z, int z_size) {
+  MPState* st = MPS(mp);
+  if (!st) return;
+  const size_t n = (size_t)mp->n_channels * z_size;
+  st->w.assign(5 * n, 0.0);
+  const double* src[5] = {w_bg, w_h, w_x, w_y, w_z};
+  for (int k = 0; k < 5; k++) std::memcpy(st->w.data() + k * n, src[k], sizeof(double) * n);
+  mp->n_weights = z_size;
+  mp->w_bg = st->w.data();
+  mp->w_h = st->w.data() + n;
+  mp->w_x = st->w.data() + 2 * n;
+  mp->w_y = st->w.data() + 3 * n;
+  mp->w_z = st->w.data() + 4 * n;
+  if (st->d_w) {
+    cudaFree(st->d_w);
+    st->d_w = nullptr;
+  }
+}
+
+// mpSetWeightsIndexing mp_fit.c:600-604.
+void mpSetWeightsIndexing(saMPFit* mp, double z_offset, double z_scale) {
+  if (!mp) return;
+  mp->w_z_offset = z_offset;
+  mp->w_z_scale = z_scale;
+}
+
+// The channel descriptors and parameters of a multi-plane launch; all
+// channels must be set, imaged and hold the same number of peaks.
+static int mp_prepare(saMPFit* mp, MPParams& p, int& frames, cudaStream_t& stream) {
+  MPState* st = MPS(mp);
+  if (!st) return -1;
+  const int nc = mp->n_channels;
+  for (int c = 0; c < nc; c++) {
+    if (!st->fit[c] || !E(st->fit[c])->d_x) {
+      set_error("multi-plane channel %d is not initialised or has no image", c);
+      return -1;
+    }
+  }
+  if (st->w.empty()) {
+    set_error("mpSetWeights has not been called");
+    return -1;
+  }
+  Engine* e0 = E(st->fit[0]);
+  std::vector<MPChan> chans(nc);
+  int ws = 0;
+  for (int c = 0; c < nc; c++) {
+    Engine* e = E(st->fit[c]);
+    if (e->F != e0->F || e->npix != e0->npix) {
+      set_error("multi-plane channels must have the same frames");
+      return -1;
+    }
+    chans[c].cfg = e->cfg;
+    chans[c].fs = e->fs<double>();
+    ws = std::max(ws, mp_ws_bytes(e->cfg));
+    CK(cudaStreamSynchronize(e->stream));
+  }
+  if (!st->d_chans) CK(cudaMalloc(&st->d_chans, sizeof(MPChan) * MP_MAXCH));
+  CK(cudaMemcpy(st->d_chans, chans.data(), sizeof(MPChan) * nc, cudaMemcpyHostToDevice));
+  if (!st->d_w) {
+    CK(cudaMalloc(&st->d_w, sizeof(double) * st->w.size()));
+    CK(cudaMemcpy(st->d_w, st->w.data(), sizeof(double) * st->w.size(), cudaMemcpyHostToDevice));
+  }
+  std::memset(&p, 0, sizeof(p));
+  p.nc = nc;
+  p.indep = mp->independent_heights;
+  p.kind = st->kind;
+  p.n_weights = mp->n_weights;
+  p.tol = mp->tolerance;
+  p.w_z_offset = mp->w_z_offset;
+  p.w_z_scale = mp->w_z_scale;
+  for (int i = 0; i < 3 * nc; i++) {
+    p.xt0N[i] = st->xt0N[i];
+    p.yt0N[i] = st->yt0N[i];
+    p.xtN0[i] = st->xtN0[i];
+    p.ytN0[i] = st->ytN0[i];
+  }
+  p.w = st->d_w;
+  p.ws_bytes = ws;
+  frames = e0->F;
+  stream = e0->stream;
+  return 0;
+}
+
+// After a multi-plane kernel: the channels' host copies are stale.
+static int mp_finish(saMPFit* mp, cudaStream_t stream) {
+  MPState* st = MPS(mp);
+  CK(cudaStreamSynchronize(stream));
+  for (int c = 0; c < mp->n_channels; c++) {
+    Engine* e = E(st->fit[c]);
+    e->host_valid = false;
+    e->unconv_cache = -1;
+    sync_counters(st->fit[c]);
+  }
+  return 0;
+}
+
+// mpArbNewPeaks mp_fit_arb.c:180-340, mpDaoNewPeaks mp_fit_dao.c:82-152.
+static void mp_new_peaks(saMPFit* mp, double* peaks, char* p_type, int n, bool arb) {
+  MPState* st = MPS(mp);
+  if (!st) return;
+  const int pt = parse_ptype(p_type);
+  if (pt < 0) {
+    set_error("Unrecognized peak type '%s'!", p_type ? p_type : "(null)");
+    return;
+  }
+  for (int c = 0; c < mp->n_channels; c++) {
+    if (!st->fit[c]) {
+      set_error("multi-plane channel %d is not initialised", c);
+      return;
+    }
+  }
+  const int start = st->fit[0]->nfit;
+  const int ncol = (pt == PT_TEXT) ? (arb ? 5 : 7) : (arb ? 3 : 4);
+  std::vector<double> mapped((size_t)ncol * std::max(n, 1));
+  for (int c = 0; c < mp->n_channels; c++) {
+    double* rows = peaks;
+    if (c > 0) {
+      for (int j = 0; j < n; j++) {
+        const double* q = peaks + (size_t)ncol * j;
+        double* o = mapped.data() + (size_t)ncol * j;
+        const double tx = q[0], ty = q[1];
+        for (int k = 0; k < ncol; k++) o[k] = q[k];
+        o[0] = st->xt0N[c * 3] + tx * st->xt0N[c * 3 + 1] + ty * st->xt0N[c * 3 + 2];
+        o[1] = st->yt0N[c * 3] + tx * st->yt0N[c * 3 + 1] + ty * st->yt0N[c * 3 + 2];
+      }
+      rows = mapped.data();
+    }
+    if (new_peaks_single(st->fit[c], rows, p_type, n)) return;
+  }
+  MPParams p;
+  int frames = 0;
+  cudaStream_t stream = nullptr;
+  if (mp_prepare(mp, p, frames, stream)) return;
+  p.start = start;
+  p.stop = start + n;
+  p.fix_heights = (arb && !mp->independent_heights && pt != PT_TEXT) ? 1 : 0;
+  cudaError_t err = mp_newpeaks(st->d_chans, p, 1, stream);
+  if (err != cudaSuccess) {
+    set_error("multi-plane new peaks: %s", cudaGetErrorString(err));
+    return;
+  }
+  mp_finish(mp, stream);
+}
+
+void mpArbNewPeaks(saMPFit* mp, double* peaks, char* p_type, int n_peaks) {
+  mp_new_peaks(mp, peaks, p_type, n_peaks, true);
+}
+
+void mpDaoNewPeaks(saMPFit* mp, double* peaks, char* p_type, int n_peaks) {
+  mp_new_peaks(mp, peaks, p_type, n_peaks, false);
+}
+
+// mpIterateLM mp_fit.c:183-478: one coupled sweep on the device.
+void mpIterateLM(saMPFit* mp) {
+  MPState* st = MPS(mp);
+  if (!st) return;
+  MPParams p;
+  int frames = 0;
+  cudaStream_t stream = nullptr;
+  if (mp_prepare(mp, p, frames, stream)) return;
+  for (int c = 1; c < mp->n_channels; c++) {
+    if (st->fit[c]->nfit != st->fit[0]->nfit) {
+      set_error("multi-plane channels hold different numbers of peaks");
+      return;
+    }
+  }
+  cudaError_t err = mp_sweep(st->d_chans, p, 1, stream);
+  if (err != cudaSuccess) {
+    set_error("mpIterateLM: %s", cudaGetErrorString(err));
+    return;
+  }
+  mp_finish(mp, stream);
+}
+
+// mpCleanup mp_fit.c:76-115 (each channel's fitter cleanup).
+void mpCleanup(saMPFit* mp) {
+  MPState* st = MPS(mp);
+  if (!st) return;
+  for (saFitData* h : st->fit)
+    if (h) mp_channel_cleanup(h);
+  if (st->d_w) cudaFree(st->d_w);
+  if (st->d_chans) cudaFree(st->d_chans);
+  delete st;
+  free(mp);
 }
 
 }  // extern "C"

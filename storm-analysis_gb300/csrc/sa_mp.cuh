@@ -1,0 +1,492 @@
+// sa_mp.cuh -- multi-plane fitting on the device: the coupled LM sweep of
+// multi_plane/mp_fit.c (mpIterateLM) with the parameter updates of
+// mp_fit_arb.c (spline, pupil-function and FFT PSFs) and mp_fit_dao.c (2D
+// Gaussians), over channel engines that each hold one image plane.
+//
+// A group is one peak per channel at the same index.  Its channels share
+// status and lambda; x / y are tied through the affine maps between the
+// planes, z (and, unless the heights are independent) the height through
+// z-dependent weighted averages of the channels' LM steps.  One warp runs a
+// frame's groups in index order, the reference's Gauss-Seidel order, so a
+// multi-frame batch is parallel over frames only.  The FP64 engine.
+#pragma once
+
+#include "sa_kernels.cuh"
+#include "sa_mp_types.h"
+
+namespace sa {
+
+__device__ __forceinline__ long long mp_fbase(const MPChan& c, int f) { return (long long)f * c.fs.npix; }
+
+// mFitCalcErr multi_fit.c:111-195 from the global state: the deviance over
+// the ROI; true (and no error) when some fi <= 0.
+__device__ inline bool mp_error(const MPChan& c, long long fbase, const PeakRec& w, double& dev, int lane) {
+  double d = 0.0;
+  bool fail = false;
+  for (int p = lane; p < c.cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(c.fs.roi_xy, p, rx, ry);
+    const long long k = pix_index(c.cfg, w.xi, w.yi, rx, ry);
+    const double fi = fi_global(c.fs, fbase + k);
+    const double xv = __ldg(c.fs.x + fbase + k);
+    if (!(fi > 0.0)) fail = true;
+    else d += deviance(fi, xv);
+  }
+  dev = warp_sum(d);
+  return __any_sync(0xffffffffu, fail);
+}
+
+// fn_calc_JH on the global state with the peak still added (the fi of the
+// preceding mFitCalcErr): gradient and packed upper Hessian into jh.
+__device__ inline void mp_jh(const MPChan& c, long long fbase, const PeakRec& w, WarpWS<double>& ws, double* jh,
+                             int lane) {
+  const ModelCfg& cfg = c.cfg;
+  const int k = cfg.jac;
+  SplinePos s = shape_tables(cfg, w, ws, lane);
+  double gxd, gyd;
+  z_factors(cfg, cfg.model, w, gxd, gyd);
+  double acc[32];
+#pragma unroll
+  for (int i = 0; i < 32; i++) acc[i] = 0.0;
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(c.fs.roi_xy, p, rx, ry);
+    const long long kk = pix_index(cfg, w.xi, w.yi, rx, ry);
+    const double fi = fi_global(c.fs, fbase + kk);
+    const double xv = __ldg(c.fs.x + fbase + kk);
+    const double rq = __ldg(c.fs.rqe + kk);
+    const double psf = psf_at(cfg, c.fs.aij, ws, s, rx, ry);
+    const double t1 = 2.0 * (1.0 - xv / fi);
+    const double t2 = 2.0 * xv / (fi * fi);
+    double jt[MAX_JAC];
+    jt_row(cfg, c.fs.aij, ws, s, w, gxd, gyd, rx, ry, rq, psf, jt);
+#pragma unroll
+    for (int l = 0; l < MAX_JAC; l++)
+      if (l < k) acc[l] += t1 * jt[l];
+#pragma unroll
+    for (int l = 0; l < MAX_JAC; l++) {
+#pragma unroll
+      for (int m = l; m < MAX_JAC; m++) {
+        if (l < k && m < k) {
+          const int id = k + l * k - (l * (l - 1)) / 2 + (m - l);
+          if (id < 32) acc[id] += t2 * jt[l] * jt[m];
+        }
+      }
+    }
+  }
+  const double v = warp_transpose_sum32(acc, lane);
+  if (lane < k + k * (k + 1) / 2) jh[lane] = v;
+  __syncwarp();
+}
+
+// Add (+1) or subtract (-1) channel c's working peak (its shape computed here).
+__device__ inline void mp_add(const MPChan& c, long long fbase, const PeakRec& w, WarpWS<double>& ws, int sign,
+                              int lane) {
+  SplinePos s = shape_tables(c.cfg, w, ws, lane, false);
+  add_peak(c.cfg, c.fs, fbase, w, s, ws, sign, lane);
+  __syncwarp();
+}
+
+// mpWeightIndex mp_fit.c:703-725 (channel 0's working z) and
+// mpWeightInterpolate :732-741.
+__device__ inline void mp_weight_index(const MPParams& p, double z0, double& dz, int& zi) {
+  const double t = p.w_z_scale * (z0 - p.w_z_offset);
+  zi = (int)t;
+  dz = t - (double)zi;
+  if (zi < 0) zi = 0;
+  if (zi > p.n_weights - 2) zi = p.n_weights - 2;
+}
+__device__ inline double mp_weight(const MPParams& p, int which, double dz, int zi, int ch) {
+  const double* w = p.w + (size_t)which * p.n_weights * p.nc;
+  const double w1 = w[p.nc * zi + ch], w2 = w[p.nc * (zi + 1) + ch];
+  return w1 + (w2 - w1) * dz;
+}
+enum { MPW_BG = 0, MPW_H = 1, MPW_X = 2, MPW_Y = 3, MPW_Z = 4 };
+
+// fn_zrange: ftFitZRangeCheck fft_fit.c:506-524, pfitZRangeCheck
+// pupil_fit.c:555-570, cfZRangeCheck cubic_fit.c:987-1005 (which sets zi).
+__device__ inline void mp_z_range(const ModelCfg& cfg, PeakRec& w) {
+  if (cfg.model == M_FFT) {
+    const double max_z = ((double)cfg.sz) * 0.5 - 1.0e-12;
+    if (w.p[PZ] < -max_z) w.p[PZ] = -max_z;
+    if (w.p[PZ] > max_z) w.p[PZ] = max_z;
+  } else if (cfg.model == M_PUPIL) {
+    if (w.p[PZ] < cfg.zmin) w.p[PZ] = cfg.zmin;
+    if (w.p[PZ] > cfg.zmax) w.p[PZ] = cfg.zmax;
+  } else if (cfg.model == M_SPLINE3D) {
+    if (w.p[PZ] < 1.0e-12) w.p[PZ] = 1.0e-12;
+    const double zmax = ((double)cfg.sz) - 1.0e-12;
+    if (w.p[PZ] > zmax) w.p[PZ] = zmax;
+    w.zi = (int)(w.p[PZ]);
+  }
+}
+
+// fn_check of a channel: daoCheck2D for the Gaussians, mFitCheck otherwise;
+// counts the margin / height failures on its frame.
+__device__ inline int mp_check(const MPChan& c, int f, PeakRec& w) {
+  const int r = (c.cfg.model == M_2D) ? model_check(c.cfg, M_2D, w) : base_check(c.cfg, w);
+  if (r == 1) c.fs.ctl[f].ctr[C_MARGIN]++;
+  else if (r == 2) c.fs.ctl[f].ctr[C_NEGH]++;
+  return r;
+}
+
+// The channels' parameter update from their steps (lane 0): mpArbUpdateFixed
+// mp_fit_arb.c:400-432 / mpArbUpdateIndependent :449-470 / mpDaoUpdate
+// mp_fit_dao.c:164-209, each with mpUpdate mp_fit.c:626-696 and (arbitrary
+// PSFs) mpArbUpdateZ mp_fit_arb.c:351-384.  The 2D Gaussian update moves the
+// x width only (the y width keeps its value) and applies daoCheck2D (its
+// clamp and counters) without using its result.
+__device__ inline void mp_update(const MPChan* ch, const MPParams& p, MPShared& S, int f) {
+  const int nc = p.nc;
+  double dz, p_ave, p_total, w;
+  int zi;
+  if (p.kind == MP_DAO || p.indep) {
+    for (int i = 0; i < nc; i++) {
+      S.w[i].p[PH] -= S.dl[i][0];
+      if (S.w[i].p[PH] < 0.01) S.w[i].p[PH] = 0.01;
+      S.heights[i] = S.w[i].p[PH];
+    }
+  }
+  if (p.kind == MP_DAO) {
+    for (int i = 0; i < nc; i++) {
+      S.w[i].p[PXW] -= S.dl[i][3];
+      (void)mp_check(ch[i], f, S.w[i]);
+    }
+  } else if (!p.indep) {
+    mp_weight_index(p, S.w[0].p[PZ], dz, zi);
+    p_ave = 0.0;
+    p_total = 0.0;
+    for (int i = 0; i < nc; i++) {
+      w = mp_weight(p, MPW_H, dz, zi, i);
+      p_ave += S.dl[i][0] * w;
+      p_total += w;
+    }
+    S.w[0].p[PH] -= p_ave / p_total;
+    for (int i = 1; i < nc; i++) S.w[i].p[PH] = S.w[0].p[PH];
+  }
+  // mpUpdate: x, y
+  mp_weight_index(p, S.w[0].p[PZ], dz, zi);
+  p_ave = 0.0;
+  p_total = 0.0;
+  for (int i = 0; i < nc; i++) {
+    w = mp_weight(p, MPW_X, dz, zi, i);
+    double d = p.xtN0[i * 3 + 1] * S.dl[i][1];
+    d += p.xtN0[i * 3 + 2] * S.dl[i][2];
+    p_ave += d * w * S.heights[i];
+    p_total += w * S.heights[i];
+  }
+  S.w[0].p[PX] -= p_ave / p_total;
+  p_ave = 0.0;
+  p_total = 0.0;
+  for (int i = 0; i < nc; i++) {
+    w = mp_weight(p, MPW_Y, dz, zi, i);
+    double d = p.ytN0[i * 3 + 1] * S.dl[i][1];
+    d += p.ytN0[i * 3 + 2] * S.dl[i][2];
+    p_ave += d * w * S.heights[i];
+    p_total += w * S.heights[i];
+  }
+  S.w[0].p[PY] -= p_ave / p_total;
+  const double xoff = ch[0].cfg.xoff, yoff = ch[0].cfg.yoff;
+  for (int i = 1; i < nc; i++) {
+    double t = p.xt0N[i * 3];
+    t += p.xt0N[i * 3 + 1] * (S.w[0].p[PX] + xoff);
+    t += p.xt0N[i * 3 + 2] * (S.w[0].p[PY] + yoff);
+    S.w[i].p[PX] = t - xoff;
+    t = p.yt0N[i * 3];
+    t += p.yt0N[i * 3 + 1] * (S.w[0].p[PX] + xoff);
+    t += p.yt0N[i * 3 + 2] * (S.w[0].p[PY] + yoff);
+    S.w[i].p[PY] = t - yoff;
+  }
+  for (int i = 0; i < nc; i++) anchor_update(S.w[i]);
+  for (int i = 0; i < nc; i++) S.w[i].p[PBG] -= S.dl[i][4];
+  if (p.kind == MP_ARB) {
+    // mpArbUpdateZ (the weight index from the updated channel-0 z is not
+    // needed: z has not moved yet)
+    mp_weight_index(p, S.w[0].p[PZ], dz, zi);
+    p_ave = 0.0;
+    p_total = 0.0;
+    for (int i = 0; i < nc; i++) {
+      w = mp_weight(p, MPW_Z, dz, zi, i);
+      p_ave += S.dl[i][3] * w * S.heights[i];
+      p_total += w * S.heights[i];
+    }
+    const double delta = p_ave / p_total;
+    for (int i = 0; i < nc; i++) {
+      S.w[i].p[PZ] -= delta;
+      mp_z_range(ch[i].cfg, S.w[i]);
+    }
+  }
+}
+
+// mpCheckError mp_fit.c:43-68 for group g.
+__device__ inline void mp_check_error(const MPChan* ch, const MPParams& p, int f, int g, char* wsbase, int lane) {
+  bool bad = false;
+  for (int c = 0; c < p.nc; c++) bad |= (ch[c].fs.pk[ch[c].fs.pk_off[f] + g].status == ERROR);
+  if (!bad) return;
+  for (int c = 0; c < p.nc; c++) {
+    PeakRec* q = ch[c].fs.pk + ch[c].fs.pk_off[f] + g;
+    PeakRec r;
+    load_rec(q, r);
+    if (r.status != ERROR) {
+      WarpWS<double> wc = warp_ws<double>(wsbase, ch[c].cfg, 0);
+      mp_add(ch[c], mp_fbase(ch[c], f), r, wc, -1, lane);
+      r.added -= 1;
+    }
+    r.status = ERROR;
+    __syncwarp();
+    if (lane == 0) *q = r;
+    __syncwarp();
+  }
+}
+
+enum { MPA_EVAL = 0, MPA_CONTINUE = 1, MPA_BREAK = 2 };
+
+// mpIterateLM mp_fit.c:183-478 for frame blockIdx.x, then mFitRecenterPeaks
+// per channel and mpCheckError per group.
+__global__ void __launch_bounds__(32) k_mp_sweep(const MPChan* chans, MPParams p) {
+  extern __shared__ __align__(16) char smem[];
+  const int lane = threadIdx.x;
+  const int f = blockIdx.x;
+  MPChan* ch = reinterpret_cast<MPChan*>(smem + p.ws_bytes + ((sizeof(MPShared) + 15) & ~(size_t)15));
+  for (int i = lane; i < (int)(p.nc * sizeof(MPChan) / 4); i += 32)
+    reinterpret_cast<int*>(ch)[i] = reinterpret_cast<const int*>(chans)[i];
+  __syncwarp();
+  MPShared& S = *reinterpret_cast<MPShared*>(smem + p.ws_bytes);
+  const int nc = p.nc;
+  const int nfit = ch[0].fs.nfit[f];
+  // relative heights: 1 for fixed heights (mpSetWeights mp_fit.c:589-591);
+  // independent and Gaussian updates set them before use
+  if (lane < MP_MAXCH) S.heights[lane] = 1.0;
+  __syncwarp();
+  for (int g = 0; g < nfit; g++) {
+    if (ch[0].fs.pk[ch[0].fs.pk_off[f] + g].status != RUNNING) continue;
+    double e0 = 0.0;
+    for (int c = 0; c < nc; c++) {
+      const long long fb = mp_fbase(ch[c], f);
+      PeakRec r;
+      load_rec(ch[c].fs.pk + ch[c].fs.pk_off[f] + g, r);
+      double dev;
+      const bool fail = mp_error(ch[c], fb, r, dev, lane);
+      if (lane == 0) S.orig[c] = r;   // the stored peak (mpResetWorkingPeaks restores it)
+      if (!fail) r.error = dev;       // the return value is ignored (mp_fit.c:220)
+      else if (lane == 0) ch[c].fs.ctl[f].ctr[C_NEGFI]++;
+      e0 += r.error;
+      if (lane == 0) S.w[c] = r;
+      __syncwarp();
+      WarpWS<double> wc = warp_ws<double>(smem, ch[c].cfg, 0);
+      mp_jh(ch[c], fb, r, wc, S.jh[c], lane);
+      mp_add(ch[c], fb, r, wc, -1, lane);
+      if (lane == 0) S.w[c].added -= 1;
+      __syncwarp();
+    }
+    for (;;) {
+      int act = MPA_EVAL;
+      if (lane == 0) {
+        if (S.w[0].lambda > LAMBDA_MAX) {
+          for (int c = 0; c < nc; c++) {
+            ch[c].fs.ctl[f].ctr[C_LOST]++;
+            S.w[c].status = ERROR;
+          }
+          act = MPA_BREAK;
+        } else {
+          for (int c = 0; c < nc; c++) S.w[c].status = RUNNING;
+          bool bad = false;
+          for (int c = 0; c < nc; c++) {
+            S.w[c].iterations++;
+            ch[c].fs.ctl[f].ctr[C_ITER]++;
+            if (solve_fp64_lane0(S.jh[c], ch[c].cfg.jac, S.w[c].lambda, S.dl[c]) != 0) {
+              ch[c].fs.ctl[f].ctr[C_DPOSV]++;
+              bad = true;
+              break;
+            }
+          }
+          if (bad) {
+            for (int c = 0; c < nc; c++) {
+              S.w[c].status = ERROR;
+              S.w[c].lambda = S.w[c].lambda * LAMBDA_UP;
+            }
+            act = MPA_CONTINUE;
+          } else {
+            mp_update(ch, p, S, f);
+            for (int c = 0; c < nc; c++)
+              if (mp_check(ch[c], f, S.w[c])) bad = true;
+            if (bad) {
+              // mpResetWorkingPeaks mp_fit.c:500-521
+              for (int c = 0; c < nc; c++) {
+                const int added = S.w[c].added;
+                const double lam = S.w[c].lambda;
+                S.w[c] = S.orig[c];
+                S.w[c].added = added;
+                S.w[c].lambda = lam * LAMBDA_UP;
+                S.w[c].status = ERROR;
+              }
+              act = MPA_CONTINUE;
+            }
+          }
+        }
+      }
+      act = __shfl_sync(0xffffffffu, act, 0);
+      __syncwarp();
+      if (act == MPA_BREAK) break;
+      if (act == MPA_CONTINUE) continue;
+      // add the trial peaks, their error (mp_fit.c:340-378)
+      double e1 = 0.0;
+      bool bad = false;
+      for (int c = 0; c < nc; c++) {
+        WarpWS<double> wc = warp_ws<double>(smem, ch[c].cfg, 0);
+        const PeakRec r = S.w[c];
+        mp_add(ch[c], mp_fbase(ch[c], f), r, wc, +1, lane);
+        if (lane == 0) S.w[c].added += 1;
+        __syncwarp();
+      }
+      for (int c = 0; c < nc; c++) {
+        double dev;
+        const bool fail = mp_error(ch[c], mp_fbase(ch[c], f), S.w[c], dev, lane);
+        if (fail) {
+          bad = true;
+          if (lane == 0) ch[c].fs.ctl[f].ctr[C_NEGFI]++;
+        } else {
+          e1 += dev;
+          if (lane == 0) S.w[c].error = dev;
+        }
+        __syncwarp();
+      }
+      int undo = 0;
+      if (lane == 0) {
+        if (bad) {
+          undo = 1;
+          act = MPA_CONTINUE;
+        } else if (e1 > e0) {
+          if (((e1 - e0) / e0) < p.tol) {
+            for (int c = 0; c < nc; c++) S.w[c].status = CONVERGED;
+            act = MPA_BREAK;
+          } else {
+            for (int c = 0; c < nc; c++) ch[c].fs.ctl[f].ctr[C_NONDECR]++;
+            undo = 1;
+            act = MPA_CONTINUE;
+          }
+        } else {
+          if (((e0 - e1) / e0) < p.tol) {
+            for (int c = 0; c < nc; c++) S.w[c].status = CONVERGED;
+          } else if (S.w[0].lambda > LAMBDA_MIN) {
+            for (int c = 0; c < nc; c++) S.w[c].lambda = S.w[c].lambda * LAMBDA_DOWN;
+          }
+          act = MPA_BREAK;
+        }
+      }
+      undo = __shfl_sync(0xffffffffu, undo, 0);
+      act = __shfl_sync(0xffffffffu, act, 0);
+      __syncwarp();
+      if (undo) {
+        for (int c = 0; c < nc; c++) {
+          WarpWS<double> wc = warp_ws<double>(smem, ch[c].cfg, 0);
+          const PeakRec r = S.w[c];
+          mp_add(ch[c], mp_fbase(ch[c], f), r, wc, -1, lane);
+        }
+        if (lane == 0) {
+          for (int c = 0; c < nc; c++) {
+            const int added = S.w[c].added - 1;
+            const double lam = S.w[c].lambda;
+            S.w[c] = S.orig[c];
+            S.w[c].added = added;
+            S.w[c].lambda = lam * LAMBDA_UP;
+            S.w[c].status = ERROR;
+          }
+        }
+        __syncwarp();
+      }
+      if (act == MPA_BREAK) break;
+    }
+    // mpCopyFromWorking mp_fit.c:124-134: channel 0's status for all
+    __syncwarp();
+    if (lane == 0) {
+      for (int c = 0; c < nc; c++) {
+        S.w[c].status = S.w[0].status;
+        ch[c].fs.pk[ch[c].fs.pk_off[f] + g] = S.w[c];
+      }
+    }
+    __syncwarp();
+  }
+  __threadfence_block();
+  // mFitRecenterPeaks multi_fit.c:1644-1690, per channel
+  for (int c = 0; c < nc; c++) {
+    const long long fb = mp_fbase(ch[c], f);
+    WarpWS<double> wc = warp_ws<double>(smem, ch[c].cfg, 0);
+    for (int g = 0; g < nfit; g++) {
+      PeakRec* q = ch[c].fs.pk + ch[c].fs.pk_off[f] + g;
+      PeakRec r;
+      load_rec(q, r);
+      if (r.status != RUNNING) continue;
+      const double dx = r.p[PX] - r.xi, dy = r.p[PY] - r.yi;
+      if (!((dx < -0.25) || (dx > 1.25) || (dy < -0.25) || (dy > 1.25))) continue;
+      mp_add(ch[c], fb, r, wc, -1, lane);
+      r.added -= 1;
+      r.xi = (int)floor(r.p[PX]);
+      r.yi = (int)floor(r.p[PY]);
+      const int chk = base_check(ch[c].cfg, r);
+      if (chk) {
+        if (lane == 0) {
+          ch[c].fs.ctl[f].ctr[C_LOST]++;
+          ch[c].fs.ctl[f].ctr[chk == 1 ? C_MARGIN : C_NEGH]++;
+        }
+        r.status = ERROR;
+      } else {
+        mp_add(ch[c], fb, r, wc, +1, lane);
+        r.added += 1;
+      }
+      __syncwarp();
+      if (lane == 0) *q = r;
+      __syncwarp();
+    }
+  }
+  for (int g = 0; g < nfit; g++) mp_check_error(ch, p, f, g, smem, lane);
+}
+
+// After the channels' own new-peak passes (mpArbNewPeaks mp_fit_arb.c:180-340,
+// mpDaoNewPeaks mp_fit_dao.c:82-152): with fixed heights the new "finder" /
+// "testing" groups take their channels' mean height (their peaks subtracted,
+// re-added at that height and their error recomputed), then every new group
+// with an ERROR peak is made ERROR in all channels (mpCheckError).
+__global__ void __launch_bounds__(32) k_mp_newpeaks(const MPChan* chans, MPParams p) {
+  extern __shared__ __align__(16) char smem[];
+  const int lane = threadIdx.x;
+  const int f = blockIdx.x;
+  MPChan* ch = reinterpret_cast<MPChan*>(smem + p.ws_bytes + ((sizeof(MPShared) + 15) & ~(size_t)15));
+  for (int i = lane; i < (int)(p.nc * sizeof(MPChan) / 4); i += 32)
+    reinterpret_cast<int*>(ch)[i] = reinterpret_cast<const int*>(chans)[i];
+  __syncwarp();
+  const int nc = p.nc;
+  for (int g = p.start; g < p.stop; g++) {
+    if (p.fix_heights) {
+      double height = 0.0;
+      for (int c = 0; c < nc; c++) height += ch[c].fs.pk[ch[c].fs.pk_off[f] + g].p[PH];
+      height = height / ((double)nc);
+      for (int c = 0; c < nc; c++) {
+        PeakRec* q = ch[c].fs.pk + ch[c].fs.pk_off[f] + g;
+        PeakRec r;
+        load_rec(q, r);
+        const long long fb = mp_fbase(ch[c], f);
+        WarpWS<double> wc = warp_ws<double>(smem, ch[c].cfg, 0);
+        if (r.status != ERROR) mp_add(ch[c], fb, r, wc, -1, lane);
+        r.p[PH] = height;
+        if (r.status != ERROR) {
+          mp_add(ch[c], fb, r, wc, +1, lane);
+          if (r.status == RUNNING) {
+            double dev;
+            if (mp_error(ch[c], fb, r, dev, lane)) {
+              if (lane == 0) ch[c].fs.ctl[f].ctr[C_NEGFI]++;
+            } else {
+              r.error = dev;
+            }
+          }
+        }
+        __syncwarp();
+        if (lane == 0) *q = r;
+        __syncwarp();
+      }
+    }
+  }
+  for (int g = p.start; g < p.stop; g++) mp_check_error(ch, p, f, g, smem, lane);
+}
+
+}  // namespace sa

@@ -1,0 +1,37 @@
+// sa_mp_types.h -- the multi-plane kernels' parameter blocks (sa_mp.cuh),
+// shared with the host code that fills them.
+#pragma once
+
+#include "sa_common.cuh"
+
+namespace sa {
+
+constexpr int MP_MAXCH = 8;
+enum { MP_ARB = 0, MP_DAO = 1 };
+
+// One channel: its engine's model and frame set.
+struct MPChan {
+  ModelCfg cfg;
+  FrameSet<double> fs;
+};
+
+struct MPParams {
+  int nc, indep, kind, n_weights;
+  double tol, w_z_offset, w_z_scale;
+  double xt0N[3 * MP_MAXCH], yt0N[3 * MP_MAXCH], xtN0[3 * MP_MAXCH], ytN0[3 * MP_MAXCH];
+  const double* w;   // weights bg, h, x, y, z: 5 x [n_weights][nc] (z the slow index)
+  int ws_bytes;      // a channel workspace (the largest of the channels')
+  int start, stop;   // k_mp_newpeaks: the new groups
+  int fix_heights;   // k_mp_newpeaks: give the new groups their channels' mean height
+};
+
+// Per-frame state in shared memory (lane 0 writes the records).
+struct MPShared {
+  PeakRec orig[MP_MAXCH];
+  PeakRec w[MP_MAXCH];
+  double jh[MP_MAXCH][36];   // gradient (k) and packed upper Hessian per channel
+  double dl[MP_MAXCH][8];    // the channels' LM steps
+  double heights[MP_MAXCH];
+};
+
+}  // namespace sa

@@ -25,7 +25,7 @@ IA_LIB = os.path.join(HERE, "libsa_ia_utilities.so")
 SHIMS = [(MF_LIB, "sa_matched_filter.cpp"), (IA_LIB, "sa_ia_utilities.cpp")]
 BUILD_DIR = os.path.join(PKG_ROOT, "_build")
 
-SOURCES = ["sa_launch_f32.cu", "sa_launch_f64.cu", "sa_api.cu", "sa_finder.cu", "sa_solve.cu", "sa_psf_fft.cu",
+SOURCES = ["sa_launch_f32.cu", "sa_launch_f64.cu", "sa_api.cu", "sa_finder.cu", "sa_solve.cu", "sa_psf_fft.cu", "sa_mp.cu",
            "sa_pupil_fn.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]

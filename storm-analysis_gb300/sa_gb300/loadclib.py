@@ -21,6 +21,10 @@ class EngineUnavailable(RuntimeError):
     pass
 
 
+class saMPFit(ctypes.Structure):
+    pass
+
+
 class saFitData(ctypes.Structure):
     """The handle's leading fields, laid out as the reference's fitData."""
     _fields_ = ([(n, ctypes.c_int) for n in
@@ -37,6 +41,19 @@ class saFitData(ctypes.Structure):
                   "x_data"]] +
                 [("working_peak", ctypes.c_void_p), ("fit", ctypes.c_void_p), ("fit_model", ctypes.c_void_p),
                  ("fn_reserved", ctypes.c_void_p * 9), ("engine", ctypes.c_void_p)])
+
+
+# The multi-plane handle's leading fields, laid out as the reference's mpFit
+# (multi_plane/mp_fit.h:12-44; mp_fit_c.py mirrors them as mpFitData).
+saMPFit._fields_ = ([(n, ctypes.c_int) for n in ["im_size_x", "im_size_y", "independent_heights", "n_channels",
+                                                  "n_weights"]] +
+                    [(n, ctypes.c_double) for n in ["tolerance", "w_z_offset", "w_z_scale", "zmin", "zmax"]] +
+                    [(n, ctypes.POINTER(ctypes.c_double)) for n in ["xt_0toN", "yt_0toN", "xt_Nto0", "yt_Nto0",
+                                                                     "w_bg", "w_h", "w_x", "w_y", "w_z", "heights"]] +
+                    [(n, ctypes.c_void_p) for n in ["jacobian", "w_jacobian", "hessian", "w_hessian"]] +
+                    [("fit_data", ctypes.POINTER(ctypes.POINTER(saFitData)))] +
+                    [(n, ctypes.c_void_p) for n in ["fn_cleanup", "fn_newpeaks", "fn_peak_xi_yi", "fn_update",
+                                                     "fn_zrange", "engine"]])
 
 
 def last_error():
@@ -143,6 +160,32 @@ def _declare(lib):
     lib.pfitSetZRange.restype = None
     lib.pfitCleanup.argtypes = [hp]
     lib.pfitCleanup.restype = None
+    # multi-plane fitting (mp_fit.c / mp_fit_arb.c / mp_fit_dao.c names)
+    mpp = ctypes.POINTER(saMPFit)
+    lib.mpInitialize.argtypes = [cd, ci, ci, ci, ci]
+    lib.mpInitialize.restype = mpp
+    lib.mpCleanup.argtypes = [mpp]
+    lib.mpCleanup.restype = None
+    lib.mpIterateLM.argtypes = [mpp]
+    lib.mpIterateLM.restype = None
+    lib.mpSetTransforms.argtypes = [mpp, f64, f64, f64, f64]
+    lib.mpSetTransforms.restype = None
+    lib.mpSetWeights.argtypes = [mpp, f64, f64, f64, f64, f64, ci]
+    lib.mpSetWeights.restype = None
+    lib.mpSetWeightsIndexing.argtypes = [mpp, cd, cd]
+    lib.mpSetWeightsIndexing.restype = None
+    lib.mpArbInitializePSFFFTChannel.argtypes = [mpp, vp, f64, f64, ci]
+    lib.mpArbInitializePSFFFTChannel.restype = None
+    lib.mpArbInitializePupilFnChannel.argtypes = [mpp, vp, f64, f64, cd, cd, ci]
+    lib.mpArbInitializePupilFnChannel.restype = None
+    lib.mpArbInitializeSplineChannel.argtypes = [mpp, vp, f64, f64, ci]
+    lib.mpArbInitializeSplineChannel.restype = None
+    lib.mpArbNewPeaks.argtypes = [mpp, f64, cs, ci]
+    lib.mpArbNewPeaks.restype = None
+    lib.mpDaoInitialize2DChannel.argtypes = [mpp, f64, f64, cd, cd, ci, ci]
+    lib.mpDaoInitialize2DChannel.restype = None
+    lib.mpDaoNewPeaks.argtypes = [mpp, f64, cs, ci]
+    lib.mpDaoNewPeaks.restype = None
     for name in ["getXSize", "getYSize", "getZSize"]:
         getattr(lib, name).argtypes = [vp]
         getattr(lib, name).restype = ci
@@ -280,6 +323,9 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "pfnGetPSF", "pfnGetPSFdx", "pfnGetPSFdy", "pfnGetPSFdz", "pfnGetPSFIntensity", "pfnGetPXEX",
            "pfnGetPXEY", "pfnGetPYEX", "pfnGetPYEY", "pfnGetPZEX", "pfnGetPZEY", "pfnGetSize",
            "pfitInitialize", "pfitNewPeaks", "pfitSetZRange", "pfitCleanup",
+           "mpInitialize", "mpCleanup", "mpIterateLM", "mpSetTransforms", "mpSetWeights", "mpSetWeightsIndexing",
+           "mpArbInitializePSFFFTChannel", "mpArbInitializePupilFnChannel", "mpArbInitializeSplineChannel",
+           "mpArbNewPeaks", "mpDaoInitialize2DChannel", "mpDaoNewPeaks",
            "mFitAnscombeTransformImage", "mFitGetFitImage", "mFitGetNError",
            "mFitGetPeakPropertyDouble", "mFitGetPeakPropertyInt", "mFitGetResidual",
            "mFitGetUnconverged", "mFitIterateLM", "mFitNewBackground", "mFitNewImage",
