@@ -907,10 +907,12 @@ def run_config_reports(args, pool, cores):
         out["cfg%d" % cfg] = rec
     out["fft"] = run_fft_report(args, pool, cores)
     out["pupil"] = run_fft_report(args, pool, cores, model="pupil")
+    out["multi_plane"] = run_mp_report(args, pool)
     return out
 
 
-FFT_FRAMES = 4
+FFT_FRAMES = 4        # frames of the oracle's CPU sample (and of the parity check)
+FFT_GPU_FRAMES = 16   # frames of the GPU fit
 
 
 def run_fft_report(args, pool, cores, model="fft"):
@@ -920,7 +922,8 @@ def run_fft_report(args, pool, cores, model="fft"):
     engine and the errors against the oracle's fits of the same frames."""
     import torch
     from sa_gb300 import engine, parity, psf_fft_c, pupil_fn, synth
-    wl = synth.fft_workload(frames=FFT_FRAMES) if model == "fft" else synth.pupil_workload(frames=FFT_FRAMES)
+    wl = (synth.fft_workload(frames=FFT_GPU_FRAMES) if model == "fft"
+          else synth.pupil_workload(frames=FFT_GPU_FRAMES))
     F = len(wl["images"])
     shape = (wl["ny"], wl["nx"])
     images = numpy.ascontiguousarray(numpy.stack(wl["images"]).astype(numpy.float32))
@@ -945,12 +948,16 @@ def run_fft_report(args, pool, cores, model="fft"):
         torch.cuda.synchronize()
         ms.append(e0.elapsed_time(e1))
     got = fit.results(props=("x", "y", "z", "height", "background"))
-    units = int(fit.counts().sum())
+    counts = fit.counts()
+    units = int(counts.sum())
     fit.close()
     obj.cleanup()
-    n_cpu, wall_cpu, ora = cpu_sample(wl, F, cores, pool)
-    ref = {k: numpy.concatenate([ora[f][k] for f in range(F)]) for k in ora[0]}
-    st = parity.compare(got, ref)
+    # the oracle fits the first FFT_FRAMES frames (a bounded CPU sample);
+    # parity on those
+    n_cpu, wall_cpu, ora = cpu_sample(wl, FFT_FRAMES, cores, pool)
+    ref = {k: numpy.concatenate([ora[f][k] for f in range(FFT_FRAMES)]) for k in ora[0]}
+    n_s = int(counts[:FFT_FRAMES].sum())
+    st = parity.compare({k: v[:n_s] for k, v in got.items()}, ref)
     if model == "fft":
         psf = wl["fitter"]["psf"]
         what = "FFT PSF model (%dx%dx%d stack)" % psf.shape
@@ -965,6 +972,68 @@ def run_fft_report(args, pool, cores, model="fft"):
             "frac_within": min([st[k] for k in st if k.startswith("frac_ok")] or [1.0]),
             "max_dx": st.get("max_dx"), "max_dy": st.get("max_dy"), "max_dz": st.get("max_dz"),
             "max_rel_height": st.get("max_rel_h"), "max_rel_background": st.get("max_rel_bg")}
+
+
+def _mp_cpu_job(args):
+    """The oracle's multi-plane fit of one frame (spawned worker): returns
+    (seconds, per-plane properties)."""
+    import oracle.oracle as O
+    wl, lib = args
+    O.LIB = os.path.join(ROOT, "oracle", lib)
+    shape = (wl["ny"], wl["nx"])
+    nc = wl["n_channels"]
+    t0 = time.perf_counter()
+    chans = [O.OracleFitter("2d", shape, roi_size=10, sigma_range=(1.0, 3.0), tol=1.0e-6 * nc) for _ in range(nc)]
+    f = O.OracleMPFitter(chans, list(wl["maps"]), kind="dao", independent_heights=1)
+    f.newImage(wl["images"])
+    f.newBackground(wl["backgrounds"])
+    f.newPeaks(wl["peaks"], "finder")
+    f.doFit(MAX_IT)
+    dt = time.perf_counter() - t0
+    props = [{k: f.getPeakProperty(k, c) for k in ("x", "y", "height", "background", "status")} for c in range(nc)]
+    f.cleanup()
+    return dt, props
+
+
+def run_mp_report(args, pool):
+    """Multi-plane fitting (multi_plane/mp_fit.c + mp_fit_dao.c, 2D
+    Gaussians) of one two-plane 256 x 256 frame with 200 emitters through
+    the reference's Python surface (MPFitDao2D: one coupled sweep per
+    iterate()): wall time and localizations/s against the oracle's fit of
+    the same frame on one host core, and the per-plane agreement."""
+    from sa_gb300 import mp_fit_dao_c, synth
+    wl = synth.multiplane_workload()
+    nc = wl["n_channels"]
+    shape = (wl["ny"], wl["nx"])
+    walls = []
+    for rep in range(2):
+        t0 = time.perf_counter()
+        f = mp_fit_dao_c.MPFitDao2D(n_channels=nc, roi_size=10, sigma_range=(1.0, 3.0))
+        for c in range(nc):
+            f.initializeChannel(numpy.ones(shape), numpy.zeros(shape), c)
+        f.setMapping(*wl["maps"])
+        f.setWeights(verbose=False)
+        f.newImage(wl["images"])
+        f.newBackground(wl["backgrounds"])
+        f.newPeaks(wl["peaks"], "finder")
+        f.doFit(MAX_IT)
+        got = [{k: f.getPeakProperty(k, c) for k in ("x", "y", "height", "background", "status")} for c in range(nc)]
+        walls.append(time.perf_counter() - t0)
+        f.cleanup(verbose=False)
+    cpu_s, ref = pool.map(_mp_cpu_job, [(wl, "liboracle_timing.so")])[0]
+    n = int(got[0]["status"].size)
+    agree = min(float((got[c]["status"] == ref[c]["status"]).mean()) for c in range(nc))
+    ok = [(got[c]["status"] == 1) & (ref[c]["status"] == 1) for c in range(nc)]
+    max_dxy = max(float(numpy.abs(got[c][k][ok[c]] - ref[c][k][ok[c]]).max(initial=0.0)) for c in range(nc)
+                  for k in ("x", "y"))
+    return {"workload": "multi-plane 2D Gaussians (MPFitDao2D), %d planes of %dx%d, %d emitters, FP64 engine, "
+                        "one frame through the reference's Python surface" % (nc, shape[1], shape[0], n),
+            "localizations_per_s": n / min(walls), "wall_s": min(walls),
+            "cpu_localizations_per_s": n / cpu_s, "cpu_wall_s": cpu_s, "cpu_cores": 1,
+            "cpu_kind": "port (the oracle's multi-plane restatement, reference compiler flags)",
+            "status_agree": agree, "max_dxy_converged": max_dxy,
+            "note": "a frame's groups run in index order in one warp, as the reference's sweep; frames are the "
+                    "unit of parallelism"}
 
 
 DENSITY_BINS = 6   # log-spaced density bins of the serving stream's frame cache

@@ -458,3 +458,50 @@ def pupil_workload(frames=4, nx=256, ny=256, n_emitters=300, seed=23, background
                                    z=0.5 * z, background=numpy.full(n_emitters, background), height=0.8 * h))
     pfn.cleanup()
     return out
+
+
+def multiplane_workload(n_channels=2, nx=256, ny=256, n_emitters=200, seed=31, background=20.0):
+    """One multi-plane frame of 2D Gaussian emitters: plane 0 as drawn, the
+    other planes through small affine maps (rotation, scale, shift) and
+    wider (defocused) with less signal, Poisson noise; "finder" starting
+    peaks (x, y within 0.4 px of the truth, z 0, sigma 1.5) in plane 0's
+    coordinates.  maps = (xt_0toN, yt_0toN, xt_Nto0, yt_Nto0), 3
+    coefficients per plane."""
+    rng = numpy.random.default_rng(seed)
+    x0N, y0N, xN0, yN0 = [], [], [], []
+    for c in range(n_channels):
+        if c == 0:
+            a, t = numpy.eye(2), numpy.zeros(2)
+        else:
+            th = rng.uniform(-0.01, 0.01)
+            s = 1.0 + rng.uniform(-0.004, 0.004)
+            a = s * numpy.array([[math.cos(th), -math.sin(th)], [math.sin(th), math.cos(th)]])
+            t = rng.uniform(-2.0, 2.0, 2)
+        ai = numpy.linalg.inv(a)
+        ti = -ai @ t
+        x0N += [t[0], a[0, 0], a[0, 1]]
+        y0N += [t[1], a[1, 0], a[1, 1]]
+        xN0 += [ti[0], ai[0, 0], ai[0, 1]]
+        yN0 += [ti[1], ai[1, 0], ai[1, 1]]
+    maps = tuple(numpy.array(v) for v in (x0N, y0N, xN0, yN0))
+    x = rng.uniform(14.0, nx - 14.0, n_emitters)
+    y = rng.uniform(14.0, ny - 14.0, n_emitters)
+    h = rng.uniform(400.0, 1500.0, n_emitters)
+    yy, xx = numpy.mgrid[0:ny, 0:nx]
+    images = []
+    for c in range(n_channels):
+        cx = maps[0][3 * c] + maps[0][3 * c + 1] * x + maps[0][3 * c + 2] * y
+        cy = maps[1][3 * c] + maps[1][3 * c + 1] * x + maps[1][3 * c + 2] * y
+        sig = 1.3 + 0.35 * c
+        img = numpy.full((ny, nx), background)
+        for i in range(n_emitters):
+            x0, x1 = max(0, int(cx[i]) - 8), min(nx, int(cx[i]) + 9)
+            y0, y1 = max(0, int(cy[i]) - 8), min(ny, int(cy[i]) + 9)
+            img[y0:y1, x0:x1] += (h[i] / (1.0 + 0.5 * c)) * numpy.exp(
+                -((xx[y0:y1, x0:x1] - cx[i]) ** 2 + (yy[y0:y1, x0:x1] - cy[i]) ** 2) / (2 * sig * sig))
+        images.append(rng.poisson(img).astype(numpy.float64))
+    peaks = {"x": numpy.round(x) + rng.uniform(-0.4, 0.4, n_emitters),
+             "y": numpy.round(y) + rng.uniform(-0.4, 0.4, n_emitters),
+             "z": numpy.zeros(n_emitters), "sigma": numpy.full(n_emitters, 1.5)}
+    return {"images": images, "backgrounds": [numpy.full((ny, nx), background) for _ in range(n_channels)],
+            "maps": maps, "peaks": peaks, "nx": nx, "ny": ny, "n_channels": n_channels}

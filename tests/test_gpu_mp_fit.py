@@ -120,9 +120,12 @@ def make_arb_case(kind, seed, n_peaks=10, shape=(96, 100), indep=0):
     else:
         objs = [synth.make_spline(seed=3)["coeff"]] * 2
         size = objs[0].shape[0]
-        zs = rng.uniform(0.25 * size, 0.75 * size, n_peaks)
+        zs = numpy.floor(rng.uniform(0.25 * size, 0.75 * size, n_peaks)) + rng.uniform(0.3, 0.6, n_peaks)
         zr = None
         pos_margin = 14
+    # the test spline has small negative lobes: a background that keeps the
+    # model positive
+    bg = 80.0 if kind == "spline" else 15.0
     ny, nx = shape
     x = rng.uniform(pos_margin, nx - pos_margin, n_peaks)
     y = rng.uniform(pos_margin, ny - pos_margin, n_peaks)
@@ -132,14 +135,14 @@ def make_arb_case(kind, seed, n_peaks=10, shape=(96, 100), indep=0):
         cx = maps[0][3 * c] + maps[0][3 * c + 1] * x + maps[0][3 * c + 2] * y
         cy = maps[1][3 * c] + maps[1][3 * c + 1] * x + maps[1][3 * c + 2] * y
         rows = numpy.stack([cx, cy, zs, numpy.zeros(n_peaks), h], axis=1)
-        img = 15.0 + render(kind, objs[c], shape, rows, zr)
+        img = bg + render(kind, objs[c], shape, rows, zr)
         images.append(rng.poisson(numpy.clip(img, 0.0, None)).astype(numpy.float64))
-    bgs = [numpy.full(shape, 15.0) for _ in range(2)]
+    bgs = [numpy.full(shape, bg) for _ in range(2)]
     # spline z starts near the truth (the test spline's z response is not
     # monotonic far from it); the others at 70 % of it
-    z0 = zs + rng.normal(0.0, 0.3, n_peaks) if kind == "spline" else 0.7 * zs
+    z0 = zs + rng.uniform(0.15, 0.35, n_peaks) if kind == "spline" else 0.7 * zs
     peaks = {"x": x + rng.normal(0.0, 0.3, n_peaks), "y": y + rng.normal(0.0, 0.3, n_peaks), "z": z0,
-             "background": numpy.full(n_peaks, 15.0), "height": 0.8 * h}
+             "background": numpy.full(n_peaks, bg), "height": 0.8 * h}
     return objs, maps, images, bgs, peaks, zr
 
 
@@ -198,8 +201,10 @@ def test_mp_arb_matches_oracle(case):
     objs, maps, images, bgs, peaks, zr = make_arb_case(kind, case["seed"], indep=indep)
     shape = images[0].shape
     if ptype != "hdf5":
+        # (spline z off the knots: at a knot the test spline's z gradient can
+        # vanish, a singular Hessian whose solve fails or not by rounding)
         peaks = {"x": numpy.round(peaks["x"]), "y": numpy.round(peaks["y"]),
-                 "z": numpy.full(peaks["x"].size, 0.0 if kind != "spline" else 0.5 * objs[0].shape[0])}
+                 "z": numpy.full(peaks["x"].size, 0.0 if kind != "spline" else 0.5 * objs[0].shape[0] + 0.37)}
     # oracle
     chans = [oracle_channel(kind, o, shape, tol=1.0e-6 * 2, zr=zr) for o in objs]
     ref = oracle.OracleMPFitter(chans, maps, kind="arb", independent_heights=indep)
