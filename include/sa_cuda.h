@@ -288,6 +288,17 @@ void mpDaoInitialize2DChannel(saMPFit *mp_fit, double *rqe, double *variance, do
 /* mp_fit_dao.c:82 mpDaoNewPeaks */
 void mpDaoNewPeaks(saMPFit *mp_fit, double *peak_params, char *p_type, int n_peaks);
 
+/* Batched multi-plane fitting (no reference counterpart): n_frames frames
+ * on every channel (saSetFrames), images with saNewImages /
+ * saNewBackgrounds on each fit_data[i], new peaks of every frame in
+ * channel 0's coordinates (counts[f] rows each, frames one after another;
+ * the frames' images just loaded), then doFit's sweeps for every frame at
+ * once (one warp per frame); results per channel with saGetResultsBatch.
+ * Return 0 (mpDoFitBatch: the number of sweeps) or -1 (saGetLastError). */
+int mpSetFrames(saMPFit *mp_fit, int n_frames, int peaks_capacity);
+int mpNewPeaksBatch(saMPFit *mp_fit, const double *peak_params, const int32_t *counts, const char *p_type);
+int mpDoFitBatch(saMPFit *mp_fit, int max_iterations);
+
 /* ---- shared LM core (sa_library/multi_fit.c) ----------------------------- */
 
 /* multi_fit.c:90 mFitAnscombeTransformImage (ALS only; reports an error) */

@@ -2095,6 +2095,8 @@ struct MPState {
   std::vector<double> w;         // bg, h, x, y, z weights, each [n_weights][nc]
   double* d_w = nullptr;
   MPChan* d_chans = nullptr;
+  int* d_unconv = nullptr;       // RUNNING groups per frame after a batched sweep
+  int unconv_n = 0;
   std::vector<saFitData*> fit;   // the channels (also in saMPFit.fit_data)
 };
 
@@ -2387,8 +2389,114 @@ void mpCleanup(saMPFit* mp) {
     if (h) mp_channel_cleanup(h);
   if (st->d_w) cudaFree(st->d_w);
   if (st->d_chans) cudaFree(st->d_chans);
+  if (st->d_unconv) cudaFree(st->d_unconv);
   delete st;
   free(mp);
+}
+
+// ---- batched multi-plane fitting (no reference counterpart): many frames
+// per channel handle, one warp per frame.  The channels' frames are set with
+// mpSetFrames, their images with saNewImages / saNewBackgrounds on each
+// fit_data[i]; the results are read per channel with saGetResultsBatch /
+// saGetPeakPropertyBatch.
+
+// saSetFrames on every channel.
+int mpSetFrames(saMPFit* mp, int n_frames, int peaks_capacity) {
+  MPState* st = MPS(mp);
+  if (!st) return -1;
+  for (int c = 0; c < mp->n_channels; c++) {
+    if (!st->fit[c]) {
+      set_error("multi-plane channel %d is not initialised", c);
+      return -1;
+    }
+    if (saSetFrames(st->fit[c], n_frames, peaks_capacity)) return -1;
+  }
+  return 0;
+}
+
+// New peaks of every frame (counts[f] rows of the peak format in channel
+// 0's coordinates, frames one after another) into frames whose images
+// were just loaded: mapped into every plane, each channel's new-peak pass,
+// then mpArbNewPeaks' / mpDaoNewPeaks' height and error synchronisation
+// per frame.
+int mpNewPeaksBatch(saMPFit* mp, const double* peaks, const int32_t* counts, const char* p_type) {
+  MPState* st = MPS(mp);
+  if (!st) return -1;
+  const int pt = parse_ptype(p_type);
+  if (pt < 0 || st->kind < 0) {
+    set_error("mpNewPeaksBatch: unknown peak type or no channels");
+    return -1;
+  }
+  const bool arb = st->kind == MP_ARB;
+  const int F = E(st->fit[0])->F;
+  long long total = 0;
+  for (int f = 0; f < F; f++) total += counts[f];
+  const int ncol = (pt == PT_TEXT) ? (arb ? 5 : 7) : (arb ? 3 : 4);
+  std::vector<double> mapped((size_t)ncol * std::max<long long>(total, 1));
+  for (int c = 0; c < mp->n_channels; c++) {
+    const double* rows = peaks;
+    if (c > 0) {
+      for (long long j = 0; j < total; j++) {
+        const double* q = peaks + (size_t)ncol * j;
+        double* o = mapped.data() + (size_t)ncol * j;
+        const double tx = q[0], ty = q[1];
+        for (int k = 0; k < ncol; k++) o[k] = q[k];
+        o[0] = st->xt0N[c * 3] + tx * st->xt0N[c * 3 + 1] + ty * st->xt0N[c * 3 + 2];
+        o[1] = st->yt0N[c * 3] + tx * st->yt0N[c * 3 + 1] + ty * st->yt0N[c * 3 + 2];
+      }
+      rows = mapped.data();
+    }
+    if (saNewPeaksBatch(st->fit[c], rows, counts, F, p_type)) return -1;
+  }
+  MPParams p;
+  int frames = 0;
+  cudaStream_t stream = nullptr;
+  if (mp_prepare(mp, p, frames, stream)) return -1;
+  p.start = 0;
+  p.stop = -1;
+  p.fix_heights = (arb && !mp->independent_heights && pt != PT_TEXT) ? 1 : 0;
+  cudaError_t err = mp_newpeaks(st->d_chans, p, frames, stream);
+  if (err != cudaSuccess) {
+    set_error("mpNewPeaksBatch: %s", cudaGetErrorString(err));
+    return -1;
+  }
+  return mp_finish(mp, stream);
+}
+
+// MultiFitter.doFit (dao_fit_c.py:332-356) for every frame at once: one
+// coupled sweep, then sweeps while any frame has RUNNING groups and fewer
+// than max_iterations were made (a frame without RUNNING groups is left
+// unchanged by a sweep).  Returns the number of sweeps, or -1.
+int mpDoFitBatch(saMPFit* mp, int max_iterations) {
+  MPState* st = MPS(mp);
+  if (!st) return -1;
+  MPParams p;
+  int frames = 0;
+  cudaStream_t stream = nullptr;
+  if (mp_prepare(mp, p, frames, stream)) return -1;
+  if (st->unconv_n < frames) {
+    if (st->d_unconv) cudaFree(st->d_unconv);
+    CK(cudaMalloc(&st->d_unconv, sizeof(int) * frames));
+    st->unconv_n = frames;
+  }
+  p.unconv = st->d_unconv;
+  std::vector<int> un(frames);
+  int sweeps = 0;
+  for (;;) {
+    cudaError_t err = mp_sweep(st->d_chans, p, frames, stream);
+    if (err != cudaSuccess) {
+      set_error("mpDoFitBatch: %s", cudaGetErrorString(err));
+      return -1;
+    }
+    sweeps++;
+    CK(cudaMemcpyAsync(un.data(), st->d_unconv, sizeof(int) * frames, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    long long running = 0;
+    for (int f = 0; f < frames; f++) running += un[f];
+    if (running == 0 || sweeps > max_iterations) break;
+  }
+  if (mp_finish(mp, stream)) return -1;
+  return sweeps;
 }
 
 }  // extern "C"

@@ -18,6 +18,11 @@ namespace sa {
 
 __device__ __forceinline__ long long mp_fbase(const MPChan& c, int f) { return (long long)f * c.fs.npix; }
 
+__device__ __forceinline__ int warp_sum_int(int v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // mFitCalcErr multi_fit.c:111-195 from the global state: the deviance over
 // the ROI; true (and no error) when some fi <= 0.
 __device__ inline bool mp_error(const MPChan& c, long long fbase, const PeakRec& w, double& dev, int lane) {
@@ -440,6 +445,12 @@ __global__ void __launch_bounds__(32) k_mp_sweep(const MPChan* chans, MPParams p
     }
   }
   for (int g = 0; g < nfit; g++) mp_check_error(ch, p, f, g, smem, lane);
+  if (p.unconv) {
+    int n = 0;
+    for (int g = lane; g < nfit; g += 32) n += (ch[0].fs.pk[ch[0].fs.pk_off[f] + g].status == RUNNING);
+    n = warp_sum_int(n);
+    if (lane == 0) p.unconv[f] = n;
+  }
 }
 
 // After the channels' own new-peak passes (mpArbNewPeaks mp_fit_arb.c:180-340,
@@ -456,7 +467,8 @@ __global__ void __launch_bounds__(32) k_mp_newpeaks(const MPChan* chans, MPParam
     reinterpret_cast<int*>(ch)[i] = reinterpret_cast<const int*>(chans)[i];
   __syncwarp();
   const int nc = p.nc;
-  for (int g = p.start; g < p.stop; g++) {
+  const int stop = p.stop < 0 ? ch[0].fs.nfit[f] : p.stop;
+  for (int g = p.start; g < stop; g++) {
     if (p.fix_heights) {
       double height = 0.0;
       for (int c = 0; c < nc; c++) height += ch[c].fs.pk[ch[c].fs.pk_off[f] + g].p[PH];
@@ -486,7 +498,7 @@ __global__ void __launch_bounds__(32) k_mp_newpeaks(const MPChan* chans, MPParam
       }
     }
   }
-  for (int g = p.start; g < p.stop; g++) mp_check_error(ch, p, f, g, smem, lane);
+  for (int g = p.start; g < stop; g++) mp_check_error(ch, p, f, g, smem, lane);
 }
 
 }  // namespace sa

@@ -21,8 +21,9 @@ struct MPParams {
   double xt0N[3 * MP_MAXCH], yt0N[3 * MP_MAXCH], xtN0[3 * MP_MAXCH], ytN0[3 * MP_MAXCH];
   const double* w;   // weights bg, h, x, y, z: 5 x [n_weights][nc] (z the slow index)
   int ws_bytes;      // a channel workspace (the largest of the channels')
-  int start, stop;   // k_mp_newpeaks: the new groups
+  int start, stop;   // k_mp_newpeaks: the new groups (stop < 0: to the frame's last)
   int fix_heights;   // k_mp_newpeaks: give the new groups their channels' mean height
+  int* unconv;       // k_mp_sweep: RUNNING groups per frame after the sweep (may be null)
 };
 
 // Per-frame state in shared memory (lane 0 writes the records).

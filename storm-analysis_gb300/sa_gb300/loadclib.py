@@ -186,6 +186,12 @@ def _declare(lib):
     lib.mpDaoInitialize2DChannel.restype = None
     lib.mpDaoNewPeaks.argtypes = [mpp, f64, cs, ci]
     lib.mpDaoNewPeaks.restype = None
+    lib.mpSetFrames.argtypes = [mpp, ci, ci]
+    lib.mpSetFrames.restype = ci
+    lib.mpNewPeaksBatch.argtypes = [mpp, f64, i32, cs]
+    lib.mpNewPeaksBatch.restype = ci
+    lib.mpDoFitBatch.argtypes = [mpp, ci]
+    lib.mpDoFitBatch.restype = ci
     for name in ["getXSize", "getYSize", "getZSize"]:
         getattr(lib, name).argtypes = [vp]
         getattr(lib, name).restype = ci
@@ -325,7 +331,8 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "pfitInitialize", "pfitNewPeaks", "pfitSetZRange", "pfitCleanup",
            "mpInitialize", "mpCleanup", "mpIterateLM", "mpSetTransforms", "mpSetWeights", "mpSetWeightsIndexing",
            "mpArbInitializePSFFFTChannel", "mpArbInitializePupilFnChannel", "mpArbInitializeSplineChannel",
-           "mpArbNewPeaks", "mpDaoInitialize2DChannel", "mpDaoNewPeaks",
+           "mpArbNewPeaks", "mpDaoInitialize2DChannel", "mpDaoNewPeaks", "mpSetFrames", "mpNewPeaksBatch",
+           "mpDoFitBatch",
            "mFitAnscombeTransformImage", "mFitGetFitImage", "mFitGetNError",
            "mFitGetPeakPropertyDouble", "mFitGetPeakPropertyInt", "mFitGetResidual",
            "mFitGetUnconverged", "mFitIterateLM", "mFitNewBackground", "mFitNewImage",

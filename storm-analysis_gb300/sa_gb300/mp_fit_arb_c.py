@@ -25,6 +25,9 @@ class MPFitArb(mp_fit_c.MPFit):
     def getSize(self):
         return self.psf_objects[0].getSize()
 
+    def formatPeaks(self, peaks, peaks_type):
+        return formatPeaksArbitraryPSF(peaks, peaks_type)
+
     def newPeaks(self, peaks, peaks_type):
         c_peaks = formatPeaksArbitraryPSF(peaks, peaks_type)
         self._clear_error()

@@ -155,6 +155,19 @@ class MPFit(MultiFitter):
     def rescaleZ(self, z):
         return z
 
+    def fitBatch(self, images, backgrounds, peaks, peaks_type, max_iterations=2000):
+        """Batched multi-plane fit of many frames at once (no reference
+        counterpart; the channels must be initialised and the mapping and
+        weights set): images / backgrounds per channel an (F, ny, nx)
+        array, peaks a list of F dicts of columns (channel 0's
+        coordinates).  Returns (per channel a dict of the frames' peaks'
+        x, y, z, height, background, xsigma, ysigma, error, status,
+        iterations, frames one after another; the number of sweeps)."""
+        rows = [self.formatPeaks(p, peaks_type) for p in peaks]
+        counts = [r.shape[0] for r in rows]
+        allrows = numpy.ascontiguousarray(numpy.concatenate(rows, axis=0))
+        return _batch_fit(self, images, backgrounds, allrows, counts, peaks_type, max_iterations)
+
     def setMapping(self, xt_0toN, yt_0toN, xt_Nto0, yt_Nto0):
         self.clib.mpSetTransforms(self.mfit, numpy.ascontiguousarray(xt_0toN, dtype=numpy.float64),
                                   numpy.ascontiguousarray(yt_0toN, dtype=numpy.float64),
@@ -177,6 +190,42 @@ class MPFit(MultiFitter):
         if verbose:
             print("weights z scaling - offset: {0:.3f} scale: {1:.3f}".format(z_offset, z_scale))
         self.clib.mpSetWeightsIndexing(self.mfit, z_offset, z_scale)
+
+
+def _batch_fit(fitter, images, backgrounds, rows, counts, peaks_type, max_iterations):
+    """The batched multi-plane fit behind MPFit.fitBatch."""
+    lib = fitter.clib
+    n_frames = images[0].shape[0]
+    cap = max(1, int(max(counts)))
+    if lib.mpSetFrames(fitter.mfit, n_frames, cap) != 0:
+        raise MultiFitterException("mpSetFrames: " + loadclib.last_error())
+    for c in range(fitter.n_channels):
+        ch = fitter._channel(c)
+        a = numpy.ascontiguousarray(images[c], dtype=numpy.float64)
+        b = numpy.ascontiguousarray(backgrounds[c], dtype=numpy.float64)
+        if lib.saNewImages(ch, a.ctypes.data_as(ctypes.c_void_p), n_frames, 64, 0) != 0:
+            raise MultiFitterException("saNewImages: " + loadclib.last_error())
+        if lib.saNewBackgrounds(ch, b.ctypes.data_as(ctypes.c_void_p), n_frames, 64, 0) != 0:
+            raise MultiFitterException("saNewBackgrounds: " + loadclib.last_error())
+    counts = numpy.ascontiguousarray(counts, dtype=numpy.int32)
+    if lib.mpNewPeaksBatch(fitter.mfit, rows, counts, peaks_type.encode()) != 0:
+        raise MultiFitterException("mpNewPeaksBatch: " + loadclib.last_error())
+    sweeps = lib.mpDoFitBatch(fitter.mfit, int(max_iterations))
+    if sweeps < 0:
+        raise MultiFitterException("mpDoFitBatch: " + loadclib.last_error())
+    out = []
+    n = int(counts.sum())
+    for c in range(fitter.n_channels):
+        vals = numpy.zeros((n, 8), dtype=numpy.float64)
+        ints = numpy.zeros((n, 2), dtype=numpy.int32)
+        if n and lib.saGetResultsBatch(fitter._channel(c), vals, ints) < 0:
+            raise MultiFitterException("saGetResultsBatch: " + loadclib.last_error())
+        d = {k: vals[:, i] for i, k in enumerate(("x", "y", "z", "height", "background", "xsigma", "ysigma",
+                                                     "error"))}
+        d["status"] = ints[:, 0]
+        d["iterations"] = ints[:, 1]
+        out.append(d)
+    return out, sweeps
 
 
 def equal_weights(n_channels):

@@ -21,6 +21,9 @@ class MPFitDao(mp_fit_c.MPFit):
         self.roi_size = roi_size
         self.sigma_range = sigma_range
 
+    def formatPeaks(self, peaks, peaks_type):
+        return formatPeaksGaussianPSF(peaks, peaks_type)
+
     def newPeaks(self, peaks, peaks_type):
         c_peaks = formatPeaksGaussianPSF(peaks, peaks_type)
         self._clear_error()

@@ -250,3 +250,45 @@ def test_mp_arb_matches_oracle(case):
         for p in psfs:
             if hasattr(p, "cleanup"):
                 p.cleanup()
+
+
+def test_mp_batch_equals_single_frames():
+    """mpSetFrames / mpNewPeaksBatch / mpDoFitBatch on three frames give
+    every frame's results bit for bit as the one-frame calls do."""
+    from sa_gb300 import mp_fit_dao_c, synth
+    wls = [synth.multiplane_workload(nx=96, ny=104, n_emitters=25, seed=s) for s in (41, 42, 43)]
+    shape = (wls[0]["ny"], wls[0]["nx"])
+    nc = wls[0]["n_channels"]
+    maps = wls[0]["maps"]
+
+    def make():
+        f = mp_fit_dao_c.MPFitDao2D(n_channels=nc, roi_size=10, sigma_range=(1.0, 3.0))
+        for c in range(nc):
+            f.initializeChannel(numpy.ones(shape), numpy.zeros(shape), c)
+        f.setMapping(*maps)
+        f.setWeights(verbose=False)
+        return f
+
+    single = []
+    for wl in wls:
+        f = make()
+        f.newImage(wl["images"])
+        f.newBackground(wl["backgrounds"])
+        f.newPeaks(wl["peaks"], "finder")
+        f.doFit(200)
+        single.append([{k: f.getPeakProperty(k, c) for k in ("x", "y", "height", "background", "xsigma", "status",
+                                                             "iterations")} for c in range(nc)])
+        f.cleanup(verbose=False)
+    f = make()
+    images = [numpy.stack([wl["images"][c] for wl in wls]) for c in range(nc)]
+    bgs = [numpy.stack([wl["backgrounds"][c] for wl in wls]) for c in range(nc)]
+    out, sweeps = f.fitBatch(images, bgs, [wl["peaks"] for wl in wls], "finder", max_iterations=200)
+    f.cleanup(verbose=False)
+    assert sweeps >= 1
+    for c in range(nc):
+        o = 0
+        for fr, wl in enumerate(wls):
+            n = single[fr][c]["x"].size
+            for k in ("x", "y", "height", "background", "xsigma", "status", "iterations"):
+                assert numpy.array_equal(out[c][k][o:o + n], single[fr][c][k]), (c, fr, k)
+            o += n
