@@ -478,6 +478,100 @@ __device__ inline int solve_fp64_lane0(const double* jh, int k, double lam, doub
   return info;
 }
 
+// solve_fp64_lane0 with one row per lane (all lanes call it): every element
+// of the factor and of the solution is computed with chol_solve's
+// operations in chol_solve's order -- lane i forms row i of L and, in turn,
+// b[i]; the back substitution's products are formed on the lanes that hold
+// them and subtracted in order -- so the result is chol_solve's to the bit,
+// with O(k^2) instead of O(k^3) instructions on a single lane (each FP64
+// instruction occupies the pipe for the whole warp however few lanes run).
+// Returns the solver status on every lane; out[0..k) on every lane.
+__device__ inline int solve_fp64_warp(const double* jh, int k, double lam, double* out, int lane) {
+  const unsigned full = 0xffffffffu;
+  double ac[MAX_JAC], L[MAX_JAC];
+#pragma unroll
+  for (int j = 0; j < MAX_JAC; j++) {
+    ac[j] = 0.0;
+    L[j] = 0.0;
+    if (lane < k && j < k && j <= lane) {
+      const int id = k + j * k - (j * (j - 1)) / 2 + (lane - j);
+      ac[j] = (j == lane) ? (1.0 + lam) * jh[id] : jh[id];
+    }
+  }
+  int info = 0;
+#pragma unroll
+  for (int j = 0; j < MAX_JAC; j++) {
+    if (j < k && info == 0) {
+      double Lj[MAX_JAC];
+#pragma unroll
+      for (int m = 0; m < MAX_JAC; m++) Lj[m] = (m < j) ? __shfl_sync(full, L[m], j) : 0.0;
+      double d = ac[j];
+#pragma unroll
+      for (int m = 0; m < MAX_JAC; m++)
+        if (m < j) d = __dsub_rn(d, __dmul_rn(L[m], L[m]));
+      d = __shfl_sync(full, d, j);
+      if (!(d > 0.0)) {
+        info = j + 1;
+      } else {
+        d = sqrt(d);
+        if (lane == j) L[j] = d;
+        if (lane > j && lane < k) {
+          double sum = ac[j];
+#pragma unroll
+          for (int m = 0; m < MAX_JAC; m++)
+            if (m < j) sum = __dsub_rn(sum, __dmul_rn(L[m], Lj[m]));
+          L[j] = sum / d;
+        }
+      }
+    }
+  }
+  if (info != 0) return info;
+  // forward substitution: lane i in turn, b[i] broadcast as it is found
+  const double bl = lane < k ? jh[lane] : 0.0;
+  double bb[MAX_JAC];
+#pragma unroll
+  for (int i = 0; i < MAX_JAC; i++) {
+    bb[i] = 0.0;
+    if (i < k) {
+      double v = 0.0;
+      if (lane == i) {
+        double sum = bl;
+#pragma unroll
+        for (int m = 0; m < MAX_JAC; m++)
+          if (m < i) sum = __dsub_rn(sum, __dmul_rn(L[m], bb[m]));
+        v = sum / L[i];
+      }
+      bb[i] = __shfl_sync(full, v, i);
+    }
+  }
+  // back substitution: the products L[m][i] x[m] formed on lane m
+  double xs[MAX_JAC];
+#pragma unroll
+  for (int i = 0; i < MAX_JAC; i++) xs[i] = 0.0;
+#pragma unroll
+  for (int i = MAX_JAC - 1; i >= 0; i--) {
+    if (i < k) {
+      double sum = bb[i];
+#pragma unroll
+      for (int m = 0; m < MAX_JAC; m++) {
+        if (m > i && m < k) {
+          const double pr = __shfl_sync(full, __dmul_rn(L[i], xs[m]), m);
+          sum = __dsub_rn(sum, pr);
+        }
+      }
+      xs[i] = sum / __shfl_sync(full, L[i], i);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < MAX_JAC; i++) {
+    if (i < k) {
+      out[i] = xs[i];
+      if (isnan(xs[i])) info = 1;
+    }
+  }
+  return info;
+}
+
 // ---------------------------------------------------------------------------
 // MLE per-pixel deviance 2((f - x) - x log(f/x))  (multi_fit.c:174)
 // ---------------------------------------------------------------------------
@@ -1740,9 +1834,7 @@ __device__ __forceinline__ void psf_and_delta(const ModelCfg& cfg, const T* aij,
 
 template <typename T>
 __device__ inline int solve_damped(WarpWS<T>& ws, int k, double lam, double* out, int lane) {
-  int info = 0;
-  if (lane == 0) info = solve_fp64_lane0(ws.jh, k, lam, out);
-  return info;
+  return solve_fp64_warp(ws.jh, k, lam, out, lane);
 }
 
 // Forward and back substitution with the factors held in r (multipliers

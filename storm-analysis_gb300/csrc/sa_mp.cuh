@@ -246,206 +246,249 @@ __device__ inline void mp_check_error(const MPChan* ch, const MPParams& p, int f
 
 enum { MPA_EVAL = 0, MPA_CONTINUE = 1, MPA_BREAK = 2 };
 
+// Per-frame coupling state of k_mp_sweep beyond MPShared (thread 0 writes).
+struct MPCtl {
+  double e[MP_MAXCH];   // the planes' errors of the latest evaluation
+  int fail[MP_MAXCH];   // the planes' fi <= 0 flags of that evaluation
+  int act, undo, run;
+};
+
 // mpIterateLM mp_fit.c:183-478 for frame blockIdx.x, then mFitRecenterPeaks
-// per channel and mpCheckError per group.
-__global__ void __launch_bounds__(32) k_mp_sweep(const MPChan* chans, MPParams p) {
+// per channel and mpCheckError per group.  One warp per plane (blockDim.x =
+// 32 * nc): each warp does its plane's error, Jacobian, solve, adds and
+// subtractions; thread 0 does the coupled update and the decisions.
+__global__ void __launch_bounds__(32 * MP_MAXCH) k_mp_sweep(const MPChan* chans, MPParams p) {
   extern __shared__ __align__(16) char smem[];
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
   const int f = blockIdx.x;
-  MPChan* ch = reinterpret_cast<MPChan*>(smem + p.ws_bytes + ((sizeof(MPShared) + 15) & ~(size_t)15));
-  for (int i = lane; i < (int)(p.nc * sizeof(MPChan) / 4); i += 32)
-    reinterpret_cast<int*>(ch)[i] = reinterpret_cast<const int*>(chans)[i];
-  __syncwarp();
-  MPShared& S = *reinterpret_cast<MPShared*>(smem + p.ws_bytes);
   const int nc = p.nc;
-  const int nfit = ch[0].fs.nfit[f];
+  char* const ws_c = smem + (size_t)c * p.ws_bytes;
+  MPShared& S = *reinterpret_cast<MPShared*>(smem + (size_t)nc * p.ws_bytes);
+  MPCtl& K = *reinterpret_cast<MPCtl*>(smem + (size_t)nc * p.ws_bytes + ((sizeof(MPShared) + 15) & ~(size_t)15));
+  MPChan* ch = reinterpret_cast<MPChan*>(smem + (size_t)nc * p.ws_bytes + ((sizeof(MPShared) + 15) & ~(size_t)15) +
+                                         ((sizeof(MPCtl) + 15) & ~(size_t)15));
+  for (int i = threadIdx.x; i < (int)(nc * sizeof(MPChan) / 4); i += blockDim.x)
+    reinterpret_cast<int*>(ch)[i] = reinterpret_cast<const int*>(chans)[i];
   // relative heights: 1 for fixed heights (mpSetWeights mp_fit.c:589-591);
   // independent and Gaussian updates set them before use
-  if (lane < MP_MAXCH) S.heights[lane] = 1.0;
-  __syncwarp();
+  if (threadIdx.x < MP_MAXCH) S.heights[threadIdx.x] = 1.0;
+  __syncthreads();
+  const MPChan& C = ch[c];
+  const long long fb = mp_fbase(C, f);
+  WarpWS<double> wc = warp_ws<double>(ws_c, C.cfg, 0);
+  const int nfit = ch[0].fs.nfit[f];
   for (int g = 0; g < nfit; g++) {
-    if (ch[0].fs.pk[ch[0].fs.pk_off[f] + g].status != RUNNING) continue;
-    double e0 = 0.0;
-    for (int c = 0; c < nc; c++) {
-      const long long fb = mp_fbase(ch[c], f);
+    if (threadIdx.x == 0) K.run = (ch[0].fs.pk[ch[0].fs.pk_off[f] + g].status == RUNNING);
+    __syncthreads();
+    if (!K.run) {
+      __syncthreads();
+      continue;
+    }
+    {
       PeakRec r;
-      load_rec(ch[c].fs.pk + ch[c].fs.pk_off[f] + g, r);
+      load_rec(C.fs.pk + C.fs.pk_off[f] + g, r);
       double dev;
-      const bool fail = mp_error(ch[c], fb, r, dev, lane);
+      const bool fail = mp_error(C, fb, r, dev, lane);
       if (lane == 0) S.orig[c] = r;   // the stored peak (mpResetWorkingPeaks restores it)
       if (!fail) r.error = dev;       // the return value is ignored (mp_fit.c:220)
-      else if (lane == 0) ch[c].fs.ctl[f].ctr[C_NEGFI]++;
-      e0 += r.error;
-      if (lane == 0) S.w[c] = r;
-      __syncwarp();
-      WarpWS<double> wc = warp_ws<double>(smem, ch[c].cfg, 0);
-      mp_jh(ch[c], fb, r, wc, S.jh[c], lane);
-      mp_add(ch[c], fb, r, wc, -1, lane);
-      if (lane == 0) S.w[c].added -= 1;
-      __syncwarp();
+      else if (lane == 0) C.fs.ctl[f].ctr[C_NEGFI]++;
+      if (lane == 0) {
+        S.orig_e[c] = r.error;        // the plane's part of the starting error
+        r.added -= 1;
+        S.w[c] = r;
+      }
+      mp_jh(C, fb, r, wc, S.jh[c], lane);
+      mp_add(C, fb, r, wc, -1, lane);
     }
+    __syncthreads();
     for (;;) {
-      int act = MPA_EVAL;
-      if (lane == 0) {
+      __syncthreads();   // every thread has read the previous pass's decisions
+      // lambda bound, the planes' solves (lane 0 of each warp), the update
+      if (threadIdx.x == 0) {
+        K.act = MPA_EVAL;
         if (S.w[0].lambda > LAMBDA_MAX) {
-          for (int c = 0; c < nc; c++) {
-            ch[c].fs.ctl[f].ctr[C_LOST]++;
-            S.w[c].status = ERROR;
+          for (int i = 0; i < nc; i++) {
+            ch[i].fs.ctl[f].ctr[C_LOST]++;
+            S.w[i].status = ERROR;
           }
-          act = MPA_BREAK;
+          K.act = MPA_BREAK;
         } else {
-          for (int c = 0; c < nc; c++) S.w[c].status = RUNNING;
-          bool bad = false;
-          for (int c = 0; c < nc; c++) {
-            S.w[c].iterations++;
-            ch[c].fs.ctl[f].ctr[C_ITER]++;
-            if (solve_fp64_lane0(S.jh[c], ch[c].cfg.jac, S.w[c].lambda, S.dl[c]) != 0) {
-              ch[c].fs.ctl[f].ctr[C_DPOSV]++;
-              bad = true;
-              break;
-            }
-          }
-          if (bad) {
-            for (int c = 0; c < nc; c++) {
-              S.w[c].status = ERROR;
-              S.w[c].lambda = S.w[c].lambda * LAMBDA_UP;
-            }
-            act = MPA_CONTINUE;
-          } else {
-            mp_update(ch, p, S, f);
-            for (int c = 0; c < nc; c++)
-              if (mp_check(ch[c], f, S.w[c])) bad = true;
-            if (bad) {
-              // mpResetWorkingPeaks mp_fit.c:500-521
-              for (int c = 0; c < nc; c++) {
-                const int added = S.w[c].added;
-                const double lam = S.w[c].lambda;
-                S.w[c] = S.orig[c];
-                S.w[c].added = added;
-                S.w[c].lambda = lam * LAMBDA_UP;
-                S.w[c].status = ERROR;
-              }
-              act = MPA_CONTINUE;
-            }
-          }
+          for (int i = 0; i < nc; i++) S.w[i].status = RUNNING;
         }
       }
-      act = __shfl_sync(0xffffffffu, act, 0);
-      __syncwarp();
-      if (act == MPA_BREAK) break;
-      if (act == MPA_CONTINUE) continue;
-      // add the trial peaks, their error (mp_fit.c:340-378)
-      double e1 = 0.0;
-      bool bad = false;
-      for (int c = 0; c < nc; c++) {
-        WarpWS<double> wc = warp_ws<double>(smem, ch[c].cfg, 0);
-        const PeakRec r = S.w[c];
-        mp_add(ch[c], mp_fbase(ch[c], f), r, wc, +1, lane);
-        if (lane == 0) S.w[c].added += 1;
-        __syncwarp();
-      }
-      for (int c = 0; c < nc; c++) {
-        double dev;
-        const bool fail = mp_error(ch[c], mp_fbase(ch[c], f), S.w[c], dev, lane);
-        if (fail) {
-          bad = true;
-          if (lane == 0) ch[c].fs.ctl[f].ctr[C_NEGFI]++;
-        } else {
-          e1 += dev;
-          if (lane == 0) S.w[c].error = dev;
+      __syncthreads();
+      if (K.act == MPA_BREAK) break;
+      {
+        // mp_fit.c:262-300: every plane counts the pass; the first failing
+        // solve ends the planes' loop (later planes neither solve nor count)
+        double dl[MAX_JAC];
+        const int info = solve_fp64_warp(S.jh[c], C.cfg.jac, S.w[c].lambda, dl, lane);
+        if (lane == 0) {
+          K.fail[c] = info;
+          for (int m = 0; m < C.cfg.jac; m++) S.dl[c][m] = dl[m];
         }
-        __syncwarp();
       }
-      int undo = 0;
-      if (lane == 0) {
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        bool bad = false;
+        for (int i = 0; i < nc; i++) {
+          S.w[i].iterations++;
+          ch[i].fs.ctl[f].ctr[C_ITER]++;
+          if (K.fail[i] != 0) {
+            ch[i].fs.ctl[f].ctr[C_DPOSV]++;
+            bad = true;
+            break;
+          }
+        }
         if (bad) {
-          undo = 1;
-          act = MPA_CONTINUE;
+          for (int i = 0; i < nc; i++) {
+            S.w[i].status = ERROR;
+            S.w[i].lambda = S.w[i].lambda * LAMBDA_UP;
+          }
+          K.act = MPA_CONTINUE;
+        } else {
+          mp_update(ch, p, S, f);
+          for (int i = 0; i < nc; i++)
+            if (mp_check(ch[i], f, S.w[i])) bad = true;
+          if (bad) {
+            // mpResetWorkingPeaks mp_fit.c:500-521
+            for (int i = 0; i < nc; i++) {
+              const int added = S.w[i].added;
+              const double lam = S.w[i].lambda;
+              S.w[i] = S.orig[i];
+              S.w[i].added = added;
+              S.w[i].lambda = lam * LAMBDA_UP;
+              S.w[i].status = ERROR;
+            }
+            K.act = MPA_CONTINUE;
+          }
+        }
+      }
+      __syncthreads();
+      if (K.act == MPA_CONTINUE) continue;
+      // add the trial peaks, their errors (mp_fit.c:340-378)
+      {
+        const PeakRec r = S.w[c];
+        mp_add(C, fb, r, wc, +1, lane);
+        double dev;
+        const bool fail = mp_error(C, fb, r, dev, lane);
+        if (lane == 0) {
+          S.w[c].added += 1;
+          K.fail[c] = fail;
+          K.e[c] = dev;
+          if (fail) C.fs.ctl[f].ctr[C_NEGFI]++;
+          else S.w[c].error = dev;
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double e0 = 0.0, e1 = 0.0;
+        bool bad = false;
+        for (int i = 0; i < nc; i++) {
+          e0 += S.orig_e[i];
+          if (K.fail[i]) bad = true;
+          else e1 += K.e[i];
+        }
+        K.undo = 0;
+        if (bad) {
+          K.undo = 1;
+          K.act = MPA_CONTINUE;
         } else if (e1 > e0) {
           if (((e1 - e0) / e0) < p.tol) {
-            for (int c = 0; c < nc; c++) S.w[c].status = CONVERGED;
-            act = MPA_BREAK;
+            for (int i = 0; i < nc; i++) S.w[i].status = CONVERGED;
+            K.act = MPA_BREAK;
           } else {
-            for (int c = 0; c < nc; c++) ch[c].fs.ctl[f].ctr[C_NONDECR]++;
-            undo = 1;
-            act = MPA_CONTINUE;
+            for (int i = 0; i < nc; i++) ch[i].fs.ctl[f].ctr[C_NONDECR]++;
+            K.undo = 1;
+            K.act = MPA_CONTINUE;
           }
         } else {
           if (((e0 - e1) / e0) < p.tol) {
-            for (int c = 0; c < nc; c++) S.w[c].status = CONVERGED;
+            for (int i = 0; i < nc; i++) S.w[i].status = CONVERGED;
           } else if (S.w[0].lambda > LAMBDA_MIN) {
-            for (int c = 0; c < nc; c++) S.w[c].lambda = S.w[c].lambda * LAMBDA_DOWN;
+            for (int i = 0; i < nc; i++) S.w[i].lambda = S.w[i].lambda * LAMBDA_DOWN;
           }
-          act = MPA_BREAK;
+          K.act = MPA_BREAK;
         }
       }
-      undo = __shfl_sync(0xffffffffu, undo, 0);
-      act = __shfl_sync(0xffffffffu, act, 0);
-      __syncwarp();
-      if (undo) {
-        for (int c = 0; c < nc; c++) {
-          WarpWS<double> wc = warp_ws<double>(smem, ch[c].cfg, 0);
-          const PeakRec r = S.w[c];
-          mp_add(ch[c], mp_fbase(ch[c], f), r, wc, -1, lane);
-        }
-        if (lane == 0) {
-          for (int c = 0; c < nc; c++) {
-            const int added = S.w[c].added - 1;
-            const double lam = S.w[c].lambda;
-            S.w[c] = S.orig[c];
-            S.w[c].added = added;
-            S.w[c].lambda = lam * LAMBDA_UP;
-            S.w[c].status = ERROR;
+      __syncthreads();
+      if (K.undo) {
+        const PeakRec r = S.w[c];
+        mp_add(C, fb, r, wc, -1, lane);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          for (int i = 0; i < nc; i++) {
+            const int added = S.w[i].added - 1;
+            const double lam = S.w[i].lambda;
+            S.w[i] = S.orig[i];
+            S.w[i].added = added;
+            S.w[i].lambda = lam * LAMBDA_UP;
+            S.w[i].status = ERROR;
           }
         }
-        __syncwarp();
       }
-      if (act == MPA_BREAK) break;
+      __syncthreads();
+      if (K.act == MPA_BREAK) break;
     }
     // mpCopyFromWorking mp_fit.c:124-134: channel 0's status for all
-    __syncwarp();
     if (lane == 0) {
-      for (int c = 0; c < nc; c++) {
-        S.w[c].status = S.w[0].status;
-        ch[c].fs.pk[ch[c].fs.pk_off[f] + g] = S.w[c];
+      PeakRec r = S.w[c];
+      r.status = S.w[0].status;
+      C.fs.pk[C.fs.pk_off[f] + g] = r;
+    }
+    __syncthreads();
+  }
+  // mFitRecenterPeaks multi_fit.c:1644-1690, each warp its plane
+  for (int g = 0; g < nfit; g++) {
+    PeakRec* q = C.fs.pk + C.fs.pk_off[f] + g;
+    PeakRec r;
+    load_rec(q, r);
+    if (r.status != RUNNING) continue;
+    const double dx = r.p[PX] - r.xi, dy = r.p[PY] - r.yi;
+    if (!((dx < -0.25) || (dx > 1.25) || (dy < -0.25) || (dy > 1.25))) continue;
+    mp_add(C, fb, r, wc, -1, lane);
+    r.added -= 1;
+    r.xi = (int)floor(r.p[PX]);
+    r.yi = (int)floor(r.p[PY]);
+    const int chk = base_check(C.cfg, r);
+    if (chk) {
+      if (lane == 0) {
+        C.fs.ctl[f].ctr[C_LOST]++;
+        C.fs.ctl[f].ctr[chk == 1 ? C_MARGIN : C_NEGH]++;
       }
+      r.status = ERROR;
+    } else {
+      mp_add(C, fb, r, wc, +1, lane);
+      r.added += 1;
     }
     __syncwarp();
+    if (lane == 0) *q = r;
+    __syncwarp();
   }
-  __threadfence_block();
-  // mFitRecenterPeaks multi_fit.c:1644-1690, per channel
-  for (int c = 0; c < nc; c++) {
-    const long long fb = mp_fbase(ch[c], f);
-    WarpWS<double> wc = warp_ws<double>(smem, ch[c].cfg, 0);
-    for (int g = 0; g < nfit; g++) {
-      PeakRec* q = ch[c].fs.pk + ch[c].fs.pk_off[f] + g;
+  __syncthreads();
+  // mpCheckError mp_fit.c:43-68 for every group, each warp its plane
+  for (int g = 0; g < nfit; g++) {
+    if (threadIdx.x == 0) {
+      bool bad = false;
+      for (int i = 0; i < nc; i++) bad |= (ch[i].fs.pk[ch[i].fs.pk_off[f] + g].status == ERROR);
+      K.run = bad;
+    }
+    __syncthreads();
+    if (K.run) {
+      PeakRec* q = C.fs.pk + C.fs.pk_off[f] + g;
       PeakRec r;
       load_rec(q, r);
-      if (r.status != RUNNING) continue;
-      const double dx = r.p[PX] - r.xi, dy = r.p[PY] - r.yi;
-      if (!((dx < -0.25) || (dx > 1.25) || (dy < -0.25) || (dy > 1.25))) continue;
-      mp_add(ch[c], fb, r, wc, -1, lane);
-      r.added -= 1;
-      r.xi = (int)floor(r.p[PX]);
-      r.yi = (int)floor(r.p[PY]);
-      const int chk = base_check(ch[c].cfg, r);
-      if (chk) {
-        if (lane == 0) {
-          ch[c].fs.ctl[f].ctr[C_LOST]++;
-          ch[c].fs.ctl[f].ctr[chk == 1 ? C_MARGIN : C_NEGH]++;
-        }
-        r.status = ERROR;
-      } else {
-        mp_add(ch[c], fb, r, wc, +1, lane);
-        r.added += 1;
+      if (r.status != ERROR) {
+        mp_add(C, fb, r, wc, -1, lane);
+        r.added -= 1;
       }
+      r.status = ERROR;
       __syncwarp();
       if (lane == 0) *q = r;
-      __syncwarp();
     }
+    __syncthreads();
   }
-  for (int g = 0; g < nfit; g++) mp_check_error(ch, p, f, g, smem, lane);
-  if (p.unconv) {
+  if (p.unconv && c == 0) {
     int n = 0;
     for (int g = lane; g < nfit; g += 32) n += (ch[0].fs.pk[ch[0].fs.pk_off[f] + g].status == RUNNING);
     n = warp_sum_int(n);

@@ -33,6 +33,7 @@ struct MPShared {
   double jh[MP_MAXCH][36];   // gradient (k) and packed upper Hessian per channel
   double dl[MP_MAXCH][8];    // the channels' LM steps
   double heights[MP_MAXCH];
+  double orig_e[MP_MAXCH];   // the planes' starting errors of the group
 };
 
 }  // namespace sa
