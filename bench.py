@@ -995,7 +995,7 @@ def _mp_cpu_job(args):
     return dt, props
 
 
-MP_FRAMES = 256       # frames of the batched multi-plane fit
+MP_FRAMES = 1024      # frames of the batched multi-plane fit
 MP_CPU_FRAMES = 32    # frames of its CPU sample
 
 
