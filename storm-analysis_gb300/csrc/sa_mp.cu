@@ -4,7 +4,7 @@
 
 namespace sa {
 
-int mp_ws_bytes(const ModelCfg& cfg) { return (int)warp_ws_bytes<double>(cfg, 0); }
+int mp_ws_bytes(const ModelCfg& cfg) { return (int)warp_ws_bytes<double>(cfg, cfg.nroi); }
 
 static size_t al16(size_t b) { return (b + 15) & ~(size_t)15; }
 

@@ -43,8 +43,8 @@ __device__ inline bool mp_error(const MPChan& c, long long fbase, const PeakRec&
 
 // fn_calc_JH on the global state with the peak still added (the fi of the
 // preceding mFitCalcErr): gradient and packed upper Hessian into jh.
-__device__ inline void mp_jh(const MPChan& c, long long fbase, const PeakRec& w, WarpWS<double>& ws, double* jh,
-                             int lane) {
+__device__ inline SplinePos mp_jh(const MPChan& c, long long fbase, const PeakRec& w, WarpWS<double>& ws,
+                                  double* jh, int lane) {
   const ModelCfg& cfg = c.cfg;
   const int k = cfg.jac;
   SplinePos s = shape_tables(cfg, w, ws, lane);
@@ -81,6 +81,77 @@ __device__ inline void mp_jh(const MPChan& c, long long fbase, const PeakRec& w,
   }
   const double v = warp_transpose_sum32(acc, lane);
   if (lane < k + k * (k + 1) / 2) jh[lane] = v;
+  __syncwarp();
+  return s;
+}
+
+// Subtract the peak (its shape tables current in ws) from the plane's image
+// and keep the base state of its ROI -- the fit image and background
+// without it, rqe, data, count with it -- in the workspace, as lm_step's
+// first loop does: the trials are then evaluated from the workspace.
+__device__ inline void mp_sub_base(const MPChan& c, long long fbase, const PeakRec& w, const SplinePos& s,
+                                   WarpWS<double>& ws, int lane) {
+  const ModelCfg& cfg = c.cfg;
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(ws.roi, p, rx, ry);
+    const long long kk = pix_index(cfg, w.xi, w.yi, rx, ry);
+    const Q2 Fq = acc_load<2>(c.fs.f, fbase + kk);
+    const Q2 Bq = acc_load<2>(c.fs.bg, fbase + kk);
+    const int Cg = __ldcg(c.fs.cnt + fbase + kk);
+    const double rq = __ldg(c.fs.rqe + kk), sc = __ldg(c.fs.scmos + kk);
+    const double psf = psf_at(cfg, c.fs.aij, ws, s, rx, ry);
+    const Q2 cf = quant_t<double>(contrib_f(w.p[PH], psf, rq));
+    const Q2 cb = quant_t<double>(contrib_bg(w.p[PBG], rq, sc));
+    acc_red<2>(c.fs.f, fbase + kk, cf, -1);
+    acc_red<2>(c.fs.bg, fbase + kk, cb, -1);
+    atomicAdd(c.fs.cnt + fbase + kk, -1);
+    ws.Fb[p] = acc_value<2>(q_sub(Fq, cf));
+    ws.Bs[p] = acc_value<2>(q_sub(Bq, cb)) + sc;
+    ws.R[p] = rq;
+    ws.X[p] = __ldg(c.fs.x + fbase + kk);
+    ws.IC[p] = ic_store<double>(Cg);
+  }
+  __syncwarp();
+}
+
+// The error of the trial w from the base state in ws (the peak added
+// virtually; mp_fit.c:340-378 adds it and runs mFitCalcErr): true when some
+// fi <= 0.  The shape goes to ws.psf for the final add.
+__device__ inline bool mp_trial_error(const MPChan& c, const PeakRec& w, WarpWS<double>& ws, double& dev,
+                                      int lane) {
+  const ModelCfg& cfg = c.cfg;
+  SplinePos s = shape_tables(cfg, w, ws, lane, false);
+  const double hh = w.p[PH], bgv = w.p[PBG];
+  double d = 0.0;
+  bool fail = false;
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(ws.roi, p, rx, ry);
+    const double psf = psf_at(cfg, c.fs.aij, ws, s, rx, ry);
+    ws.psf[p] = psf;
+    const double rq = ws.R[p];
+    const double fi = ws.Fb[p] + contrib_f(hh, psf, rq) + bg_div(ws.Bs[p] + bgv * rq, ws.IC[p]);
+    if (!(fi > 0.0)) fail = true;
+    else d += deviance(fi, ws.X[p]);
+  }
+  dev = warp_sum(d);
+  return __any_sync(0xffffffffu, fail);
+}
+
+// Add the accepted trial w (its shape in ws.psf) to the plane's image.
+__device__ inline void mp_add_from_ws(const MPChan& c, long long fbase, const PeakRec& w, WarpWS<double>& ws,
+                                      int lane) {
+  const ModelCfg& cfg = c.cfg;
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(ws.roi, p, rx, ry);
+    const long long kk = pix_index(cfg, w.xi, w.yi, rx, ry);
+    const double rq = ws.R[p], sc = __ldg(c.fs.scmos + kk);
+    acc_red<2>(c.fs.f, fbase + kk, quant_t<double>(contrib_f(w.p[PH], ws.psf[p], rq)), +1);
+    acc_red<2>(c.fs.bg, fbase + kk, quant_t<double>(contrib_bg(w.p[PBG], rq, sc)), +1);
+    atomicAdd(c.fs.cnt + fbase + kk, 1);
+  }
   __syncwarp();
 }
 
@@ -275,8 +346,10 @@ __global__ void __launch_bounds__(32 * MP_MAXCH) k_mp_sweep(const MPChan* chans,
   __syncthreads();
   const MPChan& C = ch[c];
   const long long fb = mp_fbase(C, f);
-  WarpWS<double> wc = warp_ws<double>(ws_c, C.cfg, 0);
+  WarpWS<double> wc = warp_ws<double>(ws_c, C.cfg, C.cfg.nroi);
+  wc.roi = C.fs.roi_xy;
   const int nfit = ch[0].fs.nfit[f];
+  int cax = 0, cay = 0;   // anchor of this plane's base arrays
   for (int g = 0; g < nfit; g++) {
     if (threadIdx.x == 0) K.run = (ch[0].fs.pk[ch[0].fs.pk_off[f] + g].status == RUNNING);
     __syncthreads();
@@ -297,8 +370,10 @@ __global__ void __launch_bounds__(32 * MP_MAXCH) k_mp_sweep(const MPChan* chans,
         r.added -= 1;
         S.w[c] = r;
       }
-      mp_jh(C, fb, r, wc, S.jh[c], lane);
-      mp_add(C, fb, r, wc, -1, lane);
+      const SplinePos sp = mp_jh(C, fb, r, wc, S.jh[c], lane);
+      mp_sub_base(C, fb, r, sp, wc, lane);
+      cax = r.xi;
+      cay = r.yi;
     }
     __syncthreads();
     for (;;) {
@@ -366,12 +441,19 @@ __global__ void __launch_bounds__(32 * MP_MAXCH) k_mp_sweep(const MPChan* chans,
       }
       __syncthreads();
       if (K.act == MPA_CONTINUE) continue;
-      // add the trial peaks, their errors (mp_fit.c:340-378)
+      // add the trial peaks, their errors (mp_fit.c:340-378), evaluated
+      // from the base state (reloaded where the ROI moved)
       {
         const PeakRec r = S.w[c];
-        mp_add(C, fb, r, wc, +1, lane);
+        if (r.xi != cax || r.yi != cay) {
+          __threadfence();
+          load_base(C.cfg, C.fs, fb, r.xi, r.yi, wc, lane);
+          __syncwarp();
+          cax = r.xi;
+          cay = r.yi;
+        }
         double dev;
-        const bool fail = mp_error(C, fb, r, dev, lane);
+        const bool fail = mp_trial_error(C, r, wc, dev, lane);
         if (lane == 0) {
           S.w[c].added += 1;
           K.fail[c] = fail;
@@ -413,9 +495,7 @@ __global__ void __launch_bounds__(32 * MP_MAXCH) k_mp_sweep(const MPChan* chans,
       }
       __syncthreads();
       if (K.undo) {
-        const PeakRec r = S.w[c];
-        mp_add(C, fb, r, wc, -1, lane);
-        __syncthreads();
+        // the trial was never added to the image: only the records go back
         if (threadIdx.x == 0) {
           for (int i = 0; i < nc; i++) {
             const int added = S.w[i].added - 1;
@@ -428,7 +508,11 @@ __global__ void __launch_bounds__(32 * MP_MAXCH) k_mp_sweep(const MPChan* chans,
         }
       }
       __syncthreads();
-      if (K.act == MPA_BREAK) break;
+      if (K.act == MPA_BREAK) {
+        // an accepted trial (CONVERGED or a decreased error) stays in the image
+        if (S.w[0].status != ERROR) mp_add_from_ws(C, fb, S.w[c], wc, lane);
+        break;
+      }
     }
     // mpCopyFromWorking mp_fit.c:124-134: channel 0's status for all
     if (lane == 0) {
