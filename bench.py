@@ -995,7 +995,7 @@ def _mp_cpu_job(args):
     return dt, props
 
 
-MP_FRAMES = 1024      # frames of the batched multi-plane fit
+MP_FRAMES = 512       # frames of the batched multi-plane fit
 MP_CPU_FRAMES = 32    # frames of its CPU sample
 
 
@@ -1029,7 +1029,10 @@ def run_mp_report(args, pool):
     cpu_s, ref = pool.map(_mp_cpu_job, [(wl, "liboracle_timing.so")])[0]
     # batched: MP_FRAMES frames at once (one warp each) against the oracle's
     # frames on the host cores (one frame per process)
-    wls = [synth.multiplane_workload(seed=100 + i) for i in range(MP_FRAMES)]
+    # 64 distinct frames, repeated to MP_FRAMES (the content of a frame does
+    # not depend on its neighbours in the batch)
+    distinct = [synth.multiplane_workload(seed=100 + i) for i in range(64)]
+    wls = [distinct[i % 64] for i in range(MP_FRAMES)]
     f = mp_fit_dao_c.MPFitDao2D(n_channels=nc, roi_size=10, sigma_range=(1.0, 3.0))
     for c in range(nc):
         f.initializeChannel(numpy.ones(shape), numpy.zeros(shape), c)
