@@ -1267,6 +1267,9 @@ def main():
     ap.add_argument("--ticks-per-launch", type=int, default=4)
     ap.add_argument("--ctas-per-slot", type=int, default=12)
     ap.add_argument("--serving-sizes", default="128,256,512,2048")
+    ap.add_argument("--model-report", default=None, choices=["fft", "pupil", "multi_plane"],
+                    help="run one model's report block alone (the FFT PSF, pupil-function or multi-plane fit)")
+    ap.add_argument("--report-cores", type=int, default=16, help="host processes of --model-report's CPU sample")
     args = ap.parse_args()
     from sa_gb300.replicas import rank_env
     rank, world, local_rank = rank_env()
@@ -1289,6 +1292,21 @@ def main():
     elif args.serving and args.impl == "ours":
         if rank == 0:
             run_serving(args, local_rank)
+    elif args.model_report and args.impl == "ours":
+        if rank == 0:
+            import multiprocessing
+            import torch
+            from sa_gb300 import loadclib
+            build_oracle()
+            ctx = multiprocessing.get_context("spawn")
+            with ctx.Pool(args.report_cores) as pool:
+                loadclib.load().saSetDevice(local_rank)
+                torch.cuda.set_device(local_rank)
+                if args.model_report == "multi_plane":
+                    out = run_mp_report(args, pool)
+                else:
+                    out = run_fft_report(args, pool, args.report_cores, model=args.model_report)
+            print(json.dumps({args.model_report: out}), flush=True)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:

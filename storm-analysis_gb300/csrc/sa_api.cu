@@ -2285,6 +2285,8 @@ static int mp_prepare(saMPFit* mp, MPParams& p, int& frames, cudaStream_t& strea
   }
   p.w = st->d_w;
   p.ws_bytes = ws;
+  for (int c = 0; c < nc; c++) p.grid_doubles = std::max(p.grid_doubles, E(st->fit[c])->cfg.roi * E(st->fit[c])->cfg.roi);
+  p.teams = 1;
   frames = e0->F;
   stream = e0->stream;
   return 0;

@@ -8,9 +8,12 @@ int mp_ws_bytes(const ModelCfg& cfg) { return (int)warp_ws_bytes<double>(cfg, cf
 
 static size_t al16(size_t b) { return (b + 15) & ~(size_t)15; }
 
-// k_mp_sweep: a workspace per plane's warp, the coupling state, the channels.
+// k_mp_sweep: per warp a workspace and a shape grid, per team its coupling
+// state, the channels, the batch table.
 static size_t mp_smem_sweep(const MPParams& p) {
-  return (size_t)p.nc * p.ws_bytes + al16(sizeof(MPShared)) + al16(sizeof(MPCtl)) + (size_t)p.nc * sizeof(MPChan);
+  const size_t wstride = (size_t)p.ws_bytes + al16((size_t)p.grid_doubles * 8);
+  return (size_t)p.nc * p.teams * wstride + al16(sizeof(MPTeam) * p.teams) + al16(sizeof(MPChan) * p.nc) +
+         sizeof(int) * (MP_TEAMS + 4 * MP_TEAMS * MP_MAXCH + 4);
 }
 
 // k_mp_newpeaks: one warp.
@@ -40,9 +43,13 @@ static cudaError_t mp_limits() {
 cudaError_t mp_sweep(const MPChan* d_chans, const MPParams& p, int frames, cudaStream_t s) {
   cudaError_t e = mp_limits();
   if (e != cudaSuccess) return e;
-  // a workspace per plane: too many planes of a large PSF do not fit
-  if (mp_smem_sweep(p) > (size_t)g_max_smem) return cudaErrorInvalidConfiguration;
-  k_mp_sweep<<<frames, 32 * p.nc, mp_smem_sweep(p), s>>>(d_chans, p);
+  // as many teams as fit (a workspace per plane each); none: too many planes
+  // of a large PSF
+  MPParams q = p;
+  q.teams = MP_TEAMS;
+  while (q.teams > 1 && (mp_smem_sweep(q) > (size_t)g_max_smem || 32 * q.nc * q.teams > 32 * MP_MAXCH * 2)) q.teams--;
+  if (mp_smem_sweep(q) > (size_t)g_max_smem) return cudaErrorInvalidConfiguration;
+  k_mp_sweep<<<frames, 32 * q.nc * q.teams, mp_smem_sweep(q), s>>>(d_chans, q);
   return cudaGetLastError();
 }
 

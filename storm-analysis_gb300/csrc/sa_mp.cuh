@@ -197,14 +197,33 @@ __device__ inline void mp_z_range(const ModelCfg& cfg, PeakRec& w) {
   }
 }
 
-// fn_check of a channel: daoCheck2D for the Gaussians, mFitCheck otherwise;
-// counts the margin / height failures on its frame.
-__device__ inline int mp_check(const MPChan& c, int f, PeakRec& w) {
+constexpr int MP_TEAMS = 8;   // groups per batch at most
+constexpr int MP_DIL = 2;     // ROI growth (pixels) that a bounded step may use
+
+// Per-team coupling state beyond MPShared (the team leader writes).
+struct MPCtl {
+  double e[MP_MAXCH];          // the planes' errors of the latest evaluation
+  int fail[MP_MAXCH];          // the planes' fi <= 0 / escape flags of that evaluation
+  int act, undo, esc;
+  long long ctr[MP_MAXCH][NCOUNTERS];   // the step's counters per plane (added at commit)
+};
+
+struct MPTeam {
+  MPShared S;
+  MPCtl K;
+};
+
+// fn_check of a channel (plane i of a team): daoCheck2D for the Gaussians,
+// mFitCheck otherwise; counts the margin / height failures in the team's
+// counters.
+__device__ inline int mp_check_team(const MPChan& c, PeakRec& w, MPCtl& K, int i) {
   const int r = (c.cfg.model == M_2D) ? model_check(c.cfg, M_2D, w) : base_check(c.cfg, w);
-  if (r == 1) c.fs.ctl[f].ctr[C_MARGIN]++;
-  else if (r == 2) c.fs.ctl[f].ctr[C_NEGH]++;
+  if (r == 1) K.ctr[i][C_MARGIN]++;
+  else if (r == 2) K.ctr[i][C_NEGH]++;
   return r;
 }
+
+enum { MPA_EVAL = 0, MPA_CONTINUE = 1, MPA_BREAK = 2 };
 
 // The channels' parameter update from their steps (lane 0): mpArbUpdateFixed
 // mp_fit_arb.c:400-432 / mpArbUpdateIndependent :449-470 / mpDaoUpdate
@@ -212,7 +231,7 @@ __device__ inline int mp_check(const MPChan& c, int f, PeakRec& w) {
 // PSFs) mpArbUpdateZ mp_fit_arb.c:351-384.  The 2D Gaussian update moves the
 // x width only (the y width keeps its value) and applies daoCheck2D (its
 // clamp and counters) without using its result.
-__device__ inline void mp_update(const MPChan* ch, const MPParams& p, MPShared& S, int f) {
+__device__ inline void mp_update_team(const MPChan* ch, const MPParams& p, MPShared& S, MPCtl& K) {
   const int nc = p.nc;
   double dz, p_ave, p_total, w;
   int zi;
@@ -226,7 +245,7 @@ __device__ inline void mp_update(const MPChan* ch, const MPParams& p, MPShared& 
   if (p.kind == MP_DAO) {
     for (int i = 0; i < nc; i++) {
       S.w[i].p[PXW] -= S.dl[i][3];
-      (void)mp_check(ch[i], f, S.w[i]);
+      (void)mp_check_team(ch[i], S.w[i], K, i);
     }
   } else if (!p.indep) {
     mp_weight_index(p, S.w[0].p[PZ], dz, zi);
@@ -315,255 +334,415 @@ __device__ inline void mp_check_error(const MPChan* ch, const MPParams& p, int f
   }
 }
 
-enum { MPA_EVAL = 0, MPA_CONTINUE = 1, MPA_BREAK = 2 };
+// ---------------------------------------------------------------------------
+// The sweep, several groups at once.
+//
+// A frame's groups are taken in index order in batches of at most MP_TEAMS:
+// a batch is a run of consecutive RUNNING groups whose ROIs, grown by
+// MP_DIL pixels on every side, overlap in no plane.  Every group of a batch
+// takes its step at once, one team of warps (a warp per plane) each, on
+// its own copy of its ROIs' state: nothing is written to the planes'
+// images or records until the batch commits.  A step that moves a ROI more
+// than MP_DIL pixels from where it started "escapes" and stops.  The batch
+// then commits the steps of its groups below the lowest escaped one (their
+// regions are disjoint, so committing them together is what committing
+// them one after another gives), drops the others, runs the escaped group
+// alone on the committed state (unbounded) and commits it; the next batch
+// starts after it.  So every group's step sees the state the reference's
+// index-order sweep gives it, and the results are that sweep's.
+// ---------------------------------------------------------------------------
 
-// Per-frame coupling state of k_mp_sweep beyond MPShared (thread 0 writes).
-struct MPCtl {
-  double e[MP_MAXCH];   // the planes' errors of the latest evaluation
-  int fail[MP_MAXCH];   // the planes' fi <= 0 flags of that evaluation
-  int act, undo, run;
-};
 
-// mpIterateLM mp_fit.c:183-478 for frame blockIdx.x, then mFitRecenterPeaks
-// per channel and mpCheckError per group.  One warp per plane (blockDim.x =
-// 32 * nc): each warp does its plane's error, Jacobian, solve, adds and
-// subtractions; thread 0 does the coupled update and the decisions.
-__global__ void __launch_bounds__(32 * MP_MAXCH) k_mp_sweep(const MPChan* chans, MPParams p) {
-  extern __shared__ __align__(16) char smem[];
-  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
-  const int f = blockIdx.x;
+__device__ __forceinline__ void team_sync(int team, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(team + 1), "r"(nthreads) : "memory");
+}
+
+// The base state of a ROI anchored at (ax, ay) without the peak's start
+// contribution (rec0 anchored at its start, shape grid psfo[roi][roi]):
+// the fit image and background less that contribution where the start ROI
+// covers the pixel, rqe, data, and the count with the trial peak.
+__device__ inline void mp_base_excl(const MPChan& c, long long fbase, int ax, int ay, const PeakRec& rec0,
+                                    const double* psfo, WarpWS<double>& ws, int lane) {
+  const ModelCfg& cfg = c.cfg;
+  for (int p = lane; p < cfg.nroi; p += 32) {
+    int rx, ry;
+    roi_rc(ws.roi, p, rx, ry);
+    const long long kk = pix_index(cfg, ax, ay, rx, ry);
+    Q2 Fq = acc_load<2>(c.fs.f, fbase + kk);
+    Q2 Bq = acc_load<2>(c.fs.bg, fbase + kk);
+    int Cg = __ldcg(c.fs.cnt + fbase + kk);
+    const double rq = __ldg(c.fs.rqe + kk), sc = __ldg(c.fs.scmos + kk);
+    const int ox = ax + rx - rec0.xi, oy = ay + ry - rec0.yi;
+    if (in_roi(ox, oy, cfg.roi)) {
+      Fq = q_sub(Fq, quant_t<double>(contrib_f(rec0.p[PH], psfo[oy * cfg.roi + ox], rq)));
+      Bq = q_sub(Bq, quant_t<double>(contrib_bg(rec0.p[PBG], rq, sc)));
+      Cg -= 1;
+    }
+    ws.Fb[p] = acc_value<2>(Fq);
+    ws.Bs[p] = acc_value<2>(Bq) + sc;
+    ws.R[p] = rq;
+    ws.X[p] = __ldg(c.fs.x + fbase + kk);
+    ws.IC[p] = ic_store<double>(Cg + 1);
+  }
+  __syncwarp();
+}
+
+// One group's coupled LM step (mpIterateLM mp_fit.c:199-466) by one team:
+// warp c of the team does plane c.  Nothing is written outside shared
+// memory: the final records are in T.S.w, the final shape in ws.psf and the
+// start shape in psfo (per plane).  Returns (on every thread of the team)
+// 1 if a bounded step escaped.
+__device__ inline int mp_team_step(const MPChan* ch, const MPParams& p, int f, int g, MPTeam& T,
+                                   WarpWS<double>& wc, double* psfo, int c, int lane, int team, int nthr,
+                                   bool bounded) {
   const int nc = p.nc;
-  char* const ws_c = smem + (size_t)c * p.ws_bytes;
-  MPShared& S = *reinterpret_cast<MPShared*>(smem + (size_t)nc * p.ws_bytes);
-  MPCtl& K = *reinterpret_cast<MPCtl*>(smem + (size_t)nc * p.ws_bytes + ((sizeof(MPShared) + 15) & ~(size_t)15));
-  MPChan* ch = reinterpret_cast<MPChan*>(smem + (size_t)nc * p.ws_bytes + ((sizeof(MPShared) + 15) & ~(size_t)15) +
-                                         ((sizeof(MPCtl) + 15) & ~(size_t)15));
-  for (int i = threadIdx.x; i < (int)(nc * sizeof(MPChan) / 4); i += blockDim.x)
-    reinterpret_cast<int*>(ch)[i] = reinterpret_cast<const int*>(chans)[i];
-  // relative heights: 1 for fixed heights (mpSetWeights mp_fit.c:589-591);
-  // independent and Gaussian updates set them before use
-  if (threadIdx.x < MP_MAXCH) S.heights[threadIdx.x] = 1.0;
-  __syncthreads();
+  const bool lead = (c == 0 && lane == 0);
+  MPShared& S = T.S;
+  MPCtl& K = T.K;
   const MPChan& C = ch[c];
   const long long fb = mp_fbase(C, f);
-  WarpWS<double> wc = warp_ws<double>(ws_c, C.cfg, C.cfg.nroi);
-  wc.roi = C.fs.roi_xy;
-  const int nfit = ch[0].fs.nfit[f];
-  int cax = 0, cay = 0;   // anchor of this plane's base arrays
-  for (int g = 0; g < nfit; g++) {
-    if (threadIdx.x == 0) K.run = (ch[0].fs.pk[ch[0].fs.pk_off[f] + g].status == RUNNING);
-    __syncthreads();
-    if (!K.run) {
-      __syncthreads();
-      continue;
+  if (lane == 0)
+    for (int i = 0; i < NCOUNTERS; i++) K.ctr[c][i] = 0;
+  {
+    PeakRec r;
+    load_rec(C.fs.pk + C.fs.pk_off[f] + g, r);
+    double dev;
+    const bool fail = mp_error(C, fb, r, dev, lane);
+    if (lane == 0) S.orig[c] = r;   // the stored peak (mpResetWorkingPeaks restores it)
+    if (!fail) r.error = dev;       // the return value is ignored (mp_fit.c:220)
+    else if (lane == 0) K.ctr[c][C_NEGFI]++;
+    if (lane == 0) {
+      S.orig_e[c] = r.error;
+      r.added -= 1;
+      S.w[c] = r;
     }
+    const SplinePos sp = mp_jh(C, fb, r, wc, S.jh[c], lane);
+    // the start shape on a roi x roi grid (for the exclusions and the commit)
+    for (int q = lane; q < C.cfg.roi * C.cfg.roi; q += 32) psfo[q] = 0.0;
+    __syncwarp();
+    for (int q = lane; q < C.cfg.nroi; q += 32) {
+      int rx, ry;
+      roi_rc(wc.roi, q, rx, ry);
+      psfo[ry * C.cfg.roi + rx] = psf_at(C.cfg, C.fs.aij, wc, sp, rx, ry);
+    }
+    __syncwarp();
+    mp_base_excl(C, fb, r.xi, r.yi, r, psfo, wc, lane);
+  }
+  int cax = S.orig[c].xi, cay = S.orig[c].yi;
+  const int x0 = S.orig[c].xi, y0 = S.orig[c].yi;
+  for (;;) {
+    team_sync(team, nthr);
+    if (lead) {
+      K.act = MPA_EVAL;
+      if (S.w[0].lambda > LAMBDA_MAX) {
+        for (int i = 0; i < nc; i++) {
+          K.ctr[i][C_LOST]++;
+          S.w[i].status = ERROR;
+        }
+        K.act = MPA_BREAK;
+      } else {
+        for (int i = 0; i < nc; i++) S.w[i].status = RUNNING;
+      }
+    }
+    team_sync(team, nthr);
+    if (K.act == MPA_BREAK) return 0;
     {
-      PeakRec r;
-      load_rec(C.fs.pk + C.fs.pk_off[f] + g, r);
-      double dev;
-      const bool fail = mp_error(C, fb, r, dev, lane);
-      if (lane == 0) S.orig[c] = r;   // the stored peak (mpResetWorkingPeaks restores it)
-      if (!fail) r.error = dev;       // the return value is ignored (mp_fit.c:220)
-      else if (lane == 0) C.fs.ctl[f].ctr[C_NEGFI]++;
+      double dl[MAX_JAC];
+      const int info = solve_fp64_warp(S.jh[c], C.cfg.jac, S.w[c].lambda, dl, lane);
       if (lane == 0) {
-        S.orig_e[c] = r.error;        // the plane's part of the starting error
-        r.added -= 1;
-        S.w[c] = r;
+        K.fail[c] = info;
+        for (int m = 0; m < C.cfg.jac; m++) S.dl[c][m] = dl[m];
       }
-      const SplinePos sp = mp_jh(C, fb, r, wc, S.jh[c], lane);
-      mp_sub_base(C, fb, r, sp, wc, lane);
-      cax = r.xi;
-      cay = r.yi;
     }
-    __syncthreads();
-    for (;;) {
-      __syncthreads();   // every thread has read the previous pass's decisions
-      // lambda bound, the planes' solves (lane 0 of each warp), the update
-      if (threadIdx.x == 0) {
-        K.act = MPA_EVAL;
-        if (S.w[0].lambda > LAMBDA_MAX) {
-          for (int i = 0; i < nc; i++) {
-            ch[i].fs.ctl[f].ctr[C_LOST]++;
-            S.w[i].status = ERROR;
-          }
-          K.act = MPA_BREAK;
-        } else {
-          for (int i = 0; i < nc; i++) S.w[i].status = RUNNING;
+    team_sync(team, nthr);
+    if (lead) {
+      bool bad = false;
+      for (int i = 0; i < nc; i++) {
+        S.w[i].iterations++;
+        K.ctr[i][C_ITER]++;
+        if (K.fail[i] != 0) {
+          K.ctr[i][C_DPOSV]++;
+          bad = true;
+          break;
         }
       }
-      __syncthreads();
-      if (K.act == MPA_BREAK) break;
-      {
-        // mp_fit.c:262-300: every plane counts the pass; the first failing
-        // solve ends the planes' loop (later planes neither solve nor count)
-        double dl[MAX_JAC];
-        const int info = solve_fp64_warp(S.jh[c], C.cfg.jac, S.w[c].lambda, dl, lane);
-        if (lane == 0) {
-          K.fail[c] = info;
-          for (int m = 0; m < C.cfg.jac; m++) S.dl[c][m] = dl[m];
-        }
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        bool bad = false;
+      if (bad) {
         for (int i = 0; i < nc; i++) {
-          S.w[i].iterations++;
-          ch[i].fs.ctl[f].ctr[C_ITER]++;
-          if (K.fail[i] != 0) {
-            ch[i].fs.ctl[f].ctr[C_DPOSV]++;
-            bad = true;
-            break;
-          }
+          S.w[i].status = ERROR;
+          S.w[i].lambda = S.w[i].lambda * LAMBDA_UP;
         }
+        K.act = MPA_CONTINUE;
+      } else {
+        mp_update_team(ch, p, S, K);
+        for (int i = 0; i < nc; i++)
+          if (mp_check_team(ch[i], S.w[i], K, i)) bad = true;
         if (bad) {
           for (int i = 0; i < nc; i++) {
-            S.w[i].status = ERROR;
-            S.w[i].lambda = S.w[i].lambda * LAMBDA_UP;
-          }
-          K.act = MPA_CONTINUE;
-        } else {
-          mp_update(ch, p, S, f);
-          for (int i = 0; i < nc; i++)
-            if (mp_check(ch[i], f, S.w[i])) bad = true;
-          if (bad) {
-            // mpResetWorkingPeaks mp_fit.c:500-521
-            for (int i = 0; i < nc; i++) {
-              const int added = S.w[i].added;
-              const double lam = S.w[i].lambda;
-              S.w[i] = S.orig[i];
-              S.w[i].added = added;
-              S.w[i].lambda = lam * LAMBDA_UP;
-              S.w[i].status = ERROR;
-            }
-            K.act = MPA_CONTINUE;
-          }
-        }
-      }
-      __syncthreads();
-      if (K.act == MPA_CONTINUE) continue;
-      // add the trial peaks, their errors (mp_fit.c:340-378), evaluated
-      // from the base state (reloaded where the ROI moved)
-      {
-        const PeakRec r = S.w[c];
-        if (r.xi != cax || r.yi != cay) {
-          __threadfence();
-          load_base(C.cfg, C.fs, fb, r.xi, r.yi, wc, lane);
-          __syncwarp();
-          cax = r.xi;
-          cay = r.yi;
-        }
-        double dev;
-        const bool fail = mp_trial_error(C, r, wc, dev, lane);
-        if (lane == 0) {
-          S.w[c].added += 1;
-          K.fail[c] = fail;
-          K.e[c] = dev;
-          if (fail) C.fs.ctl[f].ctr[C_NEGFI]++;
-          else S.w[c].error = dev;
-        }
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double e0 = 0.0, e1 = 0.0;
-        bool bad = false;
-        for (int i = 0; i < nc; i++) {
-          e0 += S.orig_e[i];
-          if (K.fail[i]) bad = true;
-          else e1 += K.e[i];
-        }
-        K.undo = 0;
-        if (bad) {
-          K.undo = 1;
-          K.act = MPA_CONTINUE;
-        } else if (e1 > e0) {
-          if (((e1 - e0) / e0) < p.tol) {
-            for (int i = 0; i < nc; i++) S.w[i].status = CONVERGED;
-            K.act = MPA_BREAK;
-          } else {
-            for (int i = 0; i < nc; i++) ch[i].fs.ctl[f].ctr[C_NONDECR]++;
-            K.undo = 1;
-            K.act = MPA_CONTINUE;
-          }
-        } else {
-          if (((e0 - e1) / e0) < p.tol) {
-            for (int i = 0; i < nc; i++) S.w[i].status = CONVERGED;
-          } else if (S.w[0].lambda > LAMBDA_MIN) {
-            for (int i = 0; i < nc; i++) S.w[i].lambda = S.w[i].lambda * LAMBDA_DOWN;
-          }
-          K.act = MPA_BREAK;
-        }
-      }
-      __syncthreads();
-      if (K.undo) {
-        // the trial was never added to the image: only the records go back
-        if (threadIdx.x == 0) {
-          for (int i = 0; i < nc; i++) {
-            const int added = S.w[i].added - 1;
+            const int added = S.w[i].added;
             const double lam = S.w[i].lambda;
             S.w[i] = S.orig[i];
             S.w[i].added = added;
             S.w[i].lambda = lam * LAMBDA_UP;
             S.w[i].status = ERROR;
           }
+          K.act = MPA_CONTINUE;
         }
       }
-      __syncthreads();
-      if (K.act == MPA_BREAK) {
-        // an accepted trial (CONVERGED or a decreased error) stays in the image
-        if (S.w[0].status != ERROR) mp_add_from_ws(C, fb, S.w[c], wc, lane);
-        break;
+    }
+    team_sync(team, nthr);
+    if (K.act == MPA_CONTINUE) continue;
+    // the trial: escape check, base at a moved ROI, error
+    {
+      const PeakRec r = S.w[c];
+      const int esc = bounded && (abs(r.xi - x0) > MP_DIL || abs(r.yi - y0) > MP_DIL);
+      if (lane == 0) K.fail[c] = esc;
+    }
+    team_sync(team, nthr);
+    if (lead) {
+      int e = 0;
+      for (int i = 0; i < nc; i++) e |= K.fail[i];
+      K.esc = e;
+    }
+    team_sync(team, nthr);
+    if (K.esc) return 1;
+    {
+      const PeakRec r = S.w[c];
+      if (r.xi != cax || r.yi != cay) {
+        mp_base_excl(C, fb, r.xi, r.yi, S.orig[c], psfo, wc, lane);
+        cax = r.xi;
+        cay = r.yi;
+      }
+      double dev;
+      const bool fail = mp_trial_error(C, r, wc, dev, lane);
+      if (lane == 0) {
+        S.w[c].added += 1;
+        K.fail[c] = fail;
+        K.e[c] = dev;
+        if (fail) K.ctr[c][C_NEGFI]++;
+        else S.w[c].error = dev;
       }
     }
-    // mpCopyFromWorking mp_fit.c:124-134: channel 0's status for all
-    if (lane == 0) {
-      PeakRec r = S.w[c];
-      r.status = S.w[0].status;
-      C.fs.pk[C.fs.pk_off[f] + g] = r;
+    team_sync(team, nthr);
+    if (lead) {
+      double e0 = 0.0, e1 = 0.0;
+      bool bad = false;
+      for (int i = 0; i < nc; i++) {
+        e0 += S.orig_e[i];
+        if (K.fail[i]) bad = true;
+        else e1 += K.e[i];
+      }
+      K.undo = 0;
+      if (bad) {
+        K.undo = 1;
+        K.act = MPA_CONTINUE;
+      } else if (e1 > e0) {
+        if (((e1 - e0) / e0) < p.tol) {
+          for (int i = 0; i < nc; i++) S.w[i].status = CONVERGED;
+          K.act = MPA_BREAK;
+        } else {
+          for (int i = 0; i < nc; i++) K.ctr[i][C_NONDECR]++;
+          K.undo = 1;
+          K.act = MPA_CONTINUE;
+        }
+      } else {
+        if (((e0 - e1) / e0) < p.tol) {
+          for (int i = 0; i < nc; i++) S.w[i].status = CONVERGED;
+        } else if (S.w[0].lambda > LAMBDA_MIN) {
+          for (int i = 0; i < nc; i++) S.w[i].lambda = S.w[i].lambda * LAMBDA_DOWN;
+        }
+        K.act = MPA_BREAK;
+      }
+      if (K.undo) {
+        // the trial was never added to the image: only the records go back
+        for (int i = 0; i < nc; i++) {
+          const int added = S.w[i].added - 1;
+          const double lam = S.w[i].lambda;
+          S.w[i] = S.orig[i];
+          S.w[i].added = added;
+          S.w[i].lambda = lam * LAMBDA_UP;
+          S.w[i].status = ERROR;
+        }
+      }
+    }
+    team_sync(team, nthr);
+    if (K.act == MPA_BREAK) return 0;
+  }
+}
+
+// Commit a team's step (warp c, plane c): the start contribution out of the
+// image, the accepted trial in (its shape in ws.psf), the record (with
+// channel 0's status, mpCopyFromWorking mp_fit.c:124-134) and the counters.
+__device__ inline void mp_commit(const MPChan& C, int f, int g, const MPTeam& T, const WarpWS<double>& wc,
+                                 const double* psfo, int c, int lane) {
+  const ModelCfg& cfg = C.cfg;
+  const long long fb = mp_fbase(C, f);
+  const PeakRec& r0 = T.S.orig[c];
+  PeakRec r = T.S.w[c];
+  r.status = T.S.w[0].status;
+  for (int q = lane; q < cfg.nroi; q += 32) {
+    int rx, ry;
+    roi_rc(wc.roi, q, rx, ry);
+    const long long kk = pix_index(cfg, r0.xi, r0.yi, rx, ry);
+    const double rq = __ldg(C.fs.rqe + kk), sc = __ldg(C.fs.scmos + kk);
+    acc_red<2>(C.fs.f, fb + kk, quant_t<double>(contrib_f(r0.p[PH], psfo[ry * cfg.roi + rx], rq)), -1);
+    acc_red<2>(C.fs.bg, fb + kk, quant_t<double>(contrib_bg(r0.p[PBG], rq, sc)), -1);
+    atomicAdd(C.fs.cnt + fb + kk, -1);
+  }
+  if (r.status != ERROR) {
+    for (int q = lane; q < cfg.nroi; q += 32) {
+      int rx, ry;
+      roi_rc(wc.roi, q, rx, ry);
+      const long long kk = pix_index(cfg, r.xi, r.yi, rx, ry);
+      const double rq = wc.R[q], sc = __ldg(C.fs.scmos + kk);
+      acc_red<2>(C.fs.f, fb + kk, quant_t<double>(contrib_f(r.p[PH], wc.psf[q], rq)), +1);
+      acc_red<2>(C.fs.bg, fb + kk, quant_t<double>(contrib_bg(r.p[PBG], rq, sc)), +1);
+      atomicAdd(C.fs.cnt + fb + kk, 1);
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    C.fs.pk[C.fs.pk_off[f] + g] = r;
+    for (int i = 0; i < NCOUNTERS; i++)
+      if (T.K.ctr[c][i]) atomicAdd(reinterpret_cast<unsigned long long*>(&C.fs.ctl[f].ctr[i]),
+                                   (unsigned long long)T.K.ctr[c][i]);
+  }
+}
+
+// mpIterateLM mp_fit.c:183-478 for frame blockIdx.x (batches of groups as
+// above; blockDim.x = 32 * nc * p.teams), then mFitRecenterPeaks per plane
+// and mpCheckError per group.
+__global__ void __launch_bounds__(32 * MP_MAXCH * 2) k_mp_sweep(const MPChan* chans, MPParams p) {
+  extern __shared__ __align__(16) char smem[];
+  const int nc = p.nc;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int team = warp / nc, c = warp - team * nc;
+  const int nthr = 32 * nc;
+  const int f = blockIdx.x;
+  const size_t wstride = (size_t)p.ws_bytes + (((size_t)p.grid_doubles * 8 + 15) & ~(size_t)15);
+  char* const ws_c = smem + (size_t)warp * wstride;
+  double* const psfo = reinterpret_cast<double*>(ws_c + p.ws_bytes);
+  size_t off = (size_t)nc * p.teams * wstride;
+  MPTeam* teams = reinterpret_cast<MPTeam*>(smem + off);
+  off += ((sizeof(MPTeam) * p.teams + 15) & ~(size_t)15);
+  MPChan* ch = reinterpret_cast<MPChan*>(smem + off);
+  off += ((sizeof(MPChan) * nc + 15) & ~(size_t)15);
+  int* bgrp = reinterpret_cast<int*>(smem + off);           // the batch's groups
+  int* bbox = bgrp + MP_TEAMS;                               // their grown ROIs per plane: x0, y0, x1, y1
+  int* sh = bbox + 4 * MP_TEAMS * MP_MAXCH;                  // nb, next, esc_min
+  for (int i = threadIdx.x; i < (int)(nc * sizeof(MPChan) / 4); i += blockDim.x)
+    reinterpret_cast<int*>(ch)[i] = reinterpret_cast<const int*>(chans)[i];
+  if (threadIdx.x < p.teams * MP_MAXCH) teams[threadIdx.x / MP_MAXCH].S.heights[threadIdx.x % MP_MAXCH] = 1.0;
+  __syncthreads();
+  const MPChan& C = ch[c];
+  WarpWS<double> wc = warp_ws<double>(ws_c, C.cfg, C.cfg.nroi);
+  wc.roi = C.fs.roi_xy;
+  const int nfit = ch[0].fs.nfit[f];
+  int base = 0;
+  while (base < nfit) {
+    if (threadIdx.x == 0) {
+      // the batch: consecutive RUNNING groups, grown ROIs disjoint in every plane
+      int nb = 0, g = base;
+      while (nb < p.teams && g < nfit) {
+        if (ch[0].fs.pk[ch[0].fs.pk_off[f] + g].status != RUNNING) {
+          g++;
+          continue;
+        }
+        bool clash = false;
+        int box[MP_MAXCH][4];
+        for (int i = 0; i < nc; i++) {
+          const PeakRec* q = ch[i].fs.pk + ch[i].fs.pk_off[f] + g;
+          const int xi = q->xi, yi = q->yi, roi = ch[i].cfg.roi;
+          box[i][0] = xi - MP_DIL;
+          box[i][1] = yi - MP_DIL;
+          box[i][2] = xi + roi + MP_DIL;
+          box[i][3] = yi + roi + MP_DIL;
+          for (int m = 0; m < nb && !clash; m++) {
+            const int* o = bbox + 4 * (m * MP_MAXCH + i);
+            if (box[i][0] < o[2] && o[0] < box[i][2] && box[i][1] < o[3] && o[1] < box[i][3]) clash = true;
+          }
+        }
+        if (clash) break;
+        for (int i = 0; i < nc; i++)
+          for (int k = 0; k < 4; k++) bbox[4 * (nb * MP_MAXCH + i) + k] = box[i][k];
+        bgrp[nb++] = g++;
+      }
+      sh[0] = nb;
+      sh[1] = g;
+      sh[2] = INT_MAX;
+    }
+    __syncthreads();
+    const int nb = sh[0];
+    if (nb == 0) {
+      base = sh[1];
+      __syncthreads();
+      continue;
+    }
+    int esc = 0;
+    if (team < nb) {
+      esc = mp_team_step(ch, p, f, bgrp[team], teams[team], wc, psfo, c, lane, team, nthr, true);
+      if (esc && c == 0 && lane == 0) atomicMin(&sh[2], team);
+    }
+    __syncthreads();
+    const int emin = sh[2];
+    if (team < nb && team < emin) mp_commit(C, f, bgrp[team], teams[team], wc, psfo, c, lane);
+    __syncthreads();
+    if (emin < nb) {
+      // the escaped group alone, on the committed state
+      if (team == 0) {
+        mp_team_step(ch, p, f, bgrp[emin], teams[0], wc, psfo, c, lane, 0, nthr, false);
+        mp_commit(C, f, bgrp[emin], teams[0], wc, psfo, c, lane);
+      }
+      base = bgrp[emin] + 1;
+    } else {
+      base = sh[1];
     }
     __syncthreads();
   }
-  // mFitRecenterPeaks multi_fit.c:1644-1690, each warp its plane
-  for (int g = 0; g < nfit; g++) {
-    PeakRec* q = C.fs.pk + C.fs.pk_off[f] + g;
-    PeakRec r;
-    load_rec(q, r);
-    if (r.status != RUNNING) continue;
-    const double dx = r.p[PX] - r.xi, dy = r.p[PY] - r.yi;
-    if (!((dx < -0.25) || (dx > 1.25) || (dy < -0.25) || (dy > 1.25))) continue;
-    mp_add(C, fb, r, wc, -1, lane);
-    r.added -= 1;
-    r.xi = (int)floor(r.p[PX]);
-    r.yi = (int)floor(r.p[PY]);
-    const int chk = base_check(C.cfg, r);
-    if (chk) {
-      if (lane == 0) {
-        C.fs.ctl[f].ctr[C_LOST]++;
-        C.fs.ctl[f].ctr[chk == 1 ? C_MARGIN : C_NEGH]++;
+  // mFitRecenterPeaks multi_fit.c:1644-1690: team 0, a warp per plane
+  if (team == 0) {
+    const long long fb = mp_fbase(C, f);
+    for (int g = 0; g < nfit; g++) {
+      PeakRec* q = C.fs.pk + C.fs.pk_off[f] + g;
+      PeakRec r;
+      load_rec(q, r);
+      if (r.status != RUNNING) continue;
+      const double dx = r.p[PX] - r.xi, dy = r.p[PY] - r.yi;
+      if (!((dx < -0.25) || (dx > 1.25) || (dy < -0.25) || (dy > 1.25))) continue;
+      mp_add(C, fb, r, wc, -1, lane);
+      r.added -= 1;
+      r.xi = (int)floor(r.p[PX]);
+      r.yi = (int)floor(r.p[PY]);
+      const int chk = base_check(C.cfg, r);
+      if (chk) {
+        if (lane == 0) {
+          C.fs.ctl[f].ctr[C_LOST]++;
+          C.fs.ctl[f].ctr[chk == 1 ? C_MARGIN : C_NEGH]++;
+        }
+        r.status = ERROR;
+      } else {
+        mp_add(C, fb, r, wc, +1, lane);
+        r.added += 1;
       }
-      r.status = ERROR;
-    } else {
-      mp_add(C, fb, r, wc, +1, lane);
-      r.added += 1;
+      __syncwarp();
+      if (lane == 0) *q = r;
+      __syncwarp();
     }
-    __syncwarp();
-    if (lane == 0) *q = r;
-    __syncwarp();
   }
   __syncthreads();
-  // mpCheckError mp_fit.c:43-68 for every group, each warp its plane
+  // mpCheckError mp_fit.c:43-68 for every group: team 0, a warp per plane
   for (int g = 0; g < nfit; g++) {
     if (threadIdx.x == 0) {
       bool bad = false;
       for (int i = 0; i < nc; i++) bad |= (ch[i].fs.pk[ch[i].fs.pk_off[f] + g].status == ERROR);
-      K.run = bad;
+      sh[0] = bad;
     }
     __syncthreads();
-    if (K.run) {
+    if (sh[0] && team == 0) {
       PeakRec* q = C.fs.pk + C.fs.pk_off[f] + g;
       PeakRec r;
       load_rec(q, r);
       if (r.status != ERROR) {
-        mp_add(C, fb, r, wc, -1, lane);
+        mp_add(C, mp_fbase(C, f), r, wc, -1, lane);
         r.added -= 1;
       }
       r.status = ERROR;
@@ -572,7 +751,7 @@ __global__ void __launch_bounds__(32 * MP_MAXCH) k_mp_sweep(const MPChan* chans,
     }
     __syncthreads();
   }
-  if (p.unconv && c == 0) {
+  if (p.unconv && warp == 0) {
     int n = 0;
     for (int g = lane; g < nfit; g += 32) n += (ch[0].fs.pk[ch[0].fs.pk_off[f] + g].status == RUNNING);
     n = warp_sum_int(n);

@@ -24,6 +24,8 @@ struct MPParams {
   int start, stop;   // k_mp_newpeaks: the new groups (stop < 0: to the frame's last)
   int fix_heights;   // k_mp_newpeaks: give the new groups their channels' mean height
   int* unconv;       // k_mp_sweep: RUNNING groups per frame after the sweep (may be null)
+  int teams;         // k_mp_sweep: groups of a frame stepped at once (1 .. 8)
+  int grid_doubles;  // k_mp_sweep: a plane's roi x roi shape grid (the largest of the planes')
 };
 
 // Per-frame state in shared memory (lane 0 writes the records).
