@@ -1065,8 +1065,9 @@ def run_mp_report(args, pool):
             "batch_frames": MP_FRAMES, "batch_localizations_per_s": n_batch / batch_s, "batch_wall_s": batch_s,
             "batch_cpu_localizations_per_s": n_cpu_batch / cpu_batch_s, "batch_cpu_frames": ncpu,
             "batch_cpu_cores": getattr(pool, "_processes", None),
-            "note": "a frame's groups run in index order in one warp, as the reference's sweep; frames are the "
-                    "unit of parallelism (mpDoFitBatch)"}
+            "note": "a frame is one CTA: batches of up to 8 consecutive groups whose grown ROIs do not overlap "
+                    "step at once, committed in index order (the reference's sweep order); frames run in "
+                    "parallel (mpDoFitBatch); FP64 throughout"}
 
 
 DENSITY_BINS = 6   # log-spaced density bins of the serving stream's frame cache
