@@ -1041,9 +1041,12 @@ def run_mp_report(args, pool):
     images = [numpy.stack([w["images"][c] for w in wls]) for c in range(nc)]
     bgs = [numpy.stack([w["backgrounds"][c] for w in wls]) for c in range(nc)]
     f.fitBatch(images, bgs, [w["peaks"] for w in wls], "finder", max_iterations=MAX_IT)   # warm-up
-    t0 = time.perf_counter()
-    bout, _ = f.fitBatch(images, bgs, [w["peaks"] for w in wls], "finder", max_iterations=MAX_IT)
-    batch_s = time.perf_counter() - t0
+    batch_s = None
+    for _ in range(2):
+        t0 = time.perf_counter()
+        bout, _ = f.fitBatch(images, bgs, [w["peaks"] for w in wls], "finder", max_iterations=MAX_IT)
+        w_s = time.perf_counter() - t0
+        batch_s = w_s if batch_s is None else min(batch_s, w_s)
     f.cleanup(verbose=False)
     n_batch = int(bout[0]["status"].size)
     ncpu = min(MP_CPU_FRAMES, len(wls))
@@ -1065,9 +1068,11 @@ def run_mp_report(args, pool):
             "batch_frames": MP_FRAMES, "batch_localizations_per_s": n_batch / batch_s, "batch_wall_s": batch_s,
             "batch_cpu_localizations_per_s": n_cpu_batch / cpu_batch_s, "batch_cpu_frames": ncpu,
             "batch_cpu_cores": getattr(pool, "_processes", None),
-            "note": "a frame is one CTA: batches of up to 8 consecutive groups whose grown ROIs do not overlap "
-                    "step at once, committed in index order (the reference's sweep order); frames run in "
-                    "parallel (mpDoFitBatch); FP64 throughout"}
+            "batch_timing": "best of 2 fits after a warm-up fit, host images to results",
+            "note": "a frame is one CTA: batches of consecutive groups whose grown ROIs do not overlap "
+                    "step at once (up to 8 for a lone frame, 2-3 when many frames share the GPU), committed "
+                    "in index order (the reference's sweep order); frames run in parallel (mpDoFitBatch); "
+                    "FP64 throughout"}
 
 
 DENSITY_BINS = 6   # log-spaced density bins of the serving stream's frame cache

@@ -274,6 +274,12 @@ void mpSetTransforms(saMPFit *mp_fit, double *xt_0toN, double *yt_0toN, double *
 void mpSetWeights(saMPFit *mp_fit, double *w_bg, double *w_h, double *w_x, double *w_y, double *w_z, int z_size);
 /* mp_fit.c:600 mpSetWeightsIndexing */
 void mpSetWeightsIndexing(saMPFit *mp_fit, double z_offset, double z_scale);
+/* No reference counterpart: how many non-overlapping groups of a frame step
+ * at once in a sweep (1..8), or 0 (the default) to choose it from the
+ * number of frames (8 for a lone frame, down to 2 as the frames fill the
+ * GPU).
+ * The results do not depend on it.  Returns 0, or -1 on error. */
+int mpSetTeams(saMPFit *mp_fit, int teams);
 /* mp_fit_arb.c:36 mpArbInitializePSFFFTChannel, :85 mpArbInitializePupilFnChannel,
  * :135 mpArbInitializeSplineChannel (a 3D spline) */
 void mpArbInitializePSFFFTChannel(saMPFit *mp_fit, void *psf_fft, double *rqe, double *variance, int channel);

@@ -2097,6 +2097,7 @@ struct MPState {
   MPChan* d_chans = nullptr;
   int* d_unconv = nullptr;       // RUNNING groups per frame after a batched sweep
   int unconv_n = 0;
+  int teams = 0;                 // groups stepping at once per frame (0: chosen from the frame count)
   std::vector<saFitData*> fit;   // the channels (also in saMPFit.fit_data)
 };
 
@@ -2233,6 +2234,18 @@ void mpSetWeightsIndexing(saMPFit* mp, double z_offset, double z_scale) {
   mp->w_z_scale = z_scale;
 }
 
+// How many groups of a frame may step at once (1..8; 0: chosen from the
+// frame count, 2..8).  The results do not depend on it.
+int mpSetTeams(saMPFit* mp, int teams) {
+  MPState* st = MPS(mp);
+  if (!st || teams < 0 || teams > MP_TEAMS) {
+    set_error("mpSetTeams: %d (0..%d)", teams, MP_TEAMS);
+    return -1;
+  }
+  st->teams = teams;
+  return 0;
+}
+
 // The channel descriptors and parameters of a multi-plane launch; all
 // channels must be set, imaged and hold the same number of peaks.
 static int mp_prepare(saMPFit* mp, MPParams& p, int& frames, cudaStream_t& stream) {
@@ -2286,7 +2299,7 @@ static int mp_prepare(saMPFit* mp, MPParams& p, int& frames, cudaStream_t& strea
   p.w = st->d_w;
   p.ws_bytes = ws;
   for (int c = 0; c < nc; c++) p.grid_doubles = std::max(p.grid_doubles, E(st->fit[c])->cfg.roi * E(st->fit[c])->cfg.roi);
-  p.teams = 1;
+  p.teams = st->teams;
   frames = e0->F;
   stream = e0->stream;
   return 0;

@@ -197,7 +197,6 @@ __device__ inline void mp_z_range(const ModelCfg& cfg, PeakRec& w) {
   }
 }
 
-constexpr int MP_TEAMS = 8;   // groups per batch at most
 constexpr int MP_DIL = 2;     // ROI growth (pixels) that a bounded step may use
 
 // Per-team coupling state beyond MPShared (the team leader writes).
@@ -677,9 +676,10 @@ __global__ void __launch_bounds__(32 * MP_MAXCH * 2) k_mp_sweep(const MPChan* ch
       __syncthreads();
       continue;
     }
+    // a lone group's step cannot meet another's: unbounded (no escape)
     int esc = 0;
     if (team < nb) {
-      esc = mp_team_step(ch, p, f, bgrp[team], teams[team], wc, psfo, c, lane, team, nthr, true);
+      esc = mp_team_step(ch, p, f, bgrp[team], teams[team], wc, psfo, c, lane, team, nthr, nb > 1);
       if (esc && c == 0 && lane == 0) atomicMin(&sh[2], team);
     }
     __syncthreads();

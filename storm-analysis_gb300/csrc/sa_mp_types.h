@@ -7,6 +7,7 @@
 namespace sa {
 
 constexpr int MP_MAXCH = 8;
+constexpr int MP_TEAMS = 8;   // groups of a frame stepping at once (a batch) at most
 enum { MP_ARB = 0, MP_DAO = 1 };
 
 // One channel: its engine's model and frame set.

@@ -192,6 +192,8 @@ def _declare(lib):
     lib.mpNewPeaksBatch.restype = ci
     lib.mpDoFitBatch.argtypes = [mpp, ci]
     lib.mpDoFitBatch.restype = ci
+    lib.mpSetTeams.argtypes = [mpp, ci]
+    lib.mpSetTeams.restype = ci
     for name in ["getXSize", "getYSize", "getZSize"]:
         getattr(lib, name).argtypes = [vp]
         getattr(lib, name).restype = ci
@@ -332,7 +334,7 @@ EXPORTS = ["daoInitialize", "daoInitialize2DFixed", "daoInitialize2D", "daoIniti
            "mpInitialize", "mpCleanup", "mpIterateLM", "mpSetTransforms", "mpSetWeights", "mpSetWeightsIndexing",
            "mpArbInitializePSFFFTChannel", "mpArbInitializePupilFnChannel", "mpArbInitializeSplineChannel",
            "mpArbNewPeaks", "mpDaoInitialize2DChannel", "mpDaoNewPeaks", "mpSetFrames", "mpNewPeaksBatch",
-           "mpDoFitBatch",
+           "mpDoFitBatch", "mpSetTeams",
            "mFitAnscombeTransformImage", "mFitGetFitImage", "mFitGetNError",
            "mFitGetPeakPropertyDouble", "mFitGetPeakPropertyInt", "mFitGetResidual",
            "mFitGetUnconverged", "mFitIterateLM", "mFitNewBackground", "mFitNewImage",

@@ -252,9 +252,12 @@ def test_mp_arb_matches_oracle(case):
                 p.cleanup()
 
 
-def test_mp_batch_equals_single_frames():
+@pytest.mark.parametrize("teams", [0, 1, 3])
+def test_mp_batch_equals_single_frames(teams):
     """mpSetFrames / mpNewPeaksBatch / mpDoFitBatch on three frames give
-    every frame's results bit for bit as the one-frame calls do."""
+    every frame's results bit for bit as the one-frame calls do (those step
+    up to 8 groups of a frame at once), whatever number of groups the batch
+    steps at once (mpSetTeams; 0 chooses it from the frame count)."""
     from sa_gb300 import mp_fit_dao_c, synth
     wls = [synth.multiplane_workload(nx=96, ny=104, n_emitters=25, seed=s) for s in (41, 42, 43)]
     shape = (wls[0]["ny"], wls[0]["nx"])
@@ -280,6 +283,7 @@ def test_mp_batch_equals_single_frames():
                                                              "iterations")} for c in range(nc)])
         f.cleanup(verbose=False)
     f = make()
+    assert f.clib.mpSetTeams(f.mfit, teams) == 0
     images = [numpy.stack([wl["images"][c] for wl in wls]) for c in range(nc)]
     bgs = [numpy.stack([wl["backgrounds"][c] for wl in wls]) for c in range(nc)]
     out, sweeps = f.fitBatch(images, bgs, [wl["peaks"] for wl in wls], "finder", max_iterations=200)
