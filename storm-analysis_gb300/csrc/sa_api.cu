@@ -1339,10 +1339,10 @@ saFitData* pfitInitialize(void* pupil_data, double* rqe, double* scmos, double t
   e->prec = 64;
   e->cfg.sx = p->n;
   e->cfg.sy = p->n;
-  e->cfg.sz = 0;
   e->cfg.zmin = -1.0e300;
   e->cfg.zmax = 1.0e300;
-  pupil_tables(*p, e->aij_h);
+  // the support band's rows size the per-warp row sums (pupil_scratch_doubles)
+  e->cfg.sz = std::max(1, pupil_tables(*p, e->aij_h));
   e->cfg.xoff = 0.5 * (double)p->n;
   e->cfg.yoff = 0.5 * (double)p->n;
   roi_index(e, p->n);

@@ -704,13 +704,18 @@ __host__ __device__ __forceinline__ PupilLayout pupil_layout(int n) {
   L.total = L.band + 2;
   return L;
 }
-// Doubles of a warp's pupil scratch: B, By, Bz [N][N] (complex; the sums
-// over the pupil's second index of the translated pupil function, and of it
-// times -i ky and -i kz), three row buffers [N] (complex), the shift
-// vectors sx, sy [N] (complex) and the z shift table [m+1][m+1] (complex).
-__host__ __device__ __forceinline__ int pupil_scratch_doubles(int n) {
+// Rows of the pupil function's support band (first-index rows holding a
+// nonzero value; set from the pupil's tables when the fitter is made), or
+// all N rows when unknown.
+__host__ __device__ __forceinline__ int pupil_band_rows(int n, int sz) { return (sz > 0 && sz <= n) ? sz : n; }
+// Doubles of a warp's pupil scratch: B, By, Bz [band rows][N] (complex; the
+// sums over the pupil's second index of the translated pupil function, and
+// of it times -i ky and -i kz, for the band's rows only: the others are 0),
+// three row buffers [N] (complex), the shift vectors sx, sy [N] (complex)
+// and the z shift table [m+1][m+1] (complex).
+__host__ __device__ __forceinline__ int pupil_scratch_doubles(int n, int sz) {
   const int m1 = n / 2 + 1;
-  return 6 * n * n + 10 * n + 2 * m1 * m1;
+  return 6 * pupil_band_rows(n, sz) * n + 10 * n + 2 * m1 * m1;
 }
 // Warps with a workspace in a per-frame CTA (k_prepare, k_post) and in an
 // auxiliary CTA for the pupil model: its scratch is ~54 KB per warp at a
@@ -803,7 +808,7 @@ __host__ __device__ inline size_t warp_ws_bytes(const ModelCfg& cfg, int nroi) {
   b += 3 * sizeof(PeakRec);
   if (sizeof(T) == 4 && !gauss32<T>(cfg) && nroi > 0) b += 32 * 33 * sizeof(float);
   if (is_fft(cfg.model)) b = ((b + 15) & ~(size_t)15) + fft_scratch_doubles(cfg.sx, cfg.sy, cfg.sz) * sizeof(double);
-  if (is_pupil(cfg.model)) b = ((b + 15) & ~(size_t)15) + pupil_scratch_doubles(cfg.sx) * sizeof(double);
+  if (is_pupil(cfg.model)) b = ((b + 15) & ~(size_t)15) + pupil_scratch_doubles(cfg.sx, cfg.sz) * sizeof(double);
   return (b + 127) & ~(size_t)127;
 }
 
@@ -1326,11 +1331,12 @@ template <typename T>
 __device__ inline void pupil_tables(const ModelCfg& cfg, const PeakRec& w, WarpWS<T>& ws, int lane,
                                     bool deriv) {
   const int n = cfg.sx, m = n / 2, m1 = m + 1;
+  const int hb = pupil_band_rows(n, cfg.sz);
   const PupilLayout L = pupil_layout(n);
-  double* B = ws.fw;
-  double* By = B + 2 * n * n;
-  double* Bz = By + 2 * n * n;
-  double* rw = Bz + 2 * n * n;   // the translated pupil function's row i (complex)
+  double* B = ws.fw;             // row i of the band at (i - i_lo) * n
+  double* By = B + 2 * hb * n;
+  double* Bz = By + 2 * hb * n;
+  double* rw = Bz + 2 * hb * n;  // the translated pupil function's row i (complex)
   double* rwy = rw + 2 * n;      // ... times -i ky
   double* rwz = rwy + 2 * n;     // ... times -i kz
   double* sxv = rwz + 2 * n;     // x shift per first index (complex)
@@ -1406,7 +1412,7 @@ __device__ inline void pupil_tables(const ModelCfg& cfg, const PeakRec& w, WarpW
           zr += rwz[2 * k] * er - rwz[2 * k + 1] * ei;
           zc += rwz[2 * k] * ei + rwz[2 * k + 1] * er;
         }
-        const int o = 2 * (i * n + v);
+        const int o = 2 * ((i - i_lo) * n + v);
         B[o] = br;
         B[o + 1] = bc;
         By[o] = yr;
@@ -1422,8 +1428,8 @@ __device__ inline void pupil_tables(const ModelCfg& cfg, const PeakRec& w, WarpW
           br += rw[2 * k] * er - rw[2 * k + 1] * ei;
           bc += rw[2 * k] * ei + rw[2 * k + 1] * er;
         }
-        B[2 * (i * n + v)] = br;
-        B[2 * (i * n + v) + 1] = bc;
+        B[2 * ((i - i_lo) * n + v)] = br;
+        B[2 * ((i - i_lo) * n + v) + 1] = bc;
       }
     }
     __syncwarp();
@@ -1436,10 +1442,11 @@ __device__ inline void pupil_tables(const ModelCfg& cfg, const PeakRec& w, WarpW
 // factor; dz negated as pfnGetPSFdz :199-201).
 __device__ inline double pupil_pixel(const ModelCfg& cfg, const double* fw, int rx, int ry, double* g) {
   const int n = cfg.sx;
+  const int hb = pupil_band_rows(n, cfg.sz);
   const PupilLayout L = pupil_layout(n);
-  const double* B = fw;
-  const double* By = B + 2 * n * n;
-  const double* Bz = By + 2 * n * n;
+  const double* B = fw;          // row i of the band at (i - i_lo) * n
+  const double* By = B + 2 * hb * n;
+  const double* Bz = By + 2 * hb * n;
   const double* E = cfg.fft + L.e;
   const double* KX = cfg.fft + L.kx;
   const int i_lo = (int)__ldg(cfg.fft + L.band), i_hi = (int)__ldg(cfg.fft + L.band + 1);
@@ -1447,7 +1454,7 @@ __device__ inline double pupil_pixel(const ModelCfg& cfg, const double* fw, int 
   if (!g) {
     for (int i = i_lo; i <= i_hi; i++) {
       const double er = __ldg(E + 2 * (i * n + rx)), ei = __ldg(E + 2 * (i * n + rx) + 1);
-      const int o = 2 * (i * n + ry);
+      const int o = 2 * ((i - i_lo) * n + ry);
       pr += B[o] * er - B[o + 1] * ei;
       pc += B[o] * ei + B[o + 1] * er;
     }
@@ -1456,7 +1463,7 @@ __device__ inline double pupil_pixel(const ModelCfg& cfg, const double* fw, int 
   double xr = 0.0, xc = 0.0, yr = 0.0, yc = 0.0, zr = 0.0, zc = 0.0;
   for (int i = i_lo; i <= i_hi; i++) {
     const double er = __ldg(E + 2 * (i * n + rx)), ei = __ldg(E + 2 * (i * n + rx) + 1);
-    const int o = 2 * (i * n + ry);
+    const int o = 2 * ((i - i_lo) * n + ry);
     const double tr = B[o] * er - B[o + 1] * ei, tc = B[o] * ei + B[o + 1] * er;
     pr += tr;
     pc += tc;

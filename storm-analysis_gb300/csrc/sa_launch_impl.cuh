@@ -18,12 +18,12 @@ static inline int aux_block(const ModelCfg& cfg) { return 32 * aux_warps(cfg); }
 static inline size_t roi_table_bytes(int nroi) { return ((size_t)nroi * 2 + 15) & ~(size_t)15; }
 
 // Warps of a sweep CTA whose dynamic shared memory is smem (configure
-// chooses 4, 2 or 1 so that their workspaces fit).
+// chooses 4, 3, 2 or 1 so that their workspaces fit).
 template <typename T>
 static inline int sweep_warps(const ModelCfg& cfg, size_t smem) {
   const size_t ws = warp_ws_bytes<T>(cfg, cfg.nroi);
   const size_t w = (smem - roi_table_bytes(cfg.nroi)) / ws;
-  return w >= 4 ? 4 : (w >= 2 ? 2 : 1);
+  return w >= 4 ? 4 : (w >= 1 ? (int)w : 1);
 }
 
 // The sweep kernel of a configuration: the FP32 Gaussian models have one
@@ -68,10 +68,10 @@ cudaError_t Launch<T>::configure(const ModelCfg& cfg, int* sweep_grid, size_t* s
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t ws = warp_ws_bytes<T>(cfg, cfg.nroi);
-  // four warps per sweep CTA, or two or one where their workspaces (large
-  // ROIs in the FP64 engine, the pupil model) do not fit
+  // four warps per sweep CTA, or as many as fit where their workspaces
+  // (large ROIs in the FP64 engine, the pupil model) do not
   int wpc = SWEEP_BLOCK / 32;
-  while (wpc > 1 && ws * wpc + roi_table_bytes(cfg.nroi) > (size_t)max_smem) wpc /= 2;
+  while (wpc > 1 && ws * wpc + roi_table_bytes(cfg.nroi) > (size_t)max_smem) wpc--;
   const size_t s_sweep = ws * wpc + roi_table_bytes(cfg.nroi);
   const size_t ws0 = warp_ws_bytes<T>(cfg, 0);
   const size_t grid_bytes = (size_t)(cfg.gx * cfg.gy + 1) * sizeof(int);

@@ -159,7 +159,7 @@ bool pupil_rows_separable(const PupilH& p) {
   return true;
 }
 
-void pupil_tables(const PupilH& p, std::vector<double>& out) {
+int pupil_tables(const PupilH& p, std::vector<double>& out) {
   const int n = p.n, m = n / 2, m1 = m + 1;
   const PupilLayout L = pupil_layout(n);
   out.assign(L.total, 0.0);
@@ -201,6 +201,7 @@ void pupil_tables(const PupilH& p, std::vector<double>& out) {
   }
   out[L.band] = (double)i_lo;
   out[L.band + 1] = (double)i_hi;
+  return i_hi - i_lo + 1;
 }
 
 }  // namespace sa

@@ -39,7 +39,8 @@ void pupil_transform(const PupilH& p, int which, const double* dipole, double* r
 bool pupil_rows_separable(const PupilH& p);
 
 // The device tables of the engine's pupil model (pupil_layout in
-// sa_device.cuh).
-void pupil_tables(const PupilH& p, std::vector<double>& out);
+// sa_device.cuh).  Returns the rows of the pupil's support band (0 if the
+// pupil function is zero everywhere).
+int pupil_tables(const PupilH& p, std::vector<double>& out);
 
 }  // namespace sa
